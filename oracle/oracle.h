@@ -1,0 +1,58 @@
+// CPU ORACLE — test infrastructure only (see oracle.cpp).  C entry points
+// used by the Python tests through ctypes.  Index arrays are int32, row
+// offsets int32 on input (the layout the CUDA path uses), int64 where the
+// reference's JDS offsets can exceed the input's.  Trainer flags: bit 0 =
+// L2 without USE_ETA (w -= lambda*w, regularizer.hpp:50-54).
+#ifndef FVG_ORACLE_H
+#define FVG_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+void orc_crs_spmv_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                      const double* x, double* y);
+void orc_crs_spmv_f32(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const float* val,
+                      const float* x, float* y);
+void orc_crs_transpose_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                           int32_t* toff, int32_t* tidx, double* tval);
+void orc_crs_spmm_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                      const double* X, int64_t k, double* Y);
+int64_t orc_ell_width(int64_t m, const int32_t* off);
+void orc_ell_build_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                       int32_t* eidx, double* eval);
+void orc_ell_spmv_f64(int64_t m, int64_t n, int64_t width, const int32_t* eidx, const double* eval,
+                      const double* x, double* y);
+void orc_ell_trans_mv_f64(int64_t m, int64_t n, int64_t width, const int32_t* eidx, const double* eval,
+                          const double* v, double* y);
+void orc_jds_build_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                       int32_t* perm, int64_t* joff, int32_t* jidx, double* jval, int64_t* out_ndiag);
+void orc_jds_spmv_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                      const double* x, double* y);
+void orc_hyb_info(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val, int64_t thr,
+                  int64_t* info);
+void orc_hyb_build_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                       int64_t thr, int32_t* perm, int64_t* joff, int32_t* jidx, double* jval, int64_t* coff,
+                       int32_t* cidx, double* cval);
+void orc_hyb_spmv_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                      int64_t thr, const double* x, double* y);
+void orc_fmt_mv_f64(int fmt, int trans, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                    const double* val, const double* x, double* y);
+void orc_logistic_dloss_f64(int64_t m, const double* label, const double* wtx, double* dloss, double* sumloss);
+void orc_logreg_eval_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                         const double* val, const double* label, const double* sw, const double* w, double b,
+                         int icpt, const int64_t* splits, int P, int nthreads, double* grad, double* loss);
+int orc_logreg_lbfgs_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                         const double* val, const double* label, const double* sw, const int64_t* splits, int P,
+                         int nthreads, int64_t num_iter, int64_t hist, double lambda, int rtype, int icpt,
+                         double tol, double* w, double* b, int64_t* n_iter, double* final_loss, double* trace,
+                         int flags);
+int orc_logreg_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                       const double* label, const double* sw, const int64_t* splits, int P, int nthreads,
+                       int64_t num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
+                       double* w, double* b, int64_t* n_iter, double* final_loss, int flags);
+void orc_predict_probability_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                                 const double* val, const double* w, double b, double* out);
+#ifdef __cplusplus
+}
+#endif
+#endif
