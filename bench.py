@@ -1,0 +1,341 @@
+"""Benchmark: sparse logistic-regression L-BFGS iterations/s on one GB300.
+
+Workload (default): the mixed-precision L-BFGS configuration — 10,000,000 x
+1,000,000 CRS, nnz/row 1+Poisson(59) with Zipf(1.1) columns, lognormal(0,0.5)
+values, L2 lambda=1e-4, 50 iterations per run; values stored BF16 (FP32 after
+the refinement switch), FP32 accumulation, FP64 L-BFGS.  One "step" is one
+50-iteration training run; `value` = iterations/s with the matrix, its
+transposed copy and the labels already in HBM (inputs far larger than L2).
+`e2e` is the same metric through the public C-ABI call with host buffers:
+the host CRS arrays are uploaded, the transposed copy is built, the model is
+trained and read back, every step.
+
+The plain FP64 GPU path (FP64 values and accumulation) is timed on the same
+data for the FP64 baseline, and the CPU oracle (the reference's loops, all
+host threads, rows partitioned like MPI ranks) on a row sample for the CPU
+baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fvg|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sparse LogReg L-BFGS iters/s + SpMV HBM GB/s: BF16/batched vs FP64 GPU, same loss"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def load_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return v
+
+
+def make_data(scale, threads=0):
+    from frovedis_gb300 import datagen
+    spec = datagen.logreg_10m_1m(scale)
+    off, idx, val, label = datagen.generate(spec, nthreads=threads)
+    return spec, off, idx, val, label
+
+
+def eval_bytes(m, n, nnz, s_v, s_x):
+    """Algorithmic bytes of one loss/gradient evaluation (both CRS passes):
+    A and A^T once each (values + column ids + row offsets), the input vector
+    of each pass once, the residual written and re-read, labels, gradient."""
+    s_i, s_o = 4, 4
+    p1 = nnz * (s_v + s_i) + (m + 1) * s_o + n * s_x + m * 8 + m * s_x   # A w, labels (FP64), r written
+    p2 = nnz * (s_v + s_i) + (n + 1) * s_o + m * s_x + n * 8             # A^T r, r read, g written (FP64)
+    return p1, p2
+
+
+def run_gpu(args):
+    import torch
+
+    import frovedis_gb300 as fv
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    spec, off, idx, val, label = make_data(args.scale)
+    m, n, nnz = spec.m, spec.n, int(off[-1])
+    ctx = fv.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    A = ctx.matrix(m, n, off, idx, val)
+    A.prepare("CRS", transpose=True)
+    A.add_storage("bf16")
+    A.add_storage("f32")
+    kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, storage=args.storage)
+
+    def one_step():
+        return fv.logreg_lbfgs(A, label, **kw)
+
+    for _ in range(args.warmup):
+        r = one_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    ctx.reset_profile()
+    ctx.set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    iters = 0
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = one_step()
+            iters += r["n_iter"]
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ctx.set_profiling(False)
+    ms = e0.elapsed_time(e1)
+    launches = ctx.kernel_launches - launches0
+    p1_ms, p1_n = ctx.profile("pass1")
+    p2_ms, p2_n = ctx.profile("pass2")
+    ms = allmax(world, ms)
+    total_iters = iters * world
+    value = total_iters / (ms / 1e3)
+
+    # roofline of the CRS SpMV kernel (both passes of every evaluation)
+    s_v = {"f64": 8, "f32": 4, "bf16": 2}[args.storage]
+    s_x = 8 if args.storage == "f64" else 4
+    b1, b2 = eval_bytes(m, n, nnz, s_v, s_x)
+    peak, peak_kind = load_peak()
+    spmv_ms = p1_ms + p2_ms
+    achieved = (b1 * p1_n + b2 * p2_n) / (spmv_ms / 1e3) / 1e9 if spmv_ms > 0 else 0.0
+
+    # plain FP64 GPU path on the same data (the >= 3x denominator)
+    fp64 = None
+    if args.storage != "f64" and not args.skip_fp64:
+        kw64 = dict(kw, storage="f64")
+        fv.logreg_lbfgs(A, label, **kw64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = fv.logreg_lbfgs(A, label, **kw64)
+        torch.cuda.synchronize()
+        fp64 = {"iters_per_s": r64["n_iter"] / (time.perf_counter() - t0), "final_loss": r64["loss"],
+                "loss_rel_diff_vs_low_precision": abs(r["loss"] - r64["loss"]) / abs(r64["loss"])}
+
+    # end to end through the C ABI with host buffers
+    A.close()
+    e2e_ms = 0.0
+    e2e_iters = 0
+    h2d = (m + 1) * 4 + nnz * 12 + m * 8 + n * 8
+    d2h = n * 8 + 16
+    torch.cuda.synchronize()
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        B = ctx.matrix(m, n, off, idx, val)
+        if args.storage != "f64":
+            B.add_storage(args.storage)
+        rr = fv.logreg_lbfgs(B, label, **kw)
+        B.close()
+        ctx.synchronize()
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+        e2e_iters += rr["n_iter"]
+    e2e_ms = allmax(world, e2e_ms)
+    e2e_value = e2e_iters * world / (e2e_ms / 1e3)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(off, idx, val, label, spec, args, threads=0, sample_rows=args.cpu_rows)
+    ctx.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"bf16": "bf16 values, fp32 accum, fp64 solver", "f32": "fp32",
+                                       "f64": "fp64"}[args.storage],
+        "data": "synthetic (seeded power-law CRS; the reference's Criteo data is not available)",
+        "config": {"workload": "logreg-lbfgs-10Mx1M-nnz6e8", "rows": m, "cols": n, "nnz": nnz,
+                   "iterations_per_step": args.iters, "lambda": 1e-4, "format": "CRS",
+                   "storage": args.storage, "l2_flush": "inputs larger than L2 (A is %.1f GB)" % (
+                       nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU"},
+        "final_loss": r["loss"], "iterations_per_run": r["n_iter"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)",
+                     "bytes_per_eval": b1 + b2, "launches": p1_n + p2_n, "kernel_ms": spmv_ms},
+        "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": ck,
+        "fp64_gpu": fp64,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
+    """The oracle (reference loops, FP64) on the first `sample_rows` rows,
+    rows split over `threads` emulated ranks; scaled to full-size iters/s by
+    the nonzero ratio."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    ms = min(sample_rows, spec.m)
+    z = int(off[ms])
+    a = oracle.CRS(ms, spec.n, off[: ms + 1], idx[:z], val[:z])
+    splits = np.linspace(0, ms, threads + 1).astype(np.int64)
+    kw = dict(reg_type="L2", reg_param=1e-4, splits=splits, nthreads=threads)
+    # setup (per-rank transposes) and the initial evaluation are excluded by
+    # differencing a 1-iteration run and a (1+k)-iteration run
+    t0 = time.perf_counter()
+    r1 = oracle.logreg_lbfgs(a, label[:ms], num_iter=1, **kw)
+    t1 = time.perf_counter()
+    r2 = oracle.logreg_lbfgs(a, label[:ms], num_iter=1 + args.cpu_iters, **kw)
+    t2 = time.perf_counter()
+    k = r2["n_iter"] - r1["n_iter"]
+    dt = (t2 - t1) - (t1 - t0)
+    sample_rate = k / dt if dt > 0 and k > 0 else float("nan")
+    full = sample_rate * z / int(off[-1])
+    return {"value": full, "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": f"{k} L-BFGS iterations (setup excluded) on the first {ms} rows ({z} nnz), {threads} "
+                      f"emulated ranks, scaled by nnz to the full matrix; {dt:.2f} s"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    spec, off, idx, val, label = make_data(args.scale)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(off, idx, val, label, spec, args, threads, args.cpu_rows)
+    t_all = []
+    for _ in range(args.steps):
+        c = cpu_baseline(off, idx, val, label, spec, args, threads, args.cpu_rows)
+        vals.append(c["value"])
+        t_all.append(c)
+    v = statistics.median(vals)
+    line = {
+        "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / v * args.iters if v else None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded power-law CRS)",
+        "config": {"workload": "logreg-lbfgs-10Mx1M-nnz6e8", "rows": spec.m, "cols": spec.n,
+                   "nnz": int(off[-1]), "iterations_per_step": args.iters, "lambda": 1e-4},
+        "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": t_all[-1]["sample"]},
+        "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fvg", choices=["fvg", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--storage", default="bf16", choices=["bf16", "f32", "f64"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-rows", type=int, default=500_000)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

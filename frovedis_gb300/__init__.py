@@ -1,0 +1,397 @@
+"""frovedis_gb300 — GB300 sparse logistic-regression path behind a C ABI.
+
+Python bindings (ctypes) to ``libfvg.so`` (include/fvg.h).  They mirror the
+reference's local-matrix operators and trainer entry points:
+
+* ``Matrix.spmv / trans_mv / spmm``  — operator*(crs/ell/jds/hybrid, vector),
+  trans_mv, operator*(crs, rowmajor)   (frovedis matrix/*.hpp)
+* ``logreg_lbfgs`` / ``logreg_sgd``  — logistic_regression_with_{lbfgs,sgd}::
+  train main APIs (ml/glm/logistic_regression_with_*.hpp)
+* ``logreg_eval``                    — gradient_descent::compute_gradient
+* ``predict_probability``            — logistic_regression_model::predict_probability
+
+There is no CPU fallback: every call runs the CUDA library, and loading
+fails with an error when it cannot be built or loaded.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+F64, F32, BF16 = 0, 1, 2
+CRS, JDS, ELL, HYBRID = 0, 1, 2, 3
+FORMATS = {"CRS": CRS, "JDS": JDS, "ELL": ELL, "HYBRID": HYBRID}
+REG = {"ZERO": 0, "L1": 1, "L2": 2}
+DTYPES = {"f64": F64, "f32": F32, "bf16": BF16}
+
+_p = C.c_void_p
+_i64 = C.c_int64
+_int = C.c_int
+_dbl = C.c_double
+
+
+class FvgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fvg status {code}: {msg}")
+        self.code = code
+
+
+class GlmParams(C.Structure):
+    _fields_ = [("num_iteration", C.c_int64), ("alpha", C.c_double), ("hist_size", C.c_int64),
+                ("reg_param", C.c_double), ("reg_type", C.c_int32), ("intercept", C.c_int32),
+                ("convergence_tol", C.c_double), ("mat_type", C.c_int32), ("mini_batch_fraction", C.c_double),
+                ("num_partitions", C.c_int32), ("storage", C.c_int32), ("refine", C.c_int32),
+                ("refine_stall", C.c_double), ("l2_no_eta", C.c_int32), ("use_graph", C.c_int32),
+                ("trace", C.POINTER(C.c_double)), ("row_splits", C.POINTER(C.c_int64))]
+
+
+EXPORTS = [
+    "fvg_ctx_create", "fvg_ctx_destroy", "fvg_ctx_last_error", "fvg_ctx_stream", "fvg_ctx_synchronize",
+    "fvg_ctx_set_profiling", "fvg_ctx_get_profile", "fvg_ctx_reset_profile", "fvg_ctx_kernel_launches",
+    "fvg_matrix_create_crs", "fvg_matrix_destroy", "fvg_matrix_info", "fvg_matrix_prepare",
+    "fvg_matrix_add_storage", "fvg_matrix_device_bytes", "fvg_matrix_get_transpose", "fvg_matrix_get_ell",
+    "fvg_matrix_get_jds", "fvg_matrix_get_hybrid", "fvg_spmv", "fvg_trans_mv", "fvg_spmm",
+    "fvg_glm_params_default", "fvg_logreg_lbfgs", "fvg_logreg_sgd", "fvg_logreg_eval",
+    "fvg_logreg_predict_probability",
+]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_needed: bool = True):
+    """Loads libfvg.so, building it first when it is missing or stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_needed:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise FvgError(-1, f"{_build.LIB} is missing; run frovedis_gb300.build.build()")
+    L = C.CDLL(_build.LIB)
+    sig = {
+        "fvg_ctx_create": ([_int, C.POINTER(_p)], _int),
+        "fvg_ctx_destroy": ([_p], None),
+        "fvg_ctx_last_error": ([_p], C.c_char_p),
+        "fvg_ctx_stream": ([_p], _p),
+        "fvg_ctx_synchronize": ([_p], _int),
+        "fvg_ctx_set_profiling": ([_p, _int], _int),
+        "fvg_ctx_get_profile": ([_p, C.c_char_p, C.POINTER(_dbl), C.POINTER(_i64)], _int),
+        "fvg_ctx_reset_profile": ([_p], _int),
+        "fvg_ctx_kernel_launches": ([_p], _i64),
+        "fvg_matrix_create_crs": ([_p, _i64, _i64, _p, _p, _p, _int, _int, C.POINTER(_p)], _int),
+        "fvg_matrix_destroy": ([_p], None),
+        "fvg_matrix_info": ([_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)], _int),
+        "fvg_matrix_prepare": ([_p, _p, _int, _int], _int),
+        "fvg_matrix_add_storage": ([_p, _p, _int], _int),
+        "fvg_matrix_device_bytes": ([_p], _i64),
+        "fvg_matrix_get_transpose": ([_p, _p, _p, _p, _p], _int),
+        "fvg_matrix_get_ell": ([_p, _p, C.POINTER(_i64), _p, _p], _int),
+        "fvg_matrix_get_jds": ([_p, _p, C.POINTER(_i64), _p, _p, _p, _p], _int),
+        "fvg_matrix_get_hybrid": ([_p, _p, _p, _p, _p, _p, _p, _p, _p, _p], _int),
+        "fvg_spmv": ([_p, _p, _int, _int, _int, _p, _p, _int], _int),
+        "fvg_trans_mv": ([_p, _p, _int, _int, _int, _p, _p, _int], _int),
+        "fvg_spmm": ([_p, _p, _int, _int, _int, _p, _i64, _p, _int], _int),
+        "fvg_glm_params_default": ([C.POINTER(GlmParams)], None),
+        "fvg_logreg_lbfgs": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
+                              C.POINTER(_dbl)], _int),
+        "fvg_logreg_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
+                            C.POINTER(_dbl)], _int),
+        "fvg_logreg_eval": ([_p, _p, _int, _int, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
+        "fvg_logreg_predict_probability": ([_p, _p, _p, _dbl, _p], _int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_p)
+
+
+def _fmt(f):
+    return FORMATS[f] if isinstance(f, str) else int(f)
+
+
+def _dt(d):
+    return DTYPES[d] if isinstance(d, str) else int(d)
+
+
+class Context:
+    """One GPU, one CUDA stream (fvg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = _p()
+        rc = self.L.fvg_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise FvgError(rc, "fvg_ctx_create failed (is a CUDA GPU visible?)")
+        self.h = h
+
+    def check(self, rc):
+        if rc != 0:
+            raise FvgError(rc, self.L.fvg_ctx_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fvg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        return self.L.fvg_ctx_stream(self.h) or 0
+
+    def synchronize(self):
+        self.check(self.L.fvg_ctx_synchronize(self.h))
+
+    def set_profiling(self, on: bool):
+        self.check(self.L.fvg_ctx_set_profiling(self.h, int(on)))
+
+    def profile(self, name: str):
+        ms = _dbl()
+        n = _i64()
+        self.check(self.L.fvg_ctx_get_profile(self.h, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def reset_profile(self):
+        self.check(self.L.fvg_ctx_reset_profile(self.h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.fvg_ctx_kernel_launches(self.h))
+
+    def matrix(self, m, n, off, idx, val, on_device=False):
+        return Matrix(self, m, n, off, idx, val, on_device=on_device)
+
+
+class Matrix:
+    """Device CRS matrix (fvg_matrix) with derived layouts built on demand."""
+
+    def __init__(self, ctx: Context, m, n, off, idx, val, on_device=False):
+        self.ctx = ctx
+        self.m, self.n = int(m), int(n)
+        if on_device:  # (off, idx, val, dtype) are device pointers
+            offp, idxp, valp, dt = off, idx, val[0], val[1]
+        else:
+            off = np.ascontiguousarray(off, dtype=np.int32)
+            idx = np.ascontiguousarray(idx, dtype=np.int32)
+            if isinstance(val, np.ndarray) and val.dtype == np.float32:
+                dt = F32
+            elif isinstance(val, np.ndarray) and val.dtype == np.uint16:  # raw bf16 bits
+                dt = BF16
+            else:
+                val = np.ascontiguousarray(val, dtype=np.float64)
+                dt = F64
+            val = np.ascontiguousarray(val)
+            self._keep = (off, idx, val)
+            offp, idxp, valp = _ptr(off), _ptr(idx), _ptr(val)
+        h = _p()
+        ctx.check(ctx.L.fvg_matrix_create_crs(ctx.h, self.m, self.n, offp, idxp, valp, dt, int(on_device),
+                                              C.byref(h)))
+        self.h = h
+        self._keep = None
+        self.master = dt
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fvg_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nnz(self):
+        z = _i64()
+        self.ctx.check(self.ctx.L.fvg_matrix_info(self.h, None, None, C.byref(z)))
+        return z.value
+
+    def prepare(self, fmt="CRS", transpose=True):
+        self.ctx.check(self.ctx.L.fvg_matrix_prepare(self.ctx.h, self.h, _fmt(fmt), int(transpose)))
+
+    def add_storage(self, storage):
+        self.ctx.check(self.ctx.L.fvg_matrix_add_storage(self.ctx.h, self.h, _dt(storage)))
+
+    @property
+    def device_bytes(self):
+        return int(self.ctx.L.fvg_matrix_device_bytes(self.h))
+
+    # --- products -------------------------------------------------------
+    def _product(self, fn, x, nout, fmt, storage, vec):
+        vd = np.float64 if _dt(vec) == F64 else np.float32
+        x = np.ascontiguousarray(x, dtype=vd)
+        y = np.zeros(nout, dtype=vd)
+        self.ctx.check(fn(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), _ptr(x), _ptr(y), 0))
+        return y
+
+    def spmv(self, x, fmt="CRS", storage="f64", vec="f64"):
+        return self._product(self.ctx.L.fvg_spmv, x, self.m, fmt, storage, vec)
+
+    def trans_mv(self, x, fmt="CRS", storage="f64", vec="f64"):
+        return self._product(self.ctx.L.fvg_trans_mv, x, self.n, fmt, storage, vec)
+
+    def spmv_device(self, xptr, yptr, fmt="CRS", storage="f64", vec="f64"):
+        self.ctx.check(self.ctx.L.fvg_spmv(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), xptr, yptr, 1))
+
+    def trans_mv_device(self, xptr, yptr, fmt="CRS", storage="f64", vec="f64"):
+        self.ctx.check(self.ctx.L.fvg_trans_mv(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), xptr, yptr,
+                                               1))
+
+    def spmm(self, X, fmt="CRS", storage="f64", vec="f64"):
+        vd = np.float64 if _dt(vec) == F64 else np.float32
+        X = np.ascontiguousarray(X, dtype=vd)
+        k = X.shape[1]
+        Y = np.zeros((self.m, k), dtype=vd)
+        self.ctx.check(self.ctx.L.fvg_spmm(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), _ptr(X), k,
+                                           _ptr(Y), 0))
+        return Y
+
+    # --- derived layouts (host copies) ----------------------------------
+    def get_transpose(self):
+        toff = np.zeros(self.n + 1, dtype=np.int32)
+        tidx = np.zeros(max(self.nnz, 1), dtype=np.int32)
+        tval = np.zeros(max(self.nnz, 1))
+        self.ctx.check(self.ctx.L.fvg_matrix_get_transpose(self.ctx.h, self.h, _ptr(toff), _ptr(tidx), _ptr(tval)))
+        z = self.nnz
+        return toff, tidx[:z], tval[:z]
+
+    def get_ell(self):
+        w = _i64()
+        self.ctx.check(self.ctx.L.fvg_matrix_get_ell(self.ctx.h, self.h, C.byref(w), None, None))
+        cells = self.m * w.value
+        eidx = np.zeros(max(cells, 1), dtype=np.int32)
+        ev = np.zeros(max(cells, 1))
+        self.ctx.check(self.ctx.L.fvg_matrix_get_ell(self.ctx.h, self.h, C.byref(w), _ptr(eidx), _ptr(ev)))
+        return w.value, eidx[:cells], ev[:cells]
+
+    def get_jds(self):
+        nd = _i64()
+        self.ctx.check(self.ctx.L.fvg_matrix_get_jds(self.ctx.h, self.h, C.byref(nd), None, None, None, None))
+        z = self.nnz
+        perm = np.zeros(max(self.m, 1), dtype=np.int32)
+        joff = np.zeros(nd.value + 1, dtype=np.int64)
+        jidx = np.zeros(max(z, 1), dtype=np.int32)
+        jval = np.zeros(max(z, 1))
+        self.ctx.check(self.ctx.L.fvg_matrix_get_jds(self.ctx.h, self.h, C.byref(nd), _ptr(perm), _ptr(joff),
+                                                     _ptr(jidx), _ptr(jval)))
+        return perm[: self.m if z else 0], joff, jidx[:z], jval[:z]
+
+    def get_hybrid(self):
+        info = np.zeros(5, dtype=np.int64)
+        L = self.ctx.L
+        self.ctx.check(L.fvg_matrix_get_hybrid(self.ctx.h, self.h, _ptr(info), None, None, None, None, None, None,
+                                               None))
+        nd, crows, cnnz, jnnz, plen = (int(v) for v in info)
+        perm = np.zeros(max(self.m, 1), dtype=np.int32)
+        joff = np.zeros(nd + 1, dtype=np.int64)
+        jidx = np.zeros(max(jnnz, 1), dtype=np.int32)
+        jval = np.zeros(max(jnnz, 1))
+        coff = np.zeros(crows + 1, dtype=np.int64)
+        cidx = np.zeros(max(cnnz, 1), dtype=np.int32)
+        cval = np.zeros(max(cnnz, 1))
+        self.ctx.check(L.fvg_matrix_get_hybrid(self.ctx.h, self.h, _ptr(info), _ptr(perm), _ptr(joff), _ptr(jidx),
+                                               _ptr(jval), _ptr(coff), _ptr(cidx), _ptr(cval)))
+        return dict(perm=perm[:plen], joff=joff, jidx=jidx[:jnnz], jval=jval[:jnnz], coff=coff,
+                    cidx=cidx[:cnnz], cval=cval[:cnnz], crs_rows=crows)
+
+
+def glm_params(**kw) -> GlmParams:
+    p = GlmParams()
+    load().fvg_glm_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k in ("reg_type",) and isinstance(v, str):
+            v = REG[v]
+        if k in ("mat_type",):
+            v = _fmt(v)
+        if k in ("storage",):
+            v = _dt(v)
+        setattr(p, k, v)
+    return p
+
+
+def _train(fn, mat: Matrix, label, sample_weight=None, w0=None, b0=None, trace=False, row_splits=None, **kw):
+    ctx = mat.ctx
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
+    icpt = bool(kw.get("intercept", False))
+    w = np.ones(mat.n) if w0 is None else np.array(w0, dtype=np.float64)  # weight init = 1 (linear_model.hpp:310)
+    b = C.c_double((1.0 if icpt else 0.0) if b0 is None else float(b0))
+    kw["intercept"] = int(icpt)
+    p = glm_params(**kw)
+    tr = None
+    if trace:
+        tr = np.zeros(4 * p.num_iteration)
+        p.trace = tr.ctypes.data_as(C.POINTER(C.c_double))
+    sp = None
+    if row_splits is not None:
+        sp = np.ascontiguousarray(row_splits, dtype=np.int64)
+        p.num_partitions = len(sp) - 1
+        p.row_splits = sp.ctypes.data_as(C.POINTER(C.c_int64))
+    n_iter = _i64()
+    loss = _dbl()
+    ctx.check(fn(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), _ptr(w), C.byref(b), C.byref(n_iter),
+                 C.byref(loss)))
+    out = dict(w=w, b=b.value, n_iter=n_iter.value, loss=loss.value)
+    if trace:
+        out["trace"] = tr.reshape(-1, 4)[: n_iter.value]
+    return out
+
+
+def logreg_lbfgs(mat: Matrix, label, **kw):
+    """logistic_regression_with_lbfgs::train (defaults as in the reference)."""
+    return _train(mat.ctx.L.fvg_logreg_lbfgs, mat, label, **kw)
+
+
+def logreg_sgd(mat: Matrix, label, **kw):
+    """logistic_regression_with_sgd::train (defaults as in the reference)."""
+    return _train(mat.ctx.L.fvg_logreg_sgd, mat, label, **kw)
+
+
+def logreg_eval(mat: Matrix, label, w, b=0.0, intercept=False, sample_weight=None, fmt="CRS", storage="f64"):
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    g = np.zeros(mat.n + 1)
+    loss = _dbl()
+    mat.ctx.check(mat.ctx.L.fvg_logreg_eval(mat.ctx.h, mat.h, _fmt(fmt), _dt(storage), _ptr(label), _ptr(sw),
+                                            _ptr(w), float(b), int(intercept), _ptr(g), C.byref(loss)))
+    return g, loss.value
+
+
+def predict_probability(mat: Matrix, w, b=0.0):
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.zeros(mat.m)
+    mat.ctx.check(mat.ctx.L.fvg_logreg_predict_probability(mat.ctx.h, mat.h, _ptr(w), float(b), _ptr(out)))
+    return out
+
+
+def bf16_bits(x) -> np.ndarray:
+    """Round-to-nearest-even FP64/FP32 → bf16 bit patterns (uint16)."""
+    f = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+    rounding = ((f >> 16) & 1) + 0x7FFF
+    return ((f + rounding) >> 16).astype(np.uint16)

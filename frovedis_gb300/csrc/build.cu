@@ -1,0 +1,578 @@
+// Device-side builders: CRS upload and checks, the transposed CRS copy
+// (crs_matrix.hpp:356-412), the row-bin schedule of the CRS kernel, and the
+// ELL / JDS / JDS-CRS-hybrid layouts (ell_matrix.hpp:63-95,
+// jds_matrix.hpp:81-146, jds_crs_hybrid.hpp:38-153).
+#include <algorithm>
+
+#include "fvg_internal.cuh"
+
+namespace fvg {
+
+static unsigned grid_n(i64 n, int threads = 256) {
+  i64 g = (n + threads - 1) / threads;
+  if (g > 152 * 32) g = 152 * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+#define GRID_STRIDE(i, n) for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (i64)gridDim.x * blockDim.x)
+
+static int bits_for(i64 maxval) {  // bits needed to represent values in [0, maxval]
+  int b = 0;
+  while (b < 62 && (1ll << b) <= maxval) b++;
+  return b;
+}
+
+static void alloc_plane(fvg_ctx* c, DBuf& b, i64 n, int dt) {
+  b.alloc((size_t)(n + kPad) * dtype_size(dt), c->stream);
+  FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * dtype_size(dt), 0, (size_t)kPad * dtype_size(dt), c->stream));
+}
+
+void ensure_plane_generic(fvg_ctx* c, DBuf* planes, i64 n, int dt, int master) {
+  if (planes[dt].p) return;
+  if (!planes[master].p) fail(FVG_ERR_INTERNAL, "value plane missing");
+  if (dt == FVG_F64 && master != FVG_F64)
+    fail(FVG_ERR_INVALID_ARG, "FP64 storage requested for a matrix uploaded with lower-precision values");
+  alloc_plane(c, planes[dt], n, dt);
+  convert_values(c, planes[master].p, master, planes[dt].p, dt, n);
+}
+
+void crs_ensure_plane(fvg_ctx* c, DevCRS& a, int dt, int master) { ensure_plane_generic(c, a.val, a.nnz, dt, master); }
+
+// ------------------------------------------------------------------ upload
+__global__ void k_check_crs(const i32* __restrict__ off, const i32* __restrict__ idx, i64 m, i64 n, i64 nnz,
+                            unsigned long long* __restrict__ flags /* [0]=bad off, [1]=bad idx, [2]=max len */) {
+  GRID_STRIDE(r, m) {
+    i32 s = off[r], e = off[r + 1];
+    if (e < s || s < 0 || e > nnz) atomicAdd(&flags[0], 1ull);
+    else atomicMax(&flags[2], (unsigned long long)(e - s));
+  }
+  GRID_STRIDE(p, nnz) {
+    i32 c = idx[p];
+    if (c < 0 || c >= n) atomicAdd(&flags[1], 1ull);
+  }
+}
+
+void crs_upload(fvg_ctx* c, DevCRS& a, i64 m, i64 n, const i32* off, const i32* idx, const void* val, int dt,
+                bool on_device) {
+  if (m < 0 || n < 0) fail(FVG_ERR_INVALID_ARG, "negative matrix dimension");
+  if (!off) fail(FVG_ERR_INVALID_ARG, "null row offsets");
+  i32 first = 0, last = 0;
+  cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (on_device) {
+    FVG_CUDA(cudaMemcpyAsync(&first, off, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaMemcpyAsync(&last, off + m, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+  } else {
+    first = off[0];
+    last = off[m];
+  }
+  if (first != 0) fail(FVG_ERR_INVALID_ARG, "row offsets must start at 0");
+  if (last < 0) fail(FVG_ERR_INVALID_ARG, "negative nnz");
+  i64 nnz = last;
+  if (nnz > 0 && (!idx || !val)) fail(FVG_ERR_INVALID_ARG, "null idx/val");
+  a.m = m;
+  a.n = n;
+  a.nnz = nnz;
+  a.off.alloc(sizeof(i32) * (m + 1), c->stream);
+  a.idx.alloc(sizeof(i32) * (nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(a.off.p, off, sizeof(i32) * (m + 1), kind, c->stream));
+  FVG_CUDA(cudaMemsetAsync(a.idx.as<i32>() + nnz, 0, sizeof(i32) * kPad, c->stream));
+  if (nnz) FVG_CUDA(cudaMemcpyAsync(a.idx.p, idx, sizeof(i32) * nnz, kind, c->stream));
+  alloc_plane(c, a.val[dt], nnz, dt);
+  if (nnz) FVG_CUDA(cudaMemcpyAsync(a.val[dt].p, val, (size_t)dtype_size(dt) * nnz, kind, c->stream));
+  DBuf flags;
+  flags.alloc(sizeof(unsigned long long) * 3, c->stream);
+  FVG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(unsigned long long) * 3, c->stream));
+  k_check_crs<<<grid_n(std::max(m, nnz)), 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), m, n, nnz,
+                                                                flags.as<unsigned long long>());
+  check_launch("check_crs");
+  count_launch(c);
+  unsigned long long h[3];
+  FVG_CUDA(cudaMemcpyAsync(h, flags.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  if (h[0]) fail(FVG_ERR_INVALID_ARG, "row offsets are not non-decreasing within [0, nnz]");
+  if (h[1]) fail(FVG_ERR_INVALID_ARG, "column index out of range [0, num_col)");
+  a.max_row = (i64)h[2];
+}
+
+__global__ void k_max_row(const i32* __restrict__ off, i64 m, unsigned long long* __restrict__ mx) {
+  GRID_STRIDE(r, m) atomicMax(mx, (unsigned long long)(off[r + 1] - off[r]));
+}
+
+static i64 max_row_len(fvg_ctx* c, const i32* off, i64 m) {
+  if (m <= 0) return 0;
+  DBuf mx;
+  mx.alloc(sizeof(unsigned long long), c->stream);
+  FVG_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), c->stream));
+  k_max_row<<<grid_n(m), 256, 0, c->stream>>>(off, m, mx.as<unsigned long long>());
+  check_launch("max_row");
+  count_launch(c);
+  unsigned long long h = 0;
+  FVG_CUDA(cudaMemcpyAsync(&h, mx.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  return (i64)h;
+}
+
+// --------------------------------------------------------------- transpose
+__global__ void k_iota_u32(uint32_t* p, i64 n) { GRID_STRIDE(i, n) p[i] = (uint32_t)i; }
+
+// toff[c] = first sorted position whose column is >= c
+__global__ void k_boundaries(const uint32_t* __restrict__ keys, i64 nnz, i64 ncols, i32* __restrict__ toff) {
+  GRID_STRIDE(i, nnz + 1) {
+    i64 prev = (i == 0) ? -1 : (i64)keys[i - 1];
+    i64 cur = (i == nnz) ? ncols : (i64)keys[i];
+    for (i64 c = prev + 1; c <= cur; c++) toff[c] = (i32)i;
+  }
+}
+
+// row of element e = last r with off[r] <= e (empty rows skipped)
+__device__ __forceinline__ i32 row_of(const i32* __restrict__ off, i64 m, i64 e) {
+  i64 lo = 0, hi = m;  // off[lo] <= e < off[hi] invariant (off[m] = nnz > e)
+  while (hi - lo > 1) {
+    i64 mid = (lo + hi) >> 1;
+    if (off[mid] <= e) lo = mid;
+    else hi = mid;
+  }
+  return (i32)lo;
+}
+
+__global__ void k_trans_rows(const uint32_t* __restrict__ src, const i32* __restrict__ off, i64 m, i64 nnz,
+                             i32* __restrict__ tidx) {
+  GRID_STRIDE(p, nnz) tidx[p] = row_of(off, m, (i64)src[p]);
+}
+
+void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
+  ProfScope ps(c, P_TRANSPOSE);
+  t.m = a.n;
+  t.n = a.m;
+  t.nnz = a.nnz;
+  t.off.alloc(sizeof(i32) * (t.m + 1), c->stream);
+  t.idx.alloc(sizeof(i32) * (t.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(t.idx.as<i32>() + t.nnz, 0, sizeof(i32) * kPad, c->stream));
+  alloc_plane(c, t.val[master], t.nnz, master);
+  if (a.nnz == 0) {
+    fill_i32(c, t.off.as<i32>(), 0, t.m + 1);
+    t.max_row = 0;
+    return;
+  }
+  DBuf keys, src;
+  keys.alloc(sizeof(uint32_t) * a.nnz, c->stream);
+  src.alloc(sizeof(uint32_t) * a.nnz, c->stream);
+  FVG_CUDA(cudaMemcpyAsync(keys.p, a.idx.p, sizeof(uint32_t) * a.nnz, cudaMemcpyDeviceToDevice, c->stream));
+  k_iota_u32<<<grid_n(a.nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), a.nnz);
+  check_launch("iota");
+  count_launch(c);
+  // stable by element position == stable in source-row order
+  radix_sort_pairs(c, keys.as<uint32_t>(), src.as<uint32_t>(), a.nnz, bits_for(a.n - 1));
+  k_boundaries<<<grid_n(a.nnz + 1), 256, 0, c->stream>>>(keys.as<uint32_t>(), a.nnz, a.n, t.off.as<i32>());
+  k_trans_rows<<<grid_n(a.nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), a.off.as<i32>(), a.m, a.nnz,
+                                                      t.idx.as<i32>());
+  check_launch("transpose");
+  count_launch(c, 2);
+  gather_values(c, a.val[master].p, src.as<uint32_t>(), t.val[master].p, master, a.nnz);
+  t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
+}
+
+// ---------------------------------------------------------------- schedule
+__host__ __device__ __forceinline__ int row_bin(i64 len, int ve) {
+  if (len == 0) return 0;
+  i64 nv = (len + ve - 1) / ve + 1;  // vectors touched, worst-case alignment
+  if (nv <= 2) return 0;
+  if (nv <= 4) return 1;
+  if (nv <= 8) return 2;
+  if (nv <= 16) return 3;
+  if (nv <= 32) return 4;
+  if (nv <= 256) return 5;
+  if (len <= kCtaRowMax) return 6;
+  return 7;
+}
+
+__global__ void k_row_bins(const i32* __restrict__ off, i64 m, int ve, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals, unsigned long long* __restrict__ counts) {
+  __shared__ unsigned long long cnt[kBins];
+  if (threadIdx.x < kBins) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  GRID_STRIDE(r, m) {
+    int b = row_bin((i64)off[r + 1] - off[r], ve);
+    keys[r] = (uint32_t)b;
+    vals[r] = (uint32_t)r;
+    atomicAdd(&cnt[b], 1ull);
+  }
+  __syncthreads();
+  if (threadIdx.x < kBins && cnt[threadIdx.x]) atomicAdd(&counts[threadIdx.x], cnt[threadIdx.x]);
+}
+
+__global__ void k_long_chunks(const i32* __restrict__ off, const i32* __restrict__ rows, i64 nlong,
+                              i64* __restrict__ nch) {
+  GRID_STRIDE(i, nlong) {
+    i64 s = off[rows[i]], e = off[rows[i] + 1];
+    i64 base = s & ~7ll;
+    nch[i] = (e - base + kChunk - 1) / kChunk;
+  }
+}
+
+__global__ void k_fill_chunks(const i32* __restrict__ off, const i32* __restrict__ rows, i64 nlong,
+                              const i64* __restrict__ first, i32* __restrict__ c0, i32* __restrict__ crow,
+                              i32* __restrict__ cbeg) {
+  GRID_STRIDE(i, nlong) {
+    i32 r = rows[i];
+    i64 s = off[r], e = off[r + 1];
+    i64 base = s & ~7ll;
+    i64 f = first[i], nc = (e - base + kChunk - 1) / kChunk;
+    c0[i] = (i32)f;
+    for (i64 j = 0; j < nc; j++) {
+      crow[f + j] = r;
+      cbeg[f + j] = (i32)(j == 0 ? s : base + j * kChunk);
+    }
+    if (i == nlong - 1) c0[nlong] = (i32)(f + nc);
+  }
+}
+
+const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int ve) {
+  int slot = (ve == 8) ? 1 : 0;
+  if (a.sched[slot]) return *a.sched[slot];
+  auto s = std::make_unique<Sched>();
+  s->ve = ve;
+  i64 m = a.m;
+  DBuf keys, cnt;
+  s->rows.alloc(sizeof(uint32_t) * std::max<i64>(m, 1), c->stream);
+  keys.alloc(sizeof(uint32_t) * std::max<i64>(m, 1), c->stream);
+  cnt.alloc(sizeof(unsigned long long) * kBins, c->stream);
+  FVG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long) * kBins, c->stream));
+  if (m > 0) {
+    k_row_bins<<<grid_n(m), 256, 0, c->stream>>>(a.off.as<i32>(), m, ve, keys.as<uint32_t>(),
+                                                  s->rows.as<uint32_t>(), cnt.as<unsigned long long>());
+    check_launch("row_bins");
+    count_launch(c);
+    radix_sort_pairs(c, keys.as<uint32_t>(), s->rows.as<uint32_t>(), m, 3);
+  }
+  unsigned long long h[kBins];
+  FVG_CUDA(cudaMemcpyAsync(h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  s->row_start[0] = 0;
+  for (int b = 0; b < kBins; b++) s->row_start[b + 1] = s->row_start[b] + (i64)h[b];
+  s->nlong = (i64)h[7];
+  s->nchunks = 0;
+  if (s->nlong > 0) {
+    DBuf nch, first;
+    nch.alloc(sizeof(i64) * s->nlong, c->stream);
+    first.alloc(sizeof(i64) * (s->nlong + 1), c->stream);
+    const i32* lrows = s->rows.as<i32>() + s->row_start[7];
+    k_long_chunks<<<grid_n(s->nlong), 256, 0, c->stream>>>(a.off.as<i32>(), lrows, s->nlong, nch.as<i64>());
+    check_launch("long_chunks");
+    count_launch(c);
+    scan_i64(c, nch.as<i64>(), first.as<i64>(), s->nlong);
+    i64 tot = 0;
+    FVG_CUDA(cudaMemcpyAsync(&tot, first.as<i64>() + s->nlong, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+    s->nchunks = tot;
+    s->long_rows.alloc(sizeof(i32) * s->nlong, c->stream);
+    FVG_CUDA(cudaMemcpyAsync(s->long_rows.p, lrows, sizeof(i32) * s->nlong, cudaMemcpyDeviceToDevice, c->stream));
+    s->long_chunk0.alloc(sizeof(i32) * (s->nlong + 1), c->stream);
+    s->chunk_row.alloc(sizeof(i32) * tot, c->stream);
+    s->chunk_beg.alloc(sizeof(i32) * tot, c->stream);
+    k_fill_chunks<<<grid_n(s->nlong), 256, 0, c->stream>>>(a.off.as<i32>(), lrows, s->nlong, first.as<i64>(),
+                                                          s->long_chunk0.as<i32>(), s->chunk_row.as<i32>(),
+                                                          s->chunk_beg.as<i32>());
+    check_launch("fill_chunks");
+    count_launch(c);
+  }
+  // work items: bins 0-5 hold 256/L rows per item, bin 6 one row, bin 7 one chunk
+  s->item_start[0] = 0;
+  for (int b = 0; b < kBins; b++) {
+    i64 rows = s->row_start[b + 1] - s->row_start[b];
+    i64 items;
+    if (b <= 5) {
+      i64 per = kThreads >> b;
+      items = (rows + per - 1) / per;
+    } else if (b == 6) {
+      items = rows;
+    } else {
+      items = s->nchunks;
+    }
+    s->item_start[b + 1] = s->item_start[b] + items;
+  }
+  a.sched[slot] = std::move(s);
+  return *a.sched[slot];
+}
+
+// --------------------------------------------------------------------- ELL
+template <class T>
+__global__ void k_ell_fill(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,
+                           i64 m, i32* __restrict__ eidx, T* __restrict__ eval) {
+  GRID_STRIDE(r, m) {
+    i64 s = off[r], e = off[r + 1];
+    for (i64 k = 0; k < e - s; k++) {
+      eidx[m * k + r] = idx[s + k];
+      eval[m * k + r] = val[s + k];
+    }
+  }
+}
+
+void ell_build(fvg_ctx* c, const DevCRS& a, DevELL& e, int master) {
+  e.m = a.m;
+  e.n = a.n;
+  e.width = (a.m == 0) ? 0 : a.max_row;
+  double bytes = (double)a.m * (double)e.width * (4.0 + dtype_size(master));
+  size_t freeb = 0, totb = 0;
+  cudaMemGetInfo(&freeb, &totb);
+  if (bytes > 0.6 * (double)freeb)
+    fail(FVG_ERR_OUT_OF_MEMORY, "ELL layout needs " + std::to_string(bytes / 1e9) + " GB (num_row x longest row)");
+  i64 cells = a.m * e.width;
+  e.idx.alloc(sizeof(i32) * (cells + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(e.idx.p, 0, sizeof(i32) * (cells + kPad), c->stream));
+  e.val[master].alloc((size_t)dtype_size(master) * (cells + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(e.val[master].p, 0, (size_t)dtype_size(master) * (cells + kPad), c->stream));
+  if (cells == 0) return;
+  unsigned g = grid_n(a.m);
+  if (master == FVG_F64)
+    k_ell_fill<double><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<double>(), a.m,
+                                                 e.idx.as<i32>(), e.val[master].as<double>());
+  else if (master == FVG_F32)
+    k_ell_fill<float><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<float>(), a.m,
+                                                e.idx.as<i32>(), e.val[master].as<float>());
+  else
+    k_ell_fill<bf16><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<bf16>(), a.m,
+                                               e.idx.as<i32>(), e.val[master].as<bf16>());
+  check_launch("ell_fill");
+  count_launch(c);
+}
+
+// --------------------------------------------------------------------- JDS
+__global__ void k_jds_keys(const i32* __restrict__ off, i64 m, i64 maxlen, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals, i64* __restrict__ lenhist) {
+  GRID_STRIDE(i, m) {
+    i64 r = m - 1 - i;  // rows listed in descending order: ties end up larger row first
+    i64 len = (i64)off[r + 1] - off[r];
+    keys[i] = (uint32_t)(maxlen - len);
+    vals[i] = (uint32_t)r;
+    atomicAdd((unsigned long long*)&lenhist[len], 1ull);
+  }
+}
+
+// count_gt[d] = number of rows longer than d = m - (rows with len <= d)
+__global__ void k_count_gt(const i64* __restrict__ ex, i64 m, i64 ndiag, i64* __restrict__ cgt) {
+  GRID_STRIDE(d, ndiag) cgt[d] = m - ex[d + 1];
+}
+
+template <class T>
+__global__ void k_jds_fill(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,
+                           const i32* __restrict__ perm, i64 m, const i64* __restrict__ joff, i64 cap,
+                           i32* __restrict__ jidx, T* __restrict__ jval) {
+  GRID_STRIDE(p, m) {
+    i32 r = perm[p];
+    i64 s = off[r], len = (i64)off[r + 1] - s;
+    if (len > cap) len = cap;
+    for (i64 d = 0; d < len; d++) {
+      i64 q = joff[d] + p;
+      jidx[q] = idx[s + d];
+      jval[q] = val[s + d];
+    }
+  }
+}
+
+static void jds_order(fvg_ctx* c, const DevCRS& a, DBuf& perm, i64 ndiag, DBuf& joff) {
+  i64 m = a.m;
+  DBuf keys, hist, ex, cgt;
+  perm.alloc(sizeof(i32) * std::max<i64>(m, 1), c->stream);
+  keys.alloc(sizeof(uint32_t) * std::max<i64>(m, 1), c->stream);
+  hist.alloc(sizeof(i64) * (a.max_row + 1), c->stream);
+  ex.alloc(sizeof(i64) * (a.max_row + 2), c->stream);
+  FVG_CUDA(cudaMemsetAsync(hist.p, 0, sizeof(i64) * (a.max_row + 1), c->stream));
+  k_jds_keys<<<grid_n(m), 256, 0, c->stream>>>(a.off.as<i32>(), m, a.max_row, keys.as<uint32_t>(),
+                                                perm.as<uint32_t>(), hist.as<i64>());
+  check_launch("jds_keys");
+  count_launch(c);
+  radix_sort_pairs(c, keys.as<uint32_t>(), perm.as<uint32_t>(), m, bits_for(a.max_row));
+  scan_i64(c, hist.as<i64>(), ex.as<i64>(), a.max_row + 1);
+  cgt.alloc(sizeof(i64) * std::max<i64>(ndiag, 1), c->stream);
+  joff.alloc(sizeof(i64) * (ndiag + 1), c->stream);
+  if (ndiag > 0) {
+    k_count_gt<<<grid_n(ndiag), 256, 0, c->stream>>>(ex.as<i64>(), m, ndiag, cgt.as<i64>());
+    check_launch("count_gt");
+    count_launch(c);
+  }
+  scan_i64(c, cgt.as<i64>(), joff.as<i64>(), ndiag);
+}
+
+template <class T>
+static void launch_jds_fill(fvg_ctx* c, const DevCRS& a, int master, const i32* perm, i64 rows, const i64* joff,
+                            i64 cap, i32* jidx, void* jval) {
+  if (rows <= 0) return;
+  k_jds_fill<T><<<grid_n(rows), 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<T>(), perm,
+                                                      rows, joff, cap, jidx, (T*)jval);
+  check_launch("jds_fill");
+  count_launch(c);
+}
+
+static void jds_fill(fvg_ctx* c, const DevCRS& a, int master, const i32* perm, i64 rows, const i64* joff, i64 cap,
+                     i32* jidx, void* jval) {
+  if (master == FVG_F64) launch_jds_fill<double>(c, a, master, perm, rows, joff, cap, jidx, jval);
+  else if (master == FVG_F32) launch_jds_fill<float>(c, a, master, perm, rows, joff, cap, jidx, jval);
+  else launch_jds_fill<bf16>(c, a, master, perm, rows, joff, cap, jidx, jval);
+}
+
+void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master) {
+  j.m = a.m;
+  j.n = a.n;
+  j.nnz = a.nnz;
+  if (a.nnz == 0) {  // jds_matrix.hpp:87-90: empty perm, off = {0}
+    j.ndiag = 0;
+    j.empty_perm = true;
+    j.off.alloc(sizeof(i64), c->stream);
+    FVG_CUDA(cudaMemsetAsync(j.off.p, 0, sizeof(i64), c->stream));
+    j.perm.alloc(sizeof(i32), c->stream);
+    j.idx.alloc(sizeof(i32) * kPad, c->stream);
+    alloc_plane(c, j.val[master], 0, master);
+    return;
+  }
+  j.ndiag = a.max_row;
+  jds_order(c, a, j.perm, j.ndiag, j.off);
+  j.idx.alloc(sizeof(i32) * (a.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(j.idx.as<i32>() + a.nnz, 0, sizeof(i32) * kPad, c->stream));
+  alloc_plane(c, j.val[master], a.nnz, master);
+  jds_fill(c, a, master, j.perm.as<i32>(), a.m, j.off.as<i64>(), j.ndiag, j.idx.as<i32>(), j.val[master].p);
+}
+
+// ------------------------------------------------------------------ hybrid
+template <class T>
+__global__ void k_hyb_tail(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,
+                           const i32* __restrict__ perm, i64 rows, i64 start, const i32* __restrict__ coff,
+                           i32* __restrict__ cidx, T* __restrict__ cval) {
+  for (i64 i = blockIdx.x; i < rows; i += gridDim.x) {
+    i32 r = perm[i];
+    i64 s = (i64)off[r] + start, e = off[r + 1];
+    i64 o = coff[i];
+    for (i64 k = s + threadIdx.x; k < e; k += blockDim.x) {
+      cidx[o + (k - s)] = idx[k];
+      cval[o + (k - s)] = val[k];
+    }
+  }
+}
+
+__global__ void k_sorted_lens(const i32* __restrict__ off, const i32* __restrict__ perm, i64 cnt,
+                              i64* __restrict__ lens) {
+  GRID_STRIDE(i, cnt) lens[i] = (i64)off[perm[i] + 1] - off[perm[i]];
+}
+
+__global__ void k_iota_i32(i32* p, i64 n) { GRID_STRIDE(i, n) p[i] = (i32)i; }
+
+void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 thr) {
+  h.m = a.m;
+  h.n = a.n;
+  h.jds.m = a.m;
+  h.jds.n = a.n;
+  auto copy_crs = [&](DevCRS& dst) {
+    dst.m = a.m; dst.n = a.n; dst.nnz = a.nnz; dst.max_row = a.max_row;
+    dst.off.alloc(sizeof(i32) * (a.m + 1), c->stream);
+    FVG_CUDA(cudaMemcpyAsync(dst.off.p, a.off.p, sizeof(i32) * (a.m + 1), cudaMemcpyDeviceToDevice, c->stream));
+    dst.idx.alloc(sizeof(i32) * (a.nnz + kPad), c->stream);
+    FVG_CUDA(cudaMemcpyAsync(dst.idx.p, a.idx.p, sizeof(i32) * (a.nnz + kPad), cudaMemcpyDeviceToDevice, c->stream));
+    alloc_plane(c, dst.val[master], a.nnz, master);
+    FVG_CUDA(cudaMemcpyAsync(dst.val[master].p, a.val[master].p, (size_t)dtype_size(master) * a.nnz,
+                             cudaMemcpyDeviceToDevice, c->stream));
+  };
+  auto empty_jds = [&](bool identity) {
+    h.jds.ndiag = 0;
+    h.jds.nnz = 0;
+    h.jds.off.alloc(sizeof(i64), c->stream);
+    FVG_CUDA(cudaMemsetAsync(h.jds.off.p, 0, sizeof(i64), c->stream));
+    h.jds.idx.alloc(sizeof(i32) * kPad, c->stream);
+    alloc_plane(c, h.jds.val[master], 0, master);
+    h.jds.perm.alloc(sizeof(i32) * std::max<i64>(a.m, 1), c->stream);
+    if (identity) {
+      k_iota_i32<<<grid_n(a.m), 256, 0, c->stream>>>(h.jds.perm.as<i32>(), a.m);
+      check_launch("iota");
+      count_launch(c);
+    }
+    h.jds.empty_perm = !identity;
+  };
+  if (a.nnz == 0) {  // jds_crs_hybrid.hpp:47-49
+    copy_crs(h.crs);
+    empty_jds(false);
+    h.crs_rows = a.m;
+    h.all_crs = true;
+    return;
+  }
+  if (a.m <= thr) {  // 50-56: CRS part is the whole matrix, perm = identity
+    copy_crs(h.crs);
+    empty_jds(true);
+    h.crs_rows = a.m;
+    h.all_crs = true;
+    return;
+  }
+  if (thr == 0) {  // 57-61
+    jds_build(c, a, h.jds, master);
+    h.crs_rows = 0;
+    h.crs.m = 0; h.crs.n = a.n; h.crs.nnz = 0;
+    h.crs.off.alloc(sizeof(i32), c->stream);
+    FVG_CUDA(cudaMemsetAsync(h.crs.off.p, 0, sizeof(i32), c->stream));
+    h.crs.idx.alloc(sizeof(i32) * kPad, c->stream);
+    alloc_plane(c, h.crs.val[master], 0, master);
+    return;
+  }
+  // 86-153: full JDS order, JDS width = length at sorted position thr
+  DBuf joff_full;
+  jds_order(c, a, h.jds.perm, a.max_row, joff_full);
+  std::vector<i64> lens(thr + 1);
+  {
+    DBuf dl;
+    dl.alloc(sizeof(i64) * (thr + 1), c->stream);
+    k_sorted_lens<<<grid_n(thr + 1), 256, 0, c->stream>>>(a.off.as<i32>(), h.jds.perm.as<i32>(), thr + 1,
+                                                           dl.as<i64>());
+    check_launch("sorted_lens");
+    count_launch(c);
+    FVG_CUDA(cudaMemcpyAsync(lens.data(), dl.p, sizeof(i64) * (thr + 1), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  i64 start = lens[thr];
+  i64 crs_rows = thr;
+  for (; crs_rows != 0; crs_rows--)
+    if (lens[crs_rows - 1] != start) break;
+  std::vector<i32> hcoff(crs_rows + 1, 0);
+  for (i64 i = 0; i < crs_rows; i++) hcoff[i + 1] = hcoff[i] + (i32)(lens[i] - start);
+  i64 crs_size = hcoff[crs_rows];
+  h.crs_rows = crs_rows;
+  h.all_crs = false;
+  // JDS part: first `start` elements of every row
+  h.jds.ndiag = start;
+  h.jds.nnz = a.nnz - crs_size;
+  h.jds.off.alloc(sizeof(i64) * (start + 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(h.jds.off.p, joff_full.p, sizeof(i64) * (start + 1), cudaMemcpyDeviceToDevice,
+                           c->stream));
+  h.jds.idx.alloc(sizeof(i32) * (h.jds.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(h.jds.idx.as<i32>() + h.jds.nnz, 0, sizeof(i32) * kPad, c->stream));
+  alloc_plane(c, h.jds.val[master], h.jds.nnz, master);
+  jds_fill(c, a, master, h.jds.perm.as<i32>(), a.m, h.jds.off.as<i64>(), start, h.jds.idx.as<i32>(),
+           h.jds.val[master].p);
+  // CRS tail of the crs_rows longest rows, in sorted order
+  h.crs.m = crs_rows;
+  h.crs.n = a.n;
+  h.crs.nnz = crs_size;
+  h.crs.max_row = crs_rows ? lens[0] - start : 0;
+  h.crs.off.alloc(sizeof(i32) * (crs_rows + 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(h.crs.off.p, hcoff.data(), sizeof(i32) * (crs_rows + 1), cudaMemcpyHostToDevice,
+                           c->stream));
+  h.crs.idx.alloc(sizeof(i32) * (crs_size + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(h.crs.idx.as<i32>() + crs_size, 0, sizeof(i32) * kPad, c->stream));
+  alloc_plane(c, h.crs.val[master], crs_size, master);
+  if (crs_rows > 0) {
+    unsigned g = (unsigned)std::min<i64>(crs_rows, 4096);
+    if (master == FVG_F64)
+      k_hyb_tail<double><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<double>(),
+                                                   h.jds.perm.as<i32>(), crs_rows, start, h.crs.off.as<i32>(),
+                                                   h.crs.idx.as<i32>(), h.crs.val[master].as<double>());
+    else if (master == FVG_F32)
+      k_hyb_tail<float><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<float>(),
+                                                  h.jds.perm.as<i32>(), crs_rows, start, h.crs.off.as<i32>(),
+                                                  h.crs.idx.as<i32>(), h.crs.val[master].as<float>());
+    else
+      k_hyb_tail<bf16><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<bf16>(),
+                                                 h.jds.perm.as<i32>(), crs_rows, start, h.crs.off.as<i32>(),
+                                                 h.crs.idx.as<i32>(), h.crs.val[master].as<bf16>());
+    check_launch("hyb_tail");
+    count_launch(c);
+  }
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // hcoff host buffer
+}
+
+}  // namespace fvg

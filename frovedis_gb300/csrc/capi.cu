@@ -1,0 +1,551 @@
+// C ABI (include/fvg.h): argument checks, host<->device staging, and
+// dispatch to the builders, products and drivers.  No C++ exception leaves
+// this file; every entry point returns an fvg_status and records the
+// message in the context.
+#include <cstring>
+#include <new>
+
+#include "fvg_internal.cuh"
+
+namespace fvg {
+void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
+                 double* w_h, double* b_h, i64* n_iter, double* loss_out);
+void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
+               double* w_h, double* b_h, i64* n_iter, double* loss_out);
+void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
+                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h);
+int crs_blocks_per_sm();
+void sigmoid_probability(fvg_ctx* c, double* v, i64 m, double b);
+}  // namespace fvg
+
+using namespace fvg;
+
+#define API_BEGIN try {
+#define API_END(ctxp)                                                   \
+  }                                                                     \
+  catch (const fvg::Error& e) {                                         \
+    if (ctxp) (ctxp)->last_error = e.msg;                               \
+    return e.code;                                                      \
+  }                                                                     \
+  catch (const std::bad_alloc&) {                                       \
+    if (ctxp) (ctxp)->last_error = "host allocation failed";            \
+    return FVG_ERR_OUT_OF_MEMORY;                                       \
+  }                                                                     \
+  catch (const std::exception& e) {                                     \
+    if (ctxp) (ctxp)->last_error = e.what();                            \
+    return FVG_ERR_INTERNAL;                                            \
+  }                                                                     \
+  return FVG_OK;
+
+static void need(bool cond, fvg_status code, const char* msg) {
+  if (!cond) fail(code, msg);
+}
+
+extern "C" {
+
+FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out) {
+  if (!out) return FVG_ERR_INVALID_ARG;
+  *out = nullptr;
+  fvg_ctx* c = nullptr;
+  try {
+    c = new fvg_ctx();
+    int ndev = 0;
+    FVG_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) fail(FVG_ERR_INVALID_ARG, "no such CUDA device");
+    c->device = device;
+    FVG_CUDA(cudaSetDevice(device));
+    FVG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    FVG_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    c->grid_spmv = c->num_sms * std::max(1, crs_blocks_per_sm());
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;  // keep freed blocks cached in this process
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    prof_create(c);
+    *out = c;
+    return FVG_OK;
+  } catch (const fvg::Error& e) {
+    fprintf(stderr, "fvg_ctx_create: %s\n", e.msg.c_str());
+    if (c) {
+      if (c->stream) cudaStreamDestroy(c->stream);
+      delete c;
+    }
+    return e.code;
+  } catch (...) {
+    delete c;
+    return FVG_ERR_INTERNAL;
+  }
+}
+
+FVG_API void fvg_ctx_destroy(fvg_ctx* c) {
+  if (!c) return;
+  cudaStreamSynchronize(c->stream);
+  prof_destroy(c);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+FVG_API const char* fvg_ctx_last_error(const fvg_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+FVG_API void* fvg_ctx_stream(fvg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* c) {
+  if (!c) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+static const char* kProfNames[P_NKEYS] = {"spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec",
+                                          "transpose", "spmv_ell", "spmv_jds", "spmv_hyb", "spmm"};
+
+FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* c, int enable) {
+  if (!c) return FVG_ERR_INVALID_ARG;
+  c->profiling = enable != 0;
+  return FVG_OK;
+}
+
+FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* c, const char* name, double* total_ms, int64_t* launches) {
+  if (!c || !name || !total_ms || !launches) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  int key = -1;
+  for (int k = 0; k < P_NKEYS; k++)
+    if (!strcmp(name, kProfNames[k])) key = k;
+  need(key >= 0, FVG_ERR_INVALID_ARG, "unknown profile name");
+  prof_collect(c, key, total_ms, launches);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* c) {
+  if (!c) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  prof_reset(c);
+  API_END(c)
+}
+
+FVG_API int64_t fvg_ctx_kernel_launches(fvg_ctx* c) { return c ? c->launches : -1; }
+
+// ------------------------------------------------------------------ matrix
+FVG_API fvg_status fvg_matrix_create_crs(fvg_ctx* c, int64_t num_row, int64_t num_col, const int32_t* off,
+                                         const int32_t* idx, const void* val, fvg_dtype val_dtype, int on_device,
+                                         fvg_matrix** out) {
+  if (!c || !out) return FVG_ERR_INVALID_ARG;
+  *out = nullptr;
+  fvg_matrix* M = nullptr;
+  API_BEGIN
+  need(val_dtype >= FVG_F64 && val_dtype <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown value dtype");
+  need(num_row >= 0 && num_col >= 0 && num_row < (1ll << 31) && num_col < (1ll << 31), FVG_ERR_INVALID_ARG,
+       "matrix dimensions must be in [0, 2^31)");
+  M = new fvg_matrix();
+  M->ctx = c;
+  M->master = val_dtype;
+  crs_upload(c, M->A, num_row, num_col, off, idx, val, val_dtype, on_device != 0);
+  *out = M;
+  M = nullptr;
+  }
+  catch (const fvg::Error& e) {
+    delete M;
+    c->last_error = e.msg;
+    return e.code;
+  }
+  catch (...) {
+    delete M;
+    c->last_error = "internal error";
+    return FVG_ERR_INTERNAL;
+  }
+  return FVG_OK;
+}
+
+FVG_API void fvg_matrix_destroy(fvg_matrix* M) {
+  if (!M) return;
+  cudaStream_t s = M->ctx ? M->ctx->stream : nullptr;
+  delete M;  // buffers are freed stream-ordered
+  if (s) cudaStreamSynchronize(s);
+}
+
+FVG_API fvg_status fvg_matrix_info(const fvg_matrix* M, int64_t* m, int64_t* n, int64_t* nnz) {
+  if (!M) return FVG_ERR_INVALID_ARG;
+  if (m) *m = M->A.m;
+  if (n) *n = M->A.n;
+  if (nnz) *nnz = M->A.nnz;
+  return FVG_OK;
+}
+
+static void ensure_transpose(fvg_ctx* c, fvg_matrix* M) {
+  if (!M->AT) {
+    M->AT.reset(new DevCRS());
+    crs_build_transpose(c, M->A, *M->AT, M->master);
+  }
+}
+
+static void prepare(fvg_ctx* c, fvg_matrix* M, int fmt, bool trans) {
+  if (fmt == FVG_CRS) {
+    if (trans) ensure_transpose(c, M);
+  } else if (fmt == FVG_ELL) {
+    if (!M->ell) {
+      M->ell.reset(new DevELL());
+      ell_build(c, M->A, *M->ell, M->master);
+    }
+    if (trans) ensure_transpose(c, M);
+  } else if (fmt == FVG_JDS) {
+    if (!M->jds) {
+      M->jds.reset(new DevJDS());
+      jds_build(c, M->A, *M->jds, M->master);
+    }
+    if (trans && !M->tjds) {
+      ensure_transpose(c, M);
+      M->tjds.reset(new DevJDS());
+      jds_build(c, *M->AT, *M->tjds, M->master);
+    }
+  } else if (fmt == FVG_HYBRID) {
+    if (!M->hyb) {
+      M->hyb.reset(new DevHYB());
+      hyb_build(c, M->A, *M->hyb, M->master, 256);
+    }
+    if (trans && !M->thyb) {
+      ensure_transpose(c, M);
+      M->thyb.reset(new DevHYB());
+      hyb_build(c, *M->AT, *M->thyb, M->master, 256);
+    }
+  } else {
+    fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  }
+}
+
+FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, int with_transpose) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  prepare(c, M, fmt, with_transpose != 0);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+static void ensure_plane_all(fvg_ctx* c, fvg_matrix* M, int dt) {
+  crs_ensure_plane(c, M->A, dt, M->master);
+  if (M->AT) crs_ensure_plane(c, *M->AT, dt, M->master);
+  if (M->ell) ensure_plane_generic(c, M->ell->val, M->ell->m * M->ell->width, dt, M->master);
+  for (DevJDS* j : {M->jds.get(), M->tjds.get()})
+    if (j) ensure_plane_generic(c, j->val, j->nnz, dt, M->master);
+  for (DevHYB* h : {M->hyb.get(), M->thyb.get()})
+    if (h) {
+      ensure_plane_generic(c, h->jds.val, h->jds.nnz, dt, M->master);
+      crs_ensure_plane(c, h->crs, dt, M->master);
+    }
+}
+
+FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* c, fvg_matrix* M, fvg_dtype storage) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  ensure_plane_all(c, M, storage);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+static int64_t crs_bytes(const DevCRS& a) {
+  int64_t b = (int64_t)a.off.bytes + (int64_t)a.idx.bytes;
+  for (auto& v : a.val) b += (int64_t)v.bytes;
+  for (auto& s : a.sched)
+    if (s) b += (int64_t)(s->rows.bytes + s->long_rows.bytes + s->long_chunk0.bytes + s->chunk_row.bytes +
+                          s->chunk_beg.bytes);
+  return b;
+}
+static int64_t jds_bytes(const DevJDS& j) {
+  int64_t b = (int64_t)(j.perm.bytes + j.off.bytes + j.idx.bytes);
+  for (auto& v : j.val) b += (int64_t)v.bytes;
+  return b;
+}
+
+FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* M) {
+  if (!M) return 0;
+  int64_t b = crs_bytes(M->A);
+  if (M->AT) b += crs_bytes(*M->AT);
+  if (M->ell) {
+    b += (int64_t)M->ell->idx.bytes;
+    for (auto& v : M->ell->val) b += (int64_t)v.bytes;
+  }
+  if (M->jds) b += jds_bytes(*M->jds);
+  if (M->tjds) b += jds_bytes(*M->tjds);
+  for (const DevHYB* h : {M->hyb.get(), M->thyb.get()})
+    if (h) b += jds_bytes(h->jds) + crs_bytes(h->crs);
+  return b;
+}
+
+// value plane as FP64 on the host
+static void download_values(fvg_ctx* c, const DBuf* planes, int master, int64_t n, double* out) {
+  if (!out || n <= 0) return;
+  if (master == FVG_F64) {
+    FVG_CUDA(cudaMemcpyAsync(out, planes[FVG_F64].p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    DBuf tmp;
+    tmp.alloc(sizeof(double) * n, c->stream);
+    convert_values(c, planes[master].p, master, tmp.p, FVG_F64, n);
+    FVG_CUDA(cudaMemcpyAsync(out, tmp.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+  }
+}
+
+FVG_API fvg_status fvg_matrix_get_transpose(fvg_ctx* c, fvg_matrix* M, int32_t* toff, int32_t* tidx,
+                                            double* tval) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  ensure_transpose(c, M);
+  const DevCRS& t = *M->AT;
+  if (toff) FVG_CUDA(cudaMemcpyAsync(toff, t.off.p, sizeof(int32_t) * (t.m + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (tidx && t.nnz)
+    FVG_CUDA(cudaMemcpyAsync(tidx, t.idx.p, sizeof(int32_t) * t.nnz, cudaMemcpyDeviceToHost, c->stream));
+  download_values(c, t.val, M->master, t.nnz, tval);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_get_ell(fvg_ctx* c, fvg_matrix* M, int64_t* width, int32_t* eidx, double* eval) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  prepare(c, M, FVG_ELL, false);
+  const DevELL& e = *M->ell;
+  if (width) *width = e.width;
+  int64_t cells = e.m * e.width;
+  if (eidx && cells)
+    FVG_CUDA(cudaMemcpyAsync(eidx, e.idx.p, sizeof(int32_t) * cells, cudaMemcpyDeviceToHost, c->stream));
+  download_values(c, e.val, M->master, cells, eval);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+static void get_jds(fvg_ctx* c, const DevJDS& j, int master, int32_t* perm, int64_t* joff, int32_t* jidx,
+                    double* jval) {
+  if (perm && !j.empty_perm && j.m)
+    FVG_CUDA(cudaMemcpyAsync(perm, j.perm.p, sizeof(int32_t) * j.m, cudaMemcpyDeviceToHost, c->stream));
+  if (joff) FVG_CUDA(cudaMemcpyAsync(joff, j.off.p, sizeof(int64_t) * (j.ndiag + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (jidx && j.nnz) FVG_CUDA(cudaMemcpyAsync(jidx, j.idx.p, sizeof(int32_t) * j.nnz, cudaMemcpyDeviceToHost, c->stream));
+  download_values(c, j.val, master, j.nnz, jval);
+}
+
+FVG_API fvg_status fvg_matrix_get_jds(fvg_ctx* c, fvg_matrix* M, int64_t* ndiag, int32_t* perm, int64_t* joff,
+                                      int32_t* jidx, double* jval) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  prepare(c, M, FVG_JDS, false);
+  if (ndiag) *ndiag = M->jds->ndiag;
+  get_jds(c, *M->jds, M->master, perm, joff, jidx, jval);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_get_hybrid(fvg_ctx* c, fvg_matrix* M, int64_t* info, int32_t* perm, int64_t* joff,
+                                         int32_t* jidx, double* jval, int64_t* coff, int32_t* cidx,
+                                         double* cval) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  prepare(c, M, FVG_HYBRID, false);
+  const DevHYB& h = *M->hyb;
+  if (info) {
+    info[0] = h.jds.ndiag;
+    info[1] = h.crs.m;
+    info[2] = h.crs.nnz;
+    info[3] = h.jds.nnz;
+    info[4] = h.jds.empty_perm ? 0 : h.m;
+  }
+  get_jds(c, h.jds, M->master, perm, joff, jidx, jval);
+  if (coff) {
+    std::vector<int32_t> o(h.crs.m + 1);
+    FVG_CUDA(cudaMemcpyAsync(o.data(), h.crs.off.p, sizeof(int32_t) * (h.crs.m + 1), cudaMemcpyDeviceToHost,
+                             c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+    for (int64_t i = 0; i <= h.crs.m; i++) coff[i] = o[i];
+  }
+  if (cidx && h.crs.nnz)
+    FVG_CUDA(cudaMemcpyAsync(cidx, h.crs.idx.p, sizeof(int32_t) * h.crs.nnz, cudaMemcpyDeviceToHost, c->stream));
+  download_values(c, h.crs.val, M->master, h.crs.nnz, cval);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+// --------------------------------------------------------------- products
+// Stages x (len nx) / y (len ny) on the device in the kernel's vector type.
+struct VecStage {
+  DBuf xb, yb, xconv, yconv;
+  const void* dx = nullptr;
+  void* dy = nullptr;
+  int kdt = FVG_F64;  // kernel vector dtype
+};
+
+static void stage_in(fvg_ctx* c, VecStage& v, const void* x, int64_t nx, int vec_dt, int storage, bool on_dev) {
+  v.kdt = (storage == FVG_F64) ? FVG_F64 : FVG_F32;
+  const void* src = x;
+  if (!on_dev) {
+    v.xb.alloc((size_t)dtype_size(vec_dt) * std::max<int64_t>(nx, 1), c->stream);
+    if (nx) FVG_CUDA(cudaMemcpyAsync(v.xb.p, x, (size_t)dtype_size(vec_dt) * nx, cudaMemcpyHostToDevice, c->stream));
+    src = v.xb.p;
+  }
+  if (vec_dt != v.kdt) {
+    v.xconv.alloc((size_t)dtype_size(v.kdt) * std::max<int64_t>(nx, 1), c->stream);
+    convert_values(c, src, vec_dt, v.xconv.p, v.kdt, nx);
+    src = v.xconv.p;
+  }
+  v.dx = src;
+}
+
+static void stage_out_alloc(fvg_ctx* c, VecStage& v, void* y, int64_t ny, int vec_dt, bool on_dev, int out_dt) {
+  // kernels write out_dt; y wants vec_dt
+  if (on_dev && vec_dt == out_dt) {
+    v.dy = y;
+    return;
+  }
+  v.yb.alloc((size_t)dtype_size(out_dt) * std::max<int64_t>(ny, 1), c->stream);
+  v.dy = v.yb.p;
+}
+
+static void stage_out_finish(fvg_ctx* c, VecStage& v, void* y, int64_t ny, int vec_dt, bool on_dev, int out_dt) {
+  if (v.dy == y) return;
+  const void* src = v.dy;
+  if (vec_dt != out_dt) {
+    v.yconv.alloc((size_t)dtype_size(vec_dt) * std::max<int64_t>(ny, 1), c->stream);
+    convert_values(c, src, out_dt, v.yconv.p, vec_dt, ny);
+    src = v.yconv.p;
+  }
+  if (ny)
+    FVG_CUDA(cudaMemcpyAsync(y, src, (size_t)dtype_size(vec_dt) * ny,
+                             on_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+}
+
+static void check_vec_args(int storage, int vec_dt) {
+  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  need(vec_dt == FVG_F64 || vec_dt == FVG_F32, FVG_ERR_INVALID_ARG, "vectors must be FP64 or FP32");
+  need(!(storage == FVG_F64 && vec_dt != FVG_F64), FVG_ERR_INVALID_ARG, "FP64 values need FP64 vectors");
+}
+
+static void run_product(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, int vec_dt, const void* x, void* y,
+                        bool trans, bool on_dev) {
+  check_vec_args(storage, vec_dt);
+  need(fmt >= 0 && fmt <= 3, FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  prepare(c, M, fmt, trans);
+  ensure_plane_all(c, M, storage);
+  const int64_t nx = trans ? M->A.m : M->A.n, ny = trans ? M->A.n : M->A.m;
+  VecStage v;
+  stage_in(c, v, x, nx, vec_dt, storage, on_dev);
+  // FP32-vector kernels can write FP64 directly
+  const int out_dt = (v.kdt == FVG_F64) ? FVG_F64 : vec_dt;
+  stage_out_alloc(c, v, y, ny, vec_dt, on_dev, out_dt);
+  if (!trans) {
+    if (fmt == FVG_CRS) crs_pass(c, M->A, storage, v.kdt, v.dx, out_dt, v.dy, EPI_STORE, nullptr, nullptr, P_SPMV_CRS);
+    else if (fmt == FVG_ELL) ell_spmv(c, *M->ell, storage, v.kdt, v.dx, out_dt, v.dy);
+    else if (fmt == FVG_JDS) jds_spmv(c, *M->jds, storage, v.kdt, v.dx, out_dt, v.dy, false);
+    else hyb_spmv(c, *M->hyb, storage, v.kdt, v.dx, out_dt, v.dy);
+  } else {
+    if (fmt == FVG_CRS || fmt == FVG_ELL)
+      crs_pass(c, *M->AT, storage, v.kdt, v.dx, out_dt, v.dy, EPI_STORE, nullptr, nullptr, P_SPMV_CRS);
+    else if (fmt == FVG_JDS) jds_spmv(c, *M->tjds, storage, v.kdt, v.dx, out_dt, v.dy, false);
+    else hyb_spmv(c, *M->thyb, storage, v.kdt, v.dx, out_dt, v.dy);
+  }
+  stage_out_finish(c, v, y, ny, vec_dt, on_dev, out_dt);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+FVG_API fvg_status fvg_spmv(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
+                            const void* x, void* y, int on_device) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need((x && y) || M->A.m == 0 || M->A.n == 0, FVG_ERR_INVALID_ARG, "null vector");
+  run_product(c, M, fmt, storage, vec_dtype, x, y, false, on_device != 0);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_trans_mv(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
+                                const void* x, void* y, int on_device) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need((x && y) || M->A.m == 0 || M->A.n == 0, FVG_ERR_INVALID_ARG, "null vector");
+  run_product(c, M, fmt, storage, vec_dtype, x, y, true, on_device != 0);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_spmm(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
+                            const void* X, int64_t k, void* Y, int on_device) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  check_vec_args(storage, vec_dtype);
+  need(k >= 0, FVG_ERR_INVALID_ARG, "negative number of columns");
+  need(fmt >= 0 && fmt <= 3, FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  ensure_plane_all(c, M, storage);
+  const int64_t nx = M->A.n * k, ny = M->A.m * k;
+  VecStage v;
+  stage_in(c, v, X, nx, vec_dtype, storage, on_device != 0);
+  stage_out_alloc(c, v, Y, ny, vec_dtype, on_device != 0, v.kdt);
+  crs_spmm(c, M->A, storage, v.kdt, v.dx, k, v.dy);
+  stage_out_finish(c, v, Y, ny, vec_dtype, on_device != 0, v.kdt);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+// --------------------------------------------------------------- training
+FVG_API void fvg_glm_params_default(fvg_glm_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->num_iteration = 1000;
+  p->alpha = 0.01;
+  p->hist_size = 10;
+  p->reg_param = 0.01;
+  p->reg_type = FVG_REG_ZERO;
+  p->intercept = 0;
+  p->convergence_tol = 0.001;
+  p->mat_type = FVG_CRS;
+  p->mini_batch_fraction = 1.0;
+  p->num_partitions = 1;
+  p->storage = FVG_F64;
+  p->refine = 1;
+  p->refine_stall = 0.97;
+  p->l2_no_eta = 0;
+  p->use_graph = 1;
+  p->trace = nullptr;
+  p->row_splits = nullptr;
+}
+
+FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* label, const double* sample_weight,
+                                    const fvg_glm_params* p, double* weight, double* intercept, int64_t* n_iter,
+                                    double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  lbfgs_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* c, fvg_matrix* M, const double* label, const double* sample_weight,
+                                  const fvg_glm_params* p, double* weight, double* intercept, int64_t* n_iter,
+                                  double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_logreg_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage,
+                                   const double* label, const double* sample_weight, const double* weight,
+                                   double intercept, int intercept_on, double* grad, double* loss) {
+  if (!c || !M || !grad || !loss || !weight) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_logreg_predict_probability(fvg_ctx* c, fvg_matrix* M, const double* weight,
+                                                  double intercept, double* prob) {
+  if (!c || !M || !weight || !prob) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need(M->master == FVG_F64, FVG_ERR_INVALID_ARG, "predict_probability needs FP64 values");
+  DBuf w, y;
+  w.alloc(sizeof(double) * std::max<int64_t>(M->A.n, 1), c->stream);
+  y.alloc(sizeof(double) * std::max<int64_t>(M->A.m, 1), c->stream);
+  if (M->A.n)
+    FVG_CUDA(cudaMemcpyAsync(w.p, weight, sizeof(double) * M->A.n, cudaMemcpyHostToDevice, c->stream));
+  crs_pass(c, M->A, FVG_F64, FVG_F64, w.p, FVG_F64, y.p, EPI_STORE, nullptr, nullptr, P_SPMV_CRS);
+  sigmoid_probability(c, y.as<double>(), M->A.m, intercept);
+  if (M->A.m) FVG_CUDA(cudaMemcpyAsync(prob, y.p, sizeof(double) * M->A.m, cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+// Internal declarations shared by the CUDA translation units of libfvg.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fvg.h"
+
+namespace fvg {
+
+using i64 = int64_t;
+using i32 = int32_t;
+using bf16 = __nv_bfloat16;
+
+// ------------------------------------------------------------------ errors
+struct Error {
+  fvg_status code;
+  std::string msg;
+};
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
+[[noreturn]] inline void fail(fvg_status code, const std::string& msg) { throw Error{code, msg}; }
+#define FVG_CUDA(x)                                                  \
+  do {                                                               \
+    cudaError_t e__ = (x);                                           \
+    if (e__ != cudaSuccess) ::fvg::throw_cuda(e__, #x, __FILE__, __LINE__); \
+  } while (0)
+
+// ---------------------------------------------------------- device buffers
+// Owning device allocation, stream-ordered free.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p; bytes = o.bytes; stream = o.stream;
+      o.p = nullptr; o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t nbytes, cudaStream_t s);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Elements of padding after every value/index array, so that 16-byte vector
+// loads of the last partial vector stay inside the allocation.
+constexpr i64 kPad = 32;
+
+// ---------------------------------------------------------- CRS schedule
+// Row bins of the CRS kernel: bins 0..5 give a row 1,2,4,8,16,32 lanes, bin 6
+// a whole 256-thread CTA, bin 7 splits a row into chunks of kChunk elements
+// whose partial sums are combined in order by the finalize kernel.
+constexpr int kBins = 8;
+constexpr int kThreads = 256;
+constexpr i64 kChunk = 16384;       // elements per long-row chunk (multiple of 8)
+constexpr i64 kCtaRowMax = 16384;   // rows up to this length use one CTA
+struct Sched {
+  int ve = 0;                 // elements per lane vector this schedule targets
+  i64 item_start[kBins + 1];  // work items per bin (prefix)
+  i64 row_start[kBins + 1];   // rows per bin (prefix) into `rows`
+  DBuf rows;                  // int32 row ids grouped by bin, ascending in a bin
+  i64 nlong = 0, nchunks = 0;
+  DBuf long_rows;             // int32 row ids of bin 7
+  DBuf long_chunk0;           // int32 [nlong+1] first chunk of each long row
+  DBuf chunk_row;             // int32 [nchunks] row of each chunk
+  DBuf chunk_beg;             // int32 [nchunks] first element of each chunk
+  i64 items() const { return item_start[kBins]; }
+};
+
+// Device CRS matrix with up to three value planes.
+struct DevCRS {
+  i64 m = 0, n = 0, nnz = 0;
+  DBuf off, idx;  // int32
+  DBuf val[3];    // indexed by fvg_dtype
+  std::unique_ptr<Sched> sched[2];  // [0]: 4-element vectors, [1]: 8-element
+  i64 max_row = 0;
+};
+
+struct DevELL {  // column-major m x width, zero padded (ell_matrix.hpp:63-95)
+  i64 m = 0, n = 0, width = 0;
+  DBuf idx;
+  DBuf val[3];
+};
+
+struct DevJDS {  // jds_matrix_local (jds_matrix.hpp:15-146)
+  i64 m = 0, n = 0, ndiag = 0, nnz = 0;
+  DBuf perm;     // int32 [m]
+  DBuf off;      // int64 [ndiag+1]
+  DBuf idx;      // int32 [nnz]
+  DBuf val[3];
+  bool empty_perm = false;  // all-zero matrix: the reference leaves perm empty
+};
+
+struct DevHYB {  // jds_crs_hybrid_local (jds_crs_hybrid.hpp:8-153)
+  i64 m = 0, n = 0, crs_rows = 0;
+  DevJDS jds;
+  DevCRS crs;  // tail rows, in permuted order (row i ↔ jds.perm[i])
+  bool all_crs = false;  // m <= threshold: the whole matrix is the CRS part
+};
+
+struct Profiler;
+
+}  // namespace fvg
+
+struct fvg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int num_sms = 0;
+  int grid_spmv = 0;    // persistent grid of the CRS kernel
+  int64_t launches = 0;
+  bool profiling = false;
+  fvg::Profiler* prof = nullptr;  // owned; prof_create / prof_destroy
+  // pinned host scratch for scalar read-backs
+  double* host_scalars = nullptr;
+};
+
+struct fvg_matrix {
+  fvg_ctx* ctx = nullptr;
+  int master = FVG_F64;           // dtype of the uploaded values
+  fvg::DevCRS A;
+  std::unique_ptr<fvg::DevCRS> AT;
+  std::unique_ptr<fvg::DevELL> ell;
+  std::unique_ptr<fvg::DevJDS> jds, tjds;
+  std::unique_ptr<fvg::DevHYB> hyb, thyb;
+};
+
+namespace fvg {
+
+// ------------------------------------------------------------ profiling
+enum ProfKey { P_SPMV_CRS = 0, P_PASS1, P_PASS2, P_FINALIZE, P_LBFGS, P_TRANSPOSE, P_SPMV_ELL, P_SPMV_JDS,
+               P_SPMV_HYB, P_SPMM, P_NKEYS };
+void prof_begin(fvg_ctx* c, int key);
+void prof_end(fvg_ctx* c, int key);
+void prof_collect(fvg_ctx* c, int key, double* ms, int64_t* n);
+void prof_reset(fvg_ctx* c);
+void prof_create(fvg_ctx* c);
+void prof_destroy(fvg_ctx* c);
+struct ProfScope {
+  fvg_ctx* c;
+  int k;
+  ProfScope(fvg_ctx* c_, int k_) : c(c_), k(k_) { prof_begin(c, k); }
+  ~ProfScope() { prof_end(c, k); }
+};
+inline void count_launch(fvg_ctx* c, int n = 1) { c->launches += n; }
+void check_launch(const char* what);
+
+// ------------------------------------------------------------ utilities
+int dtype_size(int dt);
+// exclusive scan of n int64 values in place (out has n+1 entries: out[n]=total)
+void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n);
+// stable LSD radix sort of (key,val) u32 pairs by the low `bits` bits of key
+void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bits);
+void fill_i32(fvg_ctx* c, i32* p, i32 v, i64 n);
+void convert_values(fvg_ctx* c, const void* src, int sdt, void* dst, int ddt, i64 n);
+void gather_values(fvg_ctx* c, const void* src, const uint32_t* perm, void* dst, int dt, i64 n);
+
+// ------------------------------------------------------------ builders
+void crs_upload(fvg_ctx* c, DevCRS& a, i64 m, i64 n, const i32* off, const i32* idx, const void* val, int dt,
+                bool on_device);
+void crs_ensure_plane(fvg_ctx* c, DevCRS& a, int dt, int master);
+void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master);
+const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int ve);
+void ell_build(fvg_ctx* c, const DevCRS& a, DevELL& e, int master);
+void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master);
+void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 threshold);
+void ensure_plane_generic(fvg_ctx* c, DBuf* planes, i64 n, int dt, int master);
+
+// ------------------------------------------------------------ products
+// Epilogue of a CRS pass.
+enum EpiKind { EPI_STORE = 0, EPI_LOGREG = 1 };
+struct LogregEpi {
+  const double* label = nullptr;
+  const double* sw = nullptr;       // nullptr: all ones
+  const double* intercept = nullptr;  // device scalar
+  int icpt = 0;
+  void* r = nullptr;                // dloss*sw, dtype r_dt
+  int r_dt = FVG_F64;
+  double* cta_part = nullptr;       // [2*grid]: loss, bias per CTA
+  double* long_part = nullptr;      // [2*nlong]
+  double* out = nullptr;            // [2]: loss, bias  (written by finalize)
+  double* grad_bias = nullptr;      // where the bias lands (grad[n]); may be null
+  unsigned* ticket = nullptr;
+};
+// y = A x over the CRS layout (any plane), optional logistic epilogue.
+void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y_dt, void* y, int epi,
+              const LogregEpi* lr, void* scratch_partials, int prof_key);
+i64 crs_pass_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage);
+void ell_spmv(fvg_ctx* c, DevELL& e, int storage, int x_dt, const void* x, int y_dt, void* y);
+void jds_spmv(fvg_ctx* c, DevJDS& j, int storage, int x_dt, const void* x, int y_dt, void* y, bool accumulate_perm);
+void hyb_spmv(fvg_ctx* c, DevHYB& h, int storage, int x_dt, const void* x, int y_dt, void* y);
+void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k, void* Y);
+void jds_spmm(fvg_ctx* c, DevJDS& j, int storage, int x_dt, const void* X, i64 k, void* Y);
+
+// Per-row logistic epilogue applied to a finished product z = A w (used by
+// the non-CRS formats): r, loss/bias partial sums; then finalize_logreg.
+void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi& lr);
+
+}  // namespace fvg

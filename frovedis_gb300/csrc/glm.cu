@@ -1,0 +1,953 @@
+// Logistic-regression drivers on the device.
+//
+// L-BFGS: lbfgs_parallelizer::do_train (ml/glm/lbfgs_parallelizer.hpp:
+// 267-364 with the transposed copy, 366-462 for ELL) with lbfgs<T>::
+// compute_hkgk / update_history (ml/glm/lbfgs.hpp:79-143) and the ring buffer
+// of matrix/cir_array_list.hpp.  All model, gradient and history vectors stay
+// on the device in FP64; every reduction is a fixed-order grid reduction (the
+// last CTA to finish combines the per-CTA partials in CTA order), so runs are
+// deterministic.  Element-wise updates use round-to-nearest intrinsics so no
+// multiply-add is contracted where the reference rounds twice.  The host only
+// reads three scalars per line-search trial (new loss, loss, rms) to take the
+// accept decision the reference takes on rank 0.
+//
+// SGD: sgd_parallelizer::do_train_with_trans (ml/glm/sgd_parallelizer.hpp:
+// 132-255) with gradient_descent::optimize / update_model (gradient_descent.hpp:
+// 128-164, 242-259); P ranks are emulated as P row blocks whose model deltas
+// are summed in rank order.
+#include <algorithm>
+#include <cmath>
+
+#include "fvg_internal.cuh"
+
+namespace fvg {
+
+constexpr int kMaxHist = 64;
+constexpr int kVecThreads = 256;
+
+struct LbState {
+  int k, rear, front, h;
+  double rho[kMaxHist], yy[kMaxHist], al[kMaxHist], beta[kMaxHist];
+  double factor[12];
+  double dot_gs, smax, stepsize, flip, bstep;
+  double loss;      // accepted loss
+  double eval[2];   // last evaluation: loss, bias
+  double b[2];      // [0] accepted intercept, [1] trial intercept
+  double gmax, gnorm, rms;              // of the accepted gradient
+  double gmax_t, gnorm_t, rms_t;        // of the last trial gradient
+  double host[4];   // newloss, loss, rms_t, factor of the last trial (read back)
+};
+
+struct VecArgs {
+  i64 n;   // weights
+  i64 n1;  // n + 1
+  int h;
+  double* part;
+  unsigned* ticket;
+  LbState* st;
+};
+
+__device__ __forceinline__ int slot(const LbState* st, int i) { return (st->rear + i) % st->h; }
+
+// Fixed-order grid reduction of NV values (sum or max per value); the last
+// CTA calls fin(totals) with thread 0.
+template <int NV, class Fin>
+__device__ __forceinline__ void grid_reduce(double (&v)[NV], const bool (&is_max)[NV], double* part,
+                                            unsigned* ticket, Fin fin) {
+  __shared__ double sm[NV][kVecThreads];
+  __shared__ bool last;
+#pragma unroll
+  for (int q = 0; q < NV; q++) sm[q][threadIdx.x] = v[q];
+  __syncthreads();
+  for (int st = kVecThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+#pragma unroll
+      for (int q = 0; q < NV; q++)
+        sm[q][threadIdx.x] = is_max[q] ? fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + st])
+                                       : sm[q][threadIdx.x] + sm[q][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) part[(i64)blockIdx.x * NV + q] = sm[q][0];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double t[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) t[q] = 0.0;
+  for (i64 b = threadIdx.x; b < gridDim.x; b += kVecThreads)
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      double x = __ldcg(&part[b * NV + q]);
+      t[q] = is_max[q] ? fmax(t[q], x) : t[q] + x;
+    }
+#pragma unroll
+  for (int q = 0; q < NV; q++) sm[q][threadIdx.x] = t[q];
+  __syncthreads();
+  for (int st = kVecThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+#pragma unroll
+      for (int q = 0; q < NV; q++)
+        sm[q][threadIdx.x] = is_max[q] ? fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + st])
+                                       : sm[q][threadIdx.x] + sm[q][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double tot[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) tot[q] = sm[q][0];
+    fin(tot);
+    *ticket = 0u;
+  }
+}
+
+#define VEC_LOOP(j, n) for (i64 j = (i64)blockIdx.x * kVecThreads + threadIdx.x; j < (n); j += (i64)gridDim.x * kVecThreads)
+
+// ---------------------------------------------------- two-loop recursion
+// first loop, i = k-1 .. 0:  al[i] = rho[i] * (s_i · q);  q -= y_i * al[i]
+// (the q update for step i is applied by the kernel of step i-1)
+__global__ void __launch_bounds__(kVecThreads) k_down(int i, const double* __restrict__ G, double* __restrict__ Q,
+                                                      const double* __restrict__ S, const double* __restrict__ Y,
+                                                      VecArgs a) {
+  LbState* st = a.st;
+  const int k = st->k;
+  if (i >= k) return;
+  const bool first = (i == k - 1);
+  const double* Si = S + (i64)slot(st, i) * a.n1;
+  const double* Yp = first ? nullptr : Y + (i64)slot(st, i + 1) * a.n1;
+  const double alp = first ? 0.0 : st->al[i + 1];
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n1) {
+    double q = first ? G[j] : __dsub_rn(Q[j], __dmul_rn(Yp[j], alp));
+    Q[j] = q;
+    v[0] += Si[j] * q;
+  }
+  const bool mx[1] = {false};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) { st->al[i] = st->rho[slot(st, i)] * t[0]; });
+}
+
+// second loop, i = 0 .. k-1:  beta = rho[i] * (y_i · z);  z += s_i * (al[i] - beta)
+// i == 0 first finishes q (q -= y_0 * al[0]) and forms z = q * H0.
+__global__ void __launch_bounds__(kVecThreads) k_up(int i, const double* __restrict__ Q, double* __restrict__ Z,
+                                                    const double* __restrict__ S, const double* __restrict__ Y,
+                                                    VecArgs a) {
+  LbState* st = a.st;
+  const int k = st->k;
+  if (i >= k) return;
+  const double* Yi = Y + (i64)slot(st, i) * a.n1;
+  double H0 = 0.0, f = 0.0, al0 = 0.0;
+  const double* Sp = nullptr;
+  if (i == 0) {
+    int sl = slot(st, k - 1);
+    double yy = st->yy[sl];
+    if (yy == 0) yy = 1.0;
+    double ys = 1.0 / st->rho[sl];
+    H0 = ys / yy;
+    al0 = st->al[0];
+  } else {
+    Sp = S + (i64)slot(st, i - 1) * a.n1;
+    f = st->al[i - 1] - st->beta[i - 1];
+  }
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n1) {
+    double z = (i == 0) ? __dmul_rn(__dsub_rn(Q[j], __dmul_rn(Yi[j], al0)), H0) : __dadd_rn(Z[j], __dmul_rn(Sp[j], f));
+    Z[j] = z;
+    v[0] += Yi[j] * z;
+  }
+  const bool mx[1] = {false};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) { st->beta[i] = st->rho[slot(st, i)] * t[0]; });
+}
+
+// step = -z (finishing the second loop), or the no-history step
+// z = -c * 0.1 * g with c = |g| <= 1 ? |g| : 1/|g| (lbfgs.hpp:86-91);
+// reduces g·step and max|step|.
+__global__ void __launch_bounds__(kVecThreads) k_step(const double* __restrict__ G, const double* __restrict__ Z,
+                                                      double* __restrict__ STEP, const double* __restrict__ S,
+                                                      VecArgs a) {
+  LbState* st = a.st;
+  const int k = st->k;
+  double c = 0.0, f = 0.0;
+  const double* Sp = nullptr;
+  if (k == 0) {
+    double gn = st->gnorm;
+    if (gn > 1) gn = 1.0 / gn;
+    c = __dmul_rn(-gn, 0.1);
+  } else {
+    Sp = S + (i64)slot(st, k - 1) * a.n1;
+    f = st->al[k - 1] - st->beta[k - 1];
+  }
+  double v[2] = {0.0, 0.0};
+  VEC_LOOP(j, a.n1) {
+    double z = (k == 0) ? __dmul_rn(c, G[j]) : __dadd_rn(Z[j], __dmul_rn(Sp[j], f));
+    double s = -z;
+    STEP[j] = s;
+    v[0] += G[j] * s;
+    v[1] = fmax(v[1], fabs(s));
+  }
+  const bool mx[2] = {false, true};
+  grid_reduce<2>(v, mx, a.part, a.ticket, [&](double* t) {
+    st->dot_gs = t[0];
+    st->smax = t[1];
+  });
+}
+
+// stepsize = vector_norm(step) (vector_operations.hpp:227-264, max-scaled),
+// uphill flip, factor cap at 1e20, the factor of each of the 10 trials.
+__global__ void __launch_bounds__(kVecThreads) k_step_norm(const double* __restrict__ STEP, VecArgs a) {
+  LbState* st = a.st;
+  const double mxv = st->smax;
+  const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n1) {
+    double t = STEP[j] * inv;
+    v[0] += t * t;
+  }
+  const bool mx[1] = {false};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) {
+    double ss = (mxv == 0) ? 0.0 : sqrt(t[0]) * mxv;
+    st->stepsize = ss;
+    st->flip = (st->dot_gs > 0) ? -1.0 : 1.0;
+    double fac = 1.0;
+    if (fac * ss > 1e20) fac = 1e20 / ss;
+    st->factor[1] = fac;
+    for (int q = 2; q <= 10; q++) st->factor[q] = st->factor[q - 1] / 10.0;
+    st->bstep = STEP[a.n1 - 1] * st->flip;
+  });
+}
+
+// trial model w' = w + factor*step, b' = b + factor*bstep, then the
+// regulariser (regularizer.hpp:14-61; eta = factor, or 1 for ELL).
+__global__ void __launch_bounds__(kVecThreads) k_trial(int j, const double* __restrict__ W,
+                                                       const double* __restrict__ STEP, double* __restrict__ NW,
+                                                       float* __restrict__ NWF, int rtype, double lambda, int eta_one,
+                                                       int no_eta, VecArgs a) {
+  LbState* st = a.st;
+  const double f = st->factor[j], fl = st->flip;
+  const double eta = eta_one ? 1.0 : f;
+  const double scale = fmax(0.0, 1.0 - (lambda * eta));
+  VEC_LOOP(i, a.n) {
+    double w = __dadd_rn(W[i], __dmul_rn(f, __dmul_rn(STEP[i], fl)));
+    if (rtype == FVG_REG_L2) {
+      w = no_eta ? __dsub_rn(w, __dmul_rn(lambda, w)) : __dmul_rn(scale, w);
+    } else if (rtype == FVG_REG_L1) {
+      double sg = (double)((w >= 0) - (w < 0));
+      w = __dsub_rn(w, __dmul_rn(lambda, sg));
+    }
+    NW[i] = w;
+    if (NWF) NWF[i] = (float)w;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->b[1] = __dadd_rn(st->b[0], __dmul_rn(f, st->bstep));
+}
+
+// max |g| of a gradient, then its max-scaled norm and rms = |g| / sqrt(n+1)
+__global__ void __launch_bounds__(kVecThreads) k_gmax(const double* __restrict__ G, VecArgs a) {
+  LbState* st = a.st;
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n1) v[0] = fmax(v[0], fabs(G[j]));
+  const bool mx[1] = {true};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) { st->gmax_t = t[0]; });
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_gnorm(const double* __restrict__ G, VecArgs a, int accepted) {
+  LbState* st = a.st;
+  const double mxv = st->gmax_t;
+  const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n1) {
+    double t = G[j] * inv;
+    v[0] += t * t;
+  }
+  const bool mx[1] = {false};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) {
+    double nrm = (mxv == 0) ? 0.0 : sqrt(t[0]) * mxv;
+    st->gnorm_t = nrm;
+    st->rms_t = nrm / sqrt((double)a.n1);
+    st->host[0] = st->eval[0];
+    st->host[1] = st->loss;
+    st->host[2] = st->rms_t;
+    if (accepted) {  // initial evaluation
+      st->gnorm = nrm;
+      st->rms = st->rms_t;
+      st->gmax = mxv;
+      st->loss = st->eval[0];
+    }
+  });
+}
+
+// Accept the trial and push the (s, y) pair (lbfgs.hpp:114-143):
+// s = [w',b'] - [w,b]; y = g' - g with |y_j| < 1e-10 → 0; rho = 1/(s·y)
+// (s·y == 0 → 1); ring push; w ← w', g ← g', loss ← new loss.
+__global__ void __launch_bounds__(kVecThreads) k_accept(double* __restrict__ W, double* __restrict__ G,
+                                                        const double* __restrict__ NW,
+                                                        const double* __restrict__ NG, double* __restrict__ S,
+                                                        double* __restrict__ Y, VecArgs a) {
+  LbState* st = a.st;
+  const int k = st->k, h = st->h;
+  int nf;
+  if (k == 0) nf = 0;
+  else nf = (st->front + 1) % h;
+  double* Sn = S + (i64)nf * a.n1;
+  double* Yn = Y + (i64)nf * a.n1;
+  const double bn = st->b[1], bo = st->b[0];
+  double v[2] = {0.0, 0.0};
+  VEC_LOOP(j, a.n1) {
+    double s = (j < a.n) ? __dsub_rn(NW[j], W[j]) : __dsub_rn(bn, bo);
+    double y = __dsub_rn(NG[j], G[j]);
+    if (fabs(y) < 1e-10) y = 0.0;
+    Sn[j] = s;
+    Yn[j] = y;
+    if (j < a.n) W[j] = NW[j];
+    G[j] = NG[j];
+    v[0] += s * y;
+    v[1] += y * y;
+  }
+  const bool mx[2] = {false, false};
+  grid_reduce<2>(v, mx, a.part, a.ticket, [&](double* t) {
+    double dv = t[0];
+    if (dv == 0) dv = 1;
+    st->rho[nf] = 1.0 / dv;
+    st->yy[nf] = t[1];
+    if (k == 0) { st->rear = 0; st->front = 0; }
+    else if (k == h) { st->rear = (st->rear + 1) % h; st->front = nf; }
+    else st->front = nf;
+    st->k = k < h ? k + 1 : h;
+    st->loss = st->eval[0];
+    st->b[0] = st->b[1];
+    st->gnorm = st->gnorm_t;
+    st->rms = st->rms_t;
+  });
+}
+
+__global__ void k_d2f(const double* __restrict__ s, float* __restrict__ d, i64 n) {
+  VEC_LOOP(j, n) d[j] = (float)s[j];
+}
+
+// -------------------------------------------------------------- operand
+// One local matrix in one format with what its forward (A x) and backward
+// (A^T r) products need.  Forward/backward mirror compute_gradient's
+// `data * w` and `trans * dloss` (gradient_descent.hpp:211) or
+// `trans_mv(data, dloss)` (gradient_descent.hpp:183, ELL: done here as a
+// gather over the transposed CRS copy).
+struct Operand {
+  int fmt = FVG_CRS;
+  i64 m = 0, n = 0;
+  DevCRS* A = nullptr;   // forward CRS (CRS format)
+  DevCRS* AT = nullptr;  // backward CRS (CRS and ELL)
+  DevHYB* H = nullptr;
+  DevHYB* HT = nullptr;
+  DevJDS* J = nullptr;
+  DevJDS* JT = nullptr;
+  DevELL* E = nullptr;
+  int master = FVG_F64;
+  // owned pieces (minibatches)
+  std::unique_ptr<DevCRS> oA, oAT;
+  std::unique_ptr<DevHYB> oH, oHT;
+  std::unique_ptr<DevJDS> oJ, oJT;
+  std::unique_ptr<DevELL> oE;
+};
+
+static void ensure_storage(fvg_ctx* c, Operand& o, int storage) {
+  if (o.A) crs_ensure_plane(c, *o.A, storage, o.master);
+  if (o.AT) crs_ensure_plane(c, *o.AT, storage, o.master);
+  if (o.H) {
+    ensure_plane_generic(c, o.H->jds.val, o.H->jds.nnz, storage, o.master);
+    crs_ensure_plane(c, o.H->crs, storage, o.master);
+  }
+  if (o.HT) {
+    ensure_plane_generic(c, o.HT->jds.val, o.HT->jds.nnz, storage, o.master);
+    crs_ensure_plane(c, o.HT->crs, storage, o.master);
+  }
+  if (o.J) ensure_plane_generic(c, o.J->val, o.J->nnz, storage, o.master);
+  if (o.JT) ensure_plane_generic(c, o.JT->val, o.JT->nnz, storage, o.master);
+  if (o.E) ensure_plane_generic(c, o.E->val, o.E->m * o.E->width, storage, o.master);
+}
+
+// Loss/gradient evaluation over an operand (compute_gradient with trans,
+// gradient_descent.hpp:196-225).  w: FP64 weights or their FP32 copy,
+// grad[n+1] FP64 (bias last), out[2] = {loss, bias} on the device.
+struct Evaluator {
+  fvg_ctx* c = nullptr;
+  Operand* op = nullptr;
+  int storage = FVG_F64;
+  const double* label = nullptr;
+  const double* sw = nullptr;
+  int icpt = 0;
+  DBuf r, z, s1, s2;
+  void init(fvg_ctx* c_, Operand* op_, int storage_, const double* label_, const double* sw_, int icpt_) {
+    c = c_;
+    op = op_;
+    storage = storage_;
+    label = label_;
+    sw = sw_;
+    icpt = icpt_;
+    ensure_storage(c, *op, storage);
+    const int vdt = storage == FVG_F64 ? FVG_F64 : FVG_F32;
+    r.alloc((size_t)dtype_size(vdt) * std::max<i64>(op->m, 1), c->stream);
+    if (op->fmt != FVG_CRS) z.alloc((size_t)dtype_size(vdt) * std::max<i64>(op->m, 1), c->stream);
+    if (op->fmt == FVG_CRS) {
+      s1.alloc(crs_pass_scratch_bytes(c, *op->A, storage), c->stream);
+      FVG_CUDA(cudaMemsetAsync(s1.p, 0, 256, c->stream));
+    }
+    if (op->AT) {
+      s2.alloc(crs_pass_scratch_bytes(c, *op->AT, storage), c->stream);
+      FVG_CUDA(cudaMemsetAsync(s2.p, 0, 256, c->stream));
+    }
+  }
+  void set_storage(int st) {
+    storage = st;
+    ensure_storage(c, *op, storage);
+  }
+  // x: weights (FP64 for FP64 storage, FP32 otherwise); b: device intercept
+  void eval(const void* x, const double* b, double* grad, double* out) {
+    const int vdt = storage == FVG_F64 ? FVG_F64 : FVG_F32;
+    LogregEpi lr;
+    lr.label = label;
+    lr.sw = sw;
+    lr.intercept = b;
+    lr.icpt = icpt;
+    lr.r = r.p;
+    lr.r_dt = vdt;
+    lr.out = out;
+    lr.grad_bias = grad + op->n;
+    if (op->m == 0) {  // compute_gradient: empty data → zero gradient, no loss
+      FVG_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * (op->n + 1), c->stream));
+      FVG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 2, c->stream));
+      return;
+    }
+    if (op->fmt == FVG_CRS) {
+      crs_pass(c, *op->A, storage, vdt, x, vdt, nullptr, EPI_LOGREG, &lr, s1.p, P_PASS1);
+    } else {
+      if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->H, storage, vdt, x, vdt, z.p);
+      else if (op->fmt == FVG_JDS) jds_spmv(c, *op->J, storage, vdt, x, vdt, z.p, false);
+      else ell_spmv(c, *op->E, storage, vdt, x, vdt, z.p);
+      logreg_rows(c, z.p, vdt, op->m, lr);
+    }
+    // backward product into grad[0..n) (FP64 output)
+    if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->HT, storage, vdt, r.p, FVG_F64, grad);
+    else if (op->fmt == FVG_JDS) jds_spmv(c, *op->JT, storage, vdt, r.p, FVG_F64, grad, false);
+    else crs_pass(c, *op->AT, storage, vdt, r.p, FVG_F64, grad, EPI_STORE, nullptr, s2.p, P_PASS2);
+  }
+};
+
+static void build_operand(fvg_ctx* c, fvg_matrix* M, int fmt, Operand& o) {
+  o.fmt = fmt;
+  o.m = M->A.m;
+  o.n = M->A.n;
+  o.master = M->master;
+  if (fmt == FVG_CRS || fmt == FVG_ELL) {
+    if (!M->AT) {
+      M->AT.reset(new DevCRS());
+      crs_build_transpose(c, M->A, *M->AT, M->master);
+    }
+    o.AT = M->AT.get();
+  }
+  if (fmt == FVG_CRS) o.A = &M->A;
+  if (fmt == FVG_ELL) {
+    if (!M->ell) {
+      M->ell.reset(new DevELL());
+      ell_build(c, M->A, *M->ell, M->master);
+    }
+    o.E = M->ell.get();
+  }
+  if (fmt == FVG_HYBRID) {
+    if (!M->hyb) {
+      M->hyb.reset(new DevHYB());
+      hyb_build(c, M->A, *M->hyb, M->master, 256);
+    }
+    if (!M->thyb) {
+      if (!M->AT) {
+        M->AT.reset(new DevCRS());
+        crs_build_transpose(c, M->A, *M->AT, M->master);
+      }
+      M->thyb.reset(new DevHYB());
+      hyb_build(c, *M->AT, *M->thyb, M->master, 256);
+    }
+    o.H = M->hyb.get();
+    o.HT = M->thyb.get();
+  }
+  if (fmt == FVG_JDS) {
+    if (!M->jds) {
+      M->jds.reset(new DevJDS());
+      jds_build(c, M->A, *M->jds, M->master);
+    }
+    if (!M->tjds) {
+      if (!M->AT) {
+        M->AT.reset(new DevCRS());
+        crs_build_transpose(c, M->A, *M->AT, M->master);
+      }
+      M->tjds.reset(new DevJDS());
+      jds_build(c, *M->AT, *M->tjds, M->master);
+    }
+    o.J = M->jds.get();
+    o.JT = M->tjds.get();
+  }
+}
+
+// rows [r0, r1) of A as their own CRS matrix (a rank block or a minibatch:
+// ml/glm/common.hpp:232-257)
+__global__ void k_rebase(const i32* __restrict__ off, i64 r0, i64 cnt, i32* __restrict__ out) {
+  VEC_LOOP(i, cnt + 1) out[i] = off[r0 + i] - off[r0];
+}
+
+static void crs_rows(fvg_ctx* c, const DevCRS& a, int master, i64 r0, i64 r1, DevCRS& b) {
+  b.m = r1 - r0;
+  b.n = a.n;
+  i32 s = 0, e = 0;
+  FVG_CUDA(cudaMemcpyAsync(&s, a.off.as<i32>() + r0, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(&e, a.off.as<i32>() + r1, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  b.nnz = e - s;
+  b.off.alloc(sizeof(i32) * (b.m + 1), c->stream);
+  k_rebase<<<(unsigned)std::max<i64>(1, std::min<i64>((b.m + 256) / 256, 4096)), kVecThreads, 0, c->stream>>>(
+      a.off.as<i32>(), r0, b.m, b.off.as<i32>());
+  check_launch("rebase");
+  count_launch(c);
+  b.idx.alloc(sizeof(i32) * (b.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(b.idx.as<i32>() + b.nnz, 0, sizeof(i32) * kPad, c->stream));
+  if (b.nnz) FVG_CUDA(cudaMemcpyAsync(b.idx.p, a.idx.as<i32>() + s, sizeof(i32) * b.nnz, cudaMemcpyDeviceToDevice,
+                                      c->stream));
+  const int sz = dtype_size(master);
+  b.val[master].alloc((size_t)sz * (b.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync((char*)b.val[master].p + (size_t)sz * b.nnz, 0, (size_t)sz * kPad, c->stream));
+  if (b.nnz) FVG_CUDA(cudaMemcpyAsync(b.val[master].p, (const char*)a.val[master].p + (size_t)sz * s,
+                                      (size_t)sz * b.nnz, cudaMemcpyDeviceToDevice, c->stream));
+  b.max_row = a.max_row;  // upper bound; only used for sizing
+  // exact max row length of the block for the layouts that need it
+  std::vector<i32> hoff(b.m + 1);
+  FVG_CUDA(cudaMemcpyAsync(hoff.data(), b.off.p, sizeof(i32) * (b.m + 1), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  i64 mr = 0;
+  for (i64 i = 0; i < b.m; i++) mr = std::max<i64>(mr, (i64)hoff[i + 1] - hoff[i]);
+  b.max_row = mr;
+}
+
+static void build_block_operand(fvg_ctx* c, fvg_matrix* M, int fmt, i64 r0, i64 r1, Operand& o) {
+  o.fmt = fmt;
+  o.master = M->master;
+  o.oA.reset(new DevCRS());
+  crs_rows(c, M->A, M->master, r0, r1, *o.oA);
+  o.m = o.oA->m;
+  o.n = o.oA->n;
+  auto trans = [&]() {
+    o.oAT.reset(new DevCRS());
+    crs_build_transpose(c, *o.oA, *o.oAT, o.master);
+  };
+  if (fmt == FVG_CRS) {
+    trans();
+    o.A = o.oA.get();
+    o.AT = o.oAT.get();
+  } else if (fmt == FVG_ELL) {
+    trans();
+    o.oE.reset(new DevELL());
+    ell_build(c, *o.oA, *o.oE, o.master);
+    o.E = o.oE.get();
+    o.AT = o.oAT.get();
+  } else if (fmt == FVG_HYBRID) {
+    trans();
+    o.oH.reset(new DevHYB());
+    hyb_build(c, *o.oA, *o.oH, o.master, 256);
+    o.oHT.reset(new DevHYB());
+    hyb_build(c, *o.oAT, *o.oHT, o.master, 256);
+    o.H = o.oH.get();
+    o.HT = o.oHT.get();
+  } else {
+    trans();
+    o.oJ.reset(new DevJDS());
+    jds_build(c, *o.oA, *o.oJ, o.master);
+    o.oJT.reset(new DevJDS());
+    jds_build(c, *o.oAT, *o.oJT, o.master);
+    o.J = o.oJ.get();
+    o.JT = o.oJT.get();
+  }
+}
+
+static void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label) {
+  if (!p) fail(FVG_ERR_INVALID_ARG, "null params");
+  if (!(p->num_iteration > 0 && p->alpha > 0 && p->reg_param >= 0 && p->convergence_tol >= 0))
+    fail(FVG_ERR_INVALID_ARG, "checkAssumption failed: numIteration > 0 && alpha > 0 && regParam >= 0 && "
+                              "convergenceTol >= 0");
+  if (M->A.n == 0 || M->A.m == 0) fail(FVG_ERR_INVALID_ARG, "Empty training data\n");
+  if (!label) fail(FVG_ERR_INVALID_ARG, "Number of label and data are different\n");
+  if (p->reg_type < 0 || p->reg_type > 2) fail(FVG_ERR_INVALID_ARG, "Unsupported regularizer!\n");
+  if (p->storage < 0 || p->storage > 2) fail(FVG_ERR_INVALID_ARG, "unknown storage precision");
+  if (p->storage == FVG_F64 && M->master != FVG_F64)
+    fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 input values");
+}
+
+struct HostPinned {
+  double* p = nullptr;
+  explicit HostPinned(size_t n) { FVG_CUDA(cudaMallocHost(&p, sizeof(double) * n)); }
+  ~HostPinned() { if (p) cudaFreeHost(p); }
+};
+
+// ============================================================== L-BFGS
+void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
+                 double* w_h, double* b_h, i64* n_iter, double* loss_out) {
+  check_common(p, M, label_h);
+  const int fmt = p->mat_type;
+  if (fmt == FVG_JDS || fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (p->hist_size < 1 || p->hist_size > kMaxHist)
+    fail(FVG_ERR_INVALID_ARG, "hist_size must be in [1, " + std::to_string(kMaxHist) + "]");
+  const i64 m = M->A.m, n = M->A.n, n1 = n + 1;
+  const int h = (int)p->hist_size;
+  cudaStream_t s = c->stream;
+
+  Operand op;
+  build_operand(c, M, fmt, op);
+  DBuf label, sw;
+  label.alloc(sizeof(double) * m, s);
+  FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (sw_h) {
+    sw.alloc(sizeof(double) * m, s);
+    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  int storage = p->storage;
+  Evaluator ev;
+  ev.init(c, &op, storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, p->intercept);
+
+  // device vectors
+  DBuf W, NW, NWF, G, NG, Q, Z, STEP, S, Y, part, stbuf;
+  W.alloc(sizeof(double) * n1, s);
+  NW.alloc(sizeof(double) * n1, s);
+  G.alloc(sizeof(double) * n1, s);
+  NG.alloc(sizeof(double) * n1, s);
+  Q.alloc(sizeof(double) * n1, s);
+  Z.alloc(sizeof(double) * n1, s);
+  STEP.alloc(sizeof(double) * n1, s);
+  S.alloc(sizeof(double) * n1 * h, s);
+  Y.alloc(sizeof(double) * n1 * h, s);
+  NWF.alloc(sizeof(float) * n1, s);
+  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 2 * c->num_sms));
+  part.alloc(sizeof(double) * 2 * vgrid + 256, s);
+  stbuf.alloc(sizeof(LbState) + 256, s);
+  unsigned* ticket = (unsigned*)((char*)part.p + sizeof(double) * 2 * vgrid);
+  FVG_CUDA(cudaMemsetAsync(ticket, 0, 256, s));
+  LbState init = {};
+  init.h = h;
+  init.b[0] = *b_h;
+  LbState* st = stbuf.as<LbState>();
+  FVG_CUDA(cudaMemcpyAsync(st, &init, sizeof(LbState), cudaMemcpyHostToDevice, s));
+  FVG_CUDA(cudaMemcpyAsync(W.p, w_h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  VecArgs va{n, n1, h, part.as<double>(), ticket, st};
+  HostPinned hp(4);
+
+  const double* W_ = W.as<double>();
+  auto weights_for = [&](const double* w64, float* wf) -> const void* {
+    if (storage == FVG_F64) return w64;
+    k_d2f<<<vgrid, kVecThreads, 0, s>>>(w64, wf, n);
+    check_launch("d2f");
+    count_launch(c);
+    return wf;
+  };
+  auto evaluate = [&](const void* x, const double* b, double* g, int accepted) {
+    ev.eval(x, b, g, st->eval);
+    ProfScope ps(c, P_LBFGS);
+    k_gmax<<<vgrid, kVecThreads, 0, s>>>(g, va);
+    k_gnorm<<<vgrid, kVecThreads, 0, s>>>(g, va, accepted);
+    check_launch("gnorm");
+    count_launch(c, 2);
+  };
+  auto read_host = [&]() {
+    FVG_CUDA(cudaMemcpyAsync(hp.p, st->host, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+    FVG_CUDA(cudaStreamSynchronize(s));
+  };
+
+  // initial evaluation (lbfgs_parallelizer.hpp:286-295)
+  evaluate(weights_for(W_, NWF.as<float>()), &st->b[0], G.as<double>(), 1);
+  read_host();
+  double loss = hp.p[0];
+
+  const bool ell = (fmt == FVG_ELL);
+  const bool mixed = storage != FVG_F64;
+  std::vector<double> rms_hist;
+  i64 i = 1;
+  double last_rms = 0;
+  for (; i <= p->num_iteration; i++) {
+    {
+      ProfScope ps(c, P_LBFGS);
+      for (int q = h - 1; q >= 0; q--)
+        k_down<<<vgrid, kVecThreads, 0, s>>>(q, G.as<double>(), Q.as<double>(), S.as<double>(), Y.as<double>(), va);
+      for (int q = 0; q < h; q++)
+        k_up<<<vgrid, kVecThreads, 0, s>>>(q, Q.as<double>(), Z.as<double>(), S.as<double>(), Y.as<double>(), va);
+      k_step<<<vgrid, kVecThreads, 0, s>>>(G.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(), va);
+      k_step_norm<<<vgrid, kVecThreads, 0, s>>>(STEP.as<double>(), va);
+      check_launch("two-loop");
+      count_launch(c, 2 * h + 2);
+    }
+    int j = 1;
+    double newloss = 0, rms_t = 0;
+    for (; j <= 10; j++) {
+      {
+        ProfScope ps(c, P_LBFGS);
+        k_trial<<<vgrid, kVecThreads, 0, s>>>(j, W_, STEP.as<double>(), NW.as<double>(),
+                                              mixed ? NWF.as<float>() : nullptr, p->reg_type, p->reg_param,
+                                              ell ? 1 : 0, p->l2_no_eta, va);
+        check_launch("trial");
+        count_launch(c);
+      }
+      evaluate(mixed ? (const void*)NWF.p : NW.p, &st->b[1], NG.as<double>(), 0);
+      read_host();
+      newloss = hp.p[0];
+      rms_t = hp.p[2];
+      if (newloss - loss < 1e-4) break;  // LBFGS_SEARCH_TOL (lbfgs_parallelizer.hpp:155, 329)
+    }
+    {
+      ProfScope ps(c, P_LBFGS);
+      k_accept<<<vgrid, kVecThreads, 0, s>>>(W.as<double>(), G.as<double>(), NW.as<double>(), NG.as<double>(),
+                                             S.as<double>(), Y.as<double>(), va);
+      check_launch("accept");
+      count_launch(c);
+    }
+    loss = newloss;
+    last_rms = rms_t;
+    if (p->trace) {
+      double fac = 0;
+      FVG_CUDA(cudaMemcpyAsync(&fac, &st->factor[std::min(j, 10)], sizeof(double), cudaMemcpyDeviceToHost, s));
+      FVG_CUDA(cudaStreamSynchronize(s));
+      p->trace[4 * (i - 1) + 0] = loss;
+      p->trace[4 * (i - 1) + 1] = (double)j;
+      p->trace[4 * (i - 1) + 2] = rms_t;
+      p->trace[4 * (i - 1) + 3] = fac;
+    }
+    if (rms_t <= p->convergence_tol) break;
+    // refinement: leave BF16 values for FP32 once the gradient norm stalls
+    if (mixed && storage == FVG_BF16 && p->refine) {
+      rms_hist.push_back(rms_t);
+      bool stall = false;
+      if (rms_hist.size() >= 4) {
+        double best = *std::min_element(rms_hist.end() - 4, rms_hist.end() - 1);
+        stall = rms_t > p->refine_stall * best;
+      }
+      if (stall) {
+        storage = FVG_F32;
+        ev.set_storage(storage);
+        // re-evaluate the accepted model with FP32 values
+        evaluate(weights_for(W_, NWF.as<float>()), &st->b[0], G.as<double>(), 1);
+        read_host();
+        loss = hp.p[0];
+      }
+    }
+  }
+  *n_iter = (i == p->num_iteration + 1) ? p->num_iteration : i;
+  *loss_out = loss;
+  (void)last_rms;
+  FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaMemcpyAsync(b_h, &st->b[0], sizeof(double), cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ============================================================ SGD
+struct SgdArgs {
+  i64 n, n1;
+  double* part;
+  unsigned* ticket;
+  double* scal;  // [0] rmse, [1] b (accepted), [2] lb (local), [3] tot_b, [4] loss sum, [5] prev b
+};
+
+// w -= ra * g; b -= ra * bias  (update_model, gradient_descent.hpp:242-259)
+__global__ void k_sgd_update(double* __restrict__ LW, const double* __restrict__ G, double ra, int icpt, SgdArgs a) {
+  VEC_LOOP(j, a.n) LW[j] = __dsub_rn(LW[j], __dmul_rn(ra, G[j]));
+  if (icpt && blockIdx.x == 0 && threadIdx.x == 0) a.scal[2] = __dsub_rn(a.scal[2], __dmul_rn(ra, G[a.n]));
+}
+
+// rank delta LW - W accumulated into TOT in rank order (calc_diff_inplace +
+// typed_allreduce, sgd_parallelizer.hpp:178-187)
+__global__ void k_sgd_delta(const double* __restrict__ LW, const double* __restrict__ W, double* __restrict__ TOT,
+                            int first, const double* __restrict__ eval, SgdArgs a) {
+  VEC_LOOP(j, a.n) {
+    double d = __dsub_rn(LW[j], W[j]);
+    TOT[j] = first ? d : __dadd_rn(TOT[j], d);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double db = __dsub_rn(a.scal[2], a.scal[1]);
+    a.scal[3] = first ? db : __dadd_rn(a.scal[3], db);
+  }
+  (void)eval;
+}
+
+// w += Σdelta; b += Σdelta_b; regularize(w, alpha/sqrt(i)); RMSE of the
+// change (sgd_parallelizer.hpp:189-217)
+__global__ void __launch_bounds__(kVecThreads) k_sgd_apply(double* __restrict__ W, const double* __restrict__ TOT,
+                                                           int rtype, double lambda, double eta, int no_eta,
+                                                           SgdArgs a) {
+  const double scale = fmax(0.0, 1.0 - (lambda * eta));
+  double v[1] = {0.0};
+  VEC_LOOP(j, a.n) {
+    double prev = W[j];
+    double w = __dadd_rn(prev, TOT[j]);
+    if (rtype == FVG_REG_L2) w = no_eta ? __dsub_rn(w, __dmul_rn(lambda, w)) : __dmul_rn(scale, w);
+    else if (rtype == FVG_REG_L1) w = __dsub_rn(w, __dmul_rn(lambda, (double)((w >= 0) - (w < 0))));
+    W[j] = w;
+    double df = prev - w;
+    v[0] += df * df;
+  }
+  const bool mx[1] = {false};
+  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) {
+    double pb = a.scal[1];
+    double nb = __dadd_rn(pb, a.scal[3]);
+    a.scal[1] = nb;
+    double red = t[0] + (pb - nb) * (pb - nb);
+    a.scal[0] = sqrt(red / (double)(a.n + 1));
+  });
+}
+
+__global__ void k_sgd_loss(const double* __restrict__ out, double* __restrict__ scal, int first) {
+  scal[4] = first ? out[0] : scal[4] + out[0];
+}
+
+void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
+               double* w_h, double* b_h, i64* n_iter, double* loss_out) {
+  check_common(p, M, label_h);
+  const int fmt = p->mat_type;
+  if (fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (!(p->mini_batch_fraction > 0.0 && p->mini_batch_fraction <= 1.0))
+    fail(FVG_ERR_INVALID_ARG, "checkAssumption failed: miniBatchFraction > 0.0 && miniBatchFraction <= 1.0");
+  const i64 m = M->A.m, n = M->A.n, n1 = n + 1;
+  const int P = std::max(1, p->num_partitions);
+  cudaStream_t s = c->stream;
+  std::vector<i64> splits(P + 1);
+  if (p->row_splits) {
+    for (int r = 0; r <= P; r++) splits[r] = p->row_splits[r];
+    if (splits[0] != 0 || splits[P] != m) fail(FVG_ERR_INVALID_ARG, "row_splits must run from 0 to num_row");
+    for (int r = 0; r < P; r++)
+      if (splits[r + 1] < splits[r]) fail(FVG_ERR_INVALID_ARG, "row_splits must be non-decreasing");
+  } else {
+    for (int r = 0; r <= P; r++) splits[r] = m * r / P;
+  }
+  DBuf label, sw;
+  label.alloc(sizeof(double) * m, s);
+  FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (sw_h) {
+    sw.alloc(sizeof(double) * m, s);
+    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  // minibatches per rank (common.hpp:283-321: ceil(frac*rows) rounded up to 1024)
+  struct Batch {
+    Operand op;
+    Evaluator ev;
+    i64 r0;
+  };
+  std::vector<std::vector<std::unique_ptr<Batch>>> ranks(P);
+  const int storage = p->storage;
+  for (int r = 0; r < P; r++) {
+    i64 ns = splits[r + 1] - splits[r];
+    i64 tmp = (i64)std::ceil(ns * p->mini_batch_fraction);
+    i64 t2 = (tmp == 0 ? 0 : (tmp - 1) / 1024 + 1) * 1024;
+    i64 mbs = t2 < ns ? t2 : ns;
+    i64 nb = (ns == 0) ? 0 : (ns - 1) / mbs + 1;
+    for (i64 k = 0; k < nb; k++) {
+      i64 r0 = splits[r] + k * mbs, r1 = std::min(splits[r] + (k + 1) * mbs, splits[r + 1]);
+      auto b = std::make_unique<Batch>();
+      b->r0 = r0;
+      build_block_operand(c, M, fmt, r0, r1, b->op);
+      b->ev.init(c, &b->op, storage, label.as<double>() + r0, sw_h ? sw.as<double>() + r0 : nullptr, p->intercept);
+      ranks[r].push_back(std::move(b));
+    }
+  }
+  DBuf W, LW, LWF, G, TOT, part, scal, out;
+  W.alloc(sizeof(double) * n1, s);
+  LW.alloc(sizeof(double) * n1, s);
+  LWF.alloc(sizeof(float) * n1, s);
+  G.alloc(sizeof(double) * n1, s);
+  TOT.alloc(sizeof(double) * n1, s);
+  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 2 * c->num_sms));
+  part.alloc(sizeof(double) * 2 * vgrid + 256, s);
+  unsigned* ticket = (unsigned*)((char*)part.p + sizeof(double) * 2 * vgrid);
+  FVG_CUDA(cudaMemsetAsync(ticket, 0, 256, s));
+  scal.alloc(sizeof(double) * 8, s);
+  out.alloc(sizeof(double) * 2, s);
+  double hs[8] = {0, *b_h, *b_h, 0, 0, 0, 0, 0};
+  FVG_CUDA(cudaMemcpyAsync(scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+  FVG_CUDA(cudaMemcpyAsync(W.p, w_h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  SgdArgs sa{n, n1, part.as<double>(), ticket, scal.as<double>()};
+  HostPinned hp(8);
+  i64 i;
+  for (i = 1; i <= p->num_iteration; i++) {
+    const double ra = p->alpha / std::sqrt((double)i);
+    bool first_rank = true, first_loss = true;
+    for (int r = 0; r < P; r++) {
+      FVG_CUDA(cudaMemcpyAsync(LW.p, W.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      FVG_CUDA(cudaMemcpyAsync(scal.as<double>() + 2, scal.as<double>() + 1, sizeof(double),
+                               cudaMemcpyDeviceToDevice, s));
+      for (auto& b : ranks[r]) {
+        const void* x = LW.p;
+        if (storage != FVG_F64) {
+          k_d2f<<<vgrid, kVecThreads, 0, s>>>(LW.as<double>(), LWF.as<float>(), n);
+          check_launch("d2f");
+          count_launch(c);
+          x = LWF.p;
+        }
+        b->ev.eval(x, scal.as<double>() + 2, G.as<double>(), out.as<double>());
+        k_sgd_loss<<<1, 1, 0, s>>>(out.as<double>(), scal.as<double>(), first_loss ? 1 : 0);
+        k_sgd_update<<<vgrid, kVecThreads, 0, s>>>(LW.as<double>(), G.as<double>(), ra, p->intercept, sa);
+        check_launch("sgd_update");
+        count_launch(c, 2);
+        first_loss = false;
+      }
+      k_sgd_delta<<<vgrid, kVecThreads, 0, s>>>(LW.as<double>(), W.as<double>(), TOT.as<double>(), first_rank ? 1 : 0,
+                                                out.as<double>(), sa);
+      check_launch("sgd_delta");
+      count_launch(c);
+      first_rank = false;
+    }
+    k_sgd_apply<<<vgrid, kVecThreads, 0, s>>>(W.as<double>(), TOT.as<double>(), p->reg_type, p->reg_param,
+                                              p->alpha / std::sqrt((double)i), p->l2_no_eta, sa);
+    check_launch("sgd_apply");
+    count_launch(c);
+    FVG_CUDA(cudaMemcpyAsync(hp.p, scal.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
+    FVG_CUDA(cudaStreamSynchronize(s));
+    if (hp.p[0] < p->convergence_tol) break;
+  }
+  *n_iter = (i == p->num_iteration + 1) ? p->num_iteration : i;
+  FVG_CUDA(cudaMemcpyAsync(hp.p, scal.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaStreamSynchronize(s));
+  *b_h = hp.p[1];
+  *loss_out = hp.p[4];
+}
+
+// ====================================================== single evaluation
+void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
+                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h) {
+  if (fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (storage == FVG_F64 && M->master != FVG_F64) fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 values");
+  const i64 m = M->A.m, n = M->A.n;
+  cudaStream_t s = c->stream;
+  Operand op;
+  build_operand(c, M, fmt, op);
+  DBuf label, sw, w, wf, g, out, bd;
+  label.alloc(sizeof(double) * std::max<i64>(m, 1), s);
+  if (m) FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (sw_h) {
+    sw.alloc(sizeof(double) * m, s);
+    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  w.alloc(sizeof(double) * (n + 1), s);
+  wf.alloc(sizeof(float) * (n + 1), s);
+  g.alloc(sizeof(double) * (n + 1), s);
+  out.alloc(sizeof(double) * 2, s);
+  bd.alloc(sizeof(double), s);
+  FVG_CUDA(cudaMemcpyAsync(w.p, w_h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  FVG_CUDA(cudaMemcpyAsync(bd.p, &b, sizeof(double), cudaMemcpyHostToDevice, s));
+  Evaluator ev;
+  ev.init(c, &op, storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, icpt);
+  const void* x = w.p;
+  if (storage != FVG_F64) {
+    k_d2f<<<256, kVecThreads, 0, s>>>(w.as<double>(), wf.as<float>(), n);
+    check_launch("d2f");
+    count_launch(c);
+    x = wf.p;
+  }
+  ev.eval(x, bd.as<double>(), g.as<double>(), out.as<double>());
+  double ho[2];
+  FVG_CUDA(cudaMemcpyAsync(grad_h, g.p, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaMemcpyAsync(ho, out.p, sizeof(ho), cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaStreamSynchronize(s));
+  *loss_h = ho[0];
+}
+
+}  // namespace fvg

@@ -1,0 +1,192 @@
+/*
+ * fvg.h — C ABI of the GB300 sparse logistic-regression path.
+ *
+ * One process drives one GPU.  A context owns a CUDA stream; matrices are
+ * uploaded once (CRS, int32 row offsets and column ids, FP64/FP32/BF16
+ * values), and the derived device layouts the reference builds on the host
+ * (transposed CRS, ELL, JDS, JDS/CRS hybrid) are built on the device.
+ * Every call returns an fvg_status; no C++ exception crosses this boundary.
+ * fvg_ctx_last_error() gives the message of the last failing call, which for
+ * argument errors repeats the reference's own message.
+ *
+ * Threading: a context is used by one host thread at a time; calls on one
+ * context run in order on its stream.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the frovedis source tree).
+ */
+#ifndef FVG_H
+#define FVG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FVG_API __attribute__((visibility("default")))
+#else
+#define FVG_API
+#endif
+
+typedef struct fvg_ctx fvg_ctx;
+typedef struct fvg_matrix fvg_matrix;
+
+typedef enum {
+  FVG_OK = 0,
+  FVG_ERR_INVALID_ARG = 1,   /* reference: REPORT_ERROR(USER_ERROR, ...) / checkAssumption */
+  FVG_ERR_SIZE_MISMATCH = 2, /* reference: std::runtime_error from operator* */
+  FVG_ERR_UNSUPPORTED = 3,   /* reference: "Unsupported input matrix type!!" */
+  FVG_ERR_CUDA = 4,
+  FVG_ERR_OUT_OF_MEMORY = 5,
+  FVG_ERR_INTERNAL = 6
+} fvg_status;
+
+/* value / vector element types */
+typedef enum { FVG_F64 = 0, FVG_F32 = 1, FVG_BF16 = 2 } fvg_dtype;
+
+/* same numbering as frovedis::MatType (ml/utility/mattype.hpp:6-11) */
+typedef enum { FVG_CRS = 0, FVG_JDS = 1, FVG_ELL = 2, FVG_HYBRID = 3 } fvg_format;
+
+/* same numbering as frovedis::RegType (ml/glm/regularizer.hpp:8-12) */
+typedef enum { FVG_REG_ZERO = 0, FVG_REG_L1 = 1, FVG_REG_L2 = 2 } fvg_regtype;
+
+/* ------------------------------------------------------------- context */
+FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out);
+FVG_API void fvg_ctx_destroy(fvg_ctx* ctx);
+FVG_API const char* fvg_ctx_last_error(const fvg_ctx* ctx);
+/* The context's cudaStream_t, for callers that order their own work with it. */
+FVG_API void* fvg_ctx_stream(fvg_ctx* ctx);
+FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* ctx);
+/* Kernel timing with CUDA events on the context stream (off by default).
+ * Names: "spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec", "transpose",
+ * "spmv_ell", "spmv_jds", "spmv_hyb", "spmm". */
+FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* ctx, int enable);
+FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* ctx, const char* name, double* total_ms, int64_t* launches);
+FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* ctx);
+/* Number of CUDA kernels this context launched since creation. */
+FVG_API int64_t fvg_ctx_kernel_launches(fvg_ctx* ctx);
+
+/* -------------------------------------------------------------- matrix */
+/* Upload a CRS matrix (crs_matrix_local<T,I,O>, matrix/crs_matrix.hpp:240-331):
+ * off[num_row+1] with off[0]=0, idx[nnz], val[nnz] of val_dtype.  Pointers
+ * are host memory unless on_device != 0 (then they are copied device to
+ * device).  nnz = off[num_row] must be < 2^31.  Column ids must lie in
+ * [0, num_col) (checked). */
+FVG_API fvg_status fvg_matrix_create_crs(fvg_ctx* ctx, int64_t num_row, int64_t num_col, const int32_t* off,
+                                         const int32_t* idx, const void* val, fvg_dtype val_dtype, int on_device,
+                                         fvg_matrix** out);
+FVG_API void fvg_matrix_destroy(fvg_matrix* mat);
+FVG_API fvg_status fvg_matrix_info(const fvg_matrix* mat, int64_t* num_row, int64_t* num_col, int64_t* nnz);
+/* Build the device layout `fmt` (and its transposed counterpart when
+ * with_transpose != 0), replacing the host conversions of
+ * ml/utility/matrix_conversion.hpp:12-111.  Idempotent. */
+FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, int with_transpose);
+/* Add a value plane of another precision (FP32 or BF16, rounded to nearest
+ * even from the uploaded values) used when a call asks for that storage. */
+FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* ctx, fvg_matrix* mat, fvg_dtype storage);
+/* Device bytes held by the matrix and everything derived from it. */
+FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* mat);
+
+/* Copies of the derived layouts to host memory, in the reference's array
+ * order, for checking the device builders against the reference's:
+ *  transpose  — crs_matrix_local::transpose (crs_matrix.hpp:356-412):
+ *               toff[num_col+1], tidx[nnz], tval[nnz] (FP64).
+ *  ELL        — ell_matrix_local(crs) (ell_matrix.hpp:63-95): width, then
+ *               eidx/eval column-major [width*num_row].
+ *  JDS        — jds_matrix_local(crs) (jds_matrix.hpp:81-146): perm[num_row],
+ *               joff[ndiag+1], jidx/jval[nnz].
+ *  hybrid     — jds_crs_hybrid_local(crs, 256) (jds_crs_hybrid.hpp:38-153):
+ *               info = {jds ndiag, crs rows, crs nnz, jds nnz, perm length},
+ *               then the JDS part and the CRS tail.
+ * Pass NULL array pointers to query sizes only. */
+FVG_API fvg_status fvg_matrix_get_transpose(fvg_ctx* ctx, fvg_matrix* mat, int32_t* toff, int32_t* tidx,
+                                            double* tval);
+FVG_API fvg_status fvg_matrix_get_ell(fvg_ctx* ctx, fvg_matrix* mat, int64_t* width, int32_t* eidx, double* eval);
+FVG_API fvg_status fvg_matrix_get_jds(fvg_ctx* ctx, fvg_matrix* mat, int64_t* ndiag, int32_t* perm, int64_t* joff,
+                                      int32_t* jidx, double* jval);
+FVG_API fvg_status fvg_matrix_get_hybrid(fvg_ctx* ctx, fvg_matrix* mat, int64_t* info, int32_t* perm,
+                                         int64_t* joff, int32_t* jidx, double* jval, int64_t* coff, int32_t* cidx,
+                                         double* cval);
+
+/* ------------------------------------------------------------ products */
+/* y = A x: operator*(crs_matrix_local, vector) (crs_matrix.hpp:1518-1525),
+ * operator*(ell_matrix_local, vector) (ell_matrix.hpp:229), operator*(
+ * jds_matrix_local, vector) (jds_matrix.hpp:419-426), operator*(
+ * jds_crs_hybrid_local, vector) (jds_crs_hybrid.hpp:213-221).
+ * x has num_col and y num_row elements of vec_dtype (FVG_F64 or FVG_F32);
+ * storage picks the value plane (FP64 values need FVG_F64 vectors).
+ * Accumulation is FP64 for FP64 vectors and FP32 otherwise.
+ * on_device != 0: x and y are device pointers (ordered on the ctx stream). */
+FVG_API fvg_status fvg_spmv(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
+                            const void* x, void* y, int on_device);
+/* y = A^T x, x has num_row and y num_col elements: trans_mv(ell_matrix_local,
+ * vector) (ell_matrix.hpp:357-380) and `trans * v` on the transposed copy
+ * (gradient_descent.hpp:211).  Always computed as a gather over a device
+ * transposed copy in `fmt` (deterministic; no atomics). */
+FVG_API fvg_status fvg_trans_mv(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage,
+                                fvg_dtype vec_dtype, const void* x, void* y, int on_device);
+/* Y = A X, X row-major num_col x k, Y row-major num_row x k:
+ * operator*(crs_matrix_local, rowmajor_matrix_local) (crs_matrix.hpp:2053-2064),
+ * jds (jds_matrix.hpp:799-807), hybrid (jds_crs_hybrid.hpp:244-252). */
+FVG_API fvg_status fvg_spmm(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
+                            const void* X, int64_t k, void* Y, int on_device);
+
+/* ------------------------------------------------------------ training */
+typedef struct {
+  int64_t num_iteration;      /* numIteration (default 1000) */
+  double alpha;               /* alpha (default 0.01) */
+  int64_t hist_size;          /* L-BFGS history (default 10) */
+  double reg_param;           /* regParam (default 0.01) */
+  int32_t reg_type;           /* fvg_regtype (default ZERO) */
+  int32_t intercept;          /* isIntercept (default 0) */
+  double convergence_tol;     /* convergenceTol (default 0.001) */
+  int32_t mat_type;           /* fvg_format (default CRS) */
+  double mini_batch_fraction; /* SGD miniBatchFraction (default 1.0) */
+  int32_t num_partitions;     /* SGD/L-BFGS: emulate this many MPI ranks
+                                 (row blocks; default 1) */
+  int32_t storage;            /* value precision: FVG_F64 (default), FVG_F32, FVG_BF16 */
+  int32_t refine;             /* BF16/F32 storage: switch to FP32 values once the
+                                 gradient norm stalls (default 1) */
+  double refine_stall;        /* stall test: rms > refine_stall * best rms of the
+                                 last 3 iterations (default 0.97) */
+  int32_t l2_no_eta;          /* L2 as w -= lambda*w (the reference built without
+                                 USE_ETA, regularizer.hpp:50-54) (default 0) */
+  int32_t use_graph;          /* capture per-trial work as CUDA graphs (default 1) */
+  double* trace;              /* optional host array, 4 doubles per iteration:
+                                 loss, line-search trials, rms, step factor */
+  const int64_t* row_splits;  /* optional num_partitions+1 row splits */
+} fvg_glm_params;
+
+FVG_API void fvg_glm_params_default(fvg_glm_params* p);
+
+/* logistic_regression_with_lbfgs::train main API
+ * (ml/glm/logistic_regression_with_lbfgs.hpp:395-437 →
+ *  lbfgs_parallelizer.hpp:267-364, 366-462, 515-600).
+ * label[num_row] (±1), sample_weight[num_row] or NULL (= all ones),
+ * weight[num_col] and intercept hold the initial model on entry and the
+ * trained model on return.  Host pointers. */
+FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                    const double* sample_weight, const fvg_glm_params* params, double* weight,
+                                    double* intercept, int64_t* n_iter, double* final_loss);
+/* logistic_regression_with_sgd::train main API
+ * (ml/glm/logistic_regression_with_sgd.hpp:392-441 →
+ *  sgd_parallelizer.hpp:132-378, 441-550). */
+FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* ctx, fvg_matrix* mat, const double* label, const double* sample_weight,
+                                  const fvg_glm_params* params, double* weight, double* intercept, int64_t* n_iter,
+                                  double* final_loss);
+/* One loss/gradient evaluation (gradient_descent::compute_gradient,
+ * gradient_descent.hpp:196-225): grad[num_col+1] (bias last), *loss. */
+FVG_API fvg_status fvg_logreg_eval(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage,
+                                   const double* label, const double* sample_weight, const double* weight,
+                                   double intercept, int intercept_on, double* grad, double* loss);
+/* logistic_regression_model<T>::predict_probability (ml/glm/linear_model.hpp:376-392). */
+FVG_API fvg_status fvg_logreg_predict_probability(fvg_ctx* ctx, fvg_matrix* mat, const double* weight,
+                                                  double intercept, double* prob);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVG_H */
