@@ -227,7 +227,7 @@ def run_gpu(args):
         e2e_ms += (time.perf_counter() - t0) * 1e3
         e2e_iters += rr["n_iter"]
     e2e_ms = allmax(world, e2e_ms)
-    e2e_value = e2e_iters * world / (e2e_ms / 1e3)
+    e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:

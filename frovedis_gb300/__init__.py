@@ -320,10 +320,18 @@ class Matrix:
                     cidx=cidx[:cnnz], cval=cval[:cnnz], crs_rows=crows)
 
 
+_ALIASES = {"num_iter": "num_iteration", "numIteration": "num_iteration", "fmt": "mat_type",
+            "regParam": "reg_param", "hist": "hist_size", "tol": "convergence_tol"}
+
+
 def glm_params(**kw) -> GlmParams:
     p = GlmParams()
     load().fvg_glm_params_default(C.byref(p))
+    fields = {f[0] for f in GlmParams._fields_}
     for k, v in kw.items():
+        k = _ALIASES.get(k, k)
+        if k not in fields:
+            raise TypeError(f"unknown training parameter {k!r}")
         if k in ("reg_type",) and isinstance(v, str):
             v = REG[v]
         if k in ("mat_type",):

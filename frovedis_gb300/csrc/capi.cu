@@ -2,6 +2,7 @@
 // dispatch to the builders, products and drivers.  No C++ exception leaves
 // this file; every entry point returns an fvg_status and records the
 // message in the context.
+#include <algorithm>
 #include <cstring>
 #include <new>
 
@@ -78,8 +79,25 @@ FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out) {
   }
 }
 
+// Frees every device buffer of a matrix (its host handle stays valid).
+static void release_device(fvg_matrix* M) {
+  M->A = DevCRS();
+  M->AT.reset();
+  M->ell.reset();
+  M->jds.reset();
+  M->tjds.reset();
+  M->hyb.reset();
+  M->thyb.reset();
+}
+
 FVG_API void fvg_ctx_destroy(fvg_ctx* c) {
   if (!c) return;
+  cudaStreamSynchronize(c->stream);
+  for (fvg_matrix* M : c->matrices) {  // orphan the matrices still alive
+    release_device(M);
+    M->ctx = nullptr;
+  }
+  c->matrices.clear();
   cudaStreamSynchronize(c->stream);
   prof_destroy(c);
   cudaStreamDestroy(c->stream);
@@ -141,6 +159,7 @@ FVG_API fvg_status fvg_matrix_create_crs(fvg_ctx* c, int64_t num_row, int64_t nu
   M->ctx = c;
   M->master = val_dtype;
   crs_upload(c, M->A, num_row, num_col, off, idx, val, val_dtype, on_device != 0);
+  c->matrices.push_back(M);
   *out = M;
   M = nullptr;
   }
@@ -159,9 +178,19 @@ FVG_API fvg_status fvg_matrix_create_crs(fvg_ctx* c, int64_t num_row, int64_t nu
 
 FVG_API void fvg_matrix_destroy(fvg_matrix* M) {
   if (!M) return;
-  cudaStream_t s = M->ctx ? M->ctx->stream : nullptr;
+  fvg_ctx* c = M->ctx;
+  if (!c) {  // its context is gone; device memory was released with it
+    delete M;
+    return;
+  }
+  auto& v = c->matrices;
+  v.erase(std::remove(v.begin(), v.end(), M), v.end());
   delete M;  // buffers are freed stream-ordered
-  if (s) cudaStreamSynchronize(s);
+  cudaStreamSynchronize(c->stream);
+}
+
+static void own(fvg_ctx* c, fvg_matrix* M) {
+  if (M->ctx != c) fail(FVG_ERR_INVALID_ARG, "the matrix belongs to another (or a destroyed) context");
 }
 
 FVG_API fvg_status fvg_matrix_info(const fvg_matrix* M, int64_t* m, int64_t* n, int64_t* nnz) {
@@ -216,6 +245,7 @@ static void prepare(fvg_ctx* c, fvg_matrix* M, int fmt, bool trans) {
 FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, int with_transpose) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   prepare(c, M, fmt, with_transpose != 0);
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -237,6 +267,7 @@ static void ensure_plane_all(fvg_ctx* c, fvg_matrix* M, int dt) {
 FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* c, fvg_matrix* M, fvg_dtype storage) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   ensure_plane_all(c, M, storage);
   FVG_CUDA(cudaStreamSynchronize(c->stream));
@@ -290,6 +321,7 @@ FVG_API fvg_status fvg_matrix_get_transpose(fvg_ctx* c, fvg_matrix* M, int32_t* 
                                             double* tval) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   ensure_transpose(c, M);
   const DevCRS& t = *M->AT;
   if (toff) FVG_CUDA(cudaMemcpyAsync(toff, t.off.p, sizeof(int32_t) * (t.m + 1), cudaMemcpyDeviceToHost, c->stream));
@@ -303,6 +335,7 @@ FVG_API fvg_status fvg_matrix_get_transpose(fvg_ctx* c, fvg_matrix* M, int32_t* 
 FVG_API fvg_status fvg_matrix_get_ell(fvg_ctx* c, fvg_matrix* M, int64_t* width, int32_t* eidx, double* eval) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   prepare(c, M, FVG_ELL, false);
   const DevELL& e = *M->ell;
   if (width) *width = e.width;
@@ -327,6 +360,7 @@ FVG_API fvg_status fvg_matrix_get_jds(fvg_ctx* c, fvg_matrix* M, int64_t* ndiag,
                                       int32_t* jidx, double* jval) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   prepare(c, M, FVG_JDS, false);
   if (ndiag) *ndiag = M->jds->ndiag;
   get_jds(c, *M->jds, M->master, perm, joff, jidx, jval);
@@ -339,6 +373,7 @@ FVG_API fvg_status fvg_matrix_get_hybrid(fvg_ctx* c, fvg_matrix* M, int64_t* inf
                                          double* cval) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   prepare(c, M, FVG_HYBRID, false);
   const DevHYB& h = *M->hyb;
   if (info) {
@@ -448,6 +483,7 @@ FVG_API fvg_status fvg_spmv(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype
                             const void* x, void* y, int on_device) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   need((x && y) || M->A.m == 0 || M->A.n == 0, FVG_ERR_INVALID_ARG, "null vector");
   run_product(c, M, fmt, storage, vec_dtype, x, y, false, on_device != 0);
   API_END(c)
@@ -457,6 +493,7 @@ FVG_API fvg_status fvg_trans_mv(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_d
                                 const void* x, void* y, int on_device) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   need((x && y) || M->A.m == 0 || M->A.n == 0, FVG_ERR_INVALID_ARG, "null vector");
   run_product(c, M, fmt, storage, vec_dtype, x, y, true, on_device != 0);
   API_END(c)
@@ -466,6 +503,7 @@ FVG_API fvg_status fvg_spmm(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype
                             const void* X, int64_t k, void* Y, int on_device) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   check_vec_args(storage, vec_dtype);
   need(k >= 0, FVG_ERR_INVALID_ARG, "negative number of columns");
   need(fmt >= 0 && fmt <= 3, FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
@@ -508,6 +546,7 @@ FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* lab
                                     double* final_loss) {
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   lbfgs_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
   API_END(c)
 }
@@ -517,6 +556,7 @@ FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* c, fvg_matrix* M, const double* label
                                   double* final_loss) {
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
   API_END(c)
 }
@@ -526,6 +566,7 @@ FVG_API fvg_status fvg_logreg_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fv
                                    double intercept, int intercept_on, double* grad, double* loss) {
   if (!c || !M || !grad || !loss || !weight) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss);
   API_END(c)
@@ -535,6 +576,7 @@ FVG_API fvg_status fvg_logreg_predict_probability(fvg_ctx* c, fvg_matrix* M, con
                                                   double intercept, double* prob) {
   if (!c || !M || !weight || !prob) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  own(c, M);
   need(M->master == FVG_F64, FVG_ERR_INVALID_ARG, "predict_probability needs FP64 values");
   DBuf w, y;
   w.alloc(sizeof(double) * std::max<int64_t>(M->A.n, 1), c->stream);

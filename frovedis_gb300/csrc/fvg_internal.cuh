@@ -124,8 +124,8 @@ struct fvg_ctx {
   int64_t launches = 0;
   bool profiling = false;
   fvg::Profiler* prof = nullptr;  // owned; prof_create / prof_destroy
-  // pinned host scratch for scalar read-backs
-  double* host_scalars = nullptr;
+  // live matrices: destroying the context releases their device memory
+  std::vector<fvg_matrix*> matrices;
 };
 
 struct fvg_matrix {

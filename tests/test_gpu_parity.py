@@ -28,7 +28,7 @@ def ctx():
 
 
 def rand_crs(rng, m, n, maxlen=40, long_rows=(), empty_every=13, dup_row=None):
-    lens = rng.integers(0, maxlen + 1, m)
+    lens = np.minimum(rng.integers(0, maxlen + 1, m), n)
     lens[::empty_every] = 0
     for r, L in long_rows:
         lens[r] = min(L, n)
