@@ -123,9 +123,11 @@ def allmax(world, v):
     return v
 
 
-def make_data(scale, threads=0):
+def make_data(scale, threads=0, cols=0):
     from frovedis_gb300 import datagen
     spec = datagen.logreg_10m_1m(scale)
+    if cols:
+        spec.n = cols
     off, idx, val, label = datagen.generate(spec, nthreads=threads)
     return spec, off, idx, val, label
 
@@ -147,7 +149,7 @@ def run_gpu(args):
 
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
-    spec, off, idx, val, label = make_data(args.scale)
+    spec, off, idx, val, label = make_data(args.scale, cols=args.cols)
     m, n, nnz = spec.m, spec.n, int(off[-1])
     ctx = fv.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -249,7 +251,9 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "kernel": "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)",
-                     "bytes_per_eval": b1 + b2, "launches": p1_n + p2_n, "kernel_ms": spmv_ms},
+                     "bytes_per_eval": b1 + b2, "launches": p1_n + p2_n, "kernel_ms": spmv_ms,
+                     "pass1_ms_avg": p1_ms / max(p1_n, 1), "pass2_ms_avg": p2_ms / max(p2_n, 1),
+                     "pass1_gbs": b1 * p1_n / max(p1_ms, 1e-9) / 1e6, "pass2_gbs": b2 * p2_n / max(p2_ms, 1e-9) / 1e6},
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": ck,
@@ -291,7 +295,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    spec, off, idx, val, label = make_data(args.scale)
+    spec, off, idx, val, label = make_data(args.scale, cols=args.cols)
     threads = os.cpu_count() or 1
     vals = []
     for _ in range(args.warmup):
@@ -323,6 +327,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fvg", choices=["fvg", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--cols", type=int, default=0, help="override the column count (profiling cases)")
     ap.add_argument("--iters", type=int, default=50)
     ap.add_argument("--storage", default="bf16", choices=["bf16", "f32", "f64"])
     ap.add_argument("--e2e-steps", type=int, default=2)

@@ -1,5 +1,5 @@
 // Device-side builders: CRS upload and checks, the transposed CRS copy
-// (crs_matrix.hpp:356-412), the row-bin schedule of the CRS kernel, and the
+// (crs_matrix.hpp:356-412), the work-item schedule of the CRS kernel, and the
 // ELL / JDS / JDS-CRS-hybrid layouts (ell_matrix.hpp:63-95,
 // jds_matrix.hpp:81-146, jds_crs_hybrid.hpp:38-153).
 #include <algorithm>
@@ -173,124 +173,64 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 }
 
 // ---------------------------------------------------------------- schedule
-__host__ __device__ __forceinline__ int row_bin(i64 len, int ve) {
-  if (len == 0) return 0;
-  i64 nv = (len + ve - 1) / ve + 1;  // vectors touched, worst-case alignment
-  if (nv <= 2) return 0;
-  if (nv <= 4) return 1;
-  if (nv <= 8) return 2;
-  if (nv <= 16) return 3;
-  if (nv <= 32) return 4;
-  if (nv <= 256) return 5;
-  if (len <= kCtaRowMax) return 6;
-  return 7;
-}
-
-__global__ void k_row_bins(const i32* __restrict__ off, i64 m, int ve, uint32_t* __restrict__ keys,
-                           uint32_t* __restrict__ vals, unsigned long long* __restrict__ counts) {
-  __shared__ unsigned long long cnt[kBins];
-  if (threadIdx.x < kBins) cnt[threadIdx.x] = 0;
-  __syncthreads();
-  GRID_STRIDE(r, m) {
-    int b = row_bin((i64)off[r + 1] - off[r], ve);
-    keys[r] = (uint32_t)b;
-    vals[r] = (uint32_t)r;
-    atomicAdd(&cnt[b], 1ull);
-  }
-  __syncthreads();
-  if (threadIdx.x < kBins && cnt[threadIdx.x]) atomicAdd(&counts[threadIdx.x], cnt[threadIdx.x]);
-}
-
-__global__ void k_long_chunks(const i32* __restrict__ off, const i32* __restrict__ rows, i64 nlong,
-                              i64* __restrict__ nch) {
-  GRID_STRIDE(i, nlong) {
-    i64 s = off[rows[i]], e = off[rows[i] + 1];
-    i64 base = s & ~7ll;
-    nch[i] = (e - base + kChunk - 1) / kChunk;
-  }
-}
-
-__global__ void k_fill_chunks(const i32* __restrict__ off, const i32* __restrict__ rows, i64 nlong,
-                              const i64* __restrict__ first, i32* __restrict__ c0, i32* __restrict__ crow,
-                              i32* __restrict__ cbeg) {
-  GRID_STRIDE(i, nlong) {
-    i32 r = rows[i];
-    i64 s = off[r], e = off[r + 1];
-    i64 base = s & ~7ll;
-    i64 f = first[i], nc = (e - base + kChunk - 1) / kChunk;
-    c0[i] = (i32)f;
-    for (i64 j = 0; j < nc; j++) {
-      crow[f + j] = r;
-      cbeg[f + j] = (i32)(j == 0 ? s : base + j * kChunk);
-    }
-    if (i == nlong - 1) c0[nlong] = (i32)(f + nc);
-  }
-}
-
-const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int ve) {
-  int slot = (ve == 8) ? 1 : 0;
+// Packs rows, in row order, into work items (see Sched): consecutive short
+// rows share a row tile while the tile stays within `tile` nonzeros and
+// kTileRows rows; a long row becomes its own pieces of at most `tile`
+// nonzeros, cut at 8-element boundaries.  Done once per matrix on the host.
+const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
+  const int slot = 0;
   if (a.sched[slot]) return *a.sched[slot];
+  const i64 kLongRow = tile;
   auto s = std::make_unique<Sched>();
-  s->ve = ve;
-  i64 m = a.m;
-  DBuf keys, cnt;
-  s->rows.alloc(sizeof(uint32_t) * std::max<i64>(m, 1), c->stream);
-  keys.alloc(sizeof(uint32_t) * std::max<i64>(m, 1), c->stream);
-  cnt.alloc(sizeof(unsigned long long) * kBins, c->stream);
-  FVG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long) * kBins, c->stream));
-  if (m > 0) {
-    k_row_bins<<<grid_n(m), 256, 0, c->stream>>>(a.off.as<i32>(), m, ve, keys.as<uint32_t>(),
-                                                  s->rows.as<uint32_t>(), cnt.as<unsigned long long>());
-    check_launch("row_bins");
-    count_launch(c);
-    radix_sort_pairs(c, keys.as<uint32_t>(), s->rows.as<uint32_t>(), m, 3);
-  }
-  unsigned long long h[kBins];
-  FVG_CUDA(cudaMemcpyAsync(h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  s->tile = tile;
+  const i64 m = a.m;
+  std::vector<i32> off(m + 1);
+  FVG_CUDA(cudaMemcpyAsync(off.data(), a.off.p, sizeof(i32) * (m + 1), cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));
-  s->row_start[0] = 0;
-  for (int b = 0; b < kBins; b++) s->row_start[b + 1] = s->row_start[b] + (i64)h[b];
-  s->nlong = (i64)h[7];
-  s->nchunks = 0;
-  if (s->nlong > 0) {
-    DBuf nch, first;
-    nch.alloc(sizeof(i64) * s->nlong, c->stream);
-    first.alloc(sizeof(i64) * (s->nlong + 1), c->stream);
-    const i32* lrows = s->rows.as<i32>() + s->row_start[7];
-    k_long_chunks<<<grid_n(s->nlong), 256, 0, c->stream>>>(a.off.as<i32>(), lrows, s->nlong, nch.as<i64>());
-    check_launch("long_chunks");
-    count_launch(c);
-    scan_i64(c, nch.as<i64>(), first.as<i64>(), s->nlong);
-    i64 tot = 0;
-    FVG_CUDA(cudaMemcpyAsync(&tot, first.as<i64>() + s->nlong, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
-    FVG_CUDA(cudaStreamSynchronize(c->stream));
-    s->nchunks = tot;
-    s->long_rows.alloc(sizeof(i32) * s->nlong, c->stream);
-    FVG_CUDA(cudaMemcpyAsync(s->long_rows.p, lrows, sizeof(i32) * s->nlong, cudaMemcpyDeviceToDevice, c->stream));
-    s->long_chunk0.alloc(sizeof(i32) * (s->nlong + 1), c->stream);
-    s->chunk_row.alloc(sizeof(i32) * tot, c->stream);
-    s->chunk_beg.alloc(sizeof(i32) * tot, c->stream);
-    k_fill_chunks<<<grid_n(s->nlong), 256, 0, c->stream>>>(a.off.as<i32>(), lrows, s->nlong, first.as<i64>(),
-                                                          s->long_chunk0.as<i32>(), s->chunk_row.as<i32>(),
-                                                          s->chunk_beg.as<i32>());
-    check_launch("fill_chunks");
-    count_launch(c);
-  }
-  // work items: bins 0-5 hold 256/L rows per item, bin 6 one row, bin 7 one chunk
-  s->item_start[0] = 0;
-  for (int b = 0; b < kBins; b++) {
-    i64 rows = s->row_start[b + 1] - s->row_start[b];
-    i64 items;
-    if (b <= 5) {
-      i64 per = kThreads >> b;
-      items = (rows + per - 1) / per;
-    } else if (b == 6) {
-      items = rows;
-    } else {
-      items = s->nchunks;
+  std::vector<Item> items;
+  std::vector<i32> lrows, lpiece0;
+  i64 npieces = 0;
+  i64 t0 = 0, tnnz = 0;  // open tile: rows [t0, r), tnnz nonzeros
+  auto flush = [&](i64 r) {
+    if (r > t0) items.push_back(Item{(int32_t)t0, (int32_t)r, off[t0], off[r]});
+    t0 = r;
+    tnnz = 0;
+  };
+  for (i64 r = 0; r < m; r++) {
+    const i64 len = (i64)off[r + 1] - off[r];
+    if (len > kLongRow) {
+      flush(r);
+      const i64 st = off[r], en = off[r + 1], base = st & ~7ll;
+      lrows.push_back((i32)r);
+      lpiece0.push_back((i32)npieces);
+      for (i64 k = 0; base + k * tile < en; k++) {
+        i64 e0 = (k == 0) ? st : base + k * tile;
+        i64 e1 = std::min<i64>(en, base + (k + 1) * tile);
+        items.push_back(Item{(int32_t)r, (int32_t)(-1 - npieces), (int32_t)e0, (int32_t)e1});
+        npieces++;
+      }
+      t0 = r + 1;
+      continue;
     }
-    s->item_start[b + 1] = s->item_start[b] + items;
+    if (r > t0 && (tnnz + len > tile || r - t0 >= kTileRows)) flush(r);
+    tnnz += len;
   }
+  flush(m);
+  lpiece0.push_back((i32)npieces);
+  s->nitems = (i64)items.size();
+  s->nlong = (i64)lrows.size();
+  s->npieces = npieces;
+  s->items.alloc(sizeof(Item) * std::max<i64>(s->nitems, 1), c->stream);
+  if (s->nitems)
+    FVG_CUDA(cudaMemcpyAsync(s->items.p, items.data(), sizeof(Item) * s->nitems, cudaMemcpyHostToDevice, c->stream));
+  s->long_rows.alloc(sizeof(i32) * std::max<i64>(s->nlong, 1), c->stream);
+  s->long_piece0.alloc(sizeof(i32) * (s->nlong + 1), c->stream);
+  if (s->nlong)
+    FVG_CUDA(cudaMemcpyAsync(s->long_rows.p, lrows.data(), sizeof(i32) * s->nlong, cudaMemcpyHostToDevice,
+                             c->stream));
+  FVG_CUDA(cudaMemcpyAsync(s->long_piece0.p, lpiece0.data(), sizeof(i32) * (s->nlong + 1), cudaMemcpyHostToDevice,
+                           c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
   a.sched[slot] = std::move(s);
   return *a.sched[slot];
 }

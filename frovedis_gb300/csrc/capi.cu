@@ -56,6 +56,8 @@ FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out) {
     c->device = device;
     FVG_CUDA(cudaSetDevice(device));
     FVG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    FVG_CUDA(cudaMalloc(&c->dev_err, 256));
+    FVG_CUDA(cudaMemset(c->dev_err, 0, 256));
     FVG_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
     c->grid_spmv = c->num_sms * std::max(1, crs_blocks_per_sm());
     cudaMemPool_t pool;
@@ -99,6 +101,7 @@ FVG_API void fvg_ctx_destroy(fvg_ctx* c) {
   }
   c->matrices.clear();
   cudaStreamSynchronize(c->stream);
+  if (c->dev_err) cudaFree(c->dev_err);
   prof_destroy(c);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -278,8 +281,7 @@ static int64_t crs_bytes(const DevCRS& a) {
   int64_t b = (int64_t)a.off.bytes + (int64_t)a.idx.bytes;
   for (auto& v : a.val) b += (int64_t)v.bytes;
   for (auto& s : a.sched)
-    if (s) b += (int64_t)(s->rows.bytes + s->long_rows.bytes + s->long_chunk0.bytes + s->chunk_row.bytes +
-                          s->chunk_beg.bytes);
+    if (s) b += (int64_t)(s->items.bytes + s->long_rows.bytes + s->long_piece0.bytes);
   return b;
 }
 static int64_t jds_bytes(const DevJDS& j) {
@@ -477,6 +479,7 @@ static void run_product(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, int vec
   }
   stage_out_finish(c, v, y, ny, vec_dt, on_dev, out_dt);
   FVG_CUDA(cudaStreamSynchronize(c->stream));
+  check_device_error(c);
 }
 
 FVG_API fvg_status fvg_spmv(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
@@ -548,6 +551,7 @@ FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* lab
   API_BEGIN
   own(c, M);
   lbfgs_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
   API_END(c)
 }
 
@@ -558,6 +562,7 @@ FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* c, fvg_matrix* M, const double* label
   API_BEGIN
   own(c, M);
   sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
   API_END(c)
 }
 
@@ -569,6 +574,7 @@ FVG_API fvg_status fvg_logreg_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fv
   own(c, M);
   need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss);
+  check_device_error(c);
   API_END(c)
 }
 
@@ -587,6 +593,7 @@ FVG_API fvg_status fvg_logreg_predict_probability(fvg_ctx* c, fvg_matrix* M, con
   sigmoid_probability(c, y.as<double>(), M->A.m, intercept);
   if (M->A.m) FVG_CUDA(cudaMemcpyAsync(prob, y.p, sizeof(double) * M->A.m, cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));
+  check_device_error(c);
   API_END(c)
 }
 

@@ -60,32 +60,40 @@ struct DBuf {
 constexpr i64 kPad = 32;
 
 // ---------------------------------------------------------- CRS schedule
-// Row bins of the CRS kernel: bins 0..5 give a row 1,2,4,8,16,32 lanes, bin 6
-// a whole 256-thread CTA, bin 7 splits a row into chunks of kChunk elements
-// whose partial sums are combined in order by the finalize kernel.
-constexpr int kBins = 8;
+// The CRS kernel walks the matrix in row order as a list of warp work items
+// of at most `tile` nonzeros each:
+//  * a row tile: consecutive short rows (each <= tile nonzeros, at most
+//    kTileRows rows), and
+//  * a piece of a long row (> tile nonzeros): rows are split into pieces at
+//    8-element boundaries; the finalize kernel adds the pieces' partial sums
+//    in piece order.
+// An item's nonzeros are contiguous, so a warp reads them with coalesced
+// 16-byte vector loads.
 constexpr int kThreads = 256;
-constexpr i64 kChunk = 16384;       // elements per long-row chunk (multiple of 8)
-constexpr i64 kCtaRowMax = 16384;   // rows up to this length use one CTA
-struct Sched {
-  int ve = 0;                 // elements per lane vector this schedule targets
-  i64 item_start[kBins + 1];  // work items per bin (prefix)
-  i64 row_start[kBins + 1];   // rows per bin (prefix) into `rows`
-  DBuf rows;                  // int32 row ids grouped by bin, ascending in a bin
-  i64 nlong = 0, nchunks = 0;
-  DBuf long_rows;             // int32 row ids of bin 7
-  DBuf long_chunk0;           // int32 [nlong+1] first chunk of each long row
-  DBuf chunk_row;             // int32 [nchunks] row of each chunk
-  DBuf chunk_beg;             // int32 [nchunks] first element of each chunk
-  i64 items() const { return item_start[kBins]; }
+constexpr int kTileRows = 31;  // lanes 0..R of a warp hold a tile's R+1 row offsets
+struct Item {
+  int32_t r0;  // first row (tile) or the long row (piece)
+  int32_t r1;  // one past the last row (tile), or -1 - piece index (piece)
+  int32_t e0;  // first nonzero
+  int32_t e1;  // one past the last nonzero
 };
+struct Sched {
+  int tile = 0;                // nonzeros per item
+  i64 nitems = 0;
+  DBuf items;                  // Item[nitems] in row order
+  i64 nlong = 0, npieces = 0;
+  DBuf long_rows;              // int32 [nlong]
+  DBuf long_piece0;            // int32 [nlong+1] first piece of each long row
+};
+constexpr int kWarpTile = 512;  // nonzeros per warp item
+inline int tile_for_storage(int) { return kWarpTile; }
 
 // Device CRS matrix with up to three value planes.
 struct DevCRS {
   i64 m = 0, n = 0, nnz = 0;
   DBuf off, idx;  // int32
   DBuf val[3];    // indexed by fvg_dtype
-  std::unique_ptr<Sched> sched[2];  // [0]: 4-element vectors, [1]: 8-element
+  std::unique_ptr<Sched> sched[2];  // built once (slot 0)
   i64 max_row = 0;
 };
 
@@ -126,6 +134,9 @@ struct fvg_ctx {
   fvg::Profiler* prof = nullptr;  // owned; prof_create / prof_destroy
   // live matrices: destroying the context releases their device memory
   std::vector<fvg_matrix*> matrices;
+  // device error word: kernels set bits instead of trapping (bit 0: a bounded
+  // wait on a bulk copy gave up)
+  unsigned* dev_err = nullptr;
 };
 
 struct fvg_matrix {
@@ -157,6 +168,8 @@ struct ProfScope {
 };
 inline void count_launch(fvg_ctx* c, int n = 1) { c->launches += n; }
 void check_launch(const char* what);
+// Reads (and clears) the device error word; fails when a kernel reported one.
+void check_device_error(fvg_ctx* c);
 
 // ------------------------------------------------------------ utilities
 int dtype_size(int dt);
@@ -173,7 +186,7 @@ void crs_upload(fvg_ctx* c, DevCRS& a, i64 m, i64 n, const i32* off, const i32* 
                 bool on_device);
 void crs_ensure_plane(fvg_ctx* c, DevCRS& a, int dt, int master);
 void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master);
-const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int ve);
+const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile);
 void ell_build(fvg_ctx* c, const DevCRS& a, DevELL& e, int master);
 void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master);
 void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 threshold);
@@ -185,6 +198,8 @@ enum EpiKind { EPI_STORE = 0, EPI_LOGREG = 1 };
 struct LogregEpi {
   const double* label = nullptr;
   const double* sw = nullptr;       // nullptr: all ones
+  const float* label_f = nullptr;   // FP32 copies used by the FP32-arithmetic path
+  const float* sw_f = nullptr;
   const double* intercept = nullptr;  // device scalar
   int icpt = 0;
   void* r = nullptr;                // dloss*sw, dtype r_dt

@@ -376,7 +376,7 @@ struct Evaluator {
   const double* label = nullptr;
   const double* sw = nullptr;
   int icpt = 0;
-  DBuf r, z, s1, s2;
+  DBuf r, z, s1, s2, label_f, sw_f;
   void init(fvg_ctx* c_, Operand* op_, int storage_, const double* label_, const double* sw_, int icpt_) {
     c = c_;
     op = op_;
@@ -385,6 +385,13 @@ struct Evaluator {
     sw = sw_;
     icpt = icpt_;
     ensure_storage(c, *op, storage);
+    // FP32 copies of labels / weights for the FP32-arithmetic epilogue
+    label_f.alloc(sizeof(float) * std::max<i64>(op->m, 1), c->stream);
+    convert_values(c, label, FVG_F64, label_f.p, FVG_F32, op->m);
+    if (sw) {
+      sw_f.alloc(sizeof(float) * std::max<i64>(op->m, 1), c->stream);
+      convert_values(c, sw, FVG_F64, sw_f.p, FVG_F32, op->m);
+    }
     const int vdt = storage == FVG_F64 ? FVG_F64 : FVG_F32;
     r.alloc((size_t)dtype_size(vdt) * std::max<i64>(op->m, 1), c->stream);
     if (op->fmt != FVG_CRS) z.alloc((size_t)dtype_size(vdt) * std::max<i64>(op->m, 1), c->stream);
@@ -407,6 +414,8 @@ struct Evaluator {
     LogregEpi lr;
     lr.label = label;
     lr.sw = sw;
+    lr.label_f = label_f.as<float>();
+    lr.sw_f = sw ? sw_f.as<float>() : nullptr;
     lr.intercept = b;
     lr.icpt = icpt;
     lr.r = r.p;

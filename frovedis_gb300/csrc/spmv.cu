@@ -1,113 +1,68 @@
 // Sparse products on the device.
 //
-// CRS (crs_matrix_spmv_impl, crs_matrix.hpp:1505-1516): one persistent,
-// row-binned kernel.  Rows are grouped by length (row bins, see build.cu);
-// a row of bin b is read by 2^b lanes (b = 0..5), by a whole CTA (bin 6), or
-// split into fixed chunks whose partial sums the finalize kernel adds in
-// chunk order (bin 7).  Every lane streams 16-byte vectors of column ids and
-// values (4 elements for FP64/FP32 values, 8 for BF16) with no-L1-allocate
-// loads, and gathers x through the read-only path.  All reductions have a
-// fixed order, so results are deterministic run to run.
+// CRS (crs_matrix_spmv_impl, crs_matrix.hpp:1505-1516): one persistent
+// kernel walks the matrix in row order as work items of <= 2048 (FP64) or
+// 4096 (FP32/BF16) nonzeros.  An item is either a tile of consecutive short
+// rows (each row read by 1..32 lanes, chosen from the tile's row count) or a
+// piece of a long row (read by the whole CTA; the finalize kernel adds the
+// pieces in order).  The item's column ids and values are contiguous and are
+// staged in shared memory by two bulk TMA copies (cp.async.bulk with an
+// mbarrier, L2 evict-first), double buffered so the next item streams in while
+// the current one is computed; x is gathered through the read-only path.
+// All reductions have a fixed order, so results are deterministic run to run.
 //
 // The optional logistic epilogue fuses compute_wtx + logistic_gradient::
 // compute_dloss + `* sample_weight` + bias sum (gradient_descent.hpp:196-211,
 // gradient.hpp:15-53) into the same pass: it writes dloss*sw per row and
-// per-CTA compensated FP64 partial sums of the loss and of dloss*sw, which
-// the finalize kernel reduces in a fixed order.
+// per-CTA compensated partial sums of the loss and of dloss*sw (FP32 Kahan
+// sums on the FP32-arithmetic path, which keep GB300's narrow FP64 unit out of
+// the per-row work; FP64 Neumaier sums on the FP64 path), which the finalize
+// kernel reduces in FP64 in a fixed order.
 #include "fvg_internal.cuh"
 
 namespace fvg {
 
-// ---------------------------------------------------------------- loads
-__device__ __forceinline__ void ld_idx4(const i32* p, int& a, int& b, int& c, int& d) {
-  asm("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
-      : "=r"(a), "=r"(b), "=r"(c), "=r"(d)
-      : "l"(p));
+// --------------------------------------------------- TMA / mbarrier PTX
+__device__ __forceinline__ unsigned smem_u32(const void* ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void ld_f64x2(const double* p, double& a, double& b) {
-  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ void ld_f32x4(const float* p, float& a, float& b, float& c, float& d) {
-  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
-      : "=f"(a), "=f"(b), "=f"(c), "=f"(d)
-      : "l"(p));
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
 }
-__device__ __forceinline__ void ld_u32x4(const void* p, unsigned& a, unsigned& b, unsigned& c, unsigned& d) {
-  asm("ld.global.nc.L1::no_allocate.v4.b32 {%0,%1,%2,%3}, [%4];"
-      : "=r"(a), "=r"(b), "=r"(c), "=r"(d)
-      : "l"(p));
+// One bulk (non-tensor) TMA copy global -> shared, completing on `bar`;
+// both addresses 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
 }
-__device__ __forceinline__ float bf_lo(unsigned u) { return __uint_as_float(u << 16); }
-__device__ __forceinline__ float bf_hi(unsigned u) { return __uint_as_float(u & 0xffff0000u); }
-
-template <class VT> struct VecTraits;
-template <> struct VecTraits<double> { static constexpr int VE = 4; };
-template <> struct VecTraits<float> { static constexpr int VE = 4; };
-template <> struct VecTraits<bf16> { static constexpr int VE = 8; };
-
-// Loads vector v (VE elements) of column ids and values, converted to AT.
-template <class VT, class AT> struct VecLoad;
-template <> struct VecLoad<double, double> {
-  static __device__ __forceinline__ void load(const i32* idx, const double* val, i64 v, int* c, double* w) {
-    ld_idx4(idx + 4 * v, c[0], c[1], c[2], c[3]);
-    ld_f64x2(val + 4 * v, w[0], w[1]);
-    ld_f64x2(val + 4 * v + 2, w[2], w[3]);
-  }
-};
-template <> struct VecLoad<float, float> {
-  static __device__ __forceinline__ void load(const i32* idx, const float* val, i64 v, int* c, float* w) {
-    ld_idx4(idx + 4 * v, c[0], c[1], c[2], c[3]);
-    ld_f32x4(val + 4 * v, w[0], w[1], w[2], w[3]);
-  }
-};
-template <> struct VecLoad<bf16, float> {
-  static __device__ __forceinline__ void load(const i32* idx, const bf16* val, i64 v, int* c, float* w) {
-    ld_idx4(idx + 8 * v, c[0], c[1], c[2], c[3]);
-    ld_idx4(idx + 8 * v + 4, c[4], c[5], c[6], c[7]);
-    unsigned u0, u1, u2, u3;
-    ld_u32x4(val + 8 * v, u0, u1, u2, u3);
-    w[0] = bf_lo(u0); w[1] = bf_hi(u0); w[2] = bf_lo(u1); w[3] = bf_hi(u1);
-    w[4] = bf_lo(u2); w[5] = bf_hi(u2); w[6] = bf_lo(u3); w[7] = bf_hi(u3);
-  }
-};
-
-template <class XT> __device__ __forceinline__ XT ldx(const XT* x, int c) { return __ldg(x + c); }
-
-// acc += Σ val*x over the elements of vector v that lie in [s, e)
-template <class VT, class XT, class AT>
-__device__ __forceinline__ void vec_accum(const i32* __restrict__ idx, const VT* __restrict__ val,
-                                          const XT* __restrict__ x, i64 v, i64 s, i64 e, AT& acc) {
-  constexpr int VE = VecTraits<VT>::VE;
-  int c[VE];
-  AT w[VE];
-  VecLoad<VT, AT>::load(idx, val, v, c, w);
-  const i64 base = v * VE;
-  if (base >= s && base + VE <= e) {
-#pragma unroll
-    for (int j = 0; j < VE; j++) acc += w[j] * (AT)ldx(x, c[j]);
-  } else {
-#pragma unroll
-    for (int j = 0; j < VE; j++)
-      if (base + j >= s && base + j < e) acc += w[j] * (AT)ldx(x, c[j]);
-  }
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
 }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-// Partial dot product of elements [s, e) handled by `lane` of an L-lane group.
-template <int L, class VT, class XT, class AT>
-__device__ __forceinline__ AT range_partial(const i32* __restrict__ idx, const VT* __restrict__ val,
-                                            const XT* __restrict__ x, i64 s, i64 e, int lane) {
-  constexpr int VE = VecTraits<VT>::VE;
-  AT a0 = 0, a1 = 0;
-  if (e > s) {
-    const i64 v1 = (e - 1) / VE + 1;
-    i64 v = s / VE + lane;
-    for (; v + L < v1; v += 2 * L) {
-      vec_accum<VT, XT, AT>(idx, val, x, v, s, e, a0);
-      vec_accum<VT, XT, AT>(idx, val, x, v + L, s, e, a1);
-    }
-    if (v < v1) vec_accum<VT, XT, AT>(idx, val, x, v, s, e, a0);
-  }
-  return a0 + a1;
+// Bounded wait: gives up after ~2^22 polls (far beyond any normal copy time)
+// and reports it through *err; never spins forever.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err) {
+  for (unsigned it = 0; it < (1u << 22); it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicOr(err, 1u);
+  return false;
 }
 
 template <class T> __device__ __forceinline__ T block_sum256(T v) {
@@ -127,9 +82,9 @@ template <class T> __device__ __forceinline__ T block_sum256(T v) {
 }
 
 // ---------------------------------------------------- compensated sums
-struct CSum {
+struct CSum {  // Neumaier, FP64 (the FP64 path)
   double s = 0.0, c = 0.0;
-  __device__ __forceinline__ void add(double v) {  // Neumaier
+  __device__ __forceinline__ void add(double v) {
     double t = s + v;
     if (fabs(s) >= fabs(v)) c += (s - t) + v;
     else c += (v - t) + s;
@@ -137,13 +92,25 @@ struct CSum {
   }
   __device__ __forceinline__ double total() const { return s + c; }
 };
+struct FSum {  // Kahan in FP32 (the FP32-arithmetic path keeps the FP64 unit idle)
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double total() const { return (double)s - (double)c; }
+};
+template <class AT> struct SumOf { using type = CSum; };
+template <> struct SumOf<float> { using type = FSum; };
 
 // Fixed-order block reduction of two compensated sums (256 threads).
-__device__ __forceinline__ void block_csum2(CSum a, CSum b, double* out_a, double* out_b) {
+__device__ __forceinline__ void block_csum2(double a, double b, double* out_a, double* out_b) {
   __shared__ double ra[256], rb[256];
   __syncthreads();
-  ra[threadIdx.x] = a.total();
-  rb[threadIdx.x] = b.total();
+  ra[threadIdx.x] = a;
+  rb[threadIdx.x] = b;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
     if (threadIdx.x < st) {
@@ -179,23 +146,30 @@ __device__ __forceinline__ void logistic_row(double wtx, double lab, double& los
 }
 // FP32 variant for the BF16/FP32-storage path (log1p form keeps small
 // losses that log(1+e) would round away in single precision).
-__device__ __forceinline__ void logistic_row(float wtx, double lab, double& loss, float& d) {
-  float z = (float)lab * wtx;
-  float neg = -(float)lab;
+__device__ __forceinline__ void logistic_row(float wtx, float lab, float& loss, float& d) {
+  float z = lab * wtx;
+  float neg = -lab;
   if (z > 18.0f) {
     float e = expf(-z);
-    loss = (double)e;
+    loss = e;
     d = e * neg;
   } else if (z < -18.0f) {
-    loss = (double)-z;
+    loss = -z;
     d = neg;
   } else {
-    loss = (double)log1pf(expf(-z));
+    loss = log1pf(expf(-z));
     d = neg / (1.0f + expf(z));
   }
   if (d > 1e12f) d = 1e12f;
   else if (d < -1e12f) d = -1e12f;
 }
+
+template <class VT> __device__ __forceinline__ float to_f(VT v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<bf16>(bf16 v) { return __bfloat162float(v); }
+
+template <class VT, class AT> __device__ __forceinline__ AT to_acc(VT v) { return (AT)to_f<VT>(v); }
+template <> __device__ __forceinline__ double to_acc<double, double>(double v) { return v; }
 
 // ------------------------------------------------------------ kernel args
 struct CrsK {
@@ -203,105 +177,180 @@ struct CrsK {
   const i32* idx;
   const void* val;
   const void* x;
-  const i32* rows;
-  const i32* chunk_row;
-  const i32* chunk_beg;
-  i64 item_start[kBins + 1];
-  i64 row_start[kBins + 1];
+  const Item* items;
+  i64 nitems;
+  int tile;
   void* y;
   void* partials;
   // logistic epilogue
   const double* label;
   const double* sw;
+  const float* label_f;
+  const float* sw_f;
   const double* intercept;
   int icpt;
   void* r;
   double* cta_part;
+  unsigned* err;
 };
 
-template <class AT, class YT, int EPI>
-__device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, CSum& ls, CSum& bs) {
+template <class AT, class YT, int EPI, class S>
+__device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, S& ls, S& bs) {
   if (EPI == EPI_STORE) {
     ((YT*)p.y)[row] = (YT)acc;
   } else {
     AT wtx = acc + b;
-    double lab = p.label[row];
-    double loss;
-    AT d;
-    logistic_row(wtx, lab, loss, d);
-    if (p.sw) d = (AT)(d * (AT)p.sw[row]);
+    AT loss, d;
+    if constexpr (sizeof(AT) == 8) {
+      logistic_row(wtx, p.label[row], loss, d);
+      if (p.sw) d = d * p.sw[row];
+    } else {
+      logistic_row(wtx, p.label_f[row], loss, d);
+      if (p.sw_f) d = d * p.sw_f[row];
+    }
     ((YT*)p.r)[row] = (YT)d;
     ls.add(loss);
-    bs.add((double)d);
+    bs.add(d);
   }
 }
 
-template <int LOG2L, class VT, class XT, class AT, class YT, int EPI>
-__device__ __forceinline__ void do_lane_rows(const CrsK& p, int bin, i64 item, AT b, CSum& ls, CSum& bs) {
-  constexpr int L = 1 << LOG2L;
-  constexpr int RPI = kThreads / L;
-  const int sub = threadIdx.x / L, lane = threadIdx.x % L;
-  const i64 ri = (item - p.item_start[bin]) * RPI + sub;
-  const bool has = ri < p.row_start[bin + 1] - p.row_start[bin];
-  i32 row = has ? p.rows[p.row_start[bin] + ri] : 0;
-  i64 s = has ? p.off[row] : 0, e = has ? p.off[row + 1] : 0;
-  AT acc = range_partial<L, VT, XT, AT>(p.idx, (const VT*)p.val, (const XT*)p.x, s, e, lane);
-#pragma unroll
-  for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (has && lane == 0) epilogue<AT, YT, EPI>(p, row, acc, b, ls, bs);
+// ------------------------------------------------------------ warp tiles
+// Vector loads of VE column ids / values (16-byte transactions).
+__device__ __forceinline__ void ld_idx4(const i32* q, int* c) {
+  int4 v = __ldcs(reinterpret_cast<const int4*>(q));
+  c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
 }
+template <class VT> struct Vec;
+template <> struct Vec<double> {
+  static constexpr int VE = 4;
+  static __device__ __forceinline__ void load(const i32* idx, const double* val, int* c, double* w) {
+    ld_idx4(idx, c);
+    double2 a = __ldcs(reinterpret_cast<const double2*>(val));
+    double2 b = __ldcs(reinterpret_cast<const double2*>(val) + 1);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+  }
+};
+template <> struct Vec<float> {
+  static constexpr int VE = 4;
+  static __device__ __forceinline__ void load(const i32* idx, const float* val, int* c, float* w) {
+    ld_idx4(idx, c);
+    float4 a = __ldcs(reinterpret_cast<const float4*>(val));
+    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+  }
+};
+template <> struct Vec<bf16> {
+  static constexpr int VE = 8;
+  static __device__ __forceinline__ void load(const i32* idx, const bf16* val, int* c, float* w) {
+    ld_idx4(idx, c);
+    ld_idx4(idx + 4, c + 4);
+    uint4 u = __ldcs(reinterpret_cast<const uint4*>(val));
+    w[0] = __uint_as_float(u.x << 16); w[1] = __uint_as_float(u.x & 0xffff0000u);
+    w[2] = __uint_as_float(u.y << 16); w[3] = __uint_as_float(u.y & 0xffff0000u);
+    w[4] = __uint_as_float(u.z << 16); w[5] = __uint_as_float(u.z & 0xffff0000u);
+    w[6] = __uint_as_float(u.w << 16); w[7] = __uint_as_float(u.w & 0xffff0000u);
+  }
+};
 
+// Persistent CRS kernel.  Warp g of the grid handles items g, g+W, g+2W, ...
+// (W = warps in the grid).  Phase 1: the warp streams the item's nonzeros
+// with 16-byte loads (all issued before any use), gathers x and writes the
+// products to its own shared-memory slice.  Phase 2: rows of a tile are
+// summed from shared memory by 1..32 lanes each (32 / rows, rounded to a
+// power of two), the lanes of a row combined by shuffles; a piece is summed
+// by the whole warp.  No CTA-wide barrier inside the loop.
 template <class VT, class XT, class AT, class YT, int EPI>
-__global__ void __launch_bounds__(kThreads) k_crs(const CrsK p) {
-  CSum ls, bs;
-  const AT b = (EPI == EPI_LOGREG && p.icpt) ? (AT)*p.intercept : (AT)0;
-  const i64 total = p.item_start[kBins];
-  int bin = 0;
-  for (i64 item = blockIdx.x; item < total; item += gridDim.x) {
-    while (item >= p.item_start[bin + 1]) bin++;
-    switch (bin) {
-      case 0: do_lane_rows<0, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 1: do_lane_rows<1, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 2: do_lane_rows<2, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 3: do_lane_rows<3, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 4: do_lane_rows<4, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 5: do_lane_rows<5, VT, XT, AT, YT, EPI>(p, bin, item, b, ls, bs); break;
-      case 6: {
-        i32 row = p.rows[p.row_start[6] + (item - p.item_start[6])];
-        AT acc = range_partial<kThreads, VT, XT, AT>(p.idx, (const VT*)p.val, (const XT*)p.x, p.off[row],
-                                                     p.off[row + 1], threadIdx.x);
-        acc = block_sum256(acc);
-        if (threadIdx.x == 0) epilogue<AT, YT, EPI>(p, row, acc, b, ls, bs);
-        break;
+__global__ void __launch_bounds__(kThreads, 3) k_crs(const CrsK p) {
+  constexpr int VE = Vec<VT>::VE;
+  constexpr int SPAN = kWarpTile + 16;              // products slice per warp
+  constexpr int NV = (SPAN + 32 * VE - 1) / (32 * VE);  // vector rounds per lane
+  constexpr int NG = sizeof(VT) == 8 ? 2 : NV;           // rounds in flight at once
+  __shared__ AT sprod[kThreads / 32][SPAN];
+  using Sum = typename SumOf<AT>::type;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  AT* prod = sprod[w];
+  const i64 W = (i64)gridDim.x * (kThreads / 32);
+  const i64 n = p.nitems;
+  const XT* __restrict__ x = (const XT*)p.x;
+  const VT* __restrict__ val = (const VT*)p.val;
+  Sum ls, bs;
+  const AT bias = (EPI == EPI_LOGREG && p.icpt) ? (AT)*p.intercept : (AT)0;
+  i64 t = (i64)blockIdx.x * (kThreads / 32) + w;
+  Item nx = (t < n) ? p.items[t] : Item{0, 0, 0, 0};
+  for (; t < n; t += W) {
+    const Item it = nx;
+    if (t + W < n) nx = p.items[t + W];  // prefetch the next descriptor
+    const int a0 = it.e0 & ~(VE - 1);
+    const int span = it.e1 - a0;
+    // row boundaries of a tile, one per lane
+    int myoff = 0;
+    if (it.r1 >= 0 && lane <= it.r1 - it.r0) myoff = __ldg(p.off + it.r0 + lane);
+    // phase 1: loads, gathers, products, NG vector rounds at a time (all of
+    // a group's loads are issued before its gathers)
+#pragma unroll
+    for (int g = 0; g < NV; g += NG) {
+      int c[NG][VE];
+      AT v[NG][VE];
+#pragma unroll
+      for (int q = 0; q < NG; q++) {
+        const int k = ((g + q) * 32 + lane) * VE;
+        if (g + q < NV && k < span) Vec<VT>::load(p.idx + a0 + k, val + a0 + k, c[q], v[q]);
       }
-      default: {
-        i64 ci = item - p.item_start[7];
-        i32 row = p.chunk_row[ci];
-        i64 beg = p.chunk_beg[ci];
-        i64 end = (beg & ~7ll) + kChunk;
-        i64 re = p.off[row + 1];
-        if (end > re) end = re;
-        AT acc = range_partial<kThreads, VT, XT, AT>(p.idx, (const VT*)p.val, (const XT*)p.x, beg, end,
-                                                     threadIdx.x);
-        acc = block_sum256(acc);
-        if (threadIdx.x == 0) ((AT*)p.partials)[ci] = acc;
-        break;
+#pragma unroll
+      for (int q = 0; q < NG; q++) {
+        const int k = ((g + q) * 32 + lane) * VE;
+        if (g + q < NV && k < span) {
+#pragma unroll
+          for (int j = 0; j < VE; j++) {
+            const int e = a0 + k + j;
+            AT pr = 0;
+            if (e >= it.e0 && e < it.e1) pr = v[q][j] * (AT)__ldg(x + c[q][j]);
+            prod[k + j] = pr;
+          }
+        }
       }
     }
+    __syncwarp();
+    // phase 2
+    if (it.r1 >= 0) {
+      const int R = it.r1 - it.r0;
+      int Gl = 32;
+      if (R > 1) {
+        int p2 = 2;
+        while (p2 < R) p2 <<= 1;
+        Gl = 32 / p2;
+      }
+      const int j = lane / Gl, sub = lane % Gl;
+      const int s = __shfl_sync(0xffffffffu, myoff, j & 31) - a0;
+      const int e = __shfl_sync(0xffffffffu, myoff, (j + 1) & 31) - a0;
+      AT acc = 0;
+      if (j < R)
+        for (int k = s + sub; k < e; k += Gl) acc += prod[k];
+      for (int o = Gl >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (j < R && sub == 0) epilogue<AT, YT, EPI>(p, it.r0 + j, acc, bias, ls, bs);
+    } else {
+      AT acc = 0;
+      for (int k = it.e0 - a0 + lane; k < span; k += 32) acc += prod[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) ((AT*)p.partials)[-1 - it.r1] = acc;
+    }
+    __syncwarp();
   }
-  if (EPI == EPI_LOGREG) block_csum2(ls, bs, &p.cta_part[2 * blockIdx.x], &p.cta_part[2 * blockIdx.x + 1]);
+  if (EPI == EPI_LOGREG) block_csum2(ls.total(), bs.total(), &p.cta_part[2 * blockIdx.x], &p.cta_part[2 * blockIdx.x + 1]);
 }
 
 // ------------------------------------------------------------- finalize
 struct FinK {
   const i32* long_rows;
-  const i32* long_chunk0;
+  const i32* long_piece0;
   i64 nlong;
   const void* partials;
   void* y;
   // logistic
   const double* label;
   const double* sw;
+  const float* label_f;
+  const float* sw_f;
   const double* intercept;
   int icpt;
   void* r;
@@ -313,11 +362,14 @@ struct FinK {
   unsigned* ticket;
 };
 
+// Long rows: sum the pieces' partials in piece order and apply the
+// epilogue; then (logistic) the last CTA reduces every partial loss / bias
+// in a fixed order.
 template <class AT, class YT, int EPI>
 __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
   const AT b = (EPI == EPI_LOGREG && f.icpt) ? (AT)*f.intercept : (AT)0;
   for (i64 i = blockIdx.x; i < f.nlong; i += gridDim.x) {
-    i64 c0 = f.long_chunk0[i], c1 = f.long_chunk0[i + 1];
+    i64 c0 = f.long_piece0[i], c1 = f.long_piece0[i + 1];
     AT acc = 0;
     for (i64 j = c0 + threadIdx.x; j < c1; j += kThreads) acc += ((const AT*)f.partials)[j];
     acc = block_sum256(acc);
@@ -326,12 +378,16 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
       if (EPI == EPI_STORE) {
         ((YT*)f.y)[row] = (YT)acc;
       } else {
-        double loss;
-        AT d;
-        logistic_row((AT)(acc + b), f.label[row], loss, d);
-        if (f.sw) d = (AT)(d * (AT)f.sw[row]);
+        AT loss, d, wtx = acc + b;
+        if constexpr (sizeof(AT) == 8) {
+          logistic_row(wtx, f.label[row], loss, d);
+          if (f.sw) d = d * f.sw[row];
+        } else {
+          logistic_row(wtx, f.label_f[row], loss, d);
+          if (f.sw_f) d = d * f.sw_f[row];
+        }
         ((YT*)f.r)[row] = (YT)d;
-        f.long_part[2 * i] = loss;
+        f.long_part[2 * i] = (double)loss;
         f.long_part[2 * i + 1] = (double)d;
       }
     }
@@ -354,7 +410,7 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
     bs.add(__ldcg(&f.long_part[2 * i + 1]));
   }
   double tl = 0, tb = 0;
-  block_csum2(ls, bs, &tl, &tb);
+  block_csum2(ls.total(), bs.total(), &tl, &tb);
   if (threadIdx.x == 0) {
     f.out[0] = tl;
     f.out[1] = f.icpt ? tb : 0.0;
@@ -381,7 +437,7 @@ static size_t carve(char* base, const Sched& s, int grid, size_t at_size, PassSc
   char* out = take(sizeof(double) * 2);
   char* cp = take(sizeof(double) * 2 * (size_t)grid);
   char* lp = take(sizeof(double) * 2 * (size_t)std::max<i64>(s.nlong, 1));
-  char* pa = take(at_size * (size_t)std::max<i64>(s.nchunks, 1));
+  char* pa = take(at_size * (size_t)std::max<i64>(s.npieces, 1));
   if (ps) {
     ps->ticket = (unsigned*)t;
     ps->out = (double*)out;
@@ -393,34 +449,49 @@ static size_t carve(char* base, const Sched& s, int grid, size_t at_size, PassSc
 }
 
 i64 crs_pass_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage) {
-  const Sched& s = crs_sched(c, a, storage == FVG_BF16 ? 8 : 4);
+  // pieces depend only on the item size, which FP32 and BF16 share
+  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
   return (i64)carve(nullptr, s, c->grid_spmv, 8, nullptr);
 }
 
 template <class VT, class XT, class AT, class YT, int EPI>
+static int crs_grid(fvg_ctx* c, int tile) {
+  static int blocks = -1;
+  auto kfn = k_crs<VT, XT, AT, YT, EPI>;
+  (void)tile;
+  if (blocks < 0) {
+    int nb = 0;
+    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, kThreads, 0));
+    blocks = std::max(1, nb);
+  }
+  return blocks * c->num_sms;
+}
+
+template <class VT, class XT, class AT, class YT, int EPI>
 static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const void* x, void* y,
-                       const LogregEpi* lr, const PassScratch& ps, int grid) {
+                       const LogregEpi* lr, const PassScratch& ps) {
   CrsK p;
   p.off = a.off.as<i32>();
   p.idx = a.idx.as<i32>();
   p.val = a.val[storage].p;
   p.x = x;
-  p.rows = s.rows.as<i32>();
-  p.chunk_row = s.chunk_row.as<i32>();
-  p.chunk_beg = s.chunk_beg.as<i32>();
-  for (int b = 0; b <= kBins; b++) {
-    p.item_start[b] = s.item_start[b];
-    p.row_start[b] = s.row_start[b];
-  }
+  p.items = s.items.as<Item>();
+  p.nitems = s.nitems;
+  p.tile = s.tile;
   p.y = y;
   p.partials = ps.partials;
   p.label = lr ? lr->label : nullptr;
   p.sw = lr ? lr->sw : nullptr;
+  p.label_f = lr ? lr->label_f : nullptr;
+  p.sw_f = lr ? lr->sw_f : nullptr;
   p.intercept = lr ? lr->intercept : nullptr;
   p.icpt = lr ? lr->icpt : 0;
   p.r = lr ? lr->r : nullptr;
   p.cta_part = ps.cta_part;
-  if (s.items() > 0) {
+  p.err = c->dev_err;
+  int grid = (int)std::max<i64>(1, std::min<i64>(crs_grid<VT, XT, AT, YT, EPI>(c, s.tile), s.nitems));
+  grid = std::min(grid, c->grid_spmv);
+  if (s.nitems > 0) {
     k_crs<VT, XT, AT, YT, EPI><<<grid, kThreads, 0, c->stream>>>(p);
     check_launch("k_crs");
     count_launch(c);
@@ -428,17 +499,19 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
   if (s.nlong > 0 || EPI == EPI_LOGREG) {
     FinK f;
     f.long_rows = s.long_rows.as<i32>();
-    f.long_chunk0 = s.long_chunk0.as<i32>();
+    f.long_piece0 = s.long_piece0.as<i32>();
     f.nlong = s.nlong;
     f.partials = ps.partials;
     f.y = y;
     f.label = p.label;
     f.sw = p.sw;
+    f.label_f = p.label_f;
+    f.sw_f = p.sw_f;
     f.intercept = p.intercept;
     f.icpt = p.icpt;
     f.r = p.r;
     f.cta_part = ps.cta_part;
-    f.ncta = s.items() > 0 ? grid : 0;
+    f.ncta = s.nitems > 0 ? grid : 0;
     f.long_part = ps.long_part;
     f.out = (lr && lr->out) ? lr->out : ps.out;
     f.grad_bias = lr ? lr->grad_bias : nullptr;
@@ -453,10 +526,8 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
 
 void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y_dt, void* y, int epi,
               const LogregEpi* lr, void* scratch, int prof_key) {
-  const int ve = storage == FVG_BF16 ? 8 : 4;
-  const Sched& s = crs_sched(c, a, ve);
+  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
   if (!a.val[storage].p) fail(FVG_ERR_INTERNAL, "missing value plane for the requested storage");
-  int grid = (int)std::max<i64>(1, std::min<i64>(c->grid_spmv, s.items()));
   const size_t at_size = (storage == FVG_F64) ? 8 : 4;
   DBuf tmp;
   PassScratch ps;
@@ -467,28 +538,30 @@ void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y
     scratch = tmp.p;
   }
   carve((char*)scratch, s, c->grid_spmv, at_size, &ps);
+  if (epi == EPI_LOGREG && storage != FVG_F64 && !(lr && lr->label_f))
+    fail(FVG_ERR_INTERNAL, "FP32 logistic pass needs FP32 labels");
   ProfScope pr(c, prof_key);
   const int out_dt = (epi == EPI_LOGREG) ? (lr ? lr->r_dt : y_dt) : y_dt;
   if (storage == FVG_F64) {
     if (x_dt != FVG_F64 || out_dt != FVG_F64) fail(FVG_ERR_INVALID_ARG, "FP64 values need FP64 vectors");
-    if (epi == EPI_STORE) launch_crs<double, double, double, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps, grid);
-    else launch_crs<double, double, double, double, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps, grid);
+    if (epi == EPI_STORE) launch_crs<double, double, double, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps);
+    else launch_crs<double, double, double, double, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps);
   } else if (storage == FVG_F32) {
     if (x_dt != FVG_F32) fail(FVG_ERR_INVALID_ARG, "FP32 values need FP32 input vectors");
     if (epi == EPI_STORE && out_dt == FVG_F64)
-      launch_crs<float, float, float, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<float, float, float, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps);
     else if (epi == EPI_STORE)
-      launch_crs<float, float, float, float, EPI_STORE>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<float, float, float, float, EPI_STORE>(c, a, s, storage, x, y, lr, ps);
     else
-      launch_crs<float, float, float, float, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<float, float, float, float, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps);
   } else {
     if (x_dt != FVG_F32) fail(FVG_ERR_INVALID_ARG, "BF16 values need FP32 input vectors");
     if (epi == EPI_STORE && out_dt == FVG_F64)
-      launch_crs<bf16, float, float, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<bf16, float, float, double, EPI_STORE>(c, a, s, storage, x, y, lr, ps);
     else if (epi == EPI_STORE)
-      launch_crs<bf16, float, float, float, EPI_STORE>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<bf16, float, float, float, EPI_STORE>(c, a, s, storage, x, y, lr, ps);
     else
-      launch_crs<bf16, float, float, float, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps, grid);
+      launch_crs<bf16, float, float, float, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps);
   }
 }
 
@@ -685,13 +758,9 @@ void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k
 
 // Resident CTAs per SM of the heaviest CRS instantiation (sizes the
 // persistent grid).
-int crs_blocks_per_sm() {
-  int a = 0, b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_crs<double, double, double, double, EPI_LOGREG>, kThreads, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_crs<bf16, float, float, float, EPI_LOGREG>, kThreads, 0);
-  int r = std::min(a > 0 ? a : 8, b > 0 ? b : 8);
-  return r < 1 ? 1 : r;
-}
+// Upper bound of resident 256-thread CTAs per SM; sizes the per-CTA partial
+// buffers (the launch itself uses the occupancy of each instantiation).
+int crs_blocks_per_sm() { return 2048 / kThreads; }
 
 // logistic_regression_model<T>::predict_probability (ml/glm/linear_model.hpp:
 // 376-392): v += intercept (when non-zero); exp argument above 709 → 0.
@@ -716,11 +785,11 @@ void sigmoid_probability(fvg_ctx* c, double* v, i64 m, double b) {
 // logistic epilogue to z = A w already in memory.
 template <class AT>
 __global__ void __launch_bounds__(256) k_logreg_rows(const AT* __restrict__ wtx, i64 m, const CrsK p) {
-  CSum ls, bs;
+  typename SumOf<AT>::type ls, bs;
   const AT b = p.icpt ? (AT)*p.intercept : (AT)0;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (i64)gridDim.x * blockDim.x)
     epilogue<AT, AT, EPI_LOGREG>(p, (i32)r, wtx[r], b, ls, bs);
-  block_csum2(ls, bs, &p.cta_part[2 * blockIdx.x], &p.cta_part[2 * blockIdx.x + 1]);
+  block_csum2(ls.total(), bs.total(), &p.cta_part[2 * blockIdx.x], &p.cta_part[2 * blockIdx.x + 1]);
 }
 
 void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi& lr) {
@@ -735,6 +804,8 @@ void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi
   CrsK p = {};
   p.label = lr.label;
   p.sw = lr.sw;
+  p.label_f = lr.label_f;
+  p.sw_f = lr.sw_f;
   p.intercept = lr.intercept;
   p.icpt = lr.icpt;
   p.r = lr.r;
@@ -747,6 +818,8 @@ void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi
   f.nlong = 0;
   f.label = lr.label;
   f.sw = lr.sw;
+  f.label_f = lr.label_f;
+  f.sw_f = lr.sw_f;
   f.intercept = lr.intercept;
   f.icpt = lr.icpt;
   f.r = lr.r;

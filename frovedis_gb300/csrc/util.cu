@@ -17,6 +17,16 @@ void check_launch(const char* what) {
   if (e != cudaSuccess) throw_cuda(e, what, __FILE__, __LINE__);
 }
 
+void check_device_error(fvg_ctx* c) {
+  unsigned h = 0;
+  FVG_CUDA(cudaMemcpyAsync(&h, c->dev_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  if (h) {
+    FVG_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(unsigned), c->stream));
+    fail(FVG_ERR_INTERNAL, "a device-side bounded wait gave up (bulk copy did not complete); results are invalid");
+  }
+}
+
 void DBuf::alloc(size_t nbytes, cudaStream_t s) {
   release();
   stream = s;
