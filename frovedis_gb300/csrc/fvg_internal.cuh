@@ -85,7 +85,19 @@ struct Sched {
   DBuf long_rows;              // int32 [nlong]
   DBuf long_piece0;            // int32 [nlong+1] first piece of each long row
 };
-constexpr int kWarpTile = 512;  // nonzeros per warp item
+// Tuning knobs of the CRS kernel (compile-time; defaults from measurements
+// on GB300): nonzeros per warp item, resident CTAs per SM the register
+// budget targets, element rounds whose loads are issued together.
+#ifndef FVG_WARP_TILE
+#define FVG_WARP_TILE 512
+#endif
+#ifndef FVG_CRS_MIN_BLOCKS
+#define FVG_CRS_MIN_BLOCKS 4
+#endif
+#ifndef FVG_CRS_ROUNDS
+#define FVG_CRS_ROUNDS 8
+#endif
+constexpr int kWarpTile = FVG_WARP_TILE;  // nonzeros per warp item
 inline int tile_for_storage(int) { return kWarpTile; }
 
 // Device CRS matrix with up to three value planes.

@@ -215,55 +215,27 @@ __device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, S
 }
 
 // ------------------------------------------------------------ warp tiles
-// Vector loads of VE column ids / values (16-byte transactions).
-__device__ __forceinline__ void ld_idx4(const i32* q, int* c) {
-  int4 v = __ldcs(reinterpret_cast<const int4*>(q));
-  c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+// Streaming (evict-first) load of one value, widened to the accumulator.
+template <class VT, class AT> __device__ __forceinline__ AT ld_val(const VT* q);
+template <> __device__ __forceinline__ double ld_val<double, double>(const double* q) { return __ldcs(q); }
+template <> __device__ __forceinline__ float ld_val<float, float>(const float* q) { return __ldcs(q); }
+template <> __device__ __forceinline__ float ld_val<bf16, float>(const bf16* q) {
+  return __uint_as_float((unsigned)__ldcs(reinterpret_cast<const unsigned short*>(q)) << 16);
 }
-template <class VT> struct Vec;
-template <> struct Vec<double> {
-  static constexpr int VE = 4;
-  static __device__ __forceinline__ void load(const i32* idx, const double* val, int* c, double* w) {
-    ld_idx4(idx, c);
-    double2 a = __ldcs(reinterpret_cast<const double2*>(val));
-    double2 b = __ldcs(reinterpret_cast<const double2*>(val) + 1);
-    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
-  }
-};
-template <> struct Vec<float> {
-  static constexpr int VE = 4;
-  static __device__ __forceinline__ void load(const i32* idx, const float* val, int* c, float* w) {
-    ld_idx4(idx, c);
-    float4 a = __ldcs(reinterpret_cast<const float4*>(val));
-    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
-  }
-};
-template <> struct Vec<bf16> {
-  static constexpr int VE = 8;
-  static __device__ __forceinline__ void load(const i32* idx, const bf16* val, int* c, float* w) {
-    ld_idx4(idx, c);
-    ld_idx4(idx + 4, c + 4);
-    uint4 u = __ldcs(reinterpret_cast<const uint4*>(val));
-    w[0] = __uint_as_float(u.x << 16); w[1] = __uint_as_float(u.x & 0xffff0000u);
-    w[2] = __uint_as_float(u.y << 16); w[3] = __uint_as_float(u.y & 0xffff0000u);
-    w[4] = __uint_as_float(u.z << 16); w[5] = __uint_as_float(u.z & 0xffff0000u);
-    w[6] = __uint_as_float(u.w << 16); w[7] = __uint_as_float(u.w & 0xffff0000u);
-  }
-};
 
 // Persistent CRS kernel.  Warp g of the grid handles items g, g+W, g+2W, ...
 // (W = warps in the grid).  Phase 1: the warp streams the item's nonzeros
-// with 16-byte loads (all issued before any use), gathers x and writes the
-// products to its own shared-memory slice.  Phase 2: rows of a tile are
+// with coalesced loads (lane L: nonzeros L, L+32, ...; a group of rounds
+// issued before any use), gathers x and writes the products to its own
+// shared-memory slice.  Phase 2: rows of a tile are
 // summed from shared memory by 1..32 lanes each (32 / rows, rounded to a
 // power of two), the lanes of a row combined by shuffles; a piece is summed
 // by the whole warp.  No CTA-wide barrier inside the loop.
 template <class VT, class XT, class AT, class YT, int EPI>
-__global__ void __launch_bounds__(kThreads, 3) k_crs(const CrsK p) {
-  constexpr int VE = Vec<VT>::VE;
-  constexpr int SPAN = kWarpTile + 16;              // products slice per warp
-  constexpr int NV = (SPAN + 32 * VE - 1) / (32 * VE);  // vector rounds per lane
-  constexpr int NG = sizeof(VT) == 8 ? 2 : NV;           // rounds in flight at once
+__global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK p) {
+  constexpr int SPAN = kWarpTile;        // products slice per warp
+  constexpr int NR = SPAN / 32;          // element rounds per lane
+  constexpr int RG = sizeof(VT) == 8 ? (FVG_CRS_ROUNDS + 1) / 2 : FVG_CRS_ROUNDS;  // rounds in flight together
   __shared__ AT sprod[kThreads / 32][SPAN];
   using Sum = typename SumOf<AT>::type;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -279,34 +251,30 @@ __global__ void __launch_bounds__(kThreads, 3) k_crs(const CrsK p) {
   for (; t < n; t += W) {
     const Item it = nx;
     if (t + W < n) nx = p.items[t + W];  // prefetch the next descriptor
-    const int a0 = it.e0 & ~(VE - 1);
+    const int a0 = it.e0;
     const int span = it.e1 - a0;
     // row boundaries of a tile, one per lane
     int myoff = 0;
     if (it.r1 >= 0 && lane <= it.r1 - it.r0) myoff = __ldg(p.off + it.r0 + lane);
-    // phase 1: loads, gathers, products, NG vector rounds at a time (all of
-    // a group's loads are issued before its gathers)
+    // phase 1: lane L takes nonzeros L, L+32, ... so one gather instruction
+    // covers 32 consecutive nonzeros (neighbouring columns / rows share
+    // sectors); RG rounds of loads are issued before their gathers.
 #pragma unroll
-    for (int g = 0; g < NV; g += NG) {
-      int c[NG][VE];
-      AT v[NG][VE];
+    for (int g = 0; g < NR; g += RG) {
+      int c[RG];
+      AT v[RG];
 #pragma unroll
-      for (int q = 0; q < NG; q++) {
-        const int k = ((g + q) * 32 + lane) * VE;
-        if (g + q < NV && k < span) Vec<VT>::load(p.idx + a0 + k, val + a0 + k, c[q], v[q]);
+      for (int q = 0; q < RG; q++) {
+        const int k = (g + q) * 32 + lane;
+        if (g + q < NR && k < span) {
+          c[q] = __ldcs(p.idx + a0 + k);
+          v[q] = ld_val<VT, AT>(val + a0 + k);
+        }
       }
 #pragma unroll
-      for (int q = 0; q < NG; q++) {
-        const int k = ((g + q) * 32 + lane) * VE;
-        if (g + q < NV && k < span) {
-#pragma unroll
-          for (int j = 0; j < VE; j++) {
-            const int e = a0 + k + j;
-            AT pr = 0;
-            if (e >= it.e0 && e < it.e1) pr = v[q][j] * (AT)__ldg(x + c[q][j]);
-            prod[k + j] = pr;
-          }
-        }
+      for (int q = 0; q < RG; q++) {
+        const int k = (g + q) * 32 + lane;
+        if (g + q < NR && k < span) prod[k] = v[q] * (AT)__ldg(x + c[q]);
       }
     }
     __syncwarp();
