@@ -56,7 +56,7 @@ EXPORTS = [
     "fvg_matrix_add_storage", "fvg_matrix_device_bytes", "fvg_matrix_get_transpose", "fvg_matrix_get_ell",
     "fvg_matrix_get_jds", "fvg_matrix_get_hybrid", "fvg_spmv", "fvg_trans_mv", "fvg_spmm",
     "fvg_glm_params_default", "fvg_logreg_lbfgs", "fvg_logreg_sgd", "fvg_logreg_eval",
-    "fvg_logreg_predict_probability",
+    "fvg_logreg_predict_probability", "fvg_spmv_no_alloc",
 ]
 
 _lib = None
@@ -106,6 +106,7 @@ def load(build_if_needed: bool = True):
                             C.POINTER(_dbl)], _int),
         "fvg_logreg_eval": ([_p, _p, _int, _int, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
         "fvg_logreg_predict_probability": ([_p, _p, _p, _dbl, _p], _int),
+        "fvg_spmv_no_alloc": ([_p, _p, _int, _int, _p, _p], _int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -213,7 +213,11 @@ static void ensure_transpose(fvg_ctx* c, fvg_matrix* M) {
 
 static void prepare(fvg_ctx* c, fvg_matrix* M, int fmt, bool trans) {
   if (fmt == FVG_CRS) {
-    if (trans) ensure_transpose(c, M);
+    crs_sched(c, M->A, kWarpTile);  // the CRS kernel's work schedule
+    if (trans) {
+      ensure_transpose(c, M);
+      crs_sched(c, *M->AT, kWarpTile);
+    }
   } else if (fmt == FVG_ELL) {
     if (!M->ell) {
       M->ell.reset(new DevELL());

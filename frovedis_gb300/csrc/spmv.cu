@@ -437,7 +437,7 @@ static int crs_grid(fvg_ctx* c, int tile) {
 
 template <class VT, class XT, class AT, class YT, int EPI>
 static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const void* x, void* y,
-                       const LogregEpi* lr, const PassScratch& ps) {
+                       const LogregEpi* lr, const PassScratch& ps, bool timed = true) {
   CrsK p;
   p.off = a.off.as<i32>();
   p.idx = a.idx.as<i32>();
@@ -485,7 +485,7 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
     f.grad_bias = lr ? lr->grad_bias : nullptr;
     f.ticket = ps.ticket;
     int fg = (int)std::max<i64>(1, std::min<i64>(s.nlong, 4 * c->num_sms));
-    ProfScope pf(c, P_FINALIZE);
+    ProfScope pf(c, timed ? P_FINALIZE : P_NKEYS);
     k_finalize<AT, YT, EPI><<<fg, kThreads, 0, c->stream>>>(f);
     check_launch("k_finalize");
     count_launch(c);
@@ -531,6 +531,29 @@ void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y
     else
       launch_crs<bf16, float, float, float, EPI_LOGREG>(c, a, s, storage, x, y, lr, ps);
   }
+}
+
+// y = A x over a CRS layout whose work schedule already exists, with the
+// caller's scratch (piece partial sums only) and no allocation of any kind.
+// Returns the scratch bytes the pass needs when scratch is null.
+size_t crs_spmv_no_alloc(fvg_ctx* c, DevCRS& a, int storage, const void* x, void* y, void* scratch,
+                         size_t scratch_bytes) {
+  const Sched* s = a.sched[0].get();
+  if (!s) fail(FVG_ERR_INVALID_ARG, "matrix not prepared: call fvg_matrix_prepare(ctx, mat, FVG_CRS, ...) first");
+  if (!a.val[storage].p) fail(FVG_ERR_INVALID_ARG, "value plane missing: call fvg_matrix_add_storage first");
+  const size_t at_size = (storage == FVG_F64) ? 8 : 4;
+  const size_t need = at_size * (size_t)std::max<i64>(s->npieces, 1);
+  if (!scratch) return need;
+  if (need > scratch_bytes) fail(FVG_ERR_INVALID_ARG, "matrix needs more scratch than the allocation-free entry point has");
+  PassScratch ps = {};
+  ps.partials = scratch;
+  if (storage == FVG_F64)
+    launch_crs<double, double, double, double, EPI_STORE>(c, a, *s, storage, x, y, nullptr, ps, false);
+  else if (storage == FVG_F32)
+    launch_crs<float, float, float, float, EPI_STORE>(c, a, *s, storage, x, y, nullptr, ps, false);
+  else
+    launch_crs<bf16, float, float, float, EPI_STORE>(c, a, *s, storage, x, y, nullptr, ps, false);
+  return need;
 }
 
 // ------------------------------------------------------------------- JDS

@@ -134,6 +134,23 @@ FVG_API fvg_status fvg_trans_mv(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, f
 FVG_API fvg_status fvg_spmm(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage, fvg_dtype vec_dtype,
                             const void* X, int64_t k, void* Y, int on_device);
 
+/* y = A x over the CRS layout, x and y device pointers (FP64 vectors for
+ * FVG_F64 storage, FP32 vectors for FVG_F32 / FVG_BF16), queued on the
+ * context stream without waiting for it.  No counterpart in the reference.
+ * It allocates nothing, for callers that cannot allocate device memory: a
+ * plug-in inside a host framework that owns all device allocations, or a
+ * latency-critical loop that must not pay cudaMalloc's implicit
+ * synchronisation.  Its scratch is a fixed 8 MiB device array inside the
+ * library (held by every GPU that loads it, until exit), enough for long rows
+ * totalling ~512 million nonzeros; larger matrices get FVG_ERR_INVALID_ARG.
+ * The matrix must be prepared first (fvg_matrix_prepare with FVG_CRS, and
+ * fvg_matrix_add_storage for FP32/BF16).  The first call on a device looks up
+ * the array's device address (one-time set-up; make it before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race, so
+ * order them on one stream. */
+FVG_API fvg_status fvg_spmv_no_alloc(fvg_ctx* ctx, fvg_matrix* mat, fvg_dtype storage, fvg_dtype vec_dtype,
+                                     const void* x, void* y);
+
 /* ------------------------------------------------------------ training */
 typedef struct {
   int64_t num_iteration;      /* numIteration (default 1000) */
