@@ -157,7 +157,9 @@ def run_gpu(args):
     A.prepare("CRS", transpose=True)
     A.add_storage("bf16")
     A.add_storage("f32")
-    kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, storage=args.storage)
+    # initModel overload with zero weights: the default all-ones start makes
+    # the reference's L-BFGS exhaust its line search and blow up on this data
+    kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, storage=args.storage, w0=np.zeros(n))
 
     def one_step():
         return fv.logreg_lbfgs(A, label, **kw)
@@ -231,6 +233,7 @@ def run_gpu(args):
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
+    spmv = None if args.skip_spmv else spmv_suite(ctx, args)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = cpu_baseline(off, idx, val, label, spec, args, threads=0, sample_rows=args.cpu_rows)
@@ -258,9 +261,61 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": ck,
         "fp64_gpu": fp64,
+        "spmv_2m": spmv,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+def spmv_suite(ctx, args, reps=10):
+    """SpMV kernel bench on the 2,000,000^2 / 80M-nonzero power-law matrix:
+    y = A x and z = A^T r per format and value precision, kernel time from
+    CUDA events on the context stream, GB/s of algorithmic bytes
+    nnz*(s_v+4) + (rows+1)*4 + cols*s_x + rows*s_y."""
+    import torch
+
+    import frovedis_gb300 as fv
+    from frovedis_gb300 import datagen
+    spec = datagen.spmv_2m_80m(args.spmv_scale)
+    off, idx, val, _ = datagen.generate(spec)
+    m = n = spec.m
+    nnz = int(off[-1])
+    A = ctx.matrix(m, n, off, idx, val)
+    A.add_storage("f32")
+    out = {"rows": m, "cols": n, "nnz": nnz, "max_row": int(np.max(np.diff(off))), "reps": reps}
+    keys = {"CRS": "spmv_crs", "JDS": "spmv_jds", "HYBRID": "spmv_hyb", "ELL": "spmv_ell"}
+    for fmt in ("CRS", "JDS", "HYBRID", "ELL"):
+        if fmt == "ELL" and m * out["max_row"] > 8 * nnz:
+            out[fmt] = (f"n/a: ELL pads every row to the longest ({out['max_row']}), "
+                        f"{m * out['max_row'] / nnz:.0f}x the nonzeros")
+            continue
+        try:
+            A.prepare(fmt, transpose=True)
+        except fv.FvgError as e:
+            out[fmt] = f"n/a: {e}"
+            continue
+        res = {}
+        for storage, tdt, s_v, s_x in (("f64", torch.float64, 8, 8), ("f32", torch.float32, 4, 4)):
+            vec = "f64" if storage == "f64" else "f32"
+            x = torch.randn(n, dtype=tdt, device="cuda")
+            y = torch.empty(m, dtype=tdt, device="cuda")
+            torch.cuda.synchronize()
+            for trans in (False, True):
+                fn = A.trans_mv_device if trans else A.spmv_device
+                for _ in range(3):
+                    fn(x.data_ptr(), y.data_ptr(), fmt=fmt, storage=storage, vec=vec)
+                ctx.reset_profile()
+                ctx.set_profiling(True)
+                for _ in range(reps):
+                    fn(x.data_ptr(), y.data_ptr(), fmt=fmt, storage=storage, vec=vec)
+                ctx.set_profiling(False)
+                key = keys["CRS"] if (trans and fmt == "ELL") else keys[fmt]
+                ms, cnt = ctx.profile(key)
+                b = nnz * (s_v + 4) + (m + 1) * 4 + n * s_x + m * s_x
+                res[f"{storage}_{'trans_mv' if trans else 'spmv'}_gbs"] = b * cnt / (ms / 1e3) / 1e9 if ms else None
+        out[fmt] = res
+    A.close()
+    return out
 
 
 def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
@@ -273,7 +328,7 @@ def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
     z = int(off[ms])
     a = oracle.CRS(ms, spec.n, off[: ms + 1], idx[:z], val[:z])
     splits = np.linspace(0, ms, threads + 1).astype(np.int64)
-    kw = dict(reg_type="L2", reg_param=1e-4, splits=splits, nthreads=threads)
+    kw = dict(reg_type="L2", reg_param=1e-4, splits=splits, nthreads=threads, w0=np.zeros(spec.n))
     # setup (per-rank transposes) and the initial evaluation are excluded by
     # differencing a 1-iteration run and a (1+k)-iteration run
     t0 = time.perf_counter()
@@ -335,6 +390,8 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-spmv", action="store_true")
+    ap.add_argument("--spmv-scale", type=float, default=1.0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
