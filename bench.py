@@ -386,13 +386,19 @@ def main():
     ap.add_argument("--iters", type=int, default=50)
     ap.add_argument("--storage", default="bf16", choices=["bf16", "f32", "f64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-rows", type=int, default=500_000)
-    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--cpu-rows", type=int, default=4_000_000)
+    ap.add_argument("--cpu-iters", type=int, default=5)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-spmv", action="store_true")
     ap.add_argument("--spmv-scale", type=float, default=1.0)
+    ap.add_argument("--spmv-only", action="store_true", help="run only the SpMV kernel suite")
     args = ap.parse_args()
+    if args.spmv_only:
+        import frovedis_gb300 as fv
+        ctx = fv.Context(0)
+        print(json.dumps({"spmv_2m": spmv_suite(ctx, args, reps=args.steps)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

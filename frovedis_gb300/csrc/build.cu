@@ -190,11 +190,12 @@ const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
   std::vector<Item> items;
   std::vector<i32> lrows, lpiece0;
   i64 npieces = 0;
-  i64 t0 = 0, tnnz = 0;  // open tile: rows [t0, r), tnnz nonzeros
+  i64 t0 = 0, tnnz = 0, tmax = 0;  // open tile: rows [t0, r), tnnz nonzeros, longest row tmax
   auto flush = [&](i64 r) {
     if (r > t0) items.push_back(Item{(int32_t)t0, (int32_t)r, off[t0], off[r]});
     t0 = r;
     tnnz = 0;
+    tmax = 0;
   };
   for (i64 r = 0; r < m; r++) {
     const i64 len = (i64)off[r + 1] - off[r];
@@ -212,8 +213,14 @@ const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
       t0 = r + 1;
       continue;
     }
-    if (r > t0 && (tnnz + len > tile || r - t0 >= kTileRows)) flush(r);
+    // close the tile when this row would overflow it, or make one lane sum
+    // more than kLaneWork products of a row (balance inside the warp)
+    if (r > t0) {
+      const i64 R = r - t0 + 1, mx = std::max(tmax, len);
+      if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) flush(r);
+    }
     tnnz += len;
+    tmax = std::max(tmax, len);
   }
   flush(m);
   lpiece0.push_back((i32)npieces);
@@ -351,6 +358,16 @@ static void jds_fill(fvg_ctx* c, const DevCRS& a, int master, const i32* perm, i
   else launch_jds_fill<bf16>(c, a, master, perm, rows, joff, cap, jidx, jval);
 }
 
+// Leading permuted rows with more than kJdsWarpLen diagonals (the rows of
+// diagonal kJdsWarpLen): the JDS product gives each of them a warp.
+static i64 jds_warp_rows(fvg_ctx* c, const DevJDS& j) {
+  if (j.ndiag <= kJdsWarpLen) return 0;
+  i64 h[2];
+  FVG_CUDA(cudaMemcpyAsync(h, j.off.as<i64>() + kJdsWarpLen, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  return h[1] - h[0];
+}
+
 void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master) {
   j.m = a.m;
   j.n = a.n;
@@ -371,6 +388,7 @@ void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master) {
   FVG_CUDA(cudaMemsetAsync(j.idx.as<i32>() + a.nnz, 0, sizeof(i32) * kPad, c->stream));
   alloc_plane(c, j.val[master], a.nnz, master);
   jds_fill(c, a, master, j.perm.as<i32>(), a.m, j.off.as<i64>(), j.ndiag, j.idx.as<i32>(), j.val[master].p);
+  j.warp_rows = jds_warp_rows(c, j);
 }
 
 // ------------------------------------------------------------------ hybrid
@@ -484,6 +502,7 @@ void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 thr) {
   alloc_plane(c, h.jds.val[master], h.jds.nnz, master);
   jds_fill(c, a, master, h.jds.perm.as<i32>(), a.m, h.jds.off.as<i64>(), start, h.jds.idx.as<i32>(),
            h.jds.val[master].p);
+  h.jds.warp_rows = jds_warp_rows(c, h.jds);
   // CRS tail of the crs_rows longest rows, in sorted order
   h.crs.m = crs_rows;
   h.crs.n = a.n;

@@ -70,7 +70,16 @@ constexpr i64 kPad = 32;
 // An item's nonzeros are contiguous, so a warp reads them with coalesced
 // 16-byte vector loads.
 constexpr int kThreads = 256;
-constexpr int kTileRows = 31;  // lanes 0..R of a warp hold a tile's R+1 row offsets
+constexpr int kTileRows = 248;  // rows per tile (their offsets are staged in shared memory)
+constexpr int kLaneWork = 32;   // products one lane may sum for one row in a tile
+// Lanes per row when a warp sums a tile of R rows: 32 / R rounded to a power
+// of two; tiles of 32 or more rows take rounds of 32 rows, one lane each.
+__host__ __device__ __forceinline__ int lanes_per_row(int R) {
+  if (R >= 32) return 1;
+  int p2 = 1;
+  while (p2 < R) p2 <<= 1;
+  return 32 / p2;
+}
 struct Item {
   int32_t r0;  // first row (tile) or the long row (piece)
   int32_t r1;  // one past the last row (tile), or -1 - piece index (piece)
@@ -122,7 +131,9 @@ struct DevJDS {  // jds_matrix_local (jds_matrix.hpp:15-146)
   DBuf idx;      // int32 [nnz]
   DBuf val[3];
   bool empty_perm = false;  // all-zero matrix: the reference leaves perm empty
+  i64 warp_rows = 0;        // leading permuted rows longer than kJdsWarpLen (a warp each)
 };
+constexpr i64 kJdsWarpLen = 128;
 
 struct DevHYB {  // jds_crs_hybrid_local (jds_crs_hybrid.hpp:8-153)
   i64 m = 0, n = 0, crs_rows = 0;

@@ -630,7 +630,7 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   S.alloc(sizeof(double) * n1 * h, s);
   Y.alloc(sizeof(double) * n1 * h, s);
   NWF.alloc(sizeof(float) * n1, s);
-  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 2 * c->num_sms));
+  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 6 * c->num_sms));
   part.alloc(sizeof(double) * 2 * vgrid + 256, s);
   stbuf.alloc(sizeof(LbState) + 256, s);
   unsigned* ticket = (unsigned*)((char*)part.p + sizeof(double) * 2 * vgrid);
@@ -863,7 +863,7 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
   LWF.alloc(sizeof(float) * n1, s);
   G.alloc(sizeof(double) * n1, s);
   TOT.alloc(sizeof(double) * n1, s);
-  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 2 * c->num_sms));
+  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 6 * c->num_sms));
   part.alloc(sizeof(double) * 2 * vgrid + 256, s);
   unsigned* ticket = (unsigned*)((char*)part.p + sizeof(double) * 2 * vgrid);
   FVG_CUDA(cudaMemsetAsync(ticket, 0, 256, s));

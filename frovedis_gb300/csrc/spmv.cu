@@ -237,9 +237,11 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
   constexpr int NR = SPAN / 32;          // element rounds per lane
   constexpr int RG = sizeof(VT) == 8 ? (FVG_CRS_ROUNDS + 1) / 2 : FVG_CRS_ROUNDS;  // rounds in flight together
   __shared__ AT sprod[kThreads / 32][SPAN];
+  __shared__ int soffs[kThreads / 32][kTileRows + 1];
   using Sum = typename SumOf<AT>::type;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   AT* prod = sprod[w];
+  int* soff = soffs[w];
   const i64 W = (i64)gridDim.x * (kThreads / 32);
   const i64 n = p.nitems;
   const XT* __restrict__ x = (const XT*)p.x;
@@ -253,9 +255,9 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
     if (t + W < n) nx = p.items[t + W];  // prefetch the next descriptor
     const int a0 = it.e0;
     const int span = it.e1 - a0;
-    // row boundaries of a tile, one per lane
-    int myoff = 0;
-    if (it.r1 >= 0 && lane <= it.r1 - it.r0) myoff = __ldg(p.off + it.r0 + lane);
+    // row boundaries of a tile into the warp's offsets slice
+    if (it.r1 >= 0)
+      for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = __ldg(p.off + it.r0 + k);
     // phase 1: lane L takes nonzeros L, L+32, ... so one gather instruction
     // covers 32 consecutive nonzeros (neighbouring columns / rows share
     // sectors); RG rounds of loads are issued before their gathers.
@@ -280,21 +282,30 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
     __syncwarp();
     // phase 2
     if (it.r1 >= 0) {
+      // Gl lanes per row: 32 / R rounded to a power of two; tiles of 32 or
+      // more (short) rows take rounds of 32 rows, one lane each
       const int R = it.r1 - it.r0;
-      int Gl = 32;
-      if (R > 1) {
-        int p2 = 2;
-        while (p2 < R) p2 <<= 1;
-        Gl = 32 / p2;
+      const int Gl = lanes_per_row(R);  // the packer keeps a lane's share <= kLaneWork
+      const int per_round = 32 / Gl;
+      for (int rb = 0; rb < R; rb += per_round) {
+        const int j = rb + lane / Gl, sub = lane % Gl;
+        AT acc = 0;
+        if (j < R) {
+          const int s = soff[j] - a0, e = soff[j + 1] - a0;
+          AT a1 = 0, a2 = 0, a3 = 0;
+          int k = s + sub;
+          for (; k + 3 * Gl < e; k += 4 * Gl) {
+            acc += prod[k];
+            a1 += prod[k + Gl];
+            a2 += prod[k + 2 * Gl];
+            a3 += prod[k + 3 * Gl];
+          }
+          for (; k < e; k += Gl) acc += prod[k];
+          acc = (acc + a1) + (a2 + a3);
+        }
+        for (int o = Gl >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (j < R && sub == 0) epilogue<AT, YT, EPI>(p, it.r0 + j, acc, bias, ls, bs);
       }
-      const int j = lane / Gl, sub = lane % Gl;
-      const int s = __shfl_sync(0xffffffffu, myoff, j & 31) - a0;
-      const int e = __shfl_sync(0xffffffffu, myoff, (j + 1) & 31) - a0;
-      AT acc = 0;
-      if (j < R)
-        for (int k = s + sub; k < e; k += Gl) acc += prod[k];
-      for (int o = Gl >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (j < R && sub == 0) epilogue<AT, YT, EPI>(p, it.r0 + j, acc, bias, ls, bs);
     } else {
       AT acc = 0;
       for (int k = it.e0 - a0 + lane; k < span; k += 32) acc += prod[k];
@@ -562,12 +573,42 @@ size_t crs_spmv_no_alloc(fvg_ctx* c, DevCRS& a, int storage, const void* x, void
 // p has exactly the diagonals d with off[d+1] - off[d] > p (binary search).
 // part (hybrid) adds the CRS tail of the first npart permuted rows after the
 // JDS sum, as jds_crs_hybrid_spmv_impl does (jds_crs_hybrid.hpp:198-211).
+// Rows with more than kJdsWarpLen diagonals (the first `nrows` permuted rows)
+// are read by a warp each instead: lanes stride over the row's diagonals.
+template <class VT, class XT, class AT, class YT>
+__global__ void __launch_bounds__(256) k_jds_warp(const i32* __restrict__ perm, const i64* __restrict__ off,
+                                                  const i32* __restrict__ idx, const VT* __restrict__ val,
+                                                  i64 nrows, i64 ndiag, const XT* __restrict__ x,
+                                                  YT* __restrict__ y, const AT* __restrict__ part, i64 npart) {
+  const int lane = threadIdx.x & 31;
+  const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
+  for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nrows; p += nw) {
+    i64 lo = 0, hi = ndiag;
+    while (lo < hi) {
+      i64 mid = (lo + hi) >> 1;
+      if (off[mid + 1] - off[mid] > p) lo = mid + 1;
+      else hi = mid;
+    }
+    AT acc = 0;
+    for (i64 d = lane; d < lo; d += 32) {
+      i64 q = off[d] + p;
+      acc += (AT)val[q] * (AT)__ldg(x + idx[q]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      if (p < npart) acc = acc + part[p];
+      y[perm[p]] = (YT)acc;
+    }
+  }
+}
+
 template <class VT, class XT, class AT, class YT>
 __global__ void __launch_bounds__(256) k_jds(const i32* __restrict__ perm, const i64* __restrict__ off,
                                              const i32* __restrict__ idx, const VT* __restrict__ val,
                                              i64 m, i64 ndiag, const XT* __restrict__ x, YT* __restrict__ y,
-                                             const AT* __restrict__ part, i64 npart) {
-  for (i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (i64)gridDim.x * blockDim.x) {
+                                             const AT* __restrict__ part, i64 npart, i64 p0) {
+  for (i64 p = p0 + (i64)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (i64)gridDim.x * blockDim.x) {
     i64 lo = 0, hi = ndiag;
     while (lo < hi) {
       i64 mid = (lo + hi) >> 1;
@@ -610,9 +651,19 @@ static void launch_jds(fvg_ctx* c, DevJDS& j, int storage, const void* x, void* 
   if (j.empty_perm) {
     k_zero<YT><<<grid_rows(j.m), 256, 0, c->stream>>>((YT*)y, j.m);
   } else {
-    k_jds<VT, XT, AT, YT><<<grid_rows(j.m), 256, 0, c->stream>>>(
-        j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(), j.m, j.ndiag, (const XT*)x,
-        (YT*)y, (const AT*)part, npart);
+    const i64 L = j.warp_rows;
+    if (L > 0) {
+      k_jds_warp<VT, XT, AT, YT><<<grid_rows(L * 32), 256, 0, c->stream>>>(
+          j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(), L, j.ndiag, (const XT*)x,
+          (YT*)y, (const AT*)part, npart);
+      check_launch("k_jds_warp");
+      count_launch(c);
+    }
+    if (j.m > L) {
+      k_jds<VT, XT, AT, YT><<<grid_rows(j.m - L), 256, 0, c->stream>>>(
+          j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(), j.m, j.ndiag, (const XT*)x,
+          (YT*)y, (const AT*)part, npart, L);
+    }
   }
   check_launch("k_jds");
   count_launch(c);
