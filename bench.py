@@ -35,6 +35,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "sparse LogReg L-BFGS iters/s + SpMV HBM GB/s: BF16/batched vs FP64 GPU, same loss"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# dram__bytes_read.sum + dram__bytes_write.sum over the algorithmic bytes of
+# the same launch, from `ncu --set full` of k_crs on the 1,000,000-row
+# version of the benchmark matrix (BF16 values): pass 1 377.56 MB / 380.0 MB,
+# pass 2 373.51 MB / 376.0 MB.
+NCU_TRAFFIC_RATIO = {"pass1": 377.56 / 380.0, "pass2": 373.51 / 376.0}
 
 
 def load_peak():
@@ -187,31 +192,62 @@ def run_gpu(args):
     ctx.set_profiling(False)
     ms = e0.elapsed_time(e1)
     launches = ctx.kernel_launches - launches0
-    p1_ms, p1_n = ctx.profile("pass1")
-    p2_ms, p2_n = ctx.profile("pass2")
+    # passes over the first value plane ("pass1"/"pass2": BF16 or FP64) and
+    # over FP32 values ("_f32": FP32 storage, or BF16 after refinement)
+    prof = {k: ctx.profile(k) for k in ("pass1", "pass2", "pass1_f32", "pass2_f32")}
     ms = allmax(world, ms)
     total_iters = iters * world
     value = total_iters / (ms / 1e3)
 
     # roofline of the CRS SpMV kernel (both passes of every evaluation)
-    s_v = {"f64": 8, "f32": 4, "bf16": 2}[args.storage]
+    s_v0 = {"f64": 8, "f32": 4, "bf16": 2}[args.storage]
     s_x = 8 if args.storage == "f64" else 4
-    b1, b2 = eval_bytes(m, n, nnz, s_v, s_x)
+    b1, b2 = eval_bytes(m, n, nnz, s_v0, s_x)
+    b1f, b2f = eval_bytes(m, n, nnz, 4, 4)
+    alg = {"pass1": b1, "pass2": b2, "pass1_f32": b1f, "pass2_f32": b2f}
     peak, peak_kind = load_peak()
-    spmv_ms = p1_ms + p2_ms
-    achieved = (b1 * p1_n + b2 * p2_n) / (spmv_ms / 1e3) / 1e9 if spmv_ms > 0 else 0.0
+    spmv_ms = sum(v[0] for v in prof.values())
+    spmv_n = sum(v[1] for v in prof.values())
+    alg_total = sum(alg[k] * prof[k][1] for k in prof)
+    achieved = alg_total / (spmv_ms / 1e3) / 1e9 if spmv_ms > 0 else 0.0
+    # DRAM bytes per launch: ratio of dram__bytes_(read+write) to algorithmic
+    # bytes from a 1/10-row ncu capture of the same kernels (BF16 values;
+    # 6.0e7 nonzeros, 1,000,000 columns), applied to this run's launches
+    traffic = (sum(NCU_TRAFFIC_RATIO[k[:5]] * alg[k] * prof[k][1] for k in prof) / spmv_n
+               if spmv_n and args.storage == "bf16" else None)
 
-    # plain FP64 GPU path on the same data (the >= 3x denominator)
-    fp64 = None
-    if args.storage != "f64" and not args.skip_fp64:
-        kw64 = dict(kw, storage="f64")
-        fv.logreg_lbfgs(A, label, **kw64)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r64 = fv.logreg_lbfgs(A, label, **kw64)
-        torch.cuda.synchronize()
-        fp64 = {"iters_per_s": r64["n_iter"] / (time.perf_counter() - t0), "final_loss": r64["loss"],
-                "loss_rel_diff_vs_low_precision": abs(r["loss"] - r64["loss"]) / abs(r64["loss"])}
+    # the same training at the other precisions on the same data: iters/s and
+    # final loss against the FP64 path (FP64 is the reference's arithmetic)
+    modes = None
+    if not args.skip_fp64:
+        modes = {}
+        for name, extra in (("f64", dict(storage="f64")), ("f32", dict(storage="f32")),
+                            ("bf16_no_refine", dict(storage="bf16", refine=0)),
+                            ("bf16_refine", dict(storage="bf16"))):
+            kwm = dict(kw, **extra)
+            fv.logreg_lbfgs(A, label, **kwm)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rm = fv.logreg_lbfgs(A, label, **kwm)
+            torch.cuda.synchronize()
+            modes[name] = {"iters_per_s": rm["n_iter"] / (time.perf_counter() - t0), "final_loss": rm["loss"],
+                           "n_iter": rm["n_iter"]}
+        l64 = modes["f64"]["final_loss"]
+        t64 = modes["f64"]["n_iter"] / modes["f64"]["iters_per_s"]
+        for name, extra in (("f32", dict(storage="f32")), ("bf16_no_refine", dict(storage="bf16", refine=0)),
+                            ("bf16_refine", dict(storage="bf16"))):
+            # matched loss: iterations (and time) until the loss is at most
+            # the FP64 path's loss after the same run (rel 1e-6)
+            rt = fv.logreg_lbfgs(A, label, trace=True, **dict(kw, num_iter=3 * args.iters, **extra))
+            hit = np.nonzero(rt["trace"][:, 0] <= l64 * (1 + 1e-6))[0]
+            v = modes[name]
+            v["iters_to_f64_loss"] = int(hit[0]) + 1 if hit.size else None
+            if hit.size:
+                v["time_to_f64_loss_s"] = v["iters_to_f64_loss"] / v["iters_per_s"]
+                v["speedup_time_to_f64_loss"] = t64 / v["time_to_f64_loss_s"]
+        for v in modes.values():
+            v["loss_rel_diff_vs_f64"] = abs(v["final_loss"] - l64) / abs(l64)
+            v["speedup_vs_f64"] = v["iters_per_s"] / modes["f64"]["iters_per_s"]
 
     # end to end through the C ABI with host buffers
     A.close()
@@ -252,15 +288,19 @@ def run_gpu(args):
                        nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU"},
         "final_loss": r["loss"], "iterations_per_run": r["n_iter"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)",
-                     "bytes_per_eval": b1 + b2, "launches": p1_n + p2_n, "kernel_ms": spmv_ms,
-                     "pass1_ms_avg": p1_ms / max(p1_n, 1), "pass2_ms_avg": p2_ms / max(p2_n, 1),
-                     "pass1_gbs": b1 * p1_n / max(p1_ms, 1e-9) / 1e6, "pass2_gbs": b2 * p2_n / max(p2_ms, 1e-9) / 1e6},
+                     "algorithmic_bytes_per_launch": alg_total / max(spmv_n, 1), "launches": spmv_n,
+                     "kernel_ms": spmv_ms,
+                     "traffic_source": "ncu dram bytes / algorithmic bytes on a 1/10-row capture, x this run's "
+                                       "algorithmic bytes per launch",
+                     "passes": {k: {"launches": prof[k][1], "ms_avg": prof[k][0] / max(prof[k][1], 1),
+                                    "gbs": alg[k] * prof[k][1] / max(prof[k][0], 1e-9) / 1e6}
+                                for k in prof if prof[k][1]}},
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": ck,
-        "fp64_gpu": fp64,
+        "precision_modes": modes,
         "spmv_2m": spmv,
         "cpu_baseline": cpu,
     }
@@ -316,6 +356,89 @@ def spmv_suite(ctx, args, reps=10):
         out[fmt] = res
     A.close()
     return out
+
+
+def run_regpath(args):
+    """Batched regularisation path: 16 datasets (500,000 columns, 1.4e7 rows
+    in all, 7e8 nonzeros), 64 L2 values log-spaced 1e-6..1 trained together
+    per dataset, `--iters` iterations (default 20).  Compared with the plain
+    FP64 GPU path run one model at a time (timed on 4 of the 64 values per
+    dataset and scaled by 16) at the same final losses."""
+    import torch
+
+    import frovedis_gb300 as fv
+    from frovedis_gb300 import datagen
+    specs = datagen.regpath_datasets(args.datasets, args.scale)
+    lams = np.logspace(-6, 0, 64)
+    probe = [0, 21, 42, 63]
+    ctx = fv.Context(0)
+    tot = {"batched_s": 0.0, "batched_model_iters": 0, "fp64_single_s_est": 0.0, "nnz": 0, "rows": 0,
+           "pass1_ms": 0.0, "pass1_n": 0, "pass2_ms": 0.0, "pass2_n": 0, "alg_bytes": 0.0, "flops": 0.0}
+    loss_err = []
+    s_v = {"f64": 8, "f32": 4, "bf16": 2}[args.storage]
+    for spec in specs:
+        off, idx, val, label = datagen.generate(spec)
+        m, n, nnz = spec.m, spec.n, int(off[-1])
+        A = ctx.matrix(m, n, off, idx, val)
+        A.prepare("CRS", transpose=True)
+        if args.storage != "f64":
+            A.add_storage(args.storage)
+            A.add_storage("f32")
+        kw = dict(num_iter=args.iters, reg_type="L2", w0=np.zeros(n))
+        fv.logreg_lbfgs_batched(A, label, lams[:2], storage=args.storage, **dict(kw, num_iter=2))
+        torch.cuda.synchronize()
+        ctx.reset_profile()
+        ctx.set_profiling(True)
+        t0 = time.perf_counter()
+        rb = fv.logreg_lbfgs_batched(A, label, lams, storage=args.storage, **kw)
+        torch.cuda.synchronize()
+        tot["batched_s"] += time.perf_counter() - t0
+        ctx.set_profiling(False)
+        for key in ("pass1", "pass2"):
+            ms, cnt = ctx.profile("batch_" + key)
+            tot[key + "_ms"] += ms
+            tot[key + "_n"] += cnt
+        evals = ctx.profile("batch_pass1")[1]
+        s_x = 8 if args.storage == "f64" else 4
+        per_eval = (2 * nnz * (s_v + 4) + (m + n + 2) * 4 + n * 64 * s_x + 2 * m * 64 * s_x + m * 8
+                    + (n + 1) * 64 * 8)
+        tot["alg_bytes"] += per_eval * evals
+        tot["flops"] += 4.0 * nnz * 64 * evals
+        tot["batched_model_iters"] += int(rb["n_iter"].sum())
+        ts = 0.0
+        for j in probe:
+            t0 = time.perf_counter()
+            rs = fv.logreg_lbfgs(A, label, reg_param=lams[j], storage="f64", **kw)
+            torch.cuda.synchronize()
+            ts += time.perf_counter() - t0
+            loss_err.append(abs(rb["loss"][j] - rs["loss"]) / abs(rs["loss"]))
+        tot["fp64_single_s_est"] += ts * len(lams) / len(probe)
+        tot["nnz"] += nnz
+        tot["rows"] += m
+        A.close()
+    ctx.close()
+    value = tot["batched_model_iters"] / tot["batched_s"]
+    base = len(specs) * len(lams) * args.iters / tot["fp64_single_s_est"]
+    kms = tot["pass1_ms"] + tot["pass2_ms"]
+    peak, peak_kind = load_peak()
+    line = {
+        "metric": "batched L-BFGS model-iterations/s (64 regularisation values per dataset)",
+        "value": value, "unit": "model-iters/s", "higher_is_better": True,
+        "config": {"workload": "logreg-regpath-16x500k-64lambda", "datasets": len(specs), "rows": tot["rows"],
+                   "cols": specs[0].n, "nnz": tot["nnz"], "models_per_dataset": 64,
+                   "iterations": args.iters, "storage": args.storage},
+        "fp64_single_model_gpu": {"value": base, "unit": "model-iters/s",
+                                  "note": "plain FP64 path, one model per call; 4 of 64 values timed per dataset"},
+        "speedup_vs_fp64_single": value / base,
+        "loss_rel_diff_vs_fp64_single": {"max": max(loss_err), "median": statistics.median(loss_err)},
+        "kernels": {"ms": kms, "launches": tot["pass1_n"] + tot["pass2_n"],
+                    "achieved_gbs": tot["alg_bytes"] / (kms / 1e3) / 1e9 if kms else None, "hbm_peak_gbs": peak,
+                    "peak_kind": peak_kind,
+                    "achieved_tflops_fp32": tot["flops"] / (kms / 1e3) / 1e12 if kms else None,
+                    "pass1_ms": tot["pass1_ms"], "pass2_ms": tot["pass2_ms"]},
+        "wall_s": tot["batched_s"],
+    }
+    print(json.dumps(line), flush=True)
 
 
 def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
@@ -387,13 +510,20 @@ def main():
     ap.add_argument("--storage", default="bf16", choices=["bf16", "f32", "f64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-rows", type=int, default=4_000_000)
-    ap.add_argument("--cpu-iters", type=int, default=5)
+    ap.add_argument("--cpu-iters", type=int, default=60)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-spmv", action="store_true")
     ap.add_argument("--spmv-scale", type=float, default=1.0)
     ap.add_argument("--spmv-only", action="store_true", help="run only the SpMV kernel suite")
+    ap.add_argument("--workload", default="lbfgs", choices=["lbfgs", "regpath"])
+    ap.add_argument("--datasets", type=int, default=16, help="regpath: number of datasets")
     args = ap.parse_args()
+    if args.workload == "regpath":
+        if args.iters == 50:
+            args.iters = 20
+        run_regpath(args)
+        return
     if args.spmv_only:
         import frovedis_gb300 as fv
         ctx = fv.Context(0)

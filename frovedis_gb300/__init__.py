@@ -56,7 +56,7 @@ EXPORTS = [
     "fvg_matrix_add_storage", "fvg_matrix_device_bytes", "fvg_matrix_get_transpose", "fvg_matrix_get_ell",
     "fvg_matrix_get_jds", "fvg_matrix_get_hybrid", "fvg_spmv", "fvg_trans_mv", "fvg_spmm",
     "fvg_glm_params_default", "fvg_logreg_lbfgs", "fvg_logreg_sgd", "fvg_logreg_eval",
-    "fvg_logreg_predict_probability", "fvg_spmv_no_alloc",
+    "fvg_logreg_predict_probability", "fvg_spmv_no_alloc", "fvg_logreg_lbfgs_batched",
 ]
 
 _lib = None
@@ -107,6 +107,7 @@ def load(build_if_needed: bool = True):
         "fvg_logreg_eval": ([_p, _p, _int, _int, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
         "fvg_logreg_predict_probability": ([_p, _p, _p, _dbl, _p], _int),
         "fvg_spmv_no_alloc": ([_p, _p, _int, _int, _p, _p], _int),
+        "fvg_logreg_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -374,6 +375,30 @@ def _train(fn, mat: Matrix, label, sample_weight=None, w0=None, b0=None, trace=F
 def logreg_lbfgs(mat: Matrix, label, **kw):
     """logistic_regression_with_lbfgs::train (defaults as in the reference)."""
     return _train(mat.ctx.L.fvg_logreg_lbfgs, mat, label, **kw)
+
+
+def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=None, b0=None, **kw):
+    """k L-BFGS trainings on one matrix, model j with reg_param = reg_params[j]
+    (fvg_logreg_lbfgs_batched).  w0: (k, n) initial weights (default all 1),
+    b0: (k,) initial intercepts.  Returns w (k, n), b, n_iter, loss (k,)."""
+    ctx = mat.ctx
+    lam = np.ascontiguousarray(reg_params, dtype=np.float64)
+    k = len(lam)
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
+    icpt = bool(kw.get("intercept", False))
+    # order="C": a copy of a broadcast view would otherwise keep its column-major memory order
+    w = (np.ones((k, mat.n)) if w0 is None
+         else np.array(np.broadcast_to(w0, (k, mat.n)), dtype=np.float64, order="C"))
+    b = (np.full(k, 1.0 if icpt else 0.0) if b0 is None
+         else np.array(np.broadcast_to(b0, (k,)), dtype=np.float64, order="C"))
+    kw["intercept"] = int(icpt)
+    p = glm_params(**kw)
+    n_iter = np.zeros(k, dtype=np.int64)
+    loss = np.zeros(k)
+    ctx.check(ctx.L.fvg_logreg_lbfgs_batched(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam),
+                                             _ptr(w), _ptr(b), _ptr(n_iter), _ptr(loss)))
+    return dict(w=w, b=b, n_iter=n_iter, loss=loss)
 
 
 def logreg_sgd(mat: Matrix, label, **kw):

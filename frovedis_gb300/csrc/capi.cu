@@ -15,6 +15,9 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
                double* w_h, double* b_h, i64* n_iter, double* loss_out);
 void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
                  const double* w_h, double b, int icpt, double* grad_h, double* loss_h);
+void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
+                         const fvg_glm_params* p, i64 k, const double* lam_h, double* w_h, double* b_h,
+                         i64* n_iter_h, double* loss_h);
 int crs_blocks_per_sm();
 void sigmoid_probability(fvg_ctx* c, double* v, i64 m, double b);
 }  // namespace fvg
@@ -119,7 +122,8 @@ FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* c) {
 }
 
 static const char* kProfNames[P_NKEYS] = {"spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec",
-                                          "transpose", "spmv_ell", "spmv_jds", "spmv_hyb", "spmm"};
+                                          "transpose", "spmv_ell", "spmv_jds", "spmv_hyb", "spmm",
+                                          "pass1_f32", "pass2_f32", "batch_pass1", "batch_pass2"};
 
 FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* c, int enable) {
   if (!c) return FVG_ERR_INVALID_ARG;
@@ -555,6 +559,18 @@ FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* lab
   API_BEGIN
   own(c, M);
   lbfgs_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* c, fvg_matrix* M, const double* label,
+                                            const double* sample_weight, const fvg_glm_params* p, int64_t k,
+                                            const double* reg_params, double* weight, double* intercept,
+                                            int64_t* n_iter, double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss || !reg_params) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  lbfgs_batched_train(c, M, label, sample_weight, p, k, reg_params, weight, intercept, n_iter, final_loss);
   check_device_error(c);
   API_END(c)
 }

@@ -157,8 +157,8 @@ struct fvg_ctx {
   fvg::Profiler* prof = nullptr;  // owned; prof_create / prof_destroy
   // live matrices: destroying the context releases their device memory
   std::vector<fvg_matrix*> matrices;
-  // device error word: kernels set bits instead of trapping (bit 0: a bounded
-  // wait on a bulk copy gave up)
+  // device error word: a kernel that must give up (a bounded wait that ran
+  // out) sets a bit here instead of trapping; read after each call
   unsigned* dev_err = nullptr;
 };
 
@@ -176,7 +176,7 @@ namespace fvg {
 
 // ------------------------------------------------------------ profiling
 enum ProfKey { P_SPMV_CRS = 0, P_PASS1, P_PASS2, P_FINALIZE, P_LBFGS, P_TRANSPOSE, P_SPMV_ELL, P_SPMV_JDS,
-               P_SPMV_HYB, P_SPMM, P_NKEYS };
+               P_SPMV_HYB, P_SPMM, P_PASS1_F32, P_PASS2_F32, P_BATCH_PASS1, P_BATCH_PASS2, P_NKEYS };
 void prof_begin(fvg_ctx* c, int key);
 void prof_end(fvg_ctx* c, int key);
 void prof_collect(fvg_ctx* c, int key, double* ms, int64_t* n);
@@ -241,7 +241,17 @@ void ell_spmv(fvg_ctx* c, DevELL& e, int storage, int x_dt, const void* x, int y
 void jds_spmv(fvg_ctx* c, DevJDS& j, int storage, int x_dt, const void* x, int y_dt, void* y, bool accumulate_perm);
 void hyb_spmv(fvg_ctx* c, DevHYB& h, int storage, int x_dt, const void* x, int y_dt, void* y);
 void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k, void* Y);
-void jds_spmm(fvg_ctx* c, DevJDS& j, int storage, int x_dt, const void* X, i64 k, void* Y);
+// One block of at most 64 columns (X, Y already offset to the block's first
+// column; ldx / ldy row strides); scratch of spmm_scratch_bytes().
+i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage);
+void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, int y_dt, void* Y, i64 ldy,
+                    void* scratch);
+void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
+                           const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
+                           void* R, i64 ldr, double* out, double* gbias, void* scratch);
+
+// Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
+void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);
 
 // Per-row logistic epilogue applied to a finished product z = A w (used by
 // the non-CRS formats): r, loss/bias partial sums; then finalize_logreg.

@@ -427,8 +427,9 @@ struct Evaluator {
       FVG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 2, c->stream));
       return;
     }
+    const bool f32v = storage == FVG_F32;  // timed apart: the passes read 4-byte values
     if (op->fmt == FVG_CRS) {
-      crs_pass(c, *op->A, storage, vdt, x, vdt, nullptr, EPI_LOGREG, &lr, s1.p, P_PASS1);
+      crs_pass(c, *op->A, storage, vdt, x, vdt, nullptr, EPI_LOGREG, &lr, s1.p, f32v ? P_PASS1_F32 : P_PASS1);
     } else {
       if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->H, storage, vdt, x, vdt, z.p);
       else if (op->fmt == FVG_JDS) jds_spmv(c, *op->J, storage, vdt, x, vdt, z.p, false);
@@ -438,7 +439,8 @@ struct Evaluator {
     // backward product into grad[0..n) (FP64 output)
     if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->HT, storage, vdt, r.p, FVG_F64, grad);
     else if (op->fmt == FVG_JDS) jds_spmv(c, *op->JT, storage, vdt, r.p, FVG_F64, grad, false);
-    else crs_pass(c, *op->AT, storage, vdt, r.p, FVG_F64, grad, EPI_STORE, nullptr, s2.p, P_PASS2);
+    else crs_pass(c, *op->AT, storage, vdt, r.p, FVG_F64, grad, EPI_STORE, nullptr, s2.p,
+                  f32v ? P_PASS2_F32 : P_PASS2);
   }
 };
 
@@ -574,7 +576,7 @@ static void build_block_operand(fvg_ctx* c, fvg_matrix* M, int fmt, i64 r0, i64 
   }
 }
 
-static void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label) {
+void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label) {
   if (!p) fail(FVG_ERR_INVALID_ARG, "null params");
   if (!(p->num_iteration > 0 && p->alpha > 0 && p->reg_param >= 0 && p->convergence_tol >= 0))
     fail(FVG_ERR_INVALID_ARG, "checkAssumption failed: numIteration > 0 && alpha > 0 && regParam >= 0 && "

@@ -1,15 +1,15 @@
 // Sparse products on the device.
 //
 // CRS (crs_matrix_spmv_impl, crs_matrix.hpp:1505-1516): one persistent
-// kernel walks the matrix in row order as work items of <= 2048 (FP64) or
-// 4096 (FP32/BF16) nonzeros.  An item is either a tile of consecutive short
-// rows (each row read by 1..32 lanes, chosen from the tile's row count) or a
-// piece of a long row (read by the whole CTA; the finalize kernel adds the
-// pieces in order).  The item's column ids and values are contiguous and are
-// staged in shared memory by two bulk TMA copies (cp.async.bulk with an
-// mbarrier, L2 evict-first), double buffered so the next item streams in while
-// the current one is computed; x is gathered through the read-only path.
-// All reductions have a fixed order, so results are deterministic run to run.
+// kernel walks the matrix in row order as warp work items of at most 512
+// nonzeros, built once per matrix on the host from the row offsets.  An item
+// is either a tile of consecutive short rows (up to 248 rows, a bounded
+// number of products per lane) or a piece of a long row (the finalize kernel
+// adds the pieces in order).  A warp streams the item's values and column ids
+// with coalesced evict-first loads, gathers x through the read-only path,
+// stages the products in its own shared-memory slice and sums each row with
+// 1..32 lanes.  All reductions have a fixed order, so results are
+// deterministic run to run.
 //
 // The optional logistic epilogue fuses compute_wtx + logistic_gradient::
 // compute_dloss + `* sample_weight` + bias sum (gradient_descent.hpp:196-211,
@@ -18,158 +18,9 @@
 // sums on the FP32-arithmetic path, which keep GB300's narrow FP64 unit out of
 // the per-row work; FP64 Neumaier sums on the FP64 path), which the finalize
 // kernel reduces in FP64 in a fixed order.
-#include "fvg_internal.cuh"
+#include "device_common.cuh"
 
 namespace fvg {
-
-// --------------------------------------------------- TMA / mbarrier PTX
-__device__ __forceinline__ unsigned smem_u32(const void* ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// One bulk (non-tensor) TMA copy global -> shared, completing on `bar`;
-// both addresses 16-byte aligned, size a multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
-      : "memory");
-}
-__device__ __forceinline__ uint64_t policy_evict_first() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-// Bounded wait: gives up after ~2^22 polls (far beyond any normal copy time)
-// and reports it through *err; never spins forever.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err) {
-  for (unsigned it = 0; it < (1u << 22); it++)
-    if (mbar_try_wait(bar, parity)) return true;
-  if (err) atomicOr(err, 1u);
-  return false;
-}
-
-template <class T> __device__ __forceinline__ T block_sum256(T v) {
-  __shared__ T red[8];
-#pragma unroll
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[w] = v;
-  __syncthreads();
-  T t = 0;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int q = 0; q < 8; q++) t += red[q];
-  }
-  return t;  // valid in thread 0
-}
-
-// ---------------------------------------------------- compensated sums
-struct CSum {  // Neumaier, FP64 (the FP64 path)
-  double s = 0.0, c = 0.0;
-  __device__ __forceinline__ void add(double v) {
-    double t = s + v;
-    if (fabs(s) >= fabs(v)) c += (s - t) + v;
-    else c += (v - t) + s;
-    s = t;
-  }
-  __device__ __forceinline__ double total() const { return s + c; }
-};
-struct FSum {  // Kahan in FP32 (the FP32-arithmetic path keeps the FP64 unit idle)
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    float y = v - c;
-    float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ double total() const { return (double)s - (double)c; }
-};
-template <class AT> struct SumOf { using type = CSum; };
-template <> struct SumOf<float> { using type = FSum; };
-
-// Fixed-order block reduction of two compensated sums (256 threads).
-__device__ __forceinline__ void block_csum2(double a, double b, double* out_a, double* out_b) {
-  __shared__ double ra[256], rb[256];
-  __syncthreads();
-  ra[threadIdx.x] = a;
-  rb[threadIdx.x] = b;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st) {
-      ra[threadIdx.x] += ra[threadIdx.x + st];
-      rb[threadIdx.x] += rb[threadIdx.x + st];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    *out_a = ra[0];
-    *out_b = rb[0];
-  }
-}
-
-// ------------------------------------------------------- logistic math
-// logistic_gradient<T>::compute_dloss for one row (gradient.hpp:24-50).
-__device__ __forceinline__ void logistic_row(double wtx, double lab, double& loss, double& d) {
-  double z = lab * wtx;
-  double neg = lab * -1.0;
-  if (z > 18.0) {
-    double e = exp(-z);
-    loss = e;
-    d = e * neg;
-  } else if (z < -18.0) {
-    loss = -z;
-    d = neg;
-  } else {
-    loss = log(1.0 + exp(-z));
-    d = neg * (1.0 / (1.0 + exp(z)));
-  }
-  if (d > 1e12) d = 1e12;
-  else if (d < -1e12) d = -1e12;
-}
-// FP32 variant for the BF16/FP32-storage path (log1p form keeps small
-// losses that log(1+e) would round away in single precision).
-__device__ __forceinline__ void logistic_row(float wtx, float lab, float& loss, float& d) {
-  float z = lab * wtx;
-  float neg = -lab;
-  if (z > 18.0f) {
-    float e = expf(-z);
-    loss = e;
-    d = e * neg;
-  } else if (z < -18.0f) {
-    loss = -z;
-    d = neg;
-  } else {
-    loss = log1pf(expf(-z));
-    d = neg / (1.0f + expf(z));
-  }
-  if (d > 1e12f) d = 1e12f;
-  else if (d < -1e12f) d = -1e12f;
-}
-
-template <class VT> __device__ __forceinline__ float to_f(VT v);
-template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
-template <> __device__ __forceinline__ float to_f<bf16>(bf16 v) { return __bfloat162float(v); }
-
-template <class VT, class AT> __device__ __forceinline__ AT to_acc(VT v) { return (AT)to_f<VT>(v); }
-template <> __device__ __forceinline__ double to_acc<double, double>(double v) { return v; }
 
 // ------------------------------------------------------------ kernel args
 struct CrsK {
@@ -215,13 +66,6 @@ __device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, S
 }
 
 // ------------------------------------------------------------ warp tiles
-// Streaming (evict-first) load of one value, widened to the accumulator.
-template <class VT, class AT> __device__ __forceinline__ AT ld_val(const VT* q);
-template <> __device__ __forceinline__ double ld_val<double, double>(const double* q) { return __ldcs(q); }
-template <> __device__ __forceinline__ float ld_val<float, float>(const float* q) { return __ldcs(q); }
-template <> __device__ __forceinline__ float ld_val<bf16, float>(const bf16* q) {
-  return __uint_as_float((unsigned)__ldcs(reinterpret_cast<const unsigned short*>(q)) << 16);
-}
 
 // Persistent CRS kernel.  Warp g of the grid handles items g, g+W, g+2W, ...
 // (W = warps in the grid).  Phase 1: the warp streams the item's nonzeros
@@ -746,55 +590,6 @@ void ell_spmv(fvg_ctx* c, DevELL& e, int storage, int x_dt, const void* x, int y
                                                                  e.width, (const float*)x, (float*)y);
   }
   check_launch("k_ell");
-  count_launch(c);
-}
-
-// ------------------------------------------------------------------ SpMM
-// Y = A X (row-major, k columns): a warp per row, lanes across columns.
-template <class VT, class XT, class AT>
-__global__ void __launch_bounds__(256) k_spmm_crs(const i32* __restrict__ off, const i32* __restrict__ idx,
-                                                  const VT* __restrict__ val, i64 m, const XT* __restrict__ X,
-                                                  i64 k, XT* __restrict__ Y) {
-  const int lane = threadIdx.x & 31;
-  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
-  for (i64 r = warp; r < m; r += nwarps) {
-    i64 s = off[r], e = off[r + 1];
-    for (i64 c0 = 0; c0 < k; c0 += 64) {
-      AT a0 = 0, a1 = 0;
-      i64 ca = c0 + lane, cb = c0 + 32 + lane;
-      for (i64 q = s; q < e; q++) {
-        AT v = (AT)val[q];
-        const XT* xr = X + (i64)idx[q] * k;
-        if (ca < k) a0 += v * (AT)__ldg(xr + ca);
-        if (cb < k) a1 += v * (AT)__ldg(xr + cb);
-      }
-      if (ca < k) Y[r * k + ca] = (XT)a0;
-      if (cb < k) Y[r * k + cb] = (XT)a1;
-    }
-  }
-}
-
-void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k, void* Y) {
-  ProfScope pr(c, P_SPMM);
-  if (a.m == 0 || k == 0) return;
-  i64 warps = std::min<i64>(a.m, (i64)c->num_sms * 64);
-  unsigned g = (unsigned)((warps * 32 + 255) / 256);
-  if (storage == FVG_F64) {
-    if (x_dt != FVG_F64) fail(FVG_ERR_INVALID_ARG, "FP64 values need FP64 vectors");
-    k_spmm_crs<double, double, double><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(),
-                                                                  a.val[storage].as<double>(), a.m,
-                                                                  (const double*)X, k, (double*)Y);
-  } else if (storage == FVG_F32) {
-    k_spmm_crs<float, float, float><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(),
-                                                               a.val[storage].as<float>(), a.m, (const float*)X, k,
-                                                               (float*)Y);
-  } else {
-    k_spmm_crs<bf16, float, float><<<g, 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(),
-                                                              a.val[storage].as<bf16>(), a.m, (const float*)X, k,
-                                                              (float*)Y);
-  }
-  check_launch("k_spmm_crs");
   count_launch(c);
 }
 

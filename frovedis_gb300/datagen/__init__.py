@@ -109,3 +109,14 @@ def logreg_10m_1m(scale: float = 1.0) -> Spec:
     """Mixed-precision LR at scale: 10,000,000 x 1,000,000, nnz/row 1+Poisson(59), Zipf(1.1), lognormal(0,0.5)."""
     return Spec(m=int(10_000_000 * scale), n=max(1000, int(1_000_000 * scale)), lam=59.0, col_kind="zipf",
                 s_col=1.1, val_kind="lognormal", val_sigma=0.5, wstar_sd=1.0 / np.sqrt(60.0))
+
+
+def regpath_datasets(count: int = 16, scale: float = 1.0):
+    """Batched regularisation path: `count` datasets with 500,000 columns,
+    rows ~ U[10,000, 2,000,000] (seeded), nnz/row 1+Poisson(49), Zipf(1.2)
+    columns, |N(0,1)| values; dataset i uses seed 100 + i."""
+    rng = np.random.default_rng(2024)
+    rows = rng.integers(10_000, 2_000_001, size=16)[:count]
+    return [Spec(m=max(100, int(r * scale)), n=max(1000, int(500_000 * scale)), seed=100 + i, lam=49.0,
+                 col_kind="zipf", s_col=1.2, val_kind="absnormal", wstar_sd=1.0 / np.sqrt(50.0))
+            for i, r in enumerate(rows)]

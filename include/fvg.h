@@ -62,7 +62,9 @@ FVG_API void* fvg_ctx_stream(fvg_ctx* ctx);
 FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* ctx);
 /* Kernel timing with CUDA events on the context stream (off by default).
  * Names: "spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec", "transpose",
- * "spmv_ell", "spmv_jds", "spmv_hyb", "spmm". */
+ * "spmv_ell", "spmv_jds", "spmv_hyb", "spmm", "pass1_f32", "pass2_f32"
+ * ("pass1"/"pass2" are the training passes over FP64 or BF16 values, the
+ * "_f32" keys those over FP32 values, e.g. after the refinement switch). */
 FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* ctx, int enable);
 FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* ctx, const char* name, double* total_ms, int64_t* launches);
 FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* ctx);
@@ -188,6 +190,23 @@ FVG_API void fvg_glm_params_default(fvg_glm_params* p);
 FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
                                     const double* sample_weight, const fvg_glm_params* params, double* weight,
                                     double* intercept, int64_t* n_iter, double* final_loss);
+/* k logistic_regression_with_lbfgs::train runs on one matrix, trained
+ * together (a regularisation path, or a hyper-parameter sweep): model j uses
+ * regParam = reg_params[j] and every other setting of params (CRS format,
+ * one partition).  One forward product A W (W num_col x k) with the logistic
+ * epilogue per (row, model) and one backward product A^T R serve all models
+ * per evaluation.  Each model takes its own line-search decisions and stops
+ * on its own convergence test, so its result is that of a separate
+ * fvg_logreg_lbfgs run up to summation order (with FVG_BF16 storage all
+ * models move to FP32 values together, once any model's gradient stalls).
+ * weight[k*num_col] (model j at j*num_col) and intercept[k] hold the initial
+ * models on entry and the trained ones on return; n_iter[k], final_loss[k].
+ * 1 <= k <= 256.  The reference runs the models one train() call at a time
+ * (logistic_regression_with_lbfgs.hpp:395-437). */
+FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                            const double* sample_weight, const fvg_glm_params* params, int64_t k,
+                                            const double* reg_params, double* weight, double* intercept,
+                                            int64_t* n_iter, double* final_loss);
 /* logistic_regression_with_sgd::train main API
  * (ml/glm/logistic_regression_with_sgd.hpp:392-441 →
  *  sgd_parallelizer.hpp:132-378, 441-550). */

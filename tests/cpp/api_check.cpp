@@ -1,0 +1,129 @@
+// Exercises the C++ API of include/frovedis_gb300.hpp the way a frovedis
+// program calls the reference: build crs_matrix_local, multiply, convert to
+// ELL/JDS/hybrid, train with logistic_regression_with_{lbfgs,sgd}::train and
+// predict.  Reads a CRS matrix, a vector and labels from the text file
+// argv[1]; writes one "name v0 v1 ..." line per result to argv[2], which
+// tests/test_cpp_api.py compares with the oracle.
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "frovedis_gb300.hpp"
+
+using namespace frovedis;
+
+template <class V> static void put(FILE* f, const char* name, const V& v) {
+  std::fprintf(f, "%s", name);
+  for (auto x : v) std::fprintf(f, " %.17g", (double)x);
+  std::fprintf(f, "\n");
+}
+static void put1(FILE* f, const char* name, double v) { std::fprintf(f, "%s %.17g\n", name, v); }
+
+int main(int argc, char** argv) {
+  if (argc != 3) {
+    std::fprintf(stderr, "usage: api_check input.txt output.txt\n");
+    return 2;
+  }
+  std::ifstream in(argv[1]);
+  size_t m, n, nnz;
+  in >> m >> n >> nnz;
+  crs_matrix_local<double> A(m, n);
+  A.off.resize(m + 1);
+  A.idx.resize(nnz);
+  A.val.resize(nnz);
+  for (auto& v : A.off) in >> v;
+  for (auto& v : A.idx) in >> v;
+  for (auto& v : A.val) in >> v;
+  std::vector<double> x(n), label(m);
+  for (auto& v : x) in >> v;
+  for (auto& v : label) in >> v;
+  if (!in) {
+    std::fprintf(stderr, "bad input\n");
+    return 2;
+  }
+  FILE* f = std::fopen(argv[2], "w");
+
+  // products (crs_matrix.hpp:1518, ell_matrix.hpp:229/357, jds_matrix.hpp:419, jds_crs_hybrid.hpp:213)
+  put(f, "crs_mv", A * x);
+  auto t = A.transpose();
+  put(f, "t_off", t.off);
+  put(f, "t_idx", t.idx);
+  put(f, "t_val", t.val);
+  put(f, "t_shape", std::vector<size_t>{t.local_num_row, t.local_num_col});
+  ell_matrix_local<double> E(A);
+  put(f, "ell_mv", E * x);
+  put(f, "ell_trans", trans_mv(E, label));
+  put(f, "ell_width", std::vector<size_t>{E.val.size() / (m ? m : 1)});
+  jds_matrix_local<double> J(A);
+  put(f, "jds_mv", J * x);
+  put(f, "jds_perm", J.perm);
+  put(f, "jds_off", J.off);
+  jds_crs_hybrid_local<double> H(A);
+  put(f, "hyb_mv", H * x);
+  put(f, "hyb_crs_rows", std::vector<size_t>{H.crs.local_num_row});
+  rowmajor_matrix_local<double> X(n, 3);
+  for (size_t i = 0; i < n; i++)
+    for (size_t j = 0; j < 3; j++) X.val[i * 3 + j] = x[i] * (double)(j + 1) + (double)j;
+  put(f, "spmm", (A * X).val);
+
+  // FP32 instantiation
+  crs_matrix_local<float, int, size_t> Af(m, n);
+  Af.off.assign(A.off.begin(), A.off.end());
+  Af.idx.assign(A.idx.begin(), A.idx.end());
+  Af.val.assign(A.val.begin(), A.val.end());
+  std::vector<float> xf(x.begin(), x.end());
+  put(f, "crs_mv_f32", Af * xf);
+
+  // the reference's error on a size mismatch (std::runtime_error)
+  int threw = 0;
+  try {
+    std::vector<double> bad(n + 1);
+    auto r = A * bad;
+    (void)r;
+  } catch (std::runtime_error&) {
+    threw = 1;
+  }
+  put1(f, "mismatch_throws", threw);
+
+  // training (logistic_regression_with_lbfgs.hpp:395, logistic_regression_with_sgd.hpp:392)
+  {
+    logistic_regression_model<double> init(n, 1.0);
+    std::vector<double> sw;
+    size_t n_iter = 0;
+    auto model = logistic_regression_with_lbfgs::train(A, label, init, sw, n_iter, 20, 0.01, 10, 1e-3, L2, true,
+                                                       0.001, CRS);
+    put(f, "lbfgs_w", model.weight);
+    put1(f, "lbfgs_b", model.intercept);
+    put1(f, "lbfgs_n_iter", (double)n_iter);
+    put(f, "lbfgs_prob", model.predict_probability(A));
+    put(f, "lbfgs_pred", model.predict(A));
+  }
+  {
+    std::vector<double> lab = label;
+    auto model = logistic_regression_with_lbfgs::train(A, lab, 20, 0.01, 10, 1e-3, ZERO, true, 0.001, HYBRID);
+    put(f, "lbfgs_hyb_w", model.weight);
+    put1(f, "lbfgs_hyb_b", model.intercept);
+    // JDS is rejected for L-BFGS (lbfgs_parallelizer.hpp:596-597)
+    int jds_threw = 0;
+    try {
+      logistic_regression_with_lbfgs::train(A, lab, 20, 0.01, 10, 1e-3, ZERO, true, 0.001, JDS);
+    } catch (frovedis_gb300::error& e) {
+      jds_threw = std::string(e.what()).find("Unsupported input matrix type") != std::string::npos;
+    }
+    put1(f, "lbfgs_jds_throws", jds_threw);
+  }
+  {
+    logistic_regression_model<double> init(n, 1.0);
+    std::vector<double> sw;
+    size_t n_iter = 0;
+    auto model = logistic_regression_with_sgd::train(A, label, init, sw, n_iter, 15, 0.05, 0.3, 1e-2, L2, true,
+                                                     0.001, CRS);
+    put(f, "sgd_w", model.weight);
+    put1(f, "sgd_b", model.intercept);
+    put1(f, "sgd_n_iter", (double)n_iter);
+  }
+  std::fclose(f);
+  return 0;
+}

@@ -1,0 +1,108 @@
+"""The C++ API (include/frovedis_gb300.hpp): a program written against the
+reference's class and function names (tests/cpp/api_check.cpp) compiles,
+links against libfvg.so, and on a GPU gives the oracle's results.
+
+Tolerances as in test_gpu_parity: layouts bit for bit, FP64 products rel
+1e-12, FP32 products rel 2e-5, trained models rel 1e-6 (loss) / 1e-5
+(weights); the L-BFGS iteration count must match exactly."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from frovedis_gb300 import build as fb
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "api_check.cpp")
+
+
+def compile_check(out_dir):
+    lib = fb.build()
+    exe = os.path.join(str(out_dir), "api_check")
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), SRC,
+           "-o", exe, "-L", os.path.dirname(lib), "-lfvg", "-Wl,-rpath," + os.path.dirname(lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_cpp_api_compiles_and_links(tmp_path):
+    assert os.access(compile_check(tmp_path), os.X_OK)
+
+
+def _write_input(path, a, x, label):
+    with open(path, "w") as f:
+        f.write(f"{a.m} {a.n} {a.nnz}\n")
+        for arr in (a.off, a.idx):
+            f.write(" ".join(str(int(v)) for v in arr) + "\n")
+        for arr in (a.val, x, label):
+            f.write(" ".join(repr(float(v)) for v in arr) + "\n")
+
+
+def _read_output(path):
+    out = {}
+    for line in open(path):
+        parts = line.split()
+        out[parts[0]] = np.array([float(v) for v in parts[1:]])
+    return out
+
+
+def close(a, b, rtol):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape
+    return np.max(np.abs(a - b) / (np.abs(b) + 1.0)) <= rtol if a.size else True
+
+
+@pytest.mark.gpu
+def test_cpp_api_matches_oracle(tmp_path):
+    from frovedis_gb300 import datagen
+    m, n = 4000, 300
+    off, idx, val, label = datagen.generate(datagen.Spec(m=m, n=n, lam=15.0, seed=4))
+    a = oracle.CRS(m, n, off, idx, val)
+    x = np.random.default_rng(9).standard_normal(n)
+    inp, outp = tmp_path / "in.txt", tmp_path / "out.txt"
+    _write_input(inp, a, x, label)
+    exe = compile_check(tmp_path)
+    r = subprocess.run([exe, str(inp), str(outp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    o = _read_output(outp)
+
+    assert close(o["crs_mv"], oracle.spmv(a, x), 1e-12)
+    t = oracle.transpose(a)
+    assert np.array_equal(o["t_off"], t.off) and np.array_equal(o["t_idx"], t.idx)
+    assert np.array_equal(o["t_val"], t.val)
+    assert list(o["t_shape"]) == [n, m]
+    w, _, _ = oracle.ell_build(a)
+    assert int(o["ell_width"][0]) == w
+    assert close(o["ell_mv"], oracle.ell_spmv(a, x), 1e-12)
+    assert close(o["ell_trans"], oracle.ell_trans_mv(a, label), 1e-12)
+    perm, joff, _, _ = oracle.jds_build(a)
+    assert np.array_equal(o["jds_perm"], perm) and np.array_equal(o["jds_off"], joff)
+    assert close(o["jds_mv"], oracle.jds_spmv(a, x), 1e-12)
+    assert close(o["hyb_mv"], oracle.hyb_spmv(a, x), 1e-12)
+    assert int(o["hyb_crs_rows"][0]) == oracle.hyb_build(a)["crs_rows"]
+    X = x[:, None] * np.arange(1, 4)[None, :] + np.arange(3)[None, :]
+    assert close(o["spmm"], oracle.spmm(a, X).ravel(), 1e-12)
+    assert close(o["crs_mv_f32"], oracle.spmv_f32(a, x.astype(np.float32)), 2e-5)
+    assert o["mismatch_throws"][0] == 1
+
+    ro = oracle.logreg_lbfgs(a, label, num_iter=20, reg_type="L2", reg_param=1e-3, intercept=True)
+    assert int(o["lbfgs_n_iter"][0]) == ro["n_iter"]
+    assert np.max(np.abs(o["lbfgs_w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))
+    assert abs(o["lbfgs_b"][0] - ro["b"]) <= 1e-5 * max(1.0, abs(ro["b"]))
+    pb = oracle.predict_probability(a, ro["w"], ro["b"])
+    assert np.max(np.abs(o["lbfgs_prob"] - pb)) <= 1e-6
+    agree = np.mean(o["lbfgs_pred"] == np.where(pb >= 0.5, 1.0, -1.0))
+    assert agree >= 0.999
+    rh = oracle.logreg_lbfgs(a, label, num_iter=20, reg_type="ZERO", reg_param=1e-3, intercept=True, fmt="HYBRID")
+    assert np.max(np.abs(o["lbfgs_hyb_w"] - rh["w"])) <= 1e-5 * max(1.0, np.max(np.abs(rh["w"])))
+    assert abs(o["lbfgs_hyb_b"][0] - rh["b"]) <= 1e-5 * max(1.0, abs(rh["b"]))
+    assert o["lbfgs_jds_throws"][0] == 1
+    rs = oracle.logreg_sgd(a, label, num_iter=15, alpha=0.05, mini_batch_fraction=0.3, reg_type="L2",
+                           reg_param=1e-2, intercept=True)
+    assert int(o["sgd_n_iter"][0]) == rs["n_iter"]
+    assert np.max(np.abs(o["sgd_w"] - rs["w"])) <= 1e-5 * max(1.0, np.max(np.abs(rs["w"])))
+    assert abs(o["sgd_b"][0] - rs["b"]) <= 1e-5 * max(1.0, abs(rs["b"]))
