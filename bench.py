@@ -398,6 +398,7 @@ def run_regpath(args):
             ms, cnt = ctx.profile("batch_" + key)
             tot[key + "_ms"] += ms
             tot[key + "_n"] += cnt
+        tot["vec_ms"] = tot.get("vec_ms", 0.0) + ctx.profile("lbfgs_vec")[0]
         evals = ctx.profile("batch_pass1")[1]
         s_x = 8 if args.storage == "f64" else 4
         per_eval = (2 * nnz * (s_v + 4) + (m + n + 2) * 4 + n * 64 * s_x + 2 * m * 64 * s_x + m * 8
@@ -435,7 +436,8 @@ def run_regpath(args):
                     "achieved_gbs": tot["alg_bytes"] / (kms / 1e3) / 1e9 if kms else None, "hbm_peak_gbs": peak,
                     "peak_kind": peak_kind,
                     "achieved_tflops_fp32": tot["flops"] / (kms / 1e3) / 1e12 if kms else None,
-                    "pass1_ms": tot["pass1_ms"], "pass2_ms": tot["pass2_ms"]},
+                    "pass1_ms": tot["pass1_ms"], "pass2_ms": tot["pass2_ms"],
+                    "lbfgs_vector_ms": tot.get("vec_ms")},
         "wall_s": tot["batched_s"],
     }
     print(json.dumps(line), flush=True)

@@ -57,6 +57,7 @@ EXPORTS = [
     "fvg_matrix_get_jds", "fvg_matrix_get_hybrid", "fvg_spmv", "fvg_trans_mv", "fvg_spmm",
     "fvg_glm_params_default", "fvg_logreg_lbfgs", "fvg_logreg_sgd", "fvg_logreg_eval",
     "fvg_logreg_predict_probability", "fvg_spmv_no_alloc", "fvg_logreg_lbfgs_batched",
+    "fvg_multinomial_train", "fvg_multinomial_probability",
 ]
 
 _lib = None
@@ -108,6 +109,8 @@ def load(build_if_needed: bool = True):
         "fvg_logreg_predict_probability": ([_p, _p, _p, _dbl, _p], _int),
         "fvg_spmv_no_alloc": ([_p, _p, _int, _int, _p, _p], _int),
         "fvg_logreg_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
+        "fvg_multinomial_train": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, C.POINTER(_i64)], _int),
+        "fvg_multinomial_probability": ([_p, _p, _p, _p, _i64, _int, _p], _int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -399,6 +402,34 @@ def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=
     ctx.check(ctx.L.fvg_logreg_lbfgs_batched(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam),
                                              _ptr(w), _ptr(b), _ptr(n_iter), _ptr(loss)))
     return dict(w=w, b=b, n_iter=n_iter, loss=loss)
+
+
+def multinomial_train(mat: Matrix, label, nclasses, sample_weight=None, W0=None, b0=None, **kw):
+    """multinomial_logistic_regression::train (fvg_multinomial_train).  label:
+    class ids 0..nclasses-1; W0 (n, nclasses) and b0 (nclasses,) default to
+    zeros as in the reference's model constructor.  Returns W, b, n_iter."""
+    ctx = mat.ctx
+    K = int(nclasses)
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
+    W = np.zeros((mat.n, K)) if W0 is None else np.array(W0, dtype=np.float64, order="C")
+    b = np.zeros(K) if b0 is None else np.array(b0, dtype=np.float64, order="C")
+    kw["intercept"] = int(bool(kw.get("intercept", False)))
+    p = glm_params(**kw)
+    n_iter = _i64()
+    ctx.check(ctx.L.fvg_multinomial_train(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), K, _ptr(W), _ptr(b),
+                                          C.byref(n_iter)))
+    return dict(W=W, b=b, n_iter=n_iter.value)
+
+
+def multinomial_probability(mat: Matrix, W, b, intercept=False):
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    K = W.shape[1]
+    out = np.zeros((mat.m, K))
+    mat.ctx.check(mat.ctx.L.fvg_multinomial_probability(mat.ctx.h, mat.h, _ptr(W), _ptr(b), K, int(intercept),
+                                                        _ptr(out)))
+    return out
 
 
 def logreg_sgd(mat: Matrix, label, **kw):

@@ -118,7 +118,7 @@ __device__ __forceinline__ void col_reduce(double (&v)[NV], const bool (&is_max)
   const bool on = j < a.k;                     \
   const i64 rstep = (i64)gridDim.x * a.rpb;    \
   const i64 r0 = (i64)blockIdx.x * a.rpb + rr
-#define BROWS(r, nrows) for (i64 r = r0; r < (nrows); r += rstep)
+#define BROWS(r, nrows) _Pragma("unroll 4") for (i64 r = r0; r < (nrows); r += rstep)
 
 __device__ __forceinline__ i64 hslot(int rear, int i, int h) { return (i64)((rear + i) % h); }
 
@@ -404,6 +404,23 @@ __global__ void __launch_bounds__(kBT) kb_status(int k, const ColState* st, int*
   if (threadIdx.x == 0) ctl[1] = cnt[0];
 }
 
+// model-major [k][n] <-> column layout [n+1][k] (row n, the bias slot, is
+// left untouched by the forward copy)
+__global__ void kb_to_cols(const double* __restrict__ src, double* __restrict__ dst, i64 n, int k) {
+  for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (i64)gridDim.x * blockDim.x) {
+    const i64 i = e / k;
+    const int j = (int)(e - i * k);
+    dst[e] = src[(i64)j * n + i];
+  }
+}
+__global__ void kb_from_cols(const double* __restrict__ src, double* __restrict__ dst, i64 n, int k) {
+  for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (i64)gridDim.x * blockDim.x) {
+    const int j = (int)(e / n);
+    const i64 i = e - (i64)j * n;
+    dst[e] = src[i * k + j];
+  }
+}
+
 __global__ void kb_d2f(const double* __restrict__ s, float* __restrict__ d, i64 n) {
   for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) d[i] = (float)s[i];
 }
@@ -414,7 +431,7 @@ struct BatchEval {
   DevCRS* A = nullptr;
   DevCRS* AT = nullptr;
   i64 m = 0, n = 0;
-  int k = 0, storage = FVG_F64, icpt = 0;
+  int k = 0, storage = FVG_F64, icpt = 0, master = FVG_F64;
   const double* label = nullptr;
   const double* sw = nullptr;
   DBuf label_f, sw_f, R, s1, s2;
@@ -423,6 +440,7 @@ struct BatchEval {
     c = c_;
     A = &M->A;
     AT = M->AT.get();
+    master = M->master;
     m = A->m;
     n = A->n;
     k = k_;
@@ -439,8 +457,8 @@ struct BatchEval {
   }
   void set_storage(int st) {
     storage = st;
-    crs_ensure_plane(c, *A, storage, FVG_F64);
-    crs_ensure_plane(c, *AT, storage, FVG_F64);
+    crs_ensure_plane(c, *A, storage, master);
+    crs_ensure_plane(c, *AT, storage, master);
     R.alloc((size_t)(storage == FVG_F64 ? 8 : 4) * std::max<i64>(m * k, 1), c->stream);
     s1.alloc((size_t)spmm_scratch_bytes(c, *A, storage), c->stream);
     s2.alloc((size_t)spmm_scratch_bytes(c, *AT, storage), c->stream);
@@ -525,12 +543,14 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
   double* B0 = B.as<double>();
   double* B1 = B0 + kk;
 
-  // initial models: weight[j*n + i] -> W[i][j]; per-model state
+  const unsigned dg = (unsigned)std::max<i64>(1, std::min<i64>((n * kk + 255) / 256, 4 * (i64)c->num_sms));
+  // initial models: weight[j*n + i] -> W[i][j] (through NW as staging); per-model state
   {
-    std::vector<double> wt((size_t)n1 * kk, 0.0);
-    for (i64 j = 0; j < k; j++)
-      for (i64 i = 0; i < n; i++) wt[(size_t)i * kk + j] = w_h[(size_t)j * n + i];
-    FVG_CUDA(cudaMemcpyAsync(W.p, wt.data(), vec, cudaMemcpyHostToDevice, s));
+    FVG_CUDA(cudaMemcpyAsync(NW.p, w_h, sizeof(double) * (size_t)n * kk, cudaMemcpyHostToDevice, s));
+    FVG_CUDA(cudaMemsetAsync(W.p, 0, vec, s));
+    kb_to_cols<<<dg, 256, 0, s>>>(NW.as<double>(), W.as<double>(), n, kk);
+    check_launch("kb_to_cols");
+    count_launch(c);
     std::vector<ColState> cs((size_t)kk);
     for (int j = 0; j < kk; j++) {
       cs[j] = ColState{};
@@ -547,7 +567,6 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
   int* hctl = (int*)hp.p;
   double* hrms = (double*)((char*)hp.p + 256);
 
-  const unsigned dg = (unsigned)std::max<i64>(1, std::min<i64>((n * kk + 255) / 256, 4 * (i64)c->num_sms));
   auto weights_for = [&](const double* w) -> const void* {
     if (!mixed) return w;
     kb_d2f<<<dg, 256, 0, s>>>(w, WF.as<float>(), n * kk);
@@ -648,14 +667,15 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
     }
   }
   // results: W[i][j] -> weight[j*n + i]
-  std::vector<double> wt((size_t)n1 * kk);
+  kb_from_cols<<<dg, 256, 0, s>>>(W.as<double>(), NW.as<double>(), n, kk);
+  check_launch("kb_from_cols");
+  count_launch(c);
   std::vector<ColState> cs((size_t)kk);
-  FVG_CUDA(cudaMemcpyAsync(wt.data(), W.p, vec, cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaMemcpyAsync(w_h, NW.p, sizeof(double) * (size_t)n * kk, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(cs.data(), ST.p, sizeof(ColState) * kk, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(b_h, B0, sizeof(double) * kk, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));
   for (i64 j = 0; j < k; j++) {
-    for (i64 i = 0; i < n; i++) w_h[(size_t)j * n + i] = wt[(size_t)i * kk + j];
     n_iter_h[j] = cs[j].active ? p->num_iteration : cs[j].n_iter;
     loss_h[j] = cs[j].loss;
   }

@@ -18,6 +18,10 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
 void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                          const fvg_glm_params* p, i64 k, const double* lam_h, double* w_h, double* b_h,
                          i64* n_iter_h, double* loss_h);
+void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
+                       const fvg_glm_params* p, i64 K, double* w_h, double* b_h, i64* n_iter);
+void multinomial_probability(fvg_ctx* c, fvg_matrix* M, const double* w_h, const double* b_h, i64 K, int icpt_on,
+                             double* prob_h);
 int crs_blocks_per_sm();
 void sigmoid_probability(fvg_ctx* c, double* v, i64 m, double b);
 }  // namespace fvg
@@ -571,6 +575,28 @@ FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* c, fvg_matrix* M, const dou
   API_BEGIN
   own(c, M);
   lbfgs_batched_train(c, M, label, sample_weight, p, k, reg_params, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* p, int64_t nclasses,
+                                         double* weight, double* intercept, int64_t* n_iter) {
+  if (!c || !M || !weight || !intercept || !n_iter) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  multinomial_train(c, M, label, sample_weight, p, nclasses, weight, intercept, n_iter);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_multinomial_probability(fvg_ctx* c, fvg_matrix* M, const double* weight,
+                                               const double* intercept, int64_t nclasses, int intercept_on,
+                                               double* prob) {
+  if (!c || !M || !weight || !intercept || !prob) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  multinomial_probability(c, M, weight, intercept, nclasses, intercept_on, prob);
   check_device_error(c);
   API_END(c)
 }

@@ -207,6 +207,26 @@ FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const
                                             const double* sample_weight, const fvg_glm_params* params, int64_t k,
                                             const double* reg_params, double* weight, double* intercept,
                                             int64_t* n_iter, double* final_loss);
+/* multinomial_logistic_regression::train main API
+ * (ml/glm/multinomial_logistic_regression.hpp:342-378 → softmax_parallelizer::
+ * parallelize / do_train, softmax_parallelizer.hpp:210-242, 277-345):
+ * gradient descent with step alpha/sqrt(i) on the softmax error, the
+ * reference's intercept update (column sums of the gradient matrix) and its
+ * RMS-of-change stop test.  label[num_row] holds class ids 0..nclasses-1;
+ * weight[num_col*nclasses] (row-major, feature-major like the reference's
+ * rowmajor_matrix_local weight) and intercept[nclasses] hold the initial model
+ * on entry and the trained one on return.  params: num_iteration, alpha,
+ * reg_param, reg_type, intercept, convergence_tol, mat_type (CRS or HYBRID,
+ * both computed on the CRS layout), storage. */
+FVG_API fvg_status fvg_multinomial_train(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* params, int64_t nclasses,
+                                         double* weight, double* intercept, int64_t* n_iter);
+/* multinomial_logistic_regression_model<T>::compute_probability_matrix
+ * (multinomial_logistic_regression_model.hpp:82-89): prob[num_row*nclasses],
+ * FP64. */
+FVG_API fvg_status fvg_multinomial_probability(fvg_ctx* ctx, fvg_matrix* mat, const double* weight,
+                                               const double* intercept, int64_t nclasses, int intercept_on,
+                                               double* prob);
 /* logistic_regression_with_sgd::train main API
  * (ml/glm/logistic_regression_with_sgd.hpp:392-441 →
  *  sgd_parallelizer.hpp:132-378, 441-550). */

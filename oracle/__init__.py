@@ -62,6 +62,9 @@ def lib():
             "orc_logreg_sgd_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _i64, _dbl, _dbl,
                                    _dbl, _int, _int, _dbl, _p, _p, _p, _p, _int],
             "orc_predict_probability_f64": [_i64, _i64, _p, _p, _p, _p, _dbl, _p],
+            "orc_softmax_train_f64": [_i64, _i64, _p, _p, _p, _p, _p, _i64, _i64, _dbl, _dbl, _int, _int, _dbl,
+                                      _p, _p, _p],
+            "orc_softmax_probability_f64": [_i64, _i64, _p, _p, _p, _p, _p, _i64, _int, _p],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -71,6 +74,7 @@ def lib():
         L.orc_ell_width.restype = _i64
         L.orc_logreg_lbfgs_f64.restype = _int
         L.orc_logreg_sgd_f64.restype = _int
+        L.orc_softmax_train_f64.restype = _int
     return _lib
 
 
@@ -275,6 +279,31 @@ def logreg_sgd(a: CRS, label, num_iter=1000, alpha=0.01, mini_batch_fraction=1.0
     if rc != 0:
         raise ValueError(f"oracle sgd rejected the arguments (code {rc})")
     return dict(w=w, b=float(b[0]), n_iter=int(n_iter[0]), loss=float(loss[0]))
+
+
+def softmax_train(a: CRS, label, K, num_iter=1000, alpha=0.01, reg_param=0.01, reg_type="ZERO", intercept=False,
+                  tol=0.001, sw=None, W0=None, b0=None):
+    """``multinomial_logistic_regression::train`` semantics (CRS); returns a dict
+    with W (n, K), b (K), n_iter.  Labels are class ids 0..K-1."""
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
+    W = np.zeros((a.n, K)) if W0 is None else np.array(W0, dtype=np.float64, order="C")
+    b = np.zeros(K) if b0 is None else np.array(b0, dtype=np.float64)
+    n_iter = np.zeros(1, dtype=np.int64)
+    rc = lib().orc_softmax_train_f64(*a.args(), _ptr(label), _ptr(sw), K, num_iter, alpha, reg_param, REG[reg_type],
+                                     int(intercept), tol, _ptr(W), _ptr(b), _ptr(n_iter))
+    if rc != 0:
+        raise ValueError(f"oracle softmax rejected the arguments (code {rc})")
+    return dict(W=W, b=b, n_iter=int(n_iter[0]))
+
+
+def softmax_probability(a: CRS, W, b, intercept=False) -> np.ndarray:
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    K = W.shape[1]
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.zeros((a.m, K))
+    lib().orc_softmax_probability_f64(*a.args(), _ptr(W), _ptr(b), K, int(intercept), _ptr(out))
+    return out
 
 
 def predict_probability(a: CRS, w, b=0.0) -> np.ndarray:

@@ -754,6 +754,88 @@ void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, 
   final_loss = sumloss;
 }
 
+// ------------------------------------------------------------ multinomial
+// softmax_gradient_descent (ml/glm/softmax_gradient_descent.hpp): compute_wtx
+// (159-177: data * weight, then + icpt per column), compute_exp_matrix
+// (179-213, the max-stabilised branch: row max starting from column 0, then
+// exp(x - max)), compute_softmax_probability (192-215: sum_of_cols, i.e. the
+// row sums in column order, rowmajor_matrix.hpp:600-625, then diag(1/sum) *
+// mat, rowmajor_matrix.hpp:452-480).
+template <class T>
+void softmax_probability(const CRS<T>& a, const std::vector<T>& W, const T* icpt, bool use_icpt, i64 K,
+                         std::vector<T>& P) {
+  const i64 m = a.nrow;
+  P.assign((size_t)(m * K), T(0));
+  crs_spmm(a, W.data(), K, P.data());
+  if (use_icpt)
+    for (i64 j = 0; j < K; j++)
+      for (i64 i = 0; i < m; i++) P[i * K + j] = P[i * K + j] + icpt[j];
+  for (i64 i = 0; i < m; i++) {
+    T* row = &P[i * K];
+    T mx = row[0];
+    for (i64 j = 1; j < K; j++)
+      if (row[j] > mx) mx = row[j];
+    for (i64 j = 0; j < K; j++) row[j] = std::exp(row[j] - mx);
+    T sum = 0;
+    for (i64 j = 0; j < K; j++) sum = sum + row[j];
+    const T inv = 1 / sum;
+    for (i64 j = 0; j < K; j++) row[j] = inv * row[j];
+  }
+}
+
+// softmax_parallelizer::do_train with the transposed copy
+// (softmax_parallelizer.hpp:210-242): per iteration the gradient
+// trans * ((softmax - onehot(label)) * sw) (compute_error_inplace 217-235),
+// then update_global_model (147-200): w -= alpha/sqrt(i) * g, intercept -=
+// alpha/sqrt(i) * sum_of_rows(g) (the column sums of the gradient matrix,
+// rowmajor_matrix.hpp:555-565), regularize(w) with eta = 1, and the
+// _CONV_RATE_CHECK_ test (common.hpp:21): RMS of the change of weights and
+// intercepts over (nfeatures [+1]) * nclasses entries <= tol stops.
+template <class T>
+void softmax_train(const CRS<T>& a, const T* label, const T* sw, i64 K, i64 num_iter, double alpha, T lambda,
+                   int rtype, bool icpt, double tol, std::vector<T>& W, std::vector<T>& b, i64& n_iter) {
+  const i64 m = a.nrow, n = a.ncol;
+  const CRS<T> t = transpose(a);
+  std::vector<T> P, G;
+  i64 i;
+  for (i = 1; i <= num_iter; i++) {
+    softmax_probability(a, W, b.data(), icpt, K, P);
+    for (i64 j = 0; j < K; j++)
+      for (i64 r = 0; r < m; r++) {
+        P[r * K + j] -= (label[r] == (T)j) ? T(1) : T(0);
+        P[r * K + j] *= sw[r];
+      }
+    G.assign((size_t)(n * K), T(0));
+    crs_spmm(t, P.data(), K, G.data());
+    const std::vector<T> Wp = W, bp = b;
+    const T ra = alpha / std::sqrt((double)i);
+    for (i64 e = 0; e < n * K; e++) W[e] = W[e] - ra * G[e];
+    if (icpt) {
+      std::vector<T> bias(K, T(0));
+      for (i64 r = 0; r < n; r++)
+        for (i64 j = 0; j < K; j++) bias[j] = bias[j] + G[r * K + j];
+      for (i64 j = 0; j < K; j++) b[j] = b[j] - ra * bias[j];
+    }
+    regularize(W, rtype, lambda, 1.0);
+    T sum = 0;
+    for (i64 e = 0; e < n * K; e++) {
+      const T d = W[e] - Wp[e];
+      sum = sum + d * d;
+    }
+    i64 nft = n;
+    if (icpt) {
+      for (i64 j = 0; j < K; j++) {
+        const T d = b[j] - bp[j];
+        sum = sum + d * d;
+      }
+      nft++;
+    }
+    const T rmse = std::sqrt(sum / (T)(nft * K));
+    if (rmse <= tol) break;
+  }
+  n_iter = (i == num_iter + 1) ? num_iter : i;
+}
+
 template <class T>
 CRS<T> make_crs(i64 m, i64 n, const i32* off, const i32* idx, const T* val) {
   CRS<T> a;
@@ -950,6 +1032,35 @@ void orc_predict_probability_f64(i64 m, i64 n, const i32* off, const i32* idx, c
     double e = -1.0 * v[i];
     out[i] = (e > 709) ? 0.0 : 1.0 / (1.0 + std::exp(e));
   }
+}
+
+// multinomial_logistic_regression::train main API
+// (ml/glm/multinomial_logistic_regression.hpp:342-378) with CRS data:
+// W[n*K] row-major and b[K] hold the initial model and receive the result.
+int orc_softmax_train_f64(i64 m, i64 n, const i32* off, const i32* idx, const double* val, const double* label,
+                          const double* sw, i64 K, i64 num_iter, double alpha, double lambda, int rtype, int icpt,
+                          double tol, double* W, double* b, i64* n_iter) {
+  if (num_iter < 1 || alpha <= 0 || lambda < 0 || tol < 0 || K < 1) return 1;
+  auto a = make_crs<double>(m, n, off, idx, val);
+  std::vector<double> w(W, W + n * K), bb(b, b + K), ones;
+  if (!sw) {
+    ones.assign((size_t)m, 1.0);
+    sw = ones.data();
+  }
+  softmax_train(a, label, sw, K, num_iter, alpha, lambda, rtype, icpt != 0, tol, w, bb, *n_iter);
+  std::copy(w.begin(), w.end(), W);
+  std::copy(bb.begin(), bb.end(), b);
+  return 0;
+}
+
+// multinomial_logistic_regression_model<T>::compute_probability_matrix
+// (multinomial_logistic_regression_model.hpp:82-89): prob[m*K].
+void orc_softmax_probability_f64(i64 m, i64 n, const i32* off, const i32* idx, const double* val, const double* W,
+                                 const double* b, i64 K, int icpt, double* prob) {
+  auto a = make_crs<double>(m, n, off, idx, val);
+  std::vector<double> w(W, W + n * K), P;
+  softmax_probability(a, w, b, icpt != 0, K, P);
+  std::copy(P.begin(), P.end(), prob);
 }
 
 }  // extern "C"

@@ -52,6 +52,11 @@ int orc_logreg_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const 
                        double* w, double* b, int64_t* n_iter, double* final_loss, int flags);
 void orc_predict_probability_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
                                  const double* val, const double* w, double b, double* out);
+int orc_softmax_train_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                          const double* label, const double* sw, int64_t K, int64_t num_iter, double alpha,
+                          double lambda, int rtype, int icpt, double tol, double* W, double* b, int64_t* n_iter);
+void orc_softmax_probability_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                                 const double* W, const double* b, int64_t K, int icpt, double* prob);
 #ifdef __cplusplus
 }
 #endif
