@@ -249,6 +249,34 @@ def test_fused_eval_matches_oracle(ctx, fmt):
             assert g[-1] == 0.0
 
 
+@pytest.mark.parametrize("n", [300, 20000])
+def test_fp32_eval_matches_fp64_on_fp32_values(ctx, n):
+    # Values are FP32- (BF16-) representable, so the FP64 evaluation is the
+    # exact reference and the only difference is FP32 arithmetic; n = 300
+    # gives dense Zipf-hot columns, n = 20000 a long tail.
+    from frovedis_gb300 import datagen
+    off, idx, val, label = datagen.generate(datagen.Spec(m=6000, n=n, lam=30.0, seed=8))
+    val = val.astype(np.float32).astype(np.float64)
+    A = ctx.matrix(6000, n, off, idx, val)
+    rng = np.random.default_rng(9)
+    w = rng.standard_normal(n) * 0.2
+    g64, l64 = fv.logreg_eval(A, label, w, b=0.3, intercept=True)
+    aref = oracle.CRS(6000, n, off, idx, np.abs(val))
+    scale = oracle.spmv(oracle.transpose(aref), np.ones(6000))  # sum |a_ij| per column
+    for storage in ("f32", "bf16"):
+        if storage == "bf16":
+            vb = (fv.bf16_bits(val).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+            B = ctx.matrix(6000, n, off, idx, vb)
+            g64b, l64b = fv.logreg_eval(B, label, w, b=0.3, intercept=True)
+            g, loss = fv.logreg_eval(B, label, w, b=0.3, intercept=True, storage="bf16")
+        else:
+            g64b, l64b = g64, l64
+            g, loss = fv.logreg_eval(A, label, w, b=0.3, intercept=True, storage="f32")
+        assert abs(loss - l64b) <= 1e-5 * abs(l64b), storage
+        assert np.max(np.abs(g[:-1] - g64b[:-1]) / (scale + 1.0)) <= 1e-5, storage
+        assert abs(g[-1] - g64b[-1]) <= 1e-5 * 6000, storage
+
+
 def test_fused_eval_extreme_margins(ctx):
     # z > 18, z < -18 and the clip branches of compute_dloss (gradient.hpp:29-48)
     a, label = _lr_data(3, m=2000, n=50)
