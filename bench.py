@@ -256,20 +256,29 @@ def run_gpu(args):
     h2d = (m + 1) * 4 + nnz * 12 + m * 8 + n * 8
     d2h = n * 8 + 16
     torch.cuda.synchronize()
+    phases = {"upload_s": 0.0, "train_s": 0.0}  # train includes the transposed build
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         B = ctx.matrix(m, n, off, idx, val)
         if args.storage != "f64":
             B.add_storage(args.storage)
+        ctx.synchronize()
+        t1 = time.perf_counter()
         rr = fv.logreg_lbfgs(B, label, **kw)
         B.close()
         ctx.synchronize()
-        e2e_ms += (time.perf_counter() - t0) * 1e3
+        t2 = time.perf_counter()
+        phases["upload_s"] += t1 - t0
+        phases["train_s"] += t2 - t1
+        e2e_ms += (t2 - t0) * 1e3
         e2e_iters += rr["n_iter"]
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
     spmv = None if args.skip_spmv else spmv_suite(ctx, args)
+    # batched training on the first datasets of the regularisation path
+    # (`--workload regpath` runs all 16)
+    rp = None if args.skip_regpath else regpath(args, args.regpath_datasets, 20)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = cpu_baseline(off, idx, val, label, spec, args, threads=0, sample_rows=args.cpu_rows)
@@ -297,11 +306,13 @@ def run_gpu(args):
                      "passes": {k: {"launches": prof[k][1], "ms_avg": prof[k][0] / max(prof[k][1], 1),
                                     "gbs": alg[k] * prof[k][1] / max(prof[k][0], 1e-9) / 1e6}
                                 for k in prof if prof[k][1]}},
-        "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "phases": {k: v / max(args.e2e_steps, 1) for k, v in phases.items()}},
         "gpu_launches": launches,
         "clocks": ck,
         "precision_modes": modes,
         "spmv_2m": spmv,
+        "batched_regpath": rp,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -358,17 +369,17 @@ def spmv_suite(ctx, args, reps=10):
     return out
 
 
-def run_regpath(args):
+def regpath(args, datasets, iters):
     """Batched regularisation path: 16 datasets (500,000 columns, 1.4e7 rows
     in all, 7e8 nonzeros), 64 L2 values log-spaced 1e-6..1 trained together
-    per dataset, `--iters` iterations (default 20).  Compared with the plain
-    FP64 GPU path run one model at a time (timed on 4 of the 64 values per
-    dataset and scaled by 16) at the same final losses."""
+    per dataset, `iters` iterations.  Compared with the plain FP64 GPU path
+    run one model at a time (timed on 4 of the 64 values per dataset and
+    scaled by 16) at the same final losses."""
     import torch
 
     import frovedis_gb300 as fv
     from frovedis_gb300 import datagen
-    specs = datagen.regpath_datasets(args.datasets, args.scale)
+    specs = datagen.regpath_datasets(datasets, args.scale)
     lams = np.logspace(-6, 0, 64)
     probe = [0, 21, 42, 63]
     ctx = fv.Context(0)
@@ -384,7 +395,7 @@ def run_regpath(args):
         if args.storage != "f64":
             A.add_storage(args.storage)
             A.add_storage("f32")
-        kw = dict(num_iter=args.iters, reg_type="L2", w0=np.zeros(n))
+        kw = dict(num_iter=iters, reg_type="L2", w0=np.zeros(n))
         fv.logreg_lbfgs_batched(A, label, lams[:2], storage=args.storage, **dict(kw, num_iter=2))
         torch.cuda.synchronize()
         ctx.reset_profile()
@@ -419,7 +430,7 @@ def run_regpath(args):
         A.close()
     ctx.close()
     value = tot["batched_model_iters"] / tot["batched_s"]
-    base = len(specs) * len(lams) * args.iters / tot["fp64_single_s_est"]
+    base = len(specs) * len(lams) * iters / tot["fp64_single_s_est"]
     kms = tot["pass1_ms"] + tot["pass2_ms"]
     peak, peak_kind = load_peak()
     line = {
@@ -427,7 +438,7 @@ def run_regpath(args):
         "value": value, "unit": "model-iters/s", "higher_is_better": True,
         "config": {"workload": "logreg-regpath-16x500k-64lambda", "datasets": len(specs), "rows": tot["rows"],
                    "cols": specs[0].n, "nnz": tot["nnz"], "models_per_dataset": 64,
-                   "iterations": args.iters, "storage": args.storage},
+                   "iterations": iters, "storage": args.storage},
         "fp64_single_model_gpu": {"value": base, "unit": "model-iters/s",
                                   "note": "plain FP64 path, one model per call; 4 of 64 values timed per dataset"},
         "speedup_vs_fp64_single": value / base,
@@ -439,6 +450,82 @@ def run_regpath(args):
                     "pass1_ms": tot["pass1_ms"], "pass2_ms": tot["pass2_ms"],
                     "lbfgs_vector_ms": tot.get("vec_ms")},
         "wall_s": tot["batched_s"],
+    }
+    return line
+
+
+def run_regpath(args):
+    print(json.dumps(regpath(args, args.datasets, args.iters)), flush=True)
+
+
+def run_multinomial(args):
+    """Multinomial logistic regression: 5,000,000 x 2,000,000, nnz/row
+    1+Poisson(99), Zipf(1.1) columns, |N(0,1)| values, 128 classes sampled
+    from softmax(X W*) with W* ~ N(0, 0.1^2) (Gumbel-max on the device),
+    `--iters` iterations (default 30) of the reference's gradient descent.
+    BF16 (or --storage) values against the plain FP64 path on the same data."""
+    import torch
+
+    import frovedis_gb300 as fv
+    from frovedis_gb300 import datagen
+    K = 128
+    spec = datagen.Spec(m=int(5_000_000 * args.scale), n=int(2_000_000 * args.scale), lam=99.0, col_kind="zipf",
+                        s_col=1.1, val_kind="absnormal", labels=False, seed=5)
+    off, idx, val, _ = datagen.generate(spec)
+    m, n, nnz = spec.m, spec.n, int(off[-1])
+    ctx = fv.Context(0)
+    A = ctx.matrix(m, n, off, idx, val)
+    del val
+    A.prepare("CRS", transpose=True)
+    A.add_storage("f32")
+    if args.storage == "bf16":
+        A.add_storage("bf16")
+    g = torch.Generator(device="cuda").manual_seed(7)
+    Wt = (torch.randn(n, K, device="cuda", generator=g) * 0.1).contiguous()
+    Z = torch.empty(m, K, device="cuda")
+    torch.cuda.synchronize()
+    A.spmm_device(Wt.data_ptr(), K, Z.data_ptr(), storage="f32", vec="f32")
+    gum = -torch.log(-torch.log(torch.rand(m, K, device="cuda", generator=g).clamp_(1e-20, 1.0)))
+    label = torch.argmax(Z + gum, dim=1).to(torch.float64).cpu().numpy()
+    del Wt, Z, gum
+    torch.cuda.empty_cache()
+    kw = dict(num_iter=args.iters, alpha=1e-5, tol=0.0)
+    out = {}
+    for storage in (args.storage, "f64"):
+        fv.multinomial_train(A, label, K, storage=storage, **dict(kw, num_iter=1))
+        ctx.reset_profile()
+        ctx.set_profiling(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fv.multinomial_train(A, label, K, storage=storage, **kw)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ctx.set_profiling(False)
+        p1, n1 = ctx.profile("batch_pass1")
+        p2, n2 = ctx.profile("batch_pass2")
+        vec_ms, _ = ctx.profile("lbfgs_vec")
+        s_v = {"f64": 8, "f32": 4, "bf16": 2}[storage]
+        s_x = 8 if storage == "f64" else 4
+        b1 = nnz * (s_v + 4) + (m + 1) * 4 + n * K * s_x + m * K * s_x + m * 8   # X W, P written
+        b2 = nnz * (s_v + 4) + (n + 1) * 4 + m * K * s_x + n * K * 8             # X^T P, G written
+        out[storage] = {"iters_per_s": r["n_iter"] / dt, "n_iter": r["n_iter"], "W": r["W"],
+                        "pass1_ms_avg": p1 / max(n1, 1), "pass2_ms_avg": p2 / max(n2, 1),
+                        "update_ms_avg": vec_ms / max(r["n_iter"], 1),
+                        "pass1_gbs": b1 * n1 / max(p1, 1e-9) / 1e6, "pass2_gbs": b2 * n2 / max(p2, 1e-9) / 1e6,
+                        "tflops_fp32_equiv": 4.0 * nnz * K * n1 / max(p1 + p2, 1e-9) / 1e9}
+    w64 = out["f64"].pop("W")
+    wlo = out[args.storage].pop("W")
+    A.close()
+    ctx.close()
+    peak, peak_kind = load_peak()
+    line = {
+        "metric": "multinomial logistic regression iterations/s (128 classes)", "value": out[args.storage]["iters_per_s"],
+        "unit": "iters/s", "higher_is_better": True,
+        "config": {"workload": "multinomial-5Mx2M-128classes", "rows": m, "cols": n, "nnz": nnz, "classes": K,
+                   "iterations": args.iters, "storage": args.storage, "alpha": kw["alpha"]},
+        "modes": out, "speedup_vs_fp64": out[args.storage]["iters_per_s"] / out["f64"]["iters_per_s"],
+        "weight_rel_diff_vs_fp64": float(np.max(np.abs(wlo - w64)) / max(np.max(np.abs(w64)), 1e-300)),
+        "hbm_peak_gbs": peak, "peak_kind": peak_kind,
     }
     print(json.dumps(line), flush=True)
 
@@ -518,13 +605,20 @@ def main():
     ap.add_argument("--skip-spmv", action="store_true")
     ap.add_argument("--spmv-scale", type=float, default=1.0)
     ap.add_argument("--spmv-only", action="store_true", help="run only the SpMV kernel suite")
-    ap.add_argument("--workload", default="lbfgs", choices=["lbfgs", "regpath"])
+    ap.add_argument("--workload", default="lbfgs", choices=["lbfgs", "regpath", "multinomial"])
     ap.add_argument("--datasets", type=int, default=16, help="regpath: number of datasets")
+    ap.add_argument("--regpath-datasets", type=int, default=4, help="datasets of the batched summary line")
+    ap.add_argument("--skip-regpath", action="store_true")
     args = ap.parse_args()
     if args.workload == "regpath":
         if args.iters == 50:
             args.iters = 20
         run_regpath(args)
+        return
+    if args.workload == "multinomial":
+        if args.iters == 50:
+            args.iters = 30
+        run_multinomial(args)
         return
     if args.spmv_only:
         import frovedis_gb300 as fv

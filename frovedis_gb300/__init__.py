@@ -267,6 +267,11 @@ class Matrix:
         self.ctx.check(self.ctx.L.fvg_trans_mv(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), xptr, yptr,
                                                1))
 
+    def spmm_device(self, xptr, k, yptr, fmt="CRS", storage="f64", vec="f64"):
+        """Y = A X with X (num_col x k) and Y (num_row x k) row-major device arrays."""
+        self.ctx.check(self.ctx.L.fvg_spmm(self.ctx.h, self.h, _fmt(fmt), _dt(storage), _dt(vec), xptr, int(k), yptr,
+                                           1))
+
     def spmm(self, X, fmt="CRS", storage="f64", vec="f64"):
         vd = np.float64 if _dt(vec) == F64 else np.float32
         X = np.ascontiguousarray(X, dtype=vd)

@@ -14,6 +14,8 @@
 //   logistic_regression_model<T>       ml/glm/linear_model.hpp:306-446
 //   logistic_regression_with_lbfgs::train   ml/glm/logistic_regression_with_lbfgs.hpp:8-437
 //   logistic_regression_with_sgd::train     ml/glm/logistic_regression_with_sgd.hpp:8-441
+//   multinomial_logistic_regression::train  ml/glm/multinomial_logistic_regression.hpp:8-378
+//   multinomial_logistic_regression_model<T> ml/glm/multinomial_logistic_regression_model.hpp:10-258
 //   MatType, RegType                   ml/utility/mattype.hpp:6-11, ml/glm/regularizer.hpp:8-12
 //
 // The matrices keep the reference's public fields (val, idx, off, perm,
@@ -25,6 +27,7 @@
 #ifndef FROVEDIS_GB300_HPP
 #define FROVEDIS_GB300_HPP
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -441,6 +444,128 @@ struct logistic_regression_with_sgd {
                            miniBatchFraction, regParam, regTyp, isIntercept, convergenceTol, mType);
     if (inputMovable) data.clear();
     return m;
+  }
+};
+
+// multinomial_logistic_regression_model<T>
+// (ml/glm/multinomial_logistic_regression_model.hpp:10-258)
+template <class T>
+struct multinomial_logistic_regression_model {
+  multinomial_logistic_regression_model() : nfeatures(0), nclasses(0), isIntercept(false), threshold(0.5) {}
+  multinomial_logistic_regression_model(size_t feature, size_t classes, bool isIcpt = false, double thr = 0.5)
+      : weight(feature, classes), intercept(classes, 0), nfeatures(feature), nclasses(classes),
+        isIntercept(isIcpt), threshold(thr) {}
+  // softmax(X W + intercept), num_row x nclasses (lines 82-89)
+  template <class I, class O>
+  rowmajor_matrix_local<T> compute_probability_matrix(const crs_matrix_local<T, I, O>& mat) const {
+    rowmajor_matrix_local<T> ret(mat.local_num_row, nclasses);
+    if (mat.local_num_row == 0 || nclasses == 0) return ret;
+    crs_matrix_local<double, I, O> m64;
+    m64.local_num_row = mat.local_num_row;
+    m64.local_num_col = mat.local_num_col;
+    m64.val.assign(mat.val.begin(), mat.val.end());
+    m64.idx = mat.idx;
+    m64.off = mat.off;
+    frovedis_gb300::device_matrix d(m64);
+    std::vector<double> w(weight.val.begin(), weight.val.end()), b(intercept.begin(), intercept.end());
+    std::vector<double> prob(mat.local_num_row * nclasses);
+    frovedis_gb300::check(fvg_multinomial_probability(frovedis_gb300::context(), d.h, w.data(), b.data(),
+                                                      (int64_t)nclasses, isIntercept, prob.data()));
+    ret.val.assign(prob.begin(), prob.end());
+    return ret;
+  }
+  // arg max class per row, ties to the lower class; a cleared threshold
+  // returns the winning probability instead (lines 91-112)
+  template <class I, class O>
+  std::vector<T> predict(const crs_matrix_local<T, I, O>& mat) const {
+    auto p = compute_probability_matrix(mat);
+    const size_t m = mat.local_num_row;
+    std::vector<T> lbl(m, 0), proba(m, 0);
+    for (size_t i = 0; i < m; i++) proba[i] = p.val[i * nclasses];
+    for (size_t j = 1; j < nclasses; j++)
+      for (size_t i = 0; i < m; i++)
+        if (p.val[i * nclasses + j] > proba[i]) {
+          lbl[i] = (T)j;
+          proba[i] = p.val[i * nclasses + j];
+        }
+    return threshold == (T)NONE ? proba : lbl;
+  }
+  template <class I, class O>
+  std::vector<T> predict_probability(const crs_matrix_local<T, I, O>& mat, bool = false) {
+    const T thr = threshold;
+    threshold = NONE;
+    auto r = predict(mat);
+    threshold = thr;
+    return r;
+  }
+  size_t get_num_features() const { return nfeatures; }
+  size_t get_num_classes() const { return nclasses; }
+  T get_threshold() const { return threshold; }
+  void set_threshold(T thr) { threshold = thr; }
+  rowmajor_matrix_local<T> weight;  // nfeatures x nclasses
+  std::vector<T> intercept;
+  size_t nfeatures, nclasses;
+  bool isIntercept;
+  T threshold;
+};
+
+// multinomial_logistic_regression (ml/glm/multinomial_logistic_regression.hpp)
+struct multinomial_logistic_regression {
+  template <class T, class I, class O>
+  static multinomial_logistic_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                                         size_t numIteration = 1000, double alpha = 0.01,
+                                                         double regParam = 0.01, RegType regTyp = ZERO,
+                                                         bool isIntercept = false, double convergenceTol = 0.001,
+                                                         MatType mType = CRS) {
+    // compute_nclasses: the number of distinct labels (line 238-240)
+    std::vector<T> u(label);
+    std::sort(u.begin(), u.end());
+    const size_t nclasses = (size_t)(std::unique(u.begin(), u.end()) - u.begin());
+    multinomial_logistic_regression_model<T> initModel(data.local_num_col, nclasses, isIntercept);
+    std::vector<T> sample_weight;
+    size_t n_iter = 0;
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, regParam, regTyp, isIntercept,
+                 convergenceTol, mType);
+  }
+  // main API (lines 342-378)
+  template <class T, class I, class O>
+  static multinomial_logistic_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                                         multinomial_logistic_regression_model<T>& initModel,
+                                                         std::vector<T>& sample_weight, size_t& n_iter,
+                                                         size_t numIteration = 1000, double alpha = 0.01,
+                                                         double regParam = 0.01, RegType regTyp = ZERO,
+                                                         bool isIntercept = false, double convergenceTol = 0.001,
+                                                         MatType mType = CRS, bool inputMovable = false) {
+    if (data.local_num_col != initModel.get_num_features())
+      throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Incompatible Test Vector with Provided Initial Model\n");
+    if (data.local_num_row != label.size())
+      throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Number of label and data are different\n");
+    if (sample_weight.empty()) sample_weight.assign(data.local_num_row, 1);
+    frovedis_gb300::device_matrix d(data);
+    fvg_glm_params p;
+    fvg_glm_params_default(&p);
+    p.num_iteration = (int64_t)numIteration;
+    p.alpha = alpha;
+    p.reg_param = regParam;
+    p.reg_type = regTyp;
+    p.intercept = isIntercept;
+    p.convergence_tol = convergenceTol;
+    p.mat_type = mType;
+    p.storage = frovedis_gb300::dtype_of<T>::value;
+    const size_t K = initModel.get_num_classes();
+    std::vector<double> lab(label.begin(), label.end()), sw(sample_weight.begin(), sample_weight.end());
+    std::vector<double> w(initModel.weight.val.begin(), initModel.weight.val.end());
+    std::vector<double> b(initModel.intercept.begin(), initModel.intercept.end());
+    int64_t it = 0;
+    frovedis_gb300::check(fvg_multinomial_train(frovedis_gb300::context(), d.h, lab.data(), sw.data(), &p,
+                                                (int64_t)K, w.data(), b.data(), &it));
+    n_iter = (size_t)it;
+    multinomial_logistic_regression_model<T> ret = initModel;
+    ret.weight.val.assign(w.begin(), w.end());
+    ret.intercept.assign(b.begin(), b.end());
+    ret.isIntercept = isIntercept;
+    if (inputMovable) data.clear();
+    return ret;
   }
 };
 

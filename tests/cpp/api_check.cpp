@@ -124,6 +124,21 @@ int main(int argc, char** argv) {
     put1(f, "sgd_b", model.intercept);
     put1(f, "sgd_n_iter", (double)n_iter);
   }
+  {
+    // multinomial: five classes assigned round-robin to the rows
+    std::vector<double> cls(m);
+    for (size_t i = 0; i < m; i++) cls[i] = (double)(i % 5);
+    multinomial_logistic_regression_model<double> init(n, 5, false);
+    std::vector<double> sw;
+    size_t n_iter = 0;
+    auto model = multinomial_logistic_regression::train(A, cls, init, sw, n_iter, 12, 0.05, 1e-3, L2, false, 0.0,
+                                                        CRS);
+    put(f, "mlr_w", model.weight.val);
+    put1(f, "mlr_n_iter", (double)n_iter);
+    put(f, "mlr_prob", model.compute_probability_matrix(A).val);
+    put(f, "mlr_pred", model.predict(A));
+    put(f, "mlr_maxprob", model.predict_probability(A));
+  }
   std::fclose(f);
   return 0;
 }
