@@ -111,8 +111,10 @@ def test_cpp_api_matches_oracle(tmp_path):
     rm = oracle.softmax_train(a, cls, 5, num_iter=12, alpha=0.05, reg_param=1e-3, reg_type="L2", tol=0.0)
     assert int(o["mlr_n_iter"][0]) == rm["n_iter"]
     W = o["mlr_w"].reshape(n, 5)
-    assert np.max(np.abs(W - rm["W"])) <= 1e-9 * max(1.0, np.max(np.abs(rm["W"])))
+    # 12 unnormalised gradient steps grow |W| to ~25: rounding differences
+    # of the summation order reach ~1e-9 of that
+    assert np.max(np.abs(W - rm["W"])) <= 1e-8 * max(1.0, np.max(np.abs(rm["W"])))
     P = oracle.softmax_probability(a, rm["W"], rm["b"])
-    assert np.max(np.abs(o["mlr_prob"].reshape(m, 5) - P)) <= 1e-9
+    assert np.max(np.abs(o["mlr_prob"].reshape(m, 5) - P)) <= 1e-7
     assert np.mean(o["mlr_pred"] == np.argmax(P, 1)) >= 0.999
-    assert np.max(np.abs(o["mlr_maxprob"] - P.max(1))) <= 1e-9
+    assert np.max(np.abs(o["mlr_maxprob"] - P.max(1))) <= 1e-7
