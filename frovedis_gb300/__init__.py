@@ -58,6 +58,8 @@ EXPORTS = [
     "fvg_glm_params_default", "fvg_logreg_lbfgs", "fvg_logreg_sgd", "fvg_logreg_eval",
     "fvg_logreg_predict_probability", "fvg_spmv_no_alloc", "fvg_logreg_lbfgs_batched",
     "fvg_multinomial_train", "fvg_multinomial_probability",
+    "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
+    "fvg_matrix_load_binary",
 ]
 
 _lib = None
@@ -111,6 +113,11 @@ def load(build_if_needed: bool = True):
         "fvg_logreg_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
         "fvg_multinomial_train": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, C.POINTER(_i64)], _int),
         "fvg_multinomial_probability": ([_p, _p, _p, _p, _i64, _int, _p], _int),
+        "fvg_matrix_get_crs": ([_p, _p, _p, _p, _p], _int),
+        "fvg_matrix_load_text": ([_p, C.c_char_p, _int, _i64, C.POINTER(_p)], _int),
+        "fvg_matrix_load_libsvm": ([_p, C.c_char_p, _int, _int, C.POINTER(_p)], _int),
+        "fvg_matrix_get_labels": ([_p, _p], _int),
+        "fvg_matrix_load_binary": ([_p, C.c_char_p, _int, C.c_char_p, C.c_char_p, C.POINTER(_p)], _int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -189,6 +196,41 @@ class Context:
 
     def matrix(self, m, n, off, idx, val, on_device=False):
         return Matrix(self, m, n, off, idx, val, on_device=on_device)
+
+    def _wrap(self, h, dt):
+        M = Matrix.__new__(Matrix)
+        M.ctx = self
+        M.h = h
+        M.master = dt
+        r, c = _i64(), _i64()
+        self.check(self.L.fvg_matrix_info(h, C.byref(r), C.byref(c), None))
+        M.m, M.n = r.value, c.value
+        M._keep = None
+        return M
+
+    def load_text(self, path, dtype="f64", num_col=-1):
+        """make_crs_matrix_local_load: "col:value" lines parsed on the device."""
+        h = _p()
+        self.check(self.L.fvg_matrix_load_text(self.h, str(path).encode(), _dt(dtype), int(num_col), C.byref(h)))
+        return self._wrap(h, _dt(dtype))
+
+    def load_libsvm(self, path, dtype="f64", index_origin=0):
+        """make_crs_matrix_local_loadlibsvm (index_origin 0 AUTO, 1 ZERO_ORIG,
+        2 ONE_ORIG); returns (matrix, labels)."""
+        h = _p()
+        self.check(self.L.fvg_matrix_load_libsvm(self.h, str(path).encode(), _dt(dtype), int(index_origin),
+                                                 C.byref(h)))
+        M = self._wrap(h, _dt(dtype))
+        lab = np.zeros(M.m)
+        self.check(self.L.fvg_matrix_get_labels(M.h, _ptr(lab)))
+        return M, lab
+
+    def load_binary(self, path, dtype="f64", idx_type="uint64_t", off_type="uint64_t"):
+        """make_crs_matrix_local_loadbinary (type names as in the type file)."""
+        h = _p()
+        self.check(self.L.fvg_matrix_load_binary(self.h, str(path).encode(), _dt(dtype), idx_type.encode(),
+                                                 off_type.encode(), C.byref(h)))
+        return self._wrap(h, _dt(dtype))
 
 
 class Matrix:
@@ -282,6 +324,15 @@ class Matrix:
         return Y
 
     # --- derived layouts (host copies) ----------------------------------
+    def get_crs(self):
+        """(off, idx, val) of the uploaded matrix (values as FP64)."""
+        z = self.nnz
+        off = np.zeros(self.m + 1, dtype=np.int32)
+        idx = np.zeros(max(z, 1), dtype=np.int32)
+        val = np.zeros(max(z, 1))
+        self.ctx.check(self.ctx.L.fvg_matrix_get_crs(self.ctx.h, self.h, _ptr(off), _ptr(idx), _ptr(val)))
+        return off, idx[:z], val[:z]
+
     def get_transpose(self):
         toff = np.zeros(self.n + 1, dtype=np.int32)
         tidx = np.zeros(max(self.nnz, 1), dtype=np.int32)

@@ -22,6 +22,10 @@ void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const d
                        const fvg_glm_params* p, i64 K, double* w_h, double* b_h, i64* n_iter);
 void multinomial_probability(fvg_ctx* c, fvg_matrix* M, const double* w_h, const double* b_h, i64 K, int icpt_on,
                              double* prob_h);
+void load_text_matrix(fvg_ctx* c, const char* path, int dt, i64 num_col, DevCRS& A);
+void load_libsvm_matrix(fvg_ctx* c, const char* path, int dt, int origin, DevCRS& A, std::vector<double>& label);
+void load_binary_matrix(fvg_ctx* c, const char* dir, int dt, const char* idx_type, const char* off_type,
+                        DevCRS& A);
 int crs_blocks_per_sm();
 void sigmoid_probability(fvg_ctx* c, double* v, i64 m, double b);
 }  // namespace fvg
@@ -48,6 +52,37 @@ using namespace fvg;
 static void need(bool cond, fvg_status code, const char* msg) {
   if (!cond) fail(code, msg);
 }
+
+// A matrix handle around a loader that fills M->A.
+template <class F>
+static fvg_status load_matrix(fvg_ctx* c, fvg_dtype dt, fvg_matrix** out, F&& fill) {
+  if (!c || !out) return FVG_ERR_INVALID_ARG;
+  *out = nullptr;
+  fvg_matrix* M = nullptr;
+  try {
+    need(dt == FVG_F64 || dt == FVG_F32, FVG_ERR_INVALID_ARG, "files hold FP64 or FP32 values");
+    M = new fvg_matrix();
+    M->ctx = c;
+    M->master = dt;
+    fill(M);
+    c->matrices.push_back(M);
+    *out = M;
+    return FVG_OK;
+  } catch (const fvg::Error& e) {
+    delete M;
+    c->last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    delete M;
+    c->last_error = "host allocation failed";
+    return FVG_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    delete M;
+    c->last_error = e.what();
+    return FVG_ERR_INTERNAL;
+  }
+}
+
 
 extern "C" {
 
@@ -344,6 +379,48 @@ FVG_API fvg_status fvg_matrix_get_transpose(fvg_ctx* c, fvg_matrix* M, int32_t* 
   download_values(c, t.val, M->master, t.nnz, tval);
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_get_crs(fvg_ctx* c, fvg_matrix* M, int32_t* off, int32_t* idx, double* val) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  const DevCRS& a = M->A;
+  if (off) FVG_CUDA(cudaMemcpyAsync(off, a.off.p, sizeof(int32_t) * (a.m + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (idx && a.nnz)
+    FVG_CUDA(cudaMemcpyAsync(idx, a.idx.p, sizeof(int32_t) * a.nnz, cudaMemcpyDeviceToHost, c->stream));
+  download_values(c, a.val, M->master, a.nnz, val);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_load_text(fvg_ctx* c, const char* path, fvg_dtype val_dtype, int64_t num_col,
+                                        fvg_matrix** out) {
+  if (!path) return FVG_ERR_INVALID_ARG;
+  return load_matrix(c, val_dtype, out, [&](fvg_matrix* M) { load_text_matrix(c, path, val_dtype, num_col, M->A); });
+}
+
+FVG_API fvg_status fvg_matrix_load_libsvm(fvg_ctx* c, const char* path, fvg_dtype val_dtype, int index_origin,
+                                          fvg_matrix** out) {
+  if (!path || index_origin < 0 || index_origin > 2) return FVG_ERR_INVALID_ARG;
+  return load_matrix(c, val_dtype, out, [&](fvg_matrix* M) {
+    load_libsvm_matrix(c, path, val_dtype, index_origin, M->A, M->labels);
+    M->has_labels = true;
+  });
+}
+
+FVG_API fvg_status fvg_matrix_get_labels(const fvg_matrix* M, double* labels) {
+  if (!M || !labels || !M->has_labels) return FVG_ERR_INVALID_ARG;
+  std::copy(M->labels.begin(), M->labels.end(), labels);
+  return FVG_OK;
+}
+
+FVG_API fvg_status fvg_matrix_load_binary(fvg_ctx* c, const char* dir, fvg_dtype val_dtype, const char* idx_type,
+                                          const char* off_type, fvg_matrix** out) {
+  if (!dir) return FVG_ERR_INVALID_ARG;
+  const char* it = idx_type ? idx_type : "uint64_t";
+  const char* ot = off_type ? off_type : "uint64_t";
+  return load_matrix(c, val_dtype, out, [&](fvg_matrix* M) { load_binary_matrix(c, dir, val_dtype, it, ot, M->A); });
 }
 
 FVG_API fvg_status fvg_matrix_get_ell(fvg_ctx* c, fvg_matrix* M, int64_t* width, int32_t* eidx, double* eval) {

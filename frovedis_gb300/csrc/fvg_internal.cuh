@@ -170,6 +170,8 @@ struct fvg_matrix {
   std::unique_ptr<fvg::DevELL> ell;
   std::unique_ptr<fvg::DevJDS> jds, tjds;
   std::unique_ptr<fvg::DevHYB> hyb, thyb;
+  std::vector<double> labels;  // libsvm loads: one label per row
+  bool has_labels = false;
 };
 
 namespace fvg {

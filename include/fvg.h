@@ -92,6 +92,33 @@ FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* ctx, fvg_matrix* mat, fvg_dty
 /* Device bytes held by the matrix and everything derived from it. */
 FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* mat);
 
+/* The uploaded matrix itself: off[num_row+1], idx[nnz], val[nnz] (FP64). */
+FVG_API fvg_status fvg_matrix_get_crs(fvg_ctx* ctx, fvg_matrix* mat, int32_t* off, int32_t* idx, double* val);
+
+/* ------------------------------------------------------------- loaders
+ * The reference's on-disk CRS formats, parsed on the device (values
+ * bit-identical to strtod / strtof; lines must be well formed: "col:value"
+ * tokens separated by white space).  val_dtype: FVG_F64 (T = double) or
+ * FVG_F32 (T = float). */
+/* make_crs_matrix_local_load(file[, num_col]) (matrix/crs_matrix.hpp:757-775):
+ * one row per line, 0-based column ids; num_col < 0: largest id + 1. */
+FVG_API fvg_status fvg_matrix_load_text(fvg_ctx* ctx, const char* path, fvg_dtype val_dtype, int64_t num_col,
+                                        fvg_matrix** out);
+/* make_crs_matrix_local_loadlibsvm(file, label, idxorg) (crs_matrix.hpp:874-899):
+ * "label col:value ..." per line; index_origin as frovedis::IndexOrigin
+ * (0 AUTO, 1 ZERO_ORIG, 2 ONE_ORIG); num_col = largest id in the file + 1.
+ * The labels are kept with the matrix: fvg_matrix_get_labels. */
+FVG_API fvg_status fvg_matrix_load_libsvm(fvg_ctx* ctx, const char* path, fvg_dtype val_dtype, int index_origin,
+                                          fvg_matrix** out);
+FVG_API fvg_status fvg_matrix_get_labels(const fvg_matrix* mat, double* labels);
+/* make_crs_matrix_local_loadbinary(dir) (crs_matrix.hpp:565-603): nums, an
+ * optional type file checked against (val_dtype, idx_type, off_type) — type
+ * names as the reference writes them ("int32_t", "uint32_t", "int64_t",
+ * "uint64_t"; NULL = "uint64_t", i.e. size_t) — and the val/idx/off arrays
+ * in native byte order. */
+FVG_API fvg_status fvg_matrix_load_binary(fvg_ctx* ctx, const char* dir, fvg_dtype val_dtype, const char* idx_type,
+                                          const char* off_type, fvg_matrix** out);
+
 /* Copies of the derived layouts to host memory, in the reference's array
  * order, for checking the device builders against the reference's:
  *  transpose  — crs_matrix_local::transpose (crs_matrix.hpp:356-412):

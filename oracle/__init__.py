@@ -340,3 +340,94 @@ def text_rank_splits(data: bytes, P: int):
     for c in counts:
         sp.append(sp[-1] + c)
     return sp
+
+
+# ------------------------------------------------------------------ loaders
+# Restatement of the reference's CRS file loaders, driving the C library's
+# strtoll / strtod / strtof through ctypes so that every number is converted
+# exactly as the reference converts it.
+_libc = None
+
+
+def _c():
+    global _libc
+    if _libc is None:
+        _libc = C.CDLL(None)
+        _libc.strtoll.restype = C.c_longlong
+        _libc.strtoll.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int]
+        _libc.strtod.restype = C.c_double
+        _libc.strtod.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        _libc.strtof.restype = C.c_float
+        _libc.strtof.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    return _libc
+
+
+def _getlines(data: bytes):
+    """std::getline over a file: a last line without newline counts."""
+    parts = data.split(b"\n")
+    if parts and parts[-1] == b"":
+        parts.pop()
+    return parts
+
+
+def _parseline(line: bytes, idx, val, as_float):
+    """make_crs_matrix_local_parseline (matrix/crs_matrix.hpp:665-679)."""
+    lc = _c()
+    buf = C.create_string_buffer(line + b"\0\0")
+    s = C.addressof(buf)
+    end = C.c_void_p()
+    while C.string_at(s, 1) != b"\0":
+        pos = lc.strtoll(s, C.byref(end), 10)
+        if end.value == s:
+            break
+        idx.append(pos)
+        s = end.value + 1
+        v = (lc.strtof if as_float else lc.strtod)(s, C.byref(end))
+        val.append(v)
+        s = end.value
+
+
+def load_text(path, num_col=None, as_float=False):
+    """make_crs_matrix_local_load (crs_matrix.hpp:757-775, x86 branch):
+    returns (off, idx, val, num_row, num_col)."""
+    off, idx, val = [0], [], []
+    for line in _getlines(open(path, "rb").read()):
+        _parseline(line, idx, val, as_float)
+        off.append(len(val))
+    if num_col is None:
+        num_col = (max(idx) + 1) if idx else 0
+    dt = np.float32 if as_float else np.float64
+    return (np.array(off, dtype=np.int64), np.array(idx, dtype=np.int64), np.array(val, dtype=dt), len(off) - 1,
+            num_col)
+
+
+def load_libsvm(path, origin=0, as_float=False):
+    """make_crs_matrix_local_loadlibsvm (crs_matrix.hpp:863-899): origin as
+    IndexOrigin (0 AUTO, 1 ZERO_ORIG, 2 ONE_ORIG); returns (off, idx, val,
+    num_row, num_col, label)."""
+    lc = _c()
+    off, idx, val, label = [0], [], [], []
+    for line in _getlines(open(path, "rb").read()):
+        buf = C.create_string_buffer(line + b"\0")
+        s = C.addressof(buf)
+        end = C.c_void_p()
+        label.append((lc.strtof if as_float else lc.strtod)(s, C.byref(end)))  # loadlibsvm_extract_label
+        _parseline(line[end.value - s:], idx, val, as_float)
+        off.append(len(val))
+    num_col = max(idx) + 1  # taken before the origin adjustment
+    idx = np.array(idx, dtype=np.int64)
+    if origin == 2 or (origin == 0 and idx.min() > 0):
+        idx = idx - 1
+    dt = np.float32 if as_float else np.float64
+    return (np.array(off, dtype=np.int64), idx, np.array(val, dtype=dt), len(off) - 1, num_col,
+            np.array(label, dtype=np.float64))
+
+
+def load_binary(path, val_dtype=np.float64, idx_dtype=np.uint64, off_dtype=np.uint64):
+    """make_crs_matrix_local_loadbinary (crs_matrix.hpp:565-603), native byte
+    order: returns (off, idx, val, num_row, num_col)."""
+    m, n = (int(x) for x in open(os.path.join(path, "nums")).read().split()[:2])
+    val = np.fromfile(os.path.join(path, "val"), dtype=val_dtype)
+    idx = np.fromfile(os.path.join(path, "idx"), dtype=idx_dtype).astype(np.int64)
+    off = np.fromfile(os.path.join(path, "off"), dtype=off_dtype).astype(np.int64)
+    return off, idx, val, m, n

@@ -3,11 +3,12 @@
 Reads (never writes) the reference tree given as argv[1] (default
 /root/reference) and extracts, as data:
 
-* the tutorial SpMV fixture ``doc/tutorial/src/tut3.2.1-1/data`` and its
+* the tutorial SpMV fixture ``doc/tutorial/src/tut3.2.1-1/data`` (also as
+  raw text, for the loaders) and its
   documented result (``doc/tutorial/tutorial.md``, block after "The result of
   the program should be"), also used for ELL/JDS/hybrid by ``tut3.2.2``;
 * the binary CRS fixture ``doc/tutorial/src/tut3.2.1-2/data_binary``
-  (nums/val/idx/off/type) and its documented transpose (tutorial.md, block
+  (nums/val/idx/off/type, also as raw files) and its documented transpose (tutorial.md, block
   after "It should be:");
 * the glm fixtures ``test/ml/test2.1-1`` (SGD) and ``test/ml/test2.1-2``
   (L-BFGS): data/label text, the hyper-parameters and expected outputs
@@ -60,6 +61,7 @@ def main():
     # --- tutorial SpMV (tut3.2.1-1, tut3.2.2) ---
     data = open(os.path.join(tut, "src", "tut3.2.1-1", "data")).read()
     g["tut_spmv"] = parse_crs_text(data)
+    g["tut_spmv"]["raw_text"] = data  # the file itself, for the loader tests
     g["tut_spmv"]["expected_y_ones"] = [
         float(v) for v in indented_block_after(md, "The result of the program should be:",
                                                md.index("src/tut3.2.1-1/tut.cc"))]
@@ -76,6 +78,9 @@ def main():
     idx = list(struct.unpack("<%dQ" % (len(raw_idx) // 8), raw_idx))
     off = list(struct.unpack("<%dQ" % (len(raw_off) // 8), raw_off))
     g["tut_binary"] = dict(m=int(nums[0]), n=int(nums[1]), off=off, idx=idx, val=val, type=types)
+    g["tut_binary"]["raw_files"] = {  # the directory itself, for the loader tests
+        "nums": open(os.path.join(d, "nums")).read(), "type": open(os.path.join(d, "type")).read(),
+        "val": raw_val.hex(), "idx": raw_idx.hex(), "off": raw_off.hex()}
     tr = indented_block_after(md, "It should be:", md.index("src/tut3.2.1-2/tut.cc"))
     g["tut_binary"]["expected_transpose_text"] = tr
 

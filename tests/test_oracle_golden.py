@@ -107,3 +107,26 @@ def test_jds_order_ties_by_descending_row():
     perm, joff, jidx, jval = oracle.jds_build(a)
     assert list(perm) == [3, 1, 0, 2]
     assert list(joff) == [0, 4, 7]
+
+
+def test_oracle_loaders_on_tutorial_files(tmp_path):
+    # make_crs_matrix_local_load on doc/tutorial/src/tut3.2.1-1/data and
+    # make_crs_matrix_local_loadbinary on tut3.2.1-2/data_binary
+    g = golden()
+    p = tmp_path / "data"
+    p.write_text(g["tut_spmv"]["raw_text"])
+    off, idx, val, m, n = oracle.load_text(str(p))
+    assert (m, n) == (g["tut_spmv"]["m"], g["tut_spmv"]["n"])
+    assert off.tolist() == g["tut_spmv"]["off"] and idx.tolist() == g["tut_spmv"]["idx"]
+    assert val.tolist() == g["tut_spmv"]["val"]
+    d = tmp_path / "data_binary"
+    d.mkdir()
+    rf = g["tut_binary"]["raw_files"]
+    for k in ("nums", "type"):
+        (d / k).write_text(rf[k])
+    for k in ("val", "idx", "off"):
+        (d / k).write_bytes(bytes.fromhex(rf[k]))
+    off, idx, val, m, n = oracle.load_binary(str(d))
+    assert (m, n) == (g["tut_binary"]["m"], g["tut_binary"]["n"])
+    assert off.tolist() == g["tut_binary"]["off"] and idx.tolist() == g["tut_binary"]["idx"]
+    assert val.tolist() == g["tut_binary"]["val"]
