@@ -16,7 +16,13 @@
 //   logistic_regression_with_sgd::train     ml/glm/logistic_regression_with_sgd.hpp:8-441
 //   multinomial_logistic_regression::train  ml/glm/multinomial_logistic_regression.hpp:8-378
 //   multinomial_logistic_regression_model<T> ml/glm/multinomial_logistic_regression_model.hpp:10-258
-//   MatType, RegType                   ml/utility/mattype.hpp:6-11, ml/glm/regularizer.hpp:8-12
+//   make_crs_matrix_local_load / _loadlibsvm / _loadbinary, save, savebinary
+//                                      crs_matrix.hpp:440-450, 565-634, 757-775, 874-899
+//   logistic_regression<T> estimator   ml/glm/logistic_regression.hpp:13-460
+//   model save / load (text, binary)   ml/glm/linear_model.hpp:39-150,
+//                                      multinomial_logistic_regression_model.hpp:136-201
+//   MatType, RegType, IndexOrigin      ml/utility/mattype.hpp:6-11, ml/glm/regularizer.hpp:8-12,
+//                                      matrix/crs_matrix.hpp:30-34
 //
 // The matrices keep the reference's public fields (val, idx, off, perm,
 // local_num_row, local_num_col) filled in the reference's array order; the
@@ -27,13 +33,19 @@
 #ifndef FROVEDIS_GB300_HPP
 #define FROVEDIS_GB300_HPP
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
+#include <fstream>
+#include <iomanip>
 #include <memory>
+#include <sstream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "fvg.h"
@@ -136,6 +148,109 @@ struct crs_matrix_local {
     local_num_row = local_num_col = 0;
   }
 };
+
+// IndexOrigin (matrix/crs_matrix.hpp:30-34)
+enum IndexOrigin { AUTO = 0, ZERO_ORIG, ONE_ORIG };
+
+namespace detail {
+// get_type_name<T>() (core/utility.hpp:76-99) for the index / offset types
+template <class X> inline const char* type_name() {
+  static_assert(std::is_integral<X>::value && (sizeof(X) == 4 || sizeof(X) == 8), "32/64-bit integer index");
+  return std::is_signed<X>::value ? (sizeof(X) == 4 ? "int32_t" : "int64_t")
+                                  : (sizeof(X) == 4 ? "uint32_t" : "uint64_t");
+}
+// a device matrix read back into the reference's struct
+template <class T, class I, class O> crs_matrix_local<T, I, O> to_local(fvg_matrix* h) {
+  int64_t m = 0, n = 0, nnz = 0;
+  frovedis_gb300::check(fvg_matrix_info(h, &m, &n, &nnz));
+  std::vector<int32_t> off(m + 1), idx(nnz ? nnz : 1);
+  std::vector<double> val(nnz ? nnz : 1);
+  frovedis_gb300::check(fvg_matrix_get_crs(frovedis_gb300::context(), h, off.data(), idx.data(), val.data()));
+  crs_matrix_local<T, I, O> r((size_t)m, (size_t)n);
+  r.off.assign(off.begin(), off.end());
+  r.idx.assign(idx.begin(), idx.begin() + nnz);
+  r.val.assign(val.begin(), val.begin() + nnz);
+  return r;
+}
+struct handle {
+  fvg_matrix* h = nullptr;
+  ~handle() { fvg_matrix_destroy(h); }
+};
+}  // namespace detail
+
+// make_crs_matrix_local_load(file[, num_col]) (crs_matrix.hpp:757-775):
+// "col:value" lines, parsed on the device
+template <class T, class I = size_t, class O = size_t>
+crs_matrix_local<T, I, O> make_crs_matrix_local_load(const std::string& file, long long num_col = -1) {
+  detail::handle d;
+  frovedis_gb300::check(fvg_matrix_load_text(frovedis_gb300::context(), file.c_str(),
+                                             frovedis_gb300::dtype_of<T>::value, num_col, &d.h));
+  return detail::to_local<T, I, O>(d.h);
+}
+
+// make_crs_matrix_local_loadlibsvm (crs_matrix.hpp:874-899)
+template <class T, class I = size_t, class O = size_t>
+crs_matrix_local<T, I, O> make_crs_matrix_local_loadlibsvm(const std::string& file, std::vector<T>& label,
+                                                           IndexOrigin idxorg = AUTO) {
+  detail::handle d;
+  frovedis_gb300::check(fvg_matrix_load_libsvm(frovedis_gb300::context(), file.c_str(),
+                                               frovedis_gb300::dtype_of<T>::value, (int)idxorg, &d.h));
+  auto r = detail::to_local<T, I, O>(d.h);
+  std::vector<double> lab(r.local_num_row);
+  if (!lab.empty()) frovedis_gb300::check(fvg_matrix_get_labels(d.h, lab.data()));
+  label.assign(lab.begin(), lab.end());
+  return r;
+}
+
+// make_crs_matrix_local_loadbinary (crs_matrix.hpp:565-603)
+template <class T, class I = size_t, class O = size_t>
+crs_matrix_local<T, I, O> make_crs_matrix_local_loadbinary(const std::string& input) {
+  detail::handle d;
+  frovedis_gb300::check(fvg_matrix_load_binary(frovedis_gb300::context(), input.c_str(),
+                                               frovedis_gb300::dtype_of<T>::value, detail::type_name<I>(),
+                                               detail::type_name<O>(), &d.h));
+  return detail::to_local<T, I, O>(d.h);
+}
+
+// crs_matrix_local::save (operator<<, crs_matrix.hpp:440-450): "col:value"
+// lines
+template <class T, class I, class O>
+void save(const crs_matrix_local<T, I, O>& mat, const std::string& file) {
+  std::ofstream str(file.c_str());
+  for (size_t row = 0; row < mat.local_num_row; row++) {
+    for (O col = mat.off[row]; col < mat.off[row + 1]; col++) {
+      str << mat.idx[col] << ":" << mat.val[col];
+      if (col != mat.off[row + 1] - 1) str << " ";
+    }
+    str << "\n";
+  }
+  if (!str) throw std::runtime_error("cannot write " + file);
+}
+
+// crs_matrix_local::savebinary (crs_matrix.hpp:604-634): nums, type and the
+// native-order val / idx / off arrays
+template <class T, class I, class O>
+void savebinary(const crs_matrix_local<T, I, O>& mat, const std::string& dir) {
+  struct stat sb;
+  if (stat(dir.c_str(), &sb) != 0) {
+    if (mkdir(dir.c_str(), S_IRWXU | S_IRWXG | S_IRWXO) != 0) throw std::runtime_error("mkdir failed");
+  } else if (!S_ISDIR(sb.st_mode)) {
+    throw std::runtime_error(dir + " is not a directory");
+  }
+  std::ofstream nums((dir + "/nums").c_str());
+  nums << mat.local_num_row << "\n" << mat.local_num_col << std::endl;
+  std::ofstream type((dir + "/type").c_str());
+  type << (sizeof(T) == 4 ? "float" : "double") << "\n" << detail::type_name<I>() << "\n"
+       << detail::type_name<O>() << std::endl;
+  auto dump = [&](const std::string& f, const void* p, size_t bytes) {
+    std::ofstream o((dir + "/" + f).c_str(), std::ios::binary);
+    o.write(static_cast<const char*>(p), (std::streamsize)bytes);
+    if (!o) throw std::runtime_error("cannot write " + dir + "/" + f);
+  };
+  dump("val", mat.val.data(), sizeof(T) * mat.val.size());
+  dump("idx", mat.idx.data(), sizeof(I) * mat.idx.size());
+  dump("off", mat.off.data(), sizeof(O) * mat.off.size());
+}
 
 namespace detail {
 template <class T, class M>
@@ -566,6 +681,339 @@ struct multinomial_logistic_regression {
     ret.isIntercept = isIntercept;
     if (inputMovable) data.clear();
     return ret;
+  }
+};
+
+// ------------------------------------------------------------ persistence
+namespace detail {
+inline void make_directory(const std::string& dir) {
+  struct stat sb;
+  if (stat(dir.c_str(), &sb) != 0) {
+    if (mkdir(dir.c_str(), S_IRWXU | S_IRWXG | S_IRWXO) != 0) throw std::runtime_error("mkdir failed");
+  } else if (!S_ISDIR(sb.st_mode)) {
+    throw std::runtime_error(dir + " is not a directory");
+  }
+}
+// dvector<T>::savebinary / make_dvector_loadbinary: a raw native array
+template <class T> void write_raw(const std::string& f, const std::vector<T>& v) {
+  std::ofstream o(f.c_str(), std::ios::binary);
+  o.write(reinterpret_cast<const char*>(v.data()), (std::streamsize)(sizeof(T) * v.size()));
+  if (!o) throw std::runtime_error("cannot write " + f);
+}
+template <class T> std::vector<T> read_raw(const std::string& f) {
+  std::ifstream i(f.c_str(), std::ios::binary | std::ios::ate);
+  if (!i) throw std::runtime_error("cannot open " + f);
+  const std::streamsize sz = i.tellg();
+  if (sz % (std::streamsize)sizeof(T)) throw std::runtime_error("make_dvector_loadbinary: incorrect filesize");
+  std::vector<T> v((size_t)sz / sizeof(T));
+  i.seekg(0);
+  i.read(reinterpret_cast<char*>(v.data()), sz);
+  return v;
+}
+template <class T> const char* value_type_name() { return sizeof(T) == 4 ? "float" : "double"; }
+}  // namespace detail
+
+// rowmajor_matrix_local<T>::save / make_rowmajor_matrix_local_load
+// (rowmajor_matrix.hpp:227-240, 323-340, 366-370): one row per line
+template <class T> void save(const rowmajor_matrix_local<T>& m, const std::string& file) {
+  std::ofstream str(file.c_str());
+  for (size_t r = 0; r < m.local_num_row; r++) {
+    for (size_t c = 0; c + 1 < m.local_num_col; c++) str << m.val[m.local_num_col * r + c] << " ";
+    if (m.local_num_col) str << m.val[m.local_num_col * r + m.local_num_col - 1];
+    str << "\n";
+  }
+}
+template <class T> rowmajor_matrix_local<T> make_rowmajor_matrix_local_load(const std::string& file) {
+  std::ifstream str(file.c_str());
+  rowmajor_matrix_local<T> ret;
+  std::string line;
+  size_t lines = 0, width = 0;
+  while (std::getline(str, line)) {
+    std::istringstream ls(line);
+    size_t k = 0;
+    for (T x; ls >> x; k++) ret.val.push_back(x);
+    if (lines == 0) width = k;
+    lines++;
+  }
+  ret.local_num_row = lines;
+  ret.local_num_col = width;
+  return ret;
+}
+// rowmajor_matrix_local<T>::savebinary / make_rowmajor_matrix_local_loadbinary
+// (rowmajor_matrix.hpp:760-810): nums, type, val
+template <class T> void savebinary(const rowmajor_matrix_local<T>& m, const std::string& dir) {
+  detail::make_directory(dir);
+  std::ofstream((dir + "/nums").c_str()) << m.local_num_row << "\n" << m.local_num_col << std::endl;
+  std::ofstream((dir + "/type").c_str()) << detail::value_type_name<T>() << std::endl;
+  detail::write_raw(dir + "/val", m.val);
+}
+template <class T> rowmajor_matrix_local<T> make_rowmajor_matrix_local_loadbinary(const std::string& dir) {
+  rowmajor_matrix_local<T> ret;
+  std::ifstream nums((dir + "/nums").c_str());
+  if (!(nums >> ret.local_num_row >> ret.local_num_col)) throw std::runtime_error("cannot read " + dir + "/nums");
+  std::ifstream ty((dir + "/type").c_str());
+  std::string t;
+  if (ty >> t && t != detail::value_type_name<T>())
+    throw std::runtime_error(std::string("make_rowmajor_matrix_local_loadbinary: val type mismatch detected! "
+                                         "expected type: ") + t + "; given type: " + detail::value_type_name<T>() +
+                             "\n");
+  ret.val = detail::read_raw<T>(dir + "/val");
+  return ret;
+}
+
+// glm_save / glm_savebinary / glm_load / glm_loadbinary of the binary model
+// (ml/glm/linear_model.hpp:39-150): weights, intercept, threshold
+template <class T> void save(const logistic_regression_model<T>& m, const std::string& path) {
+  std::ofstream out(path.c_str());
+  out << std::setprecision(12);
+  for (auto w : m.weight) out << w << "\n";
+  out << m.intercept << std::endl;
+  out << m.threshold << std::endl;
+}
+template <class T> void savebinary(const logistic_regression_model<T>& m, const std::string& path) {
+  std::vector<T> tmp(m.weight);
+  tmp.push_back(m.intercept);
+  tmp.push_back(m.threshold);
+  detail::write_raw(path, tmp);
+}
+template <class T> void load(logistic_regression_model<T>& m, const std::string& path) {
+  std::ifstream in(path.c_str());
+  m.weight.clear();
+  for (T x; in >> x;) m.weight.push_back(x);
+  if (m.weight.size() < 2) throw std::runtime_error("model file " + path + " is too short");
+  m.threshold = m.weight.back();
+  m.weight.pop_back();
+  m.intercept = m.weight.back();
+  m.weight.pop_back();
+}
+template <class T> void loadbinary(logistic_regression_model<T>& m, const std::string& path) {
+  m.weight = detail::read_raw<T>(path);
+  if (m.weight.size() < 2) throw std::runtime_error("model file " + path + " is too short");
+  m.threshold = m.weight.back();
+  m.weight.pop_back();
+  m.intercept = m.weight.back();
+  m.weight.pop_back();
+}
+
+// multinomial model save / savebinary / load / loadbinary
+// (multinomial_logistic_regression_model.hpp:136-201): weight, intercept,
+// metadata (nclasses, nfeatures, isIntercept, threshold)
+template <class T> void save(const multinomial_logistic_regression_model<T>& m, const std::string& dir) {
+  detail::make_directory(dir);
+  save(m.weight, dir + "/weight");
+  std::ofstream ic((dir + "/intercept").c_str());
+  for (auto& e : m.intercept) ic << e << std::endl;
+  std::ofstream md((dir + "/metadata").c_str());
+  md << m.nclasses << std::endl << m.nfeatures << std::endl << m.isIntercept << std::endl << m.threshold << std::endl;
+}
+template <class T> void savebinary(const multinomial_logistic_regression_model<T>& m, const std::string& dir) {
+  detail::make_directory(dir);
+  savebinary(m.weight, dir + "/weight");
+  detail::write_raw(dir + "/intercept", m.intercept);
+  std::ofstream md((dir + "/metadata").c_str());
+  md << m.nclasses << std::endl << m.nfeatures << std::endl << m.isIntercept << std::endl << m.threshold << std::endl;
+}
+template <class T> void load(multinomial_logistic_regression_model<T>& m, const std::string& dir) {
+  m.weight = make_rowmajor_matrix_local_load<T>(dir + "/weight");
+  std::ifstream ic((dir + "/intercept").c_str());
+  m.intercept.clear();
+  for (T x; ic >> x;) m.intercept.push_back(x);
+  std::ifstream md((dir + "/metadata").c_str());
+  md >> m.nclasses >> m.nfeatures >> m.isIntercept >> m.threshold;
+}
+template <class T> void loadbinary(multinomial_logistic_regression_model<T>& m, const std::string& dir) {
+  m.weight = make_rowmajor_matrix_local_loadbinary<T>(dir + "/weight");
+  m.intercept = detail::read_raw<T>(dir + "/intercept");
+  std::ifstream md((dir + "/metadata").c_str());
+  md >> m.nclasses >> m.nfeatures >> m.isIntercept >> m.threshold;
+}
+
+// accuracy_score (ml/metrics.hpp:383-396)
+template <class T> float accuracy_score(const std::vector<T>& true_label, const std::vector<T>& pred_label) {
+  if (true_label.size() != pred_label.size())
+    throw std::runtime_error("accuracy_score: size differs in predicted labels and actual labels!\n");
+  size_t count = 0;
+  for (size_t i = 0; i < true_label.size(); i++) count += true_label[i] == pred_label[i];
+  return true_label.empty() ? 0.0f : (float)count / (float)true_label.size();
+}
+
+// logistic_regression<T> estimator (ml/glm/logistic_regression.hpp:13-460),
+// on a local CRS matrix: the solver dispatch of _fit (lines 237-298), a
+// multinomial model when the labels hold more than two classes.
+template <class T>
+struct logistic_regression {
+  logistic_regression(int max_iter = 1000, double alpha = 0.01, const std::string& solver = "sgd",
+                      double reg_param = 0.01, const std::string& reg_type = "ZERO", bool fit_intercept = false,
+                      double mini_batch_fraction = 1.0, int hs = 10, double convergence_tol = 0.001,
+                      bool is_mult = false, bool warm_start = false, MatType mType = CRS)
+      : max_iter(max_iter), hist_size(hs), alpha(alpha), mbf(mini_batch_fraction), tol(convergence_tol),
+        reg_param(reg_param), solver(solver), reg_type(reg_type), fit_intercept(fit_intercept), is_mult(is_mult),
+        warm_start(warm_start), is_fitted(false), mat_type(mType), n_iter_(0), n_features_(0), n_classes_(0) {}
+
+  static void require(bool c, const std::string& msg) {
+    if (!c) throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, msg);
+  }
+  logistic_regression& set_max_iter(int v) {
+    require(v > 0, "expected a positive max_iter; received: " + std::to_string(v) + "\n");
+    max_iter = v;
+    return *this;
+  }
+  logistic_regression& set_alpha(double v) {
+    require(v > 0, "expected a positive alpha (learning rate); received: " + std::to_string(v) + "\n");
+    alpha = v;
+    return *this;
+  }
+  logistic_regression& set_solver(const std::string& s) {
+    require(s == "sgd" || s == "shrink-sgd" || s == "lbfgs", "expected sgd, shrink-sgd or lbfgs; received: " + s + "\n");
+    solver = s;
+    return *this;
+  }
+  logistic_regression& set_reg_param(double v) {
+    require(v > 0, "expected a positive regularization parameter; received: " + std::to_string(v) + "\n");
+    reg_param = v;
+    return *this;
+  }
+  logistic_regression& set_reg_type(const std::string& s) {
+    require(s == "ZERO" || s == "L1" || s == "L2", "expected ZERO, L1 or L2; received: " + s + "\n");
+    reg_type = s;
+    return *this;
+  }
+  logistic_regression& set_intercept(bool v) {
+    fit_intercept = v;
+    return *this;
+  }
+  logistic_regression& set_mini_batch_fraction(double v) {
+    require(v > 0, "expected a positive mini-batch fraction; received: " + std::to_string(v) + "\n");
+    mbf = v;
+    return *this;
+  }
+  logistic_regression& set_hist_size(int v) {
+    require(v > 0, "expected a positive history size; received: " + std::to_string(v) + "\n");
+    hist_size = v;
+    return *this;
+  }
+  logistic_regression& set_tol(double v) {
+    require(v >= 0, "expected a positive or zero convergence tolerance; received: " + std::to_string(v) + "\n");
+    tol = v;
+    return *this;
+  }
+  logistic_regression& set_is_mult(bool v) {
+    is_mult = v;
+    return *this;
+  }
+  logistic_regression& set_warm_start(bool v) {
+    warm_start = v;
+    return *this;
+  }
+  RegType get_regularizer() const {
+    if (reg_type == "ZERO") return ZERO;
+    if (reg_type == "L1") return L1;
+    if (reg_type == "L2") return L2;
+    throw frovedis_gb300::error(FVG_ERR_INVALID_ARG,
+                                "[logistic_regression] Unknown regularizer '" + reg_type + "' is encountered!\n");
+  }
+
+  template <class I, class O>
+  logistic_regression& fit(crs_matrix_local<T, I, O>& mat, std::vector<T>& label) {
+    std::vector<T> sample_weight;
+    return fit(mat, label, sample_weight);
+  }
+  template <class I, class O>
+  logistic_regression& fit(crs_matrix_local<T, I, O>& mat, std::vector<T>& label, std::vector<T>& sample_weight) {
+    std::vector<T> u(label);
+    std::sort(u.begin(), u.end());
+    const size_t nclasses = (size_t)(std::unique(u.begin(), u.end()) - u.begin());
+    if (nclasses > 2) is_mult = true;
+    const size_t nfeatures = mat.local_num_col;
+    if (!(warm_start && is_fitted)) {
+      if (is_mult) model_mult = multinomial_logistic_regression_model<T>(nfeatures, nclasses, fit_intercept);
+      else model_bin = logistic_regression_model<T>(nfeatures, fit_intercept ? 1.0 : 0.0);
+    } else {
+      require(nfeatures == n_features_, "Fitted model dimension does not match with number of features in input data\n");
+      require(nclasses == n_classes_, "Fitted model dimension does not match with number of labels in input data\n");
+    }
+    size_t n_iter = 0;
+    if (is_mult) {
+      require(solver == "sgd", "Multinomil classification is only supported for sgd solver\n");
+      model_mult = multinomial_logistic_regression::train(mat, label, model_mult, sample_weight, n_iter, max_iter,
+                                                          alpha, reg_param, get_regularizer(), fit_intercept, tol,
+                                                          mat_type);
+    } else if (solver == "sgd") {
+      model_bin = logistic_regression_with_sgd::train(mat, label, model_bin, sample_weight, n_iter, max_iter, alpha,
+                                                      mbf, reg_param, get_regularizer(), fit_intercept, tol,
+                                                      mat_type);
+    } else if (solver == "lbfgs") {
+      model_bin = logistic_regression_with_lbfgs::train(mat, label, model_bin, sample_weight, n_iter, max_iter,
+                                                        alpha, hist_size, reg_param, get_regularizer(),
+                                                        fit_intercept, tol, mat_type);
+    } else {
+      throw frovedis_gb300::error(FVG_ERR_UNSUPPORTED, "solver " + solver + " is not provided by the GB300 path\n");
+    }
+    is_fitted = true;
+    n_iter_ = n_iter;
+    n_features_ = nfeatures;
+    n_classes_ = nclasses;
+    return *this;
+  }
+  template <class I, class O> std::vector<T> predict(const crs_matrix_local<T, I, O>& mat) {
+    require(is_fitted, "[logistic_regression] predict is called before fit\n");
+    return is_mult ? model_mult.predict(mat) : model_bin.predict(mat);
+  }
+  template <class I, class O>
+  std::vector<T> predict_probability(const crs_matrix_local<T, I, O>& mat, bool use_score = false) {
+    require(is_fitted, "[logistic_regression] predict_probability is called before fit\n");
+    return is_mult ? model_mult.predict_probability(mat, use_score) : model_bin.predict_probability(mat, use_score);
+  }
+  template <class I, class O> rowmajor_matrix_local<T> compute_probability_matrix(const crs_matrix_local<T, I, O>& mat) {
+    require(is_fitted, "[logistic_regression] compute_probability_matrix is called before fit\n");
+    return is_mult ? model_mult.compute_probability_matrix(mat) : model_bin.compute_probability_matrix(mat);
+  }
+  template <class I, class O> float score(const crs_matrix_local<T, I, O>& mat, const std::vector<T>& label) {
+    require(is_fitted, "[logistic_regression] score is called before fit\n");
+    return accuracy_score(label, predict(mat));
+  }
+  std::vector<T> get_intercept() const {
+    return is_mult ? model_mult.intercept : std::vector<T>({model_bin.intercept});
+  }
+  std::vector<T> get_weight() const { return is_mult ? model_mult.weight.val : model_bin.weight; }
+  size_t get_num_features() const { return is_mult ? model_mult.get_num_features() : model_bin.get_num_features(); }
+  size_t get_num_classes() const { return is_mult ? model_mult.get_num_classes() : model_bin.get_num_classes(); }
+
+  // save / savebinary / load / loadbinary (lines 404-458): <dir>/model and
+  // <dir>/type ("binomial" or "multinomial")
+  void save(const std::string& dir) {
+    detail::make_directory(dir);
+    is_mult ? frovedis::save(model_mult, dir + "/model") : frovedis::save(model_bin, dir + "/model");
+    std::ofstream((dir + "/type").c_str()) << (is_mult ? "multinomial" : "binomial") << std::endl;
+  }
+  void savebinary(const std::string& dir) {
+    detail::make_directory(dir);
+    is_mult ? frovedis::savebinary(model_mult, dir + "/model") : frovedis::savebinary(model_bin, dir + "/model");
+    std::ofstream((dir + "/type").c_str()) << (is_mult ? "multinomial" : "binomial") << std::endl;
+  }
+  logistic_regression& load(const std::string& dir) { return load_impl(dir, false); }
+  logistic_regression& loadbinary(const std::string& dir) { return load_impl(dir, true); }
+
+  int max_iter, hist_size;
+  double alpha, mbf, tol, reg_param;
+  std::string solver, reg_type;
+  bool fit_intercept, is_mult, warm_start, is_fitted;
+  MatType mat_type;
+  size_t n_iter_, n_features_, n_classes_;
+  logistic_regression_model<T> model_bin;
+  multinomial_logistic_regression_model<T> model_mult;
+
+ private:
+  logistic_regression& load_impl(const std::string& dir, bool binary) {
+    std::string model_type;
+    std::ifstream((dir + "/type").c_str()) >> model_type;
+    is_mult = model_type == "multinomial";
+    if (is_mult) binary ? frovedis::loadbinary(model_mult, dir + "/model") : frovedis::load(model_mult, dir + "/model");
+    else binary ? frovedis::loadbinary(model_bin, dir + "/model") : frovedis::load(model_bin, dir + "/model");
+    n_classes_ = get_num_classes();
+    n_features_ = get_num_features();
+    is_fitted = true;
+    return *this;
   }
 };
 

@@ -139,6 +139,76 @@ int main(int argc, char** argv) {
     put(f, "mlr_pred", model.predict(A));
     put(f, "mlr_maxprob", model.predict_probability(A));
   }
+  {
+    // loaders: the matrix written by the reference's text and binary writers
+    // and read back on the device
+    const std::string base = std::string(argv[2]) + ".dir";
+    save(A, base + ".txt");
+    auto At = make_crs_matrix_local_load<double>(base + ".txt");
+    put(f, "load_text_off", At.off);
+    put(f, "load_text_idx", At.idx);
+    put(f, "load_text_val", At.val);
+    savebinary(A, base + ".bin");
+    auto Ab = make_crs_matrix_local_loadbinary<double>(base + ".bin");
+    put(f, "load_bin_val", Ab.val);
+    put(f, "load_bin_shape", std::vector<size_t>{Ab.local_num_row, Ab.local_num_col});
+    {
+      std::ofstream svm((base + ".svm").c_str());
+      for (size_t r = 0; r < m; r++) {
+        svm << label[r];
+        for (size_t e = A.off[r]; e < A.off[r + 1]; e++) svm << " " << A.idx[e] + 1 << ":" << A.val[e];
+        svm << "\n";
+      }
+    }
+    std::vector<double> lab;
+    auto As = make_crs_matrix_local_loadlibsvm<double>(base + ".svm", lab);
+    put(f, "load_svm_idx", As.idx);
+    put(f, "load_svm_label", lab);
+    put(f, "load_svm_shape", std::vector<size_t>{As.local_num_row, As.local_num_col});
+  }
+  {
+    // the estimator: L-BFGS binary model, then a multinomial one (five
+    // classes), each saved and loaded in the text and binary formats
+    const std::string base = std::string(argv[2]) + ".est";
+    logistic_regression<double> est(30, 0.01, "lbfgs", 1e-3, "L2", true);
+    std::vector<double> lab = label;
+    est.fit(A, lab);
+    put(f, "est_w", est.get_weight());
+    put(f, "est_b", est.get_intercept());
+    put1(f, "est_n_iter", (double)est.n_iter_);
+    put1(f, "est_score", est.score(A, label));
+    est.save(base + ".txt");
+    est.savebinary(base + ".bin");
+    logistic_regression<double> e2, e3;
+    e2.load(base + ".txt");
+    e3.loadbinary(base + ".bin");
+    put(f, "est_text_w", e2.get_weight());
+    put(f, "est_bin_w", e3.get_weight());
+    put1(f, "est_pred_same", e2.predict(A) == est.predict(A) && e3.predict(A) == est.predict(A));
+    std::vector<double> cls(m);
+    for (size_t i = 0; i < m; i++) cls[i] = (double)(i % 5);
+    logistic_regression<double> em(10, 0.05, "sgd");
+    em.fit(A, cls);
+    put1(f, "estm_is_mult", em.is_mult);
+    put(f, "estm_w", em.get_weight());
+    put1(f, "estm_n_iter", (double)em.n_iter_);
+    em.savebinary(base + ".mbin");
+    em.save(base + ".mtxt");
+    logistic_regression<double> e4, e5;
+    e4.loadbinary(base + ".mbin");
+    e5.load(base + ".mtxt");
+    put(f, "estm_bin_w", e4.get_weight());
+    put1(f, "estm_pred_same", e4.predict(A) == em.predict(A));
+    put1(f, "estm_text_classes", (double)e5.get_num_classes());
+    int lbfgs_mult_threw = 0;
+    try {
+      logistic_regression<double> bad(5, 0.01, "lbfgs");
+      bad.fit(A, cls);
+    } catch (frovedis_gb300::error&) {
+      lbfgs_mult_threw = 1;
+    }
+    put1(f, "estm_lbfgs_throws", lbfgs_mult_threw);
+  }
   std::fclose(f);
   return 0;
 }

@@ -118,3 +118,29 @@ def test_cpp_api_matches_oracle(tmp_path):
     assert np.max(np.abs(o["mlr_prob"].reshape(m, 5) - P)) <= 1e-7
     assert np.mean(o["mlr_pred"] == np.argmax(P, 1)) >= 0.999
     assert np.max(np.abs(o["mlr_maxprob"] - P.max(1))) <= 1e-7
+
+    # save (operator<< with the stream's default 6 significant digits) and
+    # reload: the text loader gives what the oracle's strtod gives
+    toff, tidx, tval, tm, tn = oracle.load_text(str(outp) + ".dir.txt")
+    assert np.array_equal(o["load_text_off"], toff) and np.array_equal(o["load_text_idx"], tidx)
+    assert np.array_equal(o["load_text_val"], tval)
+    assert np.array_equal(o["load_bin_val"], a.val) and list(o["load_bin_shape"]) == [m, n]
+    soff, sidx, sval, sm, sn, slab = oracle.load_libsvm(str(outp) + ".dir.svm")
+    assert np.array_equal(o["load_svm_idx"], sidx) and np.array_equal(o["load_svm_label"], slab)
+    assert list(o["load_svm_shape"]) == [sm, sn]
+
+    # estimator (logistic_regression::_fit): the lbfgs solver is
+    # logistic_regression_with_lbfgs::train from w = 1, b = 1
+    re = oracle.logreg_lbfgs(a, label, num_iter=30, reg_type="L2", reg_param=1e-3, intercept=True)
+    assert int(o["est_n_iter"][0]) == re["n_iter"]
+    assert np.max(np.abs(o["est_w"] - re["w"])) <= 1e-5 * max(1.0, np.max(np.abs(re["w"])))
+    pe = np.where(oracle.predict_probability(a, o["est_w"], o["est_b"][0]) >= 0.5, 1.0, -1.0)
+    assert abs(o["est_score"][0] - np.mean(pe == label)) <= 1e-6
+    assert np.max(np.abs(o["est_text_w"] - o["est_w"])) <= 1e-11 * max(1.0, np.max(np.abs(o["est_w"])))
+    assert np.array_equal(o["est_bin_w"], o["est_w"]) and o["est_pred_same"][0] == 1
+    assert o["estm_is_mult"][0] == 1
+    rm2 = oracle.softmax_train(a, cls, 5, num_iter=10, alpha=0.05, reg_param=0.01, reg_type="ZERO")
+    assert int(o["estm_n_iter"][0]) == rm2["n_iter"]
+    assert np.max(np.abs(o["estm_w"] - rm2["W"].ravel())) <= 1e-8 * max(1.0, np.max(np.abs(rm2["W"])))
+    assert np.array_equal(o["estm_bin_w"], o["estm_w"]) and o["estm_pred_same"][0] == 1
+    assert o["estm_text_classes"][0] == 5 and o["estm_lbfgs_throws"][0] == 1
