@@ -26,6 +26,8 @@ F64, F32, BF16 = 0, 1, 2
 CRS, JDS, ELL, HYBRID = 0, 1, 2, 3
 FORMATS = {"CRS": CRS, "JDS": JDS, "ELL": ELL, "HYBRID": HYBRID}
 REG = {"ZERO": 0, "L1": 1, "L2": 2}
+# fvg_loss: the GLM family's compute_dloss kinds (ml/glm/gradient.hpp)
+LOSS = {"logistic": 0, "linear": 1, "hinge": 2, "eps": 3, "sqeps": 4}
 DTYPES = {"f64": F64, "f32": F32, "bf16": BF16}
 
 _p = C.c_void_p
@@ -46,7 +48,8 @@ class GlmParams(C.Structure):
                 ("convergence_tol", C.c_double), ("mat_type", C.c_int32), ("mini_batch_fraction", C.c_double),
                 ("num_partitions", C.c_int32), ("storage", C.c_int32), ("refine", C.c_int32),
                 ("refine_stall", C.c_double), ("l2_no_eta", C.c_int32), ("use_graph", C.c_int32),
-                ("trace", C.POINTER(C.c_double)), ("row_splits", C.POINTER(C.c_int64))]
+                ("trace", C.POINTER(C.c_double)), ("row_splits", C.POINTER(C.c_int64)),
+                ("loss", C.c_int32), ("epsilon", C.c_double)]
 
 
 EXPORTS = [
@@ -59,7 +62,7 @@ EXPORTS = [
     "fvg_logreg_predict_probability", "fvg_spmv_no_alloc", "fvg_logreg_lbfgs_batched",
     "fvg_multinomial_train", "fvg_multinomial_probability",
     "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
-    "fvg_matrix_load_binary",
+    "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
 ]
 
 _lib = None
@@ -118,6 +121,12 @@ def load(build_if_needed: bool = True):
         "fvg_matrix_load_libsvm": ([_p, C.c_char_p, _int, _int, C.POINTER(_p)], _int),
         "fvg_matrix_get_labels": ([_p, _p], _int),
         "fvg_matrix_load_binary": ([_p, C.c_char_p, _int, C.c_char_p, C.c_char_p, C.POINTER(_p)], _int),
+        "fvg_glm_lbfgs": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
+                           C.POINTER(_dbl)], _int),
+        "fvg_glm_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
+                         C.POINTER(_dbl)], _int),
+        "fvg_glm_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
+        "fvg_glm_eval": ([_p, _p, _int, _int, _int, _dbl, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -382,7 +391,7 @@ class Matrix:
 
 
 _ALIASES = {"num_iter": "num_iteration", "numIteration": "num_iteration", "fmt": "mat_type",
-            "regParam": "reg_param", "hist": "hist_size", "tol": "convergence_tol"}
+            "regParam": "reg_param", "hist": "hist_size", "tol": "convergence_tol", "eps": "epsilon"}
 
 
 def glm_params(**kw) -> GlmParams:
@@ -395,6 +404,8 @@ def glm_params(**kw) -> GlmParams:
             raise TypeError(f"unknown training parameter {k!r}")
         if k in ("reg_type",) and isinstance(v, str):
             v = REG[v]
+        if k in ("loss",) and isinstance(v, str):
+            v = LOSS[v]
         if k in ("mat_type",):
             v = _fmt(v)
         if k in ("storage",):
@@ -403,13 +414,17 @@ def glm_params(**kw) -> GlmParams:
     return p
 
 
-def _train(fn, mat: Matrix, label, sample_weight=None, w0=None, b0=None, trace=False, row_splits=None, **kw):
+def _train(fn, mat: Matrix, label, sample_weight=None, w0=None, b0=None, trace=False, row_splits=None,
+           sgd=False, **kw):
     ctx = mat.ctx
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
     icpt = bool(kw.get("intercept", False))
     w = np.ones(mat.n) if w0 is None else np.array(w0, dtype=np.float64)  # weight init = 1 (linear_model.hpp:310)
-    b = C.c_double((1.0 if icpt else 0.0) if b0 is None else float(b0))
+    # initial intercept: the SGD trainers build initModel(numFeatures) (0), the
+    # L-BFGS ones initModel(numFeatures, isIntercept)
+    # (logistic_regression_with_sgd.hpp:300, logistic_regression_with_lbfgs.hpp:301)
+    b = C.c_double((0.0 if sgd or not icpt else 1.0) if b0 is None else float(b0))
     kw["intercept"] = int(icpt)
     p = glm_params(**kw)
     tr = None
@@ -436,7 +451,7 @@ def logreg_lbfgs(mat: Matrix, label, **kw):
     return _train(mat.ctx.L.fvg_logreg_lbfgs, mat, label, **kw)
 
 
-def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=None, b0=None, **kw):
+def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=None, b0=None, _fn=None, **kw):
     """k L-BFGS trainings on one matrix, model j with reg_param = reg_params[j]
     (fvg_logreg_lbfgs_batched).  w0: (k, n) initial weights (default all 1),
     b0: (k,) initial intercepts.  Returns w (k, n), b, n_iter, loss (k,)."""
@@ -455,8 +470,9 @@ def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=
     p = glm_params(**kw)
     n_iter = np.zeros(k, dtype=np.int64)
     loss = np.zeros(k)
-    ctx.check(ctx.L.fvg_logreg_lbfgs_batched(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam),
-                                             _ptr(w), _ptr(b), _ptr(n_iter), _ptr(loss)))
+    fn = ctx.L.fvg_logreg_lbfgs_batched if _fn is None else _fn
+    ctx.check(fn(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam), _ptr(w), _ptr(b), _ptr(n_iter),
+                 _ptr(loss)))
     return dict(w=w, b=b, n_iter=n_iter, loss=loss)
 
 
@@ -490,18 +506,50 @@ def multinomial_probability(mat: Matrix, W, b, intercept=False):
 
 def logreg_sgd(mat: Matrix, label, **kw):
     """logistic_regression_with_sgd::train (defaults as in the reference)."""
-    return _train(mat.ctx.L.fvg_logreg_sgd, mat, label, **kw)
+    return _train(mat.ctx.L.fvg_logreg_sgd, mat, label, sgd=True, **kw)
 
 
-def logreg_eval(mat: Matrix, label, w, b=0.0, intercept=False, sample_weight=None, fmt="CRS", storage="f64"):
+def glm_lbfgs(mat: Matrix, label, loss="linear", **kw):
+    """The GLM family's L-BFGS trainers (fvg_glm_lbfgs): loss "linear" with
+    reg_type ZERO / L2 / L1 = linear_regression / ridge_regression / lasso
+    _with_lbfgs, "hinge" = svm_with_lbfgs, "logistic" as logreg_lbfgs."""
+    return _train(mat.ctx.L.fvg_glm_lbfgs, mat, label, loss=loss, **kw)
+
+
+def glm_sgd(mat: Matrix, label, loss="linear", **kw):
+    """The GLM family's SGD trainers (fvg_glm_sgd): "linear" (linear / ridge /
+    lasso), "hinge" (svm_with_sgd), "eps" / "sqeps" (svm_regression_with_sgd
+    with SVRLossType EPS / SQEPS and ``epsilon``)."""
+    return _train(mat.ctx.L.fvg_glm_sgd, mat, label, sgd=True, loss=loss, **kw)
+
+
+def glm_lbfgs_batched(mat: Matrix, label, reg_params, loss="linear", **kw):
+    """k GLM L-BFGS trainings on one matrix (fvg_glm_lbfgs_batched)."""
+    return logreg_lbfgs_batched(mat, label, reg_params, loss=loss, _fn=mat.ctx.L.fvg_glm_lbfgs_batched, **kw)
+
+
+def logreg_eval(mat: Matrix, label, w, b=0.0, intercept=False, sample_weight=None, fmt="CRS", storage="f64",
+                loss=None, epsilon=0.0):
+    """One loss/gradient evaluation: fvg_logreg_eval, or fvg_glm_eval when a
+    loss kind is named."""
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
     w = np.ascontiguousarray(w, dtype=np.float64)
     g = np.zeros(mat.n + 1)
-    loss = _dbl()
-    mat.ctx.check(mat.ctx.L.fvg_logreg_eval(mat.ctx.h, mat.h, _fmt(fmt), _dt(storage), _ptr(label), _ptr(sw),
-                                            _ptr(w), float(b), int(intercept), _ptr(g), C.byref(loss)))
-    return g, loss.value
+    out = _dbl()
+    L = mat.ctx.L
+    if loss is None:
+        st = L.fvg_logreg_eval(mat.ctx.h, mat.h, _fmt(fmt), _dt(storage), _ptr(label), _ptr(sw), _ptr(w), float(b),
+                               int(intercept), _ptr(g), C.byref(out))
+    else:
+        st = L.fvg_glm_eval(mat.ctx.h, mat.h, _fmt(fmt), _dt(storage), LOSS[loss] if isinstance(loss, str) else loss,
+                            float(epsilon), _ptr(label), _ptr(sw), _ptr(w), float(b), int(intercept), _ptr(g),
+                            C.byref(out))
+    mat.ctx.check(st)
+    return g, out.value
+
+
+glm_eval = logreg_eval
 
 
 def predict_probability(mat: Matrix, w, b=0.0):

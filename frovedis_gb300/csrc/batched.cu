@@ -432,6 +432,8 @@ struct BatchEval {
   DevCRS* AT = nullptr;
   i64 m = 0, n = 0;
   int k = 0, storage = FVG_F64, icpt = 0, master = FVG_F64;
+  int loss = 0;      // GLM loss kind shared by the models
+  double eps = 0.0;
   const double* label = nullptr;
   const double* sw = nullptr;
   DBuf label_f, sw_f, R, s1, s2;
@@ -473,7 +475,7 @@ struct BatchEval {
         ProfScope ps(c, P_BATCH_PASS1);
         crs_spmm_logreg_block(c, *A, storage, (const char*)x + c0 * xs, k, kb, label, sw, label_f.as<float>(),
                               sw ? sw_f.as<float>() : nullptr, icpt, bias + c0, (char*)R.p + c0 * xs, k, ev + 2 * c0,
-                              g + n * k + c0, s1.p);
+                              g + n * k + c0, s1.p, loss, eps);
       }
       ProfScope ps(c, P_BATCH_PASS2);
       crs_spmm_block(c, *AT, storage, (const char*)R.p + c0 * xs, k, kb, FVG_F64, g + c0, k, s2.p);
@@ -519,6 +521,8 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
   }
   BatchEval ev;
   ev.init(c, M, storage, kk, label.as<double>(), sw_h ? sw.as<double>() : nullptr, p->intercept);
+  ev.loss = p->loss;
+  ev.eps = p->epsilon;
 
   const size_t vec = sizeof(double) * (size_t)n1 * kk;
   DBuf W, NW, G, NG, Q, Z, STEP, S, Y, WF, B, EV, ST, part, ctl;

@@ -14,7 +14,7 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
 void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
                double* w_h, double* b_h, i64* n_iter, double* loss_out);
 void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
-                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h);
+                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h, int loss_kind, double eps);
 void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                          const fvg_glm_params* p, i64 k, const double* lam_h, double* w_h, double* b_h,
                          i64* n_iter_h, double* loss_h);
@@ -631,11 +631,34 @@ FVG_API void fvg_glm_params_default(fvg_glm_params* p) {
   p->use_graph = 1;
   p->trace = nullptr;
   p->row_splits = nullptr;
+  p->loss = FVG_LOSS_LOGISTIC;
+  p->epsilon = 0.0;
+}
+
+// The fvg_logreg_* entry points train logistic regression whatever
+// params->loss holds.
+static fvg_glm_params logistic_of(const fvg_glm_params* p) {
+  fvg_glm_params q = *p;
+  q.loss = FVG_LOSS_LOGISTIC;
+  return q;
 }
 
 FVG_API fvg_status fvg_logreg_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* label, const double* sample_weight,
                                     const fvg_glm_params* p, double* weight, double* intercept, int64_t* n_iter,
                                     double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
+  const fvg_glm_params q = logistic_of(p);
+  lbfgs_train(c, M, label, sample_weight, &q, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_glm_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* label, const double* sample_weight,
+                                 const fvg_glm_params* p, double* weight, double* intercept, int64_t* n_iter,
+                                 double* final_loss) {
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
@@ -648,6 +671,20 @@ FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* c, fvg_matrix* M, const dou
                                             const double* sample_weight, const fvg_glm_params* p, int64_t k,
                                             const double* reg_params, double* weight, double* intercept,
                                             int64_t* n_iter, double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss || !reg_params) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
+  const fvg_glm_params q = logistic_of(p);
+  lbfgs_batched_train(c, M, label, sample_weight, &q, k, reg_params, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_glm_lbfgs_batched(fvg_ctx* c, fvg_matrix* M, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* p, int64_t k,
+                                         const double* reg_params, double* weight, double* intercept,
+                                         int64_t* n_iter, double* final_loss) {
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss || !reg_params) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
@@ -684,6 +721,19 @@ FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* c, fvg_matrix* M, const double* label
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
+  need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
+  const fvg_glm_params q = logistic_of(p);
+  sgd_train(c, M, label, sample_weight, &q, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_glm_sgd(fvg_ctx* c, fvg_matrix* M, const double* label, const double* sample_weight,
+                               const fvg_glm_params* p, double* weight, double* intercept, int64_t* n_iter,
+                               double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
   sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
   check_device_error(c);
   API_END(c)
@@ -696,7 +746,22 @@ FVG_API fvg_status fvg_logreg_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fv
   API_BEGIN
   own(c, M);
   need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
-  logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss);
+  logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss,
+              FVG_LOSS_LOGISTIC, 0.0);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_glm_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype storage, int32_t loss,
+                                double epsilon, const double* label, const double* sample_weight,
+                                const double* weight, double intercept, int intercept_on, double* grad,
+                                double* loss_out) {
+  if (!c || !M || !grad || !loss_out || !weight) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss_out, loss,
+              epsilon);
   check_device_error(c);
   API_END(c)
 }

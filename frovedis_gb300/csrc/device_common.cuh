@@ -106,6 +106,47 @@ __device__ __forceinline__ void logistic_row(float wtx, float lab, float& loss, 
   else if (d < -1e12f) d = -1e12f;
 }
 
+// ------------------------------------------------------ GLM loss kinds
+// compute_dloss of the GLM family for one row (ml/glm/gradient.hpp):
+// 0 logistic_gradient, 1 linear_gradient (55-87), 2 hinge_gradient
+// (89-121), 3 epsilon_insensitive (123-159), 4 squared_epsilon_insensitive
+// (161-202).  MAX_LOSS / MIN_LOSS clip at ±1e12, HINGE_THRESHOLD = 1
+// (gradient.hpp:8-10).  The squared loss comes back halved per row: the
+// reference halves a rank's sum (70-73) and scaling by 0.5 is exact, so the
+// halves add up to the same value.  The kind is uniform across a launch.
+enum GlmLossKind { LOSS_LOGISTIC = 0, LOSS_SQUARED = 1, LOSS_HINGE = 2, LOSS_EPS = 3, LOSS_SQEPS = 4 };
+
+template <class AT> __device__ __forceinline__ AT clip_dloss(AT d) {
+  return d > (AT)1e12 ? (AT)1e12 : (d < (AT)-1e12 ? (AT)-1e12 : d);
+}
+
+template <class AT>
+__device__ __forceinline__ void glm_row(int kind, AT eps, AT wtx, AT lab, AT& loss, AT& d) {
+  if (kind == LOSS_LOGISTIC) {
+    logistic_row(wtx, lab, loss, d);
+  } else if (kind == LOSS_SQUARED) {
+    const AT e = wtx - lab;
+    loss = (AT)0.5 * (e * e);
+    d = clip_dloss(e);
+  } else if (kind == LOSS_HINGE) {
+    const AT z = wtx * lab;
+    const bool in = z <= (AT)1;
+    loss = in ? (AT)1 - z : (AT)0;
+    d = in ? -lab : (AT)0;
+  } else {
+    const AT z = lab - wtx;  // positive: the prediction is below the label
+    const AT e = fabs(z) - eps;
+    if (kind == LOSS_EPS) {
+      loss = e > 0 ? e : (AT)0;
+      d = z > eps ? (AT)-1 : ((wtx - lab) > eps ? (AT)1 : (AT)0);
+    } else {
+      loss = e > 0 ? e * e : (AT)0;
+      d = z > eps ? (AT)-2 * (z - eps) : (z < -eps ? (AT)2 * (-z - eps) : (AT)0);
+      d = clip_dloss(d);
+    }
+  }
+}
+
 template <class VT> __device__ __forceinline__ float to_f(VT v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
 template <> __device__ __forceinline__ float to_f<bf16>(bf16 v) { return __bfloat162float(v); }

@@ -234,6 +234,8 @@ struct LogregEpi {
   double* out = nullptr;            // [2]: loss, bias  (written by finalize)
   double* grad_bias = nullptr;      // where the bias lands (grad[n]); may be null
   unsigned* ticket = nullptr;
+  int loss = 0;                     // GLM loss kind (0 logistic .. 4 squared eps-insensitive)
+  double eps = 0.0;                 // epsilon of the eps-insensitive kinds
 };
 // y = A x over the CRS layout (any plane), optional logistic epilogue.
 void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y_dt, void* y, int epi,
@@ -250,7 +252,8 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
                     void* scratch);
 void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
                            const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
-                           void* R, i64 ldr, double* out, double* gbias, void* scratch);
+                           void* R, i64 ldr, double* out, double* gbias, void* scratch, int loss = 0,
+                           double eps = 0.0);
 
 // Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
 void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);

@@ -376,6 +376,8 @@ struct Evaluator {
   const double* label = nullptr;
   const double* sw = nullptr;
   int icpt = 0;
+  int loss = 0;      // GLM loss kind (set after init; logistic by default)
+  double eps = 0.0;  // epsilon of the eps-insensitive kinds
   DBuf r, z, s1, s2, label_f, sw_f;
   void init(fvg_ctx* c_, Operand* op_, int storage_, const double* label_, const double* sw_, int icpt_) {
     c = c_;
@@ -422,6 +424,8 @@ struct Evaluator {
     lr.r_dt = vdt;
     lr.out = out;
     lr.grad_bias = grad + op->n;
+    lr.loss = loss;
+    lr.eps = eps;
     if (op->m == 0) {  // compute_gradient: empty data → zero gradient, no loss
       FVG_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * (op->n + 1), c->stream));
       FVG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 2, c->stream));
@@ -587,6 +591,7 @@ void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label) {
   if (p->storage < 0 || p->storage > 2) fail(FVG_ERR_INVALID_ARG, "unknown storage precision");
   if (p->storage == FVG_F64 && M->master != FVG_F64)
     fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 input values");
+  if (p->loss < FVG_LOSS_LOGISTIC || p->loss > FVG_LOSS_SQ_EPS_INSENSITIVE) fail(FVG_ERR_INVALID_ARG, "Unsupported loss kind!\n");
 }
 
 struct HostPinned {
@@ -619,6 +624,8 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   int storage = p->storage;
   Evaluator ev;
   ev.init(c, &op, storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, p->intercept);
+  ev.loss = p->loss;
+  ev.eps = p->epsilon;
 
   // device vectors
   DBuf W, NW, NWF, G, NG, Q, Z, STEP, S, Y, part, stbuf;
@@ -756,7 +763,8 @@ struct SgdArgs {
   i64 n, n1;
   double* part;
   unsigned* ticket;
-  double* scal;  // [0] rmse, [1] b (accepted), [2] lb (local), [3] tot_b, [4] loss sum, [5] prev b
+  double* scal;  // [0] rmse, [1] b (accepted), [2] lb (local), [3] tot_b, [4] loss sum, [5] prev b,
+                 // [6] the current rank's running loss
 };
 
 // w -= ra * g; b -= ra * bias  (update_model, gradient_descent.hpp:242-259)
@@ -766,9 +774,10 @@ __global__ void k_sgd_update(double* __restrict__ LW, const double* __restrict__
 }
 
 // rank delta LW - W accumulated into TOT in rank order (calc_diff_inplace +
-// typed_allreduce, sgd_parallelizer.hpp:178-187)
+// typed_allreduce, sgd_parallelizer.hpp:178-187); the rank's loss joins the
+// loss sum in the same order (a rank without rows adds 0).
 __global__ void k_sgd_delta(const double* __restrict__ LW, const double* __restrict__ W, double* __restrict__ TOT,
-                            int first, const double* __restrict__ eval, SgdArgs a) {
+                            int first, int has_rows, SgdArgs a) {
   VEC_LOOP(j, a.n) {
     double d = __dsub_rn(LW[j], W[j]);
     TOT[j] = first ? d : __dadd_rn(TOT[j], d);
@@ -776,8 +785,9 @@ __global__ void k_sgd_delta(const double* __restrict__ LW, const double* __restr
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     double db = __dsub_rn(a.scal[2], a.scal[1]);
     a.scal[3] = first ? db : __dadd_rn(a.scal[3], db);
+    const double rl = has_rows ? a.scal[6] : 0.0;
+    a.scal[4] = first ? rl : __dadd_rn(a.scal[4], rl);
   }
-  (void)eval;
 }
 
 // w += Σdelta; b += Σdelta_b; regularize(w, alpha/sqrt(i)); RMSE of the
@@ -806,8 +816,15 @@ __global__ void __launch_bounds__(kVecThreads) k_sgd_apply(double* __restrict__ 
   });
 }
 
-__global__ void k_sgd_loss(const double* __restrict__ out, double* __restrict__ scal, int first) {
-  scal[4] = first ? out[0] : scal[4] + out[0];
+// One minibatch's loss into its rank's running loss (gradient_descent::
+// optimize passes one loss variable through the rank's minibatches,
+// gradient_descent.hpp:128-145).  The squared loss halves the whole running
+// value after each batch (gradient.hpp:70-73); out[0] already holds the
+// batch's halved sum, and halving commutes with rounding, so
+// 0.5 * running + out[0] equals the reference's 0.5 * (running + sum).
+__global__ void k_sgd_loss(const double* __restrict__ out, double* __restrict__ scal, int first, int halve) {
+  const double prev = first ? 0.0 : scal[6];
+  scal[6] = __dadd_rn(halve ? 0.5 * prev : prev, out[0]);
 }
 
 void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
@@ -856,6 +873,8 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
       b->r0 = r0;
       build_block_operand(c, M, fmt, r0, r1, b->op);
       b->ev.init(c, &b->op, storage, label.as<double>() + r0, sw_h ? sw.as<double>() + r0 : nullptr, p->intercept);
+      b->ev.loss = p->loss;
+      b->ev.eps = p->epsilon;
       ranks[r].push_back(std::move(b));
     }
   }
@@ -879,8 +898,9 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
   i64 i;
   for (i = 1; i <= p->num_iteration; i++) {
     const double ra = p->alpha / std::sqrt((double)i);
-    bool first_rank = true, first_loss = true;
+    bool first_rank = true;
     for (int r = 0; r < P; r++) {
+      bool first_loss = true;
       FVG_CUDA(cudaMemcpyAsync(LW.p, W.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
       FVG_CUDA(cudaMemcpyAsync(scal.as<double>() + 2, scal.as<double>() + 1, sizeof(double),
                                cudaMemcpyDeviceToDevice, s));
@@ -893,14 +913,15 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
           x = LWF.p;
         }
         b->ev.eval(x, scal.as<double>() + 2, G.as<double>(), out.as<double>());
-        k_sgd_loss<<<1, 1, 0, s>>>(out.as<double>(), scal.as<double>(), first_loss ? 1 : 0);
+        k_sgd_loss<<<1, 1, 0, s>>>(out.as<double>(), scal.as<double>(), first_loss ? 1 : 0,
+                                   p->loss == FVG_LOSS_SQUARED ? 1 : 0);
         k_sgd_update<<<vgrid, kVecThreads, 0, s>>>(LW.as<double>(), G.as<double>(), ra, p->intercept, sa);
         check_launch("sgd_update");
         count_launch(c, 2);
         first_loss = false;
       }
       k_sgd_delta<<<vgrid, kVecThreads, 0, s>>>(LW.as<double>(), W.as<double>(), TOT.as<double>(), first_rank ? 1 : 0,
-                                                out.as<double>(), sa);
+                                                ranks[r].empty() ? 0 : 1, sa);
       check_launch("sgd_delta");
       count_launch(c);
       first_rank = false;
@@ -923,7 +944,8 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
 
 // ====================================================== single evaluation
 void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
-                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h) {
+                 const double* w_h, double b, int icpt, double* grad_h, double* loss_h, int loss_kind, double eps) {
+  if (loss_kind < FVG_LOSS_LOGISTIC || loss_kind > FVG_LOSS_SQ_EPS_INSENSITIVE) fail(FVG_ERR_INVALID_ARG, "Unsupported loss kind!\n");
   if (fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
   if (storage == FVG_F64 && M->master != FVG_F64) fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 values");
   const i64 m = M->A.m, n = M->A.n;
@@ -946,6 +968,8 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
   FVG_CUDA(cudaMemcpyAsync(bd.p, &b, sizeof(double), cudaMemcpyHostToDevice, s));
   Evaluator ev;
   ev.init(c, &op, storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, icpt);
+  ev.loss = loss_kind;
+  ev.eps = eps;
   const void* x = w.p;
   if (storage != FVG_F64) {
     k_d2f<<<256, kVecThreads, 0, s>>>(w.as<double>(), wf.as<float>(), n);

@@ -44,6 +44,8 @@ struct SpmmK {
   void* R;             // epilogue output (accumulator type), row stride ldr
   i64 ldr;
   double* cta_part;  // logistic: [grid][64][2] loss, bias
+  int loss;          // GLM loss kind of the per-model epilogue
+  double eps;
 };
 
 template <class VT, class XT, class AT, int CPL>
@@ -108,7 +110,7 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
     for (int q = 0; q < CPL; q++) {
       if (!ON(q)) continue;
       AT loss, d;
-      logistic_row(a[q] + b[q], lab, loss, d);
+      glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
       if (has_sw) d = d * w;
       r[32 * q] = d;
       ls[q].add(loss);
@@ -378,12 +380,13 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
   }
 }
 
-// Batched logistic forward pass over a block of kb <= 64 models: R = dloss(A
-// W + b) * sw per (row, model); out[2j] = loss of model j, out[2j+1] = its
-// bias sum (0 without intercept), also written to gbias[j] when given.
+// Batched GLM forward pass over a block of kb <= 64 models: R = dloss(A W +
+// b) * sw per (row, model) for the loss kind `loss`; out[2j] = loss of model
+// j, out[2j+1] = its bias sum (0 without intercept), also written to gbias[j]
+// when given.
 void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
                            const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
-                           void* R, i64 ldr, double* out, double* gbias, void* scratch) {
+                           void* R, i64 ldr, double* out, double* gbias, void* scratch, int loss, double eps) {
   if (kb < 1 || kb > 64) fail(FVG_ERR_INTERNAL, "spmm block width out of range");
   const Sched& s = crs_sched(c, a, tile_for_storage(storage));
   SpmmK p = {};
@@ -398,6 +401,8 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
   p.bias = bias;
   p.R = R;
   p.ldr = ldr;
+  p.loss = loss;
+  p.eps = eps;
   char* sc = (char*)scratch;
   FVG_CUDA(cudaMemsetAsync(sc, 0, 256, c->stream));
   if (storage == FVG_F64)

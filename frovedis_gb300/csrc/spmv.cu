@@ -43,6 +43,8 @@ struct CrsK {
   void* r;
   double* cta_part;
   unsigned* err;
+  int loss;    // GLM loss kind
+  double eps;  // its epsilon
 };
 
 template <class AT, class YT, int EPI, class S>
@@ -53,10 +55,10 @@ __device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, S
     AT wtx = acc + b;
     AT loss, d;
     if constexpr (sizeof(AT) == 8) {
-      logistic_row(wtx, p.label[row], loss, d);
+      glm_row<AT>(p.loss, (AT)p.eps, wtx, p.label[row], loss, d);
       if (p.sw) d = d * p.sw[row];
     } else {
-      logistic_row(wtx, p.label_f[row], loss, d);
+      glm_row<AT>(p.loss, (AT)p.eps, wtx, p.label_f[row], loss, d);
       if (p.sw_f) d = d * p.sw_f[row];
     }
     ((YT*)p.r)[row] = (YT)d;
@@ -183,6 +185,8 @@ struct FinK {
   double* out;        // [loss, bias]
   double* grad_bias;  // optional
   unsigned* ticket;
+  int loss;
+  double eps;
 };
 
 // Long rows: sum the pieces' partials in piece order and apply the
@@ -203,10 +207,10 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
       } else {
         AT loss, d, wtx = acc + b;
         if constexpr (sizeof(AT) == 8) {
-          logistic_row(wtx, f.label[row], loss, d);
+          glm_row<AT>(f.loss, (AT)f.eps, wtx, f.label[row], loss, d);
           if (f.sw) d = d * f.sw[row];
         } else {
-          logistic_row(wtx, f.label_f[row], loss, d);
+          glm_row<AT>(f.loss, (AT)f.eps, wtx, f.label_f[row], loss, d);
           if (f.sw_f) d = d * f.sw_f[row];
         }
         ((YT*)f.r)[row] = (YT)d;
@@ -312,6 +316,8 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
   p.r = lr ? lr->r : nullptr;
   p.cta_part = ps.cta_part;
   p.err = c->dev_err;
+  p.loss = lr ? lr->loss : 0;
+  p.eps = lr ? lr->eps : 0.0;
   int grid = (int)std::max<i64>(1, std::min<i64>(crs_grid<VT, XT, AT, YT, EPI>(c, s.tile), s.nitems));
   grid = std::min(grid, c->grid_spmv);
   if (s.nitems > 0) {
@@ -339,6 +345,8 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
     f.out = (lr && lr->out) ? lr->out : ps.out;
     f.grad_bias = lr ? lr->grad_bias : nullptr;
     f.ticket = ps.ticket;
+    f.loss = p.loss;
+    f.eps = p.eps;
     int fg = (int)std::max<i64>(1, std::min<i64>(s.nlong, 4 * c->num_sms));
     ProfScope pf(c, timed ? P_FINALIZE : P_NKEYS);
     k_finalize<AT, YT, EPI><<<fg, kThreads, 0, c->stream>>>(f);
@@ -647,6 +655,8 @@ void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi
   p.icpt = lr.icpt;
   p.r = lr.r;
   p.cta_part = cta;
+  p.loss = lr.loss;
+  p.eps = lr.eps;
   if (wtx_dt == FVG_F64) k_logreg_rows<double><<<grid, 256, 0, c->stream>>>((const double*)wtx, m, p);
   else k_logreg_rows<float><<<grid, 256, 0, c->stream>>>((const float*)wtx, m, p);
   check_launch("k_logreg_rows");
@@ -665,6 +675,8 @@ void logreg_rows(fvg_ctx* c, const void* wtx, int wtx_dt, i64 m, const LogregEpi
   f.out = lr.out ? lr.out : out;
   f.grad_bias = lr.grad_bias;
   f.ticket = ticket;
+  f.loss = lr.loss;
+  f.eps = lr.eps;
   if (wtx_dt == FVG_F64) k_finalize<double, double, EPI_LOGREG><<<1, kThreads, 0, c->stream>>>(f);
   else k_finalize<float, float, EPI_LOGREG><<<1, kThreads, 0, c->stream>>>(f);
   check_launch("k_finalize_rows");

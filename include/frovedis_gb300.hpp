@@ -450,18 +450,23 @@ struct logistic_regression_model {
   T get_threshold() const { return threshold; }
   size_t get_num_features() const { return weight.size(); }
   size_t get_num_classes() const { return 2; }
+  void save(const std::string& path) const;
+  void savebinary(const std::string& path) const;
+  void load(const std::string& path);
+  void loadbinary(const std::string& path);
   std::vector<T> weight;
   T intercept;
   T threshold;
 };
 
 namespace detail {
-template <class T, class I, class O>
-logistic_regression_model<T> train(bool sgd, crs_matrix_local<T, I, O>& data, std::vector<T>& label,
-                                   logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
-                                   size_t& n_iter, size_t numIteration, double alpha, size_t hist_size,
-                                   double miniBatchFraction, double regParam, RegType regTyp, bool isIntercept,
-                                   double convergenceTol, MatType mType) {
+// One train() of any binary GLM: the model type carries weight / intercept;
+// loss selects the gradient (fvg_loss), eps its epsilon.
+template <class T, class I, class O, class MODEL>
+MODEL train(bool sgd, crs_matrix_local<T, I, O>& data, std::vector<T>& label, MODEL& initModel,
+            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration, double alpha, size_t hist_size,
+            double miniBatchFraction, double regParam, RegType regTyp, bool isIntercept, double convergenceTol,
+            MatType mType, fvg_loss loss = FVG_LOSS_LOGISTIC, double eps = 0.0) {
   if (data.local_num_col != initModel.get_num_features())
     throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Incompatible Test Vector with Provided Initial Model\n");
   if (data.local_num_row != label.size())
@@ -480,14 +485,16 @@ logistic_regression_model<T> train(bool sgd, crs_matrix_local<T, I, O>& data, st
   p.mat_type = mType;
   p.mini_batch_fraction = miniBatchFraction;
   p.storage = frovedis_gb300::dtype_of<T>::value;
+  p.loss = loss;
+  p.epsilon = eps;
   std::vector<double> lab(label.begin(), label.end()), sw(sample_weight.begin(), sample_weight.end());
   std::vector<double> w(initModel.weight.begin(), initModel.weight.end());
-  double b = initModel.intercept, loss = 0;
+  double b = initModel.intercept, fl = 0;
   int64_t it = 0;
-  frovedis_gb300::check((sgd ? fvg_logreg_sgd : fvg_logreg_lbfgs)(frovedis_gb300::context(), d.h, lab.data(),
-                                                                  sw.data(), &p, w.data(), &b, &it, &loss));
+  frovedis_gb300::check((sgd ? fvg_glm_sgd : fvg_glm_lbfgs)(frovedis_gb300::context(), d.h, lab.data(), sw.data(),
+                                                            &p, w.data(), &b, &it, &fl));
   n_iter = (size_t)it;
-  logistic_regression_model<T> ret = initModel;
+  MODEL ret = initModel;
   ret.weight.assign(w.begin(), w.end());
   ret.intercept = (T)b;
   return ret;
@@ -540,7 +547,7 @@ struct logistic_regression_with_sgd {
                                             double miniBatchFraction = 1.0, double regParam = 0.01,
                                             RegType regTyp = ZERO, bool isIntercept = false,
                                             double convergenceTol = 0.001, MatType mType = CRS) {
-    logistic_regression_model<T> initModel(data.local_num_col, isIntercept ? 1.0 : 0.0);
+    logistic_regression_model<T> initModel(data.local_num_col);  // intercept 0 (line 300)
     size_t n_iter = 0;
     std::vector<T> sample_weight;
     return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
@@ -559,6 +566,351 @@ struct logistic_regression_with_sgd {
                            miniBatchFraction, regParam, regTyp, isIntercept, convergenceTol, mType);
     if (inputMovable) data.clear();
     return m;
+  }
+};
+
+// linear_regression_model<T> (ml/glm/linear_model.hpp:211-298): weights
+// start at 1; predict = mat * weight (+ intercept when non-zero).
+template <class T>
+struct linear_regression_model {
+  linear_regression_model() : intercept(0.0) {}
+  linear_regression_model(size_t numFtr, T intercpt = 0.0) : weight(numFtr, 1), intercept(intercpt) {}
+  template <class MATRIX>
+  std::vector<T> predict(const MATRIX& mat) const {
+    std::vector<T> v = mat * weight;
+    if (intercept != 0)
+      for (auto& x : v) x += intercept;
+    return v;
+  }
+  size_t get_num_features() const { return weight.size(); }
+  void save(const std::string& path) const;
+  void savebinary(const std::string& path) const;
+  void load(const std::string& path);
+  void loadbinary(const std::string& path);
+  std::vector<T> weight;
+  T intercept;
+};
+
+#define FVG_YES_RESPONSE 1   // linear_model.hpp:13-14
+#define FVG_NO_RESPONSE -1
+
+// svm_model<T> (ml/glm/linear_model.hpp:466-594): predict_probability is the
+// raw score mat * weight (+ intercept); predict is +1 where the score is
+// above 0, else -1 (the threshold is kept but not used, lines 538-549).
+template <class T>
+struct svm_model {
+  svm_model() : intercept(0.0), threshold(0.0) {}
+  svm_model(size_t numFtr, T intercpt = 0.0, T thr = 0.0) : weight(numFtr, 1), intercept(intercpt), threshold(thr) {
+    if (!(thr >= 0)) throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "checkAssumption failed: thr >= 0");
+  }
+  template <class MATRIX>
+  std::vector<T> predict_probability(const MATRIX& mat, bool = false) const {
+    std::vector<T> v = mat * weight;
+    if (intercept != 0)
+      for (auto& x : v) x += intercept;
+    return v;
+  }
+  template <class MATRIX>
+  std::vector<T> predict(const MATRIX& mat) const {
+    auto s = predict_probability(mat);
+    std::vector<T> r(s.size());
+    for (size_t i = 0; i < s.size(); i++) r[i] = s[i] > 0 ? FVG_YES_RESPONSE : FVG_NO_RESPONSE;
+    return r;
+  }
+  void set_threshold(T thr) {
+    if (thr < 0) throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Negative Threshold Value\n");
+    threshold = thr;
+  }
+  T get_threshold() const { return threshold; }
+  size_t get_num_features() const { return weight.size(); }
+  size_t get_num_classes() const { return 2; }
+  void save(const std::string& path) const;
+  void savebinary(const std::string& path) const;
+  void load(const std::string& path);
+  void loadbinary(const std::string& path);
+  std::vector<T> weight;
+  T intercept;
+  T threshold;
+};
+
+// The regression and SVM trainers: one template per (model, loss,
+// regulariser) over the shared device driver.  SGD trainers start from
+// initModel(numFeatures) (intercept 0), L-BFGS trainers from
+// initModel(numFeatures, isIntercept) (e.g. linear_regression_with_sgd.hpp:242,
+// linear_regression_with_lbfgs.hpp:243).
+namespace detail {
+template <class MODEL, class T, class I, class O>
+MODEL glm_sgd(crs_matrix_local<T, I, O>& data, std::vector<T>& label, MODEL& initModel,
+              std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration, double alpha,
+              double miniBatchFraction, double regParam, RegType regTyp, bool isIntercept, double convergenceTol,
+              MatType mType, bool inputMovable, fvg_loss loss, double eps = 0.0) {
+  auto m = train(true, data, label, initModel, sample_weight, n_iter, numIteration, alpha, 10, miniBatchFraction,
+                 regParam, regTyp, isIntercept, convergenceTol, mType, loss, eps);
+  if (inputMovable) data.clear();
+  return m;
+}
+template <class MODEL, class T, class I, class O>
+MODEL glm_lbfgs(crs_matrix_local<T, I, O>& data, std::vector<T>& label, MODEL& initModel,
+                std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration, double alpha, size_t hist_size,
+                double regParam, RegType regTyp, bool isIntercept, double convergenceTol, MatType mType,
+                bool inputMovable, fvg_loss loss) {
+  auto m = train(false, data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, 1.0,
+                 regParam, regTyp, isIntercept, convergenceTol, mType, loss);
+  if (inputMovable) data.clear();
+  return m;
+}
+}  // namespace detail
+
+// linear_regression_with_sgd (ml/glm/linear_regression_with_sgd.hpp:304-330):
+// linear_gradient, zero_regularizer.
+struct linear_regression_with_sgd {
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, miniBatchFraction, isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                          double alpha = 0.01, double miniBatchFraction = 1.0,
+                                          bool isIntercept = false, double convergenceTol = 0.001,
+                                          MatType mType = CRS) {
+    linear_regression_model<T> initModel(data.local_num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          linear_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                          size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS,
+                                          bool inputMovable = false) {
+    return detail::glm_sgd(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, 0.0,
+                           ZERO, isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_SQUARED);
+  }
+};
+
+// linear_regression_with_lbfgs (ml/glm/linear_regression_with_lbfgs.hpp:319-352)
+struct linear_regression_with_lbfgs {
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          size_t numIteration = 1000, double alpha = 0.01, size_t hist_size = 10,
+                                          bool isIntercept = false, double convergenceTol = 0.001,
+                                          MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, hist_size, isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                          double alpha = 0.01, size_t hist_size = 10, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS) {
+    linear_regression_model<T> initModel(data.local_num_col, isIntercept);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          linear_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                          size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                          size_t hist_size = 10, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS,
+                                          bool inputMovable = false) {
+    return detail::glm_lbfgs(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, 0.0, ZERO,
+                             isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_SQUARED);
+  }
+};
+
+// lasso_with_sgd / ridge_regression_with_sgd (ml/glm/lasso_with_sgd.hpp,
+// ridge_regression_with_sgd.hpp): linear_gradient with l1_regularizer /
+// l2_regularizer(regParam).
+template <RegType REG>
+struct penalized_regression_with_sgd {
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, double regParam = 0.01,
+                                          bool isIntercept = false, double convergenceTol = 0.001,
+                                          MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, miniBatchFraction, regParam, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                          double alpha = 0.01, double miniBatchFraction = 1.0,
+                                          double regParam = 0.01, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS) {
+    linear_regression_model<T> initModel(data.local_num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          linear_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                          size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, double regParam = 0.01,
+                                          bool isIntercept = false, double convergenceTol = 0.001,
+                                          MatType mType = CRS, bool inputMovable = false) {
+    return detail::glm_sgd(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction,
+                           regParam, REG, isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_SQUARED);
+  }
+};
+using lasso_with_sgd = penalized_regression_with_sgd<L1>;
+using ridge_regression_with_sgd = penalized_regression_with_sgd<L2>;
+
+// lasso_with_lbfgs / ridge_regression_with_lbfgs (lasso_with_lbfgs.hpp,
+// ridge_regression_with_lbfgs.hpp)
+template <RegType REG>
+struct penalized_regression_with_lbfgs {
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          size_t numIteration = 1000, double alpha = 0.01, size_t hist_size = 10,
+                                          double regParam = 0.01, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, hist_size, regParam, isIntercept, convergenceTol,
+                 mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                          double alpha = 0.01, size_t hist_size = 10, double regParam = 0.01,
+                                          bool isIntercept = false, double convergenceTol = 0.001,
+                                          MatType mType = CRS) {
+    linear_regression_model<T> initModel(data.local_num_col, isIntercept);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam,
+                 isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          linear_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                          size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                          size_t hist_size = 10, double regParam = 0.01, bool isIntercept = false,
+                                          double convergenceTol = 0.001, MatType mType = CRS,
+                                          bool inputMovable = false) {
+    return detail::glm_lbfgs(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size,
+                             regParam, REG, isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_SQUARED);
+  }
+};
+using lasso_with_lbfgs = penalized_regression_with_lbfgs<L1>;
+using ridge_regression_with_lbfgs = penalized_regression_with_lbfgs<L2>;
+
+// svm_with_sgd (ml/glm/svm_with_sgd.hpp): hinge_gradient, labels +-1.
+struct svm_with_sgd {
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, size_t numIteration = 1000,
+                            double alpha = 0.01, double miniBatchFraction = 1.0, double regParam = 0.01,
+                            RegType regTyp = ZERO, bool isIntercept = false, double convergenceTol = 0.001,
+                            MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, miniBatchFraction, regParam, regTyp, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, std::vector<T>& sample_weight,
+                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                            double miniBatchFraction = 1.0, double regParam = 0.01, RegType regTyp = ZERO,
+                            bool isIntercept = false, double convergenceTol = 0.001, MatType mType = CRS) {
+    svm_model<T> initModel(data.local_num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, svm_model<T>& initModel,
+                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                            double alpha = 0.01, double miniBatchFraction = 1.0, double regParam = 0.01,
+                            RegType regTyp = ZERO, bool isIntercept = false, double convergenceTol = 0.001,
+                            MatType mType = CRS, bool inputMovable = false) {
+    return detail::glm_sgd(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction,
+                           regParam, regTyp, isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_HINGE);
+  }
+};
+
+// svm_with_lbfgs (ml/glm/svm_with_lbfgs.hpp)
+struct svm_with_lbfgs {
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, size_t numIteration = 1000,
+                            double alpha = 0.01, size_t hist_size = 10, double regParam = 0.01,
+                            RegType regTyp = ZERO, bool isIntercept = false, double convergenceTol = 0.001,
+                            MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, hist_size, regParam, regTyp, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, std::vector<T>& sample_weight,
+                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01, size_t hist_size = 10,
+                            double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                            double convergenceTol = 0.001, MatType mType = CRS) {
+    svm_model<T> initModel(data.local_num_col, isIntercept);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static svm_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label, svm_model<T>& initModel,
+                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                            double alpha = 0.01, size_t hist_size = 10, double regParam = 0.01,
+                            RegType regTyp = ZERO, bool isIntercept = false, double convergenceTol = 0.001,
+                            MatType mType = CRS, bool inputMovable = false) {
+    return detail::glm_lbfgs(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam,
+                             regTyp, isIntercept, convergenceTol, mType, inputMovable, FVG_LOSS_HINGE);
+  }
+};
+
+// SVRLossType and svm_regression_with_sgd (ml/glm/svm_regression_with_sgd.hpp:
+// 8-11, 373-444): epsilon_insensitive (EPS) or squared_epsilon_insensitive
+// (SQEPS) with epsilon; a linear_regression_model.
+enum SVRLossType { EPS = 0, SQEPS };
+struct svm_regression_with_sgd {
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, double regParam = 0.01,
+                                          RegType regTyp = ZERO, bool isIntercept = false,
+                                          double convergenceTol = 0.001, double epsilon = 0.0,
+                                          SVRLossType lossType = EPS, MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, miniBatchFraction, regParam, regTyp, isIntercept,
+                 convergenceTol, epsilon, lossType, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                          double alpha = 0.01, double miniBatchFraction = 1.0,
+                                          double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                                          double convergenceTol = 0.001, double epsilon = 0.0,
+                                          SVRLossType lossType = EPS, MatType mType = CRS) {
+    linear_regression_model<T> initModel(data.local_num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, epsilon, lossType, mType);
+  }
+  template <class T, class I, class O>
+  static linear_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                          linear_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                          size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                          double miniBatchFraction = 1.0, double regParam = 0.01,
+                                          RegType regTyp = ZERO, bool isIntercept = false,
+                                          double convergenceTol = 0.001, double epsilon = 0.0,
+                                          SVRLossType lossType = EPS, MatType mType = CRS,
+                                          bool inputMovable = false) {
+    if (lossType != EPS && lossType != SQEPS)
+      throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Unsupported SVR Loss!\n");
+    return detail::glm_sgd(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction,
+                           regParam, regTyp, isIntercept, convergenceTol, mType, inputMovable,
+                           lossType == EPS ? FVG_LOSS_EPS_INSENSITIVE : FVG_LOSS_SQ_EPS_INSENSITIVE, epsilon);
   }
 };
 
@@ -617,6 +969,10 @@ struct multinomial_logistic_regression_model {
   size_t get_num_classes() const { return nclasses; }
   T get_threshold() const { return threshold; }
   void set_threshold(T thr) { threshold = thr; }
+  void save(const std::string& dir) const;
+  void savebinary(const std::string& dir) const;
+  void load(const std::string& dir);
+  void loadbinary(const std::string& dir);
   rowmajor_matrix_local<T> weight;  // nfeatures x nclasses
   std::vector<T> intercept;
   size_t nfeatures, nclasses;
@@ -761,38 +1117,80 @@ template <class T> rowmajor_matrix_local<T> make_rowmajor_matrix_local_loadbinar
   return ret;
 }
 
-// glm_save / glm_savebinary / glm_load / glm_loadbinary of the binary model
-// (ml/glm/linear_model.hpp:39-150): weights, intercept, threshold
-template <class T> void save(const logistic_regression_model<T>& m, const std::string& path) {
+// glm_save / glm_savebinary / glm_load / glm_loadbinary
+// (ml/glm/linear_model.hpp:39-140): the weights, the intercept and, for the
+// classifiers, the threshold, one value per line (12 significant digits) or
+// as one raw array.  The linear-regression overloads have no threshold.
+namespace detail {
+template <class T> void glm_save(const std::vector<T>& w, T icpt, const T* thr, const std::string& path) {
   std::ofstream out(path.c_str());
   out << std::setprecision(12);
-  for (auto w : m.weight) out << w << "\n";
-  out << m.intercept << std::endl;
-  out << m.threshold << std::endl;
+  for (auto x : w) out << x << "\n";
+  out << icpt << std::endl;
+  if (thr) out << *thr << std::endl;
+}
+template <class T> void glm_savebinary(const std::vector<T>& w, T icpt, const T* thr, const std::string& path) {
+  std::vector<T> tmp(w);
+  tmp.push_back(icpt);
+  if (thr) tmp.push_back(*thr);
+  write_raw(path, tmp);
+}
+template <class T> void glm_split(std::vector<T>& w, T& icpt, T* thr, const std::string& path) {
+  if (w.size() < (thr ? 2u : 1u)) throw std::runtime_error("model file " + path + " is too short");
+  if (thr) {
+    *thr = w.back();
+    w.pop_back();
+  }
+  icpt = w.back();
+  w.pop_back();
+}
+template <class T> void glm_load(std::vector<T>& w, T& icpt, T* thr, const std::string& path) {
+  std::ifstream in(path.c_str());
+  w.clear();
+  for (T x; in >> x;) w.push_back(x);
+  glm_split(w, icpt, thr, path);
+}
+template <class T> void glm_loadbinary(std::vector<T>& w, T& icpt, T* thr, const std::string& path) {
+  w = read_raw<T>(path);
+  glm_split(w, icpt, thr, path);
+}
+}  // namespace detail
+
+template <class T> void save(const logistic_regression_model<T>& m, const std::string& path) {
+  detail::glm_save(m.weight, m.intercept, &m.threshold, path);
 }
 template <class T> void savebinary(const logistic_regression_model<T>& m, const std::string& path) {
-  std::vector<T> tmp(m.weight);
-  tmp.push_back(m.intercept);
-  tmp.push_back(m.threshold);
-  detail::write_raw(path, tmp);
+  detail::glm_savebinary(m.weight, m.intercept, &m.threshold, path);
 }
 template <class T> void load(logistic_regression_model<T>& m, const std::string& path) {
-  std::ifstream in(path.c_str());
-  m.weight.clear();
-  for (T x; in >> x;) m.weight.push_back(x);
-  if (m.weight.size() < 2) throw std::runtime_error("model file " + path + " is too short");
-  m.threshold = m.weight.back();
-  m.weight.pop_back();
-  m.intercept = m.weight.back();
-  m.weight.pop_back();
+  detail::glm_load(m.weight, m.intercept, &m.threshold, path);
 }
 template <class T> void loadbinary(logistic_regression_model<T>& m, const std::string& path) {
-  m.weight = detail::read_raw<T>(path);
-  if (m.weight.size() < 2) throw std::runtime_error("model file " + path + " is too short");
-  m.threshold = m.weight.back();
-  m.weight.pop_back();
-  m.intercept = m.weight.back();
-  m.weight.pop_back();
+  detail::glm_loadbinary(m.weight, m.intercept, &m.threshold, path);
+}
+template <class T> void save(const svm_model<T>& m, const std::string& path) {
+  detail::glm_save(m.weight, m.intercept, &m.threshold, path);
+}
+template <class T> void savebinary(const svm_model<T>& m, const std::string& path) {
+  detail::glm_savebinary(m.weight, m.intercept, &m.threshold, path);
+}
+template <class T> void load(svm_model<T>& m, const std::string& path) {
+  detail::glm_load(m.weight, m.intercept, &m.threshold, path);
+}
+template <class T> void loadbinary(svm_model<T>& m, const std::string& path) {
+  detail::glm_loadbinary(m.weight, m.intercept, &m.threshold, path);
+}
+template <class T> void save(const linear_regression_model<T>& m, const std::string& path) {
+  detail::glm_save<T>(m.weight, m.intercept, nullptr, path);
+}
+template <class T> void savebinary(const linear_regression_model<T>& m, const std::string& path) {
+  detail::glm_savebinary<T>(m.weight, m.intercept, nullptr, path);
+}
+template <class T> void load(linear_regression_model<T>& m, const std::string& path) {
+  detail::glm_load<T>(m.weight, m.intercept, nullptr, path);
+}
+template <class T> void loadbinary(linear_regression_model<T>& m, const std::string& path) {
+  detail::glm_loadbinary<T>(m.weight, m.intercept, nullptr, path);
 }
 
 // multinomial model save / savebinary / load / loadbinary
@@ -827,6 +1225,19 @@ template <class T> void loadbinary(multinomial_logistic_regression_model<T>& m, 
   std::ifstream md((dir + "/metadata").c_str());
   md >> m.nclasses >> m.nfeatures >> m.isIntercept >> m.threshold;
 }
+
+// Member forms of the persistence calls (model.save(path) ... as the
+// reference's models declare them).
+#define FVG_GLM_MEMBERS(MODEL)                                                                            \
+  template <class T> void MODEL<T>::save(const std::string& p) const { frovedis::save(*this, p); }             \
+  template <class T> void MODEL<T>::savebinary(const std::string& p) const { frovedis::savebinary(*this, p); } \
+  template <class T> void MODEL<T>::load(const std::string& p) { frovedis::load(*this, p); }                   \
+  template <class T> void MODEL<T>::loadbinary(const std::string& p) { frovedis::loadbinary(*this, p); }
+FVG_GLM_MEMBERS(logistic_regression_model)
+FVG_GLM_MEMBERS(linear_regression_model)
+FVG_GLM_MEMBERS(svm_model)
+FVG_GLM_MEMBERS(multinomial_logistic_regression_model)
+#undef FVG_GLM_MEMBERS
 
 // accuracy_score (ml/metrics.hpp:383-396)
 template <class T> float accuracy_score(const std::vector<T>& true_label, const std::vector<T>& pred_label) {

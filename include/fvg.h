@@ -52,6 +52,18 @@ typedef enum { FVG_CRS = 0, FVG_JDS = 1, FVG_ELL = 2, FVG_HYBRID = 3 } fvg_forma
 
 /* same numbering as frovedis::RegType (ml/glm/regularizer.hpp:8-12) */
 typedef enum { FVG_REG_ZERO = 0, FVG_REG_L1 = 1, FVG_REG_L2 = 2 } fvg_regtype;
+/* Loss of the GLM family (ml/glm/gradient.hpp): logistic_gradient (logistic
+ * regression), linear_gradient (linear / ridge / lasso regression),
+ * hinge_gradient (linear SVM), epsilon_insensitive and
+ * squared_epsilon_insensitive (SVM regression, SVRLossType EPS / SQEPS,
+ * svm_regression_with_sgd.hpp:8-11). */
+typedef enum {
+  FVG_LOSS_LOGISTIC = 0,
+  FVG_LOSS_SQUARED = 1,
+  FVG_LOSS_HINGE = 2,
+  FVG_LOSS_EPS_INSENSITIVE = 3,
+  FVG_LOSS_SQ_EPS_INSENSITIVE = 4
+} fvg_loss;
 
 /* ------------------------------------------------------------- context */
 FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out);
@@ -204,6 +216,10 @@ typedef struct {
   double* trace;              /* optional host array, 4 doubles per iteration:
                                  loss, line-search trials, rms, step factor */
   const int64_t* row_splits;  /* optional num_partitions+1 row splits */
+  int32_t loss;               /* fvg_loss of fvg_glm_* trainers (default
+                                 LOGISTIC; the fvg_logreg_* entry points
+                                 always use LOGISTIC) */
+  double epsilon;             /* epsilon of the eps-insensitive losses (default 0) */
 } fvg_glm_params;
 
 FVG_API void fvg_glm_params_default(fvg_glm_params* p);
@@ -265,6 +281,37 @@ FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* ctx, fvg_matrix* mat, const double* l
 FVG_API fvg_status fvg_logreg_eval(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage,
                                    const double* label, const double* sample_weight, const double* weight,
                                    double intercept, int intercept_on, double* grad, double* loss);
+/* The GLM family on the same device path, the loss taken from params->loss
+ * (params->epsilon for the eps-insensitive kinds); otherwise as
+ * fvg_logreg_lbfgs / fvg_logreg_sgd / fvg_logreg_lbfgs_batched:
+ *   FVG_LOSS_SQUARED: linear_regression_with_{sgd,lbfgs} (reg_type ZERO),
+ *     ridge_regression_with_{sgd,lbfgs} (L2), lasso_with_{sgd,lbfgs} (L1)
+ *     (ml/glm/linear_regression_with_sgd.hpp:304-330, ..._with_lbfgs.hpp,
+ *     ridge_regression_with_*.hpp, lasso_with_*.hpp);
+ *   FVG_LOSS_HINGE: svm_with_{sgd,lbfgs} (svm_with_sgd.hpp, svm_with_lbfgs.hpp),
+ *     label +-1;
+ *   FVG_LOSS_EPS_INSENSITIVE / FVG_LOSS_SQ_EPS_INSENSITIVE:
+ *     svm_regression_with_sgd (svm_regression_with_sgd.hpp:373-444).
+ * The reference's SGD trainers start from intercept 0, its L-BFGS trainers
+ * from intercept = isIntercept (…_with_sgd.hpp initModel(numFeatures) vs
+ * …_with_lbfgs.hpp initModel(numFeatures, intercept)); the caller passes the
+ * initial model. */
+FVG_API fvg_status fvg_glm_lbfgs(fvg_ctx* ctx, fvg_matrix* mat, const double* label, const double* sample_weight,
+                                 const fvg_glm_params* params, double* weight, double* intercept, int64_t* n_iter,
+                                 double* final_loss);
+FVG_API fvg_status fvg_glm_sgd(fvg_ctx* ctx, fvg_matrix* mat, const double* label, const double* sample_weight,
+                               const fvg_glm_params* params, double* weight, double* intercept, int64_t* n_iter,
+                               double* final_loss);
+FVG_API fvg_status fvg_glm_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* params, int64_t k,
+                                         const double* reg_params, double* weight, double* intercept,
+                                         int64_t* n_iter, double* final_loss);
+/* One loss/gradient evaluation for any fvg_loss (compute_gradient with the
+ * kind's compute_dloss, gradient.hpp). */
+FVG_API fvg_status fvg_glm_eval(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage, int32_t loss,
+                                double epsilon, const double* label, const double* sample_weight,
+                                const double* weight, double intercept, int intercept_on, double* grad,
+                                double* loss_out);
 /* logistic_regression_model<T>::predict_probability (ml/glm/linear_model.hpp:376-392). */
 FVG_API fvg_status fvg_logreg_predict_probability(fvg_ctx* ctx, fvg_matrix* mat, const double* weight,
                                                   double intercept, double* prob);

@@ -19,6 +19,9 @@ _lib = None
 
 FMT = {"CRS": 0, "JDS": 1, "ELL": 2, "HYBRID": 3}
 REG = {"ZERO": 0, "L1": 1, "L2": 2}
+# GLM loss kinds (ml/glm/gradient.hpp): logistic_gradient, linear_gradient,
+# hinge_gradient, epsilon_insensitive, squared_epsilon_insensitive.
+LOSS = {"logistic": 0, "linear": 1, "hinge": 2, "eps": 3, "sqeps": 4}
 
 _i64 = C.c_int64
 _int = C.c_int
@@ -54,13 +57,13 @@ def lib():
             "orc_hyb_build_f64": [_i64, _i64, _p, _p, _p, _i64, _p, _p, _p, _p, _p, _p, _p],
             "orc_hyb_spmv_f64": [_i64, _i64, _p, _p, _p, _i64, _p, _p],
             "orc_fmt_mv_f64": [_int, _int, _i64, _i64, _p, _p, _p, _p, _p],
-            "orc_logistic_dloss_f64": [_i64, _p, _p, _p, _p],
-            "orc_logreg_eval_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _dbl, _int, _p, _int, _int,
-                                    _p, _p],
-            "orc_logreg_lbfgs_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _i64, _i64, _dbl,
-                                     _int, _int, _dbl, _p, _p, _p, _p, _p, _int],
-            "orc_logreg_sgd_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _i64, _dbl, _dbl,
-                                   _dbl, _int, _int, _dbl, _p, _p, _p, _p, _int],
+            "orc_glm_dloss_f64": [_int, _dbl, _i64, _p, _p, _p, _p],
+            "orc_glm_eval_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _dbl, _int, _p, _int, _int,
+                                 _p, _p, _int, _dbl],
+            "orc_glm_lbfgs_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _i64, _i64, _dbl,
+                                  _int, _int, _dbl, _p, _p, _p, _p, _p, _int, _int, _dbl],
+            "orc_glm_sgd_f64": [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _i64, _dbl, _dbl,
+                                _dbl, _int, _int, _dbl, _p, _p, _p, _p, _int, _int, _dbl],
             "orc_predict_probability_f64": [_i64, _i64, _p, _p, _p, _p, _dbl, _p],
             "orc_softmax_train_f64": [_i64, _i64, _p, _p, _p, _p, _p, _i64, _i64, _dbl, _dbl, _int, _int, _dbl,
                                       _p, _p, _p],
@@ -72,8 +75,8 @@ def lib():
             f.restype = None
         L.orc_ell_width.argtypes = [_i64, _p]
         L.orc_ell_width.restype = _i64
-        L.orc_logreg_lbfgs_f64.restype = _int
-        L.orc_logreg_sgd_f64.restype = _int
+        L.orc_glm_lbfgs_f64.restype = _int
+        L.orc_glm_sgd_f64.restype = _int
         L.orc_softmax_train_f64.restype = _int
     return _lib
 
@@ -213,13 +216,18 @@ def fmt_mv(a: CRS, fmt: str, x, trans: bool = False) -> np.ndarray:
     return y
 
 
-def logistic_dloss(label, wtx):
+def glm_dloss(label, wtx, loss="logistic", eps=0.0):
+    """``<kind>_gradient::compute_dloss`` on one vector: (dloss, sumloss)."""
     label = np.ascontiguousarray(label, dtype=np.float64)
     wtx = np.ascontiguousarray(wtx, dtype=np.float64)
     d = np.zeros(len(wtx))
     s = np.zeros(1)
-    lib().orc_logistic_dloss_f64(len(wtx), _ptr(label), _ptr(wtx), _ptr(d), _ptr(s))
+    lib().orc_glm_dloss_f64(LOSS[loss], float(eps), len(wtx), _ptr(label), _ptr(wtx), _ptr(d), _ptr(s))
     return d, float(s[0])
+
+
+def logistic_dloss(label, wtx):
+    return glm_dloss(label, wtx)
 
 
 def _splits(a: CRS, splits):
@@ -229,56 +237,61 @@ def _splits(a: CRS, splits):
     return s, len(s) - 1
 
 
-def logreg_eval(a: CRS, label, w, b=0.0, sw=None, intercept=False, fmt="CRS", splits=None, nthreads=1):
+def logreg_eval(a: CRS, label, w, b=0.0, sw=None, intercept=False, fmt="CRS", splits=None, nthreads=1,
+                loss="logistic", eps=0.0):
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = np.ones(a.m) if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
     w = np.ascontiguousarray(w, dtype=np.float64)
     sp, P = _splits(a, splits)
     g = np.zeros(a.n + 1)
-    loss = np.zeros(1)
-    lib().orc_logreg_eval_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(w), float(b), int(intercept),
-                              _ptr(sp), P, nthreads, _ptr(g), _ptr(loss))
-    return g, float(loss[0])
+    out = np.zeros(1)
+    lib().orc_glm_eval_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(w), float(b), int(intercept),
+                           _ptr(sp), P, nthreads, _ptr(g), _ptr(out), LOSS[loss], float(eps))
+    return g, float(out[0])
 
 
 def logreg_lbfgs(a: CRS, label, num_iter=1000, alpha=0.01, hist_size=10, reg_param=0.01, reg_type="ZERO",
                  intercept=False, tol=0.001, fmt="CRS", sw=None, w0=None, b0=None, splits=None, nthreads=1,
-                 l2_no_eta=False):
-    """``logistic_regression_with_lbfgs::train`` semantics; returns a dict."""
+                 l2_no_eta=False, loss="logistic", eps=0.0):
+    """``logistic_regression_with_lbfgs::train`` semantics (``loss`` selects
+    the other GLMs' gradient); returns a dict."""
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = np.ones(a.m) if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
     w = np.ones(a.n) if w0 is None else np.array(w0, dtype=np.float64)
     b = np.array([(1.0 if intercept else 0.0) if b0 is None else float(b0)])
     sp, P = _splits(a, splits)
     n_iter = np.zeros(1, dtype=np.int64)
-    loss = np.zeros(1)
+    fl = np.zeros(1)
     trace = np.zeros(4 * num_iter)
-    rc = lib().orc_logreg_lbfgs_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(sp), P, nthreads,
-                                    num_iter, hist_size, reg_param, REG[reg_type], int(intercept), tol,
-                                    _ptr(w), _ptr(b), _ptr(n_iter), _ptr(loss), _ptr(trace), int(l2_no_eta))
+    rc = lib().orc_glm_lbfgs_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(sp), P, nthreads,
+                                 num_iter, hist_size, reg_param, REG[reg_type], int(intercept), tol,
+                                 _ptr(w), _ptr(b), _ptr(n_iter), _ptr(fl), _ptr(trace), int(l2_no_eta),
+                                 LOSS[loss], float(eps))
     if rc != 0:
         raise ValueError(f"oracle lbfgs rejected the arguments (code {rc})")
     it = int(n_iter[0])
-    return dict(w=w, b=float(b[0]), n_iter=it, loss=float(loss[0]), trace=trace.reshape(-1, 4)[:it])
+    return dict(w=w, b=float(b[0]), n_iter=it, loss=float(fl[0]), trace=trace.reshape(-1, 4)[:it])
 
 
 def logreg_sgd(a: CRS, label, num_iter=1000, alpha=0.01, mini_batch_fraction=1.0, reg_param=0.01,
                reg_type="ZERO", intercept=False, tol=0.001, fmt="CRS", sw=None, w0=None, b0=None, splits=None,
-               nthreads=1, l2_no_eta=False):
-    """``logistic_regression_with_sgd::train`` semantics; returns a dict."""
+               nthreads=1, l2_no_eta=False, loss="logistic", eps=0.0):
+    """``logistic_regression_with_sgd::train`` semantics (``loss`` selects the
+    other GLMs' gradient); returns a dict."""
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = np.ones(a.m) if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
     w = np.ones(a.n) if w0 is None else np.array(w0, dtype=np.float64)
-    b = np.array([(1.0 if intercept else 0.0) if b0 is None else float(b0)])
+    # initModel(numFeatures): intercept 0 (logistic_regression_with_sgd.hpp:300)
+    b = np.array([0.0 if b0 is None else float(b0)])
     sp, P = _splits(a, splits)
     n_iter = np.zeros(1, dtype=np.int64)
-    loss = np.zeros(1)
-    rc = lib().orc_logreg_sgd_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(sp), P, nthreads, num_iter,
-                                  alpha, mini_batch_fraction, reg_param, REG[reg_type], int(intercept), tol,
-                                  _ptr(w), _ptr(b), _ptr(n_iter), _ptr(loss), int(l2_no_eta))
+    fl = np.zeros(1)
+    rc = lib().orc_glm_sgd_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(sp), P, nthreads, num_iter,
+                               alpha, mini_batch_fraction, reg_param, REG[reg_type], int(intercept), tol,
+                               _ptr(w), _ptr(b), _ptr(n_iter), _ptr(fl), int(l2_no_eta), LOSS[loss], float(eps))
     if rc != 0:
         raise ValueError(f"oracle sgd rejected the arguments (code {rc})")
-    return dict(w=w, b=float(b[0]), n_iter=int(n_iter[0]), loss=float(loss[0]))
+    return dict(w=w, b=float(b[0]), n_iter=int(n_iter[0]), loss=float(fl[0]))
 
 
 def softmax_train(a: CRS, label, K, num_iter=1000, alpha=0.01, reg_param=0.01, reg_type="ZERO", intercept=False,

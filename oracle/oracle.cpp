@@ -403,6 +403,72 @@ std::vector<T> logistic_dloss(const std::vector<T>& label, const std::vector<T>&
   return d;
 }
 
+// ------------------------------------------------------- other GLM losses
+// Loss kinds of the GLM family (ml/glm/gradient.hpp): 0 logistic_gradient,
+// 1 linear_gradient (55-87), 2 hinge_gradient (89-121), 3 epsilon_insensitive
+// (123-159), 4 squared_epsilon_insensitive (161-202).  MAX_LOSS / MIN_LOSS
+// clip ±1e12, HINGE_THRESHOLD 1 (gradient.hpp:8-10).
+enum LossKind { L_LOGISTIC = 0, L_LINEAR = 1, L_HINGE = 2, L_EPS = 3, L_SQEPS = 4 };
+struct Loss {
+  int kind = L_LOGISTIC;
+  double eps = 0.0;
+};
+
+template <class T> inline T clip_loss(T d) {
+  if (d > 1e12) return (T)1e12;
+  if (d < -1e12) return (T)-1e12;
+  return d;
+}
+
+// compute_dloss of the chosen kind.  sumloss is the caller's running loss:
+// the linear kind halves the whole running value (gradient.hpp:70-73), so a
+// minibatch sequence accumulating into one variable halves earlier batches
+// again; kept as the reference does it.
+template <class T>
+std::vector<T> glm_dloss(const Loss& L, const std::vector<T>& label, const std::vector<T>& wtx, double& sumloss) {
+  if (L.kind == L_LOGISTIC) return logistic_dloss(label, wtx, sumloss);
+  size_t n = wtx.size();
+  std::vector<T> d(n, T(0));
+  const double eps = L.eps;
+  if (L.kind == L_LINEAR) {
+    for (size_t i = 0; i < n; i++) {
+      T e = wtx[i] - label[i];
+      sumloss += (e * e);
+    }
+    sumloss *= 0.5;
+    for (size_t i = 0; i < n; i++) d[i] = clip_loss<T>(wtx[i] - label[i]);
+  } else if (L.kind == L_HINGE) {
+    for (size_t i = 0; i < n; i++) {
+      T z = wtx[i] * label[i];
+      sumloss += (z <= 1.0) ? (double)(1.0 - z) : 0.0;
+    }
+    for (size_t i = 0; i < n; i++) d[i] = (wtx[i] * label[i] <= 1.0) ? -label[i] : T(0);
+  } else if (L.kind == L_EPS) {
+    for (size_t i = 0; i < n; i++) {
+      double e = std::fabs(label[i] - wtx[i]) - eps;
+      sumloss += (e > 0) ? e : 0.0;
+    }
+    for (size_t i = 0; i < n; i++) {
+      if ((label[i] - wtx[i]) > eps) d[i] = -1;
+      else if ((wtx[i] - label[i]) > eps) d[i] = 1;
+      else d[i] = 0;
+    }
+  } else {
+    for (size_t i = 0; i < n; i++) {
+      double e = std::fabs(label[i] - wtx[i]) - eps;
+      sumloss += (e > 0) ? e * e : 0.0;
+    }
+    for (size_t i = 0; i < n; i++) {
+      T z = label[i] - wtx[i];
+      if (z > eps) d[i] = (T)(-2 * (z - eps));
+      else if (z < -eps) d[i] = (T)(2 * (-z - eps));
+      else d[i] = 0;
+      d[i] = clip_loss<T>(d[i]);
+    }
+  }
+  return d;
+}
+
 // ---------------------------------------------- per-rank matrices (glm)
 enum Fmt { CRS_F = 0, JDS_F = 1, ELL_F = 2, HYB_F = 3 };
 
@@ -459,11 +525,11 @@ template <class T> CRS<T> rows_of(const CRS<T>& a, i64 r0, i64 r1) {
 template <class T>
 std::vector<T> compute_gradient(const RankData<T>& d, const std::vector<T>& w, T b,
                                 const std::vector<T>& label, const std::vector<T>& sw,
-                                bool icpt, T& bias, double& loss) {
+                                bool icpt, T& bias, double& loss, const Loss& L = Loss()) {
   if (d.nrow == 0) return std::vector<T>(w.size(), T(0));
   auto wtx = d.fwd(w);                        // compute_wtx  (227-240)
   if (icpt) for (auto& v : wtx) v += b;
-  auto dl = logistic_dloss(label, wtx, loss);
+  auto dl = glm_dloss(L, label, wtx, loss);
   for (size_t i = 0; i < dl.size(); i++) dl[i] = dl[i] * sw[i];
   if (icpt) bias = vsum(dl);
   return d.bwd(dl);
@@ -487,6 +553,7 @@ template <class T> struct Problem {
   std::vector<std::vector<T>> label, sw;
   i64 ncol = 0;
   int nthreads = 1;
+  Loss loss;
 };
 
 template <class T>
@@ -519,7 +586,7 @@ std::vector<T> evaluate(const Problem<T>& pr, const std::vector<T>& w, T b, bool
   for_ranks(P, pr.nthreads, [&](int r) {
     T bias = 0;
     double l = 0.0;
-    auto g = compute_gradient(pr.ranks[r], w, b, pr.label[r], pr.sw[r], icpt, bias, l);
+    auto g = compute_gradient(pr.ranks[r], w, b, pr.label[r], pr.sw[r], icpt, bias, l, pr.loss);
     g.push_back(bias);
     parts[r] = std::move(g);
     losses[r] = l;
@@ -683,7 +750,8 @@ inline i64 minibatch_size(i64 ns, double frac) {
 template <class T>
 void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, int P, int fmt,
                std::vector<T>& w, T& b, i64 num_iter, double alpha, double frac, T lambda, int rtype,
-               bool icpt, double tol, i64& n_iter, double& final_loss, int nthreads, bool no_eta = false) {
+               bool icpt, double tol, i64& n_iter, double& final_loss, int nthreads, bool no_eta = false,
+               const Loss& L = Loss()) {
   struct RankSGD {
     std::vector<RankData<T>> batches;
     std::vector<std::vector<T>> label, sw;
@@ -714,7 +782,7 @@ void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, 
       double loss = 0.0;
       T ra = (T)(alpha / std::sqrt((double)i));  // update_model (247)
       for (size_t k = 0; k < rk[r].batches.size(); k++) {
-        auto g = compute_gradient(rk[r].batches[k], lw, lb, rk[r].label[k], rk[r].sw[k], icpt, bias, loss);
+        auto g = compute_gradient(rk[r].batches[k], lw, lb, rk[r].label[k], rk[r].sw[k], icpt, bias, loss, L);
         for (i64 q = 0; q < n; q++) lw[q] -= ra * g[q];
         if (icpt) lb -= ra * bias;
       }
@@ -969,33 +1037,39 @@ void orc_fmt_mv_f64(int fmt, int trans, i64 m, i64 n, const i32* off, const i32*
   std::copy(r.begin(), r.end(), y);
 }
 
-void orc_logistic_dloss_f64(i64 m, const double* label, const double* wtx, double* dloss, double* sumloss) {
+void orc_glm_dloss_f64(int lkind, double eps, i64 m, const double* label, const double* wtx, double* dloss,
+                       double* sumloss) {
   double s = 0;
-  auto d = logistic_dloss(std::vector<double>(label, label + m), std::vector<double>(wtx, wtx + m), s);
+  auto d = glm_dloss(Loss{lkind, eps}, std::vector<double>(label, label + m), std::vector<double>(wtx, wtx + m), s);
   std::copy(d.begin(), d.end(), dloss);
   *sumloss = s;
 }
 
 // One loss/gradient evaluation; grad has n+1 entries (bias last).
-void orc_logreg_eval_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
-                         const double* label, const double* sw, const double* w, double b, int icpt,
-                         const i64* splits, int P, int nthreads, double* grad, double* loss) {
+// loss: 0 logistic, 1 linear (squared), 2 hinge, 3 epsilon-insensitive,
+// 4 squared epsilon-insensitive; eps used by 3 and 4.
+void orc_glm_eval_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
+                      const double* label, const double* sw, const double* w, double b, int icpt,
+                      const i64* splits, int P, int nthreads, double* grad, double* loss, int lkind, double eps) {
   auto a = make_crs<double>(m, n, off, idx, val);
   auto sp = default_splits(m, splits, P);
   auto pr = make_problem(a, label, sw, sp.data(), P, fmt, nthreads);
+  pr.loss = Loss{lkind, eps};
   auto g = evaluate(pr, std::vector<double>(w, w + n), b, icpt != 0, *loss);
   std::copy(g.begin(), g.end(), grad);
 }
 
-int orc_logreg_lbfgs_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
-                         const double* label, const double* sw, const i64* splits, int P, int nthreads,
-                         i64 num_iter, i64 hist, double lambda, int rtype, int icpt, double tol, double* w,
-                         double* b, i64* n_iter, double* final_loss, double* trace, int flags) {
+int orc_glm_lbfgs_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
+                      const double* label, const double* sw, const i64* splits, int P, int nthreads,
+                      i64 num_iter, i64 hist, double lambda, int rtype, int icpt, double tol, double* w,
+                      double* b, i64* n_iter, double* final_loss, double* trace, int flags, int lkind, double eps) {
   if (fmt == JDS_F || fmt < 0 || fmt > 3) return 4;  // lbfgs_parallelizer.hpp:596-597
   if (hist < 1 || num_iter < 1 || lambda < 0 || tol < 0) return 1;
+  if (lkind < 0 || lkind > 4) return 1;
   auto a = make_crs<double>(m, n, off, idx, val);
   auto sp = default_splits(m, splits, P);
   auto pr = make_problem(a, label, sw, sp.data(), P, fmt, nthreads);
+  pr.loss = Loss{lkind, eps};
   std::vector<double> wv(w, w + n);
   double bb = *b;
   lbfgs_train(pr, fmt, wv, bb, num_iter, hist, lambda, rtype, icpt != 0, tol, *n_iter, *final_loss, trace,
@@ -1005,18 +1079,19 @@ int orc_logreg_lbfgs_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, 
   return 0;
 }
 
-int orc_logreg_sgd_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
-                       const double* label, const double* sw, const i64* splits, int P, int nthreads,
-                       i64 num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
-                       double* w, double* b, i64* n_iter, double* final_loss, int flags) {
+int orc_glm_sgd_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
+                    const double* label, const double* sw, const i64* splits, int P, int nthreads,
+                    i64 num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
+                    double* w, double* b, i64* n_iter, double* final_loss, int flags, int lkind, double eps) {
   if (fmt < 0 || fmt > 3) return 4;
   if (num_iter < 1 || alpha <= 0 || frac <= 0 || frac > 1 || lambda < 0 || tol < 0) return 1;
+  if (lkind < 0 || lkind > 4) return 1;
   auto a = make_crs<double>(m, n, off, idx, val);
   auto sp = default_splits(m, splits, P);
   std::vector<double> wv(w, w + n);
   double bb = *b;
   sgd_train(a, label, sw, sp.data(), P, fmt, wv, bb, num_iter, alpha, frac, lambda, rtype, icpt != 0, tol, *n_iter,
-            *final_loss, nthreads, (flags & 1) != 0);
+            *final_loss, nthreads, (flags & 1) != 0, Loss{lkind, eps});
   std::copy(wv.begin(), wv.end(), w);
   *b = bb;
   return 0;

@@ -37,19 +37,23 @@ void orc_hyb_spmv_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* i
                       int64_t thr, const double* x, double* y);
 void orc_fmt_mv_f64(int fmt, int trans, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
                     const double* val, const double* x, double* y);
-void orc_logistic_dloss_f64(int64_t m, const double* label, const double* wtx, double* dloss, double* sumloss);
-void orc_logreg_eval_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
-                         const double* val, const double* label, const double* sw, const double* w, double b,
-                         int icpt, const int64_t* splits, int P, int nthreads, double* grad, double* loss);
-int orc_logreg_lbfgs_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
-                         const double* val, const double* label, const double* sw, const int64_t* splits, int P,
-                         int nthreads, int64_t num_iter, int64_t hist, double lambda, int rtype, int icpt,
-                         double tol, double* w, double* b, int64_t* n_iter, double* final_loss, double* trace,
-                         int flags);
-int orc_logreg_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
-                       const double* label, const double* sw, const int64_t* splits, int P, int nthreads,
-                       int64_t num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
-                       double* w, double* b, int64_t* n_iter, double* final_loss, int flags);
+// GLM loss kinds (lkind): 0 logistic, 1 linear, 2 hinge, 3 epsilon-
+// insensitive, 4 squared epsilon-insensitive (eps used by 3 and 4).
+void orc_glm_dloss_f64(int lkind, double eps, int64_t m, const double* label, const double* wtx, double* dloss,
+                       double* sumloss);
+void orc_glm_eval_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                      const double* val, const double* label, const double* sw, const double* w, double b,
+                      int icpt, const int64_t* splits, int P, int nthreads, double* grad, double* loss, int lkind,
+                      double eps);
+int orc_glm_lbfgs_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
+                      const double* val, const double* label, const double* sw, const int64_t* splits, int P,
+                      int nthreads, int64_t num_iter, int64_t hist, double lambda, int rtype, int icpt,
+                      double tol, double* w, double* b, int64_t* n_iter, double* final_loss, double* trace,
+                      int flags, int lkind, double eps);
+int orc_glm_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                    const double* label, const double* sw, const int64_t* splits, int P, int nthreads,
+                    int64_t num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
+                    double* w, double* b, int64_t* n_iter, double* final_loss, int flags, int lkind, double eps);
 void orc_predict_probability_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
                                  const double* val, const double* w, double b, double* out);
 int orc_softmax_train_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,

@@ -1,7 +1,7 @@
 // Exercises the C++ API of include/frovedis_gb300.hpp the way a frovedis
 // program calls the reference: build crs_matrix_local, multiply, convert to
 // ELL/JDS/hybrid, train with logistic_regression_with_{lbfgs,sgd}::train and
-// predict.  Reads a CRS matrix, a vector and labels from the text file
+// the other GLM trainers, and predict.  Reads a CRS matrix, a vector and labels from the text file
 // argv[1]; writes one "name v0 v1 ..." line per result to argv[2], which
 // tests/test_cpp_api.py compares with the oracle.
 #include <cstdio>
@@ -208,6 +208,57 @@ int main(int argc, char** argv) {
       lbfgs_mult_threw = 1;
     }
     put1(f, "estm_lbfgs_throws", lbfgs_mult_threw);
+  }
+  {
+    // the regression and SVM trainers (linear_regression_with_*, lasso_with_*,
+    // ridge_regression_with_*, svm_with_*, svm_regression_with_sgd)
+    auto z = A * x;
+    std::vector<double> y(m);
+    for (size_t i = 0; i < m; i++) y[i] = 0.25 * z[i] + 0.5 * label[i];
+    put(f, "reg_y", y);
+    std::vector<double> sw;
+    size_t it = 0;
+    auto lr = linear_regression_with_sgd::train(A, y, sw, it, 20, 1e-4, 0.3, true, 0.0);
+    put(f, "lin_sgd_w", lr.weight);
+    put1(f, "lin_sgd_b", lr.intercept);
+    put1(f, "lin_sgd_n_iter", (double)it);
+    put(f, "lin_pred", lr.predict(A));
+    auto ll = linear_regression_with_lbfgs::train(A, y, sw, it, 25, 0.01, 10, true);
+    put(f, "lin_lbfgs_w", ll.weight);
+    put1(f, "lin_lbfgs_b", ll.intercept);
+    put1(f, "lin_lbfgs_n_iter", (double)it);
+    put(f, "lasso_sgd_w", lasso_with_sgd::train(A, y, 20, 1e-4, 1.0, 1e-3, false, 0.0).weight);
+    put(f, "ridge_lbfgs_w", ridge_regression_with_lbfgs::train(A, y, 25, 0.01, 10, 1e-2, true).weight);
+    auto sv = svm_with_sgd::train(A, label, 30, 0.05, 1.0, 1e-2, L2, true, 0.0);
+    put(f, "svm_sgd_w", sv.weight);
+    put1(f, "svm_sgd_b", sv.intercept);
+    put(f, "svm_pred", sv.predict(A));
+    put(f, "svm_score", sv.predict_probability(A));
+    auto sl = svm_with_lbfgs::train(A, label, sw, it, 25, 0.01, 10, 1e-2, L1, true);
+    put(f, "svm_lbfgs_w", sl.weight);
+    put1(f, "svm_lbfgs_n_iter", (double)it);
+    put(f, "svr_eps_w", svm_regression_with_sgd::train(A, y, 20, 0.01, 1.0, 0.0, ZERO, true, 0.0, 0.1, EPS).weight);
+    put(f, "svr_sqeps_w",
+        svm_regression_with_sgd::train(A, y, 20, 1e-4, 1.0, 1e-3, L2, false, 0.0, 0.05, SQEPS).weight);
+    int svm_jds_threw = 0;
+    try {
+      svm_with_lbfgs::train(A, label, 5, 0.01, 10, 0.01, ZERO, false, 0.001, JDS);
+    } catch (frovedis_gb300::error& e) {
+      svm_jds_threw = std::string(e.what()).find("Unsupported input matrix type") != std::string::npos;
+    }
+    put1(f, "svm_jds_throws", svm_jds_threw);
+    // member persistence (linear_model.hpp:284-295, 569-583)
+    const std::string base = std::string(argv[2]);
+    lr.save(base + ".lin.txt");
+    sv.savebinary(base + ".svm.bin");
+    linear_regression_model<double> lr2;
+    svm_model<double> sv2;
+    lr2.load(base + ".lin.txt");
+    sv2.loadbinary(base + ".svm.bin");
+    put(f, "lin_loaded_w", lr2.weight);
+    put1(f, "lin_loaded_b", lr2.intercept);
+    put1(f, "svm_loaded_same", sv2.weight == sv.weight && sv2.intercept == sv.intercept &&
+                                   sv2.threshold == sv.threshold);
   }
   std::fclose(f);
   return 0;

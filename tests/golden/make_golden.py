@@ -11,9 +11,12 @@ Reads (never writes) the reference tree given as argv[1] (default
   (nums/val/idx/off/type, also as raw files) and its documented transpose (tutorial.md, block
   after "It should be:");
 * the glm fixtures ``test/ml/test2.1-1`` (SGD) and ``test/ml/test2.1-2``
-  (L-BFGS): data/label text, the hyper-parameters and expected outputs
-  written in their ``test.cc``, plus the raw bytes-per-line layout needed to
-  reproduce the 4-rank row split of ``mpirun -np 4`` (test/ml/exec.sh).
+  (L-BFGS) of logistic regression, ``test1.1-*`` (linear regression),
+  ``test1.2-*`` (lasso), ``test1.3-*`` (ridge) and ``test2.2-*`` (SVM), each
+  ``-1`` SGD and ``-2`` L-BFGS: data/label text, the trainer, the
+  hyper-parameters and expected outputs written in their ``test.cc``, plus
+  the raw bytes-per-line layout needed to reproduce the 4-rank row split of
+  ``mpirun -np 4`` (test/ml/exec.sh).
 
 Run:  python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -85,7 +88,10 @@ def main():
     g["tut_binary"]["expected_transpose_text"] = tr
 
     # --- glm tests ---
-    for name in ("test2.1-1", "test2.1-2"):
+    trainers = {"logistic_regression": ("logistic", None), "linear_regression": ("linear", "ZERO"),
+                "lasso": ("linear", "L1"), "ridge_regression": ("linear", "L2"), "svm": ("hinge", None)}
+    for name in ("test2.1-1", "test2.1-2", "test1.1-1", "test1.1-2", "test1.2-1", "test1.2-2", "test1.3-1",
+                 "test1.3-2", "test2.2-1", "test2.2-2"):
         td = os.path.join(ref, "test", "ml", name)
         raw = open(os.path.join(td, "data"), "rb").read()
         src = open(os.path.join(td, "test.cc")).read()
@@ -99,11 +105,16 @@ def main():
                 ent[key] = float(mm.group(1))
         mm = re.search(r"bool intercept\s*=\s*(true|false)", src)
         ent["intercept"] = mm.group(1) == "true"
+        mm = re.search(r"auto model = (\w+)_with_(sgd|lbfgs)::train", src)
+        ent["trainer"] = mm.group(1) + "_with_" + mm.group(2)
+        ent["loss"], reg = trainers[mm.group(1)]
         mm = re.search(r"RegType rt\s*=\s*(\w+)", src)
-        ent["reg_type"] = mm.group(1)
-        for key in ("expected_out_p", "expected_out_pb"):
-            mm = re.search(key + r"\s*=\s*\{([^}]*)\}", src)
-            ent[key] = [float(x) for x in mm.group(1).split(",")]
+        ent["reg_type"] = mm.group(1) if mm else reg
+        for key in ("expected_out", "expected_out_p", "expected_out_pb"):
+            # the live (not commented-out) initialiser
+            mm = re.search(r"(?m)^\s*std::vector<double>\s+" + key + r"\s*=\s*\{([^}]*)\}", src)
+            if mm:
+                ent[key] = [float(x) for x in mm.group(1).split(",")]
         mm = re.search(r"double tol\s*=\s*([0-9.eE+-]+)", src)
         ent["rms_tol"] = float(mm.group(1))
         ent["solver"] = "sgd" if "with_sgd" in src else "lbfgs"

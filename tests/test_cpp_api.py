@@ -102,7 +102,7 @@ def test_cpp_api_matches_oracle(tmp_path):
     assert abs(o["lbfgs_hyb_b"][0] - rh["b"]) <= 1e-5 * max(1.0, abs(rh["b"]))
     assert o["lbfgs_jds_throws"][0] == 1
     rs = oracle.logreg_sgd(a, label, num_iter=15, alpha=0.05, mini_batch_fraction=0.3, reg_type="L2",
-                           reg_param=1e-2, intercept=True)
+                           reg_param=1e-2, intercept=True, b0=1.0)
     assert int(o["sgd_n_iter"][0]) == rs["n_iter"]
     assert np.max(np.abs(o["sgd_w"] - rs["w"])) <= 1e-5 * max(1.0, np.max(np.abs(rs["w"])))
     assert abs(o["sgd_b"][0] - rs["b"]) <= 1e-5 * max(1.0, abs(rs["b"]))
@@ -144,3 +144,37 @@ def test_cpp_api_matches_oracle(tmp_path):
     assert np.max(np.abs(o["estm_w"] - rm2["W"].ravel())) <= 1e-8 * max(1.0, np.max(np.abs(rm2["W"])))
     assert np.array_equal(o["estm_bin_w"], o["estm_w"]) and o["estm_pred_same"][0] == 1
     assert o["estm_text_classes"][0] == 5 and o["estm_lbfgs_throws"][0] == 1
+
+    # the GLM family: initial intercept 0 for SGD, isIntercept for L-BFGS
+    y = o["reg_y"]
+
+    def wclose(got, ref):
+        return np.max(np.abs(got - ref)) <= 1e-5 * max(1.0, np.max(np.abs(ref)))
+    r = oracle.logreg_sgd(a, y, loss="linear", num_iter=20, alpha=1e-4, mini_batch_fraction=0.3, reg_type="ZERO",
+                          intercept=True, tol=0.0)
+    assert wclose(o["lin_sgd_w"], r["w"]) and abs(o["lin_sgd_b"][0] - r["b"]) <= 1e-5 * max(1.0, abs(r["b"]))
+    assert int(o["lin_sgd_n_iter"][0]) == r["n_iter"] == 20
+    assert np.max(np.abs(o["lin_pred"] - (a.to_dense() @ o["lin_sgd_w"] + o["lin_sgd_b"][0]))) <= 1e-9
+    r = oracle.logreg_lbfgs(a, y, loss="linear", num_iter=25, hist_size=10, reg_type="ZERO", intercept=True)
+    assert wclose(o["lin_lbfgs_w"], r["w"]) and int(o["lin_lbfgs_n_iter"][0]) == r["n_iter"]
+    r = oracle.logreg_sgd(a, y, loss="linear", num_iter=20, alpha=1e-4, reg_type="L1", reg_param=1e-3, tol=0.0)
+    assert wclose(o["lasso_sgd_w"], r["w"])
+    r = oracle.logreg_lbfgs(a, y, loss="linear", num_iter=25, reg_type="L2", reg_param=1e-2, intercept=True)
+    assert wclose(o["ridge_lbfgs_w"], r["w"])
+    r = oracle.logreg_sgd(a, label, loss="hinge", num_iter=30, alpha=0.05, reg_type="L2", reg_param=1e-2,
+                          intercept=True, tol=0.0)
+    assert wclose(o["svm_sgd_w"], r["w"])
+    score = a.to_dense() @ o["svm_sgd_w"] + o["svm_sgd_b"][0]
+    assert np.max(np.abs(o["svm_score"] - score)) <= 1e-9
+    assert np.array_equal(o["svm_pred"], np.where(o["svm_score"] > 0, 1.0, -1.0))
+    r = oracle.logreg_lbfgs(a, label, loss="hinge", num_iter=25, reg_type="L1", reg_param=1e-2, intercept=True)
+    assert wclose(o["svm_lbfgs_w"], r["w"]) and int(o["svm_lbfgs_n_iter"][0]) == r["n_iter"]
+    r = oracle.logreg_sgd(a, y, loss="eps", eps=0.1, num_iter=20, alpha=0.01, reg_type="ZERO", intercept=True,
+                          tol=0.0)
+    assert wclose(o["svr_eps_w"], r["w"])
+    r = oracle.logreg_sgd(a, y, loss="sqeps", eps=0.05, num_iter=20, alpha=1e-4, reg_type="L2", reg_param=1e-3,
+                          tol=0.0)
+    assert wclose(o["svr_sqeps_w"], r["w"])
+    assert o["svm_jds_throws"][0] == 1
+    assert np.max(np.abs(o["lin_loaded_w"] - o["lin_sgd_w"])) <= 1e-11 * max(1.0, np.max(np.abs(o["lin_sgd_w"])))
+    assert o["svm_loaded_same"][0] == 1

@@ -97,7 +97,7 @@ def test_sgd_golden_test2_1_1(ctx, ranks):
     splits = oracle.text_rank_splits(bytes.fromhex(e["data_bytes_hex"]), 4) if ranks == 4 else None
     r = fv.logreg_sgd(A, label, num_iter=int(e["num_iteration"]), alpha=e["alpha"],
                       mini_batch_fraction=e["minibatch_fraction"], reg_param=e["regParam"], reg_type=e["reg_type"],
-                      intercept=e["intercept"], w0=np.zeros(a.n), l2_no_eta=1, row_splits=splits)
+                      intercept=e["intercept"], w0=np.zeros(a.n), b0=1.0, l2_no_eta=1, row_splits=splits)
     pb = fv.predict_probability(A, r["w"], r["b"])
     assert np.max(np.abs(pb - e["expected_out_pb"])) < 5e-7
     assert r["n_iter"] == 129

@@ -59,14 +59,15 @@ def test_lbfgs_golden(ranks):
 def test_sgd_golden(ranks):
     # test/ml/test2.1-1/test.cc stores probabilities {0.952718, 0.437991,
     # 0.958198, 0.955715}.  They are reproduced to all six printed digits with
-    # all-zero initial weights and the L2 branch built without USE_ETA
-    # (regularizer.hpp:50-54); the current source's defaults (weights = 1,
-    # eta = alpha/sqrt(i)) give other values, checked against labels only.
+    # an earlier source's initial model (weights 0, intercept 1) and the L2
+    # branch built without USE_ETA (regularizer.hpp:50-54); the current
+    # source's defaults (weights 1, intercept 0, eta = alpha/sqrt(i)) give
+    # other values, checked against labels only.
     e, a, label, splits = _glm("test2.1-1")
     kw = dict(num_iter=int(e["num_iteration"]), alpha=e["alpha"], mini_batch_fraction=e["minibatch_fraction"],
               reg_param=e["regParam"], reg_type=e["reg_type"], intercept=e["intercept"],
               splits=splits if ranks == 4 else None)
-    r = oracle.logreg_sgd(a, label, w0=np.zeros(a.n), l2_no_eta=True, **kw)
+    r = oracle.logreg_sgd(a, label, w0=np.zeros(a.n), b0=1.0, l2_no_eta=True, **kw)
     pb = oracle.predict_probability(a, r["w"], r["b"])
     assert np.max(np.abs(pb - e["expected_out_pb"])) < 5e-7
     assert r["n_iter"] == 129
@@ -130,3 +131,69 @@ def test_oracle_loaders_on_tutorial_files(tmp_path):
     assert (m, n) == (g["tut_binary"]["m"], g["tut_binary"]["n"])
     assert off.tolist() == g["tut_binary"]["off"] and idx.tolist() == g["tut_binary"]["idx"]
     assert val.tolist() == g["tut_binary"]["val"]
+
+
+@pytest.mark.parametrize("name", ["test1.1-1", "test1.2-1", "test1.3-1"])
+@pytest.mark.parametrize("ranks", [1, 4])
+def test_regression_sgd_golden(name, ranks):
+    # test/ml/test1.{1,2,3}-1/test.cc: linear_regression_with_sgd,
+    # lasso_with_sgd, ridge_regression_with_sgd, predictions stored with six
+    # significant digits.  Reproduced to those digits (|err| <= 5e-6) by the
+    # same earlier initial model as test2.1-1 (weights 0, intercept 1; L2
+    # without USE_ETA); all three stop at iteration 3 on the RMS test.
+    e, a, label, splits = _glm(name)
+    r = oracle.logreg_sgd(a, label, loss=e["loss"], num_iter=int(e["num_iteration"]), alpha=e["alpha"],
+                          mini_batch_fraction=e["minibatch_fraction"], reg_param=e.get("regParam", 0.0),
+                          reg_type=e["reg_type"], intercept=e["intercept"], w0=np.zeros(a.n), b0=1.0,
+                          l2_no_eta=True, splits=splits if ranks == 4 else None)
+    pred = a.to_dense() @ r["w"] + r["b"]
+    assert np.max(np.abs(pred - e["expected_out"])) <= 5e-6
+    assert r["n_iter"] == 3
+
+
+@pytest.mark.parametrize("name", ["test1.1-2", "test1.2-2", "test1.3-2"])
+def test_regression_lbfgs_golden(name):
+    # test/ml/test1.{1,2,3}-2/test.cc store predictions of an earlier L-BFGS
+    # (they sit next to the SGD ones, a model barely moved from its start);
+    # the current lbfgs_parallelizer (unit first step, line search on the
+    # loss) fits the six points far better.  Not reproducible from the
+    # current source: the check is that the current trainer's squared loss
+    # is below the stored model's.
+    e, a, label, splits = _glm(name)
+    r = oracle.logreg_lbfgs(a, label, loss="linear", num_iter=int(e["num_iteration"]), alpha=e["alpha"],
+                            hist_size=int(e["hist_size"]), reg_param=e.get("regParam", 0.0), reg_type=e["reg_type"],
+                            intercept=e["intercept"], splits=splits)
+    stored = 0.5 * np.sum((np.array(e["expected_out"]) - label) ** 2)
+    assert r["loss"] < stored
+
+
+@pytest.mark.parametrize("name", ["test2.2-1", "test2.2-2"])
+def test_svm_golden_predictions(name):
+    # test/ml/test2.2-{1,2}/test.cc: svm_with_sgd / svm_with_lbfgs, predicted
+    # classes {1,-1,1,1}.  The stored raw scores (predict_probability) come
+    # from an earlier source and are not reproducible; the classes are.
+    e, a, label, splits = _glm(name)
+    kw = dict(loss="hinge", num_iter=int(e["num_iteration"]), alpha=e["alpha"], reg_param=e["regParam"],
+              reg_type=e["reg_type"], intercept=e["intercept"], splits=splits)
+    if e["solver"] == "sgd":
+        r = oracle.logreg_sgd(a, label, mini_batch_fraction=e["minibatch_fraction"], **kw)
+    else:
+        r = oracle.logreg_lbfgs(a, label, hist_size=int(e["hist_size"]), **kw)
+    pred = np.where(a.to_dense() @ r["w"] + r["b"] > 0, 1.0, -1.0)
+    assert np.array_equal(pred, e["expected_out_p"])
+
+
+def test_glm_dloss_kinds():
+    # gradient.hpp:55-202 on hand-checked values
+    lab = np.array([1.0, -1.0, 1.0])
+    wtx = np.array([0.5, 2.0, 3.0])
+    d, s = oracle.glm_dloss(lab, wtx, "hinge")
+    assert d.tolist() == [-1.0, 1.0, 0.0] and s == 3.5
+    d, s = oracle.glm_dloss(lab, wtx, "linear")
+    assert d.tolist() == [-0.5, 3.0, 2.0] and s == 0.5 * (0.25 + 9.0 + 4.0)
+    d, s = oracle.glm_dloss(lab, wtx, "eps", 0.6)
+    assert d.tolist() == [0.0, 1.0, 1.0] and abs(s - 3.8) < 1e-15
+    d, s = oracle.glm_dloss(lab, wtx, "sqeps", 0.6)
+    assert np.allclose(d, [0.0, 4.8, 2.8], rtol=0, atol=1e-15) and abs(s - (2.4 ** 2 + 1.4 ** 2)) < 1e-12
+    d, _ = oracle.glm_dloss(np.zeros(2), np.array([2e12, -3e12]), "linear")
+    assert d.tolist() == [1e12, -1e12]  # MAX_LOSS / MIN_LOSS clip
