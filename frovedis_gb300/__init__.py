@@ -63,6 +63,7 @@ EXPORTS = [
     "fvg_multinomial_train", "fvg_multinomial_probability",
     "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
+    "fvg_logreg_shrink_sgd",
 ]
 
 _lib = None
@@ -126,6 +127,8 @@ def load(build_if_needed: bool = True):
         "fvg_glm_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
                          C.POINTER(_dbl)], _int),
         "fvg_glm_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
+        "fvg_logreg_shrink_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
+                                   C.POINTER(_dbl)], _int),
         "fvg_glm_eval": ([_p, _p, _int, _int, _int, _dbl, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
     }
     for name, (args, res) in sig.items():
@@ -507,6 +510,11 @@ def multinomial_probability(mat: Matrix, W, b, intercept=False):
 def logreg_sgd(mat: Matrix, label, **kw):
     """logistic_regression_with_sgd::train (defaults as in the reference)."""
     return _train(mat.ctx.L.fvg_logreg_sgd, mat, label, sgd=True, **kw)
+
+
+def logreg_shrink_sgd(mat: Matrix, label, **kw):
+    """shrink::logistic_regression_with_sgd::train (fvg_logreg_shrink_sgd)."""
+    return _train(mat.ctx.L.fvg_logreg_shrink_sgd, mat, label, sgd=True, **kw)
 
 
 def glm_lbfgs(mat: Matrix, label, loss="linear", **kw):

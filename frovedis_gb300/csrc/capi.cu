@@ -12,7 +12,7 @@ namespace fvg {
 void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
                  double* w_h, double* b_h, i64* n_iter, double* loss_out);
 void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
-               double* w_h, double* b_h, i64* n_iter, double* loss_out);
+               double* w_h, double* b_h, i64* n_iter, double* loss_out, bool shrink);
 void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* label_h, const double* sw_h,
                  const double* w_h, double b, int icpt, double* grad_h, double* loss_h, int loss_kind, double eps);
 void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
@@ -723,7 +723,20 @@ FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* c, fvg_matrix* M, const double* label
   own(c, M);
   need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
   const fvg_glm_params q = logistic_of(p);
-  sgd_train(c, M, label, sample_weight, &q, weight, intercept, n_iter, final_loss);
+  sgd_train(c, M, label, sample_weight, &q, weight, intercept, n_iter, final_loss, false);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_logreg_shrink_sgd(fvg_ctx* c, fvg_matrix* M, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* p, double* weight,
+                                         double* intercept, int64_t* n_iter, double* final_loss) {
+  if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
+  const fvg_glm_params q = logistic_of(p);
+  sgd_train(c, M, label, sample_weight, &q, weight, intercept, n_iter, final_loss, true);
   check_device_error(c);
   API_END(c)
 }
@@ -734,7 +747,7 @@ FVG_API fvg_status fvg_glm_sgd(fvg_ctx* c, fvg_matrix* M, const double* label, c
   if (!c || !M || !weight || !intercept || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
-  sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss);
+  sgd_train(c, M, label, sample_weight, p, weight, intercept, n_iter, final_loss, false);
   check_device_error(c);
   API_END(c)
 }

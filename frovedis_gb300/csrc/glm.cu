@@ -764,7 +764,11 @@ struct SgdArgs {
   double* part;
   unsigned* ticket;
   double* scal;  // [0] rmse, [1] b (accepted), [2] lb (local), [3] tot_b, [4] loss sum, [5] prev b,
-                 // [6] the current rank's running loss
+                 // [6] the current rank's running loss, [7] rank 0's intercept change
+  // shrink variant (shrink_sgd_parallelizer.hpp): columns with a nonzero in
+  // any rank's rows (used[j] != 0) and rank 0's count of its own columns
+  const int* used;
+  double n_used0;
 };
 
 // w -= ra * g; b -= ra * bias  (update_model, gradient_descent.hpp:242-259)
@@ -785,25 +789,31 @@ __global__ void k_sgd_delta(const double* __restrict__ LW, const double* __restr
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     double db = __dsub_rn(a.scal[2], a.scal[1]);
     a.scal[3] = first ? db : __dadd_rn(a.scal[3], db);
+    if (first) a.scal[7] = db;
     const double rl = has_rows ? a.scal[6] : 0.0;
     a.scal[4] = first ? rl : __dadd_rn(a.scal[4], rl);
   }
 }
 
 // w += Σdelta; b += Σdelta_b; regularize(w, alpha/sqrt(i)); RMSE of the
-// change (sgd_parallelizer.hpp:189-217)
+// change (sgd_parallelizer.hpp:189-217).  Shrink variant
+// (update_model_local, shrink_sgd_parallelizer.hpp:99-151): only the used
+// columns exist and are regularised (eta = 1); the RMSE is taken over the
+// summed change before regularisation plus rank 0's own intercept change,
+// divided by rank 0's column count + 1.
 __global__ void __launch_bounds__(kVecThreads) k_sgd_apply(double* __restrict__ W, const double* __restrict__ TOT,
                                                            int rtype, double lambda, double eta, int no_eta,
-                                                           SgdArgs a) {
+                                                           int icpt, SgdArgs a) {
   const double scale = fmax(0.0, 1.0 - (lambda * eta));
   double v[1] = {0.0};
   VEC_LOOP(j, a.n) {
+    if (a.used && !a.used[j]) continue;
     double prev = W[j];
     double w = __dadd_rn(prev, TOT[j]);
     if (rtype == FVG_REG_L2) w = no_eta ? __dsub_rn(w, __dmul_rn(lambda, w)) : __dmul_rn(scale, w);
     else if (rtype == FVG_REG_L1) w = __dsub_rn(w, __dmul_rn(lambda, (double)((w >= 0) - (w < 0))));
     W[j] = w;
-    double df = prev - w;
+    double df = a.used ? TOT[j] : prev - w;
     v[0] += df * df;
   }
   const bool mx[1] = {false};
@@ -811,9 +821,30 @@ __global__ void __launch_bounds__(kVecThreads) k_sgd_apply(double* __restrict__ 
     double pb = a.scal[1];
     double nb = __dadd_rn(pb, a.scal[3]);
     a.scal[1] = nb;
-    double red = t[0] + (pb - nb) * (pb - nb);
-    a.scal[0] = sqrt(red / (double)(a.n + 1));
+    if (a.used) {
+      double red = t[0] + (icpt ? a.scal[7] * a.scal[7] : 0.0);
+      a.scal[0] = sqrt(red / (a.n_used0 + 1.0));
+    } else {
+      double red = t[0] + (pb - nb) * (pb - nb);
+      a.scal[0] = sqrt(red / (double)(a.n + 1));
+    }
   });
+}
+
+// shrink_column_local (matrix/shrink_matrix.hpp): marks the columns a block
+// of nonzeros uses; the count of newly marked columns is added to *count.
+__global__ void k_mark_used(const i32* __restrict__ idx, i64 nnz, int* __restrict__ used,
+                            unsigned long long* __restrict__ count) {
+  unsigned long long mine = 0;
+  for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (i64)gridDim.x * blockDim.x)
+    if (atomicExch(&used[idx[e]], 1) == 0) mine++;
+  if (count && mine) atomicAdd(count, mine);
+}
+
+// shrink_vector_merge: columns no rank holds come back as 0.
+__global__ void k_zero_unused(double* __restrict__ W, const int* __restrict__ used, i64 n) {
+  for (i64 j = (i64)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (i64)gridDim.x * blockDim.x)
+    if (!used[j]) W[j] = 0.0;
 }
 
 // One minibatch's loss into its rank's running loss (gradient_descent::
@@ -828,7 +859,7 @@ __global__ void k_sgd_loss(const double* __restrict__ out, double* __restrict__ 
 }
 
 void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
-               double* w_h, double* b_h, i64* n_iter, double* loss_out) {
+               double* w_h, double* b_h, i64* n_iter, double* loss_out, bool shrink) {
   check_common(p, M, label_h);
   const int fmt = p->mat_type;
   if (fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
@@ -893,7 +924,32 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
   double hs[8] = {0, *b_h, *b_h, 0, 0, 0, 0, 0};
   FVG_CUDA(cudaMemcpyAsync(scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
   FVG_CUDA(cudaMemcpyAsync(W.p, w_h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  SgdArgs sa{n, n1, part.as<double>(), ticket, scal.as<double>()};
+  SgdArgs sa{n, n1, part.as<double>(), ticket, scal.as<double>(), nullptr, 0.0};
+  DBuf used, used0;
+  if (shrink) {
+    // used columns over all ranks, and rank 0's own count (each rank's
+    // shrink table covers all of its minibatches)
+    used.alloc(sizeof(int) * std::max<i64>(n, 1), s);
+    used0.alloc(sizeof(int) * std::max<i64>(n, 1) + 256, s);
+    FVG_CUDA(cudaMemsetAsync(used.p, 0, sizeof(int) * std::max<i64>(n, 1), s));
+    FVG_CUDA(cudaMemsetAsync(used0.p, 0, sizeof(int) * std::max<i64>(n, 1) + 256, s));
+    unsigned long long* cnt0 = (unsigned long long*)((char*)used0.p + sizeof(int) * std::max<i64>(n, 1));
+    for (int r = 0; r < P; r++)
+      for (auto& b : ranks[r]) {
+        const DevCRS& A = *b->op.oA;
+        if (A.nnz == 0) continue;
+        const int g = (int)std::max<i64>(1, std::min<i64>((A.nnz + 255) / 256, 4 * (i64)c->num_sms));
+        k_mark_used<<<g, 256, 0, s>>>(A.idx.as<i32>(), A.nnz, used.as<int>(), nullptr);
+        if (r == 0) k_mark_used<<<g, 256, 0, s>>>(A.idx.as<i32>(), A.nnz, used0.as<int>(), cnt0);
+        check_launch("mark_used");
+        count_launch(c, r == 0 ? 2 : 1);
+      }
+    unsigned long long n0 = 0;
+    FVG_CUDA(cudaMemcpyAsync(&n0, cnt0, sizeof(n0), cudaMemcpyDeviceToHost, s));
+    FVG_CUDA(cudaStreamSynchronize(s));
+    sa.used = used.as<int>();
+    sa.n_used0 = (double)n0;
+  }
   HostPinned hp(8);
   i64 i;
   for (i = 1; i <= p->num_iteration; i++) {
@@ -926,8 +982,11 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
       count_launch(c);
       first_rank = false;
     }
+    // the shrink driver calls regularize(w) with its default eta = 1
+    // (shrink_sgd_parallelizer.hpp:134; regularizer.hpp:43)
     k_sgd_apply<<<vgrid, kVecThreads, 0, s>>>(W.as<double>(), TOT.as<double>(), p->reg_type, p->reg_param,
-                                              p->alpha / std::sqrt((double)i), p->l2_no_eta, sa);
+                                              shrink ? 1.0 : p->alpha / std::sqrt((double)i), p->l2_no_eta,
+                                              p->intercept, sa);
     check_launch("sgd_apply");
     count_launch(c);
     FVG_CUDA(cudaMemcpyAsync(hp.p, scal.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
@@ -935,6 +994,14 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
     if (hp.p[0] < p->convergence_tol) break;
   }
   *n_iter = (i == p->num_iteration + 1) ? p->num_iteration : i;
+  // the shrink driver's no-trans (ELL) loop reports i as is: numIteration+1
+  // when it ran out (shrink_sgd_parallelizer.hpp:315)
+  if (shrink && fmt == FVG_ELL) *n_iter = i;
+  if (shrink && n > 0) {
+    k_zero_unused<<<vgrid, kVecThreads, 0, s>>>(W.as<double>(), used.as<int>(), n);
+    check_launch("zero_unused");
+    count_launch(c);
+  }
   FVG_CUDA(cudaMemcpyAsync(hp.p, scal.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));

@@ -466,7 +466,7 @@ template <class T, class I, class O, class MODEL>
 MODEL train(bool sgd, crs_matrix_local<T, I, O>& data, std::vector<T>& label, MODEL& initModel,
             std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration, double alpha, size_t hist_size,
             double miniBatchFraction, double regParam, RegType regTyp, bool isIntercept, double convergenceTol,
-            MatType mType, fvg_loss loss = FVG_LOSS_LOGISTIC, double eps = 0.0) {
+            MatType mType, fvg_loss loss = FVG_LOSS_LOGISTIC, double eps = 0.0, bool shrink = false) {
   if (data.local_num_col != initModel.get_num_features())
     throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Incompatible Test Vector with Provided Initial Model\n");
   if (data.local_num_row != label.size())
@@ -491,8 +491,9 @@ MODEL train(bool sgd, crs_matrix_local<T, I, O>& data, std::vector<T>& label, MO
   std::vector<double> w(initModel.weight.begin(), initModel.weight.end());
   double b = initModel.intercept, fl = 0;
   int64_t it = 0;
-  frovedis_gb300::check((sgd ? fvg_glm_sgd : fvg_glm_lbfgs)(frovedis_gb300::context(), d.h, lab.data(), sw.data(),
-                                                            &p, w.data(), &b, &it, &fl));
+  auto fn = sgd ? fvg_glm_sgd : fvg_glm_lbfgs;
+  if (shrink) fn = fvg_logreg_shrink_sgd;
+  frovedis_gb300::check(fn(frovedis_gb300::context(), d.h, lab.data(), sw.data(), &p, w.data(), &b, &it, &fl));
   n_iter = (size_t)it;
   MODEL ret = initModel;
   ret.weight.assign(w.begin(), w.end());
@@ -568,6 +569,49 @@ struct logistic_regression_with_sgd {
     return m;
   }
 };
+
+namespace shrink {
+// shrink::logistic_regression_with_sgd (ml/glm/shrink_logistic_regression_with_sgd.hpp
+// → shrink_sgd_parallelizer.hpp): SGD over per-rank shrunk column sets.
+struct logistic_regression_with_sgd {
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                            size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    std::vector<T> sw;
+    size_t n_iter = 0;
+    return train(data, label, sw, n_iter, numIteration, alpha, miniBatchFraction, regParam, regTyp, isIntercept,
+                 convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                            std::vector<T>& sample_weight, size_t& n_iter,
+                                            size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.local_num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix_local<T, I, O>& data, std::vector<T>& label,
+                                            logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS,
+                                            bool inputMovable = false) {
+    auto m = detail::train(true, data, label, initModel, sample_weight, n_iter, numIteration, alpha, 10,
+                           miniBatchFraction, regParam, regTyp, isIntercept, convergenceTol, mType,
+                           FVG_LOSS_LOGISTIC, 0.0, true);
+    if (inputMovable) data.clear();
+    return m;
+  }
+};
+}  // namespace shrink
 
 // linear_regression_model<T> (ml/glm/linear_model.hpp:211-298): weights
 // start at 1; predict = mat * weight (+ intercept when non-zero).
@@ -1353,12 +1397,16 @@ struct logistic_regression {
       model_bin = logistic_regression_with_sgd::train(mat, label, model_bin, sample_weight, n_iter, max_iter, alpha,
                                                       mbf, reg_param, get_regularizer(), fit_intercept, tol,
                                                       mat_type);
+    } else if (solver == "shrink-sgd") {
+      model_bin = shrink::logistic_regression_with_sgd::train(mat, label, model_bin, sample_weight, n_iter, max_iter,
+                                                              alpha, mbf, reg_param, get_regularizer(),
+                                                              fit_intercept, tol, mat_type);
     } else if (solver == "lbfgs") {
       model_bin = logistic_regression_with_lbfgs::train(mat, label, model_bin, sample_weight, n_iter, max_iter,
                                                         alpha, hist_size, reg_param, get_regularizer(),
                                                         fit_intercept, tol, mat_type);
     } else {
-      throw frovedis_gb300::error(FVG_ERR_UNSUPPORTED, "solver " + solver + " is not provided by the GB300 path\n");
+      throw frovedis_gb300::error(FVG_ERR_INVALID_ARG, "Unknown solver is encountered!\n");
     }
     is_fitted = true;
     n_iter_ = n_iter;

@@ -276,6 +276,18 @@ FVG_API fvg_status fvg_multinomial_probability(fvg_ctx* ctx, fvg_matrix* mat, co
 FVG_API fvg_status fvg_logreg_sgd(fvg_ctx* ctx, fvg_matrix* mat, const double* label, const double* sample_weight,
                                   const fvg_glm_params* params, double* weight, double* intercept, int64_t* n_iter,
                                   double* final_loss);
+/* shrink::logistic_regression_with_sgd::train main API
+ * (ml/glm/shrink_logistic_regression_with_sgd.hpp → shrink_sgd_parallelizer.hpp:
+ * 82-151, 153-253, 378-494): SGD as fvg_logreg_sgd, except that every rank
+ * keeps only the columns its rows use (shrink_column) — those alone are
+ * regularised, with eta = 1, and columns no rank uses come back as 0; the
+ * RMS stop test takes the summed change before regularisation plus rank 0's
+ * intercept change over rank 0's column count + 1; with FVG_ELL the
+ * reported iteration count is numIteration + 1 when the test never passed
+ * (the driver's no-trans loop). */
+FVG_API fvg_status fvg_logreg_shrink_sgd(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* params, double* weight,
+                                         double* intercept, int64_t* n_iter, double* final_loss);
 /* One loss/gradient evaluation (gradient_descent::compute_gradient,
  * gradient_descent.hpp:196-225): grad[num_col+1] (bias last), *loss. */
 FVG_API fvg_status fvg_logreg_eval(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage,

@@ -275,9 +275,10 @@ def logreg_lbfgs(a: CRS, label, num_iter=1000, alpha=0.01, hist_size=10, reg_par
 
 def logreg_sgd(a: CRS, label, num_iter=1000, alpha=0.01, mini_batch_fraction=1.0, reg_param=0.01,
                reg_type="ZERO", intercept=False, tol=0.001, fmt="CRS", sw=None, w0=None, b0=None, splits=None,
-               nthreads=1, l2_no_eta=False, loss="logistic", eps=0.0):
+               nthreads=1, l2_no_eta=False, loss="logistic", eps=0.0, shrink=False):
     """``logistic_regression_with_sgd::train`` semantics (``loss`` selects the
-    other GLMs' gradient); returns a dict."""
+    other GLMs' gradient; ``shrink`` the shrink::logistic_regression_with_sgd
+    driver); returns a dict."""
     label = np.ascontiguousarray(label, dtype=np.float64)
     sw = np.ones(a.m) if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
     w = np.ones(a.n) if w0 is None else np.array(w0, dtype=np.float64)
@@ -288,7 +289,8 @@ def logreg_sgd(a: CRS, label, num_iter=1000, alpha=0.01, mini_batch_fraction=1.0
     fl = np.zeros(1)
     rc = lib().orc_glm_sgd_f64(FMT[fmt], *a.args(), _ptr(label), _ptr(sw), _ptr(sp), P, nthreads, num_iter,
                                alpha, mini_batch_fraction, reg_param, REG[reg_type], int(intercept), tol,
-                               _ptr(w), _ptr(b), _ptr(n_iter), _ptr(fl), int(l2_no_eta), LOSS[loss], float(eps))
+                               _ptr(w), _ptr(b), _ptr(n_iter), _ptr(fl), int(l2_no_eta) | (2 if shrink else 0),
+                               LOSS[loss], float(eps))
     if rc != 0:
         raise ValueError(f"oracle sgd rejected the arguments (code {rc})")
     return dict(w=w, b=float(b[0]), n_iter=int(n_iter[0]), loss=float(fl[0]))

@@ -751,7 +751,7 @@ template <class T>
 void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, int P, int fmt,
                std::vector<T>& w, T& b, i64 num_iter, double alpha, double frac, T lambda, int rtype,
                bool icpt, double tol, i64& n_iter, double& final_loss, int nthreads, bool no_eta = false,
-               const Loss& L = Loss()) {
+               const Loss& L = Loss(), bool shrink = false) {
   struct RankSGD {
     std::vector<RankData<T>> batches;
     std::vector<std::vector<T>> label, sw;
@@ -771,6 +771,17 @@ void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, 
     }
   });
   i64 n = (i64)w.size();
+  // shrink::sgd_parallelizer: shrink_column per rank (matrix/shrink_matrix.hpp);
+  // used = columns of any rank, n_used0 = rank 0's own column count
+  std::vector<char> used(n, 0), used0(n, 0);
+  if (shrink)
+    for (int r = 0; r < P; r++)
+      for (i64 q = a.off[splits[r]]; q < a.off[splits[r + 1]]; q++) {
+        used[a.idx[q]] = 1;
+        if (r == 0) used0[a.idx[q]] = 1;
+      }
+  i64 n_used0 = 0;
+  for (char u : used0) n_used0 += u;
   double sumloss = 0.0;
   i64 i;
   for (i = 1; i <= num_iter; i++) {
@@ -797,6 +808,29 @@ void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, 
       for (i64 q = 0; q <= n; q++) tot[q] += delta[r][q];
     sumloss = lloss[0];
     for (int r = 1; r < P; r++) sumloss += lloss[r];
+    if (shrink) {
+      // update_model_local (shrink_sgd_parallelizer.hpp:99-151): global -=
+      // Σ(global - local) on the used columns, regularize(w) with eta = 1,
+      // RMSE of the summed change + rank 0's own intercept change over rank
+      // 0's column count + 1
+      T sq = 0;
+      for (i64 q = 0; q < n; q++) {
+        if (!used[q]) continue;
+        w[q] += tot[q];
+        sq += tot[q] * tot[q];
+      }
+      if (icpt) b += tot[n];
+      std::vector<T> uw;
+      for (i64 q = 0; q < n; q++)
+        if (used[q]) uw.push_back(w[q]);
+      regularize(uw, rtype, lambda, 1.0, no_eta);
+      for (i64 q = 0, k = 0; q < n; q++)
+        if (used[q]) w[q] = uw[k++];
+      if (icpt) sq += delta[0][n] * delta[0][n];
+      double rmse = std::sqrt(sq / (T)(n_used0 + 1));
+      if (rmse < tol) break;
+      continue;
+    }
     std::vector<T> prev = w;
     T prevb = b;
     for (i64 q = 0; q < n; q++) w[q] += tot[q];
@@ -819,6 +853,10 @@ void sgd_train(const CRS<T>& a, const T* label, const T* sw, const i64* splits, 
     if (rmse < tol) break;
   }
   n_iter = (i == num_iter + 1) ? num_iter : i;
+  if (shrink && fmt == ELL_F) n_iter = i;  // do_train_notrans reports i (shrink_sgd_parallelizer.hpp:315)
+  if (shrink)
+    for (i64 q = 0; q < n; q++)
+      if (!used[q]) w[q] = 0;  // shrink_vector_merge: unheld columns are 0
   final_loss = sumloss;
 }
 
@@ -1079,6 +1117,7 @@ int orc_glm_lbfgs_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, con
   return 0;
 }
 
+// shrink::logistic_regression_with_sgd::train (flags bit 1 of orc_glm_sgd_f64)
 int orc_glm_sgd_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
                     const double* label, const double* sw, const i64* splits, int P, int nthreads,
                     i64 num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,
@@ -1091,7 +1130,7 @@ int orc_glm_sgd_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const
   std::vector<double> wv(w, w + n);
   double bb = *b;
   sgd_train(a, label, sw, sp.data(), P, fmt, wv, bb, num_iter, alpha, frac, lambda, rtype, icpt != 0, tol, *n_iter,
-            *final_loss, nthreads, (flags & 1) != 0, Loss{lkind, eps});
+            *final_loss, nthreads, (flags & 1) != 0, Loss{lkind, eps}, (flags & 2) != 0);
   std::copy(wv.begin(), wv.end(), w);
   *b = bb;
   return 0;

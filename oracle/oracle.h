@@ -2,7 +2,8 @@
 // used by the Python tests through ctypes.  Index arrays are int32, row
 // offsets int32 on input (the layout the CUDA path uses), int64 where the
 // reference's JDS offsets can exceed the input's.  Trainer flags: bit 0 =
-// L2 without USE_ETA (w -= lambda*w, regularizer.hpp:50-54).
+// L2 without USE_ETA (w -= lambda*w, regularizer.hpp:50-54); bit 1 (SGD) =
+// the shrink driver (shrink_sgd_parallelizer.hpp).
 #ifndef FVG_ORACLE_H
 #define FVG_ORACLE_H
 #include <stdint.h>

@@ -260,6 +260,20 @@ int main(int argc, char** argv) {
     put1(f, "svm_loaded_same", sv2.weight == sv.weight && sv2.intercept == sv.intercept &&
                                    sv2.threshold == sv.threshold);
   }
+  {
+    // shrink::logistic_regression_with_sgd and the estimator's shrink-sgd solver
+    std::vector<double> sw;
+    size_t it = 0;
+    auto sm = shrink::logistic_regression_with_sgd::train(A, label, sw, it, 15, 0.05, 0.3, 1e-2, L2, true, 0.0);
+    put(f, "shrink_w", sm.weight);
+    put1(f, "shrink_b", sm.intercept);
+    put1(f, "shrink_n_iter", (double)it);
+    logistic_regression<double> es(12, 0.05, "shrink-sgd", 1e-3, "L1", true);
+    std::vector<double> lab = label;
+    es.fit(A, lab);
+    put(f, "est_shrink_w", es.get_weight());
+    put1(f, "est_shrink_n_iter", (double)es.n_iter_);
+  }
   std::fclose(f);
   return 0;
 }

@@ -178,3 +178,12 @@ def test_cpp_api_matches_oracle(tmp_path):
     assert o["svm_jds_throws"][0] == 1
     assert np.max(np.abs(o["lin_loaded_w"] - o["lin_sgd_w"])) <= 1e-11 * max(1.0, np.max(np.abs(o["lin_sgd_w"])))
     assert o["svm_loaded_same"][0] == 1
+
+    rs = oracle.logreg_sgd(a, label, shrink=True, num_iter=15, alpha=0.05, mini_batch_fraction=0.3, reg_type="L2",
+                           reg_param=1e-2, intercept=True, tol=0.0)
+    assert wclose(o["shrink_w"], rs["w"]) and abs(o["shrink_b"][0] - rs["b"]) <= 1e-5 * max(1.0, abs(rs["b"]))
+    assert int(o["shrink_n_iter"][0]) == rs["n_iter"] == 15
+    # estimator: initial model (w = 1, b = fit_intercept) as logistic_regression::_fit builds it
+    rs = oracle.logreg_sgd(a, label, shrink=True, num_iter=12, alpha=0.05, reg_type="L1", reg_param=1e-3,
+                           intercept=True, b0=1.0)
+    assert wclose(o["est_shrink_w"], rs["w"]) and int(o["est_shrink_n_iter"][0]) == rs["n_iter"]

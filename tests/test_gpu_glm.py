@@ -218,3 +218,44 @@ def test_glm_errors_and_logistic_entry_points(ctx):
     assert np.array_equal(r1["w"], r2["w"])
     r3 = fv.glm_lbfgs(A, label, loss="logistic", num_iter=5)
     assert np.array_equal(r1["w"], r3["w"])
+
+
+# ------------------------------------------------------------- shrink SGD
+def _shrunk_problem():
+    """Columns 260.. unused by every rank; column 255 used only by the last
+    rank's rows (splits 0 / 1000 / 2500 / 4000)."""
+    a, label, _ = _data(10, m=4000, n=300)
+    rows = np.repeat(np.arange(a.m), np.diff(a.off))
+    keep = (a.idx < 260) & ~((a.idx == 255) & (rows < 2500))
+    off = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=a.m))]).astype(np.int32)
+    return oracle.CRS(a.m, a.n, off, a.idx[keep], a.val[keep]), label
+
+
+@pytest.mark.parametrize("fmt", FMTS)
+@pytest.mark.parametrize("reg", ["L1", "L2"])
+def test_shrink_sgd_matches_oracle(ctx, fmt, reg):
+    a, label = _shrunk_problem()
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    splits = [0, 1000, 2500, 4000]
+    kw = dict(num_iter=20, alpha=0.05, mini_batch_fraction=0.4, reg_type=reg, reg_param=1e-2, intercept=True)
+    r = fv.logreg_shrink_sgd(A, label, mat_type=fmt, row_splits=splits, **kw)
+    ro = oracle.logreg_sgd(a, label, shrink=True, fmt=fmt, splits=splits, **kw)
+    # ELL: the no-trans driver reports numIteration + 1 (shrink_sgd_parallelizer.hpp:315)
+    assert r["n_iter"] == ro["n_iter"] == (21 if fmt == "ELL" else 20)
+    assert abs(r["loss"] - ro["loss"]) <= 1e-6 * abs(ro["loss"])
+    assert np.max(np.abs(r["w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))
+    assert abs(r["b"] - ro["b"]) <= 1e-5 * max(1.0, abs(ro["b"]))
+    assert np.all(r["w"][260:] == 0.0) and r["w"][255] != 0.0
+
+
+def test_shrink_sgd_stop_test(ctx):
+    # RMS of the summed change before regularisation + rank 0's intercept
+    # change over rank 0's column count + 1: stops earlier than plain SGD here
+    a, label, _ = _data(10, m=4000, n=300)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    splits = [0, 1000, 2500, 4000]
+    kw = dict(num_iter=50, alpha=3e-5, reg_type="L2", reg_param=1e-2, intercept=True, tol=1e-3)
+    r = fv.logreg_shrink_sgd(A, label, row_splits=splits, **kw)
+    ro = oracle.logreg_sgd(a, label, shrink=True, splits=splits, **kw)
+    assert r["n_iter"] == ro["n_iter"] < 50
+    assert np.max(np.abs(r["w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))

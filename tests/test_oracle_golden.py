@@ -197,3 +197,22 @@ def test_glm_dloss_kinds():
     assert np.allclose(d, [0.0, 4.8, 2.8], rtol=0, atol=1e-15) and abs(s - (2.4 ** 2 + 1.4 ** 2)) < 1e-12
     d, _ = oracle.glm_dloss(np.zeros(2), np.array([2e12, -3e12]), "linear")
     assert d.tolist() == [1e12, -1e12]  # MAX_LOSS / MIN_LOSS clip
+
+
+def test_shrink_sgd_equals_sgd_without_regulariser():
+    # with no regulariser and no stop test the shrink driver only differs in
+    # the columns no rank uses (returned as 0); the update is the same
+    rng = np.random.default_rng(12)
+    m, n = 600, 80
+    lens = rng.integers(0, 8, m)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    idx = np.concatenate([np.sort(rng.choice(60, k, replace=False)) for k in lens]).astype(np.int32)
+    a = oracle.CRS(m, n, off, idx, rng.standard_normal(off[-1]))
+    label = np.where(rng.random(m) < 0.5, 1.0, -1.0)
+    kw = dict(num_iter=10, alpha=0.05, reg_type="ZERO", intercept=True, tol=0.0, splits=[0, 200, 600])
+    r1 = oracle.logreg_sgd(a, label, shrink=True, **kw)
+    r2 = oracle.logreg_sgd(a, label, **kw)
+    used = np.zeros(n, bool)
+    used[idx] = True
+    assert np.array_equal(r1["w"][used], r2["w"][used]) and r1["b"] == r2["b"]
+    assert np.all(r1["w"][~used] == 0.0) and np.all(r2["w"][~used] == 1.0)
