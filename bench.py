@@ -249,6 +249,29 @@ def run_gpu(args):
             v["loss_rel_diff_vs_f64"] = abs(v["final_loss"] - l64) / abs(l64)
             v["speedup_vs_f64"] = v["iters_per_s"] / modes["f64"]["iters_per_s"]
 
+    # the other GLM losses on the same matrix and the same fused kernels
+    # (ridge regression = squared loss with L2, linear SVM = hinge with L2;
+    # the +-1 labels serve as regression targets): iterations/s at the
+    # benchmark precision and at FP64, and the final-loss difference
+    glm = None
+    if not args.skip_glm:
+        glm = {}
+        for loss in ("linear", "hinge"):
+            row = {}
+            for st in (args.storage, "f64"):
+                kwg = dict(kw, storage=st, num_iter=20)
+                fv.glm_lbfgs(A, label, loss=loss, **dict(kwg, num_iter=2))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                rg = fv.glm_lbfgs(A, label, loss=loss, **kwg)
+                torch.cuda.synchronize()
+                row["iters_per_s_" + st] = rg["n_iter"] / (time.perf_counter() - t0)
+                row["final_loss_" + st] = rg["loss"]
+            row["speedup_vs_f64"] = row["iters_per_s_" + args.storage] / row["iters_per_s_f64"]
+            row["loss_rel_diff_vs_f64"] = abs(row["final_loss_" + args.storage] - row["final_loss_f64"]) / abs(
+                row["final_loss_f64"])
+            glm[{"linear": "ridge_regression_lbfgs", "hinge": "svm_lbfgs"}[loss]] = row
+
     # end to end through the C ABI with host buffers
     A.close()
     e2e_ms = 0.0
@@ -296,6 +319,8 @@ def run_gpu(args):
                    "storage": args.storage, "l2_flush": "inputs larger than L2 (A is %.1f GB)" % (
                        nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU"},
         "final_loss": r["loss"], "iterations_per_run": r["n_iter"],
+        # loss/gradient evaluations (one pass 1 each; line-search trials included)
+        "evaluations_per_s": (prof["pass1"][1] + prof["pass1_f32"][1]) * world / (ms / 1e3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)",
@@ -311,6 +336,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": ck,
         "precision_modes": modes,
+        "glm_losses": glm,
         "spmv_2m": spmv,
         "batched_regpath": rp,
         "cpu_baseline": cpu,
@@ -609,6 +635,7 @@ def main():
     ap.add_argument("--datasets", type=int, default=16, help="regpath: number of datasets")
     ap.add_argument("--regpath-datasets", type=int, default=4, help="datasets of the batched summary line")
     ap.add_argument("--skip-regpath", action="store_true")
+    ap.add_argument("--skip-glm", action="store_true", help="skip the ridge / SVM summary")
     args = ap.parse_args()
     if args.workload == "regpath":
         if args.iters == 50:

@@ -343,3 +343,24 @@ def test_predict_probability(ctx):
     w = np.random.default_rng(0).standard_normal(a.n) * 5
     for b in (0.0, 1.5):
         assert close(fv.predict_probability(A, w, b), oracle.predict_probability(a, w, b), 1e-13)
+
+
+def test_lbfgs_logreg_100k_20k_configuration(ctx):
+    # the reference's CPU-sized configuration at full size: 100,000 x 20,000,
+    # nnz/row 1+Poisson(39), Zipf(1.1) columns, |N(0,1)| values, L2 1e-3,
+    # 20 iterations, FP64 — every line-search decision as the oracle's
+    from frovedis_gb300 import datagen
+    spec = datagen.logreg_100k_20k()
+    off, idx, val, label = datagen.generate(spec)
+    a = oracle.CRS(spec.m, spec.n, off, idx, val)
+    A = ctx.matrix(spec.m, spec.n, off, idx, val)
+    kw = dict(num_iter=20, reg_type="L2", reg_param=1e-3)
+    r = fv.logreg_lbfgs(A, label, trace=True, **kw)
+    ro = oracle.logreg_lbfgs(a, label, nthreads=8, **kw)
+    assert r["n_iter"] == ro["n_iter"] == 20
+    assert np.array_equal(r["trace"][:, 1], ro["trace"][:, 1])
+    assert abs(r["loss"] - ro["loss"]) <= 1e-6 * abs(ro["loss"])
+    assert np.max(np.abs(r["w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))
+    for storage in ("f32", "bf16"):
+        rs = fv.logreg_lbfgs(A, label, storage=storage, **kw)
+        assert abs(rs["loss"] - ro["loss"]) <= 1e-3 * abs(ro["loss"]), storage
