@@ -304,7 +304,7 @@ def run_gpu(args):
     rp = None if args.skip_regpath else regpath(args, args.regpath_datasets, 20)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_baseline(off, idx, val, label, spec, args, threads=0, sample_rows=args.cpu_rows)
+        cpu = cpu_baseline(off, idx, val, label, spec, args, threads=0, sample_rows=args.cpu_rows, single=True)
     ctx.close()
     if rank != 0:
         return
@@ -556,7 +556,7 @@ def run_multinomial(args):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
+def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows, single=False):
     """The oracle (reference loops, FP64) on the first `sample_rows` rows,
     rows split over `threads` emulated ranks; scaled to full-size iters/s by
     the nonzero ratio."""
@@ -578,9 +578,27 @@ def cpu_baseline(off, idx, val, label, spec, args, threads, sample_rows):
     dt = (t2 - t1) - (t1 - t0)
     sample_rate = k / dt if dt > 0 and k > 0 else float("nan")
     full = sample_rate * z / int(off[-1])
-    return {"value": full, "unit": "iters/s", "cores": threads, "kind": "port",
-            "sample": f"{k} L-BFGS iterations (setup excluded) on the first {ms} rows ({z} nnz), {threads} "
-                      f"emulated ranks, scaled by nnz to the full matrix; {dt:.2f} s"}
+    out = {"value": full, "unit": "iters/s", "cores": threads, "kind": "port",
+           "sample": f"{k} L-BFGS iterations (setup excluded) on the first {ms} rows ({z} nnz), {threads} "
+                     f"emulated ranks, scaled by nnz to the full matrix; {dt:.2f} s"}
+    if single:
+        # the reference's exact single-rank loops on one core (a smaller sample)
+        ms1 = min(sample_rows // 8, spec.m)
+        z1 = int(off[ms1])
+        a1 = oracle.CRS(ms1, spec.n, off[: ms1 + 1], idx[:z1], val[:z1])
+        kw1 = dict(reg_type="L2", reg_param=1e-4, nthreads=1, w0=np.zeros(spec.n))
+        t0 = time.perf_counter()
+        q1 = oracle.logreg_lbfgs(a1, label[:ms1], num_iter=1, **kw1)
+        t1 = time.perf_counter()
+        q2 = oracle.logreg_lbfgs(a1, label[:ms1], num_iter=1 + max(2, args.cpu_iters // 10), **kw1)
+        t2 = time.perf_counter()
+        k1 = q2["n_iter"] - q1["n_iter"]
+        d1 = (t2 - t1) - (t1 - t0)
+        r1v = k1 / d1 * z1 / int(off[-1]) if d1 > 0 and k1 > 0 else float("nan")
+        out["single_thread"] = {"value": r1v, "unit": "iters/s", "cores": 1,
+                                "sample": f"{k1} iterations on the first {ms1} rows ({z1} nnz), one rank, "
+                                          f"scaled by nnz to the full matrix; {d1:.2f} s"}
+    return out
 
 
 def run_reference(args):
