@@ -82,13 +82,28 @@ __device__ __forceinline__ void col_reduce(double (&v)[NV], const bool (&is_max)
   double t[NV];
 #pragma unroll
   for (int q = 0; q < NV; q++) t[q] = 0.0;
-  if (j < a.k)
-    for (i64 b = rr; b < gridDim.x; b += a.rpb)
+  if (j < a.k) {
+    // the CTAs' partials in CTA order; eight loads issued before they are
+    // combined (same order as one at a time)
+    i64 b = rr;
+    for (; b + 7 * a.rpb < gridDim.x; b += 8 * a.rpb) {
+      double x[8][NV];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int q = 0; q < NV; q++) x[u][q] = __ldcg(&a.part[((b + u * a.rpb) * a.k + j) * NV + q]);
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int q = 0; q < NV; q++) t[q] = is_max[q] ? fmax(t[q], x[u][q]) : t[q] + x[u][q];
+    }
+    for (; b < gridDim.x; b += a.rpb)
 #pragma unroll
       for (int q = 0; q < NV; q++) {
         const double x = __ldcg(&a.part[(b * a.k + j) * NV + q]);
         t[q] = is_max[q] ? fmax(t[q], x) : t[q] + x;
       }
+  }
 #pragma unroll
   for (int q = 0; q < NV; q++) sm[q][threadIdx.x] = t[q];
   __syncthreads();
@@ -118,12 +133,36 @@ __device__ __forceinline__ void col_reduce(double (&v)[NV], const bool (&is_max)
   const bool on = j < a.k;                     \
   const i64 rstep = (i64)gridDim.x * a.rpb;    \
   const i64 r0 = (i64)blockIdx.x * a.rpb + rr
-#define BROWS(r, nrows) _Pragma("unroll 4") for (i64 r = r0; r < (nrows); r += rstep)
+// The rows of a column in groups of U: every load of a group is issued
+// before the first use, so a thread keeps U row-loads in flight (the column
+// kernels stream 256 MB planes and are bound by memory-level parallelism).
+// use() runs in increasing row order, as the plain loop does.
+template <int U, class Load, class Use>
+__device__ __forceinline__ void rows_grouped(i64 r0, i64 rstep, i64 nrows, Load load, Use use) {
+  using V = decltype(load(r0));
+  for (i64 rb = r0; rb < nrows; rb += (i64)U * rstep) {
+    V buf[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const i64 r = rb + u * rstep;
+      if (r < nrows) buf[u] = load(r);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const i64 r = rb + u * rstep;
+      if (r < nrows) use(r, buf[u]);
+    }
+  }
+}
+constexpr int kRowGroup = 4;
+struct V2 { double a, b; };
+struct V3 { double a, b, c; };
+struct V4 { double a, b, c, d; };
 
 __device__ __forceinline__ i64 hslot(int rear, int i, int h) { return (i64)((rear + i) % h); }
 
 // two-loop recursion, first loop (see the single-model k_down)
-__global__ void __launch_bounds__(kBT) kb_down(int i, int kh, int rear, const double* __restrict__ G,
+__global__ void __launch_bounds__(kBT, 4) kb_down(int i, int kh, int rear, const double* __restrict__ G,
                                                double* __restrict__ Q, const double* __restrict__ S,
                                                const double* __restrict__ Y, BArgs a) {
   BCOL;
@@ -134,12 +173,21 @@ __global__ void __launch_bounds__(kBT) kb_down(int i, int kh, int rear, const do
   const double* Yp = Y + hslot(rear, i + 1, a.h) * plane;
   const double alp = (act && !first) ? a.st[j].al[i + 1] : 0.0;
   double v[1] = {0.0};
-  if (act) BROWS(r, a.n1) {
-      const i64 e = r * a.k + j;
-      const double q = first ? G[e] : __dsub_rn(Q[e], __dmul_rn(Yp[e], alp));
-      Q[e] = q;
-      v[0] += Si[e] * q;
-    }
+  const int k = a.k;
+  if (act && first)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1, [&](i64 r) { const i64 e = r * k + j; return V2{G[e], Si[e]}; },
+                            [&](i64 r, const V2& x) {
+                              Q[r * k + j] = x.a;
+                              v[0] += x.b * x.a;
+                            });
+  else if (act)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1,
+                            [&](i64 r) { const i64 e = r * k + j; return V3{Q[e], Yp[e], Si[e]}; },
+                            [&](i64 r, const V3& x) {
+                              const double q = __dsub_rn(x.a, __dmul_rn(x.b, alp));
+                              Q[r * k + j] = q;
+                              v[0] += x.c * q;
+                            });
   const bool mx[1] = {false};
   col_reduce<1>(v, mx, a, [&](int c, double* t) {
     ColState& s = a.st[c];
@@ -148,7 +196,7 @@ __global__ void __launch_bounds__(kBT) kb_down(int i, int kh, int rear, const do
 }
 
 // second loop (see k_up)
-__global__ void __launch_bounds__(kBT) kb_up(int i, int kh, int rear, const double* __restrict__ Q,
+__global__ void __launch_bounds__(kBT, 4) kb_up(int i, int kh, int rear, const double* __restrict__ Q,
                                              double* __restrict__ Z, const double* __restrict__ S,
                                              const double* __restrict__ Y, BArgs a) {
   BCOL;
@@ -171,13 +219,22 @@ __global__ void __launch_bounds__(kBT) kb_up(int i, int kh, int rear, const doub
     }
   }
   double v[1] = {0.0};
-  if (act) BROWS(r, a.n1) {
-      const i64 e = r * a.k + j;
-      const double z =
-          (i == 0) ? __dmul_rn(__dsub_rn(Q[e], __dmul_rn(Yi[e], al0)), H0) : __dadd_rn(Z[e], __dmul_rn(Sp[e], f));
-      Z[e] = z;
-      v[0] += Yi[e] * z;
-    }
+  const int k = a.k;
+  if (act && i == 0)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1, [&](i64 r) { const i64 e = r * k + j; return V2{Q[e], Yi[e]}; },
+                            [&](i64 r, const V2& x) {
+                              const double z = __dmul_rn(__dsub_rn(x.a, __dmul_rn(x.b, al0)), H0);
+                              Z[r * k + j] = z;
+                              v[0] += x.b * z;
+                            });
+  else if (act)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1,
+                            [&](i64 r) { const i64 e = r * k + j; return V3{Z[e], Sp[e], Yi[e]}; },
+                            [&](i64 r, const V3& x) {
+                              const double z = __dadd_rn(x.a, __dmul_rn(x.b, f));
+                              Z[r * k + j] = z;
+                              v[0] += x.c * z;
+                            });
   const bool mx[1] = {false};
   col_reduce<1>(v, mx, a, [&](int c, double* t) {
     ColState& s = a.st[c];
@@ -186,7 +243,7 @@ __global__ void __launch_bounds__(kBT) kb_up(int i, int kh, int rear, const doub
 }
 
 // step = -z, or the no-history step (see k_step)
-__global__ void __launch_bounds__(kBT) kb_step(int kh, int rear, const double* __restrict__ G,
+__global__ void __launch_bounds__(kBT, 4) kb_step(int kh, int rear, const double* __restrict__ G,
                                                const double* __restrict__ Z, double* __restrict__ STEP,
                                                const double* __restrict__ S, BArgs a) {
   BCOL;
@@ -204,14 +261,20 @@ __global__ void __launch_bounds__(kBT) kb_step(int kh, int rear, const double* _
     }
   }
   double v[2] = {0.0, 0.0};
-  if (act) BROWS(r, a.n1) {
-      const i64 e = r * a.k + j;
-      const double z = (kh == 0) ? __dmul_rn(c, G[e]) : __dadd_rn(Z[e], __dmul_rn(Sp[e], f));
-      const double st = -z;
-      STEP[e] = st;
-      v[0] += G[e] * st;
-      v[1] = fmax(v[1], fabs(st));
-    }
+  const int k = a.k;
+  if (act)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1,
+                            [&](i64 r) {
+                              const i64 e = r * k + j;
+                              return kh == 0 ? V3{G[e], 0.0, 0.0} : V3{G[e], Z[e], Sp[e]};
+                            },
+                            [&](i64 r, const V3& x) {
+                              const double z = (kh == 0) ? __dmul_rn(c, x.a) : __dadd_rn(x.b, __dmul_rn(x.c, f));
+                              const double st = -z;
+                              STEP[r * k + j] = st;
+                              v[0] += x.a * st;
+                              v[1] = fmax(v[1], fabs(st));
+                            });
   const bool mx[2] = {false, true};
   col_reduce<2>(v, mx, a, [&](int c2, double* t) {
     ColState& s = a.st[c2];
@@ -222,16 +285,19 @@ __global__ void __launch_bounds__(kBT) kb_step(int kh, int rear, const double* _
 }
 
 // max-scaled step norm, uphill flip, factors of the 10 trials (see k_step_norm)
-__global__ void __launch_bounds__(kBT) kb_step_norm(const double* __restrict__ STEP, BArgs a) {
+__global__ void __launch_bounds__(kBT, 4) kb_step_norm(const double* __restrict__ STEP, BArgs a) {
   BCOL;
   const bool act = on && a.st[j].active;
   const double mxv = act ? a.st[j].smax : 0.0;
   const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
   double v[1] = {0.0};
-  if (act) BROWS(r, a.n1) {
-      const double t = STEP[r * a.k + j] * inv;
-      v[0] += t * t;
-    }
+  const int k = a.k;
+  if (act)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1, [&](i64 r) { return STEP[r * k + j]; },
+                            [&](i64, double x) {
+                              const double t = x * inv;
+                              v[0] += t * t;
+                            });
   const bool mx[1] = {false};
   col_reduce<1>(v, mx, a, [&](int c, double* t) {
     ColState& s = a.st[c];
@@ -249,7 +315,7 @@ __global__ void __launch_bounds__(kBT) kb_step_norm(const double* __restrict__ S
 }
 
 // models still searching: trial model + regulariser (see k_trial)
-__global__ void __launch_bounds__(kBT) kb_trial(int t, const double* __restrict__ W, const double* __restrict__ STEP,
+__global__ void __launch_bounds__(kBT, 4) kb_trial(int t, const double* __restrict__ W, const double* __restrict__ STEP,
                                                 double* __restrict__ NW, float* __restrict__ NWF,
                                                 const double* __restrict__ B0, double* __restrict__ B1, int rtype,
                                                 int eta_one, int no_eta, BArgs a) {
@@ -260,41 +326,49 @@ __global__ void __launch_bounds__(kBT) kb_trial(int t, const double* __restrict_
   const double f = s.factor[t], fl = s.flip, lambda = s.lambda;
   const double eta = eta_one ? 1.0 : f;
   const double scale = fmax(0.0, 1.0 - (lambda * eta));
-  BROWS(r, a.n) {
-    const i64 e = r * a.k + j;
-    double w = __dadd_rn(W[e], __dmul_rn(f, __dmul_rn(STEP[e], fl)));
-    if (rtype == FVG_REG_L2) {
-      w = no_eta ? __dsub_rn(w, __dmul_rn(lambda, w)) : __dmul_rn(scale, w);
-    } else if (rtype == FVG_REG_L1) {
-      const double sg = (double)((w >= 0) - (w < 0));
-      w = __dsub_rn(w, __dmul_rn(lambda, sg));
-    }
-    NW[e] = w;
-    if (NWF) NWF[e] = (float)w;
-  }
+  const int k = a.k;
+  rows_grouped<kRowGroup>(r0, rstep, a.n, [&](i64 r) { const i64 e = r * k + j; return V2{W[e], STEP[e]}; },
+                          [&](i64 r, const V2& x) {
+                            const i64 e = r * k + j;
+                            double w = __dadd_rn(x.a, __dmul_rn(f, __dmul_rn(x.b, fl)));
+                            if (rtype == FVG_REG_L2) {
+                              w = no_eta ? __dsub_rn(w, __dmul_rn(lambda, w)) : __dmul_rn(scale, w);
+                            } else if (rtype == FVG_REG_L1) {
+                              const double sg = (double)((w >= 0) - (w < 0));
+                              w = __dsub_rn(w, __dmul_rn(lambda, sg));
+                            }
+                            NW[e] = w;
+                            if (NWF) NWF[e] = (float)w;
+                          });
   if (r0 == 0) B1[j] = __dadd_rn(B0[j], __dmul_rn(f, s.bstep));
 }
 
-__global__ void __launch_bounds__(kBT) kb_gmax(const double* __restrict__ G, BArgs a) {
+__global__ void __launch_bounds__(kBT, 4) kb_gmax(const double* __restrict__ G, BArgs a) {
   BCOL;
   double v[1] = {0.0};
-  if (on) BROWS(r, a.n1) v[0] = fmax(v[0], fabs(G[r * a.k + j]));
+  const int k = a.k;
+  if (on)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1, [&](i64 r) { return G[r * k + j]; },
+                            [&](i64, double x) { v[0] = fmax(v[0], fabs(x)); });
   const bool mx[1] = {true};
   col_reduce<1>(v, mx, a, [&](int c, double* t) { a.st[c].gmax_t = t[0]; });
 }
 
 // gradient norm and rms; `accepted`: the evaluation is of the accepted
 // model (the initial one, or the re-evaluation after a precision switch)
-__global__ void __launch_bounds__(kBT) kb_gnorm(const double* __restrict__ G, const double* __restrict__ EV,
+__global__ void __launch_bounds__(kBT, 4) kb_gnorm(const double* __restrict__ G, const double* __restrict__ EV,
                                                 int accepted, BArgs a) {
   BCOL;
   const double mxv = on ? a.st[j].gmax_t : 0.0;
   const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
   double v[1] = {0.0};
-  if (on) BROWS(r, a.n1) {
-      const double t = G[r * a.k + j] * inv;
-      v[0] += t * t;
-    }
+  const int k = a.k;
+  if (on)
+    rows_grouped<kRowGroup>(r0, rstep, a.n1, [&](i64 r) { return G[r * k + j]; },
+                            [&](i64, double x) {
+                              const double t = x * inv;
+                              v[0] += t * t;
+                            });
   const bool mx[1] = {false};
   col_reduce<1>(v, mx, a, [&](int c, double* t) {
     ColState& s = a.st[c];
@@ -314,7 +388,7 @@ __global__ void __launch_bounds__(kBT) kb_gnorm(const double* __restrict__ G, co
 // accept decision of trial t (LBFGS_SEARCH_TOL, lbfgs_parallelizer.hpp:
 // 155, 329; the 10th trial is taken whatever its loss); ctl[0] = models
 // still searching
-__global__ void __launch_bounds__(kBT) kb_decide(int t, const double* __restrict__ EV, int k, ColState* st,
+__global__ void __launch_bounds__(kBT, 4) kb_decide(int t, const double* __restrict__ EV, int k, ColState* st,
                                                  int* ctl) {
   __shared__ int cnt[kBT];
   int n = 0;
@@ -337,12 +411,12 @@ __global__ void __launch_bounds__(kBT) kb_decide(int t, const double* __restrict
   if (threadIdx.x == 0) ctl[0] = cnt[0];
 }
 
-__global__ void __launch_bounds__(kBT) kb_begin_search(int k, ColState* st) {
+__global__ void __launch_bounds__(kBT, 4) kb_begin_search(int k, ColState* st) {
   for (int j = threadIdx.x; j < k; j += kBT) st[j].searching = st[j].active;
 }
 
 // accept + history push (see k_accept); convergence: rms <= tol stops the model
-__global__ void __launch_bounds__(kBT) kb_accept(int nf, int it, double tol, double* __restrict__ W,
+__global__ void __launch_bounds__(kBT, 4) kb_accept(int nf, int it, double tol, double* __restrict__ W,
                                                  double* __restrict__ G, const double* __restrict__ NW,
                                                  const double* __restrict__ NG, double* __restrict__ S,
                                                  double* __restrict__ Y, double* __restrict__ B0,
@@ -355,18 +429,26 @@ __global__ void __launch_bounds__(kBT) kb_accept(int nf, int it, double tol, dou
   double* Yn = Y + (i64)nf * plane;
   const double bn = act ? B1[j] : 0.0, bo = act ? B0[j] : 0.0;
   double v[2] = {0.0, 0.0};
-  if (act) BROWS(r, a.n1) {
-      const i64 e = r * a.k + j;
-      const double s = (r < a.n) ? __dsub_rn(NW[e], W[e]) : __dsub_rn(bn, bo);
-      double y = __dsub_rn(NG[e], G[e]);
-      if (fabs(y) < 1e-10) y = 0.0;
-      Sn[e] = s;
-      Yn[e] = y;
-      if (r < a.n) W[e] = NW[e];
-      G[e] = NG[e];
-      v[0] += s * y;
-      v[1] += y * y;
-    }
+  const int k = a.k;
+  const i64 n = a.n;
+  if (act)  // four planes read per row: groups of two rows keep it within 64 registers
+    rows_grouped<2>(r0, rstep, a.n1,
+                    [&](i64 r) {
+                      const i64 e = r * k + j;
+                      return (r < n) ? V4{NW[e], W[e], NG[e], G[e]} : V4{bn, bo, NG[e], G[e]};
+                    },
+                    [&](i64 r, const V4& x) {
+                      const i64 e = r * k + j;
+                      const double s = __dsub_rn(x.a, x.b);
+                      double y = __dsub_rn(x.c, x.d);
+                      if (fabs(y) < 1e-10) y = 0.0;
+                      Sn[e] = s;
+                      Yn[e] = y;
+                      if (r < n) W[e] = x.a;
+                      G[e] = x.c;
+                      v[0] += s * y;
+                      v[1] += y * y;
+                    });
   const bool mx[2] = {false, false};
   col_reduce<2>(v, mx, a, [&](int c, double* t) {
     ColState& s = a.st[c];
@@ -388,7 +470,7 @@ __global__ void __launch_bounds__(kBT) kb_accept(int nf, int it, double tol, dou
 
 // ctl[1] = active models; rms[j] = rms of model j's last gradient, -1 once
 // the model has stopped
-__global__ void __launch_bounds__(kBT) kb_status(int k, const ColState* st, int* ctl, double* rms) {
+__global__ void __launch_bounds__(kBT, 4) kb_status(int k, const ColState* st, int* ctl, double* rms) {
   __shared__ int cnt[kBT];
   int n = 0;
   for (int j = threadIdx.x; j < k; j += kBT) {
@@ -537,7 +619,8 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
   while (kp < kk && kp < kBT) kp <<= 1;
   if (kk > kBT) fail(FVG_ERR_INVALID_ARG, "at most 256 models per batch");
   const int rpb = kBT / kp;
-  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + rpb - 1) / rpb, 6 * (i64)c->num_sms));
+  // one wave: the column kernels are built for 4 CTAs of 256 threads per SM
+  const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + rpb - 1) / rpb, 4 * (i64)c->num_sms));
   part.alloc(sizeof(double) * 2 * (size_t)vgrid * kk + 256, s);
   ctl.alloc(256 + sizeof(double) * kk, s);
   unsigned* ticket = (unsigned*)((char*)part.p + sizeof(double) * 2 * (size_t)vgrid * kk);
