@@ -48,12 +48,68 @@ struct SpmmK {
   double eps;
 };
 
-template <class VT, class XT, class AT, int CPL>
+// Lane layouts of the block's columns.  Strided (VEC = false): lane L owns
+// columns L, L+32, ...; every load is one element.  Packed (VEC = true):
+// lane L owns columns CPL*L .. CPL*L+CPL-1 and reads / writes them with one
+// vector access (needs ldx, the output stride and kb to be multiples of CPL
+// and CPL-aligned bases).  Each column's sum runs over the nonzeros in the
+// same order in both layouts; only the softmax denominator's lane partials
+// group the classes differently.
+template <bool VEC, int CPL> __device__ __forceinline__ int colof(int lane, int q) {
+  return VEC ? lane * CPL + q : lane + 32 * q;
+}
+
+// CPL consecutive elements at an aligned address
+template <class XT, int CPL> struct VecLd;
+template <int CPL> struct VecLd<float, CPL> {
+  static __device__ __forceinline__ void ld(const float* x, float (&o)[CPL]) {
+    if constexpr (CPL == 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(x));
+      o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    } else if constexpr (CPL == 2) {
+      const float2 v = __ldg(reinterpret_cast<const float2*>(x));
+      o[0] = v.x; o[1] = v.y;
+    } else {
+      o[0] = __ldg(x);
+    }
+  }
+};
+template <int CPL> struct VecLd<double, CPL> {
+  static __device__ __forceinline__ void ld(const double* x, double (&o)[CPL]) {
+#pragma unroll
+    for (int h = 0; h < CPL; h += 2) {
+      if constexpr (CPL >= 2) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(x + h));
+        o[h] = v.x; o[h + 1] = v.y;
+      } else {
+        o[0] = __ldg(x);
+      }
+    }
+  }
+};
+
+// CPL consecutive elements stored at an aligned address
+template <class T, int CPL> __device__ __forceinline__ void vec_st(T* y, const T (&v)[CPL]) {
+  if constexpr (sizeof(T) == 4 && CPL == 4) {
+    *reinterpret_cast<float4*>(y) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (sizeof(T) == 4 && CPL == 2) {
+    *reinterpret_cast<float2*>(y) = make_float2(v[0], v[1]);
+  } else if constexpr (sizeof(T) == 8 && CPL >= 2) {
+#pragma unroll
+    for (int h = 0; h < CPL; h += 2) *reinterpret_cast<double2*>(y + h) = make_double2(v[h], v[h + 1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPL; q++) y[q] = v[q];
+  }
+}
+
+template <class VT, class XT, class AT, int CPL, bool VEC>
 __device__ __forceinline__ void row_dot(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[CPL]) {
   const XT* X = (const XT*)p.X;
   const VT* val = (const VT*)p.val;
 #pragma unroll
   for (int q = 0; q < CPL; q++) a[q] = 0;
+  const bool mine = !VEC || lane * CPL < p.kb;
   for (i32 e = e0; e < e1; e += 32) {
     const int cnt = min(32, e1 - e);
     i32 mi = 0;
@@ -66,10 +122,19 @@ __device__ __forceinline__ void row_dot(const SpmmK& p, i32 e0, i32 e1, int lane
     for (int t = 0; t < cnt; t++) {
       const i32 col = __shfl_sync(0xffffffffu, mi, t);
       const AT v = __shfl_sync(0xffffffffu, mv, t);
-      const XT* xr = X + (i64)col * p.ldx + lane;
+      if constexpr (VEC) {
+        if (mine) {
+          XT x[CPL];
+          VecLd<XT, CPL>::ld(X + (i64)col * p.ldx + lane * CPL, x);
 #pragma unroll
-      for (int q = 0; q < CPL; q++)
-        if (lane + 32 * q < p.kb) a[q] += v * (AT)__ldg(xr + 32 * q);
+          for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
+        }
+      } else {
+        const XT* xr = X + (i64)col * p.ldx + lane;
+#pragma unroll
+        for (int q = 0; q < CPL; q++)
+          if (lane + 32 * q < p.kb) a[q] += v * (AT)__ldg(xr + 32 * q);
+      }
     }
   }
 }
@@ -78,15 +143,24 @@ template <class AT> __device__ __forceinline__ AT exp_acc(AT x);
 template <> __device__ __forceinline__ double exp_acc<double>(double x) { return exp(x); }
 template <> __device__ __forceinline__ float exp_acc<float>(float x) { return expf(x); }
 
-template <class AT, class YT, int EPI, int CPL, class S>
+template <class AT, class YT, int EPI, int CPL, bool VEC, class S>
 __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[CPL], const AT (&b)[CPL], int lane,
                                          S (&ls)[CPL], S (&bs)[CPL]) {
-#define ON(q) (lane + 32 * (q) < p.kb)
+#define ON(q) (colof<VEC, CPL>(lane, q) < p.kb)
   if (EPI == EPI_STORE) {
-    YT* y = (YT*)p.Y + (i64)row * p.ldy + lane;
+    YT* y = (YT*)p.Y + (i64)row * p.ldy;
+    if constexpr (VEC) {
+      if (lane * CPL < p.kb) {
+        YT o[CPL];
 #pragma unroll
-    for (int q = 0; q < CPL; q++)
-      if (ON(q)) y[32 * q] = (YT)a[q];
+        for (int q = 0; q < CPL; q++) o[q] = (YT)a[q];
+        vec_st<YT, CPL>(y + lane * CPL, o);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < CPL; q++)
+        if (ON(q)) y[colof<VEC, CPL>(lane, q)] = (YT)a[q];
+    }
     return;
   }
   // softmax without labels: the probability matrix alone (compute_probability_matrix)
@@ -104,15 +178,17 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
       if (has_sw) w = p.sw_f[row];
     }
   }
-  AT* r = (AT*)p.R + (i64)row * p.ldr + lane;
+  AT* r = (AT*)p.R + (i64)row * p.ldr;
+  AT out[CPL];
   if (EPI == EPI_LOGREG) {
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
+      out[q] = 0;
       if (!ON(q)) continue;
       AT loss, d;
       glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
       if (has_sw) d = d * w;
-      r[32 * q] = d;
+      out[q] = d;
       ls[q].add(loss);
       bs[q].add(d);
     }
@@ -136,19 +212,25 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
     const AT inv = (AT)1 / sum;
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
-      if (!ON(q)) continue;
       AT pr = inv * z[q];
       if (has_label) {
-        pr -= (lab == (AT)(lane + 32 * q)) ? (AT)1 : (AT)0;
+        pr -= (lab == (AT)colof<VEC, CPL>(lane, q)) ? (AT)1 : (AT)0;
         if (has_sw) pr *= w;
       }
-      r[32 * q] = pr;
+      out[q] = pr;
     }
+  }
+  if constexpr (VEC) {
+    if (lane * CPL < p.kb) vec_st<AT, CPL>(r + lane * CPL, out);
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPL; q++)
+      if (ON(q)) r[colof<VEC, CPL>(lane, q)] = out[q];
   }
 #undef ON
 }
 
-template <class VT, class XT, class AT, class YT, int EPI, int CPL>
+template <class VT, class XT, class AT, class YT, int EPI, int CPL, bool VEC>
 __global__ void __launch_bounds__(kThreads, 4) k_spmm(const SpmmK p) {
   using Sum = typename SumOf<AT>::type;
   constexpr int NC = 32 * CPL;
@@ -158,21 +240,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm(const SpmmK p) {
   const i64 nw = (i64)gridDim.x * (kThreads / 32);
   AT b[CPL];
 #pragma unroll
-  for (int q = 0; q < CPL; q++)
-    b[q] = (EPI != EPI_STORE && p.icpt && lane + 32 * q < p.kb) ? (AT)p.bias[lane + 32 * q] : (AT)0;
+  for (int q = 0; q < CPL; q++) {
+    const int c = colof<VEC, CPL>(lane, q);
+    b[q] = (EPI != EPI_STORE && p.icpt && c < p.kb) ? (AT)p.bias[c] : (AT)0;
+  }
   Sum ls[CPL], bs[CPL];
   for (i64 it = gw; it < p.nitems; it += nw) {
     const Item item = p.items[it];
     AT a[CPL];
     if (item.r1 < 0) {  // piece of a long row
-      row_dot<VT, XT, AT, CPL>(p, item.e0, item.e1, lane, a);
-      AT* part = (AT*)p.partials + (i64)(-1 - item.r1) * NC + lane;
+      row_dot<VT, XT, AT, CPL, VEC>(p, item.e0, item.e1, lane, a);
+      AT* part = (AT*)p.partials + (i64)(-1 - item.r1) * NC;
 #pragma unroll
-      for (int q = 0; q < CPL; q++) part[32 * q] = a[q];
+      for (int q = 0; q < CPL; q++) part[colof<VEC, CPL>(lane, q)] = a[q];
     } else {
       for (i32 r = item.r0; r < item.r1; r++) {
-        row_dot<VT, XT, AT, CPL>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a);
-        spmm_epi<AT, YT, EPI, CPL>(p, r, a, b, lane, ls, bs);
+        row_dot<VT, XT, AT, CPL, VEC>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a);
+        spmm_epi<AT, YT, EPI, CPL, VEC>(p, r, a, b, lane, ls, bs);
       }
     }
   }
@@ -180,8 +264,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm(const SpmmK p) {
     __shared__ double red[kThreads / 32][NC][2];
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
-      red[wib][lane + 32 * q][0] = ls[q].total();
-      red[wib][lane + 32 * q][1] = bs[q].total();
+      red[wib][colof<VEC, CPL>(lane, q)][0] = ls[q].total();
+      red[wib][colof<VEC, CPL>(lane, q)][1] = bs[q].total();
     }
     __syncthreads();
     if (threadIdx.x < 2 * NC) {
@@ -209,7 +293,7 @@ struct SpmmFin {
 // Long rows (a warp each): add the pieces' partials in piece order, apply the
 // epilogue; then (logistic) the last CTA reduces all loss / bias partials per
 // column in a fixed order.
-template <class AT, class YT, int EPI, int CPL>
+template <class AT, class YT, int EPI, int CPL, bool VEC>
 __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
   using Sum = typename SumOf<AT>::type;
   constexpr int NC = 32 * CPL;
@@ -218,8 +302,10 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
   const int wib = threadIdx.x >> 5;
   AT b[CPL];
 #pragma unroll
-  for (int q = 0; q < CPL; q++)
-    b[q] = (EPI != EPI_STORE && p.icpt && lane + 32 * q < p.kb) ? (AT)p.bias[lane + 32 * q] : (AT)0;
+  for (int q = 0; q < CPL; q++) {
+    const int c = colof<VEC, CPL>(lane, q);
+    b[q] = (EPI != EPI_STORE && p.icpt && c < p.kb) ? (AT)p.bias[c] : (AT)0;
+  }
   Sum ls[CPL], bs[CPL];
   for (i64 i = (i64)blockIdx.x * (kThreads / 32) + wib; i < f.nlong; i += (i64)gridDim.x * (kThreads / 32)) {
     const i64 q0 = f.long_piece0[i], q1 = f.long_piece0[i + 1];
@@ -227,11 +313,11 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 #pragma unroll
     for (int q = 0; q < CPL; q++) a[q] = 0;
     for (i64 pc = q0; pc < q1; pc++) {
-      const AT* part = (const AT*)p.partials + pc * NC + lane;
+      const AT* part = (const AT*)p.partials + pc * NC;
 #pragma unroll
-      for (int q = 0; q < CPL; q++) a[q] += part[32 * q];
+      for (int q = 0; q < CPL; q++) a[q] += part[colof<VEC, CPL>(lane, q)];
     }
-    spmm_epi<AT, YT, EPI, CPL>(p, f.long_rows[i], a, b, lane, ls, bs);
+    spmm_epi<AT, YT, EPI, CPL, VEC>(p, f.long_rows[i], a, b, lane, ls, bs);
   }
   if constexpr (EPI == EPI_LOGREG) {
     __shared__ double red[kThreads / 32][NC][2];
@@ -239,8 +325,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
     __shared__ bool last;
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
-      red[wib][lane + 32 * q][0] = ls[q].total();
-      red[wib][lane + 32 * q][1] = bs[q].total();
+      red[wib][colof<VEC, CPL>(lane, q)][0] = ls[q].total();
+      red[wib][colof<VEC, CPL>(lane, q)][1] = bs[q].total();
     }
     __syncthreads();
     if (threadIdx.x < 2 * NC) {
@@ -284,12 +370,12 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 // ------------------------------------------------------------ host side
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-template <class VT, class XT, class AT, class YT, int EPI, int CPL>
+template <class VT, class XT, class AT, class YT, int EPI, int CPL, bool VEC>
 static int spmm_grid(fvg_ctx* c) {
   static int blocks = -1;
   if (blocks < 0) {
     int nb = 0;
-    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spmm<VT, XT, AT, YT, EPI, CPL>, kThreads, 0));
+    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spmm<VT, XT, AT, YT, EPI, CPL, VEC>, kThreads, 0));
     blocks = std::max(1, nb);
   }
   return blocks * c->num_sms;
@@ -310,11 +396,11 @@ i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage) {
                al256(at * kSpmmMaxCols * std::max<i64>(s.npieces, 1)));
 }
 
-template <class VT, class XT, class AT, class YT, int EPI, int CPL>
-static void launch_spmm(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, SpmmK p, double* out, double* gbias,
-                        char* scratch) {
+template <class VT, class XT, class AT, class YT, int EPI, int CPL, bool VEC>
+static void launch_spmm_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, SpmmK p, double* out, double* gbias,
+                          char* scratch) {
   const int grid =
-      (int)std::max<i64>(1, std::min<i64>(spmm_grid<VT, XT, AT, YT, EPI, CPL>(c), (s.nitems + 7) / 8));
+      (int)std::max<i64>(1, std::min<i64>(spmm_grid<VT, XT, AT, YT, EPI, CPL, VEC>(c), (s.nitems + 7) / 8));
   const int fg = spmm_fin_grid(c, s.nlong);
   unsigned* ticket = (unsigned*)scratch;
   double* cta = (double*)(scratch + al256(256));
@@ -327,7 +413,7 @@ static void launch_spmm(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, Spmm
   p.nitems = s.nitems;
   p.cta_part = cta;
   if (s.nitems > 0) {
-    k_spmm<VT, XT, AT, YT, EPI, CPL><<<grid, kThreads, 0, c->stream>>>(p);
+    k_spmm<VT, XT, AT, YT, EPI, CPL, VEC><<<grid, kThreads, 0, c->stream>>>(p);
     check_launch("k_spmm");
     count_launch(c);
   }
@@ -342,10 +428,30 @@ static void launch_spmm(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, Spmm
     f.out = out;
     f.gbias = gbias;
     f.ticket = ticket;
-    k_spmm_fin<AT, YT, EPI, CPL><<<fg, kThreads, 0, c->stream>>>(f);
+    k_spmm_fin<AT, YT, EPI, CPL, VEC><<<fg, kThreads, 0, c->stream>>>(f);
     check_launch("k_spmm_fin");
     count_launch(c);
   }
+}
+
+static bool aligned_to(const void* ptr, size_t b) { return ((uintptr_t)ptr % b) == 0; }
+
+// Packed lane layout when every access it makes is aligned: the block's
+// width and the strides of X and of the output are multiples of CPL and the
+// bases are aligned to CPL elements.
+template <class VT, class XT, class AT, class YT, int EPI, int CPL>
+static void launch_spmm(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, SpmmK p, double* out, double* gbias,
+                        char* scratch) {
+  bool vec = CPL >= 2 && p.kb % CPL == 0 && p.ldx % CPL == 0 && aligned_to(p.X, CPL * sizeof(XT));
+  if (EPI == EPI_STORE) vec = vec && p.ldy % CPL == 0 && aligned_to(p.Y, CPL * sizeof(YT));
+  else vec = vec && p.ldr % CPL == 0 && aligned_to(p.R, CPL * sizeof(AT));
+  if constexpr (CPL >= 2) {
+    if (vec) {
+      launch_spmm_l<VT, XT, AT, YT, EPI, CPL, true>(c, a, s, storage, p, out, gbias, scratch);
+      return;
+    }
+  }
+  launch_spmm_l<VT, XT, AT, YT, EPI, CPL, false>(c, a, s, storage, p, out, gbias, scratch);
 }
 
 template <class VT, class XT, class AT, class YT>
