@@ -279,22 +279,41 @@ def run_gpu(args):
     h2d = (m + 1) * 4 + nnz * 12 + m * 8 + n * 8
     d2h = n * 8 + 16
     torch.cuda.synchronize()
-    phases = {"upload_s": 0.0, "train_s": 0.0}  # train includes the transposed build
+    # upload: host CRS -> device (validated) + the benchmark's value plane;
+    # prepare: transposed copy (device sort) and its plane; train: the call
+    # (work-item schedules, the FP32 planes at the refinement switch, 50
+    # iterations, read-back)
+    phases = {"upload_s": 0.0, "prepare_s": 0.0, "train_s": 0.0}
+    # the step's inputs come from pinned host memory (a loader's staging
+    # buffers), allocated and filled once before the timed steps
+    pinned = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (off, idx, val, label)] \
+        if args.e2e_steps else []
+    p_off, p_idx, p_val, p_label = (t.numpy() for t in pinned) if pinned else (off, idx, val, label)
+    ctx.reset_profile()
+    ctx.set_profiling(True)  # device time of the transposed build inside `prepare`
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
-        B = ctx.matrix(m, n, off, idx, val)
+        B = ctx.matrix(m, n, p_off, p_idx, p_val)
         if args.storage != "f64":
             B.add_storage(args.storage)
         ctx.synchronize()
         t1 = time.perf_counter()
-        rr = fv.logreg_lbfgs(B, label, **kw)
-        B.close()
+        B.prepare("CRS", transpose=True)
+        if args.storage != "f64":
+            B.add_storage(args.storage)
         ctx.synchronize()
         t2 = time.perf_counter()
+        rr = fv.logreg_lbfgs(B, p_label, **kw)
+        B.close()
+        ctx.synchronize()
+        t3 = time.perf_counter()
         phases["upload_s"] += t1 - t0
-        phases["train_s"] += t2 - t1
-        e2e_ms += (t2 - t0) * 1e3
+        phases["prepare_s"] += t2 - t1
+        phases["train_s"] += t3 - t2
+        e2e_ms += (t3 - t0) * 1e3
         e2e_iters += rr["n_iter"]
+    ctx.set_profiling(False)
+    phases["transpose_device_s"] = ctx.profile("transpose")[0] / 1e3
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
@@ -332,6 +351,7 @@ def run_gpu(args):
                                     "gbs": alg[k] * prof[k][1] / max(prof[k][0], 1e-9) / 1e6}
                                 for k in prof if prof[k][1]}},
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "host_memory": "pinned",
                 "phases": {k: v / max(args.e2e_steps, 1) for k, v in phases.items()}},
         "gpu_launches": launches,
         "clocks": ck,

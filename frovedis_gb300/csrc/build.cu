@@ -3,6 +3,8 @@
 // ELL / JDS / JDS-CRS-hybrid layouts (ell_matrix.hpp:63-95,
 // jds_matrix.hpp:81-146, jds_crs_hybrid.hpp:38-153).
 #include <algorithm>
+#include <thread>
+#include <vector>
 
 #include "fvg_internal.cuh"
 
@@ -38,16 +40,27 @@ void ensure_plane_generic(fvg_ctx* c, DBuf* planes, i64 n, int dt, int master) {
 void crs_ensure_plane(fvg_ctx* c, DevCRS& a, int dt, int master) { ensure_plane_generic(c, a.val, a.nnz, dt, master); }
 
 // ------------------------------------------------------------------ upload
+// Counts and the longest row are combined per warp first: one atomic per
+// warp instead of one per row on a single address.
 __global__ void k_check_crs(const i32* __restrict__ off, const i32* __restrict__ idx, i64 m, i64 n, i64 nnz,
                             unsigned long long* __restrict__ flags /* [0]=bad off, [1]=bad idx, [2]=max len */) {
+  unsigned bad_off = 0, bad_idx = 0, mx = 0;
   GRID_STRIDE(r, m) {
     i32 s = off[r], e = off[r + 1];
-    if (e < s || s < 0 || e > nnz) atomicAdd(&flags[0], 1ull);
-    else atomicMax(&flags[2], (unsigned long long)(e - s));
+    if (e < s || s < 0 || e > nnz) bad_off++;
+    else mx = max(mx, (unsigned)(e - s));
   }
   GRID_STRIDE(p, nnz) {
     i32 c = idx[p];
-    if (c < 0 || c >= n) atomicAdd(&flags[1], 1ull);
+    if (c < 0 || c >= n) bad_idx++;
+  }
+  bad_off = __reduce_add_sync(0xffffffffu, bad_off);
+  bad_idx = __reduce_add_sync(0xffffffffu, bad_idx);
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if ((threadIdx.x & 31) == 0) {
+    if (bad_off) atomicAdd(&flags[0], (unsigned long long)bad_off);
+    if (bad_idx) atomicAdd(&flags[1], (unsigned long long)bad_idx);
+    if (mx) atomicMax(&flags[2], (unsigned long long)mx);
   }
 }
 
@@ -95,7 +108,10 @@ void crs_upload(fvg_ctx* c, DevCRS& a, i64 m, i64 n, const i32* off, const i32* 
 }
 
 __global__ void k_max_row(const i32* __restrict__ off, i64 m, unsigned long long* __restrict__ mx) {
-  GRID_STRIDE(r, m) atomicMax(mx, (unsigned long long)(off[r + 1] - off[r]));
+  unsigned v = 0;
+  GRID_STRIDE(r, m) v = max(v, (unsigned)(off[r + 1] - off[r]));
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(mx, (unsigned long long)v);
 }
 
 static i64 max_row_len(fvg_ctx* c, const i32* off, i64 m) {
@@ -124,20 +140,25 @@ __global__ void k_boundaries(const uint32_t* __restrict__ keys, i64 nnz, i64 nco
   }
 }
 
-// row of element e = last r with off[r] <= e (empty rows skipped)
-__device__ __forceinline__ i32 row_of(const i32* __restrict__ off, i64 m, i64 e) {
-  i64 lo = 0, hi = m;  // off[lo] <= e < off[hi] invariant (off[m] = nnz > e)
-  while (hi - lo > 1) {
-    i64 mid = (lo + hi) >> 1;
-    if (off[mid] <= e) lo = mid;
-    else hi = mid;
-  }
-  return (i32)lo;
+// Row id of every nonzero: a warp per row, lanes write consecutive entries.
+__global__ void k_expand_rows(const i32* __restrict__ off, i64 m, uint32_t* __restrict__ rowid) {
+  const int lane = threadIdx.x & 31;
+  const i64 w = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
+  for (i64 r = w; r < m; r += nw)
+    for (i64 e = (i64)off[r] + lane; e < off[r + 1]; e += 32) rowid[e] = (uint32_t)r;
 }
 
-__global__ void k_trans_rows(const uint32_t* __restrict__ src, const i32* __restrict__ off, i64 m, i64 nnz,
-                             i32* __restrict__ tidx) {
-  GRID_STRIDE(p, nnz) tidx[p] = row_of(off, m, (i64)src[p]);
+// Transposed entry p comes from source position src[p]: its column id in
+// the transpose is the source row, its value the source value.
+template <class T>
+__global__ void k_trans_fill(const uint32_t* __restrict__ src, const uint32_t* __restrict__ rowid,
+                             const T* __restrict__ val, i64 nnz, i32* __restrict__ tidx, T* __restrict__ tval) {
+  GRID_STRIDE(p, nnz) {
+    const uint32_t q = src[p];
+    tidx[p] = (i32)rowid[q];
+    tval[p] = val[q];
+  }
 }
 
 void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
@@ -164,11 +185,21 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
   // stable by element position == stable in source-row order
   radix_sort_pairs(c, keys.as<uint32_t>(), src.as<uint32_t>(), a.nnz, bits_for(a.n - 1));
   k_boundaries<<<grid_n(a.nnz + 1), 256, 0, c->stream>>>(keys.as<uint32_t>(), a.nnz, a.n, t.off.as<i32>());
-  k_trans_rows<<<grid_n(a.nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), a.off.as<i32>(), a.m, a.nnz,
-                                                      t.idx.as<i32>());
+  // the sorted column ids are done with: their buffer takes the row ids
+  uint32_t* rowid = keys.as<uint32_t>();
+  k_expand_rows<<<grid_n(32 * a.m), 256, 0, c->stream>>>(a.off.as<i32>(), a.m, rowid);
+  const unsigned g = grid_n(a.nnz);
+  if (master == FVG_F64)
+    k_trans_fill<double><<<g, 256, 0, c->stream>>>(src.as<uint32_t>(), rowid, a.val[master].as<double>(), a.nnz,
+                                                   t.idx.as<i32>(), t.val[master].as<double>());
+  else if (master == FVG_F32)
+    k_trans_fill<float><<<g, 256, 0, c->stream>>>(src.as<uint32_t>(), rowid, a.val[master].as<float>(), a.nnz,
+                                                  t.idx.as<i32>(), t.val[master].as<float>());
+  else
+    k_trans_fill<bf16><<<g, 256, 0, c->stream>>>(src.as<uint32_t>(), rowid, a.val[master].as<bf16>(), a.nnz,
+                                                 t.idx.as<i32>(), t.val[master].as<bf16>());
   check_launch("transpose");
-  count_launch(c, 2);
-  gather_values(c, a.val[master].p, src.as<uint32_t>(), t.val[master].p, master, a.nnz);
+  count_launch(c, 3);
   t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
 }
 
@@ -176,30 +207,33 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 // Packs rows, in row order, into work items (see Sched): consecutive short
 // rows share a row tile while the tile stays within `tile` nonzeros and
 // kTileRows rows; a long row becomes its own pieces of at most `tile`
-// nonzeros, cut at 8-element boundaries.  Done once per matrix on the host.
-const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
-  const int slot = 0;
-  if (a.sched[slot]) return *a.sched[slot];
-  const i64 kLongRow = tile;
-  auto s = std::make_unique<Sched>();
-  s->tile = tile;
-  const i64 m = a.m;
-  std::vector<i32> off(m + 1);
-  FVG_CUDA(cudaMemcpyAsync(off.data(), a.off.p, sizeof(i32) * (m + 1), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));
+// nonzeros, cut at 8-element boundaries.  Built on the host once per
+// matrix.  The greedy packing is sequential; to spread it over host threads
+// every chunk of 65,536 rows is first packed as if a tile started at its
+// first row, then the chunks are stitched in order: the packing carried over
+// from the previous chunk is continued row by row until it starts a tile at
+// a row where the chunk's own packing also starts one — from there both are
+// in the same state and the chunk's items are taken as they are.  The result
+// is the sequential packing exactly.
+namespace {
+constexpr i64 kSchedChunk = 1 << 16;
+struct Packer {
+  const i32* off;
+  int tile;
   std::vector<Item> items;
   std::vector<i32> lrows, lpiece0;
   i64 npieces = 0;
   i64 t0 = 0, tnnz = 0, tmax = 0;  // open tile: rows [t0, r), tnnz nonzeros, longest row tmax
-  auto flush = [&](i64 r) {
+  void flush(i64 r) {
     if (r > t0) items.push_back(Item{(int32_t)t0, (int32_t)r, off[t0], off[r]});
     t0 = r;
     tnnz = 0;
     tmax = 0;
-  };
-  for (i64 r = 0; r < m; r++) {
+  }
+  // one row; returns true when a tile (or a long row's pieces) starts at r
+  bool row(i64 r) {
     const i64 len = (i64)off[r + 1] - off[r];
-    if (len > kLongRow) {
+    if (len > tile) {
       flush(r);
       const i64 st = off[r], en = off[r + 1], base = st & ~7ll;
       lrows.push_back((i32)r);
@@ -211,18 +245,116 @@ const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
         npieces++;
       }
       t0 = r + 1;
-      continue;
+      return true;
     }
     // close the tile when this row would overflow it, or make one lane sum
     // more than kLaneWork products of a row (balance inside the warp)
+    bool starts = (r == t0);
     if (r > t0) {
       const i64 R = r - t0 + 1, mx = std::max(tmax, len);
-      if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) flush(r);
+      if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) {
+        flush(r);
+        starts = true;
+      }
     }
     tnnz += len;
     tmax = std::max(tmax, len);
+    return starts;
   }
-  flush(m);
+};
+}  // namespace
+
+const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
+  const int slot = 0;
+  if (a.sched[slot]) return *a.sched[slot];
+  auto s = std::make_unique<Sched>();
+  s->tile = tile;
+  const i64 m = a.m;
+  std::vector<i32> off(m + 1);
+  FVG_CUDA(cudaMemcpyAsync(off.data(), a.off.p, sizeof(i32) * (m + 1), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  const i64 nchunks = std::max<i64>(1, (m + kSchedChunk - 1) / kSchedChunk);
+  // each chunk packed as if a tile started at its first row
+  std::vector<Packer> spec((size_t)nchunks);
+  std::vector<std::vector<i64>> starts((size_t)nchunks);  // rows where spec starts a tile
+  {
+    const int nt = (int)std::max<i64>(1, std::min<i64>(nchunks, std::max(1u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, t]() {
+        for (i64 k = t; k < nchunks; k += nt) {
+          Packer& P = spec[(size_t)k];
+          P.off = off.data();
+          P.tile = tile;
+          const i64 r0 = k * kSchedChunk, r1 = std::min(m, (k + 1) * kSchedChunk);
+          P.t0 = r0;
+          for (i64 r = r0; r < r1; r++)
+            if (P.row(r)) starts[(size_t)k].push_back(r);
+        }
+      });
+    for (auto& x : th) x.join();
+  }
+  // stitch in chunk order
+  Packer G;
+  G.off = off.data();
+  G.tile = tile;
+  for (i64 k = 0; k < nchunks; k++) {
+    Packer& P = spec[(size_t)k];
+    const std::vector<i64>& st = starts[(size_t)k];
+    const i64 r0 = k * kSchedChunk, r1 = std::min(m, (k + 1) * kSchedChunk);
+    i64 sync = -1;
+    if (k == 0) {
+      sync = r0;  // the chunk's packing is the sequential one
+    } else {
+      for (i64 r = r0; r < r1; r++) {
+        const bool g_starts = G.row(r);
+        if (g_starts && std::binary_search(st.begin(), st.end(), r)) {
+          sync = r;
+          break;
+        }
+      }
+    }
+    if (sync < 0) continue;  // carried through the whole chunk: G holds it
+    // G has just started a tile (or long row) at `sync` exactly as P did:
+    // drop G's copy of that row and take P's items from it on
+    size_t gi = G.items.size();
+    while (gi > 0 && G.items[gi - 1].r0 == (int32_t)sync) gi--;
+    if (k > 0) {
+      // pieces G numbered for the row at `sync` are re-taken from P below
+      for (size_t q = gi; q < G.items.size(); q++)
+        if (G.items[q].r1 < 0) G.npieces--;
+      if (!G.lrows.empty() && G.lrows.back() == (i32)sync) {
+        G.lrows.pop_back();
+        G.lpiece0.pop_back();
+      }
+      G.items.resize(gi);
+    }
+    size_t pi = 0;
+    while (pi < P.items.size() && P.items[pi].r0 < (int32_t)sync) pi++;
+    i64 p_first = 0;  // P's pieces before `sync`
+    for (size_t q = 0; q < pi; q++)
+      if (P.items[q].r1 < 0) p_first++;
+    const i64 shift = G.npieces - p_first;
+    for (size_t q = pi; q < P.items.size(); q++) {
+      Item it = P.items[q];
+      if (it.r1 < 0) it.r1 = (int32_t)(-1 - ((-1 - (i64)it.r1) + shift));
+      G.items.push_back(it);
+    }
+    for (size_t q = 0; q < P.lrows.size(); q++)
+      if (P.lrows[q] >= (i32)sync) {
+        G.lrows.push_back(P.lrows[q]);
+        G.lpiece0.push_back((i32)(P.lpiece0[q] + shift));
+      }
+    G.npieces = P.npieces + shift;
+    G.t0 = P.t0;
+    G.tnnz = P.tnnz;
+    G.tmax = P.tmax;
+  }
+  G.flush(m);
+  std::vector<Item>& items = G.items;
+  std::vector<i32>& lrows = G.lrows;
+  std::vector<i32>& lpiece0 = G.lpiece0;
+  const i64 npieces = G.npieces;
   lpiece0.push_back((i32)npieces);
   s->nitems = (i64)items.size();
   s->nlong = (i64)lrows.size();

@@ -360,8 +360,15 @@ __global__ void k_col_range(const int64_t* __restrict__ col, i64 ne, long long* 
     a = min(a, (long long)col[i]);
     b = max(b, (long long)col[i]);
   }
-  atomicMin(mn, a);
-  atomicMax(mx, b);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {  // one atomic per warp
+    a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mn, a);
+    atomicMax(mx, b);
+  }
 }
 __global__ void k_col_narrow(const int64_t* __restrict__ col, i64 ne, long long shift, i32* __restrict__ out) {
   for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += (i64)gridDim.x * blockDim.x)

@@ -233,10 +233,33 @@ __global__ void k_rs_upsweep(const uint32_t* __restrict__ keys, i64 n, int shift
   hist[(i64)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
+// Exclusive scan of 256 ints in shared memory by a 256-thread CTA.
+__device__ __forceinline__ void scan256_exclusive(int* v) {
+  __shared__ int wsum[kRsWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int x = v[threadIdx.x];
+  int inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  int before = 0;
+  for (int q = 0; q < w; q++) before += wsum[q];
+  v[threadIdx.x] = before + inc - x;
+}
+
+// Downsweep: ranks as above, then the tile is sorted by digit in shared
+// memory (digit-major, input order within a digit) and written back in that
+// order, so consecutive threads store consecutive positions of a digit's run.
 __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, i64 n, int shift,
                                i64 nblocks, const i64* __restrict__ goff) {
   __shared__ int wcnt[kRsWarps][256];
+  __shared__ int dstart[256];
+  __shared__ uint32_t skey[kRsTile], sval[kRsTile];
   for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -260,22 +283,35 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
     rank[r] = ok ? cur + before : -1;
   }
   __syncthreads();
-  {  // exclusive prefix over warps for digit = threadIdx.x
+  {  // exclusive prefix over warps for digit = threadIdx.x; the digit's tile total
     int d = threadIdx.x, acc = 0;
     for (int q = 0; q < kRsWarps; q++) {
       int t = wcnt[q][d];
       wcnt[q][d] = acc;
       acc += t;
     }
+    dstart[d] = acc;
   }
+  __syncthreads();
+  scan256_exclusive(dstart);  // first tile slot of each digit
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
     if (rank[r] < 0) continue;
-    int d = (int)((key[r] >> shift) & 255u);
-    i64 pos = goff[(i64)d * nblocks + blockIdx.x] + wcnt[w][d] + rank[r];
-    kout[pos] = key[r];
-    vout[pos] = val[r];
+    const int d = (int)((key[r] >> shift) & 255u);
+    const int lp = dstart[d] + wcnt[w][d] + rank[r];
+    skey[lp] = key[r];
+    sval[lp] = val[r];
+  }
+  __syncthreads();
+  const i64 t0 = (i64)blockIdx.x * kRsTile;
+  const int cnt = (int)(n - t0 < kRsTile ? n - t0 : kRsTile);
+  for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
+    const uint32_t k = skey[i];
+    const int d = (int)((k >> shift) & 255u);
+    const i64 pos = goff[(i64)d * nblocks + blockIdx.x] + (i - dstart[d]);
+    kout[pos] = k;
+    vout[pos] = sval[i];
   }
 }
 
