@@ -82,6 +82,11 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
   constexpr int SPAN = kWarpTile;        // products slice per warp
   constexpr int NR = SPAN / 32;          // element rounds per lane
   constexpr int RG = sizeof(VT) == 8 ? (FVG_CRS_ROUNDS + 1) / 2 : FVG_CRS_ROUNDS;  // rounds in flight together
+  // FP64: GB300 issues FP64 at a small fraction of the FP32 rate, so phase 1
+  // only gathers x and phase 2 does one fused multiply-add per nonzero
+  // (instead of a multiply here and an add there) with the value re-read
+  // (the warp streamed it just before: L1/L2)
+  constexpr bool kFmaRows = sizeof(AT) == 8;
   __shared__ AT sprod[kThreads / 32][SPAN];
   __shared__ int soffs[kThreads / 32][kTileRows + 1];
   using Sum = typename SumOf<AT>::type;
@@ -116,13 +121,16 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
         const int k = (g + q) * 32 + lane;
         if (g + q < NR && k < span) {
           c[q] = __ldcs(p.idx + a0 + k);
-          v[q] = ld_val<VT, AT>(val + a0 + k);
+          if constexpr (!kFmaRows) v[q] = ld_val<VT, AT>(val + a0 + k);
         }
       }
 #pragma unroll
       for (int q = 0; q < RG; q++) {
         const int k = (g + q) * 32 + lane;
-        if (g + q < NR && k < span) prod[k] = v[q] * (AT)__ldg(x + c[q]);
+        if (g + q < NR && k < span) {
+          if constexpr (kFmaRows) prod[k] = (AT)__ldg(x + c[q]);  // the value joins in phase 2
+          else prod[k] = v[q] * (AT)__ldg(x + c[q]);
+        }
       }
     }
     __syncwarp();
@@ -138,23 +146,44 @@ __global__ void __launch_bounds__(kThreads, FVG_CRS_MIN_BLOCKS) k_crs(const CrsK
         AT acc = 0;
         if (j < R) {
           const int s = soff[j] - a0, e = soff[j + 1] - a0;
-          AT a1 = 0, a2 = 0, a3 = 0;
           int k = s + sub;
-          for (; k + 3 * Gl < e; k += 4 * Gl) {
-            acc += prod[k];
-            a1 += prod[k + Gl];
-            a2 += prod[k + 2 * Gl];
-            a3 += prod[k + 3 * Gl];
+          if constexpr (kFmaRows) {
+            const VT* vr = val + a0;
+            if (e - s > 4 * Gl) {
+              AT a1 = 0, a2 = 0, a3 = 0;
+              for (; k + 3 * Gl < e; k += 4 * Gl) {
+                acc = fma((AT)vr[k], prod[k], acc);
+                a1 = fma((AT)vr[k + Gl], prod[k + Gl], a1);
+                a2 = fma((AT)vr[k + 2 * Gl], prod[k + 2 * Gl], a2);
+                a3 = fma((AT)vr[k + 3 * Gl], prod[k + 3 * Gl], a3);
+              }
+              for (; k < e; k += Gl) acc = fma((AT)vr[k], prod[k], acc);
+              acc = (acc + a1) + (a2 + a3);
+            } else {
+              for (; k < e; k += Gl) acc = fma((AT)vr[k], prod[k], acc);
+            }
+          } else {
+            AT a1 = 0, a2 = 0, a3 = 0;
+            for (; k + 3 * Gl < e; k += 4 * Gl) {
+              acc += prod[k];
+              a1 += prod[k + Gl];
+              a2 += prod[k + 2 * Gl];
+              a3 += prod[k + 3 * Gl];
+            }
+            for (; k < e; k += Gl) acc += prod[k];
+            acc = (acc + a1) + (a2 + a3);
           }
-          for (; k < e; k += Gl) acc += prod[k];
-          acc = (acc + a1) + (a2 + a3);
         }
         for (int o = Gl >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (j < R && sub == 0) epilogue<AT, YT, EPI>(p, it.r0 + j, acc, bias, ls, bs);
       }
     } else {
       AT acc = 0;
-      for (int k = it.e0 - a0 + lane; k < span; k += 32) acc += prod[k];
+      if constexpr (kFmaRows) {
+        for (int k = it.e0 - a0 + lane; k < span; k += 32) acc = fma((AT)val[a0 + k], prod[k], acc);
+      } else {
+        for (int k = it.e0 - a0 + lane; k < span; k += 32) acc += prod[k];
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       if (lane == 0) ((AT*)p.partials)[-1 - it.r1] = acc;
@@ -195,12 +224,16 @@ struct FinK {
 template <class AT, class YT, int EPI>
 __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
   const AT b = (EPI == EPI_LOGREG && f.icpt) ? (AT)*f.intercept : (AT)0;
-  for (i64 i = blockIdx.x; i < f.nlong; i += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  // a warp per long row: lane L adds pieces L, L+32, ..., then the warp's tree
+  for (i64 i = (i64)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); i < f.nlong;
+       i += (i64)gridDim.x * (kThreads / 32)) {
     i64 c0 = f.long_piece0[i], c1 = f.long_piece0[i + 1];
     AT acc = 0;
-    for (i64 j = c0 + threadIdx.x; j < c1; j += kThreads) acc += ((const AT*)f.partials)[j];
-    acc = block_sum256(acc);
-    if (threadIdx.x == 0) {
+    for (i64 j = c0 + lane; j < c1; j += 32) acc += ((const AT*)f.partials)[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
       i32 row = f.long_rows[i];
       if (EPI == EPI_STORE) {
         ((YT*)f.y)[row] = (YT)acc;
@@ -347,7 +380,7 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
     f.ticket = ps.ticket;
     f.loss = p.loss;
     f.eps = p.eps;
-    int fg = (int)std::max<i64>(1, std::min<i64>(s.nlong, 4 * c->num_sms));
+    int fg = (int)std::max<i64>(1, std::min<i64>((s.nlong + 7) / 8, 4 * c->num_sms));  // a warp per long row
     ProfScope pf(c, timed ? P_FINALIZE : P_NKEYS);
     k_finalize<AT, YT, EPI><<<fg, kThreads, 0, c->stream>>>(f);
     check_launch("k_finalize");
