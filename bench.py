@@ -147,6 +147,17 @@ def eval_bytes(m, n, nnz, s_v, s_x):
     return p1, p2
 
 
+def set_panels(A, spec):
+    """--panels: "auto" (the library's choice), "off", or ROWS[:MIN_PER_PANEL]."""
+    if spec == "auto":
+        return
+    if spec == "off":
+        A.set_panels(0)
+        return
+    rows, _, mpp = spec.partition(":")
+    A.set_panels(int(rows), float(mpp) if mpp else 0.0)
+
+
 def run_gpu(args):
     import torch
 
@@ -159,9 +170,11 @@ def run_gpu(args):
     ctx = fv.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     A = ctx.matrix(m, n, off, idx, val)
+    set_panels(A, args.panels)
     A.prepare("CRS", transpose=True)
     A.add_storage("bf16")
     A.add_storage("f32")
+    panel_info = A.panel_info()
     # initModel overload with zero weights: the default all-ones start makes
     # the reference's L-BFGS exhaust its line search and blow up on this data
     kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, storage=args.storage, w0=np.zeros(n))
@@ -294,6 +307,7 @@ def run_gpu(args):
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         B = ctx.matrix(m, n, p_off, p_idx, p_val)
+        set_panels(B, args.panels)
         if args.storage != "f64":
             B.add_storage(args.storage)
         ctx.synchronize()
@@ -336,7 +350,9 @@ def run_gpu(args):
         "config": {"workload": "logreg-lbfgs-10Mx1M-nnz6e8", "rows": m, "cols": n, "nnz": nnz,
                    "iterations_per_step": args.iters, "lambda": 1e-4, "format": "CRS",
                    "storage": args.storage, "l2_flush": "inputs larger than L2 (A is %.1f GB)" % (
-                       nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU"},
+                       nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU",
+                   "backward_panels": {"rows": panel_info[0], "panels": panel_info[1], "hot_columns": panel_info[2],
+                                       "hot_entries": panel_info[3]}},
         "final_loss": r["loss"], "iterations_per_run": r["n_iter"],
         # loss/gradient evaluations (one pass 1 each; line-search trials included)
         "evaluations_per_s": (prof["pass1"][1] + prof["pass1_f32"][1]) * world / (ms / 1e3),
@@ -674,6 +690,8 @@ def main():
     ap.add_argument("--regpath-datasets", type=int, default=4, help="datasets of the batched summary line")
     ap.add_argument("--skip-regpath", action="store_true")
     ap.add_argument("--skip-glm", action="store_true", help="skip the ridge / SVM summary")
+    ap.add_argument("--panels", default="auto",
+                    help='row-panel backward product: "auto", "off" or ROWS[:MIN_PER_PANEL]')
     args = ap.parse_args()
     if args.workload == "regpath":
         if args.iters == 50:

@@ -297,6 +297,39 @@ FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* c, fvg_matrix* M, fvg_format fmt,
   API_BEGIN
   own(c, M);
   prepare(c, M, fmt, with_transpose != 0);
+  // a matrix that already holds FP32 / BF16 values gets its row-panel
+  // backward layout now rather than at the first product
+  if (with_transpose && (fmt == FVG_CRS || fmt == FVG_ELL) && (M->A.val[FVG_F32].p || M->A.val[FVG_BF16].p)) {
+    DevPanels* pt = panels_for(c, M);
+    for (int dt : {FVG_F32, FVG_BF16})
+      if (pt && M->A.val[dt].p) panel_ensure_plane(c, *pt, dt);
+  }
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_set_panels(fvg_ctx* c, fvg_matrix* M, int64_t rows, double min_per_panel) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  need(rows < 0 || rows == 0 || rows % 4 == 0, FVG_ERR_INVALID_ARG, "panel rows must be a multiple of 4");
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  M->pan.reset();
+  M->pan_tried = false;
+  M->panel_rows = rows < 0 ? -1 : rows;
+  M->panel_min = min_per_panel;
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_panel_info(fvg_ctx* c, fvg_matrix* M, int64_t* info) {
+  if (!c || !M || !info) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  DevPanels* pt = panels_for(c, M);
+  info[0] = pt ? pt->rows : 0;
+  info[1] = pt ? pt->npanels : 0;
+  info[2] = pt ? pt->nhot : 0;
+  info[3] = pt ? pt->E : 0;
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
 }
@@ -349,6 +382,13 @@ FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* M) {
   if (M->tjds) b += jds_bytes(*M->tjds);
   for (const DevHYB* h : {M->hyb.get(), M->thyb.get()})
     if (h) b += jds_bytes(h->jds) + crs_bytes(h->crs);
+  if (const DevPanels* p = M->pan.get()) {
+    b += crs_bytes(p->cold);
+    for (const DBuf* d : {&p->hot_cols, &p->poff, &p->prow, &p->items, &p->pitem0, &p->long_rows, &p->plong0,
+                          &p->long_piece0, &p->ypan, &p->partials})
+      b += (int64_t)d->bytes;
+    for (auto& v : p->val) b += (int64_t)v.bytes;
+  }
   return b;
 }
 
@@ -561,7 +601,10 @@ static void run_product(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, int vec
     else if (fmt == FVG_JDS) jds_spmv(c, *M->jds, storage, v.kdt, v.dx, out_dt, v.dy, false);
     else hyb_spmv(c, *M->hyb, storage, v.kdt, v.dx, out_dt, v.dy);
   } else {
-    if (fmt == FVG_CRS || fmt == FVG_ELL)
+    DevPanels* pt = (storage != FVG_F64 && (fmt == FVG_CRS || fmt == FVG_ELL)) ? panels_for(c, M) : nullptr;
+    if (pt)
+      panel_trans_mv(c, *pt, storage, (const float*)v.dx, out_dt, v.dy, nullptr, P_SPMV_CRS);
+    else if (fmt == FVG_CRS || fmt == FVG_ELL)
       crs_pass(c, *M->AT, storage, v.kdt, v.dx, out_dt, v.dy, EPI_STORE, nullptr, nullptr, P_SPMV_CRS);
     else if (fmt == FVG_JDS) jds_spmv(c, *M->tjds, storage, v.kdt, v.dx, out_dt, v.dy, false);
     else hyb_spmv(c, *M->thyb, storage, v.kdt, v.dx, out_dt, v.dy);

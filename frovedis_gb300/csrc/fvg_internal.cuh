@@ -142,6 +142,36 @@ struct DevHYB {  // jds_crs_hybrid_local (jds_crs_hybrid.hpp:8-153)
   bool all_crs = false;  // m <= threshold: the whole matrix is the CRS part
 };
 
+// Row-panel layout of the backward product g = A^T r (FP32 arithmetic).
+// A's rows are cut into panels of `rows` consecutive rows; a CTA stages one
+// panel's slice of r in shared memory and sums, for every hot column h, the
+// products of the column's entries that fall in the panel ("panel row"
+// q = panel * nhot + h, local row ids as uint16).  Hot columns are those with
+// at least `min_per_panel` entries per panel on average; the other columns
+// keep their rows in `cold`, the transposed CRS with the hot rows emptied,
+// whose product gathers r from L2 as before.  g[hot] is the fixed-order sum
+// of the panels' partial sums.
+struct DevPanels {
+  i64 m = 0, n = 0;                 // A: m rows (cut into panels), n columns
+  i64 rows = 0, npanels = 0, nhot = 0, E = 0;
+  double min_per_panel = 0.0;
+  int master = FVG_F64;
+  DBuf hot_cols;                    // int32 [nhot], ascending
+  DBuf poff;                        // int32 [npanels*nhot + 1]
+  DBuf prow;                        // uint16 [E + kPad]: row within the panel
+  DBuf val[3];                      // [E + kPad] per dtype
+  DevCRS cold;                      // n rows, hot rows empty
+  // work items over the panel rows, panel by panel (Item as in Sched)
+  i64 nitems = 0, nlong = 0, npieces = 0;
+  DBuf items, pitem0, long_rows, plong0, long_piece0;
+  DBuf ypan;                        // float [npanels*nhot]
+  DBuf partials;                    // float [npieces]
+};
+// Packs rows [r0, r1) of a CRS (host offsets) into work items with the CRS
+// schedule's rules; piece indices continue from `npieces`.
+void pack_rows(const i32* off, i64 r0, i64 r1, int tile, std::vector<Item>& items, std::vector<i32>& lrows,
+               std::vector<i32>& lpiece0, i64& npieces);
+
 struct Profiler;
 
 }  // namespace fvg
@@ -172,6 +202,12 @@ struct fvg_matrix {
   std::unique_ptr<fvg::DevHYB> hyb, thyb;
   std::vector<double> labels;  // libsvm loads: one label per row
   bool has_labels = false;
+  // row-panel layout of A^T r: built on demand; panel_rows < 0 picks the
+  // layout from the matrix, 0 turns it off, > 0 forces that panel height
+  std::unique_ptr<fvg::DevPanels> pan;
+  bool pan_tried = false;
+  int64_t panel_rows = -1;
+  double panel_min = -1.0;
 };
 
 namespace fvg {
@@ -254,6 +290,16 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
                            const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
                            void* R, i64 ldr, double* out, double* gbias, void* scratch, int loss = 0,
                            double eps = 0.0);
+
+// Row-panel backward product (FP32/BF16 storage): builds the layout when the
+// matrix's column counts make it pay (or as forced); returns null when the
+// plain transposed CRS is used.
+DevPanels* panels_for(fvg_ctx* c, fvg_matrix* M);
+void panel_ensure_plane(fvg_ctx* c, DevPanels& pn, int dt);
+i64 panel_scratch_bytes(fvg_ctx* c, DevPanels& pn, int storage);
+// y[0..n) = A^T r for FP32 r; y FP64 or FP32.
+void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int y_dt, void* y, void* scratch,
+                    int prof_key);
 
 // Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
 void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);

@@ -343,6 +343,7 @@ struct Operand {
   DevJDS* JT = nullptr;
   DevELL* E = nullptr;
   int master = FVG_F64;
+  fvg_matrix* M = nullptr;  // the whole matrix (row-panel backward product); null for row blocks
   // owned pieces (minibatches)
   std::unique_ptr<DevCRS> oA, oAT;
   std::unique_ptr<DevHYB> oH, oHT;
@@ -405,10 +406,25 @@ struct Evaluator {
       s2.alloc(crs_pass_scratch_bytes(c, *op->AT, storage), c->stream);
       FVG_CUDA(cudaMemsetAsync(s2.p, 0, 256, c->stream));
     }
+    use_panels();
+  }
+  // FP32 / BF16 values: the row-panel layout for the backward product when
+  // the matrix has one (CRS and ELL operands share the transposed CRS)
+  DevPanels* PT = nullptr;
+  DBuf s3;
+  void use_panels() {
+    if (PT || storage == FVG_F64 || !op->M || !op->AT) return;
+    PT = panels_for(c, op->M);
+    if (!PT) return;
+    panel_ensure_plane(c, *PT, storage);
+    s3.alloc(panel_scratch_bytes(c, *PT, storage), c->stream);
+    FVG_CUDA(cudaMemsetAsync(s3.p, 0, 256, c->stream));
   }
   void set_storage(int st) {
     storage = st;
     ensure_storage(c, *op, storage);
+    use_panels();
+    if (PT && storage != FVG_F64) panel_ensure_plane(c, *PT, storage);
   }
   // x: weights (FP64 for FP64 storage, FP32 otherwise); b: device intercept
   void eval(const void* x, const double* b, double* grad, double* out) {
@@ -443,6 +459,8 @@ struct Evaluator {
     // backward product into grad[0..n) (FP64 output)
     if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->HT, storage, vdt, r.p, FVG_F64, grad);
     else if (op->fmt == FVG_JDS) jds_spmv(c, *op->JT, storage, vdt, r.p, FVG_F64, grad, false);
+    else if (PT && storage != FVG_F64)
+      panel_trans_mv(c, *PT, storage, r.as<float>(), FVG_F64, grad, s3.p, f32v ? P_PASS2_F32 : P_PASS2);
     else crs_pass(c, *op->AT, storage, vdt, r.p, FVG_F64, grad, EPI_STORE, nullptr, s2.p,
                   f32v ? P_PASS2_F32 : P_PASS2);
   }
@@ -450,6 +468,7 @@ struct Evaluator {
 
 static void build_operand(fvg_ctx* c, fvg_matrix* M, int fmt, Operand& o) {
   o.fmt = fmt;
+  o.M = M;
   o.m = M->A.m;
   o.n = M->A.n;
   o.master = M->master;

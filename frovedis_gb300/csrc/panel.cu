@@ -1,0 +1,677 @@
+// Row-panel backward product g = A^T r for the FP32-arithmetic passes.
+//
+// The reference multiplies its transposed copy (crs_matrix.hpp:356-412 builds
+// it, gradient_descent.hpp:211 multiplies it with dloss), and so does the
+// plain path here: every nonzero of A^T gathers r[source row].  With millions
+// of rows r sits in L2 and each gather of a sparsely used column fetches a
+// 32-byte sector for 4 useful bytes, so that pass is bound by L2-to-SM
+// traffic, far below HBM speed.
+//
+// This layout regroups the columns that occur in most stretches of rows.  A's
+// rows are cut into panels of `rows` consecutive rows.  A CTA copies one
+// panel's slice of r into shared memory with coalesced loads and then walks
+// the panel's entries of the hot columns in (column, row) order, gathering
+// from shared memory; each (panel, hot column) pair gives one FP32 partial sum
+// ("panel row" q = panel * nhot + h).  g[hot column] is the FP64 sum of its
+// partials in panel order.  Columns with fewer entries keep their rows in a
+// transposed CRS of their own (the hot rows emptied), multiplied by the plain
+// CRS kernel first.  Every sum has a fixed order, so the result is the same
+// on every run.
+#include <algorithm>
+#include <cmath>
+#include <thread>
+
+#include "device_common.cuh"
+
+namespace fvg {
+
+namespace {
+
+unsigned grid_n(i64 n, int threads = 256) {
+  i64 g = (n + threads - 1) / threads;
+  if (g > 152 * 32) g = 152 * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+#define PGRID_STRIDE(i, n) for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (i64)gridDim.x * blockDim.x)
+#define PWARP_STRIDE(q, n)                                                              \
+  for (i64 q = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < (n);             \
+       q += ((i64)gridDim.x * blockDim.x) >> 5)
+
+constexpr int kPanelWarps = 16;          // one CTA of 16 warps per SM
+constexpr i64 kPanelRowsAuto = 1 << 30;  // auto: the tallest panels shared memory holds
+constexpr double kPanelMinAuto = 2.0;    // hot: >= this many entries per panel on average
+
+// ------------------------------------------------------------------ build
+__global__ void k_hot_flags(const i32* __restrict__ toff, i64 n, i64 thresh, i64* __restrict__ flag) {
+  PGRID_STRIDE(c, n) flag[c] = ((i64)toff[c + 1] - toff[c] >= thresh) ? 1 : 0;
+}
+
+__global__ void k_hot_list(const i64* __restrict__ flag, const i64* __restrict__ pos, i64 n, i32* __restrict__ hot) {
+  PGRID_STRIDE(c, n) if (flag[c]) hot[pos[c]] = (i32)c;
+}
+
+// B[h*(np+1) + p]: position in A^T of the first entry of hot column h whose
+// source row is >= p*rows (the column's source rows ascend).
+__global__ void k_panel_bounds(const i32* __restrict__ toff, const i32* __restrict__ tidx, const i32* __restrict__ hot,
+                               i64 nhot, i64 np, i64 rows, i32* __restrict__ B) {
+  PGRID_STRIDE(i, nhot * (np + 1)) {
+    const i64 h = i / (np + 1), p = i - h * (np + 1);
+    const i32 c = hot[h];
+    i64 lo = toff[c], hi = toff[c + 1];
+    const i64 target = p * rows;
+    while (lo < hi) {
+      const i64 mid = (lo + hi) >> 1;
+      if ((i64)tidx[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    B[i] = (i32)lo;
+  }
+}
+
+__global__ void k_panel_lens(const i32* __restrict__ B, i64 nhot, i64 np, i64* __restrict__ len) {
+  PGRID_STRIDE(q, np * nhot) {
+    const i64 p = q / nhot, h = q - p * nhot;
+    len[q] = (i64)B[h * (np + 1) + p + 1] - B[h * (np + 1) + p];
+  }
+}
+
+__global__ void k_i64_to_i32(const i64* __restrict__ s, i32* __restrict__ d, i64 n) {
+  PGRID_STRIDE(i, n) d[i] = (i32)s[i];
+}
+
+// a warp per panel row: its entries copied with the row made panel-local
+template <class T>
+__global__ void k_panel_fill(const i32* __restrict__ B, const i64* __restrict__ poff, const i32* __restrict__ tidx,
+                             const T* __restrict__ tval, i64 nhot, i64 np, i64 rows, uint16_t* __restrict__ prow,
+                             T* __restrict__ pval) {
+  const int lane = threadIdx.x & 31;
+  PWARP_STRIDE(q, np * nhot) {
+    const i64 p = q / nhot, h = q - p * nhot;
+    const i64 s = B[h * (np + 1) + p], e = B[h * (np + 1) + p + 1], d = poff[q];
+    const i64 r0 = p * rows;
+    for (i64 k = lane; k < e - s; k += 32) {
+      prow[d + k] = (uint16_t)(tidx[s + k] - r0);
+      pval[d + k] = tval[s + k];
+    }
+  }
+}
+
+__global__ void k_cold_lens(const i32* __restrict__ toff, const i64* __restrict__ flag, i64 n, i64* __restrict__ len) {
+  PGRID_STRIDE(c, n) len[c] = flag[c] ? 0 : (i64)toff[c + 1] - toff[c];
+}
+
+template <class T>
+__global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict__ flag, const i64* __restrict__ coff,
+                            i64 n, const i32* __restrict__ tidx, const T* __restrict__ tval, i32* __restrict__ cidx,
+                            T* __restrict__ cval) {
+  const int lane = threadIdx.x & 31;
+  PWARP_STRIDE(c, n) {
+    if (flag[c]) continue;
+    const i64 s = toff[c], e = toff[c + 1], d = coff[c];
+    for (i64 k = lane; k < e - s; k += 32) {
+      cidx[d + k] = tidx[s + k];
+      cval[d + k] = tval[s + k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- product
+struct PanK {
+  const i32* poff;
+  const uint16_t* prow;
+  const void* val;
+  const float* r;
+  i64 m, rows, npanels;
+  const Item* items;
+  const i32* pitem0;
+  const i32* long_rows;
+  const i32* plong0;
+  const i32* long_piece0;
+  float* partials;
+  float* ypan;
+  unsigned* err;
+  int aligned;  // r is 16-byte aligned: the slice is staged with 16-byte loads
+};
+
+// ---- bulk copies (TMA, non-tensor) completing on an mbarrier
+__device__ __forceinline__ unsigned smem_u32(const void* ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared, both addresses 16-byte aligned, size a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Bounded wait: gives up after 2^22 polls (far beyond any copy's time) and
+// reports it in the device error word instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err) {
+  for (unsigned it = 0; it < (1u << 22); it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicOr(err, 2u);
+  return false;
+}
+
+// Shared memory of one CTA: per warp two staging buffers of one work item's
+// entries (panel rows as uint16, values) with their mbarriers, the tile's
+// row offsets and the item's products; then the panel's slice of r.
+template <class VT> struct PanelSmem {
+  static constexpr int kCap = kWarpTile + 16;              // entries of one copy: 16-byte aligned ends
+  static constexpr int kIdxB = kCap * 2;
+  static constexpr int kValB = kCap * (int)sizeof(VT);
+  static constexpr int kStageB = kIdxB + kValB;
+  static constexpr int kSoffB = ((kTileRows + 1) * 2 + 15) / 16 * 16;
+  static constexpr int kProdB = kCap * 4;                  // products of the staged entries
+  static constexpr int kWarpB = 2 * kStageB + kSoffB + kProdB;
+  static constexpr int kStatic = 16 * kPanelWarps + kPanelWarps * kWarpB;  // bars, then the warps' areas
+};
+
+// One CTA (kPanelWarps warps) per SM takes panels b, b+G, ...  Per panel: r's
+// slice into shared memory; then the warps walk the panel's work items
+// (tiles of short panel rows, pieces of long ones; warp w takes items w,
+// w+W, ...).  A warp's next item streams into its second staging buffer by
+// bulk copy while it sums the current one: each row's entries are multiplied
+// by r gathered from shared memory and added by 1..32 lanes in a fixed order.
+// After a barrier the pieces of long panel rows are added in piece order.
+template <class VT>
+__global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
+  using SM = PanelSmem<VT>;
+  constexpr int NW = kPanelWarps;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + 2 * w;
+  unsigned char* area = smem + 16 * NW + w * SM::kWarpB;
+  unsigned short* soff = reinterpret_cast<unsigned short*>(area + 2 * SM::kStageB);
+  float* prod = reinterpret_cast<float*>(area + 2 * SM::kStageB + SM::kSoffB);
+  float2* prod2 = reinterpret_cast<float2*>(prod);
+  float* xs = reinterpret_cast<float*>(smem + SM::kStatic);  // [rows], 16-byte aligned
+  const VT* __restrict__ val = (const VT*)p.val;
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+  }
+  fence_mbar_init();
+  __syncthreads();
+  const uint64_t pol = policy_evict_first();
+  unsigned parity = 0;   // bit s: parity of stage s's next completion
+  unsigned pending = 0;  // bit s: a copy into stage s not yet waited for
+  bool dead = false;     // a wait ran out: this warp stops working (error word set)
+  // lane 0 starts the copy of item `it` into stage s
+  auto issue = [&](const Item& it, int s) {
+    const int q0 = it.e0 & ~7, q1 = (it.e1 + 7) & ~7;
+    const unsigned n = (unsigned)(q1 - q0);
+    if (lane == 0) {
+      fence_proxy_async();  // this warp's reads of the buffer come before the copy's writes
+      // a tile of empty rows copies nothing: the arrival alone completes the phase
+      mbar_arrive_expect_tx(bar + s, n * 2u + n * (unsigned)sizeof(VT));
+      if (n > 0) {
+        unsigned char* dst = area + s * SM::kStageB;
+        bulk_g2s(dst, p.prow + q0, n * 2u, bar + s, pol);
+        bulk_g2s(dst + SM::kIdxB, val + q0, n * (unsigned)sizeof(VT), bar + s, pol);
+      }
+    }
+    pending |= 1u << s;
+  };
+  // a tile's row offsets, relative to the item's first staged entry: lane L
+  // holds offsets L, L+32, ... (at most kTileRows + 1 of them)
+  constexpr int kSoffRegs = (kTileRows + 1 + 31) / 32;
+  auto load_soff = [&](const Item& it, int (&so)[kSoffRegs]) {
+    if (it.r1 < 0) return;
+#pragma unroll
+    for (int j = 0; j < kSoffRegs; j++) {
+      const int k = lane + 32 * j;
+      if (k <= it.r1 - it.r0) so[j] = __ldg(p.poff + it.r0 + k);
+    }
+  };
+  int stage = 0;
+  for (i64 pn = blockIdx.x; pn < p.npanels; pn += gridDim.x) {
+    const i64 base = pn * p.rows;
+    const int nr = (int)min(p.rows, p.m - base);
+    // descriptors two items ahead, the next item's copy and row offsets in
+    // flight while the current one is summed: no load latency is exposed
+    // per item
+    const int t1 = p.pitem0[pn + 1];
+    int t = p.pitem0[pn] + w;
+    Item d0 = (t < t1) ? p.items[t] : Item{0, 0, 0, 0};
+    Item d1 = (t + NW < t1) ? p.items[t + NW] : Item{0, 0, 0, 0};
+    int so[kSoffRegs], so_nx[kSoffRegs];
+    if (t < t1 && !dead) {
+      issue(d0, stage);  // the copy needs no r: it starts before the slice is staged
+      load_soff(d0, so);
+    }
+    __syncthreads();  // the previous panel's gathers are done
+    {
+      const int n4 = p.aligned ? nr >> 2 : 0;  // rows is a multiple of 4: an aligned r gives aligned slices
+      const float4* src = reinterpret_cast<const float4*>(p.r + base);
+      float4* dst = reinterpret_cast<float4*>(xs);
+      int i = threadIdx.x;
+      for (; i + 3 * NW * 32 < n4; i += 4 * NW * 32) {
+        const float4 a0 = src[i], a1 = src[i + NW * 32], a2 = src[i + 2 * NW * 32], a3 = src[i + 3 * NW * 32];
+        dst[i] = a0;
+        dst[i + NW * 32] = a1;
+        dst[i + 2 * NW * 32] = a2;
+        dst[i + 3 * NW * 32] = a3;
+      }
+      for (; i < n4; i += NW * 32) dst[i] = src[i];
+      for (i = (n4 << 2) + threadIdx.x; i < nr; i += NW * 32) xs[i] = p.r[base + i];
+    }
+    __syncthreads();
+    for (; t < t1 && !dead; t += NW) {
+      const Item it = d0;
+      const Item d2 = (t + 2 * NW < t1) ? p.items[t + 2 * NW] : Item{0, 0, 0, 0};
+      if (t + NW < t1) {
+        issue(d1, stage ^ 1);  // streams in while this item is summed
+        load_soff(d1, so_nx);
+      }
+      const int q0 = it.e0 & ~7;
+      if (it.r1 >= 0) {
+#pragma unroll
+        for (int j = 0; j < kSoffRegs; j++) {
+          const int k = lane + 32 * j;
+          if (k <= it.r1 - it.r0) soff[k] = (unsigned short)(so[j] - q0);
+        }
+      }
+      if (!mbar_wait_bounded(bar + stage, (parity >> stage) & 1u, p.err)) {
+        dead = true;
+        break;
+      }
+      parity ^= 1u << stage;
+      pending &= ~(1u << stage);
+      __syncwarp();
+      {
+        // products of the staged entries, two per lane and step (entries of
+        // neighbouring items staged with them are valid panel rows too;
+        // their products are never summed)
+        const unsigned* sidx2 = reinterpret_cast<const unsigned*>(area + stage * SM::kStageB);
+        const VT* sval = reinterpret_cast<const VT*>(area + stage * SM::kStageB + SM::kIdxB);
+        const int n2 = (((it.e1 + 7) & ~7) - q0) >> 1;
+        for (int k2 = lane; k2 < n2; k2 += 32) {
+          const unsigned c = sidx2[k2];
+          const float v0 = (float)sval[2 * k2], v1 = (float)sval[2 * k2 + 1];
+          prod2[k2] = make_float2(v0 * xs[c & 0xffffu], v1 * xs[c >> 16]);
+        }
+      }
+      __syncwarp();
+      if (it.r1 >= 0) {
+        const int R = it.r1 - it.r0;
+        const int Gl = lanes_per_row(R);
+        const int per_round = 32 / Gl;
+        for (int rb = 0; rb < R; rb += per_round) {
+          const int j = rb + lane / Gl, sub = lane % Gl;
+          float acc = 0.f;
+          if (j < R) {
+            const int s = soff[j], e = soff[j + 1];
+            float a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            int k = s + sub;
+            for (; k + 3 * Gl < e; k += 4 * Gl) {
+              acc += prod[k];
+              a1 += prod[k + Gl];
+              a2 += prod[k + 2 * Gl];
+              a3 += prod[k + 3 * Gl];
+            }
+            for (; k < e; k += Gl) acc += prod[k];
+            acc = (acc + a1) + (a2 + a3);
+          }
+          for (int o = Gl >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (j < R && sub == 0) p.ypan[it.r0 + j] = acc;
+        }
+      } else {
+        float acc = 0.f;
+        const int e = it.e1 - q0;
+        for (int k = it.e0 - q0 + lane; k < e; k += 32) acc += prod[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) p.partials[-1 - it.r1] = acc;
+      }
+      __syncwarp();  // the buffers are read: the next issue may overwrite the stage
+      stage ^= 1;
+      d0 = d1;
+      d1 = d2;
+#pragma unroll
+      for (int j = 0; j < kSoffRegs; j++) so[j] = so_nx[j];
+    }
+    __syncthreads();  // every piece of this panel is written
+    const int l1 = p.plong0[pn + 1];
+    for (int L = p.plong0[pn] + w; L < l1; L += NW) {
+      const int c0 = p.long_piece0[L], c1 = p.long_piece0[L + 1];
+      float acc = 0.f;
+      for (int j = c0 + lane; j < c1; j += 32) acc += __ldcg(p.partials + j);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) p.ypan[p.long_rows[L]] = acc;
+    }
+  }
+  // a warp that gave up still lets its copies in flight land (bounded)
+  for (int s = 0; s < 2; s++)
+    if (pending & (1u << s)) mbar_wait_bounded(bar + s, (parity >> s) & 1u, nullptr);
+}
+
+// g[hot[h]] = sum over panels of ypan[panel*nhot + h] in a fixed order:
+// 32 columns per CTA of 1024 threads; warp w adds panels w, w+32, ... in two
+// compensated FP32 sums (GB300's FP64 unit is too narrow for one FP64 add per
+// partial), then warp 0 adds the 32 warp sums in FP64, in order.
+template <class YT>
+__global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__ ypan, const i32* __restrict__ hot,
+                                                       i64 nhot, i64 np, YT* __restrict__ y) {
+  __shared__ double part[32][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (i64 h0 = (i64)blockIdx.x * 32; h0 < nhot; h0 += (i64)gridDim.x * 32) {
+    const i64 h = h0 + lane;
+    FSum a, b;
+    if (h < nhot) {
+      i64 pn = w;
+      for (; pn + 32 < np; pn += 64) {
+        a.add(__ldcs(ypan + pn * nhot + h));
+        b.add(__ldcs(ypan + (pn + 32) * nhot + h));
+      }
+      if (pn < np) a.add(__ldcs(ypan + pn * nhot + h));
+    }
+    part[w][lane] = a.total() + b.total();
+    __syncthreads();
+    if (w == 0 && h < nhot) {
+      double s = 0.0;
+#pragma unroll 8
+      for (int q = 0; q < 32; q++) s += part[q][lane];
+      y[hot[h]] = (YT)s;
+    }
+    __syncthreads();
+  }
+}
+
+template <class VT> int panel_smem_bytes(i64 rows) { return PanelSmem<VT>::kStatic + (int)(rows * 4); }
+
+// Tallest panel one CTA can stage beside the FP32 staging buffers (the
+// larger ones: a layout serves FP32 and BF16 values).
+i64 panel_rows_cap(fvg_ctx* c) {
+  cudaDeviceProp prop;
+  FVG_CUDA(cudaGetDeviceProperties(&prop, c->device));
+  const i64 per_cta = std::min<i64>((i64)prop.sharedMemPerMultiprocessor - (i64)prop.reservedSharedMemPerBlock,
+                                    (i64)prop.sharedMemPerBlockOptin);
+  i64 cap = (per_cta - PanelSmem<float>::kStatic) / 4;
+  cap = std::min<i64>(cap, 65536);  // panel-local rows are uint16
+  return cap & ~3ll;
+}
+
+template <class T>
+void fill_planes(fvg_ctx* c, const DevCRS& at, DevPanels& pn, const i32* B, const i64* poff64, const i64* flag,
+                 const i64* coff) {
+  const T* tv = at.val[pn.master].as<T>();
+  k_panel_fill<T><<<grid_n(32 * pn.npanels * pn.nhot), 256, 0, c->stream>>>(
+      B, poff64, at.idx.as<i32>(), tv, pn.nhot, pn.npanels, pn.rows, pn.prow.as<uint16_t>(), pn.val[pn.master].as<T>());
+  check_launch("panel_fill");
+  k_cold_fill<T><<<grid_n(32 * pn.n), 256, 0, c->stream>>>(at.off.as<i32>(), flag, coff, pn.n, at.idx.as<i32>(), tv,
+                                                           pn.cold.idx.as<i32>(), pn.cold.val[pn.master].as<T>());
+  check_launch("cold_fill");
+  count_launch(c, 2);
+}
+
+void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
+  b.alloc((size_t)(n + kPad) * elem, c->stream);
+  FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * elem, 0, (size_t)kPad * elem, c->stream));
+}
+
+// Builds the layout from the transposed CRS; null when it would not pay
+// (too few panels or too little of the matrix in hot columns) or does not fit
+// its index types.
+std::unique_ptr<DevPanels> panel_build(fvg_ctx* c, const DevCRS& at, int master, i64 force_rows, double min_pp) {
+  const i64 m = at.n, n = at.m, nnz = at.nnz;
+  const bool forced = force_rows > 0;
+  if (m <= 0 || n <= 0 || nnz <= 0) return nullptr;
+  const i64 cap = panel_rows_cap(c);
+  i64 rows;
+  if (forced) {
+    if (force_rows % 4 != 0 || force_rows > cap)
+      fail(FVG_ERR_INVALID_ARG, "panel rows must be a multiple of 4 and at most " + std::to_string(cap));
+    rows = force_rows;
+  } else {
+    const i64 target = std::min<i64>(kPanelRowsAuto, cap);
+    const i64 grid = c->num_sms;  // one CTA per SM
+    const i64 np0 = (m + target - 1) / target;
+    if (np0 < 8) return nullptr;  // too few panels to pay for the split
+    if (np0 >= grid) {
+      // the fewest whole rounds over the persistent grid whose panels fit in
+      // shared memory (the tallest panels: the most columns count as hot)
+      const i64 rounds = (m + cap * grid - 1) / (cap * grid);
+      rows = ((m + rounds * grid - 1) / (rounds * grid) + 3) & ~3ll;
+    } else {
+      rows = target;
+    }
+  }
+  const double mpp = min_pp > 0 ? min_pp : kPanelMinAuto;
+  auto pn = std::make_unique<DevPanels>();
+  pn->m = m;
+  pn->n = n;
+  pn->rows = rows;
+  pn->npanels = (m + rows - 1) / rows;
+  pn->min_per_panel = mpp;
+  pn->master = master;
+  const i64 np = pn->npanels;
+  const i64 thresh = std::max<i64>(1, (i64)std::ceil(mpp * (double)np));
+  // hot columns
+  DBuf flag, pos;
+  flag.alloc(sizeof(i64) * n, c->stream);
+  pos.alloc(sizeof(i64) * (n + 1), c->stream);
+  k_hot_flags<<<grid_n(n), 256, 0, c->stream>>>(at.off.as<i32>(), n, thresh, flag.as<i64>());
+  check_launch("hot_flags");
+  count_launch(c);
+  scan_i64(c, flag.as<i64>(), pos.as<i64>(), n);
+  i64 nhot = 0;
+  FVG_CUDA(cudaMemcpyAsync(&nhot, pos.as<i64>() + n, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  if (nhot == 0 || np * nhot >= (1ll << 31) - 1) return nullptr;
+  pn->nhot = nhot;
+  pn->hot_cols.alloc(sizeof(i32) * nhot, c->stream);
+  k_hot_list<<<grid_n(n), 256, 0, c->stream>>>(flag.as<i64>(), pos.as<i64>(), n, pn->hot_cols.as<i32>());
+  check_launch("hot_list");
+  count_launch(c);
+  // per (panel, hot column) ranges and their offsets
+  DBuf B, len, poff64;
+  B.alloc(sizeof(i32) * nhot * (np + 1), c->stream);
+  k_panel_bounds<<<grid_n(nhot * (np + 1)), 256, 0, c->stream>>>(at.off.as<i32>(), at.idx.as<i32>(),
+                                                                  pn->hot_cols.as<i32>(), nhot, np, rows, B.as<i32>());
+  check_launch("panel_bounds");
+  const i64 Q = np * nhot;
+  len.alloc(sizeof(i64) * Q, c->stream);
+  poff64.alloc(sizeof(i64) * (Q + 1), c->stream);
+  k_panel_lens<<<grid_n(Q), 256, 0, c->stream>>>(B.as<i32>(), nhot, np, len.as<i64>());
+  check_launch("panel_lens");
+  count_launch(c, 2);
+  scan_i64(c, len.as<i64>(), poff64.as<i64>(), Q);
+  i64 E = 0;
+  FVG_CUDA(cudaMemcpyAsync(&E, poff64.as<i64>() + Q, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  if (!forced && (double)E < 0.25 * (double)nnz) return nullptr;  // mostly cold: the plain path
+  pn->E = E;
+  pn->poff.alloc(sizeof(i32) * (Q + 1), c->stream);
+  k_i64_to_i32<<<grid_n(Q + 1), 256, 0, c->stream>>>(poff64.as<i64>(), pn->poff.as<i32>(), Q + 1);
+  check_launch("poff");
+  count_launch(c);
+  alloc_padded(c, pn->prow, E, 2);
+  alloc_padded(c, pn->val[master], E, dtype_size(master));
+  // cold columns: A^T with the hot rows emptied
+  DevCRS& cold = pn->cold;
+  cold.m = n;
+  cold.n = m;
+  DBuf clen, coff64;
+  clen.alloc(sizeof(i64) * n, c->stream);
+  coff64.alloc(sizeof(i64) * (n + 1), c->stream);
+  k_cold_lens<<<grid_n(n), 256, 0, c->stream>>>(at.off.as<i32>(), flag.as<i64>(), n, clen.as<i64>());
+  check_launch("cold_lens");
+  count_launch(c);
+  scan_i64(c, clen.as<i64>(), coff64.as<i64>(), n);
+  FVG_CUDA(cudaMemcpyAsync(&cold.nnz, coff64.as<i64>() + n, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  cold.off.alloc(sizeof(i32) * (n + 1), c->stream);
+  k_i64_to_i32<<<grid_n(n + 1), 256, 0, c->stream>>>(coff64.as<i64>(), cold.off.as<i32>(), n + 1);
+  check_launch("cold_off");
+  count_launch(c);
+  alloc_padded(c, cold.idx, cold.nnz, 4);
+  alloc_padded(c, cold.val[master], cold.nnz, dtype_size(master));
+  if (master == FVG_F64) fill_planes<double>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
+  else if (master == FVG_F32) fill_planes<float>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
+  else fill_planes<bf16>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
+  cold.max_row = 0;  // not used by the product
+  // work items, panel by panel (host threads over panels)
+  std::vector<i32> off((size_t)Q + 1);
+  FVG_CUDA(cudaMemcpyAsync(off.data(), pn->poff.p, sizeof(i32) * (Q + 1), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  struct Part {
+    std::vector<Item> items;
+    std::vector<i32> lrows, lpiece0;
+    i64 npieces = 0;
+  };
+  std::vector<Part> parts((size_t)np);
+  {
+    const int nt = (int)std::max<i64>(1, std::min<i64>(np, std::max(1u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, t]() {
+        for (i64 p = t; p < np; p += nt) {
+          Part& P = parts[(size_t)p];
+          pack_rows(off.data(), p * nhot, (p + 1) * nhot, kWarpTile, P.items, P.lrows, P.lpiece0, P.npieces);
+        }
+      });
+    for (auto& x : th) x.join();
+  }
+  std::vector<Item> items;
+  std::vector<i32> pitem0((size_t)np + 1), lrows, plong0((size_t)np + 1), lpiece0;
+  i64 pieces = 0;
+  for (i64 p = 0; p < np; p++) {
+    Part& P = parts[(size_t)p];
+    pitem0[(size_t)p] = (i32)items.size();
+    plong0[(size_t)p] = (i32)lrows.size();
+    for (Item it : P.items) {
+      if (it.r1 < 0) it.r1 = (int32_t)(-1 - ((-1 - (i64)it.r1) + pieces));
+      items.push_back(it);
+    }
+    for (size_t k = 0; k < P.lrows.size(); k++) {
+      lrows.push_back(P.lrows[k]);
+      lpiece0.push_back((i32)(P.lpiece0[k] + pieces));
+    }
+    pieces += P.npieces;
+    std::vector<Item>().swap(P.items);
+  }
+  pitem0[(size_t)np] = (i32)items.size();
+  plong0[(size_t)np] = (i32)lrows.size();
+  lpiece0.push_back((i32)pieces);
+  pn->nitems = (i64)items.size();
+  pn->nlong = (i64)lrows.size();
+  pn->npieces = pieces;
+  auto up = [&](DBuf& b, const void* src, size_t bytes) {
+    b.alloc(std::max<size_t>(bytes, 4), c->stream);
+    if (bytes) FVG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  };
+  up(pn->items, items.data(), sizeof(Item) * items.size());
+  up(pn->pitem0, pitem0.data(), sizeof(i32) * pitem0.size());
+  up(pn->long_rows, lrows.data(), sizeof(i32) * lrows.size());
+  up(pn->plong0, plong0.data(), sizeof(i32) * plong0.size());
+  up(pn->long_piece0, lpiece0.data(), sizeof(i32) * lpiece0.size());
+  crs_sched(c, pn->cold, kWarpTile);  // the cold product's work items
+  pn->ypan.alloc(sizeof(float) * Q, c->stream);
+  pn->partials.alloc(sizeof(float) * std::max<i64>(pieces, 1), c->stream);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  return pn;
+}
+
+template <class VT>
+void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
+  static int blocks = -1, set_for = -1;
+  const int smem = panel_smem_bytes<VT>(rows);
+  if (set_for != smem) {
+    FVG_CUDA(cudaFuncSetAttribute(k_panel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int nb = 0;
+    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_panel<VT>, kPanelWarps * 32, smem));
+    blocks = std::max(1, nb);
+    set_for = smem;
+  }
+  const int grid = (int)std::max<i64>(1, std::min<i64>(k.npanels, (i64)blocks * c->num_sms));
+  k_panel<VT><<<grid, kPanelWarps * 32, smem, c->stream>>>(k);
+  check_launch("k_panel");
+  count_launch(c);
+}
+
+}  // namespace
+
+DevPanels* panels_for(fvg_ctx* c, fvg_matrix* M) {
+  if (M->panel_rows == 0) return nullptr;
+  if (M->pan) return M->pan.get();
+  if (M->pan_tried) return nullptr;
+  if (!M->AT) {
+    M->AT.reset(new DevCRS());
+    crs_build_transpose(c, M->A, *M->AT, M->master);
+  }
+  // a forced layout that cannot be built throws here, on every call
+  std::unique_ptr<DevPanels> pn = panel_build(c, *M->AT, M->master, M->panel_rows, M->panel_min);
+  M->pan_tried = true;
+  M->pan = std::move(pn);
+  return M->pan.get();
+}
+
+void panel_ensure_plane(fvg_ctx* c, DevPanels& pn, int dt) {
+  ensure_plane_generic(c, pn.val, pn.E, dt, pn.master);
+  crs_ensure_plane(c, pn.cold, dt, pn.master);
+}
+
+i64 panel_scratch_bytes(fvg_ctx* c, DevPanels& pn, int storage) { return crs_pass_scratch_bytes(c, pn.cold, storage); }
+
+void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int y_dt, void* y, void* scratch,
+                    int prof_key) {
+  if (storage == FVG_F64) fail(FVG_ERR_INTERNAL, "the panel product runs on FP32 or BF16 values");
+  if (y_dt != FVG_F64 && y_dt != FVG_F32) fail(FVG_ERR_INTERNAL, "panel product output must be FP64 or FP32");
+  panel_ensure_plane(c, pn, storage);
+  ProfScope pr(c, prof_key);
+  // cold columns (and zeros for the hot ones) by the transposed CRS kernel
+  crs_pass(c, pn.cold, storage, FVG_F32, r, y_dt, y, EPI_STORE, nullptr, scratch, P_NKEYS);
+  PanK k;
+  k.poff = pn.poff.as<i32>();
+  k.prow = pn.prow.as<uint16_t>();
+  k.val = pn.val[storage].p;
+  k.r = r;
+  k.m = pn.m;
+  k.rows = pn.rows;
+  k.npanels = pn.npanels;
+  k.items = pn.items.as<Item>();
+  k.pitem0 = pn.pitem0.as<i32>();
+  k.long_rows = pn.long_rows.as<i32>();
+  k.plong0 = pn.plong0.as<i32>();
+  k.long_piece0 = pn.long_piece0.as<i32>();
+  k.partials = pn.partials.as<float>();
+  k.ypan = pn.ypan.as<float>();
+  k.err = c->dev_err;
+  k.aligned = ((reinterpret_cast<uintptr_t>(r) & 15) == 0) ? 1 : 0;
+  if (storage == FVG_F32) launch_panel<float>(c, k, pn.rows);
+  else launch_panel<bf16>(c, k, pn.rows);
+  const unsigned cg = (unsigned)std::max<i64>(1, std::min<i64>((pn.nhot + 31) / 32, 2 * c->num_sms));
+  if (y_dt == FVG_F64)
+    k_panel_colsum<double><<<cg, 1024, 0, c->stream>>>(pn.ypan.as<float>(), pn.hot_cols.as<i32>(), pn.nhot,
+                                                        pn.npanels, (double*)y);
+  else
+    k_panel_colsum<float><<<cg, 1024, 0, c->stream>>>(pn.ypan.as<float>(), pn.hot_cols.as<i32>(), pn.nhot,
+                                                       pn.npanels, (float*)y);
+  check_launch("k_panel_colsum");
+  count_launch(c);
+}
+
+}  // namespace fvg

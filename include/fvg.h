@@ -101,6 +101,21 @@ FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* ctx, fvg_matrix* mat, fvg_format 
 /* Add a value plane of another precision (FP32 or BF16, rounded to nearest
  * even from the uploaded values) used when a call asks for that storage. */
 FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* ctx, fvg_matrix* mat, fvg_dtype storage);
+/* Layout of the backward product A^T r on FP32 / BF16 values.  No reference
+ * counterpart (the reference multiplies its transposed copy,
+ * gradient_descent.hpp:211; this is a GPU data-layout choice with the same
+ * sums).  A's rows are cut into panels; columns with at least min_per_panel
+ * entries per panel on average are summed panel by panel from a shared-memory
+ * copy of r's slice, the rest through the transposed CRS.
+ * rows < 0: chosen from the matrix (the default; off for small matrices or
+ * when few entries fall in such columns); 0: off; > 0: panels of that many
+ * rows (a multiple of 4, at most what four CTAs per SM can hold in shared
+ * memory).  min_per_panel <= 0 takes the default (2).  Drops a layout built
+ * earlier; the next FP32 / BF16 backward product builds the new one. */
+FVG_API fvg_status fvg_matrix_set_panels(fvg_ctx* ctx, fvg_matrix* mat, int64_t rows, double min_per_panel);
+/* The layout in use (built if needed): info[0] rows per panel (0: none),
+ * info[1] panels, info[2] columns kept in the panels, info[3] their entries. */
+FVG_API fvg_status fvg_matrix_panel_info(fvg_ctx* ctx, fvg_matrix* mat, int64_t* info);
 /* Device bytes held by the matrix and everything derived from it. */
 FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* mat);
 
