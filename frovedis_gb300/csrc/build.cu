@@ -264,24 +264,6 @@ struct Packer {
 };
 }  // namespace
 
-void pack_rows(const i32* off, i64 r0, i64 r1, int tile, std::vector<Item>& items, std::vector<i32>& lrows,
-               std::vector<i32>& lpiece0, i64& npieces) {
-  Packer P;
-  P.off = off;
-  P.tile = tile;
-  P.t0 = r0;
-  P.npieces = npieces;
-  P.items.swap(items);
-  P.lrows.swap(lrows);
-  P.lpiece0.swap(lpiece0);
-  for (i64 r = r0; r < r1; r++) P.row(r);
-  P.flush(r1);
-  items.swap(P.items);
-  lrows.swap(P.lrows);
-  lpiece0.swap(P.lpiece0);
-  npieces = P.npieces;
-}
-
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
   const int slot = 0;
   if (a.sched[slot]) return *a.sched[slot];

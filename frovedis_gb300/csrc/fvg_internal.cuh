@@ -167,11 +167,6 @@ struct DevPanels {
   DBuf ypan;                        // float [npanels*nhot]
   DBuf partials;                    // float [npieces]
 };
-// Packs rows [r0, r1) of a CRS (host offsets) into work items with the CRS
-// schedule's rules; piece indices continue from `npieces`.
-void pack_rows(const i32* off, i64 r0, i64 r1, int tile, std::vector<Item>& items, std::vector<i32>& lrows,
-               std::vector<i32>& lpiece0, i64& npieces);
-
 struct Profiler;
 
 }  // namespace fvg

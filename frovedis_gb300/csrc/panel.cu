@@ -19,7 +19,7 @@
 // on every run.
 #include <algorithm>
 #include <cmath>
-#include <thread>
+#include <vector>
 
 #include "device_common.cuh"
 
@@ -111,6 +111,85 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
     for (i64 k = lane; k < e - s; k += 32) {
       cidx[d + k] = tidx[s + k];
       cval[d + k] = tval[s + k];
+    }
+  }
+}
+
+// Work items of the panel rows, one warp per panel, with the CRS schedule's
+// packing rules (tiles of short rows within kWarpTile entries, kTileRows rows
+// and kLaneWork products per lane; longer rows in pieces cut at 8-element
+// boundaries).  The greedy packing is sequential: every lane runs it on the
+// same offsets (loaded 32 at a time and broadcast by shuffles, so control
+// flow is uniform) and lane 0 writes.  Pass 0 counts each panel's items,
+// long rows and pieces; pass 1 writes them at the scanned offsets `base`
+// (panel-major: a panel's items, long rows and pieces are contiguous and
+// numbered globally).
+__global__ void k_panel_pack(const i32* __restrict__ off, i64 nhot, i64 np, int tile, int write,
+                             i32* __restrict__ cnt, const i32* __restrict__ base, Item* __restrict__ items,
+                             i32* __restrict__ lrows, i32* __restrict__ lpiece0) {
+  const int lane = threadIdx.x & 31;
+  const bool w0 = write && lane == 0;
+  for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np;
+       p += ((i64)gridDim.x * blockDim.x) >> 5) {
+    const i64 r0 = p * nhot, r1 = r0 + nhot;
+    const i32 bi = write ? base[p] : 0, bl = write ? base[(np + 1) + p] : 0, bp = write ? base[2 * (np + 1) + p] : 0;
+    i32 ni = 0, nl = 0, npc = 0;
+    i64 t0 = r0, tnnz = 0, tmax = 0;
+    i32 o_cur = off[r0], o_t0 = o_cur;  // off[r], off[t0]
+    for (i64 rb = r0; rb < r1; rb += 32) {
+      const i32 v = (rb + lane < r1) ? off[rb + lane + 1] : 0;  // off[r + 1] for r = rb + lane
+      const int nrow = (int)min((i64)32, r1 - rb);
+      for (int j = 0; j < nrow; j++) {
+        const i64 r = rb + j;
+        const i32 o_next = __shfl_sync(0xffffffffu, v, j);
+        const i64 len = (i64)o_next - o_cur;
+        if (len > tile) {
+          if (r > t0) {
+            if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
+            ni++;
+          }
+          const i64 st = o_cur, en = o_next, b8 = st & ~7ll;
+          if (w0) {
+            lrows[bl + nl] = (i32)r;
+            lpiece0[bl + nl] = bp + npc;
+          }
+          nl++;
+          for (i64 k = 0; b8 + k * tile < en; k++) {
+            const i64 e0 = (k == 0) ? st : b8 + k * tile, e1 = min(en, b8 + (k + 1) * tile);
+            if (w0) items[bi + ni] = Item{(int32_t)r, (int32_t)(-1 - (bp + npc)), (int32_t)e0, (int32_t)e1};
+            ni++;
+            npc++;
+          }
+          t0 = r + 1;
+          o_t0 = o_next;
+          tnnz = 0;
+          tmax = 0;
+        } else {
+          if (r > t0) {
+            const i64 R = r - t0 + 1, mx = max(tmax, len);
+            if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) {
+              if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
+              ni++;
+              t0 = r;
+              o_t0 = o_cur;
+              tnnz = 0;
+              tmax = 0;
+            }
+          }
+          tnnz += len;
+          tmax = max(tmax, len);
+        }
+        o_cur = o_next;
+      }
+    }
+    if (r1 > t0) {
+      if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r1, o_t0, o_cur};
+      ni++;
+    }
+    if (!write && lane == 0) {
+      cnt[p] = ni;
+      cnt[np + p] = nl;
+      cnt[2 * np + p] = npc;
     }
   }
 }
@@ -533,61 +612,51 @@ std::unique_ptr<DevPanels> panel_build(fvg_ctx* c, const DevCRS& at, int master,
   else if (master == FVG_F32) fill_planes<float>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
   else fill_planes<bf16>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
   cold.max_row = 0;  // not used by the product
-  // work items, panel by panel (host threads over panels)
-  std::vector<i32> off((size_t)Q + 1);
-  FVG_CUDA(cudaMemcpyAsync(off.data(), pn->poff.p, sizeof(i32) * (Q + 1), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));
-  struct Part {
-    std::vector<Item> items;
-    std::vector<i32> lrows, lpiece0;
-    i64 npieces = 0;
-  };
-  std::vector<Part> parts((size_t)np);
+  // work items, panel by panel, packed on the device: counts, their
+  // exclusive scans (a few thousand numbers, on the host), then the items
   {
-    const int nt = (int)std::max<i64>(1, std::min<i64>(np, std::max(1u, std::thread::hardware_concurrency())));
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t++)
-      th.emplace_back([&, t]() {
-        for (i64 p = t; p < np; p += nt) {
-          Part& P = parts[(size_t)p];
-          pack_rows(off.data(), p * nhot, (p + 1) * nhot, kWarpTile, P.items, P.lrows, P.lpiece0, P.npieces);
-        }
-      });
-    for (auto& x : th) x.join();
-  }
-  std::vector<Item> items;
-  std::vector<i32> pitem0((size_t)np + 1), lrows, plong0((size_t)np + 1), lpiece0;
-  i64 pieces = 0;
-  for (i64 p = 0; p < np; p++) {
-    Part& P = parts[(size_t)p];
-    pitem0[(size_t)p] = (i32)items.size();
-    plong0[(size_t)p] = (i32)lrows.size();
-    for (Item it : P.items) {
-      if (it.r1 < 0) it.r1 = (int32_t)(-1 - ((-1 - (i64)it.r1) + pieces));
-      items.push_back(it);
+    DBuf cnt, basev;
+    cnt.alloc(sizeof(i32) * 3 * np, c->stream);
+    const unsigned pg = (unsigned)std::max<i64>(1, np);  // a warp per panel
+    k_panel_pack<<<pg, 32, 0, c->stream>>>(pn->poff.as<i32>(), nhot, np, kWarpTile, 0, cnt.as<i32>(), nullptr,
+                                           nullptr, nullptr, nullptr);
+    check_launch("panel_pack");
+    count_launch(c);
+    std::vector<i32> hc((size_t)(3 * np)), hb((size_t)(3 * (np + 1)));
+    FVG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(i32) * 3 * np, cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+    i64 tot[3] = {0, 0, 0};
+    for (int kind = 0; kind < 3; kind++) {
+      for (i64 p = 0; p < np; p++) {
+        hb[(size_t)(kind * (np + 1) + p)] = (i32)tot[kind];
+        tot[kind] += hc[(size_t)(kind * np + p)];
+      }
+      hb[(size_t)(kind * (np + 1) + np)] = (i32)tot[kind];
     }
-    for (size_t k = 0; k < P.lrows.size(); k++) {
-      lrows.push_back(P.lrows[k]);
-      lpiece0.push_back((i32)(P.lpiece0[k] + pieces));
-    }
-    pieces += P.npieces;
-    std::vector<Item>().swap(P.items);
+    if (tot[0] >= (1ll << 31) - 1 || tot[2] >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "panel schedule too large");
+    pn->nitems = tot[0];
+    pn->nlong = tot[1];
+    pn->npieces = tot[2];
+    basev.alloc(sizeof(i32) * 3 * (np + 1), c->stream);
+    FVG_CUDA(cudaMemcpyAsync(basev.p, hb.data(), sizeof(i32) * 3 * (np + 1), cudaMemcpyHostToDevice, c->stream));
+    pn->items.alloc(sizeof(Item) * std::max<i64>(pn->nitems, 1), c->stream);
+    pn->long_rows.alloc(sizeof(i32) * std::max<i64>(pn->nlong, 1), c->stream);
+    pn->long_piece0.alloc(sizeof(i32) * (pn->nlong + 1), c->stream);
+    k_panel_pack<<<pg, 32, 0, c->stream>>>(pn->poff.as<i32>(), nhot, np, kWarpTile, 1, nullptr, basev.as<i32>(),
+                                           pn->items.as<Item>(), pn->long_rows.as<i32>(), pn->long_piece0.as<i32>());
+    check_launch("panel_pack");
+    count_launch(c);
+    const i32 npc = (i32)pn->npieces;
+    FVG_CUDA(cudaMemcpyAsync(pn->long_piece0.as<i32>() + pn->nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice,
+                             c->stream));
+    pn->pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
+    pn->plong0.alloc(sizeof(i32) * (np + 1), c->stream);
+    FVG_CUDA(cudaMemcpyAsync(pn->pitem0.p, hb.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+    FVG_CUDA(cudaMemcpyAsync(pn->plong0.p, hb.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
+                             c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
   }
-  pitem0[(size_t)np] = (i32)items.size();
-  plong0[(size_t)np] = (i32)lrows.size();
-  lpiece0.push_back((i32)pieces);
-  pn->nitems = (i64)items.size();
-  pn->nlong = (i64)lrows.size();
-  pn->npieces = pieces;
-  auto up = [&](DBuf& b, const void* src, size_t bytes) {
-    b.alloc(std::max<size_t>(bytes, 4), c->stream);
-    if (bytes) FVG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, c->stream));
-  };
-  up(pn->items, items.data(), sizeof(Item) * items.size());
-  up(pn->pitem0, pitem0.data(), sizeof(i32) * pitem0.size());
-  up(pn->long_rows, lrows.data(), sizeof(i32) * lrows.size());
-  up(pn->plong0, plong0.data(), sizeof(i32) * plong0.size());
-  up(pn->long_piece0, lpiece0.data(), sizeof(i32) * lpiece0.size());
+  const i64 pieces = pn->npieces;
   crs_sched(c, pn->cold, kWarpTile);  // the cold product's work items
   pn->ypan.alloc(sizeof(float) * Q, c->stream);
   pn->partials.alloc(sizeof(float) * std::max<i64>(pieces, 1), c->stream);
