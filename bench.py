@@ -36,10 +36,13 @@ sys.path.insert(0, ROOT)
 METRIC = "sparse LogReg L-BFGS iters/s + SpMV HBM GB/s: BF16/batched vs FP64 GPU, same loss"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # dram__bytes_read.sum + dram__bytes_write.sum over the algorithmic bytes of
-# the same launch, from `ncu --set full` of k_crs on the 1,000,000-row
-# version of the benchmark matrix (BF16 values): pass 1 377.56 MB / 380.0 MB,
-# pass 2 373.51 MB / 376.0 MB.
-NCU_TRAFFIC_RATIO = {"pass1": 377.56 / 380.0, "pass2": 373.51 / 376.0}
+# the same pass, from ncu captures on the 1,000,000-row version of the
+# benchmark matrix (BF16 values, all 1,000,000 columns): pass 1 (k_crs)
+# 375.52 MB / 380.01 MB; pass 2 with the row-panel layout (cold k_crs +
+# k_panel + k_panel_colsum) 288.54 MB / 376.01 MB — below the algorithmic
+# bytes because panel rows are stored as 2-byte ids; pass 2 on the plain
+# transposed CRS 373.51 MB / 376.0 MB.
+NCU_TRAFFIC_RATIO = {"pass1": 375.52 / 380.01, "pass2": 288.54 / 376.01, "pass2_plain": 373.51 / 376.0}
 
 
 def load_peak():
@@ -226,7 +229,10 @@ def run_gpu(args):
     # DRAM bytes per launch: ratio of dram__bytes_(read+write) to algorithmic
     # bytes from a 1/10-row ncu capture of the same kernels (BF16 values;
     # 6.0e7 nonzeros, 1,000,000 columns), applied to this run's launches
-    traffic = (sum(NCU_TRAFFIC_RATIO[k[:5]] * alg[k] * prof[k][1] for k in prof) / spmv_n
+    ratio = dict(NCU_TRAFFIC_RATIO)
+    if not panel_info[0]:
+        ratio["pass2"] = ratio["pass2_plain"]
+    traffic = (sum(ratio[k[:5]] * alg[k] * prof[k][1] for k in prof) / spmv_n
                if spmv_n and args.storage == "bf16" else None)
 
     # the same training at the other precisions on the same data: iters/s and
@@ -358,7 +364,9 @@ def run_gpu(args):
         "evaluations_per_s": (prof["pass1"][1] + prof["pass1_f32"][1]) * world / (ms / 1e3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)",
+                     "kernel": ("k_crs pass1 A*w + logistic epilogue; pass2 A^T*r: k_panel (row panels) + "
+                                "k_crs (rare columns) + k_panel_colsum" if panel_info[0] else
+                                "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)"),
                      "algorithmic_bytes_per_launch": alg_total / max(spmv_n, 1), "launches": spmv_n,
                      "kernel_ms": spmv_ms,
                      "traffic_source": "ncu dram bytes / algorithmic bytes on a 1/10-row capture, x this run's "
