@@ -211,6 +211,8 @@ def run_gpu(args):
     # passes over the first value plane ("pass1"/"pass2": BF16 or FP64) and
     # over FP32 values ("_f32": FP32 storage, or BF16 after refinement)
     prof = {k: ctx.profile(k) for k in ("pass1", "pass2", "pass1_f32", "pass2_f32")}
+    # the rest of the timed region: L-BFGS vector kernels, loss/bias finalize
+    other = {k: ctx.profile(k) for k in ("lbfgs_vec", "finalize")}
     ms = allmax(world, ms)
     total_iters = iters * world
     value = total_iters / (ms / 1e3)
@@ -374,6 +376,10 @@ def run_gpu(args):
                      "passes": {k: {"launches": prof[k][1], "ms_avg": prof[k][0] / max(prof[k][1], 1),
                                     "gbs": alg[k] * prof[k][1] / max(prof[k][0], 1e-9) / 1e6}
                                 for k in prof if prof[k][1]}},
+        "step_split_ms": {"products": spmv_ms / args.steps,
+                          "lbfgs_vector": other["lbfgs_vec"][0] / args.steps,
+                          "finalize_in_products": other["finalize"][0] / args.steps,
+                          "total": ms / args.steps},
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "host_memory": "pinned",
                 "phases": {k: v / max(args.e2e_steps, 1) for k, v in phases.items()}},

@@ -107,116 +107,243 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], const bool (&is_max
 
 #define VEC_LOOP(j, n) for (i64 j = (i64)blockIdx.x * kVecThreads + threadIdx.x; j < (n); j += (i64)gridDim.x * kVecThreads)
 
-// ---------------------------------------------------- two-loop recursion
-// first loop, i = k-1 .. 0:  al[i] = rho[i] * (s_i · q);  q -= y_i * al[i]
-// (the q update for step i is applied by the kernel of step i-1)
-__global__ void __launch_bounds__(kVecThreads) k_down(int i, const double* __restrict__ G, double* __restrict__ Q,
-                                                      const double* __restrict__ S, const double* __restrict__ Y,
-                                                      VecArgs a) {
-  LbState* st = a.st;
-  const int k = st->k;
-  if (i >= k) return;
-  const bool first = (i == k - 1);
-  const double* Si = S + (i64)slot(st, i) * a.n1;
-  const double* Yp = first ? nullptr : Y + (i64)slot(st, i + 1) * a.n1;
-  const double alp = first ? 0.0 : st->al[i + 1];
-  double v[1] = {0.0};
-  VEC_LOOP(j, a.n1) {
-    double q = first ? G[j] : __dsub_rn(Q[j], __dmul_rn(Yp[j], alp));
-    Q[j] = q;
-    v[0] += Si[j] * q;
-  }
-  const bool mx[1] = {false};
-  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) { st->al[i] = st->rho[slot(st, i)] * t[0]; });
+// ---------------------------------------------------- L-BFGS direction
+// The whole direction in one cooperative launch: the two loops of
+// compute_hkgk (lbfgs.hpp:79-112) —
+//   first loop, i = k-1 .. 0:  al[i] = rho[i] * (s_i · q);  q -= y_i * al[i]
+//   second loop, i = 0 .. k-1: beta = rho[i] * (y_i · z);  z += s_i * (al[i] - beta)
+//   (z = q * H0 before it, H0 = (1/rho) / (y·y) of the newest pair)
+// — then step = -z (or the no-history step z = -c * 0.1 * g with
+// c = |g| <= 1 ? |g| : 1/|g|, lbfgs.hpp:86-91), g·step, max|step| and the
+// max-scaled step norm (vector_operations.hpp:227-264) with the uphill flip,
+// the 1e20 factor cap and the factors of the 10 trials.  Each update of q
+// (z) is applied in the same pass as the next dot product.  Where a dot
+// product must be complete the CTAs meet at a grid barrier; every CTA then
+// adds all CTAs' partial sums in the same fixed order, so each holds the same
+// value and no second barrier is needed.  Partial-sum slots alternate
+// between two buffers: a CTA may write the next step's partials while slower
+// CTAs still read this step's.  Each thread always handles the same elements,
+// so the vectors it reads back were written by itself.
+struct DirArgs {
+  const double* G;
+  double* Q;
+  double* Z;
+  double* STEP;
+  const double* S;
+  const double* Y;
+  VecArgs a;
+  double* part;              // [2][2 * gridDim.x]
+  unsigned long long* bar;   // barrier arrivals, zeroed before the launch
+  unsigned* err;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
 }
 
-// second loop, i = 0 .. k-1:  beta = rho[i] * (y_i · z);  z += s_i * (al[i] - beta)
-// i == 0 first finishes q (q -= y_0 * al[0]) and forms z = q * H0.
-__global__ void __launch_bounds__(kVecThreads) k_up(int i, const double* __restrict__ Q, double* __restrict__ Z,
-                                                    const double* __restrict__ S, const double* __restrict__ Y,
-                                                    VecArgs a) {
-  LbState* st = a.st;
-  const int k = st->k;
-  if (i >= k) return;
-  const double* Yi = Y + (i64)slot(st, i) * a.n1;
-  double H0 = 0.0, f = 0.0, al0 = 0.0;
-  const double* Sp = nullptr;
-  if (i == 0) {
-    int sl = slot(st, k - 1);
-    double yy = st->yy[sl];
-    if (yy == 0) yy = 1.0;
-    double ys = 1.0 / st->rho[sl];
-    H0 = ys / yy;
-    al0 = st->al[0];
-  } else {
-    Sp = S + (i64)slot(st, i - 1) * a.n1;
-    f = st->al[i - 1] - st->beta[i - 1];
+// Grid barrier `b` of this launch.  The wait is bounded: a CTA that gives up
+// sets the error word and stops waiting at later barriers (the results are
+// then garbage and the call reports the error).
+__device__ __forceinline__ void dir_sync(const DirArgs& d, int b, bool* dead) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(d.bar, 1ull);
+    const unsigned long long target = (unsigned long long)gridDim.x * (unsigned long long)(b + 1);
+    if (!*dead) {
+      for (unsigned it = 0; ld_acquire_u64(d.bar) < target; it++) {
+        if (it > (1u << 24)) {
+          atomicOr(d.err, 4u);
+          *dead = true;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
   }
-  double v[1] = {0.0};
-  VEC_LOOP(j, a.n1) {
-    double z = (i == 0) ? __dmul_rn(__dsub_rn(Q[j], __dmul_rn(Yi[j], al0)), H0) : __dadd_rn(Z[j], __dmul_rn(Sp[j], f));
-    Z[j] = z;
-    v[0] += Yi[j] * z;
-  }
-  const bool mx[1] = {false};
-  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) { st->beta[i] = st->rho[slot(st, i)] * t[0]; });
+  __syncthreads();
 }
 
-// step = -z (finishing the second loop), or the no-history step
-// z = -c * 0.1 * g with c = |g| <= 1 ? |g| : 1/|g| (lbfgs.hpp:86-91);
-// reduces g·step and max|step|.
-__global__ void __launch_bounds__(kVecThreads) k_step(const double* __restrict__ G, const double* __restrict__ Z,
-                                                      double* __restrict__ STEP, const double* __restrict__ S,
-                                                      VecArgs a) {
-  LbState* st = a.st;
-  const int k = st->k;
-  double c = 0.0, f = 0.0;
-  const double* Sp = nullptr;
-  if (k == 0) {
-    double gn = st->gnorm;
-    if (gn > 1) gn = 1.0 / gn;
-    c = __dmul_rn(-gn, 0.1);
-  } else {
-    Sp = S + (i64)slot(st, k - 1) * a.n1;
-    f = st->al[k - 1] - st->beta[k - 1];
+constexpr int kDirThreads = 256;  // (one CTA of 1024 per SM measured slower)
+#define DIR_LOOP(j, n) for (i64 j = (i64)blockIdx.x * kDirThreads + threadIdx.x; j < (n); j += (i64)gridDim.x * kDirThreads)
+
+// CTA partials of NV values (sum, or max where is_max) into slot[blockIdx.x * NV + q]
+template <int NV>
+__device__ __forceinline__ void dir_partial(double (&v)[NV], const bool (&is_max)[NV], double* slot,
+                                            double (*sm)[kDirThreads]) {
+#pragma unroll
+  for (int q = 0; q < NV; q++) sm[q][threadIdx.x] = v[q];
+  __syncthreads();
+  for (int st = kDirThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+#pragma unroll
+      for (int q = 0; q < NV; q++)
+        sm[q][threadIdx.x] = is_max[q] ? fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + st])
+                                       : sm[q][threadIdx.x] + sm[q][threadIdx.x + st];
+    __syncthreads();
   }
-  double v[2] = {0.0, 0.0};
-  VEC_LOOP(j, a.n1) {
-    double z = (k == 0) ? __dmul_rn(c, G[j]) : __dadd_rn(Z[j], __dmul_rn(Sp[j], f));
-    double s = -z;
-    STEP[j] = s;
-    v[0] += G[j] * s;
-    v[1] = fmax(v[1], fabs(s));
-  }
-  const bool mx[2] = {false, true};
-  grid_reduce<2>(v, mx, a.part, a.ticket, [&](double* t) {
-    st->dot_gs = t[0];
-    st->smax = t[1];
-  });
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) slot[(i64)blockIdx.x * NV + q] = sm[q][0];
 }
 
-// stepsize = vector_norm(step) (vector_operations.hpp:227-264, max-scaled),
-// uphill flip, factor cap at 1e20, the factor of each of the 10 trials.
-__global__ void __launch_bounds__(kVecThreads) k_step_norm(const double* __restrict__ STEP, VecArgs a) {
-  LbState* st = a.st;
-  const double mxv = st->smax;
-  const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
-  double v[1] = {0.0};
-  VEC_LOOP(j, a.n1) {
-    double t = STEP[j] * inv;
-    v[0] += t * t;
+// every CTA: the totals of all CTAs' partials, in a fixed order, into tot
+template <int NV>
+__device__ __forceinline__ void dir_total(const double* slot, const bool (&is_max)[NV], double (&tot)[NV],
+                                          double (*sm)[kDirThreads]) {
+  double t[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) t[q] = 0.0;
+  for (i64 b = threadIdx.x; b < gridDim.x; b += kDirThreads)
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const double x = __ldcg(&slot[b * NV + q]);
+      t[q] = is_max[q] ? fmax(t[q], x) : t[q] + x;
+    }
+  __syncthreads();  // sm is free (the partial's reads are done)
+#pragma unroll
+  for (int q = 0; q < NV; q++) sm[q][threadIdx.x] = t[q];
+  __syncthreads();
+  for (int st = kDirThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+#pragma unroll
+      for (int q = 0; q < NV; q++)
+        sm[q][threadIdx.x] = is_max[q] ? fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + st])
+                                       : sm[q][threadIdx.x] + sm[q][threadIdx.x + st];
+    __syncthreads();
   }
-  const bool mx[1] = {false};
-  grid_reduce<1>(v, mx, a.part, a.ticket, [&](double* t) {
-    double ss = (mxv == 0) ? 0.0 : sqrt(t[0]) * mxv;
-    st->stepsize = ss;
-    st->flip = (st->dot_gs > 0) ? -1.0 : 1.0;
-    double fac = 1.0;
-    if (fac * ss > 1e20) fac = 1e20 / ss;
-    st->factor[1] = fac;
-    for (int q = 2; q <= 10; q++) st->factor[q] = st->factor[q - 1] / 10.0;
-    st->bstep = STEP[a.n1 - 1] * st->flip;
-  });
+#pragma unroll
+  for (int q = 0; q < NV; q++) tot[q] = sm[q][0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kDirThreads) k_direction(DirArgs d) {
+  const VecArgs a = d.a;
+  LbState* st = a.st;
+  const int k = st->k;
+  __shared__ double sm[2][kDirThreads];
+  __shared__ double s_al[kMaxHist], s_beta[kMaxHist];
+  __shared__ bool dead;
+  if (threadIdx.x == 0) dead = false;
+  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  const i64 G2 = 2 * (i64)gridDim.x;
+  int b = 0;
+  const bool sum1[1] = {false};
+  // first loop
+  for (int i = k - 1; i >= 0; i--, b++) {
+    const bool first = (i == k - 1);
+    const double* Si = d.S + (i64)slot(st, i) * a.n1;
+    const double* Yp = first ? nullptr : d.Y + (i64)slot(st, i + 1) * a.n1;
+    const double alp = first ? 0.0 : s_al[i + 1];
+    double v[1] = {0.0};
+    DIR_LOOP(j, a.n1) {
+      double q = first ? d.G[j] : __dsub_rn(d.Q[j], __dmul_rn(Yp[j], alp));
+      d.Q[j] = q;
+      v[0] += Si[j] * q;
+    }
+    double* sl = d.part + (b & 1) * G2;
+    dir_partial<1>(v, sum1, sl, sm);
+    dir_sync(d, b, &dead);
+    double t[1];
+    dir_total<1>(sl, sum1, t, sm);
+    const double al = st->rho[slot(st, i)] * t[0];
+    if (threadIdx.x == 0) s_al[i] = al;
+    if (lead) st->al[i] = al;
+    __syncthreads();
+  }
+  // second loop
+  for (int i = 0; i < k; i++, b++) {
+    const double* Yi = d.Y + (i64)slot(st, i) * a.n1;
+    double H0 = 0.0, f = 0.0, al0 = 0.0;
+    const double* Sp = nullptr;
+    if (i == 0) {
+      const int sl0 = slot(st, k - 1);
+      double yy = st->yy[sl0];
+      if (yy == 0) yy = 1.0;
+      const double ys = 1.0 / st->rho[sl0];
+      H0 = ys / yy;
+      al0 = s_al[0];
+    } else {
+      Sp = d.S + (i64)slot(st, i - 1) * a.n1;
+      f = s_al[i - 1] - s_beta[i - 1];
+    }
+    double v[1] = {0.0};
+    DIR_LOOP(j, a.n1) {
+      double z = (i == 0) ? __dmul_rn(__dsub_rn(d.Q[j], __dmul_rn(Yi[j], al0)), H0)
+                          : __dadd_rn(d.Z[j], __dmul_rn(Sp[j], f));
+      d.Z[j] = z;
+      v[0] += Yi[j] * z;
+    }
+    double* sl = d.part + (b & 1) * G2;
+    dir_partial<1>(v, sum1, sl, sm);
+    dir_sync(d, b, &dead);
+    double t[1];
+    dir_total<1>(sl, sum1, t, sm);
+    const double be = st->rho[slot(st, i)] * t[0];
+    if (threadIdx.x == 0) s_beta[i] = be;
+    if (lead) st->beta[i] = be;
+    __syncthreads();
+  }
+  // step = -z (finishing the second loop) or the no-history step
+  double dot_gs, smax;
+  {
+    double c = 0.0, f = 0.0;
+    const double* Sp = nullptr;
+    if (k == 0) {
+      double gn = st->gnorm;
+      if (gn > 1) gn = 1.0 / gn;
+      c = __dmul_rn(-gn, 0.1);
+    } else {
+      Sp = d.S + (i64)slot(st, k - 1) * a.n1;
+      f = s_al[k - 1] - s_beta[k - 1];
+    }
+    double v[2] = {0.0, 0.0};
+    DIR_LOOP(j, a.n1) {
+      double z = (k == 0) ? __dmul_rn(c, d.G[j]) : __dadd_rn(d.Z[j], __dmul_rn(Sp[j], f));
+      double s = -z;
+      d.STEP[j] = s;
+      v[0] += d.G[j] * s;
+      v[1] = fmax(v[1], fabs(s));
+    }
+    const bool mx[2] = {false, true};
+    double* sl = d.part + (b & 1) * G2;
+    dir_partial<2>(v, mx, sl, sm);
+    dir_sync(d, b, &dead);
+    double t[2];
+    dir_total<2>(sl, mx, t, sm);
+    dot_gs = t[0];
+    smax = t[1];
+    b++;
+  }
+  // stepsize = max-scaled norm of the step; flip, factors, intercept step
+  {
+    const double inv = smax == 0 ? 0.0 : 1.0 / smax;
+    double v[1] = {0.0};
+    DIR_LOOP(j, a.n1) {
+      double t = d.STEP[j] * inv;
+      v[0] += t * t;
+    }
+    double* sl = d.part + (b & 1) * G2;
+    dir_partial<1>(v, sum1, sl, sm);
+    dir_sync(d, b, &dead);
+    double t[1];
+    dir_total<1>(sl, sum1, t, sm);
+    if (lead) {
+      st->dot_gs = dot_gs;
+      st->smax = smax;
+      double ss = (smax == 0) ? 0.0 : sqrt(t[0]) * smax;
+      st->stepsize = ss;
+      st->flip = (dot_gs > 0) ? -1.0 : 1.0;
+      double fac = 1.0;
+      if (fac * ss > 1e20) fac = 1e20 / ss;
+      st->factor[1] = fac;
+      for (int q = 2; q <= 10; q++) st->factor[q] = st->factor[q - 1] / 10.0;
+      st->bstep = __ldcg(&d.STEP[a.n1 - 1]) * st->flip;
+    }
+  }
 }
 
 // trial model w' = w + factor*step, b' = b + factor*bstep, then the
@@ -671,6 +798,21 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   FVG_CUDA(cudaMemcpyAsync(W.p, w_h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
   VecArgs va{n, n1, h, part.as<double>(), ticket, st};
   HostPinned hp(4);
+  // the direction kernel: a cooperative grid (every CTA resident), its
+  // partial sums and barrier counter
+  static int dir_blocks = -1;
+  if (dir_blocks < 0) {
+    int nb = 0;
+    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_direction, kDirThreads, 0));
+    dir_blocks = std::max(1, nb);
+  }
+  const int dgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kDirThreads - 1) / kDirThreads,
+                                                        (i64)std::min(dir_blocks, 8) * c->num_sms));
+  DBuf dpart, dbar;
+  dpart.alloc(sizeof(double) * 4 * dgrid, s);
+  dbar.alloc(sizeof(unsigned long long), s);
+  DirArgs dargs{G.as<double>(), Q.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(), Y.as<double>(),
+                va, dpart.as<double>(), dbar.as<unsigned long long>(), c->dev_err};
 
   const double* W_ = W.as<double>();
   auto weights_for = [&](const double* w64, float* wf) -> const void* {
@@ -706,14 +848,11 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   for (; i <= p->num_iteration; i++) {
     {
       ProfScope ps(c, P_LBFGS);
-      for (int q = h - 1; q >= 0; q--)
-        k_down<<<vgrid, kVecThreads, 0, s>>>(q, G.as<double>(), Q.as<double>(), S.as<double>(), Y.as<double>(), va);
-      for (int q = 0; q < h; q++)
-        k_up<<<vgrid, kVecThreads, 0, s>>>(q, Q.as<double>(), Z.as<double>(), S.as<double>(), Y.as<double>(), va);
-      k_step<<<vgrid, kVecThreads, 0, s>>>(G.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(), va);
-      k_step_norm<<<vgrid, kVecThreads, 0, s>>>(STEP.as<double>(), va);
-      check_launch("two-loop");
-      count_launch(c, 2 * h + 2);
+      FVG_CUDA(cudaMemsetAsync(dbar.p, 0, sizeof(unsigned long long), s));
+      void* args[] = {&dargs};
+      FVG_CUDA(cudaLaunchCooperativeKernel((void*)k_direction, dgrid, kDirThreads, args, 0, s));
+      check_launch("direction");
+      count_launch(c);
     }
     int j = 1;
     double newloss = 0, rms_t = 0;
