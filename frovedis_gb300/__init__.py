@@ -63,7 +63,8 @@ EXPORTS = [
     "fvg_multinomial_train", "fvg_multinomial_probability",
     "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
-    "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info",
+    "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info", "fvg_matrix_set_head",
+    "fvg_matrix_head_info",
 ]
 
 _lib = None
@@ -100,6 +101,8 @@ def load(build_if_needed: bool = True):
         "fvg_matrix_add_storage": ([_p, _p, _int], _int),
         "fvg_matrix_set_panels": ([_p, _p, _i64, _dbl], _int),
         "fvg_matrix_panel_info": ([_p, _p, C.POINTER(_i64)], _int),
+        "fvg_matrix_set_head": ([_p, _p, _i64], _int),
+        "fvg_matrix_head_info": ([_p, _p, C.POINTER(_i64)], _int),
         "fvg_matrix_device_bytes": ([_p], _i64),
         "fvg_matrix_get_transpose": ([_p, _p, _p, _p, _p], _int),
         "fvg_matrix_get_ell": ([_p, _p, C.POINTER(_i64), _p, _p], _int),
@@ -302,6 +305,17 @@ class Matrix:
         """Row-panel layout of the FP32/BF16 backward product: rows < 0 picks it
         from the matrix, 0 turns it off, > 0 forces panels of that height."""
         self.ctx.check(self.ctx.L.fvg_matrix_set_panels(self.ctx.h, self.h, int(rows), float(min_per_panel)))
+
+    def set_head(self, columns=-1):
+        """Forward head of the FP32/BF16 forward product: columns < 0 picks it
+        from the matrix, 0 turns it off, > 0 forces that many columns."""
+        self.ctx.check(self.ctx.L.fvg_matrix_set_head(self.ctx.h, self.h, int(columns)))
+
+    def head_info(self):
+        """(columns in the head, their entries); zeros when unused."""
+        info = (_i64 * 2)()
+        self.ctx.check(self.ctx.L.fvg_matrix_head_info(self.ctx.h, self.h, info))
+        return tuple(int(v) for v in info)
 
     def panel_info(self):
         """(rows per panel, panels, columns in the panels, their entries); zeros when unused."""

@@ -298,11 +298,15 @@ FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* c, fvg_matrix* M, fvg_format fmt,
   own(c, M);
   prepare(c, M, fmt, with_transpose != 0);
   // a matrix that already holds FP32 / BF16 values gets its row-panel
-  // backward layout now rather than at the first product
+  // backward layout and its forward head now rather than at the first product
   if (with_transpose && (fmt == FVG_CRS || fmt == FVG_ELL) && (M->A.val[FVG_F32].p || M->A.val[FVG_BF16].p)) {
     DevPanels* pt = panels_for(c, M);
+    DevPanels* hd = fmt == FVG_CRS ? head_for(c, M) : nullptr;
     for (int dt : {FVG_F32, FVG_BF16})
-      if (pt && M->A.val[dt].p) panel_ensure_plane(c, *pt, dt);
+      if (M->A.val[dt].p) {
+        if (pt) panel_ensure_plane(c, *pt, dt);
+        if (hd) head_ensure_plane(c, *hd, dt);
+      }
   }
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -318,6 +322,28 @@ FVG_API fvg_status fvg_matrix_set_panels(fvg_ctx* c, fvg_matrix* M, int64_t rows
   M->pan_tried = false;
   M->panel_rows = rows < 0 ? -1 : rows;
   M->panel_min = min_per_panel;
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_set_head(fvg_ctx* c, fvg_matrix* M, int64_t columns) {
+  if (!c || !M) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  M->head.reset();
+  M->head_tried = false;
+  M->head_cols = columns < 0 ? -1 : columns;
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_matrix_head_info(fvg_ctx* c, fvg_matrix* M, int64_t* info) {
+  if (!c || !M || !info) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  DevPanels* hd = head_for(c, M);
+  info[0] = hd ? hd->rows : 0;
+  info[1] = hd ? hd->E : 0;
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
 }
 
@@ -382,7 +408,8 @@ FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* M) {
   if (M->tjds) b += jds_bytes(*M->tjds);
   for (const DevHYB* h : {M->hyb.get(), M->thyb.get()})
     if (h) b += jds_bytes(h->jds) + crs_bytes(h->crs);
-  if (const DevPanels* p = M->pan.get()) {
+  for (const DevPanels* p : {M->pan.get(), M->head.get()}) {
+    if (!p) continue;
     b += crs_bytes(p->cold);
     for (const DBuf* d : {&p->hot_cols, &p->poff, &p->prow, &p->items, &p->pitem0, &p->long_rows, &p->plong0,
                           &p->long_piece0, &p->ypan, &p->partials})

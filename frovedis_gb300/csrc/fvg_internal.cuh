@@ -166,6 +166,10 @@ struct DevPanels {
   DBuf items, pitem0, long_rows, plong0, long_piece0;
   DBuf ypan;                        // float [npanels*nhot]
   DBuf partials;                    // float [npieces]
+  // forward head (shared = true): every CTA stages w at the columns
+  // hot_cols[0..rows) once; panels are stretches of nhot rows of A; `cold`
+  // holds the rest of each row (m rows, int32 column ids)
+  bool shared = false;
 };
 struct Profiler;
 
@@ -203,6 +207,12 @@ struct fvg_matrix {
   bool pan_tried = false;
   int64_t panel_rows = -1;
   double panel_min = -1.0;
+  // forward head of A (frequent columns staged in shared memory): built on
+  // demand; head_cols < 0 picks it from the matrix, 0 turns it off, > 0
+  // forces that many columns
+  std::unique_ptr<fvg::DevPanels> head;
+  bool head_tried = false;
+  int64_t head_cols = -1;
 };
 
 namespace fvg {
@@ -267,6 +277,7 @@ struct LogregEpi {
   unsigned* ticket = nullptr;
   int loss = 0;                     // GLM loss kind (0 logistic .. 4 squared eps-insensitive)
   double eps = 0.0;                 // epsilon of the eps-insensitive kinds
+  const float* ybase = nullptr;     // FP32 path: per-row partial products added before the epilogue
 };
 // y = A x over the CRS layout (any plane), optional logistic epilogue.
 void crs_pass(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* x, int y_dt, void* y, int epi,
@@ -295,6 +306,14 @@ i64 panel_scratch_bytes(fvg_ctx* c, DevPanels& pn, int storage);
 // y[0..n) = A^T r for FP32 r; y FP64 or FP32.
 void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int y_dt, void* y, void* scratch,
                     int prof_key);
+// Forward head of A for the FP32/BF16 pass 1 (null when the plain CRS pass
+// is used), and that pass: head partials, then the tail's CRS pass with the
+// logistic epilogue over head + tail.
+DevPanels* head_for(fvg_ctx* c, fvg_matrix* M);
+void head_ensure_plane(fvg_ctx* c, DevPanels& hd, int dt);
+i64 head_scratch_bytes(fvg_ctx* c, DevPanels& hd, int storage);
+void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, const LogregEpi& lr, void* scratch,
+                      int prof_key);
 
 // Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
 void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);

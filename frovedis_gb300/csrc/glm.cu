@@ -536,22 +536,36 @@ struct Evaluator {
     use_panels();
   }
   // FP32 / BF16 values: the row-panel layout for the backward product when
-  // the matrix has one (CRS and ELL operands share the transposed CRS)
+  // the matrix has one (CRS and ELL operands share the transposed CRS), and
+  // the forward head for the CRS forward product
   DevPanels* PT = nullptr;
-  DBuf s3;
+  DevPanels* HD = nullptr;
+  DBuf s3, s4;
   void use_panels() {
-    if (PT || storage == FVG_F64 || !op->M || !op->AT) return;
-    PT = panels_for(c, op->M);
-    if (!PT) return;
-    panel_ensure_plane(c, *PT, storage);
-    s3.alloc(panel_scratch_bytes(c, *PT, storage), c->stream);
-    FVG_CUDA(cudaMemsetAsync(s3.p, 0, 256, c->stream));
+    if (storage == FVG_F64 || !op->M) return;
+    if (!PT && op->AT) {
+      PT = panels_for(c, op->M);
+      if (PT) {
+        panel_ensure_plane(c, *PT, storage);
+        s3.alloc(panel_scratch_bytes(c, *PT, storage), c->stream);
+        FVG_CUDA(cudaMemsetAsync(s3.p, 0, 256, c->stream));
+      }
+    }
+    if (!HD && op->fmt == FVG_CRS && op->A) {
+      HD = head_for(c, op->M);
+      if (HD) {
+        head_ensure_plane(c, *HD, storage);
+        s4.alloc(head_scratch_bytes(c, *HD, storage), c->stream);
+        FVG_CUDA(cudaMemsetAsync(s4.p, 0, 256, c->stream));
+      }
+    }
   }
   void set_storage(int st) {
     storage = st;
     ensure_storage(c, *op, storage);
     use_panels();
     if (PT && storage != FVG_F64) panel_ensure_plane(c, *PT, storage);
+    if (HD && storage != FVG_F64) head_ensure_plane(c, *HD, storage);
   }
   // x: weights (FP64 for FP64 storage, FP32 otherwise); b: device intercept
   void eval(const void* x, const double* b, double* grad, double* out) {
@@ -575,7 +589,9 @@ struct Evaluator {
       return;
     }
     const bool f32v = storage == FVG_F32;  // timed apart: the passes read 4-byte values
-    if (op->fmt == FVG_CRS) {
+    if (op->fmt == FVG_CRS && HD && storage != FVG_F64) {
+      head_logreg_pass(c, *HD, storage, (const float*)x, lr, s4.p, f32v ? P_PASS1_F32 : P_PASS1);
+    } else if (op->fmt == FVG_CRS) {
       crs_pass(c, *op->A, storage, vdt, x, vdt, nullptr, EPI_LOGREG, &lr, s1.p, f32v ? P_PASS1_F32 : P_PASS1);
     } else {
       if (op->fmt == FVG_HYBRID) hyb_spmv(c, *op->H, storage, vdt, x, vdt, z.p);

@@ -194,6 +194,73 @@ __global__ void k_panel_pack(const i32* __restrict__ off, i64 nhot, i64 np, int 
   }
 }
 
+// ---------------------------------------------------------- forward head
+// The forward product y = A w gathers w[col] for every nonzero; the
+// frequent columns' part of it takes the same route as the panels: A's
+// entries in the H most frequent columns ("head") form their own CRS with
+// uint16 column slots, and every CTA stages w at those columns in shared
+// memory once.  The rows are cut into one stretch per CTA ("virtual
+// panels" of the panel kernel); the rest of each row ("tail") stays a CRS
+// with int32 column ids whose pass adds the head partial before the
+// logistic epilogue.
+
+// per row: entries in head columns (slot >= 0) and in the tail
+__global__ void k_head_counts(const i32* __restrict__ off, const i32* __restrict__ idx, i64 m,
+                              const i32* __restrict__ slot, i64* __restrict__ hcnt, i64* __restrict__ tcnt) {
+  const int lane = threadIdx.x & 31;
+  PWARP_STRIDE(r, m) {
+    const i64 s0 = off[r], e0 = off[r + 1];
+    int h = 0;
+    for (i64 e = s0 + lane; e < e0; e += 32) h += slot[idx[e]] >= 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if (lane == 0) {
+      hcnt[r] = h;
+      tcnt[r] = (e0 - s0) - h;
+    }
+  }
+}
+
+// head offsets padded to Q rows (rows past m are empty)
+__global__ void k_head_off(const i64* __restrict__ hoff, i64 m, i64 Q, i32* __restrict__ poff) {
+  PGRID_STRIDE(q, Q + 1) poff[q] = (i32)hoff[q < m ? q : m];
+}
+
+// a warp per row: head entries (slot, value) and tail entries (column,
+// value), each in the row's order
+template <class T>
+__global__ void k_head_fill(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,
+                            i64 m, const i32* __restrict__ slot, const i64* __restrict__ hoff,
+                            const i64* __restrict__ toff, uint16_t* __restrict__ hslot, T* __restrict__ hval,
+                            i32* __restrict__ tidx, T* __restrict__ tval) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  PWARP_STRIDE(r, m) {
+    const i64 s0 = off[r], e0 = off[r + 1];
+    i64 hp = hoff[r], tp = toff[r];
+    for (i64 b = s0; b < e0; b += 32) {
+      const i64 e = b + lane;
+      const bool ok = e < e0;
+      const i32 col = ok ? idx[e] : 0;
+      const i32 sl = ok ? slot[col] : -1;
+      const bool head = ok && sl >= 0;
+      const unsigned hb = __ballot_sync(0xffffffffu, head);
+      const unsigned tb = __ballot_sync(0xffffffffu, ok && !head);
+      if (head) {
+        const i64 q = hp + __popc(hb & lt);
+        hslot[q] = (uint16_t)sl;
+        hval[q] = val[e];
+      } else if (ok) {
+        const i64 q = tp + __popc(tb & lt);
+        tidx[q] = col;
+        tval[q] = val[e];
+      }
+      hp += __popc(hb);
+      tp += __popc(tb);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- product
 struct PanK {
   const i32* poff;
@@ -210,6 +277,9 @@ struct PanK {
   float* ypan;
   unsigned* err;
   int aligned;  // r is 16-byte aligned: the slice is staged with 16-byte loads
+  // forward head: every CTA stages the same slice r[xmap[0..rows)] once
+  // (the frequent columns of w), panels are stretches of A's rows
+  const i32* xmap;
 };
 
 // ---- bulk copies (TMA, non-tensor) completing on an mbarrier
@@ -296,11 +366,15 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
   const uint64_t pol = policy_evict_first();
   unsigned parity = 0;
   bool pend = false, dead = false;
+  const bool shared = p.xmap != nullptr;
   for (i64 pn = blockIdx.x; pn < p.npanels; pn += gridDim.x) {
-    const i64 base = pn * p.rows;
-    const int nr = (int)min(p.rows, p.m - base);
+    const i64 base = shared ? 0 : pn * p.rows;
+    const int nr = shared ? (int)p.rows : (int)min(p.rows, p.m - base);
     __syncthreads();
-    {
+    if (shared) {
+      if (pn == blockIdx.x)
+        for (int i = threadIdx.x; i < nr; i += NW * 32) xs[i] = __ldg(p.r + p.xmap[i]);
+    } else {
       const int n4 = p.aligned ? nr >> 2 : 0;
       const float4* src = reinterpret_cast<const float4*>(p.r + base);
       float4* dst = reinterpret_cast<float4*>(xs);
@@ -477,6 +551,51 @@ void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
   FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * elem, 0, (size_t)kPad * elem, c->stream));
 }
 
+// Work items of every panel, packed on the device: counts, their exclusive
+// scans (a few thousand numbers, on the host), then the items.
+void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
+  DBuf cnt, basev;
+  cnt.alloc(sizeof(i32) * 3 * np, c->stream);
+  const unsigned pg = (unsigned)std::max<i64>(1, np);  // a warp per panel
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(pn.poff.as<i32>(), nhot, np, kWarpTile, 0, cnt.as<i32>(), nullptr,
+                                         nullptr, nullptr, nullptr);
+  check_launch("panel_pack");
+  count_launch(c);
+  std::vector<i32> hc((size_t)(3 * np)), hb((size_t)(3 * (np + 1)));
+  FVG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(i32) * 3 * np, cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  i64 tot[3] = {0, 0, 0};
+  for (int kind = 0; kind < 3; kind++) {
+    for (i64 p = 0; p < np; p++) {
+      hb[(size_t)(kind * (np + 1) + p)] = (i32)tot[kind];
+      tot[kind] += hc[(size_t)(kind * np + p)];
+    }
+    hb[(size_t)(kind * (np + 1) + np)] = (i32)tot[kind];
+  }
+  if (tot[0] >= (1ll << 31) - 1 || tot[2] >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "panel schedule too large");
+  pn.nitems = tot[0];
+  pn.nlong = tot[1];
+  pn.npieces = tot[2];
+  basev.alloc(sizeof(i32) * 3 * (np + 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(basev.p, hb.data(), sizeof(i32) * 3 * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  pn.items.alloc(sizeof(Item) * std::max<i64>(pn.nitems, 1), c->stream);
+  pn.long_rows.alloc(sizeof(i32) * std::max<i64>(pn.nlong, 1), c->stream);
+  pn.long_piece0.alloc(sizeof(i32) * (pn.nlong + 1), c->stream);
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(pn.poff.as<i32>(), nhot, np, kWarpTile, 1, nullptr, basev.as<i32>(),
+                                         pn.items.as<Item>(), pn.long_rows.as<i32>(), pn.long_piece0.as<i32>());
+  check_launch("panel_pack");
+  count_launch(c);
+  const i32 npc = (i32)pn.npieces;
+  FVG_CUDA(cudaMemcpyAsync(pn.long_piece0.as<i32>() + pn.nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice,
+                           c->stream));
+  pn.pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
+  pn.plong0.alloc(sizeof(i32) * (np + 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(pn.pitem0.p, hb.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(pn.plong0.p, hb.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
+                           c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
+}
+
 // Builds the layout from the transposed CRS; null when it would not pay
 // (too few panels or too little of the matrix in hot columns) or does not fit
 // its index types.
@@ -578,50 +697,7 @@ std::unique_ptr<DevPanels> panel_build(fvg_ctx* c, const DevCRS& at, int master,
   else if (master == FVG_F32) fill_planes<float>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
   else fill_planes<bf16>(c, at, *pn, B.as<i32>(), poff64.as<i64>(), flag.as<i64>(), coff64.as<i64>());
   cold.max_row = 0;  // not used by the product
-  // work items, panel by panel, packed on the device: counts, their
-  // exclusive scans (a few thousand numbers, on the host), then the items
-  {
-    DBuf cnt, basev;
-    cnt.alloc(sizeof(i32) * 3 * np, c->stream);
-    const unsigned pg = (unsigned)std::max<i64>(1, np);  // a warp per panel
-    k_panel_pack<<<pg, 32, 0, c->stream>>>(pn->poff.as<i32>(), nhot, np, kWarpTile, 0, cnt.as<i32>(), nullptr,
-                                           nullptr, nullptr, nullptr);
-    check_launch("panel_pack");
-    count_launch(c);
-    std::vector<i32> hc((size_t)(3 * np)), hb((size_t)(3 * (np + 1)));
-    FVG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(i32) * 3 * np, cudaMemcpyDeviceToHost, c->stream));
-    FVG_CUDA(cudaStreamSynchronize(c->stream));
-    i64 tot[3] = {0, 0, 0};
-    for (int kind = 0; kind < 3; kind++) {
-      for (i64 p = 0; p < np; p++) {
-        hb[(size_t)(kind * (np + 1) + p)] = (i32)tot[kind];
-        tot[kind] += hc[(size_t)(kind * np + p)];
-      }
-      hb[(size_t)(kind * (np + 1) + np)] = (i32)tot[kind];
-    }
-    if (tot[0] >= (1ll << 31) - 1 || tot[2] >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "panel schedule too large");
-    pn->nitems = tot[0];
-    pn->nlong = tot[1];
-    pn->npieces = tot[2];
-    basev.alloc(sizeof(i32) * 3 * (np + 1), c->stream);
-    FVG_CUDA(cudaMemcpyAsync(basev.p, hb.data(), sizeof(i32) * 3 * (np + 1), cudaMemcpyHostToDevice, c->stream));
-    pn->items.alloc(sizeof(Item) * std::max<i64>(pn->nitems, 1), c->stream);
-    pn->long_rows.alloc(sizeof(i32) * std::max<i64>(pn->nlong, 1), c->stream);
-    pn->long_piece0.alloc(sizeof(i32) * (pn->nlong + 1), c->stream);
-    k_panel_pack<<<pg, 32, 0, c->stream>>>(pn->poff.as<i32>(), nhot, np, kWarpTile, 1, nullptr, basev.as<i32>(),
-                                           pn->items.as<Item>(), pn->long_rows.as<i32>(), pn->long_piece0.as<i32>());
-    check_launch("panel_pack");
-    count_launch(c);
-    const i32 npc = (i32)pn->npieces;
-    FVG_CUDA(cudaMemcpyAsync(pn->long_piece0.as<i32>() + pn->nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice,
-                             c->stream));
-    pn->pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
-    pn->plong0.alloc(sizeof(i32) * (np + 1), c->stream);
-    FVG_CUDA(cudaMemcpyAsync(pn->pitem0.p, hb.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
-    FVG_CUDA(cudaMemcpyAsync(pn->plong0.p, hb.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
-                             c->stream));
-    FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
-  }
+  pack_panels(c, *pn, nhot, np);
   const i64 pieces = pn->npieces;
   crs_sched(c, pn->cold, kWarpTile);  // the cold product's work items
   pn->ypan.alloc(sizeof(float) * Q, c->stream);
@@ -634,19 +710,136 @@ template <class VT>
 void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
   constexpr int threads = kPanelWarps * 32;
   auto kfn = k_panel<VT>;
-  static int blocks = -1, set_for = -1;
+  // the attribute once, at the device's limit (row panels and the forward
+  // head ask for different sizes call after call); resident CTAs per SM for
+  // the sizes seen so far
+  static bool attr = false;
+  static std::vector<std::pair<int, int>> blocks_for;
   const int smem = panel_smem_bytes<VT>(rows);
-  if (set_for != smem) {
-    FVG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  if (!attr) {
+    cudaDeviceProp prop;
+    FVG_CUDA(cudaGetDeviceProperties(&prop, c->device));
+    FVG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prop.sharedMemPerBlockOptin));
+    attr = true;
+  }
+  int blocks = 0;
+  for (auto& e : blocks_for)
+    if (e.first == smem) blocks = e.second;
+  if (!blocks) {
     int nb = 0;
     FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, threads, smem));
     blocks = std::max(1, nb);
-    set_for = smem;
+    blocks_for.push_back({smem, blocks});
   }
   const int grid = (int)std::max<i64>(1, std::min<i64>(k.npanels, (i64)blocks * c->num_sms));
   kfn<<<grid, threads, smem, c->stream>>>(k);
   check_launch("k_panel");
   count_launch(c);
+}
+
+
+// The forward head of A: the H most frequent columns (ties: lower column
+// first), H at most what one CTA stages beside the staging buffers.  Null
+// when it would not pay (small matrices, or the head holding less than half
+// of the entries) unless forced (force_cols > 0).
+std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS& at, int master, i64 force_cols) {
+  const i64 m = a.m, n = a.n, nnz = a.nnz;
+  const bool forced = force_cols > 0;
+  if (m <= 0 || n <= 0 || nnz <= 0) return nullptr;
+  const i64 cap = panel_rows_cap(c);
+  if (forced && force_cols > cap)
+    fail(FVG_ERR_INVALID_ARG, "head columns must be at most " + std::to_string(cap));
+  const i64 grid = c->num_sms;  // one CTA (one stretch of rows) per SM
+  if (!forced && m < 64 * grid * kPanelWarps) return nullptr;
+  const i64 H = std::min<i64>(n, forced ? force_cols : cap);
+  // column counts from the transposed offsets; the H largest
+  std::vector<i32> toff((size_t)n + 1);
+  FVG_CUDA(cudaMemcpyAsync(toff.data(), at.off.p, sizeof(i32) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<i32> cnt((size_t)n);
+  for (i64 j = 0; j < n; j++) cnt[(size_t)j] = toff[(size_t)j + 1] - toff[(size_t)j];
+  std::vector<i32> srt(cnt);
+  std::nth_element(srt.begin(), srt.begin() + (H - 1), srt.end(), std::greater<i32>());
+  const i32 T = srt[(size_t)(H - 1)];  // the H-th largest count
+  i64 above = 0;
+  for (i64 j = 0; j < n; j++) above += cnt[(size_t)j] > T;
+  std::vector<i32> slot((size_t)n, -1), xmap;
+  xmap.reserve((size_t)H);
+  i64 ties = H - above, E = 0;
+  for (i64 j = 0; j < n; j++) {
+    const i32 v = cnt[(size_t)j];
+    if (v > T || (v == T && ties > 0)) {
+      if (v == T) ties--;
+      slot[(size_t)j] = (i32)xmap.size();
+      xmap.push_back((i32)j);
+      E += v;
+    }
+  }
+  if (!forced && (double)E < 0.5 * (double)nnz) return nullptr;
+  auto hd = std::make_unique<DevPanels>();
+  hd->shared = true;
+  hd->master = master;
+  hd->m = H;  // the staged slice: w at the head columns
+  hd->n = n;
+  hd->rows = H;
+  hd->nhot = (m + grid - 1) / grid;  // rows per stretch
+  hd->npanels = (m + hd->nhot - 1) / hd->nhot;
+  const i64 np = hd->npanels, chunk = hd->nhot, Q = np * chunk;
+  hd->hot_cols.alloc(sizeof(i32) * std::max<i64>(H, 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(hd->hot_cols.p, xmap.data(), sizeof(i32) * H, cudaMemcpyHostToDevice, c->stream));
+  DBuf dslot;
+  dslot.alloc(sizeof(i32) * n, c->stream);
+  FVG_CUDA(cudaMemcpyAsync(dslot.p, slot.data(), sizeof(i32) * n, cudaMemcpyHostToDevice, c->stream));
+  DBuf hcnt, tcnt, hoff, tof;
+  hcnt.alloc(sizeof(i64) * m, c->stream);
+  tcnt.alloc(sizeof(i64) * m, c->stream);
+  hoff.alloc(sizeof(i64) * (m + 1), c->stream);
+  tof.alloc(sizeof(i64) * (m + 1), c->stream);
+  k_head_counts<<<grid_n(32 * m), 256, 0, c->stream>>>(a.off.as<i32>(), a.idx.as<i32>(), m, dslot.as<i32>(),
+                                                       hcnt.as<i64>(), tcnt.as<i64>());
+  check_launch("head_counts");
+  count_launch(c);
+  scan_i64(c, hcnt.as<i64>(), hoff.as<i64>(), m);
+  scan_i64(c, tcnt.as<i64>(), tof.as<i64>(), m);
+  i64 tot[2];
+  FVG_CUDA(cudaMemcpyAsync(&tot[0], hoff.as<i64>() + m, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(&tot[1], tof.as<i64>() + m, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  hd->E = tot[0];
+  hd->poff.alloc(sizeof(i32) * (Q + 1), c->stream);
+  k_head_off<<<grid_n(Q + 1), 256, 0, c->stream>>>(hoff.as<i64>(), m, Q, hd->poff.as<i32>());
+  check_launch("head_off");
+  count_launch(c);
+  alloc_padded(c, hd->prow, hd->E, 2);
+  alloc_padded(c, hd->val[master], hd->E, dtype_size(master));
+  DevCRS& tail = hd->cold;
+  tail.m = m;
+  tail.n = n;
+  tail.nnz = tot[1];
+  tail.off.alloc(sizeof(i32) * (m + 1), c->stream);
+  k_i64_to_i32<<<grid_n(m + 1), 256, 0, c->stream>>>(tof.as<i64>(), tail.off.as<i32>(), m + 1);
+  check_launch("tail_off");
+  count_launch(c);
+  alloc_padded(c, tail.idx, tail.nnz, 4);
+  alloc_padded(c, tail.val[master], tail.nnz, dtype_size(master));
+  auto fill = [&](auto tag) {
+    using T = decltype(tag);
+    k_head_fill<T><<<grid_n(32 * m), 256, 0, c->stream>>>(
+        a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<T>(), m, dslot.as<i32>(), hoff.as<i64>(), tof.as<i64>(),
+        hd->prow.as<uint16_t>(), hd->val[master].as<T>(), tail.idx.as<i32>(), tail.val[master].as<T>());
+    check_launch("head_fill");
+    count_launch(c);
+  };
+  if (master == FVG_F64) fill(double{});
+  else if (master == FVG_F32) fill(float{});
+  else fill(bf16{});
+  tail.max_row = 0;
+  pack_panels(c, *hd, chunk, np);
+  crs_sched(c, tail, kWarpTile);
+  hd->ypan.alloc(sizeof(float) * Q, c->stream);
+  hd->partials.alloc(sizeof(float) * std::max<i64>(hd->npieces, 1), c->stream);
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  return hd;
 }
 
 }  // namespace
@@ -698,6 +891,7 @@ void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int 
   k.ypan = pn.ypan.as<float>();
   k.err = c->dev_err;
   k.aligned = ((reinterpret_cast<uintptr_t>(r) & 15) == 0) ? 1 : 0;
+  k.xmap = nullptr;
   if (storage == FVG_F32) launch_panel<float>(c, k, pn.rows);
   else launch_panel<bf16>(c, k, pn.rows);
   const unsigned cg = (unsigned)std::max<i64>(1, std::min<i64>((pn.nhot + 31) / 32, 2 * c->num_sms));
@@ -709,6 +903,61 @@ void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int 
                                                        pn.npanels, (float*)y);
   check_launch("k_panel_colsum");
   count_launch(c);
+}
+
+}  // namespace fvg
+
+namespace fvg {
+
+DevPanels* head_for(fvg_ctx* c, fvg_matrix* M) {
+  if (M->head_cols == 0) return nullptr;
+  if (M->head) return M->head.get();
+  if (M->head_tried) return nullptr;
+  if (!M->AT) {
+    M->AT.reset(new DevCRS());
+    crs_build_transpose(c, M->A, *M->AT, M->master);
+  }
+  std::unique_ptr<DevPanels> hd = head_build(c, M->A, *M->AT, M->master, M->head_cols);
+  M->head_tried = true;
+  M->head = std::move(hd);
+  return M->head.get();
+}
+
+void head_ensure_plane(fvg_ctx* c, DevPanels& hd, int dt) {
+  ensure_plane_generic(c, hd.val, hd.E, dt, hd.master);
+  crs_ensure_plane(c, hd.cold, dt, hd.master);
+}
+
+i64 head_scratch_bytes(fvg_ctx* c, DevPanels& hd, int storage) { return crs_pass_scratch_bytes(c, hd.cold, storage); }
+
+void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, const LogregEpi& lr, void* scratch,
+                      int prof_key) {
+  if (storage == FVG_F64) fail(FVG_ERR_INTERNAL, "the head pass runs on FP32 or BF16 values");
+  head_ensure_plane(c, hd, storage);
+  ProfScope pr(c, prof_key);
+  PanK k;
+  k.poff = hd.poff.as<i32>();
+  k.prow = hd.prow.as<uint16_t>();
+  k.val = hd.val[storage].p;
+  k.r = w;
+  k.m = hd.m;
+  k.rows = hd.rows;
+  k.npanels = hd.npanels;
+  k.items = hd.items.as<Item>();
+  k.pitem0 = hd.pitem0.as<i32>();
+  k.long_rows = hd.long_rows.as<i32>();
+  k.plong0 = hd.plong0.as<i32>();
+  k.long_piece0 = hd.long_piece0.as<i32>();
+  k.partials = hd.partials.as<float>();
+  k.ypan = hd.ypan.as<float>();
+  k.err = c->dev_err;
+  k.aligned = 0;
+  k.xmap = hd.hot_cols.as<i32>();
+  if (storage == FVG_F32) launch_panel<float>(c, k, hd.rows);
+  else launch_panel<bf16>(c, k, hd.rows);
+  LogregEpi t = lr;
+  t.ybase = hd.ypan.as<float>();
+  crs_pass(c, hd.cold, storage, FVG_F32, w, FVG_F32, nullptr, EPI_LOGREG, &t, scratch, P_NKEYS);
 }
 
 }  // namespace fvg

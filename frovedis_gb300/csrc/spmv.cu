@@ -45,6 +45,7 @@ struct CrsK {
   unsigned* err;
   int loss;    // GLM loss kind
   double eps;  // its epsilon
+  const float* ybase;  // FP32 path: per-row partial sums from another pass, added before the epilogue
 };
 
 template <class AT, class YT, int EPI, class S>
@@ -53,6 +54,8 @@ __device__ __forceinline__ void epilogue(const CrsK& p, i32 row, AT acc, AT b, S
     ((YT*)p.y)[row] = (YT)acc;
   } else {
     AT wtx = acc + b;
+    if constexpr (sizeof(AT) == 4)
+      if (p.ybase) wtx += p.ybase[row];
     AT loss, d;
     if constexpr (sizeof(AT) == 8) {
       glm_row<AT>(p.loss, (AT)p.eps, wtx, p.label[row], loss, d);
@@ -216,6 +219,7 @@ struct FinK {
   unsigned* ticket;
   int loss;
   double eps;
+  const float* ybase;
 };
 
 // Long rows: sum the pieces' partials in piece order and apply the
@@ -239,6 +243,8 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const FinK f) {
         ((YT*)f.y)[row] = (YT)acc;
       } else {
         AT loss, d, wtx = acc + b;
+        if constexpr (sizeof(AT) == 4)
+          if (f.ybase) wtx += f.ybase[row];
         if constexpr (sizeof(AT) == 8) {
           glm_row<AT>(f.loss, (AT)f.eps, wtx, f.label[row], loss, d);
           if (f.sw) d = d * f.sw[row];
@@ -347,6 +353,7 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
   p.intercept = lr ? lr->intercept : nullptr;
   p.icpt = lr ? lr->icpt : 0;
   p.r = lr ? lr->r : nullptr;
+  p.ybase = lr ? lr->ybase : nullptr;
   p.cta_part = ps.cta_part;
   p.err = c->dev_err;
   p.loss = lr ? lr->loss : 0;
@@ -372,6 +379,7 @@ static void launch_crs(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const
     f.intercept = p.intercept;
     f.icpt = p.icpt;
     f.r = p.r;
+    f.ybase = p.ybase;
     f.cta_part = ps.cta_part;
     f.ncta = s.nitems > 0 ? grid : 0;
     f.long_part = ps.long_part;

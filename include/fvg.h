@@ -116,6 +116,18 @@ FVG_API fvg_status fvg_matrix_set_panels(fvg_ctx* ctx, fvg_matrix* mat, int64_t 
 /* The layout in use (built if needed): info[0] rows per panel (0: none),
  * info[1] panels, info[2] columns kept in the panels, info[3] their entries. */
 FVG_API fvg_status fvg_matrix_panel_info(fvg_ctx* ctx, fvg_matrix* mat, int64_t* info);
+/* Forward head of A for the FP32 / BF16 forward product A w.  No reference
+ * counterpart (the reference multiplies the CRS matrix row by row,
+ * crs_matrix.hpp:1505-1516; this is a GPU data-layout choice with the same
+ * sums): the entries of A's most frequent columns are multiplied from a
+ * shared-memory copy of w at those columns, the rest of each row through the
+ * CRS kernel, whose epilogue adds both parts.  columns < 0: chosen from the
+ * matrix (the default; off for small matrices or when those columns hold
+ * less than half of the entries); 0: off; > 0: that many columns (at most
+ * what a CTA can hold in shared memory).  Drops a head built earlier. */
+FVG_API fvg_status fvg_matrix_set_head(fvg_ctx* ctx, fvg_matrix* mat, int64_t columns);
+/* The head in use (built if needed): info[0] columns (0: none), info[1] their entries. */
+FVG_API fvg_status fvg_matrix_head_info(fvg_ctx* ctx, fvg_matrix* mat, int64_t* info);
 /* Device bytes held by the matrix and everything derived from it. */
 FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* mat);
 

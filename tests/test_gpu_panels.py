@@ -195,3 +195,89 @@ def test_panel_lbfgs_close_to_oracle(ctx):
         r = fv.logreg_lbfgs(A, label, storage=storage, **kw)
         assert abs(r["loss"] - ro["loss"]) <= 1e-3 * abs(ro["loss"]), storage
     assert A.panel_info()[2] > 0
+
+
+# ------------------------------------------------------------ forward head
+def _eval_check(A, a_rounded, label, storage, rng, sw=None):
+    """FP32/BF16 evaluation against FP64 arithmetic on the same rounded values."""
+    B = A
+    w = rng.standard_normal(a_rounded.n) * 0.2
+    g, loss = fv.logreg_eval(B, label, w, b=0.3, intercept=True, storage=storage, sample_weight=sw)
+    g64, l64 = oracle.logreg_eval(a_rounded, label, w, b=0.3, intercept=True, sw=sw)
+    absa = oracle.CRS(a_rounded.m, a_rounded.n, a_rounded.off, a_rounded.idx, np.abs(a_rounded.val))
+    scale = oracle.spmv(oracle.transpose(absa), np.ones(a_rounded.m))
+    assert abs(loss - l64) <= 1e-5 * abs(l64), (storage, loss, l64)
+    assert np.max(np.abs(g[:-1] - g64[:-1]) / (scale + 1.0)) <= 1e-5, storage
+    assert abs(g[-1] - g64[-1]) <= 1e-5 * a_rounded.m, storage
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+@pytest.mark.parametrize("head,panels", [(64, 0), (700, 512), (1500, 0)])
+def test_head_eval_matches_fp64(ctx, storage, head, panels):
+    # the forward head (the most frequent columns from shared memory, the rest
+    # of each row through the CRS pass whose epilogue adds both); 1500 = every
+    # column: the tail holds no entries and its pass only applies the epilogue
+    a, label = _zipf(24000, 1500, seed=21)
+    ar = _rounded(a, storage)
+    B = ctx.matrix(a.m, a.n, ar.off, ar.idx, ar.val)
+    B.set_head(head)
+    B.set_panels(panels, 1.0)
+    cols, ent = B.head_info()
+    counts = np.bincount(a.idx, minlength=a.n)
+    assert cols == head
+    assert ent == int(np.sort(counts)[::-1][:head].sum())
+    _eval_check(B, ar, label, storage, np.random.default_rng(head), sw=np.random.default_rng(3).uniform(0.5, 2, a.m))
+
+
+def test_head_long_rows_and_empty_rows(ctx):
+    # rows with more than 512 head entries are summed in pieces (added in
+    # order after the CTA's barrier); empty rows and rows without tail entries
+    rng = np.random.default_rng(22)
+    m, n = 9000, 3000
+    rows = []
+    for i in range(m):
+        if i % 97 == 0:
+            rows.append(np.zeros(0, np.int64))
+        elif i % 1000 == 5:
+            rows.append(np.sort(rng.choice(n, 2600, replace=False)))
+        else:
+            k = rng.integers(1, 40)
+            rows.append(np.sort(rng.choice(n, k, replace=False, p=None)))
+    off = np.concatenate([[0], np.cumsum([len(x) for x in rows])]).astype(np.int32)
+    idx = np.concatenate(rows).astype(np.int32)
+    val = np.abs(rng.standard_normal(int(off[-1])))
+    ar = _rounded(oracle.CRS(m, n, off, idx, val), "f32")
+    label = np.where(rng.random(m) < 0.5, 1.0, -1.0)
+    B = ctx.matrix(m, n, ar.off, ar.idx, ar.val)
+    B.set_head(2048)
+    assert B.head_info()[0] == 2048
+    _eval_check(B, ar, label, "f32", rng)
+
+
+def test_head_deterministic_and_errors(ctx):
+    a, label = _zipf(20000, 2000, seed=23)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    A.set_head(300)
+    w = np.random.default_rng(1).standard_normal(a.n) * 0.1
+    g0, l0 = fv.logreg_eval(A, label, w, storage="bf16")
+    for _ in range(3):
+        g, l = fv.logreg_eval(A, label, w, storage="bf16")
+        assert np.array_equal(g, g0) and l == l0
+    A.set_head(1 << 20)  # more columns than shared memory holds: refused when the head is built
+    with pytest.raises(fv.FvgError):
+        fv.logreg_eval(A, label, w, storage="f32")
+    A.set_head(0)
+    assert A.head_info() == (0, 0)
+
+
+def test_head_lbfgs_close_to_oracle(ctx):
+    a, label = _zipf(40000, 2000, seed=24)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    kw = dict(num_iter=20, reg_type="L2", reg_param=1e-3, w0=np.zeros(a.n))
+    ro = oracle.logreg_lbfgs(a, label, nthreads=8, **kw)
+    A.set_head(500)
+    A.set_panels(1024, 1.0)
+    for storage in ("f32", "bf16"):
+        r = fv.logreg_lbfgs(A, label, storage=storage, **kw)
+        assert abs(r["loss"] - ro["loss"]) <= 1e-3 * abs(ro["loss"]), storage
+    assert A.head_info()[0] == 500
