@@ -335,7 +335,12 @@ def run_gpu(args):
         e2e_ms += (t3 - t0) * 1e3
         e2e_iters += rr["n_iter"]
     ctx.set_profiling(False)
-    phases["transpose_device_s"] = ctx.profile("transpose")[0] / 1e3
+    for key in ("transpose", "panel_build", "head_build", "schedule"):
+        phases[key + "_device_s"] = ctx.profile(key)[0] / 1e3
+    # inside `train`: the products and the L-BFGS vector kernels (the rest is
+    # one-time set-up: value planes at the refinement switch, the evaluator)
+    phases["train_products_s"] = sum(ctx.profile(k)[0] for k in ("pass1", "pass2", "pass1_f32", "pass2_f32")) / 1e3
+    phases["train_lbfgs_vector_s"] = ctx.profile("lbfgs_vec")[0] / 1e3
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 

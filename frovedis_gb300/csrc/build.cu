@@ -3,7 +3,6 @@
 // ELL / JDS / JDS-CRS-hybrid layouts (ell_matrix.hpp:63-95,
 // jds_matrix.hpp:81-146, jds_crs_hybrid.hpp:38-153).
 #include <algorithm>
-#include <thread>
 #include <vector>
 
 #include "fvg_internal.cuh"
@@ -223,171 +222,29 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 
 // ---------------------------------------------------------------- schedule
 // Packs rows, in row order, into work items (see Sched): consecutive short
-// rows share a row tile while the tile stays within `tile` nonzeros and
-// kTileRows rows; a long row becomes its own pieces of at most `tile`
-// nonzeros, cut at 8-element boundaries.  Built on the host once per
-// matrix.  The greedy packing is sequential; to spread it over host threads
-// every chunk of 65,536 rows is first packed as if a tile started at its
-// first row, then the chunks are stitched in order: the packing carried over
-// from the previous chunk is continued row by row until it starts a tile at
-// a row where the chunk's own packing also starts one — from there both are
-// in the same state and the chunk's items are taken as they are.  The result
-// is the sequential packing exactly.
-namespace {
-constexpr i64 kSchedChunk = 1 << 16;
-struct Packer {
-  const i32* off;
-  int tile;
-  std::vector<Item> items;
-  std::vector<i32> lrows, lpiece0;
-  i64 npieces = 0;
-  i64 t0 = 0, tnnz = 0, tmax = 0;  // open tile: rows [t0, r), tnnz nonzeros, longest row tmax
-  void flush(i64 r) {
-    if (r > t0) items.push_back(Item{(int32_t)t0, (int32_t)r, off[t0], off[r]});
-    t0 = r;
-    tnnz = 0;
-    tmax = 0;
-  }
-  // one row; returns true when a tile (or a long row's pieces) starts at r
-  bool row(i64 r) {
-    const i64 len = (i64)off[r + 1] - off[r];
-    if (len > tile) {
-      flush(r);
-      const i64 st = off[r], en = off[r + 1], base = st & ~7ll;
-      lrows.push_back((i32)r);
-      lpiece0.push_back((i32)npieces);
-      for (i64 k = 0; base + k * tile < en; k++) {
-        i64 e0 = (k == 0) ? st : base + k * tile;
-        i64 e1 = std::min<i64>(en, base + (k + 1) * tile);
-        items.push_back(Item{(int32_t)r, (int32_t)(-1 - npieces), (int32_t)e0, (int32_t)e1});
-        npieces++;
-      }
-      t0 = r + 1;
-      return true;
-    }
-    // close the tile when this row would overflow it, or make one lane sum
-    // more than kLaneWork products of a row (balance inside the warp)
-    bool starts = (r == t0);
-    if (r > t0) {
-      const i64 R = r - t0 + 1, mx = std::max(tmax, len);
-      if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) {
-        flush(r);
-        starts = true;
-      }
-    }
-    tnnz += len;
-    tmax = std::max(tmax, len);
-    return starts;
-  }
-};
-}  // namespace
+// rows share a row tile while the tile stays within `tile` nonzeros,
+// kTileRows rows and kLaneWork products per lane; a long row becomes its own
+// pieces of at most `tile` nonzeros, cut at 8-element boundaries.  Built on
+// the device once per matrix, in chunks of kSchedChunk rows packed by one
+// warp each (a tile never spans two chunks).
+constexpr i64 kSchedChunk = 4096;
 
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
   const int slot = 0;
   if (a.sched[slot]) return *a.sched[slot];
+  ProfScope ps(c, P_SCHED);
   auto s = std::make_unique<Sched>();
   s->tile = tile;
   const i64 m = a.m;
-  std::vector<i32> off(m + 1);
-  FVG_CUDA(cudaMemcpyAsync(off.data(), a.off.p, sizeof(i32) * (m + 1), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));
   const i64 nchunks = std::max<i64>(1, (m + kSchedChunk - 1) / kSchedChunk);
-  // each chunk packed as if a tile started at its first row
-  std::vector<Packer> spec((size_t)nchunks);
-  std::vector<std::vector<i64>> starts((size_t)nchunks);  // rows where spec starts a tile
-  {
-    const int nt = (int)std::max<i64>(1, std::min<i64>(nchunks, std::max(1u, std::thread::hardware_concurrency())));
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t++)
-      th.emplace_back([&, t]() {
-        for (i64 k = t; k < nchunks; k += nt) {
-          Packer& P = spec[(size_t)k];
-          P.off = off.data();
-          P.tile = tile;
-          const i64 r0 = k * kSchedChunk, r1 = std::min(m, (k + 1) * kSchedChunk);
-          P.t0 = r0;
-          for (i64 r = r0; r < r1; r++)
-            if (P.row(r)) starts[(size_t)k].push_back(r);
-        }
-      });
-    for (auto& x : th) x.join();
-  }
-  // stitch in chunk order
-  Packer G;
-  G.off = off.data();
-  G.tile = tile;
-  for (i64 k = 0; k < nchunks; k++) {
-    Packer& P = spec[(size_t)k];
-    const std::vector<i64>& st = starts[(size_t)k];
-    const i64 r0 = k * kSchedChunk, r1 = std::min(m, (k + 1) * kSchedChunk);
-    i64 sync = -1;
-    if (k == 0) {
-      sync = r0;  // the chunk's packing is the sequential one
-    } else {
-      for (i64 r = r0; r < r1; r++) {
-        const bool g_starts = G.row(r);
-        if (g_starts && std::binary_search(st.begin(), st.end(), r)) {
-          sync = r;
-          break;
-        }
-      }
-    }
-    if (sync < 0) continue;  // carried through the whole chunk: G holds it
-    // G has just started a tile (or long row) at `sync` exactly as P did:
-    // drop G's copy of that row and take P's items from it on
-    size_t gi = G.items.size();
-    while (gi > 0 && G.items[gi - 1].r0 == (int32_t)sync) gi--;
-    if (k > 0) {
-      // pieces G numbered for the row at `sync` are re-taken from P below
-      for (size_t q = gi; q < G.items.size(); q++)
-        if (G.items[q].r1 < 0) G.npieces--;
-      if (!G.lrows.empty() && G.lrows.back() == (i32)sync) {
-        G.lrows.pop_back();
-        G.lpiece0.pop_back();
-      }
-      G.items.resize(gi);
-    }
-    size_t pi = 0;
-    while (pi < P.items.size() && P.items[pi].r0 < (int32_t)sync) pi++;
-    i64 p_first = 0;  // P's pieces before `sync`
-    for (size_t q = 0; q < pi; q++)
-      if (P.items[q].r1 < 0) p_first++;
-    const i64 shift = G.npieces - p_first;
-    for (size_t q = pi; q < P.items.size(); q++) {
-      Item it = P.items[q];
-      if (it.r1 < 0) it.r1 = (int32_t)(-1 - ((-1 - (i64)it.r1) + shift));
-      G.items.push_back(it);
-    }
-    for (size_t q = 0; q < P.lrows.size(); q++)
-      if (P.lrows[q] >= (i32)sync) {
-        G.lrows.push_back(P.lrows[q]);
-        G.lpiece0.push_back((i32)(P.lpiece0[q] + shift));
-      }
-    G.npieces = P.npieces + shift;
-    G.t0 = P.t0;
-    G.tnnz = P.tnnz;
-    G.tmax = P.tmax;
-  }
-  G.flush(m);
-  std::vector<Item>& items = G.items;
-  std::vector<i32>& lrows = G.lrows;
-  std::vector<i32>& lpiece0 = G.lpiece0;
-  const i64 npieces = G.npieces;
-  lpiece0.push_back((i32)npieces);
-  s->nitems = (i64)items.size();
-  s->nlong = (i64)lrows.size();
-  s->npieces = npieces;
-  s->items.alloc(sizeof(Item) * std::max<i64>(s->nitems, 1), c->stream);
-  if (s->nitems)
-    FVG_CUDA(cudaMemcpyAsync(s->items.p, items.data(), sizeof(Item) * s->nitems, cudaMemcpyHostToDevice, c->stream));
-  s->long_rows.alloc(sizeof(i32) * std::max<i64>(s->nlong, 1), c->stream);
-  s->long_piece0.alloc(sizeof(i32) * (s->nlong + 1), c->stream);
-  if (s->nlong)
-    FVG_CUDA(cudaMemcpyAsync(s->long_rows.p, lrows.data(), sizeof(i32) * s->nlong, cudaMemcpyHostToDevice,
-                             c->stream));
-  FVG_CUDA(cudaMemcpyAsync(s->long_piece0.p, lpiece0.data(), sizeof(i32) * (s->nlong + 1), cudaMemcpyHostToDevice,
-                           c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  PackOut o;
+  device_pack(c, a.off.as<i32>(), m, kSchedChunk, nchunks, tile, o);
+  s->nitems = o.nitems;
+  s->nlong = o.nlong;
+  s->npieces = o.npieces;
+  s->items = std::move(o.items);
+  s->long_rows = std::move(o.long_rows);
+  s->long_piece0 = std::move(o.long_piece0);
   a.sched[slot] = std::move(s);
   return *a.sched[slot];
 }

@@ -162,7 +162,8 @@ FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* c) {
 
 static const char* kProfNames[P_NKEYS] = {"spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec",
                                           "transpose", "spmv_ell", "spmv_jds", "spmv_hyb", "spmm",
-                                          "pass1_f32", "pass2_f32", "batch_pass1", "batch_pass2"};
+                                          "pass1_f32", "pass2_f32", "batch_pass1", "batch_pass2",
+                                          "panel_build", "head_build", "schedule"};
 
 FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* c, int enable) {
   if (!c) return FVG_ERR_INVALID_ARG;

@@ -171,6 +171,17 @@ struct DevPanels {
   // holds the rest of each row (m rows, int32 column ids)
   bool shared = false;
 };
+// Work items of a CRS packed on the device, in chunks of `chunk` rows
+// (items never span chunks): counts per chunk, their exclusive scans
+// (`base`: items, long rows, pieces, each np+1 entries), the items, the long
+// rows and the first piece of each long row (nlong+1 entries).
+struct PackOut {
+  i64 nitems = 0, nlong = 0, npieces = 0;
+  DBuf items, long_rows, long_piece0;
+  std::vector<i32> base;
+};
+void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o);
+
 struct Profiler;
 
 }  // namespace fvg
@@ -219,7 +230,8 @@ namespace fvg {
 
 // ------------------------------------------------------------ profiling
 enum ProfKey { P_SPMV_CRS = 0, P_PASS1, P_PASS2, P_FINALIZE, P_LBFGS, P_TRANSPOSE, P_SPMV_ELL, P_SPMV_JDS,
-               P_SPMV_HYB, P_SPMM, P_PASS1_F32, P_PASS2_F32, P_BATCH_PASS1, P_BATCH_PASS2, P_NKEYS };
+               P_SPMV_HYB, P_SPMM, P_PASS1_F32, P_PASS2_F32, P_BATCH_PASS1, P_BATCH_PASS2, P_PANEL_BUILD,
+               P_HEAD_BUILD, P_SCHED, P_NKEYS };
 void prof_begin(fvg_ctx* c, int key);
 void prof_end(fvg_ctx* c, int key);
 void prof_collect(fvg_ctx* c, int key, double* ms, int64_t* n);

@@ -124,14 +124,14 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
 // long rows and pieces; pass 1 writes them at the scanned offsets `base`
 // (panel-major: a panel's items, long rows and pieces are contiguous and
 // numbered globally).
-__global__ void k_panel_pack(const i32* __restrict__ off, i64 nhot, i64 np, int tile, int write,
+__global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 np, int tile, int write,
                              i32* __restrict__ cnt, const i32* __restrict__ base, Item* __restrict__ items,
                              i32* __restrict__ lrows, i32* __restrict__ lpiece0) {
   const int lane = threadIdx.x & 31;
   const bool w0 = write && lane == 0;
   for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np;
        p += ((i64)gridDim.x * blockDim.x) >> 5) {
-    const i64 r0 = p * nhot, r1 = r0 + nhot;
+    const i64 r0 = min(p * nhot, nrows), r1 = min(r0 + nhot, nrows);
     const i32 bi = write ? base[p] : 0, bl = write ? base[(np + 1) + p] : 0, bp = write ? base[2 * (np + 1) + p] : 0;
     i32 ni = 0, nl = 0, npc = 0;
     i64 t0 = r0, tnnz = 0, tmax = 0;
@@ -149,17 +149,19 @@ __global__ void k_panel_pack(const i32* __restrict__ off, i64 nhot, i64 np, int 
             ni++;
           }
           const i64 st = o_cur, en = o_next, b8 = st & ~7ll;
+          const i64 npr = (en - b8 + tile - 1) / tile;  // pieces: b8 + k*tile < en
           if (w0) {
             lrows[bl + nl] = (i32)r;
             lpiece0[bl + nl] = bp + npc;
           }
+          if (write)  // the lanes write the pieces of a long row together
+            for (i64 k = lane; k < npr; k += 32) {
+              const i64 e0 = (k == 0) ? st : b8 + k * tile, e1 = min(en, b8 + (k + 1) * tile);
+              items[bi + ni + k] = Item{(int32_t)r, (int32_t)(-1 - (bp + npc + k)), (int32_t)e0, (int32_t)e1};
+            }
           nl++;
-          for (i64 k = 0; b8 + k * tile < en; k++) {
-            const i64 e0 = (k == 0) ? st : b8 + k * tile, e1 = min(en, b8 + (k + 1) * tile);
-            if (w0) items[bi + ni] = Item{(int32_t)r, (int32_t)(-1 - (bp + npc)), (int32_t)e0, (int32_t)e1};
-            ni++;
-            npc++;
-          }
+          ni += (i32)npr;
+          npc += (i32)npr;
           t0 = r + 1;
           o_t0 = o_next;
           tnnz = 0;
@@ -524,10 +526,11 @@ template <class VT> int panel_smem_bytes(i64 rows) { return PanelSmem<VT>::kStat
 // Tallest panel one CTA can stage beside the FP32 staging buffers (the
 // larger ones: a layout serves FP32 and BF16 values).
 i64 panel_rows_cap(fvg_ctx* c) {
-  cudaDeviceProp prop;
-  FVG_CUDA(cudaGetDeviceProperties(&prop, c->device));
-  const i64 per_cta = std::min<i64>((i64)prop.sharedMemPerMultiprocessor - (i64)prop.reservedSharedMemPerBlock,
-                                    (i64)prop.sharedMemPerBlockOptin);
+  int per_sm = 0, reserved = 0, optin = 0;
+  FVG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device));
+  FVG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->device));
+  FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  const i64 per_cta = std::min<i64>((i64)per_sm - (i64)reserved, (i64)optin);
   i64 cap = (per_cta - PanelSmem<float>::kStatic) / 4;
   cap = std::min<i64>(cap, 65536);  // panel-local rows are uint16
   return cap & ~3ll;
@@ -551,47 +554,66 @@ void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
   FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * elem, 0, (size_t)kPad * elem, c->stream));
 }
 
-// Work items of every panel, packed on the device: counts, their exclusive
-// scans (a few thousand numbers, on the host), then the items.
-void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
+}  // namespace
+
+// Work items of a CRS cut into chunks of `chunk` rows (a chunk's items, long
+// rows and pieces are contiguous, numbered globally), packed on the device:
+// counts, their exclusive scans (a few thousand numbers, on the host), then
+// the items.
+void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o) {
+  const i64 np = std::max<i64>(nchunks, 1);
   DBuf cnt, basev;
   cnt.alloc(sizeof(i32) * 3 * np, c->stream);
-  const unsigned pg = (unsigned)std::max<i64>(1, np);  // a warp per panel
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(pn.poff.as<i32>(), nhot, np, kWarpTile, 0, cnt.as<i32>(), nullptr,
-                                         nullptr, nullptr, nullptr);
-  check_launch("panel_pack");
+  const unsigned pg = (unsigned)std::min<i64>(np, 1 << 20);  // a warp per chunk
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, np, tile, 0, cnt.as<i32>(), nullptr, nullptr, nullptr,
+                                         nullptr);
+  check_launch("pack");
   count_launch(c);
-  std::vector<i32> hc((size_t)(3 * np)), hb((size_t)(3 * (np + 1)));
+  std::vector<i32> hc((size_t)(3 * np));
+  o.base.assign((size_t)(3 * (np + 1)), 0);
   FVG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(i32) * 3 * np, cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   i64 tot[3] = {0, 0, 0};
   for (int kind = 0; kind < 3; kind++) {
     for (i64 p = 0; p < np; p++) {
-      hb[(size_t)(kind * (np + 1) + p)] = (i32)tot[kind];
+      o.base[(size_t)(kind * (np + 1) + p)] = (i32)tot[kind];
       tot[kind] += hc[(size_t)(kind * np + p)];
     }
-    hb[(size_t)(kind * (np + 1) + np)] = (i32)tot[kind];
+    o.base[(size_t)(kind * (np + 1) + np)] = (i32)tot[kind];
   }
-  if (tot[0] >= (1ll << 31) - 1 || tot[2] >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "panel schedule too large");
-  pn.nitems = tot[0];
-  pn.nlong = tot[1];
-  pn.npieces = tot[2];
+  if (tot[0] >= (1ll << 31) - 1 || tot[2] >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "work schedule too large");
+  o.nitems = tot[0];
+  o.nlong = tot[1];
+  o.npieces = tot[2];
   basev.alloc(sizeof(i32) * 3 * (np + 1), c->stream);
-  FVG_CUDA(cudaMemcpyAsync(basev.p, hb.data(), sizeof(i32) * 3 * (np + 1), cudaMemcpyHostToDevice, c->stream));
-  pn.items.alloc(sizeof(Item) * std::max<i64>(pn.nitems, 1), c->stream);
-  pn.long_rows.alloc(sizeof(i32) * std::max<i64>(pn.nlong, 1), c->stream);
-  pn.long_piece0.alloc(sizeof(i32) * (pn.nlong + 1), c->stream);
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(pn.poff.as<i32>(), nhot, np, kWarpTile, 1, nullptr, basev.as<i32>(),
-                                         pn.items.as<Item>(), pn.long_rows.as<i32>(), pn.long_piece0.as<i32>());
-  check_launch("panel_pack");
+  FVG_CUDA(cudaMemcpyAsync(basev.p, o.base.data(), sizeof(i32) * 3 * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  o.items.alloc(sizeof(Item) * std::max<i64>(o.nitems, 1), c->stream);
+  o.long_rows.alloc(sizeof(i32) * std::max<i64>(o.nlong, 1), c->stream);
+  o.long_piece0.alloc(sizeof(i32) * (o.nlong + 1), c->stream);
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, np, tile, 1, nullptr, basev.as<i32>(), o.items.as<Item>(),
+                                         o.long_rows.as<i32>(), o.long_piece0.as<i32>());
+  check_launch("pack");
   count_launch(c);
-  const i32 npc = (i32)pn.npieces;
-  FVG_CUDA(cudaMemcpyAsync(pn.long_piece0.as<i32>() + pn.nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice,
-                           c->stream));
+  const i32 npc = (i32)o.npieces;
+  FVG_CUDA(cudaMemcpyAsync(o.long_piece0.as<i32>() + o.nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host values go out of scope
+}
+
+namespace {
+
+void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
+  PackOut o;
+  device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o);
+  pn.nitems = o.nitems;
+  pn.nlong = o.nlong;
+  pn.npieces = o.npieces;
+  pn.items = std::move(o.items);
+  pn.long_rows = std::move(o.long_rows);
+  pn.long_piece0 = std::move(o.long_piece0);
   pn.pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
   pn.plong0.alloc(sizeof(i32) * (np + 1), c->stream);
-  FVG_CUDA(cudaMemcpyAsync(pn.pitem0.p, hb.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
-  FVG_CUDA(cudaMemcpyAsync(pn.plong0.p, hb.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
+  FVG_CUDA(cudaMemcpyAsync(pn.pitem0.p, o.base.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(pn.plong0.p, o.base.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
                            c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
 }
@@ -600,6 +622,7 @@ void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
 // (too few panels or too little of the matrix in hot columns) or does not fit
 // its index types.
 std::unique_ptr<DevPanels> panel_build(fvg_ctx* c, const DevCRS& at, int master, i64 force_rows, double min_pp) {
+  ProfScope ps(c, P_PANEL_BUILD);
   const i64 m = at.n, n = at.m, nnz = at.nnz;
   const bool forced = force_rows > 0;
   if (m <= 0 || n <= 0 || nnz <= 0) return nullptr;
@@ -717,9 +740,9 @@ void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
   static std::vector<std::pair<int, int>> blocks_for;
   const int smem = panel_smem_bytes<VT>(rows);
   if (!attr) {
-    cudaDeviceProp prop;
-    FVG_CUDA(cudaGetDeviceProperties(&prop, c->device));
-    FVG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prop.sharedMemPerBlockOptin));
+    int optin = 0;
+    FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    FVG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     attr = true;
   }
   int blocks = 0;
@@ -743,6 +766,7 @@ void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
 // when it would not pay (small matrices, or the head holding less than half
 // of the entries) unless forced (force_cols > 0).
 std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS& at, int master, i64 force_cols) {
+  ProfScope ps(c, P_HEAD_BUILD);
   const i64 m = a.m, n = a.n, nnz = a.nnz;
   const bool forced = force_cols > 0;
   if (m <= 0 || n <= 0 || nnz <= 0) return nullptr;
@@ -782,7 +806,10 @@ std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS&
   hd->m = H;  // the staged slice: w at the head columns
   hd->n = n;
   hd->rows = H;
-  hd->nhot = (m + grid - 1) / grid;  // rows per stretch
+  // stretches of at most ~4096 rows, a whole number of them per CTA: the
+  // device packer takes one warp per stretch
+  const i64 per_cta = std::max<i64>(1, (m + grid * 4096 - 1) / (grid * 4096));
+  hd->nhot = (m + grid * per_cta - 1) / (grid * per_cta);  // rows per stretch
   hd->npanels = (m + hd->nhot - 1) / hd->nhot;
   const i64 np = hd->npanels, chunk = hd->nhot, Q = np * chunk;
   hd->hot_cols.alloc(sizeof(i32) * std::max<i64>(H, 1), c->stream);
