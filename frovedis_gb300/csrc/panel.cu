@@ -282,6 +282,7 @@ struct PanK {
   // forward head: every CTA stages the same slice r[xmap[0..rows)] once
   // (the frequent columns of w), panels are stretches of A's rows
   const i32* xmap;
+  i64 group;  // consecutive panels a CTA takes at a time
 };
 
 // ---- bulk copies (TMA, non-tensor) completing on an mbarrier
@@ -369,12 +370,17 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
   unsigned parity = 0;
   bool pend = false, dead = false;
   const bool shared = p.xmap != nullptr;
-  for (i64 pn = blockIdx.x; pn < p.npanels; pn += gridDim.x) {
-    const i64 base = shared ? 0 : pn * p.rows;
+  // a CTA takes `group` consecutive panels at a time (their items and long
+  // rows are contiguous): one per step for row panels, a whole share of the
+  // rows at once for the forward head (one barrier per CTA)
+  const int nunits = (int)((p.npanels + p.group - 1) / p.group);
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const int pn = u * (int)p.group, pe = (int)min((i64)pn + p.group, p.npanels);
+    const i64 base = shared ? 0 : (i64)pn * p.rows;
     const int nr = shared ? (int)p.rows : (int)min(p.rows, p.m - base);
     __syncthreads();
     if (shared) {
-      if (pn == blockIdx.x)
+      if (u == blockIdx.x)
         for (int i = threadIdx.x; i < nr; i += NW * 32) xs[i] = __ldg(p.r + p.xmap[i]);
     } else {
       const int n4 = p.aligned ? nr >> 2 : 0;
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
       for (i = (n4 << 2) + threadIdx.x; i < nr; i += NW * 32) xs[i] = p.r[base + i];
     }
     __syncthreads();
-    const int t1 = p.pitem0[pn + 1];
+    const int t1 = p.pitem0[pe];
     int t = p.pitem0[pn] + w;
     Item nx = (t < t1) ? p.items[t] : Item{0, 0, 0, 0};
     for (; t < t1 && !dead; t += NW) {
@@ -476,7 +482,7 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
       __syncwarp();
     }
     __syncthreads();
-    const int l1 = p.plong0[pn + 1];
+    const int l1 = p.plong0[pe];
     for (int L = p.plong0[pn] + w; L < l1; L += NW) {
       const int c0 = p.long_piece0[L], c1 = p.long_piece0[L + 1];
       float acc = 0.f;
@@ -754,7 +760,8 @@ void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
     blocks = std::max(1, nb);
     blocks_for.push_back({smem, blocks});
   }
-  const int grid = (int)std::max<i64>(1, std::min<i64>(k.npanels, (i64)blocks * c->num_sms));
+  const i64 nunits = (k.npanels + k.group - 1) / k.group;
+  const int grid = (int)std::max<i64>(1, std::min<i64>(nunits, (i64)blocks * c->num_sms));
   kfn<<<grid, threads, smem, c->stream>>>(k);
   check_launch("k_panel");
   count_launch(c);
@@ -919,6 +926,7 @@ void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int 
   k.err = c->dev_err;
   k.aligned = ((reinterpret_cast<uintptr_t>(r) & 15) == 0) ? 1 : 0;
   k.xmap = nullptr;
+  k.group = 1;
   if (storage == FVG_F32) launch_panel<float>(c, k, pn.rows);
   else launch_panel<bf16>(c, k, pn.rows);
   const unsigned cg = (unsigned)std::max<i64>(1, std::min<i64>((pn.nhot + 31) / 32, 2 * c->num_sms));
@@ -980,6 +988,7 @@ void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, co
   k.err = c->dev_err;
   k.aligned = 0;
   k.xmap = hd.hot_cols.as<i32>();
+  k.group = (hd.npanels + c->num_sms - 1) / c->num_sms;  // a CTA's whole share of the stretches
   if (storage == FVG_F32) launch_panel<float>(c, k, hd.rows);
   else launch_panel<bf16>(c, k, hd.rows);
   LogregEpi t = lr;
