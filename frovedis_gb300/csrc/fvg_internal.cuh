@@ -180,7 +180,9 @@ struct PackOut {
   DBuf items, long_rows, long_piece0;
   std::vector<i32> base;
 };
-void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o);
+// Each chunk may itself be packed in `sub` pieces (a warp each; items never
+// span two pieces); base then has nchunks*sub+1 entries per kind.
+void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o, i64 sub = 1);
 
 struct Profiler;
 

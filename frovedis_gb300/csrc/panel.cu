@@ -124,14 +124,17 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
 // long rows and pieces; pass 1 writes them at the scanned offsets `base`
 // (panel-major: a panel's items, long rows and pieces are contiguous and
 // numbered globally).
-__global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 np, int tile, int write,
+__global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 sub, i64 np, int tile, int write,
                              i32* __restrict__ cnt, const i32* __restrict__ base, Item* __restrict__ items,
                              i32* __restrict__ lrows, i32* __restrict__ lpiece0) {
   const int lane = threadIdx.x & 31;
   const bool w0 = write && lane == 0;
+  // chunk p: piece j of `sub` of stretch p / sub (stretches of nhot rows)
+  const i64 step = (nhot + sub - 1) / sub;
   for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np;
        p += ((i64)gridDim.x * blockDim.x) >> 5) {
-    const i64 r0 = min(p * nhot, nrows), r1 = min(r0 + nhot, nrows);
+    const i64 s0 = (p / sub) * nhot, s1 = min(s0 + nhot, nrows), j = p % sub;
+    const i64 r0 = min(s0 + j * step, s1), r1 = min(r0 + step, s1);
     const i32 bi = write ? base[p] : 0, bl = write ? base[(np + 1) + p] : 0, bp = write ? base[2 * (np + 1) + p] : 0;
     i32 ni = 0, nl = 0, npc = 0;
     i64 t0 = r0, tnnz = 0, tmax = 0;
@@ -566,13 +569,13 @@ void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
 // rows and pieces are contiguous, numbered globally), packed on the device:
 // counts, their exclusive scans (a few thousand numbers, on the host), then
 // the items.
-void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o) {
-  const i64 np = std::max<i64>(nchunks, 1);
+void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, int tile, PackOut& o, i64 sub) {
+  const i64 np = std::max<i64>(nchunks, 1) * sub;
   DBuf cnt, basev;
   cnt.alloc(sizeof(i32) * 3 * np, c->stream);
   const unsigned pg = (unsigned)std::min<i64>(np, 1 << 20);  // a warp per chunk
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, np, tile, 0, cnt.as<i32>(), nullptr, nullptr, nullptr,
-                                         nullptr);
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 0, cnt.as<i32>(), nullptr, nullptr,
+                                         nullptr, nullptr);
   check_launch("pack");
   count_launch(c);
   std::vector<i32> hc((size_t)(3 * np));
@@ -596,8 +599,8 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
   o.items.alloc(sizeof(Item) * std::max<i64>(o.nitems, 1), c->stream);
   o.long_rows.alloc(sizeof(i32) * std::max<i64>(o.nlong, 1), c->stream);
   o.long_piece0.alloc(sizeof(i32) * (o.nlong + 1), c->stream);
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, np, tile, 1, nullptr, basev.as<i32>(), o.items.as<Item>(),
-                                         o.long_rows.as<i32>(), o.long_piece0.as<i32>());
+  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 1, nullptr, basev.as<i32>(),
+                                         o.items.as<Item>(), o.long_rows.as<i32>(), o.long_piece0.as<i32>());
   check_launch("pack");
   count_launch(c);
   const i32 npc = (i32)o.npieces;
@@ -609,18 +612,26 @@ namespace {
 
 void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
   PackOut o;
-  device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o);
+  // each panel's rows in pieces of ~4096 rows, a warp each
+  const i64 sub = std::max<i64>(1, (nhot + 4095) / 4096);
+  device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o, sub);
   pn.nitems = o.nitems;
   pn.nlong = o.nlong;
   pn.npieces = o.npieces;
   pn.items = std::move(o.items);
   pn.long_rows = std::move(o.long_rows);
   pn.long_piece0 = std::move(o.long_piece0);
+  // a panel's items and long rows: from its first piece's on
+  const i64 nc = np * sub;
+  std::vector<i32> pi((size_t)np + 1), pl((size_t)np + 1);
+  for (i64 q = 0; q <= np; q++) {
+    pi[(size_t)q] = o.base[(size_t)(q * sub)];
+    pl[(size_t)q] = o.base[(size_t)((nc + 1) + q * sub)];
+  }
   pn.pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
   pn.plong0.alloc(sizeof(i32) * (np + 1), c->stream);
-  FVG_CUDA(cudaMemcpyAsync(pn.pitem0.p, o.base.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
-  FVG_CUDA(cudaMemcpyAsync(pn.plong0.p, o.base.data() + (np + 1), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice,
-                           c->stream));
+  FVG_CUDA(cudaMemcpyAsync(pn.pitem0.p, pi.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(pn.plong0.p, pl.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
 }
 
