@@ -1,22 +1,31 @@
-// Row-panel backward product g = A^T r for the FP32-arithmetic passes.
+// Shared-memory gathers for the FP32-arithmetic passes, and the device
+// packing of every work-item schedule.
 //
-// The reference multiplies its transposed copy (crs_matrix.hpp:356-412 builds
-// it, gradient_descent.hpp:211 multiplies it with dloss), and so does the
-// plain path here: every nonzero of A^T gathers r[source row].  With millions
-// of rows r sits in L2 and each gather of a sparsely used column fetches a
-// 32-byte sector for 4 useful bytes, so that pass is bound by L2-to-SM
-// traffic, far below HBM speed.
+// Backward product g = A^T r (row panels).  The reference multiplies its
+// transposed copy (crs_matrix.hpp:356-412 builds it, gradient_descent.hpp:211
+// multiplies it with dloss), and so does the plain path here: every nonzero
+// of A^T gathers r[source row].  With millions of rows r sits in L2 and each
+// gather of a sparsely used column fetches a 32-byte sector for 4 useful
+// bytes, so that pass is bound by L2-to-SM traffic, far below HBM speed.
+// The row-panel layout regroups the columns that occur in most stretches of
+// rows.  A's rows are cut into panels of `rows` consecutive rows.  A CTA
+// copies one panel's slice of r into shared memory and walks the panel's
+// entries of the hot columns in (column, row) order, gathering from shared
+// memory; each (panel, hot column) pair gives one FP32 partial sum ("panel
+// row" q = panel * nhot + h).  g[hot column] is the compensated sum of its
+// partials in a fixed order.  Columns with fewer entries keep their rows in
+// a transposed CRS of their own (the hot rows emptied), multiplied by the
+// plain CRS kernel first.
 //
-// This layout regroups the columns that occur in most stretches of rows.  A's
-// rows are cut into panels of `rows` consecutive rows.  A CTA copies one
-// panel's slice of r into shared memory with coalesced loads and then walks
-// the panel's entries of the hot columns in (column, row) order, gathering
-// from shared memory; each (panel, hot column) pair gives one FP32 partial sum
-// ("panel row" q = panel * nhot + h).  g[hot column] is the compensated sum
-// of its partials in a fixed order.  Columns with fewer entries keep their rows in a
-// transposed CRS of their own (the hot rows emptied), multiplied by the plain
-// CRS kernel first.  Every sum has a fixed order, so the result is the same
-// on every run.
+// Forward product A w (forward head).  The entries of A's most frequent
+// columns form a CRS of their own with 2-byte column slots; every CTA stages
+// w at those columns once and sums its share of the rows' head entries with
+// the same kernel; the rest of each row goes through the plain CRS kernel,
+// whose logistic epilogue adds the head partial (crs_matrix.hpp:1505-1516 is
+// the product, gradient_descent.hpp:227-240 and gradient.hpp:15-53 the
+// epilogue).
+//
+// Every sum has a fixed order, so results are the same on every run.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -750,26 +759,27 @@ template <class VT>
 void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
   constexpr int threads = kPanelWarps * 32;
   auto kfn = k_panel<VT>;
-  // the attribute once, at the device's limit (row panels and the forward
-  // head ask for different sizes call after call); resident CTAs per SM for
-  // the sizes seen so far
-  static bool attr = false;
-  static std::vector<std::pair<int, int>> blocks_for;
+  // the attribute once per device, at the device's limit (row panels and
+  // the forward head ask for different sizes call after call); resident
+  // CTAs per SM for the (device, size) pairs seen so far
+  static std::vector<int> attr_set;
+  static std::vector<std::pair<long long, int>> blocks_for;
   const int smem = panel_smem_bytes<VT>(rows);
-  if (!attr) {
+  if (std::find(attr_set.begin(), attr_set.end(), c->device) == attr_set.end()) {
     int optin = 0;
     FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     FVG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    attr = true;
+    attr_set.push_back(c->device);
   }
+  const long long key = ((long long)c->device << 32) | (unsigned)smem;
   int blocks = 0;
   for (auto& e : blocks_for)
-    if (e.first == smem) blocks = e.second;
+    if (e.first == key) blocks = e.second;
   if (!blocks) {
     int nb = 0;
     FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, threads, smem));
     blocks = std::max(1, nb);
-    blocks_for.push_back({smem, blocks});
+    blocks_for.push_back({key, blocks});
   }
   const i64 nunits = (k.npanels + k.group - 1) / k.group;
   const int grid = (int)std::max<i64>(1, std::min<i64>(nunits, (i64)blocks * c->num_sms));
