@@ -281,3 +281,27 @@ def test_head_lbfgs_close_to_oracle(ctx):
         r = fv.logreg_lbfgs(A, label, storage=storage, **kw)
         assert abs(r["loss"] - ro["loss"]) <= 1e-3 * abs(ro["loss"]), storage
     assert A.head_info()[0] == 500
+
+
+@pytest.mark.parametrize("master", ["f32", "bf16"])
+def test_panels_and_head_on_lower_precision_uploads(ctx, master):
+    # matrices uploaded with FP32 or BF16 values: the panel, cold, head and tail
+    # copies are filled from that plane (their FP32 plane converted from BF16)
+    a, label = _zipf(24000, 1500, seed=31)
+    ar = _rounded(a, master)
+    if master == "f32":
+        vals = ar.val.astype(np.float32)
+    else:
+        vals = (ar.val.astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
+    B = ctx.matrix(a.m, a.n, ar.off, ar.idx, vals)
+    B.set_panels(512, 1.0)
+    B.set_head(300)
+    rng = np.random.default_rng(32)
+    storages = ("f32",) if master == "f32" else ("bf16", "f32")
+    for storage in storages:
+        r = rng.standard_normal(a.m).astype(np.float32)
+        ref = oracle.spmv(oracle.transpose(ar), r.astype(np.float64))
+        got = B.trans_mv(r, storage=storage, vec="f32").astype(np.float64)
+        assert np.all(np.abs(got - ref) <= 2e-5 * (_colabs(ar, r.astype(np.float64)) + 1e-30)), storage
+        _eval_check(B, ar, label, storage, rng)
+    assert B.panel_info()[2] > 0 and B.head_info()[0] == 300
