@@ -36,13 +36,18 @@ sys.path.insert(0, ROOT)
 METRIC = "sparse LogReg L-BFGS iters/s + SpMV HBM GB/s: BF16/batched vs FP64 GPU, same loss"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # dram__bytes_read.sum + dram__bytes_write.sum over the algorithmic bytes of
-# the same pass, from ncu captures on the 1,000,000-row version of the
-# benchmark matrix (BF16 values, all 1,000,000 columns): pass 1 (k_crs)
-# 375.52 MB / 380.01 MB; pass 2 with the row-panel layout (cold k_crs +
-# k_panel + k_panel_colsum) 288.54 MB / 376.01 MB — below the algorithmic
-# bytes because panel rows are stored as 2-byte ids; pass 2 on the plain
-# transposed CRS 373.51 MB / 376.0 MB.
-NCU_TRAFFIC_RATIO = {"pass1": 375.52 / 380.01, "pass2": 288.54 / 376.01, "pass2_plain": 373.51 / 376.0}
+# the same pass (the CRS formulas of eval_bytes), from ncu captures of the
+# benchmark matrix.  BF16 values, the 1,000,000-row version (all 1,000,000
+# columns): pass 1 with the forward head (k_panel + tail k_crs + k_finalize)
+# 285.42 MB / 380.01 MB; pass 2 with the row panels (rare-column k_crs +
+# k_panel + k_panel_colsum) 288.54 MB / 376.01 MB.  FP32 values, full size:
+# pass 1 4060.5 MB / 4964.0 MB, pass 2 4150.6 MB / 4852.0 MB.  Both passes move
+# less than their algorithmic bytes: panel rows and head columns are stored
+# as 2-byte ids.  The plain CRS kernel over whole rows (head and panels off):
+# pass 1 375.52 MB / 380.01 MB, pass 2 373.51 MB / 376.0 MB (BF16, 1,000,000 rows).
+NCU_TRAFFIC_RATIO = {"pass1": 285.42 / 380.01, "pass2": 288.54 / 376.01,
+                     "pass1_f32": 4060.5 / 4964.0, "pass2_f32": 4150.6 / 4852.0,
+                     "pass1_plain": 375.52 / 380.01, "pass2_plain": 373.51 / 376.0}
 
 
 def load_peak():
@@ -178,6 +183,7 @@ def run_gpu(args):
     A.add_storage("bf16")
     A.add_storage("f32")
     panel_info = A.panel_info()
+    head_info = A.head_info()
     # initModel overload with zero weights: the default all-ones start makes
     # the reference's L-BFGS exhaust its line search and blow up on this data
     kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, storage=args.storage, w0=np.zeros(n))
@@ -232,9 +238,11 @@ def run_gpu(args):
     # bytes from a 1/10-row ncu capture of the same kernels (BF16 values;
     # 6.0e7 nonzeros, 1,000,000 columns), applied to this run's launches
     ratio = dict(NCU_TRAFFIC_RATIO)
+    if not head_info[0]:
+        ratio["pass1"] = ratio["pass1_f32"] = ratio["pass1_plain"]
     if not panel_info[0]:
-        ratio["pass2"] = ratio["pass2_plain"]
-    traffic = (sum(ratio[k[:5]] * alg[k] * prof[k][1] for k in prof) / spmv_n
+        ratio["pass2"] = ratio["pass2_f32"] = ratio["pass2_plain"]
+    traffic = (sum(ratio[k] * alg[k] * prof[k][1] for k in prof) / spmv_n
                if spmv_n and args.storage == "bf16" else None)
 
     # the same training at the other precisions on the same data: iters/s and
@@ -365,7 +373,8 @@ def run_gpu(args):
                    "storage": args.storage, "l2_flush": "inputs larger than L2 (A is %.1f GB)" % (
                        nnz * 12 / 1e9), "parallelism": "replicas" if world > 1 else "single GPU",
                    "backward_panels": {"rows": panel_info[0], "panels": panel_info[1], "hot_columns": panel_info[2],
-                                       "hot_entries": panel_info[3]}},
+                                       "hot_entries": panel_info[3]},
+                   "forward_head": {"columns": head_info[0], "entries": head_info[1]}},
         "final_loss": r["loss"], "iterations_per_run": r["n_iter"],
         # loss/gradient evaluations (one pass 1 each; line-search trials included)
         "evaluations_per_s": (prof["pass1"][1] + prof["pass1_f32"][1]) * world / (ms / 1e3),
@@ -376,8 +385,8 @@ def run_gpu(args):
                                 "k_crs (pass1 A*w + logistic epilogue, pass2 A^T*r)"),
                      "algorithmic_bytes_per_launch": alg_total / max(spmv_n, 1), "launches": spmv_n,
                      "kernel_ms": spmv_ms,
-                     "traffic_source": "ncu dram bytes / algorithmic bytes on a 1/10-row capture, x this run's "
-                                       "algorithmic bytes per launch",
+                     "traffic_source": "ncu dram bytes / algorithmic bytes per pass (BF16: 1/10-row capture; "
+                                       "FP32: full-size capture), x this run's algorithmic bytes per launch",
                      "passes": {k: {"launches": prof[k][1], "ms_avg": prof[k][0] / max(prof[k][1], 1),
                                     "gbs": alg[k] * prof[k][1] / max(prof[k][0], 1e-9) / 1e6}
                                 for k in prof if prof[k][1]}},
