@@ -218,6 +218,19 @@ __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i
 // with int32 column ids whose pass adds the head partial before the
 // logistic epilogue.
 
+// sort keys of the head selection: decreasing count (31-bit), the column
+__global__ void k_head_keys(const i32* __restrict__ toff, i64 n, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ cols) {
+  PGRID_STRIDE(j, n) {
+    keys[j] = 0x7fffffffu - (uint32_t)(toff[j + 1] - toff[j]);
+    cols[j] = (uint32_t)j;
+  }
+}
+
+__global__ void k_head_slots(const uint32_t* __restrict__ cols, i64 H, i32* __restrict__ slot) {
+  PGRID_STRIDE(i, H) slot[cols[i]] = (i32)i;
+}
+
 // per row: entries in head columns (slot >= 0) and in the tail
 __global__ void k_head_counts(const i32* __restrict__ off, const i32* __restrict__ idx, i64 m,
                               const i32* __restrict__ slot, i64* __restrict__ hcnt, i64* __restrict__ tcnt) {
@@ -804,34 +817,25 @@ std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS&
   const i64 grid = c->num_sms;  // one CTA (one stretch of rows) per SM
   if (!forced && m < 64 * grid * kPanelWarps) return nullptr;
   const i64 H = std::min<i64>(n, forced ? force_cols : cap);
-  // column counts from the transposed offsets; the H largest
-  std::vector<i32> toff((size_t)n + 1);
-  FVG_CUDA(cudaMemcpyAsync(toff.data(), at.off.p, sizeof(i32) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));
-  std::vector<i32> cnt((size_t)n);
-  for (i64 j = 0; j < n; j++) cnt[(size_t)j] = toff[(size_t)j + 1] - toff[(size_t)j];
-  std::vector<i32> srt(cnt);
-  std::nth_element(srt.begin(), srt.begin() + (H - 1), srt.end(), std::greater<i32>());
-  const i32 T = srt[(size_t)(H - 1)];  // the H-th largest count
-  i64 above = 0;
-  for (i64 j = 0; j < n; j++) above += cnt[(size_t)j] > T;
-  std::vector<i32> slot((size_t)n, -1), xmap;
-  xmap.reserve((size_t)H);
-  i64 ties = H - above, E = 0;
-  for (i64 j = 0; j < n; j++) {
-    const i32 v = cnt[(size_t)j];
-    if (v > T || (v == T && ties > 0)) {
-      if (v == T) ties--;
-      slot[(size_t)j] = (i32)xmap.size();
-      xmap.push_back((i32)j);
-      E += v;
-    }
-  }
-  if (!forced && (double)E < 0.5 * (double)nnz) return nullptr;
+  // the H largest column counts (from the transposed offsets), on the
+  // device: a stable sort of the columns by decreasing count (ties keep
+  // column order), the first H take slots 0..H-1
+  DBuf keys, cols, dslot;
+  keys.alloc(sizeof(uint32_t) * n, c->stream);
+  cols.alloc(sizeof(uint32_t) * n, c->stream);
+  dslot.alloc(sizeof(i32) * n, c->stream);
+  k_head_keys<<<grid_n(n), 256, 0, c->stream>>>(at.off.as<i32>(), n, keys.as<uint32_t>(), cols.as<uint32_t>());
+  check_launch("head_keys");
+  count_launch(c);
+  radix_sort_pairs(c, keys.as<uint32_t>(), cols.as<uint32_t>(), n, 31);
+  fill_i32(c, dslot.as<i32>(), -1, n);
+  k_head_slots<<<grid_n(H), 256, 0, c->stream>>>(cols.as<uint32_t>(), H, dslot.as<i32>());
+  check_launch("head_slots");
+  count_launch(c);
   auto hd = std::make_unique<DevPanels>();
   hd->shared = true;
   hd->master = master;
-  hd->m = H;  // the staged slice: w at the head columns
+  hd->m = H;  // the staged slice: w at the head columns (slot order)
   hd->n = n;
   hd->rows = H;
   // stretches of at most ~4096 rows, a whole number of them per CTA: the
@@ -841,10 +845,7 @@ std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS&
   hd->npanels = (m + hd->nhot - 1) / hd->nhot;
   const i64 np = hd->npanels, chunk = hd->nhot, Q = np * chunk;
   hd->hot_cols.alloc(sizeof(i32) * std::max<i64>(H, 1), c->stream);
-  FVG_CUDA(cudaMemcpyAsync(hd->hot_cols.p, xmap.data(), sizeof(i32) * H, cudaMemcpyHostToDevice, c->stream));
-  DBuf dslot;
-  dslot.alloc(sizeof(i32) * n, c->stream);
-  FVG_CUDA(cudaMemcpyAsync(dslot.p, slot.data(), sizeof(i32) * n, cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(hd->hot_cols.p, cols.p, sizeof(i32) * H, cudaMemcpyDeviceToDevice, c->stream));
   DBuf hcnt, tcnt, hoff, tof;
   hcnt.alloc(sizeof(i64) * m, c->stream);
   tcnt.alloc(sizeof(i64) * m, c->stream);
@@ -860,6 +861,7 @@ std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS&
   FVG_CUDA(cudaMemcpyAsync(&tot[0], hoff.as<i64>() + m, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaMemcpyAsync(&tot[1], tof.as<i64>() + m, sizeof(i64), cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));
+  if (!forced && (double)tot[0] < 0.5 * (double)nnz) return nullptr;  // most entries outside the head
   hd->E = tot[0];
   hd->poff.alloc(sizeof(i32) * (Q + 1), c->stream);
   k_head_off<<<grid_n(Q + 1), 256, 0, c->stream>>>(hoff.as<i64>(), m, Q, hd->poff.as<i32>());
