@@ -161,7 +161,7 @@ struct V4 { double a, b, c, d; };
 
 __device__ __forceinline__ i64 hslot(int rear, int i, int h) { return (i64)((rear + i) % h); }
 
-// two-loop recursion, first loop (see the single-model k_down)
+// two-loop recursion, first loop (as in the single-model k_direction)
 __global__ void __launch_bounds__(kBT, 4) kb_down(int i, int kh, int rear, const double* __restrict__ G,
                                                double* __restrict__ Q, const double* __restrict__ S,
                                                const double* __restrict__ Y, BArgs a) {
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kBT, 4) kb_down(int i, int kh, int rear, const
   });
 }
 
-// second loop (see k_up)
+// second loop (as in the single-model k_direction)
 __global__ void __launch_bounds__(kBT, 4) kb_up(int i, int kh, int rear, const double* __restrict__ Q,
                                              double* __restrict__ Z, const double* __restrict__ S,
                                              const double* __restrict__ Y, BArgs a) {
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kBT, 4) kb_up(int i, int kh, int rear, const d
   });
 }
 
-// step = -z, or the no-history step (see k_step)
+// step = -z, or the no-history step (as in k_direction)
 __global__ void __launch_bounds__(kBT, 4) kb_step(int kh, int rear, const double* __restrict__ G,
                                                const double* __restrict__ Z, double* __restrict__ STEP,
                                                const double* __restrict__ S, BArgs a) {
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kBT, 4) kb_step(int kh, int rear, const double
   });
 }
 
-// max-scaled step norm, uphill flip, factors of the 10 trials (see k_step_norm)
+// max-scaled step norm, uphill flip, factors of the 10 trials (as in k_direction)
 __global__ void __launch_bounds__(kBT, 4) kb_step_norm(const double* __restrict__ STEP, BArgs a) {
   BCOL;
   const bool act = on && a.st[j].active;
