@@ -124,15 +124,16 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
   }
 }
 
-// Work items of the panel rows, one warp per panel, with the CRS schedule's
-// packing rules (tiles of short rows within kWarpTile entries, kTileRows rows
-// and kLaneWork products per lane; longer rows in pieces cut at 8-element
-// boundaries).  The greedy packing is sequential: every lane runs it on the
-// same offsets (loaded 32 at a time and broadcast by shuffles, so control
-// flow is uniform) and lane 0 writes.  Pass 0 counts each panel's items,
-// long rows and pieces; pass 1 writes them at the scanned offsets `base`
-// (panel-major: a panel's items, long rows and pieces are contiguous and
-// numbered globally).
+// Work items of a CRS, one warp per chunk of rows (chunk p: piece p % sub of
+// the stretch of nhot rows p / sub), with the CRS schedule's packing rules
+// (tiles of short rows within `tile` entries, kTileRows rows and kLaneWork
+// products per lane; longer rows in pieces cut at 8-element boundaries).  The
+// greedy packing is sequential: every lane runs it on the same offsets
+// (loaded 32 at a time and broadcast by shuffles, so control flow is
+// uniform); lane 0 writes the tiles, all lanes write a long row's pieces.
+// Pass 0 counts each chunk's items, long rows and pieces; pass 1 writes them
+// at the scanned offsets `base` (chunk-major: a chunk's items, long rows and
+// pieces are contiguous and numbered globally).
 __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 sub, i64 np, int tile, int write,
                              i32* __restrict__ cnt, const i32* __restrict__ base, Item* __restrict__ items,
                              i32* __restrict__ lrows, i32* __restrict__ lpiece0) {
@@ -364,16 +365,18 @@ template <class VT> struct PanelSmem {
   static constexpr int kStatic = 16 * kPanelWarps + kPanelWarps * kWarpB;  // mbarriers, then the warps' areas
 };
 
-// One CTA of kPanelWarps warps per SM takes panels b, b+G, ...  Per panel:
-// r's slice into shared memory; then the warps walk the panel's work items
-// (tiles of short panel rows, pieces of long ones; warp w takes items w,
-// w+W, ...).  Per item a bulk copy stages the entries in the warp's buffer
-// (the copies of the other 31 warps cover its latency); the products with r
-// gathered from shared memory overwrite the staged entries, and each row is
-// added by 1..32 lanes in a fixed order.  After a barrier the pieces of long
-// panel rows are added in piece order.  (Measured on GB300 against a
-// double-buffered variant with 16 warps and a separate product buffer: this
-// one is 10% faster on the 10M x 1M benchmark matrix.)
+// One CTA of kPanelWarps warps per SM takes units of `group` consecutive
+// panels: b, b+G, ...  Per unit: the vector's slice into shared memory (row
+// panels: r's rows of the panel; forward head: w at the head columns, staged
+// once); then the warps walk the unit's work items (tiles of short rows,
+// pieces of long ones; warp w takes items w, w+W, ...).  Per item a bulk copy
+// stages the entries in the warp's buffer (the copies of the other 31 warps
+// cover its latency); the products with the vector gathered from shared
+// memory overwrite the staged entries, and each row is added by 1..32 lanes
+// in a fixed order.  After a barrier the pieces of long rows are added in
+// piece order.  (Measured on GB300 against a double-buffered variant with 16
+// warps and a separate product buffer: this one is 10% faster on the 10M x 1M
+// benchmark matrix.)
 template <class VT>
 __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
   using SM = PanelSmem<VT>;
