@@ -93,9 +93,22 @@ def test_glm_eval_reduced_precision(ctx, loss):
     A = ctx.matrix(6000, n, off, idx, val)
     w = np.random.default_rng(9).standard_normal(n) * 0.2
     g64, l64 = fv.glm_eval(A, t, w, b=0.3, intercept=True, loss=loss, epsilon=EPS[loss])
+    plain = {}
     for storage in ("f32", "bf16"):
         g, lo = fv.glm_eval(A, t, w, b=0.3, intercept=True, storage=storage, loss=loss, epsilon=EPS[loss])
         assert abs(lo - l64) <= 1e-5 * abs(l64), (loss, storage)
+        plain[storage] = g
+    # the same through the forward head and the row-panel backward product
+    # (forced on this small matrix): the loss kind rides in the tail pass's
+    # epilogue
+    A.set_panels(512, 1.0)
+    A.set_head(300)
+    for storage in ("f32", "bf16"):
+        g, lo = fv.glm_eval(A, t, w, b=0.3, intercept=True, storage=storage, loss=loss, epsilon=EPS[loss])
+        assert abs(lo - l64) <= 1e-5 * abs(l64), (loss, storage, "head/panels")
+        gp = plain[storage]
+        assert np.max(np.abs(g - gp)) <= 1e-4 * max(1.0, np.max(np.abs(gp))), (loss, storage, "head/panels")
+    assert A.head_info()[0] == 300 and A.panel_info()[2] > 0
 
 
 @pytest.mark.parametrize("loss,reg,fmt", [("linear", "ZERO", "CRS"), ("linear", "L1", "CRS"), ("linear", "L2", "CRS"),
