@@ -1,0 +1,38 @@
+"""Host-side pieces of bench.py that need no GPU: the algorithmic-byte
+formulas the roofline uses, the --panels option and the traffic ratios."""
+import bench
+
+
+def test_eval_bytes_formula():
+    # A and A^T once each (value + 4-byte id per nonzero), row offsets, the
+    # input vector of each pass, labels (FP64), r written then read, g (FP64)
+    m, n, nnz = 10, 7, 40
+    p1, p2 = bench.eval_bytes(m, n, nnz, 2, 4)
+    assert p1 == nnz * 6 + (m + 1) * 4 + n * 4 + m * 8 + m * 4
+    assert p2 == nnz * 6 + (n + 1) * 4 + m * 4 + n * 8
+
+
+class _FakeMatrix:
+    def __init__(self):
+        self.calls = []
+
+    def set_panels(self, rows=-1, min_per_panel=0.0):
+        self.calls.append((rows, min_per_panel))
+
+
+def test_panels_option():
+    A = _FakeMatrix()
+    bench.set_panels(A, "auto")
+    assert A.calls == []
+    bench.set_panels(A, "off")
+    bench.set_panels(A, "8192")
+    bench.set_panels(A, "4096:1.5")
+    assert A.calls == [(0, 0.0), (8192, 0.0), (4096, 1.5)]
+
+
+def test_traffic_ratios():
+    r = bench.NCU_TRAFFIC_RATIO
+    for k in ("pass1", "pass2", "pass1_f32", "pass2_f32", "pass1_plain", "pass2_plain"):
+        assert 0.5 < r[k] <= 1.0, k
+    # 2-byte panel rows / head columns: the layouts move fewer bytes than the plain kernel
+    assert r["pass1"] < r["pass1_plain"] and r["pass2"] < r["pass2_plain"]
