@@ -28,6 +28,7 @@
 // Every sum has a fixed order, so results are the same on every run.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "device_common.cuh"
@@ -778,9 +779,11 @@ void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
   // the attribute once per device, at the device's limit (row panels and
   // the forward head ask for different sizes call after call); resident
   // CTAs per SM for the (device, size) pairs seen so far
+  static std::mutex mu;  // contexts of different host threads launch concurrently
   static std::vector<int> attr_set;
   static std::vector<std::pair<long long, int>> blocks_for;
   const int smem = panel_smem_bytes<VT>(rows);
+  std::unique_lock<std::mutex> lock(mu);
   if (std::find(attr_set.begin(), attr_set.end(), c->device) == attr_set.end()) {
     int optin = 0;
     FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
@@ -797,6 +800,7 @@ void launch_panel(fvg_ctx* c, const PanK& k, i64 rows) {
     blocks = std::max(1, nb);
     blocks_for.push_back({key, blocks});
   }
+  lock.unlock();
   const i64 nunits = (k.npanels + k.group - 1) / k.group;
   const int grid = (int)std::max<i64>(1, std::min<i64>(nunits, (i64)blocks * c->num_sms));
   kfn<<<grid, threads, smem, c->stream>>>(k);
