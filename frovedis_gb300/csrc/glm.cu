@@ -860,7 +860,6 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   const bool mixed = storage != FVG_F64;
   std::vector<double> rms_hist;
   i64 i = 1;
-  double last_rms = 0;
   for (; i <= p->num_iteration; i++) {
     {
       ProfScope ps(c, P_LBFGS);
@@ -895,7 +894,6 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
       count_launch(c);
     }
     loss = newloss;
-    last_rms = rms_t;
     if (p->trace) {
       double fac = 0;
       FVG_CUDA(cudaMemcpyAsync(&fac, &st->factor[std::min(j, 10)], sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -926,7 +924,6 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   }
   *n_iter = (i == p->num_iteration + 1) ? p->num_iteration : i;
   *loss_out = loss;
-  (void)last_rms;
   FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(b_h, &st->b[0], sizeof(double), cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));
