@@ -36,3 +36,37 @@ def test_traffic_ratios():
         assert 0.5 < r[k] <= 1.0, k
     # 2-byte panel rows / head columns: the layouts move fewer bytes than the plain kernel
     assert r["pass1"] < r["pass1_plain"] and r["pass2"] < r["pass2_plain"]
+
+
+def _replica(rank, port, out):
+    import os
+    os.environ.update({"WORLD_SIZE": "2", "RANK": str(rank), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    import bench as b
+    world, r, local = b.dist_setup(None)
+    b.barrier(world)
+    # each replica's step time; the job's time is the slowest replica's
+    t = b.allmax(world, 10.0 + rank)
+    out.put((r, world, local, t))
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def test_replicas_gloo_two_ranks():
+    # the bench's N > 1 path: replicas (nothing sharded), a barrier and the
+    # max over ranks of the timed region, here on two gloo ranks on the CPU
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    ps = [ctx.Process(target=_replica, args=(r, port, out)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(out.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, 2, 0, 11.0), (1, 2, 1, 11.0)]
