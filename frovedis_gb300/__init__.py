@@ -28,7 +28,8 @@ FORMATS = {"CRS": CRS, "JDS": JDS, "ELL": ELL, "HYBRID": HYBRID}
 REG = {"ZERO": 0, "L1": 1, "L2": 2}
 # fvg_loss: the GLM family's compute_dloss kinds (ml/glm/gradient.hpp)
 LOSS = {"logistic": 0, "linear": 1, "hinge": 2, "eps": 3, "sqeps": 4}
-DTYPES = {"f64": F64, "f32": F32, "bf16": BF16}
+SPLIT = 3
+DTYPES = {"f64": F64, "f32": F32, "bf16": BF16, "split": SPLIT}
 
 _p = C.c_void_p
 _i64 = C.c_int64
@@ -64,7 +65,7 @@ EXPORTS = [
     "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
     "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info", "fvg_matrix_set_head",
-    "fvg_matrix_head_info",
+    "fvg_matrix_head_info", "fvg_ctx_set_wait_limit", "fvg_debug_inject_alloc_failure",
 ]
 
 _lib = None
@@ -94,6 +95,8 @@ def load(build_if_needed: bool = True):
         "fvg_ctx_get_profile": ([_p, C.c_char_p, C.POINTER(_dbl), C.POINTER(_i64)], _int),
         "fvg_ctx_reset_profile": ([_p], _int),
         "fvg_ctx_kernel_launches": ([_p], _i64),
+        "fvg_ctx_set_wait_limit": ([_p, _i64], _int),
+        "fvg_debug_inject_alloc_failure": ([_i64], None),
         "fvg_matrix_create_crs": ([_p, _i64, _i64, _p, _p, _p, _int, _int, C.POINTER(_p)], _int),
         "fvg_matrix_destroy": ([_p], None),
         "fvg_matrix_info": ([_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)], _int),
@@ -210,6 +213,11 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.fvg_ctx_kernel_launches(self.h))
+
+    def set_wait_limit(self, polls=-1):
+        """Poll budget of the kernels' bounded device-side waits (< 0: the
+        defaults; 0: a wait that is not complete at once gives up)."""
+        self.check(self.L.fvg_ctx_set_wait_limit(self.h, int(polls)))
 
     def matrix(self, m, n, off, idx, val, on_device=False):
         return Matrix(self, m, n, off, idx, val, on_device=on_device)

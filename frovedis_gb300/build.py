@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfvg.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["util.cu", "build.cu", "spmv.cu", "spmm.cu", "glm.cu", "batched.cu", "multinomial.cu", "loader.cu", "capi.cu", "noalloc.cu", "panel.cu"]
+SOURCES = ["util.cu", "build.cu", "spmv.cu", "spmm.cu", "glm.cu", "batched.cu", "multinomial.cu", "loader.cu", "capi.cu", "noalloc.cu", "panel.cu", "split.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE]
@@ -31,7 +31,7 @@ def nvcc() -> str:
 
 def _deps():
     files = [os.path.join(CSRC, s) for s in SOURCES]
-    files += [os.path.join(CSRC, "fvg_internal.cuh"), os.path.join(CSRC, "device_common.cuh"), os.path.join(INCLUDE, "fvg.h"), __file__]
+    files += [os.path.join(CSRC, "fvg_internal.cuh"), os.path.join(CSRC, "device_common.cuh"), os.path.join(CSRC, "df64.cuh"), os.path.join(INCLUDE, "fvg.h"), __file__]
     return files
 
 

@@ -592,6 +592,7 @@ void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const
     crs_build_transpose(c, M->A, *M->AT, M->master);
   }
   int storage = p->storage;
+  if (storage == FVG_SPLIT) fail(FVG_ERR_UNSUPPORTED, "split storage is offered by the L-BFGS trainers, single evaluations and the products");
   const bool mixed = storage != FVG_F64;
 
   DBuf label, sw;

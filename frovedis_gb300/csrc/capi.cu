@@ -108,6 +108,7 @@ FVG_API fvg_status fvg_ctx_create(int device, fvg_ctx** out) {
       cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
     prof_create(c);
+    df64_init(c);
     *out = c;
     return FVG_OK;
   } catch (const fvg::Error& e) {
@@ -190,6 +191,14 @@ FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* c) {
 }
 
 FVG_API int64_t fvg_ctx_kernel_launches(fvg_ctx* c) { return c ? c->launches : -1; }
+
+FVG_API fvg_status fvg_ctx_set_wait_limit(fvg_ctx* c, int64_t polls) {
+  if (!c) return FVG_ERR_INVALID_ARG;
+  c->wait_limit = polls < 0 ? -1 : std::min<int64_t>(polls, 0xffffffffll);
+  return FVG_OK;
+}
+
+FVG_API void fvg_debug_inject_alloc_failure(int64_t after) { inject_alloc_failure(after < 0 ? -1 : after); }
 
 // ------------------------------------------------------------------ matrix
 FVG_API fvg_status fvg_matrix_create_crs(fvg_ctx* c, int64_t num_row, int64_t num_col, const int32_t* off,
@@ -298,6 +307,7 @@ FVG_API fvg_status fvg_matrix_prepare(fvg_ctx* c, fvg_matrix* M, fvg_format fmt,
   API_BEGIN
   own(c, M);
   prepare(c, M, fmt, with_transpose != 0);
+  if (with_transpose && M->A.lo.p && M->AT) crs_ensure_split(c, *M->AT, M->master);
   // a matrix that already holds FP32 / BF16 values gets its row-panel
   // backward layout and its forward head now rather than at the first product
   if (with_transpose && (fmt == FVG_CRS || fmt == FVG_ELL) && (M->A.val[FVG_F32].p || M->A.val[FVG_BF16].p)) {
@@ -362,6 +372,11 @@ FVG_API fvg_status fvg_matrix_panel_info(fvg_ctx* c, fvg_matrix* M, int64_t* inf
 }
 
 static void ensure_plane_all(fvg_ctx* c, fvg_matrix* M, int dt) {
+  if (dt == FVG_SPLIT) {  // the CRS layouts only (the products run on them)
+    crs_ensure_split(c, M->A, M->master);
+    if (M->AT) crs_ensure_split(c, *M->AT, M->master);
+    return;
+  }
   crs_ensure_plane(c, M->A, dt, M->master);
   if (M->AT) crs_ensure_plane(c, *M->AT, dt, M->master);
   if (M->ell) ensure_plane_generic(c, M->ell->val, M->ell->m * M->ell->width, dt, M->master);
@@ -378,7 +393,7 @@ FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* c, fvg_matrix* M, fvg_dtype s
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
-  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  need(storage >= FVG_F64 && storage <= FVG_SPLIT, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   ensure_plane_all(c, M, storage);
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -387,6 +402,7 @@ FVG_API fvg_status fvg_matrix_add_storage(fvg_ctx* c, fvg_matrix* M, fvg_dtype s
 static int64_t crs_bytes(const DevCRS& a) {
   int64_t b = (int64_t)a.off.bytes + (int64_t)a.idx.bytes;
   for (auto& v : a.val) b += (int64_t)v.bytes;
+  b += (int64_t)a.lo.bytes;
   for (auto& s : a.sched)
     if (s) b += (int64_t)(s->items.bytes + s->long_rows.bytes + s->long_piece0.bytes);
   return b;
@@ -606,15 +622,47 @@ static void stage_out_finish(fvg_ctx* c, VecStage& v, void* y, int64_t ny, int v
 }
 
 static void check_vec_args(int storage, int vec_dt) {
-  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  need(storage >= FVG_F64 && storage <= FVG_SPLIT, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   need(vec_dt == FVG_F64 || vec_dt == FVG_F32, FVG_ERR_INVALID_ARG, "vectors must be FP64 or FP32");
   need(!(storage == FVG_F64 && vec_dt != FVG_F64), FVG_ERR_INVALID_ARG, "FP64 values need FP64 vectors");
+  need(!(storage == FVG_SPLIT && vec_dt != FVG_F64), FVG_ERR_INVALID_ARG, "split storage needs FP64 vectors");
+}
+
+// split storage: y = A x or A^T x over the CRS layouts in df64 arithmetic
+static void run_product_split(fvg_ctx* c, fvg_matrix* M, int fmt, const void* x, void* y, bool trans, bool on_dev) {
+  need(fmt == FVG_CRS, FVG_ERR_UNSUPPORTED, "split storage runs on the CRS format");
+  prepare(c, M, fmt, trans);
+  ensure_plane_all(c, M, FVG_SPLIT);
+  const int64_t nx = trans ? M->A.m : M->A.n, ny = trans ? M->A.n : M->A.m;
+  DBuf xb, x2, yb;
+  const double* dx = (const double*)x;
+  if (!on_dev) {
+    xb.alloc(sizeof(double) * std::max<int64_t>(nx, 1), c->stream);
+    if (nx) FVG_CUDA(cudaMemcpyAsync(xb.p, x, sizeof(double) * nx, cudaMemcpyHostToDevice, c->stream));
+    dx = xb.as<double>();
+  }
+  x2.alloc(sizeof(float2) * std::max<int64_t>(nx, 1), c->stream);
+  split_vector(c, dx, x2.p, nx);
+  double* dy = (double*)y;
+  if (!on_dev) {
+    yb.alloc(sizeof(double) * std::max<int64_t>(ny, 1), c->stream);
+    dy = yb.as<double>();
+  }
+  crs_pass_split(c, trans ? *M->AT : M->A, x2.p, false, dy, nullptr, P_SPMV_CRS);
+  if (!on_dev && ny)
+    FVG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * ny, cudaMemcpyDeviceToHost, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  check_device_error(c);
 }
 
 static void run_product(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, int vec_dt, const void* x, void* y,
                         bool trans, bool on_dev) {
   check_vec_args(storage, vec_dt);
   need(fmt >= 0 && fmt <= 3, FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (storage == FVG_SPLIT) {
+    run_product_split(c, M, fmt, x, y, trans, on_dev);
+    return;
+  }
   prepare(c, M, fmt, trans);
   ensure_plane_all(c, M, storage);
   const int64_t nx = trans ? M->A.m : M->A.n, ny = trans ? M->A.n : M->A.m;
@@ -668,6 +716,7 @@ FVG_API fvg_status fvg_spmm(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_dtype
   API_BEGIN
   own(c, M);
   check_vec_args(storage, vec_dtype);
+  need(storage != FVG_SPLIT, FVG_ERR_UNSUPPORTED, "split storage is not offered by the SpMM");
   need(k >= 0, FVG_ERR_INVALID_ARG, "negative number of columns");
   need(fmt >= 0 && fmt <= 3, FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
   ensure_plane_all(c, M, storage);
@@ -829,7 +878,7 @@ FVG_API fvg_status fvg_logreg_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fv
   if (!c || !M || !grad || !loss || !weight) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
-  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  need(storage >= FVG_F64 && storage <= FVG_SPLIT, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss,
               FVG_LOSS_LOGISTIC, 0.0);
   check_device_error(c);
@@ -843,7 +892,7 @@ FVG_API fvg_status fvg_glm_eval(fvg_ctx* c, fvg_matrix* M, fvg_format fmt, fvg_d
   if (!c || !M || !grad || !loss_out || !weight) return FVG_ERR_INVALID_ARG;
   API_BEGIN
   own(c, M);
-  need(storage >= FVG_F64 && storage <= FVG_BF16, FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  need(storage >= FVG_F64 && storage <= FVG_SPLIT, FVG_ERR_INVALID_ARG, "unknown storage dtype");
   logreg_eval(c, M, fmt, storage, label, sample_weight, weight, intercept, intercept_on, grad, loss_out, loss,
               epsilon);
   check_device_error(c);

@@ -114,6 +114,7 @@ struct DevCRS {
   i64 m = 0, n = 0, nnz = 0;
   DBuf off, idx;  // int32
   DBuf val[3];    // indexed by fvg_dtype
+  DBuf lo;        // bf16 [nnz+kPad]: value - FP32 value (split storage; with val[FVG_F32])
   std::unique_ptr<Sched> sched[2];  // built once (slot 0)
   i64 max_row = 0;
 };
@@ -160,6 +161,7 @@ struct DevPanels {
   DBuf poff;                        // int32 [npanels*nhot + 1]
   DBuf prow;                        // uint16 [E + kPad]: row within the panel
   DBuf val[3];                      // [E + kPad] per dtype
+  DBuf lo;                          // bf16 [E + kPad]: residual of the FP32 values (split storage)
   DevCRS cold;                      // n rows, hot rows empty
   // work items over the panel rows, panel by panel (Item as in Sched)
   i64 nitems = 0, nlong = 0, npieces = 0;
@@ -202,6 +204,8 @@ struct fvg_ctx {
   // device error word: a kernel that must give up (a bounded wait that ran
   // out) sets a bit here instead of trapping; read after each call
   unsigned* dev_err = nullptr;
+  // poll budget of the bounded device-side waits (< 0: the defaults below)
+  int64_t wait_limit = -1;
 };
 
 struct fvg_matrix {
@@ -248,11 +252,21 @@ struct ProfScope {
 };
 inline void count_launch(fvg_ctx* c, int n = 1) { c->launches += n; }
 void check_launch(const char* what);
+// Default poll budgets of the bounded device-side waits: the L-BFGS
+// direction's grid barriers (2^24 polls of ~32 ns) and the panel kernels'
+// bulk-copy waits (2^22 polls); a context may lower them for testing.
+constexpr unsigned kBarrierPolls = 1u << 24;
+constexpr unsigned kCopyPolls = 1u << 22;
+inline unsigned barrier_polls(const fvg_ctx* c) { return c->wait_limit < 0 ? kBarrierPolls : (unsigned)c->wait_limit; }
+inline unsigned copy_polls(const fvg_ctx* c) { return c->wait_limit < 0 ? kCopyPolls : (unsigned)c->wait_limit; }
 // Reads (and clears) the device error word; fails when a kernel reported one.
 void check_device_error(fvg_ctx* c);
 
 // ------------------------------------------------------------ utilities
 int dtype_size(int dt);
+void inject_alloc_failure(long long after);
+// resident CTAs per SM of `kernel` on the current device (cached per device)
+int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem = 0);
 // exclusive scan of n int64 values in place (out has n+1 entries: out[n]=total)
 void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n);
 // stable LSD radix sort of (key,val) u32 pairs by the low `bits` bits of key
@@ -328,6 +342,32 @@ void head_ensure_plane(fvg_ctx* c, DevPanels& hd, int dt);
 i64 head_scratch_bytes(fvg_ctx* c, DevPanels& hd, int storage);
 void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, const LogregEpi& lr, void* scratch,
                       int prof_key);
+
+// ------------------------------------------------------- split storage
+// FP64 values kept as an FP32 plane plus a BF16 residual plane, multiplied
+// in double-FP32 arithmetic (split.cu).  Vectors are df pairs (float2).
+void df64_init(fvg_ctx* c);  // the exp table of the df64 math, once per device
+void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master);
+void split_vector(fvg_ctx* c, const double* x, void* y, i64 n);  // y: float2[n]
+i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a);
+// y = A x, x float2 pairs; y FP64 (y_df false) or float2 pairs
+void crs_pass_split(fvg_ctx* c, DevCRS& a, const void* x, bool y_df, void* y, void* scratch, int prof_key);
+struct GlmSplitArgs {
+  const void* lab = nullptr;  // float2[m]
+  const void* sw = nullptr;   // float2[m] or null
+  const double* intercept = nullptr;
+  int icpt = 0;
+  int kind = 0;
+  double eps = 0.0;
+  void* r = nullptr;          // float2[m]: dloss * sw
+  double* cta_part = nullptr; // [2 * glm_split_grid(m)]
+  unsigned* ticket = nullptr; // zero on entry, left zero
+  double* out = nullptr;      // [2]: loss, bias
+  double* grad_bias = nullptr;
+};
+int glm_split_grid(fvg_ctx* c, i64 m);
+// per-row loss/gradient over z = wtx (+ head) + intercept (float2 pairs)
+void glm_split_rows(fvg_ctx* c, const void* wtx, const void* head, i64 m, const GlmSplitArgs& e);
 
 // Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
 void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);

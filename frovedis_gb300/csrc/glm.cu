@@ -135,6 +135,7 @@ struct DirArgs {
   double* part;              // [2][2 * gridDim.x]
   unsigned long long* bar;   // barrier arrivals, zeroed before the launch
   unsigned* err;
+  unsigned limit;            // poll budget of each barrier wait
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -154,7 +155,7 @@ __device__ __forceinline__ void dir_sync(const DirArgs& d, int b, bool* dead) {
     const unsigned long long target = (unsigned long long)gridDim.x * (unsigned long long)(b + 1);
     if (!*dead) {
       for (unsigned it = 0; ld_acquire_u64(d.bar) < target; it++) {
-        if (it > (1u << 24)) {
+        if (it >= d.limit) {
           atomicOr(d.err, 4u);
           *dead = true;
           break;
@@ -479,6 +480,12 @@ struct Operand {
 };
 
 static void ensure_storage(fvg_ctx* c, Operand& o, int storage) {
+  if (storage == FVG_SPLIT) {
+    if (o.fmt != FVG_CRS) fail(FVG_ERR_UNSUPPORTED, "split storage runs on the CRS format");
+    if (o.A) crs_ensure_split(c, *o.A, o.master);
+    if (o.AT) crs_ensure_split(c, *o.AT, o.master);
+    return;
+  }
   if (o.A) crs_ensure_plane(c, *o.A, storage, o.master);
   if (o.AT) crs_ensure_plane(c, *o.AT, storage, o.master);
   if (o.H) {
@@ -515,6 +522,10 @@ struct Evaluator {
     sw = sw_;
     icpt = icpt_;
     ensure_storage(c, *op, storage);
+    if (storage == FVG_SPLIT) {
+      init_split();
+      return;
+    }
     // FP32 copies of labels / weights for the FP32-arithmetic epilogue
     label_f.alloc(sizeof(float) * std::max<i64>(op->m, 1), c->stream);
     convert_values(c, label, FVG_F64, label_f.p, FVG_F32, op->m);
@@ -535,6 +546,46 @@ struct Evaluator {
     }
     use_panels();
   }
+  // split storage: labels / weights as df pairs, the forward product per row
+  // as df pairs, r = dloss * sw as df pairs, the row kernel's partial sums
+  DBuf wtx2, gpart;
+  void init_split() {
+    const i64 m1 = std::max<i64>(op->m, 1);
+    label_f.alloc(sizeof(float2) * m1, c->stream);
+    split_vector(c, label, label_f.p, op->m);
+    if (sw) {
+      sw_f.alloc(sizeof(float2) * m1, c->stream);
+      split_vector(c, sw, sw_f.p, op->m);
+    }
+    r.alloc(sizeof(float2) * m1, c->stream);
+    wtx2.alloc(sizeof(float2) * m1, c->stream);
+    s1.alloc(crs_split_scratch_bytes(c, *op->A), c->stream);
+    s2.alloc(crs_split_scratch_bytes(c, *op->AT), c->stream);
+    const i64 g = glm_split_grid(c, op->m);
+    gpart.alloc(sizeof(double) * 2 * g + 256, c->stream);
+    FVG_CUDA(cudaMemsetAsync((char*)gpart.p + sizeof(double) * 2 * g, 0, 256, c->stream));
+  }
+  void eval_split(const void* x, const double* b, double* grad, double* out) {
+    const i64 g = glm_split_grid(c, op->m);
+    {
+      ProfScope ps(c, P_PASS1);
+      crs_pass_split(c, *op->A, x, true, wtx2.p, s1.p, P_NKEYS);
+      GlmSplitArgs e;
+      e.lab = label_f.p;
+      e.sw = sw ? sw_f.p : nullptr;
+      e.intercept = b;
+      e.icpt = icpt;
+      e.kind = loss;
+      e.eps = eps;
+      e.r = r.p;
+      e.cta_part = gpart.as<double>();
+      e.ticket = (unsigned*)((char*)gpart.p + sizeof(double) * 2 * g);
+      e.out = out;
+      e.grad_bias = grad + op->n;
+      glm_split_rows(c, wtx2.p, nullptr, op->m, e);
+    }
+    crs_pass_split(c, *op->AT, r.p, false, grad, s2.p, P_PASS2);
+  }
   // FP32 / BF16 values: the row-panel layout for the backward product when
   // the matrix has one (CRS and ELL operands share the transposed CRS), and
   // the forward head for the CRS forward product
@@ -542,7 +593,7 @@ struct Evaluator {
   DevPanels* HD = nullptr;
   DBuf s3, s4;
   void use_panels() {
-    if (storage == FVG_F64 || !op->M) return;
+    if (storage == FVG_F64 || storage == FVG_SPLIT || !op->M) return;
     if (!PT && op->AT) {
       PT = panels_for(c, op->M);
       if (PT) {
@@ -586,6 +637,10 @@ struct Evaluator {
     if (op->m == 0) {  // compute_gradient: empty data → zero gradient, no loss
       FVG_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * (op->n + 1), c->stream));
       FVG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 2, c->stream));
+      return;
+    }
+    if (storage == FVG_SPLIT) {
+      eval_split(x, b, grad, out);
       return;
     }
     const bool f32v = storage == FVG_F32;  // timed apart: the passes read 4-byte values
@@ -750,7 +805,7 @@ void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label) {
   if (M->A.n == 0 || M->A.m == 0) fail(FVG_ERR_INVALID_ARG, "Empty training data\n");
   if (!label) fail(FVG_ERR_INVALID_ARG, "Number of label and data are different\n");
   if (p->reg_type < 0 || p->reg_type > 2) fail(FVG_ERR_INVALID_ARG, "Unsupported regularizer!\n");
-  if (p->storage < 0 || p->storage > 2) fail(FVG_ERR_INVALID_ARG, "unknown storage precision");
+  if (p->storage < 0 || p->storage > FVG_SPLIT) fail(FVG_ERR_INVALID_ARG, "unknown storage precision");
   if (p->storage == FVG_F64 && M->master != FVG_F64)
     fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 input values");
   if (p->loss < FVG_LOSS_LOGISTIC || p->loss > FVG_LOSS_SQ_EPS_INSENSITIVE) fail(FVG_ERR_INVALID_ARG, "Unsupported loss kind!\n");
@@ -816,23 +871,26 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   HostPinned hp(4);
   // the direction kernel: a cooperative grid (every CTA resident), its
   // partial sums and barrier counter
-  static int dir_blocks = -1;
-  if (dir_blocks < 0) {
-    int nb = 0;
-    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_direction, kDirThreads, 0));
-    dir_blocks = std::max(1, nb);
-  }
+  const int dir_blocks = occupancy_blocks((const void*)k_direction, kDirThreads);
   const int dgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kDirThreads - 1) / kDirThreads,
                                                         (i64)std::min(dir_blocks, 8) * c->num_sms));
   DBuf dpart, dbar;
   dpart.alloc(sizeof(double) * 4 * dgrid, s);
   dbar.alloc(sizeof(unsigned long long), s);
   DirArgs dargs{G.as<double>(), Q.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(), Y.as<double>(),
-                va, dpart.as<double>(), dbar.as<unsigned long long>(), c->dev_err};
+                va, dpart.as<double>(), dbar.as<unsigned long long>(), c->dev_err, barrier_polls(c)};
 
   const double* W_ = W.as<double>();
+  // split storage: the model as df pairs for the products
+  const bool split = storage == FVG_SPLIT;
+  DBuf W2;
+  if (split) W2.alloc(sizeof(float2) * n1, s);
   auto weights_for = [&](const double* w64, float* wf) -> const void* {
     if (storage == FVG_F64) return w64;
+    if (split) {
+      split_vector(c, w64, W2.p, n);
+      return W2.p;
+    }
     k_d2f<<<vgrid, kVecThreads, 0, s>>>(w64, wf, n);
     check_launch("d2f");
     count_launch(c);
@@ -857,7 +915,7 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   double loss = hp.p[0];
 
   const bool ell = (fmt == FVG_ELL);
-  const bool mixed = storage != FVG_F64;
+  const bool mixed = storage == FVG_F32 || storage == FVG_BF16;
   std::vector<double> rms_hist;
   i64 i = 1;
   for (; i <= p->num_iteration; i++) {
@@ -880,7 +938,8 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
         check_launch("trial");
         count_launch(c);
       }
-      evaluate(mixed ? (const void*)NWF.p : NW.p, &st->b[1], NG.as<double>(), 0);
+      evaluate(mixed ? (const void*)NWF.p : split ? weights_for(NW.as<double>(), nullptr) : NW.p, &st->b[1],
+               NG.as<double>(), 0);
       read_host();
       newloss = hp.p[0];
       rms_t = hp.p[2];
@@ -1063,6 +1122,7 @@ void sgd_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* s
   };
   std::vector<std::vector<std::unique_ptr<Batch>>> ranks(P);
   const int storage = p->storage;
+  if (storage == FVG_SPLIT) fail(FVG_ERR_UNSUPPORTED, "split storage is offered by the L-BFGS trainers, single evaluations and the products");
   for (int r = 0; r < P; r++) {
     i64 ns = splits[r + 1] - splits[r];
     i64 tmp = (i64)std::ceil(ns * p->mini_batch_fraction);
@@ -1209,7 +1269,12 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
   ev.loss = loss_kind;
   ev.eps = eps;
   const void* x = w.p;
-  if (storage != FVG_F64) {
+  DBuf w2;
+  if (storage == FVG_SPLIT) {
+    w2.alloc(sizeof(float2) * (n + 1), s);
+    split_vector(c, w.as<double>(), w2.p, n);
+    x = w2.p;
+  } else if (storage != FVG_F64) {
     k_d2f<<<256, kVecThreads, 0, s>>>(w.as<double>(), wf.as<float>(), n);
     check_launch("d2f");
     count_launch(c);

@@ -223,6 +223,7 @@ void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const d
     crs_build_transpose(c, M->A, *M->AT, M->master);
   }
   const int storage = p->storage;
+  if (storage == FVG_SPLIT) fail(FVG_ERR_UNSUPPORTED, "split storage is offered by the L-BFGS trainers, single evaluations and the products");
   const bool mixed = storage != FVG_F64;
   crs_ensure_plane(c, *M->AT, storage, M->master);
 

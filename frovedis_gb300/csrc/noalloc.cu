@@ -28,18 +28,28 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of g_no_alloc_scratch on `device` (the name is only a host
-// stand-in); looked up once per device, with that device current.
+// Makes the context's device current for the whole call (the symbol lookup
+// and the launches on the context's stream) and restores the caller's device
+// on the way out.
+struct DeviceGuard {
+  int prev = -1, dev;
+  explicit DeviceGuard(int d) : dev(d) {
+    FVG_CUDA(cudaGetDevice(&prev));
+    if (prev != dev) FVG_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() {
+    if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+  }
+};
+
+// Device address of g_no_alloc_scratch on `device`, which must be current
+// (the name is only a host stand-in); looked up once per device.
 void* scratch_for(int device) {
   if (device < 0 || device >= kMaxDevices) fail(FVG_ERR_INVALID_ARG, "device id out of range");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_ptr[device]) {
-    int cur = -1;
-    FVG_CUDA(cudaGetDevice(&cur));
-    if (cur != device) FVG_CUDA(cudaSetDevice(device));
     void* ptr = nullptr;
     cudaError_t rc = cudaGetSymbolAddress(&ptr, g_no_alloc_scratch);
-    if (cur != device) cudaSetDevice(cur);
     if (rc != cudaSuccess || !ptr) throw_cuda(rc, "cudaGetSymbolAddress(g_no_alloc_scratch)", __FILE__, __LINE__);
     g_scratch_ptr[device] = ptr;
   }
@@ -58,6 +68,7 @@ extern "C" FVG_API fvg_status fvg_spmv_no_alloc(fvg_ctx* c, fvg_matrix* M, fvg_d
       fail(FVG_ERR_INVALID_ARG, storage == FVG_F64 ? "FP64 values need FP64 vectors"
                                                    : "FP32/BF16 values need FP32 vectors here");
     if ((M->A.m > 0 && !y) || (M->A.n > 0 && !x)) fail(FVG_ERR_INVALID_ARG, "null vector");
+    DeviceGuard guard(c->device);
     const size_t need = crs_spmv_no_alloc(c, M->A, storage, x, y, nullptr, 0);
     if (need > kNoAllocScratchBytes)
       fail(FVG_ERR_INVALID_ARG, "matrix too large for fvg_spmv_no_alloc: its long rows need " + std::to_string(need) +

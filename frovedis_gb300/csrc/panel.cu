@@ -305,6 +305,7 @@ struct PanK {
   float* partials;
   float* ypan;
   unsigned* err;
+  unsigned wait_limit;  // poll budget of the copy waits
   int aligned;  // r is 16-byte aligned: the slice is staged with 16-byte loads
   // forward head: every CTA stages the same slice r[xmap[0..rows)] once
   // (the frequent columns of w), panels are stretches of A's rows
@@ -344,11 +345,13 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-// Bounded wait: gives up after 2^22 polls (far beyond any copy's time) and
-// reports it in the device error word instead of spinning forever.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err) {
-  for (unsigned it = 0; it < (1u << 22); it++)
-    if (mbar_try_wait(bar, parity)) return true;
+// Bounded wait of a whole warp: gives up after `limit` polls (by default
+// 2^22, far beyond any copy's time) and reports it in the device error word
+// instead of spinning forever.  The lanes vote on every poll (a completed
+// phase stays completed), so the outcome is the same for the whole warp.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err, unsigned limit) {
+  for (unsigned it = 0; it < limit; it++)
+    if (__any_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
   if (err) atomicOr(err, 2u);
   return false;
 }
@@ -446,7 +449,7 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
       pend = true;
       if (it.r1 >= 0)
         for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = (unsigned short)(__ldg(p.poff + it.r0 + k) - q0);
-      if (!mbar_wait_bounded(bar, parity, p.err)) {
+      if (!mbar_wait_bounded(bar, parity, p.err, p.wait_limit)) {
         dead = true;
         break;
       }
@@ -521,7 +524,9 @@ __global__ void __launch_bounds__(kPanelWarps * 32, 1) k_panel(const PanK p) {
       if (lane == 0) p.ypan[p.long_rows[L]] = acc;
     }
   }
-  if (pend) mbar_wait_bounded(bar, parity, nullptr);
+  // a warp that gave up still drains its copy in flight (default budget)
+  // before the CTA's shared memory is released
+  if (pend) mbar_wait_bounded(bar, parity, nullptr, kCopyPolls);
 }
 
 // g[hot[h]] = sum over panels of ypan[panel*nhot + h] in a fixed order:
@@ -954,6 +959,7 @@ void panel_trans_mv(fvg_ctx* c, DevPanels& pn, int storage, const float* r, int 
   k.partials = pn.partials.as<float>();
   k.ypan = pn.ypan.as<float>();
   k.err = c->dev_err;
+  k.wait_limit = copy_polls(c);
   k.aligned = ((reinterpret_cast<uintptr_t>(r) & 15) == 0) ? 1 : 0;
   k.xmap = nullptr;
   k.group = 1;
@@ -1016,6 +1022,7 @@ void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, co
   k.partials = hd.partials.as<float>();
   k.ypan = hd.ypan.as<float>();
   k.err = c->dev_err;
+  k.wait_limit = copy_polls(c);
   k.aligned = 0;
   k.xmap = hd.hot_cols.as<i32>();
   k.group = (hd.npanels + c->num_sms - 1) / c->num_sms;  // a CTA's whole share of the stretches

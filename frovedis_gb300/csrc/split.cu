@@ -1,0 +1,377 @@
+// Split-value storage: FP64-accurate products at FP32 speed.
+//
+// The reference multiplies FP64 values (crs_matrix_spmv_impl,
+// crs_matrix.hpp:1505-1516) and evaluates the loss/gradient in FP64
+// (gradient_descent.hpp:196-225, gradient.hpp:15-53).  On GB300 FP64 issues
+// at a small fraction of the FP32 rate, and FP32 or BF16 values alone move the
+// L-BFGS trajectory far from the FP64 one (their rounding, 2^-24 or 2^-9 per
+// value, grows over the iterations).  Split storage keeps each value v as
+//   hi = FP32(v)                 (the FP32 plane, shared with FP32 storage)
+//   lo = BF16(v - hi)            (a 2-byte residual plane)
+// so hi + lo is within 2^-33 of v, and multiplies in double-FP32 (df64.cuh):
+// x arrives as (hi, lo) pairs, each product hi*x is made exact with an FMA,
+// rows are summed with TwoSum, and the per-row GLM loss/gradient runs in df64
+// (table-driven exp, Newton-corrected log1p).  FP64 appears only in O(rows)
+// conversions of the results.
+//
+// Pass 1 (A w): k_crs_split over the CRS items writes each row's product as a
+// df pair; k_fin_split adds long rows' pieces in order; k_glm_split applies
+// the loss kind (compute_dloss * sample_weight), writes r = dloss * sw as df
+// pairs and reduces loss and bias in a fixed order.  Pass 2 (A^T r) is
+// k_crs_split over the transposed copy.  Every sum has a fixed order, so
+// results are identical run to run.
+#include <cmath>
+#include <mutex>
+
+#include "device_common.cuh"
+#include "df64.cuh"
+
+namespace fvg {
+
+// 2^(j/64), j = 0..63, as df pairs, into the device table of df_exp.  The
+// host's exp2 is accurate to an ulp of FP64, far below the df64 resolution.
+void df64_init(fvg_ctx* c) {
+  float2 tab[64];
+  for (int j = 0; j < 64; j++) {
+    const double v = std::exp2(j / 64.0);
+    const float h = (float)v;
+    tab[j] = make_float2(h, (float)(v - (double)h));
+  }
+  FVG_CUDA(cudaMemcpyToSymbol(g_exp2_tab, tab, sizeof(tab)));
+}
+
+namespace {
+
+constexpr int kSplitThreads = 256;
+
+unsigned grid_rows(fvg_ctx* c, i64 n, int per_sm = 8) {
+  i64 g = (n + kSplitThreads - 1) / kSplitThreads;
+  g = std::min<i64>(g, (i64)per_sm * c->num_sms);
+  return (unsigned)std::max<i64>(g, 1);
+}
+
+// residual plane: lo = BF16(v - FP32(v)) (one-off per matrix); flags a value
+// whose FP32 rounding overflows
+__global__ void k_split_plane(const double* __restrict__ v, const float* __restrict__ hi, bf16* __restrict__ lo,
+                              i64 n, unsigned* __restrict__ bad) {
+  unsigned b = 0;
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const double x = v[i];
+    const float h = hi[i];
+    if (isinf(h) && !isinf(x)) b = 1;
+    lo[i] = __double2bfloat16(isinf(h) ? 0.0 : x - (double)h);
+  }
+  if (b) atomicOr(bad, 1u);
+}
+
+__global__ void k_split_vec(const double* __restrict__ x, float2* __restrict__ y, i64 n) {
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+    y[i] = df_pack(df_from_double(x[i]));
+}
+
+// ------------------------------------------------------------- CRS pass
+struct SplitK {
+  const i32* off;
+  const i32* idx;
+  const float* vh;
+  const unsigned short* vl;
+  const float2* x;
+  const Item* items;
+  i64 nitems;
+  void* y;           // double[rows] or float2[rows]
+  float2* partials;  // long-row pieces
+};
+
+template <class YT> __device__ __forceinline__ void store_row(void* y, i64 row, df a);
+template <> __device__ __forceinline__ void store_row<double>(void* y, i64 row, df a) {
+  ((double*)y)[row] = df_to_double(a);
+}
+template <> __device__ __forceinline__ void store_row<float2>(void* y, i64 row, df a) {
+  ((float2*)y)[row] = df_pack(a);
+}
+
+__device__ __forceinline__ df shfl_df(df a, int o) {
+  return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+
+// Persistent kernel over the CRS work items (the schedule of k_crs: tiles of
+// short rows, pieces of long rows).  Phase 1: lane L streams nonzeros L,
+// L+32, ... (column id, FP32 value, BF16 residual), gathers x's pair and
+// stages the exact product (p, t) in the warp's shared-memory slice.  Phase
+// 2: each row is summed by 1..32 lanes with TwoSum, the lanes combined by a
+// butterfly of df additions (commutative, so every lane of a row holds the
+// same sum); a piece is summed by the whole warp.
+template <class YT>
+__global__ void __launch_bounds__(kThreads, 4) k_crs_split(const SplitK p) {
+  constexpr int SPAN = kWarpTile;
+  constexpr int NR = SPAN / 32;
+  constexpr int RG = 4;
+  __shared__ float2 sprod[kThreads / 32][SPAN];
+  __shared__ int soffs[kThreads / 32][kTileRows + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float2* prod = sprod[w];
+  int* soff = soffs[w];
+  const i64 W = (i64)gridDim.x * (kThreads / 32);
+  const i64 n = p.nitems;
+  i64 t = (i64)blockIdx.x * (kThreads / 32) + w;
+  Item nx = (t < n) ? p.items[t] : Item{0, 0, 0, 0};
+  for (; t < n; t += W) {
+    const Item it = nx;
+    if (t + W < n) nx = p.items[t + W];
+    const int a0 = it.e0;
+    const int span = it.e1 - a0;
+    if (it.r1 >= 0)
+      for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = __ldg(p.off + it.r0 + k);
+#pragma unroll
+    for (int g = 0; g < NR; g += RG) {
+      int c[RG];
+      float vh[RG];
+      unsigned short vl[RG];
+#pragma unroll
+      for (int q = 0; q < RG; q++) {
+        const int k = (g + q) * 32 + lane;
+        if (k < span) {
+          c[q] = __ldcs(p.idx + a0 + k);
+          vh[q] = __ldcs(p.vh + a0 + k);
+          vl[q] = __ldcs(p.vl + a0 + k);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RG; q++) {
+        const int k = (g + q) * 32 + lane;
+        if (k < span) {
+          const float2 xv = __ldg(p.x + c[q]);
+          float pp, tt;
+          df_prod(vh[q], __uint_as_float((unsigned)vl[q] << 16), xv, pp, tt);
+          prod[k] = make_float2(pp, tt);
+        }
+      }
+    }
+    __syncwarp();
+    if (it.r1 >= 0) {
+      const int R = it.r1 - it.r0;
+      const int Gl = lanes_per_row(R);
+      const int per_round = 32 / Gl;
+      for (int rb = 0; rb < R; rb += per_round) {
+        const int j = rb + lane / Gl, sub = lane % Gl;
+        DfAcc acc;
+        if (j < R) {
+          const int s = soff[j] - a0, e = soff[j + 1] - a0;
+          for (int k = s + sub; k < e; k += Gl) {
+            const float2 v = prod[k];
+            acc.add(v.x, v.y);
+          }
+        }
+        df a = acc.get();
+        for (int o = Gl >> 1; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
+        if (j < R && sub == 0) store_row<YT>(p.y, it.r0 + j, a);
+      }
+    } else {
+      DfAcc acc;
+      for (int k = lane; k < span; k += 32) {
+        const float2 v = prod[k];
+        acc.add(v.x, v.y);
+      }
+      df a = acc.get();
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
+      if (lane == 0) p.partials[-1 - it.r1] = df_pack(a);
+    }
+    __syncwarp();
+  }
+}
+
+// long rows: a warp adds a row's pieces (lane L: pieces L, L+32, ...; then
+// the butterfly), in the same order on every run
+template <class YT>
+__global__ void __launch_bounds__(kThreads) k_fin_split(const i32* __restrict__ long_rows,
+                                                        const i32* __restrict__ long_piece0, i64 nlong,
+                                                        const float2* __restrict__ partials, void* y) {
+  const int lane = threadIdx.x & 31;
+  for (i64 i = (i64)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); i < nlong;
+       i += (i64)gridDim.x * (kThreads / 32)) {
+    const i64 c0 = long_piece0[i], c1 = long_piece0[i + 1];
+    df a = {0.f, 0.f};
+    for (i64 j = c0 + lane; j < c1; j += 32) a = df_add(a, df_unpack(__ldcg(partials + j)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
+    if (lane == 0) store_row<YT>(y, long_rows[i], a);
+  }
+}
+
+// ------------------------------------------------------------- GLM rows
+struct GlmSplitK {
+  const float2* wtx;
+  const float2* head;  // optional second partial product per row
+  i64 m;
+  const float2* lab;
+  const float2* sw;  // null: all ones
+  const double* intercept;
+  int icpt;
+  int kind;
+  double eps;
+  float2* r;
+  double* cta_part;  // [2 * gridDim.x]
+  unsigned* ticket;
+  double* out;        // [2]: loss, bias
+  double* grad_bias;  // optional
+};
+
+__device__ __forceinline__ df block_df_sum(df a, df* red /* [8] */) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = a;
+  __syncthreads();
+  df t = {0.f, 0.f};
+  if (threadIdx.x == 0)
+    for (int q = 0; q < kSplitThreads / 32; q++) t = df_add(t, red[q]);
+  return t;  // thread 0
+}
+
+// compute_dloss * sample_weight per row (gradient_descent.hpp:196-211), the
+// loss summed unweighted and the bias as the sum of dloss * sw; the CTAs'
+// partial sums are added in CTA order by the last CTA (FP64, compensated).
+__global__ void __launch_bounds__(kSplitThreads) k_glm_split(const GlmSplitK p) {
+  __shared__ df red_l[kSplitThreads / 32], red_b[kSplitThreads / 32];
+  const df b = p.icpt ? df_from_double(*p.intercept) : df{0.f, 0.f};
+  const df eps = df_from_double(p.eps);
+  df ls = {0.f, 0.f}, bs = {0.f, 0.f};
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < p.m; i += (i64)gridDim.x * blockDim.x) {
+    df z = df_unpack(p.wtx[i]);
+    if (p.head) z = df_add_acc(z, df_unpack(p.head[i]));
+    z = df_add_acc(z, b);
+    df loss, d;
+    glm_row_df(p.kind, eps, z, df_unpack(p.lab[i]), loss, d);
+    if (p.sw) d = df_mul(d, df_unpack(p.sw[i]));
+    p.r[i] = df_pack(d);
+    ls = df_add(ls, loss);
+    bs = df_add(bs, d);
+  }
+  const df tl = block_df_sum(ls, red_l);
+  const df tb = block_df_sum(bs, red_b);
+  if (threadIdx.x == 0) {
+    p.cta_part[2 * blockIdx.x] = df_to_double(tl);
+    p.cta_part[2 * blockIdx.x + 1] = df_to_double(tb);
+  }
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(p.ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  CSum l, s;
+  for (unsigned q = 0; q < gridDim.x; q++) {
+    l.add(__ldcg(&p.cta_part[2 * q]));
+    s.add(__ldcg(&p.cta_part[2 * q + 1]));
+  }
+  p.out[0] = l.total();
+  p.out[1] = p.icpt ? s.total() : 0.0;
+  if (p.grad_bias) *p.grad_bias = p.icpt ? s.total() : 0.0;
+  *p.ticket = 0u;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) {
+  crs_ensure_plane(c, a, FVG_F32, master);
+  if (a.lo.p) return;
+  DBuf lo;
+  lo.alloc(sizeof(bf16) * (size_t)(a.nnz + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(lo.p, 0, sizeof(bf16) * (size_t)(a.nnz + kPad), c->stream));
+  if (master == FVG_F64 && a.nnz > 0) {
+    DBuf bad;
+    bad.alloc(sizeof(unsigned), c->stream);
+    FVG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), c->stream));
+    k_split_plane<<<grid_rows(c, a.nnz, 16), kSplitThreads, 0, c->stream>>>(
+        a.val[FVG_F64].as<double>(), a.val[FVG_F32].as<float>(), lo.as<bf16>(), a.nnz, bad.as<unsigned>());
+    check_launch("split_plane");
+    count_launch(c);
+    unsigned hb = 0;
+    FVG_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+    if (hb) fail(FVG_ERR_INVALID_ARG, "split storage: a value lies outside the FP32 range");
+  }
+  a.lo = std::move(lo);
+}
+
+void split_vector(fvg_ctx* c, const double* x, void* y, i64 n) {
+  if (n <= 0) return;
+  k_split_vec<<<grid_rows(c, n), kSplitThreads, 0, c->stream>>>(x, (float2*)y, n);
+  check_launch("split_vec");
+  count_launch(c);
+}
+
+i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a) {
+  const Sched& s = crs_sched(c, a, kWarpTile);
+  return (i64)sizeof(float2) * std::max<i64>(s.npieces, 1);
+}
+
+void crs_pass_split(fvg_ctx* c, DevCRS& a, const void* x, bool y_df, void* y, void* scratch, int prof_key) {
+  const Sched& s = crs_sched(c, a, kWarpTile);
+  if (!a.val[FVG_F32].p || !a.lo.p) fail(FVG_ERR_INTERNAL, "split storage planes missing");
+  DBuf tmp;
+  if (!scratch) {
+    tmp.alloc((size_t)crs_split_scratch_bytes(c, a), c->stream);
+    scratch = tmp.p;
+  }
+  ProfScope pr(c, prof_key);
+  SplitK p;
+  p.off = a.off.as<i32>();
+  p.idx = a.idx.as<i32>();
+  p.vh = a.val[FVG_F32].as<float>();
+  p.vl = a.lo.as<unsigned short>();
+  p.x = (const float2*)x;
+  p.items = s.items.as<Item>();
+  p.nitems = s.nitems;
+  p.y = y;
+  p.partials = (float2*)scratch;
+  if (s.nitems > 0) {
+    const void* kfn = y_df ? (const void*)k_crs_split<float2> : (const void*)k_crs_split<double>;
+    int grid = occupancy_blocks(kfn, kThreads) * c->num_sms;
+    grid = (int)std::max<i64>(1, std::min<i64>(grid, s.nitems));
+    if (y_df) k_crs_split<float2><<<grid, kThreads, 0, c->stream>>>(p);
+    else k_crs_split<double><<<grid, kThreads, 0, c->stream>>>(p);
+    check_launch("k_crs_split");
+    count_launch(c);
+  }
+  if (s.nlong > 0) {
+    const int fg = (int)std::max<i64>(1, std::min<i64>((s.nlong + 7) / 8, 4 * c->num_sms));
+    if (y_df)
+      k_fin_split<float2><<<fg, kThreads, 0, c->stream>>>(s.long_rows.as<i32>(), s.long_piece0.as<i32>(), s.nlong,
+                                                          (const float2*)scratch, y);
+    else
+      k_fin_split<double><<<fg, kThreads, 0, c->stream>>>(s.long_rows.as<i32>(), s.long_piece0.as<i32>(), s.nlong,
+                                                          (const float2*)scratch, y);
+    check_launch("k_fin_split");
+    count_launch(c);
+  }
+}
+
+int glm_split_grid(fvg_ctx* c, i64 m) { return (int)grid_rows(c, m, 4); }
+
+void glm_split_rows(fvg_ctx* c, const void* wtx, const void* head, i64 m, const GlmSplitArgs& e) {
+  GlmSplitK p;
+  p.wtx = (const float2*)wtx;
+  p.head = (const float2*)head;
+  p.m = m;
+  p.lab = (const float2*)e.lab;
+  p.sw = (const float2*)e.sw;
+  p.intercept = e.intercept;
+  p.icpt = e.icpt;
+  p.kind = e.kind;
+  p.eps = e.eps;
+  p.r = (float2*)e.r;
+  p.cta_part = e.cta_part;
+  p.ticket = e.ticket;
+  p.out = e.out;
+  p.grad_bias = e.grad_bias;
+  k_glm_split<<<glm_split_grid(c, m), kSplitThreads, 0, c->stream>>>(p);
+  check_launch("k_glm_split");
+  count_launch(c);
+}
+
+}  // namespace fvg

@@ -372,13 +372,7 @@ static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 template <class VT, class XT, class AT, class YT, int EPI, int CPL, bool VEC>
 static int spmm_grid(fvg_ctx* c) {
-  static int blocks = -1;
-  if (blocks < 0) {
-    int nb = 0;
-    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spmm<VT, XT, AT, YT, EPI, CPL, VEC>, kThreads, 0));
-    blocks = std::max(1, nb);
-  }
-  return blocks * c->num_sms;
+  return occupancy_blocks((const void*)k_spmm<VT, XT, AT, YT, EPI, CPL, VEC>, kThreads) * c->num_sms;
 }
 
 static int spmm_fin_grid(fvg_ctx* c, i64 nlong) {

@@ -322,15 +322,8 @@ i64 crs_pass_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage) {
 
 template <class VT, class XT, class AT, class YT, int EPI>
 static int crs_grid(fvg_ctx* c, int tile) {
-  static int blocks = -1;
-  auto kfn = k_crs<VT, XT, AT, YT, EPI>;
   (void)tile;
-  if (blocks < 0) {
-    int nb = 0;
-    FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, kThreads, 0));
-    blocks = std::max(1, nb);
-  }
-  return blocks * c->num_sms;
+  return occupancy_blocks((const void*)k_crs<VT, XT, AT, YT, EPI>, kThreads) * c->num_sms;
 }
 
 template <class VT, class XT, class AT, class YT, int EPI>

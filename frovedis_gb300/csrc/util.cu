@@ -1,6 +1,10 @@
 // Device utilities: buffers, error plumbing, profiler, exclusive scan,
 // stable LSD radix sort, value conversion and gathers.
+#include <atomic>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "fvg_internal.cuh"
 
@@ -23,15 +27,25 @@ void check_device_error(fvg_ctx* c) {
   FVG_CUDA(cudaStreamSynchronize(c->stream));
   if (h) {
     FVG_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(unsigned), c->stream));
-    fail(FVG_ERR_INTERNAL, "a device-side bounded wait gave up (bulk copy did not complete); results are invalid");
+    std::string what;
+    if (h & 2u) what += " a bulk copy did not complete in its poll budget;";
+    if (h & 4u) what += " a grid barrier was not reached in its poll budget;";
+    fail(FVG_ERR_INTERNAL, "a device-side bounded wait gave up:" + what + " results are invalid");
   }
 }
+
+// Testing aid: the `after`-th next device allocation fails as if the device
+// were out of memory (< 0: off).
+static std::atomic<long long> g_alloc_fail_after{-1};
+void inject_alloc_failure(long long after) { g_alloc_fail_after.store(after); }
 
 void DBuf::alloc(size_t nbytes, cudaStream_t s) {
   release();
   stream = s;
   bytes = nbytes;
   if (nbytes == 0) return;
+  if (g_alloc_fail_after.load() >= 0 && g_alloc_fail_after.fetch_sub(1) == 0)
+    throw_cuda(cudaErrorMemoryAllocation, "cudaMallocAsync (injected failure)", __FILE__, __LINE__);
   FVG_CUDA(cudaMallocAsync(&p, nbytes, s));
   // the SpMV kernels issue 16-byte vector loads from the start of every
   // index/value array
@@ -45,6 +59,25 @@ void DBuf::release() {
 }
 
 int dtype_size(int dt) { return dt == FVG_F64 ? 8 : dt == FVG_F32 ? 4 : 2; }
+
+// Resident CTAs per SM of a kernel on the current device, computed once per
+// (device, kernel, block size, dynamic shared memory) under a mutex: the
+// library may be driven from several host threads, each with its own context.
+int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem) {
+  static std::mutex mu;
+  static std::map<std::pair<std::pair<int, const void*>, std::pair<int, size_t>>, int> cache;
+  int dev = 0;
+  FVG_CUDA(cudaGetDevice(&dev));
+  const auto key = std::make_pair(std::make_pair(dev, kernel), std::make_pair(threads, dyn_smem));
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  FVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, dyn_smem));
+  nb = nb < 1 ? 1 : nb;
+  cache.emplace(key, nb);
+  return nb;
+}
 
 // ------------------------------------------------------------- profiler
 // Event pairs are recorded around the timed launches without synchronising;

@@ -44,8 +44,12 @@ typedef enum {
   FVG_ERR_INTERNAL = 6
 } fvg_status;
 
-/* value / vector element types */
-typedef enum { FVG_F64 = 0, FVG_F32 = 1, FVG_BF16 = 2 } fvg_dtype;
+/* value / vector element types.  FVG_SPLIT is a storage choice only: each
+ * FP64 value kept as its FP32 rounding plus the BF16 rounding of the
+ * remainder (relative error below 2^-32), multiplied in double-FP32
+ * arithmetic (about 48 significant bits) with FP64 vectors at the interface;
+ * results agree with FP64 storage to about 1e-10 relative. */
+typedef enum { FVG_F64 = 0, FVG_F32 = 1, FVG_BF16 = 2, FVG_SPLIT = 3 } fvg_dtype;
 
 /* same numbering as frovedis::MatType (ml/utility/mattype.hpp:6-11) */
 typedef enum { FVG_CRS = 0, FVG_JDS = 1, FVG_ELL = 2, FVG_HYBRID = 3 } fvg_format;
@@ -82,6 +86,24 @@ FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* ctx, const char* name, double* t
 FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* ctx);
 /* Number of CUDA kernels this context launched since creation. */
 FVG_API int64_t fvg_ctx_kernel_launches(fvg_ctx* ctx);
+/* Poll budget of the bounded device-side waits of this context's kernels
+ * (the L-BFGS direction's grid barriers, the row-panel and forward-head
+ * kernels' bulk-copy waits).  A wait that runs out is abandoned: the kernel
+ * records it in the context's error word and finishes (a copy in flight is
+ * still drained), and the call returns FVG_ERR_INTERNAL; the context stays
+ * usable.  polls < 0 restores the defaults (2^24 barrier polls, 2^22 copy
+ * polls, far beyond any healthy wait); 0 makes every wait that is not
+ * already complete give up at once.  No reference counterpart (the
+ * reference's ranks report failures through MPI, core/mpi_rpc.cc:471-491);
+ * a small budget lets a test exercise the give-up path. */
+FVG_API fvg_status fvg_ctx_set_wait_limit(fvg_ctx* ctx, int64_t polls);
+/* Testing aid: the `after`-th next device allocation made by the library
+ * (any context; 0 = the next one) fails as if the device were out of memory,
+ * so the call returns FVG_ERR_OUT_OF_MEMORY after releasing what it had
+ * allocated.  after < 0 switches it off.  No reference counterpart (the
+ * reference surfaces allocation failures as std::bad_alloc,
+ * core/exceptions.hpp:22-43). */
+FVG_API void fvg_debug_inject_alloc_failure(int64_t after);
 
 /* -------------------------------------------------------------- matrix */
 /* Upload a CRS matrix (crs_matrix_local<T,I,O>, matrix/crs_matrix.hpp:240-331):
@@ -214,8 +236,13 @@ FVG_API fvg_status fvg_spmm(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_d
  * The matrix must be prepared first (fvg_matrix_prepare with FVG_CRS, and
  * fvg_matrix_add_storage for FP32/BF16).  The first call on a device looks up
  * the array's device address (one-time set-up; make it before any stream
- * capture).  Calls share the array: calls that overlap on the GPU race, so
- * order them on one stream. */
+ * capture).  The call runs with the context's device current and restores
+ * the caller's device before it returns.  Calls share the array: calls that
+ * overlap on the GPU race.  Calls on one context are ordered by its stream;
+ * calls from different contexts on the same device (each context has its own
+ * stream, e.g. one per host thread) must be serialised by the caller —
+ * synchronise the first context, or make the second context's stream wait on
+ * an event recorded after the first call. */
 FVG_API fvg_status fvg_spmv_no_alloc(fvg_ctx* ctx, fvg_matrix* mat, fvg_dtype storage, fvg_dtype vec_dtype,
                                      const void* x, void* y);
 

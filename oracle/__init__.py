@@ -73,6 +73,12 @@ def lib():
             f = getattr(L, name)
             f.argtypes = args
             f.restype = None
+        L.orc_problem_create.argtypes = [_int, _i64, _i64, _p, _p, _p, _p, _p, _p, _int, _int, _int, _dbl]
+        L.orc_problem_create.restype = _p
+        L.orc_problem_lbfgs.argtypes = [_p, _i64, _i64, _dbl, _int, _int, _dbl, _p, _p, _p, _p, _p, _int]
+        L.orc_problem_lbfgs.restype = _int
+        L.orc_problem_destroy.argtypes = [_p]
+        L.orc_problem_destroy.restype = None
         L.orc_ell_width.argtypes = [_i64, _p]
         L.orc_ell_width.restype = _i64
         L.orc_glm_lbfgs_f64.restype = _int
@@ -271,6 +277,47 @@ def logreg_lbfgs(a: CRS, label, num_iter=1000, alpha=0.01, hist_size=10, reg_par
         raise ValueError(f"oracle lbfgs rejected the arguments (code {rc})")
     it = int(n_iter[0])
     return dict(w=w, b=float(b[0]), n_iter=it, loss=float(fl[0]), trace=trace.reshape(-1, 4)[:it])
+
+
+class Problem:
+    """An L-BFGS problem built once (per-rank matrices and transposed copies,
+    rows split like MPI ranks) for repeated oracle runs whose timing covers
+    the training loop alone."""
+
+    def __init__(self, a: CRS, label, sw=None, fmt="CRS", splits=None, nthreads=1, loss="logistic", eps=0.0):
+        self.n = a.n
+        self._label = np.ascontiguousarray(label, dtype=np.float64)
+        self._sw = np.ones(a.m) if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
+        sp, P = _splits(a, splits)
+        self.h = lib().orc_problem_create(FMT[fmt], *a.args(), _ptr(self._label), _ptr(self._sw), _ptr(sp), P,
+                                          nthreads, LOSS[loss], float(eps))
+        if not self.h:
+            raise ValueError("oracle problem rejected the arguments")
+
+    def lbfgs(self, num_iter=1000, hist_size=10, reg_param=0.01, reg_type="ZERO", intercept=False, tol=0.001,
+              w0=None, b0=None, l2_no_eta=False):
+        w = np.ones(self.n) if w0 is None else np.array(w0, dtype=np.float64)
+        b = np.array([(1.0 if intercept else 0.0) if b0 is None else float(b0)])
+        n_iter = np.zeros(1, dtype=np.int64)
+        fl = np.zeros(1)
+        trace = np.zeros(4 * num_iter)
+        rc = lib().orc_problem_lbfgs(self.h, num_iter, hist_size, reg_param, REG[reg_type], int(intercept), tol,
+                                     _ptr(w), _ptr(b), _ptr(n_iter), _ptr(fl), _ptr(trace), int(l2_no_eta))
+        if rc != 0:
+            raise ValueError(f"oracle lbfgs rejected the arguments (code {rc})")
+        it = int(n_iter[0])
+        return dict(w=w, b=float(b[0]), n_iter=it, loss=float(fl[0]), trace=trace.reshape(-1, 4)[:it])
+
+    def close(self):
+        if self.h:
+            lib().orc_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def logreg_sgd(a: CRS, label, num_iter=1000, alpha=0.01, mini_batch_fraction=1.0, reg_param=0.01,

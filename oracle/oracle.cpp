@@ -1117,6 +1117,45 @@ int orc_glm_lbfgs_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, con
   return 0;
 }
 
+// The same trainer on a problem built once: the per-rank matrices and their
+// transposed copies (lbfgs_parallelizer.hpp:562-597) are made by
+// orc_problem_create and reused by every orc_problem_lbfgs call, so a timing
+// of orc_problem_lbfgs covers the training loop alone.
+struct OrcProblem {
+  int fmt = CRS_F;
+  i64 n = 0;
+  Problem<double> pr;
+};
+
+void* orc_problem_create(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
+                         const double* label, const double* sw, const i64* splits, int P, int nthreads, int lkind,
+                         double eps) {
+  if (fmt == JDS_F || fmt < 0 || fmt > 3 || lkind < 0 || lkind > 4) return nullptr;
+  auto* h = new OrcProblem();
+  h->fmt = fmt;
+  h->n = n;
+  auto a = make_crs<double>(m, n, off, idx, val);
+  auto sp = default_splits(m, splits, P);
+  h->pr = make_problem(a, label, sw, sp.data(), P, fmt, nthreads);
+  h->pr.loss = Loss{lkind, eps};
+  return h;
+}
+
+int orc_problem_lbfgs(void* hp, i64 num_iter, i64 hist, double lambda, int rtype, int icpt, double tol, double* w,
+                      double* b, i64* n_iter, double* final_loss, double* trace, int flags) {
+  auto* h = static_cast<OrcProblem*>(hp);
+  if (!h || hist < 1 || num_iter < 1 || lambda < 0 || tol < 0) return 1;
+  std::vector<double> wv(w, w + h->n);
+  double bb = *b;
+  lbfgs_train(h->pr, h->fmt, wv, bb, num_iter, hist, lambda, rtype, icpt != 0, tol, *n_iter, *final_loss, trace,
+              (flags & 1) != 0);
+  std::copy(wv.begin(), wv.end(), w);
+  *b = bb;
+  return 0;
+}
+
+void orc_problem_destroy(void* hp) { delete static_cast<OrcProblem*>(hp); }
+
 // shrink::logistic_regression_with_sgd::train (flags bit 1 of orc_glm_sgd_f64)
 int orc_glm_sgd_f64(int fmt, i64 m, i64 n, const i32* off, const i32* idx, const double* val,
                     const double* label, const double* sw, const i64* splits, int P, int nthreads,

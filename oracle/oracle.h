@@ -51,6 +51,14 @@ int orc_glm_lbfgs_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const i
                       int nthreads, int64_t num_iter, int64_t hist, double lambda, int rtype, int icpt,
                       double tol, double* w, double* b, int64_t* n_iter, double* final_loss, double* trace,
                       int flags, int lkind, double eps);
+// A problem built once (per-rank matrices and transposed copies) for
+// repeated L-BFGS runs; orc_problem_create returns NULL on bad arguments.
+void* orc_problem_create(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                         const double* label, const double* sw, const int64_t* splits, int P, int nthreads,
+                         int lkind, double eps);
+int orc_problem_lbfgs(void* h, int64_t num_iter, int64_t hist, double lambda, int rtype, int icpt, double tol,
+                      double* w, double* b, int64_t* n_iter, double* final_loss, double* trace, int flags);
+void orc_problem_destroy(void* h);
 int orc_glm_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
                     const double* label, const double* sw, const int64_t* splits, int P, int nthreads,
                     int64_t num_iter, double alpha, double frac, double lambda, int rtype, int icpt, double tol,

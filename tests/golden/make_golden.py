@@ -1,7 +1,8 @@
 """Regenerates tests/golden/golden.json from the reference's own fixtures.
 
-Reads (never writes) the reference tree given as argv[1] (default
-/root/reference) and extracts, as data:
+Reads (never writes) the reference tree whose path is the required first
+argument (``python tests/golden/make_golden.py <frovedis source tree>``) and
+extracts, as data:
 
 * the tutorial SpMV fixture ``doc/tutorial/src/tut3.2.1-1/data`` (also as
   raw text, for the loaders) and its
@@ -56,7 +57,9 @@ def indented_block_after(md, marker, start=0):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the frovedis source tree>")
+    ref = sys.argv[1]
     tut = os.path.join(ref, "doc", "tutorial")
     md = open(os.path.join(tut, "tutorial.md")).read()
     g = {}

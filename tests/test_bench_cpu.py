@@ -31,11 +31,28 @@ def test_panels_option():
 
 
 def test_traffic_ratios():
-    r = bench.NCU_TRAFFIC_RATIO
-    for k in ("pass1", "pass2", "pass1_f32", "pass2_f32", "pass1_plain", "pass2_plain"):
-        assert 0.5 < r[k] <= 1.0, k
-    # 2-byte panel rows / head columns: the layouts move fewer bytes than the plain kernel
-    assert r["pass1"] < r["pass1_plain"] and r["pass2"] < r["pass2_plain"]
+    for storage, r in bench.NCU_TRAFFIC_RATIO.items():
+        for k in ("pass1", "pass2"):
+            assert 0.5 < r[k] <= 1.2, (storage, k)
+        assert storage in bench.TRAFFIC_SOURCE
+
+
+def test_split_arm_bytes():
+    # split storage: a 4-byte FP32 value, a 2-byte residual and a 4-byte id
+    # per nonzero; vectors as FP32 pairs
+    m, n, nnz = 10, 7, 40
+    p1, p2 = bench.train_bytes_per_eval(m, n, nnz, "split")
+    assert (p1, p2) == bench.eval_bytes(m, n, nnz, 6, 8)
+    assert bench.train_bytes_per_eval(m, n, nnz, "bf16") == bench.eval_bytes(m, n, nnz, 2, 4)
+
+
+def test_parity_of():
+    import numpy as np
+    ref = {"loss": 100.0, "w": np.array([1.0, -2.0]), "trace": np.array([[1.0, 1.0, 0, 0], [1.0, 2.0, 0, 0]])}
+    ok = bench.parity_of({"loss": 100.00005, "w": np.array([1.0, -2.00001]), "trace": ref["trace"]}, ref)
+    assert ok["within_bar"] and ok["trials_same"]
+    bad = bench.parity_of({"loss": 100.001, "w": np.array([1.0, -2.0])}, ref)
+    assert not bad["within_bar"] and "trials_same" not in bad
 
 
 def _replica(rank, port, out):

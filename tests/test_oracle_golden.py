@@ -216,3 +216,21 @@ def test_shrink_sgd_equals_sgd_without_regulariser():
     used[idx] = True
     assert np.array_equal(r1["w"][used], r2["w"][used]) and r1["b"] == r2["b"]
     assert np.all(r1["w"][~used] == 0.0) and np.all(r2["w"][~used] == 1.0)
+
+
+def test_oracle_problem_matches_one_shot_trainer():
+    # the prebuilt problem (per-rank matrices built once) runs the same
+    # trainer: identical results to the one-shot call, run after run
+    from frovedis_gb300 import datagen
+    off, idx, val, label = datagen.generate(datagen.Spec(m=3000, n=400, lam=12.0, seed=21))
+    a = oracle.CRS(3000, 400, off, idx, val)
+    splits = [0, 900, 2000, 3000]
+    kw = dict(num_iter=12, reg_type="L2", reg_param=1e-3, intercept=True)
+    ro = oracle.logreg_lbfgs(a, label, splits=splits, nthreads=3, **kw)
+    pr = oracle.Problem(a, label, splits=splits, nthreads=3)
+    for _ in range(2):
+        rp = pr.lbfgs(**kw)
+        assert rp["n_iter"] == ro["n_iter"] and rp["loss"] == ro["loss"]
+        assert np.array_equal(rp["w"], ro["w"]) and rp["b"] == ro["b"]
+        assert np.array_equal(rp["trace"], ro["trace"])
+    pr.close()

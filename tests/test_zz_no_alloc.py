@@ -17,6 +17,35 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# CUmemPool_attribute values (cuda.h): the default pool's usage counters
+_USED_MEM_CURRENT, _USED_MEM_HIGH = 7, 8
+
+
+class _PoolWatch:
+    """The device's default memory pool (where the library's stream-ordered
+    allocations come from), read through the CUDA driver API: resetting the
+    used-memory high-water mark and reading it back shows whether anything
+    was allocated from the pool in between, even if it was freed again."""
+
+    def __init__(self, device=0):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        dev = ctypes.c_int()
+        assert self.cu.cuDeviceGet(ctypes.byref(dev), device) == 0
+        self.pool = ctypes.c_void_p()
+        assert self.cu.cuDeviceGetDefaultMemPool(ctypes.byref(self.pool), dev) == 0
+
+    def _get(self, attr):
+        v = ctypes.c_uint64()
+        assert self.cu.cuMemPoolGetAttribute(self.pool, attr, ctypes.byref(v)) == 0
+        return v.value
+
+    def reset_high(self):
+        zero = ctypes.c_uint64(0)  # resets the high-water mark to the current usage
+        assert self.cu.cuMemPoolSetAttribute(self.pool, _USED_MEM_HIGH, ctypes.byref(zero)) == 0
+
+    def used(self):
+        return self._get(_USED_MEM_CURRENT), self._get(_USED_MEM_HIGH)
+
 
 def _matrix(rng, m=600, n=50000):
     lens = rng.integers(0, 60, m)
@@ -61,6 +90,31 @@ def test_no_alloc_spmv_matches_allocating_entry_point():
             ctx.synchronize()
             got = y.cpu().numpy().astype(np.float64)
             assert np.all(np.abs(got - ref) <= tol * (scale + 1e-30)), (storage, call)
+    # the property the entry point exists for: two calls in a row take no
+    # memory from the device's pool (not even briefly) and no other device
+    # memory (free memory unchanged)
+    watch = _PoolWatch(0)
+    x = torch.randn(n, dtype=torch.float64, device="cuda")
+    y = torch.empty(m, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    watch.reset_high()
+    cur0, _ = watch.used()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        rc = ctx.L.fvg_spmv_no_alloc(ctx.h, A.h, fv.F64, fv.F64, ctypes.c_void_p(x.data_ptr()),
+                                     ctypes.c_void_p(y.data_ptr()))
+        assert rc == 0, ctx.L.fvg_ctx_last_error(ctx.h)
+    ctx.synchronize()
+    cur1, high1 = watch.used()
+    free1, _ = torch.cuda.mem_get_info()
+    assert (cur1, high1) == (cur0, cur0), "the allocation-free entry point allocated from the pool"
+    assert free1 == free0, "device memory changed across the allocation-free calls"
+    # the allocating entry point does use the pool (the check can see it)
+    watch.reset_high()
+    A.spmv(x.cpu().numpy())
+    ctx.synchronize()
+    assert watch.used()[1] > cur0
     A.close()
     ctx.close()
 
