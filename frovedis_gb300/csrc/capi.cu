@@ -648,7 +648,13 @@ static void run_product_split(fvg_ctx* c, fvg_matrix* M, int fmt, const void* x,
     yb.alloc(sizeof(double) * std::max<int64_t>(ny, 1), c->stream);
     dy = yb.as<double>();
   }
-  crs_pass_split(c, trans ? *M->AT : M->A, x2.p, false, dy, nullptr, P_SPMV_CRS);
+  DevPanels* pt = trans ? panels_for(c, M) : nullptr;
+  if (pt) {
+    ProfScope ps(c, P_SPMV_CRS);
+    panel_trans_mv_split(c, *pt, x2.p, dy, nullptr);
+  } else {
+    crs_pass_split(c, trans ? *M->AT : M->A, x2.p, false, dy, nullptr, P_SPMV_CRS);
+  }
   if (!on_dev && ny)
     FVG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * ny, cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));

@@ -168,6 +168,7 @@ struct DevPanels {
   DBuf items, pitem0, long_rows, plong0, long_piece0;
   DBuf ypan;                        // float [npanels*nhot]
   DBuf partials;                    // float [npieces]
+  DBuf ypan2, partials2;            // split storage: the same as df pairs (float2)
   // forward head (shared = true): every CTA stages w at the columns
   // hot_cols[0..rows) once; panels are stretches of nhot rows of A; `cold`
   // holds the rest of each row (m rows, int32 column ids)
@@ -342,12 +343,21 @@ void head_ensure_plane(fvg_ctx* c, DevPanels& hd, int dt);
 i64 head_scratch_bytes(fvg_ctx* c, DevPanels& hd, int storage);
 void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, const LogregEpi& lr, void* scratch,
                       int prof_key);
+// Split storage on the same layouts: g = A^T r (r df pairs, g FP64: hot
+// columns from the panels, the rest from the cold CRS); the forward head's
+// partial per row into hd.ypan2 and the tail's product into wtx (df pairs).
+void panel_ensure_split(fvg_ctx* c, DevPanels& pn);
+i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn);
+void panel_trans_mv_split(fvg_ctx* c, DevPanels& pn, const void* r, double* y, void* scratch);
+void head_pass_split(fvg_ctx* c, DevPanels& hd, const void* w, void* wtx, void* scratch);
 
 // ------------------------------------------------------- split storage
 // FP64 values kept as an FP32 plane plus a BF16 residual plane, multiplied
 // in double-FP32 arithmetic (split.cu).  Vectors are df pairs (float2).
 void df64_init(fvg_ctx* c);  // the exp table of the df64 math, once per device
 void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master);
+// lo = BF16(v - FP32 plane) for n values of planes[] (the FP64 and FP32 planes)
+void split_residual_plane(fvg_ctx* c, const DBuf* planes, i64 n, int master, DBuf& lo);
 void split_vector(fvg_ctx* c, const double* x, void* y, i64 n);  // y: float2[n]
 i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a);
 // y = A x, x float2 pairs; y FP64 (y_df false) or float2 pairs

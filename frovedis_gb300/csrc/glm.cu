@@ -564,12 +564,26 @@ struct Evaluator {
     const i64 g = glm_split_grid(c, op->m);
     gpart.alloc(sizeof(double) * 2 * g + 256, c->stream);
     FVG_CUDA(cudaMemsetAsync((char*)gpart.p + sizeof(double) * 2 * g, 0, 256, c->stream));
+    // the row-panel layout (backward) and the forward head, when the matrix has them
+    if (op->M && op->fmt == FVG_CRS) {
+      PT = panels_for(c, op->M);
+      if (PT) {
+        panel_ensure_split(c, *PT);
+        s3.alloc(panel_split_scratch_bytes(c, *PT), c->stream);
+      }
+      HD = head_for(c, op->M);
+      if (HD) {
+        panel_ensure_split(c, *HD);
+        s4.alloc(panel_split_scratch_bytes(c, *HD), c->stream);
+      }
+    }
   }
   void eval_split(const void* x, const double* b, double* grad, double* out) {
     const i64 g = glm_split_grid(c, op->m);
     {
       ProfScope ps(c, P_PASS1);
-      crs_pass_split(c, *op->A, x, true, wtx2.p, s1.p, P_NKEYS);
+      if (HD) head_pass_split(c, *HD, x, wtx2.p, s4.p);
+      else crs_pass_split(c, *op->A, x, true, wtx2.p, s1.p, P_NKEYS);
       GlmSplitArgs e;
       e.lab = label_f.p;
       e.sw = sw ? sw_f.p : nullptr;
@@ -582,9 +596,14 @@ struct Evaluator {
       e.ticket = (unsigned*)((char*)gpart.p + sizeof(double) * 2 * g);
       e.out = out;
       e.grad_bias = grad + op->n;
-      glm_split_rows(c, wtx2.p, nullptr, op->m, e);
+      glm_split_rows(c, wtx2.p, HD ? HD->ypan2.p : nullptr, op->m, e);
     }
-    crs_pass_split(c, *op->AT, r.p, false, grad, s2.p, P_PASS2);
+    if (PT) {
+      ProfScope ps(c, P_PASS2);
+      panel_trans_mv_split(c, *PT, r.p, grad, s3.p);
+    } else {
+      crs_pass_split(c, *op->AT, r.p, false, grad, s2.p, P_PASS2);
+    }
   }
   // FP32 / BF16 values: the row-panel layout for the backward product when
   // the matrix has one (CRS and ELL operands share the transposed CRS), and

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "df64.cuh"
 
 namespace fvg {
 
@@ -561,17 +562,230 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
   }
 }
 
+// ------------------------------------------------------ split storage
+// The row-panel / forward-head kernel for split values (FP32 value + BF16
+// residual per entry, df64 products: df64.cuh).  Same layout and work items
+// as k_panel; the staged entry is 8 bytes (uint16 slot, FP32 value, BF16
+// residual), so one CTA of kSplitWarps warps per SM stages its items beside a
+// vector slice kept as an FP32 plane plus a BF16 plane of its remainders (6
+// bytes a row: the slice's own rounding, 2^-33 relative, matches the values').
+// Each entry's product is made exact as p + t (an FMA) and overwrites the
+// staged entry; rows are summed with TwoSum; partial sums are df pairs.
+constexpr int kSplitWarps = 16;
+struct SplitSmem {
+  static constexpr int kCap = kWarpTile + 16;          // entries of one copy
+  static constexpr int kHiB = kCap * 2;                // offset of the FP32 values
+  static constexpr int kLoB = kHiB + kCap * 4;         // offset of the BF16 residuals
+  static constexpr int kStageB = kLoB + kCap * 2;      // = kCap * 8: room for the (p, t) products
+  static constexpr int kSoffB = ((kTileRows + 1) * 2 + 15) / 16 * 16;
+  static constexpr int kWarpB = kStageB + kSoffB;
+  static constexpr int kStatic = 16 * kSplitWarps + kSplitWarps * kWarpB;
+};
+
+struct PanSK {
+  const i32* poff;
+  const uint16_t* prow;
+  const float* vh;
+  const unsigned short* vl;
+  const float2* x;  // df pairs: r (row panels) or w (forward head)
+  i64 m, rows, npanels;
+  const Item* items;
+  const i32* pitem0;
+  const i32* long_rows;
+  const i32* plong0;
+  const i32* long_piece0;
+  float2* partials;
+  float2* ypan;
+  unsigned* err;
+  unsigned wait_limit;
+  const i32* xmap;  // forward head: the slice is x[xmap[0..rows)], staged once
+  i64 group;
+};
+
+__device__ __forceinline__ df shfl_xor_df(df a, int o) {
+  return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+
+__global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK p) {
+  using SM = SplitSmem;
+  constexpr int NW = kSplitWarps;
+  constexpr int NR2 = (SM::kCap + 63) / 64;  // pair rounds of a staged copy
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + 2 * w;
+  unsigned char* area = smem + 16 * NW + w * SM::kWarpB;
+  unsigned short* soff = reinterpret_cast<unsigned short*>(area + SM::kStageB);
+  float2* prod2 = reinterpret_cast<float2*>(area);
+  float4* prod4 = reinterpret_cast<float4*>(area);
+  float* xh = reinterpret_cast<float*>(smem + SM::kStatic);
+  bf16* xl = reinterpret_cast<bf16*>(smem + SM::kStatic + p.rows * 4);
+  if (lane == 0) mbar_init(bar, 1);
+  fence_mbar_init();
+  __syncthreads();
+  const uint64_t pol = policy_evict_first();
+  unsigned parity = 0;
+  bool pend = false, dead = false;
+  const bool shared = p.xmap != nullptr;
+  const int nunits = (int)((p.npanels + p.group - 1) / p.group);
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const int pn = u * (int)p.group, pe = (int)min((i64)pn + p.group, p.npanels);
+    const i64 base = shared ? 0 : (i64)pn * p.rows;
+    const int nr = shared ? (int)p.rows : (int)min(p.rows, p.m - base);
+    __syncthreads();
+    if (!shared || u == blockIdx.x)
+      for (int i = threadIdx.x; i < nr; i += NW * 32) {
+        const float2 v = __ldg(p.x + (shared ? (i64)p.xmap[i] : base + i));
+        xh[i] = v.x;
+        xl[i] = __float2bfloat16_rn(v.y);
+      }
+    __syncthreads();
+    const int t1 = p.pitem0[pe];
+    int t = p.pitem0[pn] + w;
+    Item nx = (t < t1) ? p.items[t] : Item{0, 0, 0, 0};
+    for (; t < t1 && !dead; t += NW) {
+      const Item it = nx;
+      if (t + NW < t1) nx = p.items[t + NW];
+      const int q0 = it.e0 & ~7, q1 = (it.e1 + 7) & ~7;
+      const unsigned n = (unsigned)(q1 - q0);
+      if (lane == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, n * 8u);
+        if (n > 0) {
+          bulk_g2s(area, p.prow + q0, n * 2u, bar, pol);
+          bulk_g2s(area + SM::kHiB, p.vh + q0, n * 4u, bar, pol);
+          bulk_g2s(area + SM::kLoB, p.vl + q0, n * 2u, bar, pol);
+        }
+      }
+      pend = true;
+      if (it.r1 >= 0)
+        for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = (unsigned short)(__ldg(p.poff + it.r0 + k) - q0);
+      if (!mbar_wait_bounded(bar, parity, p.err, p.wait_limit)) {
+        dead = true;
+        break;
+      }
+      parity ^= 1u;
+      pend = false;
+      __syncwarp();
+      {
+        // every staged pair into registers first: the products overwrite them
+        const unsigned* sidx2 = reinterpret_cast<const unsigned*>(area);
+        const float2* shi2 = reinterpret_cast<const float2*>(area + SM::kHiB);
+        const unsigned* slo2 = reinterpret_cast<const unsigned*>(area + SM::kLoB);
+        const int n2 = (int)(n >> 1);
+        unsigned c[NR2], lo[NR2];
+        float2 hi[NR2];
+#pragma unroll
+        for (int q = 0; q < NR2; q++) {
+          const int k2 = q * 32 + lane;
+          if (k2 < n2) {
+            c[q] = sidx2[k2];
+            hi[q] = shi2[k2];
+            lo[q] = slo2[k2];
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < NR2; q++) {
+          const int k2 = q * 32 + lane;
+          if (k2 < n2) {
+            const unsigned c0 = c[q] & 0xffffu, c1 = c[q] >> 16;
+            const float2 x0 = make_float2(xh[c0], __bfloat162float(xl[c0]));
+            const float2 x1 = make_float2(xh[c1], __bfloat162float(xl[c1]));
+            float p0, t0, p1, t1;
+            df_prod(hi[q].x, __uint_as_float(lo[q] << 16), x0, p0, t0);
+            df_prod(hi[q].y, __uint_as_float(lo[q] & 0xffff0000u), x1, p1, t1);
+            prod4[k2] = make_float4(p0, t0, p1, t1);
+          }
+        }
+      }
+      __syncwarp();
+      if (it.r1 >= 0) {
+        const int R = it.r1 - it.r0;
+        const int Gl = lanes_per_row(R);
+        const int per_round = 32 / Gl;
+        for (int rb = 0; rb < R; rb += per_round) {
+          const int j = rb + lane / Gl, sub = lane % Gl;
+          DfAcc acc;
+          if (j < R) {
+            const int s = soff[j], e = soff[j + 1];
+            for (int k = s + sub; k < e; k += Gl) {
+              const float2 v = prod2[k];
+              acc.add(v.x, v.y);
+            }
+          }
+          df a = acc.get();
+          for (int o = Gl >> 1; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
+          if (j < R && sub == 0) p.ypan[it.r0 + j] = df_pack(a);
+        }
+      } else {
+        DfAcc acc;
+        const int e = it.e1 - q0;
+        for (int k = it.e0 - q0 + lane; k < e; k += 32) {
+          const float2 v = prod2[k];
+          acc.add(v.x, v.y);
+        }
+        df a = acc.get();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
+        if (lane == 0) p.partials[-1 - it.r1] = df_pack(a);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    const int l1 = p.plong0[pe];
+    for (int L = p.plong0[pn] + w; L < l1; L += NW) {
+      const int c0 = p.long_piece0[L], c1 = p.long_piece0[L + 1];
+      df a = {0.f, 0.f};
+      for (int j = c0 + lane; j < c1; j += 32) a = df_add(a, df_unpack(__ldcg(p.partials + j)));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
+      if (lane == 0) p.ypan[p.long_rows[L]] = df_pack(a);
+    }
+  }
+  // a warp that gave up still drains its copy in flight (default budget)
+  if (pend) mbar_wait_bounded(bar, parity, nullptr, kCopyPolls);
+}
+
+// g[hot[h]] = sum over panels of the df partials ypan[panel*nhot + h]:
+// 32 columns per CTA of 1024 threads, warp w adds panels w, w+32, ...; warp
+// 0 adds the 32 warp sums in order; FP64 result.
+__global__ void __launch_bounds__(1024) k_panel_colsum_split(const float2* __restrict__ ypan,
+                                                             const i32* __restrict__ hot, i64 nhot, i64 np,
+                                                             double* __restrict__ y) {
+  __shared__ float2 part[32][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (i64 h0 = (i64)blockIdx.x * 32; h0 < nhot; h0 += (i64)gridDim.x * 32) {
+    const i64 h = h0 + lane;
+    df a = {0.f, 0.f};
+    if (h < nhot)
+      for (i64 pn = w; pn < np; pn += 32) a = df_add(a, df_unpack(__ldcs(ypan + pn * nhot + h)));
+    part[w][lane] = df_pack(a);
+    __syncthreads();
+    if (w == 0 && h < nhot) {
+      df s = {0.f, 0.f};
+#pragma unroll 8
+      for (int q = 0; q < 32; q++) s = df_add(s, df_unpack(part[q][lane]));
+      y[hot[h]] = df_to_double(s);
+    }
+    __syncthreads();
+  }
+}
+
+int panel_split_smem_bytes(i64 rows) { return SplitSmem::kStatic + (int)(rows * 6); }
+
 template <class VT> int panel_smem_bytes(i64 rows) { return PanelSmem<VT>::kStatic + (int)(rows * 4); }
 
-// Tallest panel one CTA can stage beside the FP32 staging buffers (the
-// larger ones: a layout serves FP32 and BF16 values).
+// Tallest panel (or head) one CTA can stage beside the staging buffers, for
+// the FP32 / BF16 kernel and the split kernel alike.
 i64 panel_rows_cap(fvg_ctx* c) {
   int per_sm = 0, reserved = 0, optin = 0;
   FVG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device));
   FVG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->device));
   FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
   const i64 per_cta = std::min<i64>((i64)per_sm - (i64)reserved, (i64)optin);
-  i64 cap = (per_cta - PanelSmem<float>::kStatic) / 4;
+  // the FP32 kernel stages 4 bytes a row, the split kernel 6 (beside
+  // smaller staging buffers): a layout serves both
+  i64 cap = std::min<i64>((per_cta - PanelSmem<float>::kStatic) / 4, (per_cta - SplitSmem::kStatic) / 6);
   cap = std::min<i64>(cap, 65536);  // panel-local rows are uint16
   return cap & ~3ll;
 }
@@ -1031,6 +1245,94 @@ void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, co
   LogregEpi t = lr;
   t.ybase = hd.ypan.as<float>();
   crs_pass(c, hd.cold, storage, FVG_F32, w, FVG_F32, nullptr, EPI_LOGREG, &t, scratch, P_NKEYS);
+}
+
+}  // namespace fvg
+
+// ------------------------------------------------------------ split storage
+namespace fvg {
+
+namespace {
+void launch_panel_split(fvg_ctx* c, const PanSK& k, i64 rows) {
+  constexpr int threads = kSplitWarps * 32;
+  static std::mutex mu;  // contexts of different host threads launch concurrently
+  static std::vector<int> attr_set;
+  const int smem = panel_split_smem_bytes(rows);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (std::find(attr_set.begin(), attr_set.end(), c->device) == attr_set.end()) {
+      int optin = 0;
+      FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+      FVG_CUDA(cudaFuncSetAttribute(k_panel_split, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+      attr_set.push_back(c->device);
+    }
+  }
+  const int blocks = occupancy_blocks((const void*)k_panel_split, threads, (size_t)smem);
+  const i64 nunits = (k.npanels + k.group - 1) / k.group;
+  const int grid = (int)std::max<i64>(1, std::min<i64>(nunits, (i64)blocks * c->num_sms));
+  k_panel_split<<<grid, threads, smem, c->stream>>>(k);
+  check_launch("k_panel_split");
+  count_launch(c);
+}
+
+PanSK split_args(fvg_ctx* c, DevPanels& pn, const void* x) {
+  PanSK k;
+  k.poff = pn.poff.as<i32>();
+  k.prow = pn.prow.as<uint16_t>();
+  k.vh = pn.val[FVG_F32].as<float>();
+  k.vl = pn.lo.as<unsigned short>();
+  k.x = (const float2*)x;
+  k.m = pn.m;
+  k.rows = pn.rows;
+  k.npanels = pn.npanels;
+  k.items = pn.items.as<Item>();
+  k.pitem0 = pn.pitem0.as<i32>();
+  k.long_rows = pn.long_rows.as<i32>();
+  k.plong0 = pn.plong0.as<i32>();
+  k.long_piece0 = pn.long_piece0.as<i32>();
+  k.partials = pn.partials2.as<float2>();
+  k.ypan = pn.ypan2.as<float2>();
+  k.err = c->dev_err;
+  k.wait_limit = copy_polls(c);
+  k.xmap = nullptr;
+  k.group = 1;
+  return k;
+}
+}  // namespace
+
+void panel_ensure_split(fvg_ctx* c, DevPanels& pn) {
+  if (pn.rows * 6 + SplitSmem::kStatic > (i64)panel_split_smem_bytes(panel_rows_cap(c)))
+    fail(FVG_ERR_INTERNAL, "panel layout too tall for the split kernel");
+  ensure_plane_generic(c, pn.val, pn.E, FVG_F32, pn.master);
+  if (!pn.lo.p) split_residual_plane(c, pn.val, pn.E, pn.master, pn.lo);
+  crs_ensure_split(c, pn.cold, pn.master);
+  if (!pn.ypan2.p) {
+    pn.ypan2.alloc(sizeof(float2) * std::max<i64>(pn.npanels * pn.nhot, 1), c->stream);
+    pn.partials2.alloc(sizeof(float2) * std::max<i64>(pn.npieces, 1), c->stream);
+  }
+}
+
+i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn) { return crs_split_scratch_bytes(c, pn.cold); }
+
+void panel_trans_mv_split(fvg_ctx* c, DevPanels& pn, const void* r, double* y, void* scratch) {
+  panel_ensure_split(c, pn);
+  // cold columns (and zeros for the hot ones) by the transposed CRS kernel
+  crs_pass_split(c, pn.cold, r, false, y, scratch, P_NKEYS);
+  launch_panel_split(c, split_args(c, pn, r), pn.rows);
+  const unsigned cg = (unsigned)std::max<i64>(1, std::min<i64>((pn.nhot + 31) / 32, 2 * c->num_sms));
+  k_panel_colsum_split<<<cg, 1024, 0, c->stream>>>(pn.ypan2.as<float2>(), pn.hot_cols.as<i32>(), pn.nhot,
+                                                    pn.npanels, y);
+  check_launch("k_panel_colsum_split");
+  count_launch(c);
+}
+
+void head_pass_split(fvg_ctx* c, DevPanels& hd, const void* w, void* wtx, void* scratch) {
+  panel_ensure_split(c, hd);
+  PanSK k = split_args(c, hd, w);
+  k.xmap = hd.hot_cols.as<i32>();
+  k.group = (hd.npanels + c->num_sms - 1) / c->num_sms;  // a CTA's whole share of the stretches
+  launch_panel_split(c, k, hd.rows);
+  crs_pass_split(c, hd.cold, w, true, wtx, scratch, P_NKEYS);
 }
 
 }  // namespace fvg

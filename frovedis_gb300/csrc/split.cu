@@ -276,18 +276,16 @@ __global__ void __launch_bounds__(kSplitThreads) k_glm_split(const GlmSplitK p) 
 }  // namespace
 
 // ------------------------------------------------------------------ host
-void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) {
-  crs_ensure_plane(c, a, FVG_F32, master);
-  if (a.lo.p) return;
-  DBuf lo;
-  lo.alloc(sizeof(bf16) * (size_t)(a.nnz + kPad), c->stream);
-  FVG_CUDA(cudaMemsetAsync(lo.p, 0, sizeof(bf16) * (size_t)(a.nnz + kPad), c->stream));
-  if (master == FVG_F64 && a.nnz > 0) {
+void split_residual_plane(fvg_ctx* c, const DBuf* planes, i64 n, int master, DBuf& lo) {
+  DBuf out;
+  out.alloc(sizeof(bf16) * (size_t)(n + kPad), c->stream);
+  FVG_CUDA(cudaMemsetAsync(out.p, 0, sizeof(bf16) * (size_t)(n + kPad), c->stream));
+  if (master == FVG_F64 && n > 0) {  // FP32 / BF16 uploads: the FP32 plane is exact, the residual 0
     DBuf bad;
     bad.alloc(sizeof(unsigned), c->stream);
     FVG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), c->stream));
-    k_split_plane<<<grid_rows(c, a.nnz, 16), kSplitThreads, 0, c->stream>>>(
-        a.val[FVG_F64].as<double>(), a.val[FVG_F32].as<float>(), lo.as<bf16>(), a.nnz, bad.as<unsigned>());
+    k_split_plane<<<grid_rows(c, n, 16), kSplitThreads, 0, c->stream>>>(
+        planes[FVG_F64].as<double>(), planes[FVG_F32].as<float>(), out.as<bf16>(), n, bad.as<unsigned>());
     check_launch("split_plane");
     count_launch(c);
     unsigned hb = 0;
@@ -295,7 +293,12 @@ void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) {
     FVG_CUDA(cudaStreamSynchronize(c->stream));
     if (hb) fail(FVG_ERR_INVALID_ARG, "split storage: a value lies outside the FP32 range");
   }
-  a.lo = std::move(lo);
+  lo = std::move(out);
+}
+
+void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) {
+  crs_ensure_plane(c, a, FVG_F32, master);
+  if (!a.lo.p) split_residual_plane(c, a.val, a.nnz, master, a.lo);
 }
 
 void split_vector(fvg_ctx* c, const double* x, void* y, i64 n) {

@@ -195,3 +195,83 @@ def test_split_rejects_values_beyond_fp32(ctx):
     A = ctx.matrix(2, 2, off, idx, np.array([1.0, 1e300, 2.0]))
     with pytest.raises(fv.FvgError):
         A.spmv(np.ones(2), storage="split")
+
+
+def _zipf(m, n, lam=30.0, seed=3, val_kind="lognormal"):
+    from frovedis_gb300 import datagen
+    off, idx, val, label = datagen.generate(datagen.Spec(m=m, n=n, lam=lam, seed=seed, val_kind=val_kind))
+    return oracle.CRS(m, n, off, idx, val), label
+
+
+@pytest.mark.parametrize("rows,mpp", [(512, 1.0), (1000, 2.0), (4, 0.5), (8192, 1.0)])
+def test_split_panel_trans_mv(ctx, rows, mpp):
+    # the row-panel layout on split values: hot columns from the panels,
+    # the rest from the cold transposed CRS; FP64 oracle on the FP64 values
+    a, _ = _zipf(12000, 900, seed=rows)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    A.set_panels(rows, mpp)
+    rng = np.random.default_rng(rows)
+    r = rng.standard_normal(a.m)
+    z = A.trans_mv(r, storage="split")
+    assert A.panel_info()[2] > 0
+    at = oracle.transpose(a)
+    zo = oracle.spmv(at, r)
+    assert np.all(np.abs(z - zo) <= SPLIT_RTOL * _abs_rowsum(at, r) + 1e-300)
+    assert np.array_equal(A.trans_mv(r, storage="split"), z)
+
+
+def test_split_panel_long_segments(ctx):
+    # a column with more entries in one panel than a work item holds (its
+    # pieces are added after the CTA barrier) and rows of one entry
+    rng = np.random.default_rng(17)
+    m, n = 20000, 300
+    rows = [np.sort(rng.choice(n, rng.integers(0, 6), replace=False)) for _ in range(m)]
+    for i in range(0, m, 3):  # column 7 in every third row: ~6,700 entries
+        if 7 not in rows[i]:
+            rows[i] = np.sort(np.append(rows[i], 7))
+    off = np.concatenate([[0], np.cumsum([len(x) for x in rows])]).astype(np.int32)
+    idx = np.concatenate(rows).astype(np.int32)
+    val = rng.standard_normal(int(off[-1])) * np.exp(rng.uniform(-2, 2, int(off[-1])))
+    a = oracle.CRS(m, n, off, idx, val)
+    A = ctx.matrix(m, n, off, idx, val)
+    A.set_panels(19996, 1.0)
+    r = rng.standard_normal(m)
+    z = A.trans_mv(r, storage="split")
+    at = oracle.transpose(a)
+    assert np.all(np.abs(z - oracle.spmv(at, r)) <= SPLIT_RTOL * _abs_rowsum(at, r) + 1e-300)
+
+
+@pytest.mark.parametrize("head,panels", [(64, 0), (700, 512), (1500, 0), (0, 256)])
+def test_split_head_and_panels_eval(ctx, head, panels):
+    # evaluation with the forward head and/or the row panels forced on
+    a, label = _zipf(9000, 1600, seed=head + panels)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    A.set_head(head)
+    A.set_panels(panels, 1.0)
+    rng = np.random.default_rng(4)
+    w = rng.standard_normal(a.n) * 0.2
+    sw = rng.uniform(0.5, 2.0, a.m)
+    g, loss = fv.logreg_eval(A, label, w, b=0.4, intercept=True, sample_weight=sw, storage="split")
+    assert A.head_info()[0] == head and (A.panel_info()[2] > 0) == (panels > 0)
+    go, lo = oracle.logreg_eval(a, label, w, b=0.4, intercept=True, sw=sw)
+    colscale = oracle.spmv(oracle.transpose(oracle.CRS(a.m, a.n, a.off, a.idx, np.abs(a.val))), sw)
+    assert abs(loss - lo) <= 1e-10 * abs(lo)
+    assert np.all(np.abs(g[:-1] - go[:-1]) <= 1e-9 * colscale + 1e-12)
+    assert abs(g[-1] - go[-1]) <= 1e-9 * np.sum(sw)
+    g2, loss2 = fv.logreg_eval(A, label, w, b=0.4, intercept=True, sample_weight=sw, storage="split")
+    assert loss2 == loss and np.array_equal(g2, g)
+
+
+def test_split_head_and_panels_lbfgs(ctx):
+    # training with both layouts on: the FP64 bar and the same decisions
+    a, label = _zipf(20000, 3000, seed=31)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    A.set_head(1024)
+    A.set_panels(2048, 1.0)
+    kw = dict(num_iter=20, reg_type="L2", reg_param=1e-3, w0=np.zeros(a.n))
+    r = fv.logreg_lbfgs(A, label, trace=True, storage="split", **kw)
+    ro = oracle.logreg_lbfgs(a, label, **kw)
+    assert r["n_iter"] == ro["n_iter"]
+    assert np.array_equal(r["trace"][:, 1], ro["trace"][:, 1])
+    assert abs(r["loss"] - ro["loss"]) <= 1e-6 * abs(ro["loss"])
+    assert np.max(np.abs(r["w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))
