@@ -143,6 +143,14 @@ struct DevHYB {  // jds_crs_hybrid_local (jds_crs_hybrid.hpp:8-153)
   bool all_crs = false;  // m <= threshold: the whole matrix is the CRS part
 };
 
+// Work items over a panel layout's rows, panel by panel (Item as in Sched):
+// a panel's items start at pitem0[panel], its long rows at plong0[panel].
+struct PanelItems {
+  int tile = 0;
+  i64 nitems = 0, nlong = 0, npieces = 0;
+  DBuf items, pitem0, long_rows, plong0, long_piece0;
+};
+
 // Row-panel layout of the backward product g = A^T r (FP32 arithmetic).
 // A's rows are cut into panels of `rows` consecutive rows; a CTA stages one
 // panel's slice of r in shared memory and sums, for every hot column h, the
@@ -168,7 +176,10 @@ struct DevPanels {
   DBuf items, pitem0, long_rows, plong0, long_piece0;
   DBuf ypan;                        // float [npanels*nhot]
   DBuf partials;                    // float [npieces]
-  DBuf ypan2, partials2;            // split storage: the same as df pairs (float2)
+  // split storage: its own work items (smaller staging buffers) and df-pair
+  // partial sums (float2)
+  std::unique_ptr<PanelItems> split_items;
+  DBuf ypan2, partials2;
   // forward head (shared = true): every CTA stages w at the columns
   // hot_cols[0..rows) once; panels are stretches of nhot rows of A; `cold`
   // holds the rest of each row (m rows, int32 column ids)

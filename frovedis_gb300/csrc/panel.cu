@@ -564,16 +564,20 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
 
 // ------------------------------------------------------ split storage
 // The row-panel / forward-head kernel for split values (FP32 value + BF16
-// residual per entry, df64 products: df64.cuh).  Same layout and work items
-// as k_panel; the staged entry is 8 bytes (uint16 slot, FP32 value, BF16
-// residual), so one CTA of kSplitWarps warps per SM stages its items beside a
-// vector slice kept as an FP32 plane plus a BF16 plane of its remainders (6
-// bytes a row: the slice's own rounding, 2^-33 relative, matches the values').
-// Each entry's product is made exact as p + t (an FMA) and overwrites the
-// staged entry; rows are summed with TwoSum; partial sums are df pairs.
+// residual per entry, df64 products: df64.cuh).  Same layout as k_panel; the
+// staged entry is 8 bytes (uint16 slot, FP32 value, BF16 residual) and the
+// vector slice keeps both FP32 words of each df pair (8 bytes a row: rounding
+// the slice's low word would add noise that changes from one evaluation to
+// the next and, unlike the fixed rounding of the values, does not cancel in
+// the L-BFGS gradient differences).  To fit a panel beside the staging
+// buffers, one CTA of kSplitWarps warps per SM walks its own work items of at
+// most kSplitTile entries.  Each entry's product is made exact as p + t (an
+// FMA) and overwrites the staged entry; rows are summed with TwoSum; partial
+// sums are df pairs.
 constexpr int kSplitWarps = 16;
+constexpr int kSplitTile = 256;
 struct SplitSmem {
-  static constexpr int kCap = kWarpTile + 16;          // entries of one copy
+  static constexpr int kCap = kSplitTile + 16;         // entries of one copy
   static constexpr int kHiB = kCap * 2;                // offset of the FP32 values
   static constexpr int kLoB = kHiB + kCap * 4;         // offset of the BF16 residuals
   static constexpr int kStageB = kLoB + kCap * 2;      // = kCap * 8: room for the (p, t) products
@@ -618,7 +622,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
   float2* prod2 = reinterpret_cast<float2*>(area);
   float4* prod4 = reinterpret_cast<float4*>(area);
   float* xh = reinterpret_cast<float*>(smem + SM::kStatic);
-  bf16* xl = reinterpret_cast<bf16*>(smem + SM::kStatic + p.rows * 4);
+  float* xl = reinterpret_cast<float*>(smem + SM::kStatic + p.rows * 4);
   if (lane == 0) mbar_init(bar, 1);
   fence_mbar_init();
   __syncthreads();
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
       for (int i = threadIdx.x; i < nr; i += NW * 32) {
         const float2 v = __ldg(p.x + (shared ? (i64)p.xmap[i] : base + i));
         xh[i] = v.x;
-        xl[i] = __float2bfloat16_rn(v.y);
+        xl[i] = v.y;
       }
     __syncthreads();
     const int t1 = p.pitem0[pe];
@@ -689,8 +693,8 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           const int k2 = q * 32 + lane;
           if (k2 < n2) {
             const unsigned c0 = c[q] & 0xffffu, c1 = c[q] >> 16;
-            const float2 x0 = make_float2(xh[c0], __bfloat162float(xl[c0]));
-            const float2 x1 = make_float2(xh[c1], __bfloat162float(xl[c1]));
+            const float2 x0 = make_float2(xh[c0], xl[c0]);
+            const float2 x1 = make_float2(xh[c1], xl[c1]);
             float p0, t0, p1, t1;
             df_prod(hi[q].x, __uint_as_float(lo[q] << 16), x0, p0, t0);
             df_prod(hi[q].y, __uint_as_float(lo[q] & 0xffff0000u), x1, p1, t1);
@@ -771,7 +775,7 @@ __global__ void __launch_bounds__(1024) k_panel_colsum_split(const float2* __res
   }
 }
 
-int panel_split_smem_bytes(i64 rows) { return SplitSmem::kStatic + (int)(rows * 6); }
+int panel_split_smem_bytes(i64 rows) { return SplitSmem::kStatic + (int)(rows * 8); }
 
 template <class VT> int panel_smem_bytes(i64 rows) { return PanelSmem<VT>::kStatic + (int)(rows * 4); }
 
@@ -783,9 +787,9 @@ i64 panel_rows_cap(fvg_ctx* c) {
   FVG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->device));
   FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
   const i64 per_cta = std::min<i64>((i64)per_sm - (i64)reserved, (i64)optin);
-  // the FP32 kernel stages 4 bytes a row, the split kernel 6 (beside
+  // the FP32 kernel stages 4 bytes a row, the split kernel 8 (beside
   // smaller staging buffers): a layout serves both
-  i64 cap = std::min<i64>((per_cta - PanelSmem<float>::kStatic) / 4, (per_cta - SplitSmem::kStatic) / 6);
+  i64 cap = std::min<i64>((per_cta - PanelSmem<float>::kStatic) / 4, (per_cta - SplitSmem::kStatic) / 8);
   cap = std::min<i64>(cap, 65536);  // panel-local rows are uint16
   return cap & ~3ll;
 }
@@ -854,6 +858,34 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
 }
 
 namespace {
+
+// The split kernel's work items: the same packing with kSplitTile-entry items
+void pack_split_items(fvg_ctx* c, DevPanels& pn) {
+  const i64 nhot = pn.nhot, np = pn.npanels;
+  PackOut o;
+  const i64 sub = std::max<i64>(1, (nhot + 4095) / 4096);
+  device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kSplitTile, o, sub);
+  auto it = std::make_unique<PanelItems>();
+  it->tile = kSplitTile;
+  it->nitems = o.nitems;
+  it->nlong = o.nlong;
+  it->npieces = o.npieces;
+  it->items = std::move(o.items);
+  it->long_rows = std::move(o.long_rows);
+  it->long_piece0 = std::move(o.long_piece0);
+  const i64 nc = np * sub;
+  std::vector<i32> pi((size_t)np + 1), pl((size_t)np + 1);
+  for (i64 q = 0; q <= np; q++) {
+    pi[(size_t)q] = o.base[(size_t)(q * sub)];
+    pl[(size_t)q] = o.base[(size_t)((nc + 1) + q * sub)];
+  }
+  it->pitem0.alloc(sizeof(i32) * (np + 1), c->stream);
+  it->plong0.alloc(sizeof(i32) * (np + 1), c->stream);
+  FVG_CUDA(cudaMemcpyAsync(it->pitem0.p, pi.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaMemcpyAsync(it->plong0.p, pl.data(), sizeof(i32) * (np + 1), cudaMemcpyHostToDevice, c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host arrays go out of scope
+  pn.split_items = std::move(it);
+}
 
 void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
   PackOut o;
@@ -1285,11 +1317,12 @@ PanSK split_args(fvg_ctx* c, DevPanels& pn, const void* x) {
   k.m = pn.m;
   k.rows = pn.rows;
   k.npanels = pn.npanels;
-  k.items = pn.items.as<Item>();
-  k.pitem0 = pn.pitem0.as<i32>();
-  k.long_rows = pn.long_rows.as<i32>();
-  k.plong0 = pn.plong0.as<i32>();
-  k.long_piece0 = pn.long_piece0.as<i32>();
+  const PanelItems& si = *pn.split_items;
+  k.items = si.items.as<Item>();
+  k.pitem0 = si.pitem0.as<i32>();
+  k.long_rows = si.long_rows.as<i32>();
+  k.plong0 = si.plong0.as<i32>();
+  k.long_piece0 = si.long_piece0.as<i32>();
   k.partials = pn.partials2.as<float2>();
   k.ypan = pn.ypan2.as<float2>();
   k.err = c->dev_err;
@@ -1301,14 +1334,15 @@ PanSK split_args(fvg_ctx* c, DevPanels& pn, const void* x) {
 }  // namespace
 
 void panel_ensure_split(fvg_ctx* c, DevPanels& pn) {
-  if (pn.rows * 6 + SplitSmem::kStatic > (i64)panel_split_smem_bytes(panel_rows_cap(c)))
+  if (pn.rows > panel_rows_cap(c))
     fail(FVG_ERR_INTERNAL, "panel layout too tall for the split kernel");
   ensure_plane_generic(c, pn.val, pn.E, FVG_F32, pn.master);
   if (!pn.lo.p) split_residual_plane(c, pn.val, pn.E, pn.master, pn.lo);
   crs_ensure_split(c, pn.cold, pn.master);
+  if (!pn.split_items) pack_split_items(c, pn);
   if (!pn.ypan2.p) {
     pn.ypan2.alloc(sizeof(float2) * std::max<i64>(pn.npanels * pn.nhot, 1), c->stream);
-    pn.partials2.alloc(sizeof(float2) * std::max<i64>(pn.npieces, 1), c->stream);
+    pn.partials2.alloc(sizeof(float2) * std::max<i64>(pn.split_items->npieces, 1), c->stream);
   }
 }
 

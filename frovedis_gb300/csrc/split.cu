@@ -260,17 +260,23 @@ __global__ void __launch_bounds__(kSplitThreads) k_glm_split(const GlmSplitK p) 
   __syncthreads();
   if (threadIdx.x == 0) last = (atomicAdd(p.ticket, 1u) == gridDim.x - 1);
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
+  // the last CTA: thread t adds CTAs t, t + 256, ... (compensated), then a
+  // fixed tree over the threads
   CSum l, s;
-  for (unsigned q = 0; q < gridDim.x; q++) {
+  for (unsigned q = threadIdx.x; q < gridDim.x; q += kSplitThreads) {
     l.add(__ldcg(&p.cta_part[2 * q]));
     s.add(__ldcg(&p.cta_part[2 * q + 1]));
   }
-  p.out[0] = l.total();
-  p.out[1] = p.icpt ? s.total() : 0.0;
-  if (p.grad_bias) *p.grad_bias = p.icpt ? s.total() : 0.0;
-  *p.ticket = 0u;
+  double tl2 = 0.0, tb2 = 0.0;
+  block_csum2(l.total(), s.total(), &tl2, &tb2);
+  if (threadIdx.x == 0) {
+    p.out[0] = tl2;
+    p.out[1] = p.icpt ? tb2 : 0.0;
+    if (p.grad_bias) *p.grad_bias = p.icpt ? tb2 : 0.0;
+    *p.ticket = 0u;
+  }
 }
 
 }  // namespace

@@ -212,6 +212,64 @@ crs_matrix_local<T, I, O> make_crs_matrix_local_loadbinary(const std::string& in
   return detail::to_local<T, I, O>(d.h);
 }
 
+// ------------------------------------------------ distributed containers
+// The reference's distributed types hold one block per MPI rank:
+// crs_matrix<T,I,O> (matrix/crs_matrix.hpp) a node_local<crs_matrix_local>
+// plus the global num_row / num_col, dvector<T> (core/dvector.hpp) a
+// distributed vector.  One process drives one GPU here, so each holds a single
+// block; gather() returns it as the reference's gather() returns the
+// concatenated blocks.  The trainers take them as the reference's do
+// (logistic_regression_with_lbfgs.hpp:11-128, logistic_regression_with_sgd.hpp:
+// 11-128), so reference programs such as samples/glm/lr.cc compile unchanged.
+template <class T> struct dvector {
+  dvector() = default;
+  explicit dvector(const std::vector<T>& v) : val(v) {}
+  explicit dvector(std::vector<T>&& v) : val(std::move(v)) {}
+  std::vector<T> gather() const { return val; }
+  size_t size() const { return val.size(); }
+  void clear() { std::vector<T>().swap(val); }
+  std::vector<T> val;  // the one block
+};
+template <class T> dvector<T> make_dvector_scatter(const std::vector<T>& v) { return dvector<T>(v); }
+
+template <class T, class I = size_t, class O = size_t> struct crs_matrix {
+  crs_matrix() = default;
+  explicit crs_matrix(const crs_matrix_local<T, I, O>& m)
+      : data(m), num_row(m.local_num_row), num_col(m.local_num_col) {}
+  explicit crs_matrix(crs_matrix_local<T, I, O>&& m)
+      : data(std::move(m)), num_row(data.local_num_row), num_col(data.local_num_col) {}
+  crs_matrix_local<T, I, O> gather() const { return data; }
+  crs_matrix<T, I, O> transpose() const { return crs_matrix<T, I, O>(data.transpose()); }
+  size_t get_local_num_row() const { return data.local_num_row; }
+  void clear() {
+    data.clear();
+    num_row = num_col = 0;
+  }
+  crs_matrix_local<T, I, O> data;  // the one block (the reference: a node_local of them)
+  size_t num_row = 0, num_col = 0;
+};
+template <class T, class I, class O>
+crs_matrix<T, I, O> make_crs_matrix_scatter(const crs_matrix_local<T, I, O>& m) {
+  return crs_matrix<T, I, O>(m);
+}
+// make_crs_matrix_load / _loadbinary / _loadlibsvm (crs_matrix.hpp:720-899,
+// 1549-1627): the local loaders into one block
+template <class T, class I = size_t, class O = size_t>
+crs_matrix<T, I, O> make_crs_matrix_load(const std::string& file, long long num_col = -1) {
+  return crs_matrix<T, I, O>(make_crs_matrix_local_load<T, I, O>(file, num_col));
+}
+template <class T, class I = size_t, class O = size_t>
+crs_matrix<T, I, O> make_crs_matrix_loadbinary(const std::string& input) {
+  return crs_matrix<T, I, O>(make_crs_matrix_local_loadbinary<T, I, O>(input));
+}
+template <class T, class I = size_t, class O = size_t>
+crs_matrix<T, I, O> make_crs_matrix_loadlibsvm(const std::string& file, dvector<T>& label, IndexOrigin idxorg = AUTO) {
+  std::vector<T> lab;
+  auto r = crs_matrix<T, I, O>(make_crs_matrix_local_loadlibsvm<T, I, O>(file, lab, idxorg));
+  label = dvector<T>(std::move(lab));
+  return r;
+}
+
 // crs_matrix_local::save (operator<<, crs_matrix.hpp:440-450): "col:value"
 // lines
 template <class T, class I, class O>
@@ -538,6 +596,73 @@ struct logistic_regression_with_lbfgs {
     if (inputMovable) data.clear();
     return m;
   }
+  // the distributed overloads (logistic_regression_with_lbfgs.hpp:11-128);
+  // the && ones set inputMovable, so the matrix is cleared after training
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                            size_t hist_size = 10, double regParam = 0.01, RegType regTyp = ZERO,
+                                            bool isIntercept = false, double convergenceTol = 0.001,
+                                            MatType mType = CRS, bool inputMovable = false) {
+    auto lab = label.gather();
+    auto m = train(data.data, lab, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                   isIntercept, convergenceTol, mType, false);
+    if (inputMovable) data.clear();
+    return m;
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            size_t numIteration = 1000, double alpha = 0.01, size_t hist_size = 10,
+                                            double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col, isIntercept ? 1.0 : 0.0);
+    size_t n_iter = 0;
+    std::vector<T> sample_weight;
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType, false);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                            double alpha = 0.01, size_t hist_size = 10, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col, isIntercept ? 1.0 : 0.0);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType, false);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            size_t numIteration = 1000, double alpha = 0.01, size_t hist_size = 10,
+                                            double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col, isIntercept ? 1.0 : 0.0);
+    size_t n_iter = 0;
+    std::vector<T> sample_weight;
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType, true);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                            double alpha = 0.01, size_t hist_size = 10, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col, isIntercept ? 1.0 : 0.0);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType, true);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                            size_t hist_size = 10, double regParam = 0.01, RegType regTyp = ZERO,
+                                            bool isIntercept = false, double convergenceTol = 0.001,
+                                            MatType mType = CRS) {
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, hist_size, regParam, regTyp,
+                 isIntercept, convergenceTol, mType, true);
+  }
 };
 
 // logistic_regression_with_sgd (ml/glm/logistic_regression_with_sgd.hpp)
@@ -567,6 +692,76 @@ struct logistic_regression_with_sgd {
                            miniBatchFraction, regParam, regTyp, isIntercept, convergenceTol, mType);
     if (inputMovable) data.clear();
     return m;
+  }
+  // the distributed overloads (logistic_regression_with_sgd.hpp:11-128);
+  // the && ones set inputMovable
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS,
+                                            bool inputMovable = false) {
+    auto lab = label.gather();
+    auto m = train(data.data, lab, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction,
+                   regParam, regTyp, isIntercept, convergenceTol, mType, false);
+    if (inputMovable) data.clear();
+    return m;
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col);
+    size_t n_iter = 0;
+    std::vector<T> sample_weight;
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType, false);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>& data, dvector<T>& label,
+                                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                            double alpha = 0.01, double miniBatchFraction = 1.0,
+                                            double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType, false);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col);
+    size_t n_iter = 0;
+    std::vector<T> sample_weight;
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType, true);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            std::vector<T>& sample_weight, size_t& n_iter, size_t numIteration = 1000,
+                                            double alpha = 0.01, double miniBatchFraction = 1.0,
+                                            double regParam = 0.01, RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    logistic_regression_model<T> initModel(data.num_col);
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType, true);
+  }
+  template <class T, class I, class O>
+  static logistic_regression_model<T> train(crs_matrix<T, I, O>&& data, dvector<T>& label,
+                                            logistic_regression_model<T>& initModel, std::vector<T>& sample_weight,
+                                            size_t& n_iter, size_t numIteration = 1000, double alpha = 0.01,
+                                            double miniBatchFraction = 1.0, double regParam = 0.01,
+                                            RegType regTyp = ZERO, bool isIntercept = false,
+                                            double convergenceTol = 0.001, MatType mType = CRS) {
+    return train(data, label, initModel, sample_weight, n_iter, numIteration, alpha, miniBatchFraction, regParam,
+                 regTyp, isIntercept, convergenceTol, mType, true);
   }
 };
 
