@@ -65,7 +65,7 @@ EXPORTS = [
     "fvg_matrix_get_crs", "fvg_matrix_load_text", "fvg_matrix_load_libsvm", "fvg_matrix_get_labels",
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
     "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info", "fvg_matrix_set_head",
-    "fvg_matrix_head_info", "fvg_ctx_set_wait_limit", "fvg_debug_inject_alloc_failure",
+    "fvg_matrix_head_info", "fvg_ctx_set_wait_limit", "fvg_debug_inject_alloc_failure", "fvg_matrix_autotune",
 ]
 
 _lib = None
@@ -96,6 +96,7 @@ def load(build_if_needed: bool = True):
         "fvg_ctx_reset_profile": ([_p], _int),
         "fvg_ctx_kernel_launches": ([_p], _i64),
         "fvg_ctx_set_wait_limit": ([_p, _i64], _int),
+        "fvg_matrix_autotune": ([_p, _p, _int, _p, _int, _p, _p, _i64, C.POINTER(_i64)], _int),
         "fvg_debug_inject_alloc_failure": ([_i64], None),
         "fvg_matrix_create_crs": ([_p, _i64, _i64, _p, _p, _p, _int, _int, C.POINTER(_p)], _int),
         "fvg_matrix_destroy": ([_p], None),
@@ -318,6 +319,27 @@ class Matrix:
         """Forward head of the FP32/BF16 forward product: columns < 0 picks it
         from the matrix, 0 turns it off, > 0 forces that many columns."""
         self.ctx.check(self.ctx.L.fvg_matrix_set_head(self.ctx.h, self.h, int(columns)))
+
+    def autotune(self, storage="split", label=None, reps=3):
+        """Times the candidate training layouts (fvg_matrix_autotune) and
+        leaves the fastest set on the matrix.  Returns (best, tried): dicts
+        with format (name), head (bool), panel_min (0 = panels off) and
+        eval_ms; train with mat_type=best["format"]."""
+        class _Choice(C.Structure):
+            _fields_ = [("format", C.c_int32), ("head", C.c_int32), ("panel_min", C.c_double),
+                        ("eval_ms", C.c_double)]
+        names = {v: k for k, v in FORMATS.items()}
+        best = _Choice()
+        tried = (_Choice * 32)()
+        n = _i64()
+        lab = None if label is None else np.ascontiguousarray(label, dtype=np.float64)
+        self.ctx.check(self.ctx.L.fvg_matrix_autotune(self.ctx.h, self.h, _dt(storage), _ptr(lab), int(reps),
+                                                      C.byref(best), tried, 32, C.byref(n)))
+
+        def d(ch):
+            return {"format": names[ch.format], "head": bool(ch.head), "panel_min": ch.panel_min,
+                    "eval_ms": ch.eval_ms}
+        return d(best), [d(tried[i]) for i in range(min(n.value, 32))]
 
     def head_info(self):
         """(columns in the head, their entries); zeros when unused."""

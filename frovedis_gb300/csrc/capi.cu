@@ -336,6 +336,19 @@ FVG_API fvg_status fvg_matrix_set_panels(fvg_ctx* c, fvg_matrix* M, int64_t rows
   API_END(c)
 }
 
+FVG_API fvg_status fvg_matrix_autotune(fvg_ctx* c, fvg_matrix* M, fvg_dtype storage, const double* label,
+                                       int32_t reps, fvg_tune_choice* best, fvg_tune_choice* tried,
+                                       int64_t max_tried, int64_t* n_tried) {
+  if (!c || !M || !best) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  std::vector<fvg_tune_choice> all;
+  autotune(c, M, storage, label, reps, all, *best);
+  if (n_tried) *n_tried = (int64_t)all.size();
+  for (size_t i = 0; tried && i < all.size() && (int64_t)i < max_tried; i++) tried[i] = all[i];
+  API_END(c)
+}
+
 FVG_API fvg_status fvg_matrix_set_head(fvg_ctx* c, fvg_matrix* M, int64_t columns) {
   if (!c || !M) return FVG_ERR_INVALID_ARG;
   API_BEGIN

@@ -390,6 +390,10 @@ int glm_split_grid(fvg_ctx* c, i64 m);
 // per-row loss/gradient over z = wtx (+ head) + intercept (float2 pairs)
 void glm_split_rows(fvg_ctx* c, const void* wtx, const void* head, i64 m, const GlmSplitArgs& e);
 
+// Times the candidate training layouts of a matrix and leaves the fastest set.
+void autotune(fvg_ctx* c, fvg_matrix* M, int storage, const double* label_h, int reps,
+              std::vector<fvg_tune_choice>& tried, fvg_tune_choice& best);
+
 // Argument checks shared by the trainers (lbfgs_parallelizer.hpp:536-552).
 void check_common(const fvg_glm_params* p, fvg_matrix* M, const double* label);
 

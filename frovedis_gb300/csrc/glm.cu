@@ -1308,3 +1308,109 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
 }
 
 }  // namespace fvg
+
+namespace fvg {
+
+// ============================================================ autotuner
+// The reference picks the product format by MatType (CRS on x86, HYBRID on
+// VE: logistic_regression_with_lbfgs.hpp:280-285) and has no layout knobs.
+// Here every candidate layout gives the same sums up to summation order, so
+// the choice is a matter of speed: each candidate — format (CRS, and for
+// FP32/BF16 values ELL when its padding stays within 4x the nonzeros, and
+// the hybrid), the forward head on or off, the row panels off or on with a
+// hot threshold of 1, 2 or 4 entries per panel — is timed over `reps` loss/
+// gradient evaluations (CUDA events on the context stream, after one warm
+// evaluation), and the fastest is left set on the matrix.
+namespace {
+void set_layout(fvg_ctx* c, fvg_matrix* M, int head, double panel_min) {
+  FVG_CUDA(cudaStreamSynchronize(c->stream));
+  M->head.reset();
+  M->head_tried = false;
+  M->head_cols = head ? -1 : 0;
+  M->pan.reset();
+  M->pan_tried = false;
+  M->panel_rows = panel_min > 0 ? -1 : 0;
+  M->panel_min = panel_min > 0 ? panel_min : -1.0;
+}
+}  // namespace
+
+void autotune(fvg_ctx* c, fvg_matrix* M, int storage, const double* label_h, int reps,
+              std::vector<fvg_tune_choice>& tried, fvg_tune_choice& best) {
+  if (storage < FVG_F64 || storage > FVG_SPLIT) fail(FVG_ERR_INVALID_ARG, "unknown storage dtype");
+  if (storage == FVG_F64 && M->master != FVG_F64) fail(FVG_ERR_INVALID_ARG, "FP64 storage needs FP64 values");
+  if (M->A.m == 0 || M->A.n == 0) fail(FVG_ERR_INVALID_ARG, "Empty training data\n");
+  reps = std::max(1, reps);
+  const i64 m = M->A.m, n = M->A.n;
+  cudaStream_t s = c->stream;
+  DBuf label, w, wx, g, out, bd;
+  label.alloc(sizeof(double) * m, s);
+  if (label_h) {
+    FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  } else {
+    std::vector<double> ones((size_t)m, 1.0);
+    FVG_CUDA(cudaMemcpyAsync(label.p, ones.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    FVG_CUDA(cudaStreamSynchronize(s));
+  }
+  w.alloc(sizeof(double) * (n + 1), s);
+  FVG_CUDA(cudaMemsetAsync(w.p, 0, sizeof(double) * (n + 1), s));
+  wx.alloc(sizeof(float2) * (n + 1), s);
+  g.alloc(sizeof(double) * (n + 1), s);
+  out.alloc(sizeof(double) * 2, s);
+  bd.alloc(sizeof(double), s);
+  FVG_CUDA(cudaMemsetAsync(bd.p, 0, sizeof(double), s));
+  const void* x = w.p;
+  if (storage == FVG_SPLIT) {
+    split_vector(c, w.as<double>(), wx.p, n);
+    x = wx.p;
+  } else if (storage != FVG_F64) {
+    FVG_CUDA(cudaMemsetAsync(wx.p, 0, sizeof(float) * (n + 1), s));
+    x = wx.p;
+  }
+  // candidates
+  std::vector<fvg_tune_choice> cand;
+  const bool lowp = storage == FVG_F32 || storage == FVG_BF16;
+  const bool layouts = storage != FVG_F64;  // the head and the panels exist for FP32 / BF16 / split values
+  for (int head : {0, 1})
+    for (double pm : {0.0, 1.0, 2.0, 4.0}) {
+      if (!layouts && (head || pm > 0)) continue;
+      cand.push_back({FVG_CRS, head, pm, 0.0});
+    }
+  if (lowp) {
+    if (M->A.max_row * m <= 4 * M->A.nnz) cand.push_back({FVG_ELL, 0, 0.0, 0.0});
+    cand.push_back({FVG_HYBRID, 0, 0.0, 0.0});
+  }
+  cudaEvent_t e0, e1;
+  FVG_CUDA(cudaEventCreate(&e0));
+  FVG_CUDA(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } evs{e0, e1};
+  best = {FVG_CRS, 0, 0.0, -1.0};
+  for (auto ch : cand) {
+    set_layout(c, M, ch.head, ch.panel_min);
+    Operand op;
+    build_operand(c, M, ch.format, op);
+    Evaluator ev;
+    ev.init(c, &op, storage, label.as<double>(), nullptr, 0);
+    if ((ch.head && !ev.HD) || (ch.panel_min > 0 && !ev.PT)) continue;  // the layout does not apply
+    ev.eval(x, bd.as<double>(), g.as<double>(), out.as<double>());
+    FVG_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; r++) ev.eval(x, bd.as<double>(), g.as<double>(), out.as<double>());
+    FVG_CUDA(cudaEventRecord(e1, s));
+    FVG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    FVG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    ch.eval_ms = ms / reps;
+    tried.push_back(ch);
+    if (best.eval_ms < 0 || ch.eval_ms < best.eval_ms) best = ch;
+  }
+  if (best.eval_ms < 0) fail(FVG_ERR_INTERNAL, "no candidate layout could be timed");
+  set_layout(c, M, best.head, best.panel_min);
+  check_device_error(c);
+}
+
+}  // namespace fvg

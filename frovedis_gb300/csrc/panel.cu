@@ -571,16 +571,15 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
 // the next and, unlike the fixed rounding of the values, does not cancel in
 // the L-BFGS gradient differences).  To fit a panel beside the staging
 // buffers, one CTA of kSplitWarps warps per SM walks its own work items of at
-// most kSplitTile entries.  Each entry's product is made exact as p + t (an
-// FMA) and overwrites the staged entry; rows are summed with TwoSum; partial
-// sums are df pairs.
-constexpr int kSplitWarps = 16;
-constexpr int kSplitTile = 256;
+// most kSplitTile entries, so that one item is one pass of 32 lanes x 8
+// entries: no products are staged and no second pass re-reads them.
+constexpr int kSplitWarps = 20;
+constexpr int kSplitTile = 240;  // an item's staged copy (8-aligned ends) fits 32 lanes x 8 entries
 struct SplitSmem {
-  static constexpr int kCap = kSplitTile + 16;         // entries of one copy
+  static constexpr int kCap = 256;                     // entries of one copy
   static constexpr int kHiB = kCap * 2;                // offset of the FP32 values
   static constexpr int kLoB = kHiB + kCap * 4;         // offset of the BF16 residuals
-  static constexpr int kStageB = kLoB + kCap * 2;      // = kCap * 8: room for the (p, t) products
+  static constexpr int kStageB = kLoB + kCap * 2;      // = kCap * 8
   static constexpr int kSoffB = ((kTileRows + 1) * 2 + 15) / 16 * 16;
   static constexpr int kWarpB = kStageB + kSoffB;
   static constexpr int kStatic = 16 * kSplitWarps + kSplitWarps * kWarpB;
@@ -609,18 +608,45 @@ struct PanSK {
 __device__ __forceinline__ df shfl_xor_df(df a, int o) {
   return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
 }
+__device__ __forceinline__ df shfl_up_df(df a, int o) {
+  return {__shfl_up_sync(0xffffffffu, a.h, o), __shfl_up_sync(0xffffffffu, a.l, o)};
+}
 
+// Segmented inclusive scan over the warp's lanes, in lane order:
+// S_L = v_L + (reset_L ? 0 : S_{L-1}) (Hillis-Steele; a lane stops adding
+// once a reset lies between it and the lane it reads).
+__device__ __forceinline__ df seg_scan_df(df v, bool reset, int lane) {
+  bool f = reset;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const df u = shfl_up_df(v, o);
+    const bool fu = __shfl_up_sync(0xffffffffu, (int)f, o) != 0;
+    if (lane >= o) {
+      if (!f) v = df_add(u, v);
+      f = f || fu;
+    }
+  }
+  return v;
+}
+
+// One CTA of kSplitWarps warps per SM takes units of `group` consecutive
+// panels (as k_panel).  Per work item (at most kSplitTile entries) a bulk
+// copy stages the entries (uint16 slots, FP32 values, BF16 residuals); lane L
+// then takes the 8 staged entries 8L..8L+7 (16-byte shared loads), makes each
+// product exact (p + t), and adds its row segments in registers with TwoSum:
+// a row that ends inside the chunk is written at once when it also started
+// there; the row that was open at the chunk's start and the one open at its
+// end join the neighbouring lanes' segments through a segmented scan in lane
+// order.  Pieces of long rows: a warp reduction, added after the CTA barrier
+// in piece order.  Every sum has a fixed order.
 __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK p) {
   using SM = SplitSmem;
   constexpr int NW = kSplitWarps;
-  constexpr int NR2 = (SM::kCap + 63) / 64;  // pair rounds of a staged copy
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + 2 * w;
   unsigned char* area = smem + 16 * NW + w * SM::kWarpB;
   unsigned short* soff = reinterpret_cast<unsigned short*>(area + SM::kStageB);
-  float2* prod2 = reinterpret_cast<float2*>(area);
-  float4* prod4 = reinterpret_cast<float4*>(area);
   float* xh = reinterpret_cast<float*>(smem + SM::kStatic);
   float* xl = reinterpret_cast<float*>(smem + SM::kStatic + p.rows * 4);
   if (lane == 0) mbar_init(bar, 1);
@@ -661,8 +687,10 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         }
       }
       pend = true;
-      if (it.r1 >= 0)
-        for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = (unsigned short)(__ldg(p.poff + it.r0 + k) - q0);
+      const bool tile = it.r1 >= 0;
+      const int R = tile ? it.r1 - it.r0 : 0;
+      if (tile)
+        for (int k = lane; k <= R; k += 32) soff[k] = (unsigned short)(__ldg(p.poff + it.r0 + k) - q0);
       if (!mbar_wait_bounded(bar, parity, p.err, p.wait_limit)) {
         dead = true;
         break;
@@ -670,68 +698,82 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
       parity ^= 1u;
       pend = false;
       __syncwarp();
-      {
-        // every staged pair into registers first: the products overwrite them
-        const unsigned* sidx2 = reinterpret_cast<const unsigned*>(area);
-        const float2* shi2 = reinterpret_cast<const float2*>(area + SM::kHiB);
-        const unsigned* slo2 = reinterpret_cast<const unsigned*>(area + SM::kLoB);
-        const int n2 = (int)(n >> 1);
-        unsigned c[NR2], lo[NR2];
-        float2 hi[NR2];
-#pragma unroll
-        for (int q = 0; q < NR2; q++) {
-          const int k2 = q * 32 + lane;
-          if (k2 < n2) {
-            c[q] = sidx2[k2];
-            hi[q] = shi2[k2];
-            lo[q] = slo2[k2];
-          }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < NR2; q++) {
-          const int k2 = q * 32 + lane;
-          if (k2 < n2) {
-            const unsigned c0 = c[q] & 0xffffu, c1 = c[q] >> 16;
-            const float2 x0 = make_float2(xh[c0], xl[c0]);
-            const float2 x1 = make_float2(xh[c1], xl[c1]);
-            float p0, t0, p1, t1;
-            df_prod(hi[q].x, __uint_as_float(lo[q] << 16), x0, p0, t0);
-            df_prod(hi[q].y, __uint_as_float(lo[q] & 0xffff0000u), x1, p1, t1);
-            prod4[k2] = make_float4(p0, t0, p1, t1);
-          }
-        }
-      }
-      __syncwarp();
-      if (it.r1 >= 0) {
-        const int R = it.r1 - it.r0;
-        const int Gl = lanes_per_row(R);
-        const int per_round = 32 / Gl;
-        for (int rb = 0; rb < R; rb += per_round) {
-          const int j = rb + lane / Gl, sub = lane % Gl;
-          DfAcc acc;
-          if (j < R) {
-            const int s = soff[j], e = soff[j + 1];
-            for (int k = s + sub; k < e; k += Gl) {
-              const float2 v = prod2[k];
-              acc.add(v.x, v.y);
-            }
-          }
-          df a = acc.get();
-          for (int o = Gl >> 1; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
-          if (j < R && sub == 0) p.ypan[it.r0 + j] = df_pack(a);
-        }
-      } else {
+      // this lane's 8 staged entries
+      const uint4 s4 = reinterpret_cast<const uint4*>(area)[lane];
+      const float4 h0 = reinterpret_cast<const float4*>(area + SM::kHiB)[2 * lane];
+      const float4 h1 = reinterpret_cast<const float4*>(area + SM::kHiB)[2 * lane + 1];
+      const uint4 l4 = reinterpret_cast<const uint4*>(area + SM::kLoB)[lane];
+      const unsigned sw[4] = {s4.x, s4.y, s4.z, s4.w}, lw[4] = {l4.x, l4.y, l4.z, l4.w};
+      const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+      const int lo_e = max(it.e0 - q0, lane * 8), hi_e = min(it.e1 - q0, lane * 8 + 8);
+      if (!tile) {
         DfAcc acc;
-        const int e = it.e1 - q0;
-        for (int k = it.e0 - q0 + lane; k < e; k += 32) {
-          const float2 v = prod2[k];
-          acc.add(v.x, v.y);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int e = lane * 8 + k;
+          if (e >= lo_e && e < hi_e) {
+            const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+            const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+            float pp, tt;
+            df_prod(hv[k], vl, make_float2(xh[c], xl[c]), pp, tt);
+            acc.add(pp, tt);
+          }
         }
         df a = acc.get();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
         if (lane == 0) p.partials[-1 - it.r1] = df_pack(a);
+      } else {
+        __syncwarp();  // soff
+        for (int j = lane; j < R; j += 32)
+          if (soff[j] == soff[j + 1]) p.ypan[it.r0 + j] = make_float2(0.f, 0.f);  // empty rows
+        DfAcc acc;
+        df H = {0.f, 0.f};
+        int j = 0, j0 = 0, nb = 0;
+        bool starts = false, hasb = false, any = lo_e < hi_e;
+        if (any) {
+          int a = 0, b = R;  // the last row starting at or before lo_e (the non-empty one holding it)
+          while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if ((int)soff[mid] <= lo_e) a = mid;
+            else b = mid;
+          }
+          j = j0 = a;
+          starts = (int)soff[j] == lo_e;
+          nb = soff[j + 1];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int e = lane * 8 + k;
+          if (e >= lo_e && e < hi_e) {
+            if (e == nb) {  // row j ended before e
+              if (!hasb) {
+                H = acc.get();
+                hasb = true;
+              } else {
+                p.ypan[it.r0 + j] = df_pack(acc.get());  // started and ended in this chunk
+              }
+              acc = DfAcc();
+              do {
+                j++;
+                nb = soff[j + 1];
+              } while (nb == e);
+            }
+            const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+            const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+            float pp, tt;
+            df_prod(hv[k], vl, make_float2(xh[c], xl[c]), pp, tt);
+            acc.add(pp, tt);
+          }
+        }
+        // the tail segment (row j) starts inside this lane when a row ended
+        // here or the lane's first entry starts its row
+        const df T = acc.get();
+        const df S = seg_scan_df(any ? T : df{0.f, 0.f}, any && (hasb || starts), lane);
+        df carry = shfl_up_df(S, 1);
+        if (lane == 0) carry = {0.f, 0.f};
+        if (hasb) p.ypan[it.r0 + j0] = df_pack(starts ? H : df_add(carry, H));
+        if (any && nb == hi_e) p.ypan[it.r0 + j] = df_pack(S);  // the tail row ends with this lane's range
       }
       __syncwarp();
     }
@@ -740,7 +782,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
     for (int L = p.plong0[pn] + w; L < l1; L += NW) {
       const int c0 = p.long_piece0[L], c1 = p.long_piece0[L + 1];
       df a = {0.f, 0.f};
-      for (int j = c0 + lane; j < c1; j += 32) a = df_add(a, df_unpack(__ldcg(p.partials + j)));
+      for (int jj = c0 + lane; jj < c1; jj += 32) a = df_add(a, df_unpack(__ldcg(p.partials + jj)));
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
       if (lane == 0) p.ypan[p.long_rows[L]] = df_pack(a);

@@ -150,6 +150,27 @@ FVG_API fvg_status fvg_matrix_panel_info(fvg_ctx* ctx, fvg_matrix* mat, int64_t*
 FVG_API fvg_status fvg_matrix_set_head(fvg_ctx* ctx, fvg_matrix* mat, int64_t columns);
 /* The head in use (built if needed): info[0] columns (0: none), info[1] their entries. */
 FVG_API fvg_status fvg_matrix_head_info(fvg_ctx* ctx, fvg_matrix* mat, int64_t* info);
+/* Autotuner of the training layout.  The reference picks the format by
+ * MatType alone (CRS on x86, HYBRID on VE,
+ * ml/glm/logistic_regression_with_lbfgs.hpp:280-285); every layout here gives
+ * the same sums up to summation order, so the choice is one of speed.  Each
+ * candidate — format (CRS; for FP32 / BF16 values also ELL when its padding
+ * stays within 4x the nonzeros, and HYBRID), the forward head on or off, the
+ * row panels off or on with a hot threshold of 1, 2 or 4 entries per panel —
+ * is timed over `reps` loss/gradient evaluations with `label` (NULL: all
+ * ones), and the fastest layout is left set on the matrix (as
+ * fvg_matrix_set_head / fvg_matrix_set_panels would); train with
+ * mat_type = best->format.  tried[0..max_tried) receives the candidates that
+ * applied, *n_tried their number (both may be NULL). */
+typedef struct {
+  int32_t format;   /* fvg_format */
+  int32_t head;     /* forward head: 0 off, 1 on (columns chosen from the matrix) */
+  double panel_min; /* row panels: 0 off, > 0 the hot threshold (entries per panel) */
+  double eval_ms;   /* time of one loss/gradient evaluation */
+} fvg_tune_choice;
+FVG_API fvg_status fvg_matrix_autotune(fvg_ctx* ctx, fvg_matrix* mat, fvg_dtype storage, const double* label,
+                                       int32_t reps, fvg_tune_choice* best, fvg_tune_choice* tried,
+                                       int64_t max_tried, int64_t* n_tried);
 /* Device bytes held by the matrix and everything derived from it. */
 FVG_API int64_t fvg_matrix_device_bytes(const fvg_matrix* mat);
 

@@ -187,3 +187,70 @@ def test_cpp_api_matches_oracle(tmp_path):
     rs = oracle.logreg_sgd(a, label, shrink=True, num_iter=12, alpha=0.05, reg_type="L1", reg_param=1e-3,
                            intercept=True, b0=1.0)
     assert wclose(o["est_shrink_w"], rs["w"]) and int(o["est_shrink_n_iter"][0]) == rs["n_iter"]
+
+
+# ---------------------------------------------------------------------------
+# The distributed containers (crs_matrix / dvector on one rank) and the
+# INTEGRATION.md binding: its C++ block is pasted into tests/cpp/dist_check.cpp
+# verbatim, where it specialises logistic_regression_with_lbfgs::train for
+# crs_matrix<double,int,int>.
+DIST_SRC = os.path.join(ROOT, "tests", "cpp", "dist_check.cpp")
+
+
+def integration_binding():
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sec = text.index("## The binding a frovedis maintainer would add (C++)")
+    start = text.index("```cpp\n", sec) + len("```cpp\n")
+    return text[start:text.index("```", start)]
+
+
+def compile_dist(out_dir):
+    lib = fb.build()
+    src = os.path.join(str(out_dir), "dist_check.cpp")
+    code = open(DIST_SRC).read()
+    assert "// @@BINDING@@" in code
+    with open(src, "w") as f:
+        f.write(code.replace("// @@BINDING@@", integration_binding()))
+    exe = os.path.join(str(out_dir), "dist_check")
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), src,
+           "-o", exe, "-L", os.path.dirname(lib), "-lfvg", "-Wl,-rpath," + os.path.dirname(lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_integration_binding_compiles(tmp_path):
+    assert "logistic_regression_with_lbfgs::train(crs_matrix<double,int,int>& data" in integration_binding()
+    assert os.access(compile_dist(tmp_path), os.X_OK)
+
+
+@pytest.mark.gpu
+def test_distributed_overloads_and_binding_match_oracle(tmp_path):
+    from frovedis_gb300 import datagen
+    m, n = 3000, 250
+    off, idx, val, label = datagen.generate(datagen.Spec(m=m, n=n, lam=12.0, seed=6))
+    a = oracle.CRS(m, n, off, idx, val)
+    inp, outp = tmp_path / "in.txt", tmp_path / "out.txt"
+    with open(inp, "w") as f:
+        f.write(f"{m} {n} {a.nnz}\n")
+        for arr in (a.off, a.idx):
+            f.write(" ".join(str(int(v)) for v in arr) + "\n")
+        for arr in (a.val, label):
+            f.write(" ".join(repr(float(v)) for v in arr) + "\n")
+    exe = compile_dist(tmp_path)
+    r = subprocess.run([exe, str(inp), str(outp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    o = _read_output(outp)
+    kw = dict(num_iter=15, reg_type="L2", reg_param=1e-3)
+    ro = oracle.logreg_lbfgs(a, label, w0=np.zeros(n), **kw)
+    # the binding and the library's own overload make the same call
+    assert np.array_equal(o["binding_w"], o["own_w"])
+    assert int(o["binding_iter"][0]) == int(o["own_iter"][0]) == ro["n_iter"]
+    assert np.max(np.abs(o["binding_w"] - ro["w"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["w"])))
+    rd = oracle.logreg_lbfgs(a, label, intercept=True, **kw)
+    assert np.max(np.abs(o["defaults_w"] - rd["w"])) <= 1e-5 * max(1.0, np.max(np.abs(rd["w"])))
+    assert abs(o["defaults_b"][0] - rd["b"]) <= 1e-5 * max(1.0, abs(rd["b"]))
+    assert np.array_equal(o["moved_w"], o["defaults_w"]) and o["moved_cleared"][0] == 1
+    rs = oracle.logreg_sgd(a, label, num_iter=10, alpha=0.05, reg_type="L2", reg_param=1e-2, intercept=True)
+    assert np.max(np.abs(o["sgd_w"] - rs["w"])) <= 1e-5 * max(1.0, np.max(np.abs(rs["w"])))
+    assert abs(o["sgd_b"][0] - rs["b"]) <= 1e-5 * max(1.0, abs(rs["b"]))
