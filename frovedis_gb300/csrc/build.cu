@@ -230,8 +230,13 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 constexpr i64 kSchedChunk = 4096;
 
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
-  const int slot = 0;
-  if (a.sched[slot]) return *a.sched[slot];
+  // slot 0: the CRS kernel's items (kWarpTile); slot 1: another item size
+  // (the split kernel's), built on its first use
+  const int slot = tile == kWarpTile ? 0 : 1;
+  if (a.sched[slot]) {
+    if (a.sched[slot]->tile != tile) fail(FVG_ERR_INTERNAL, "a second work-item size for one matrix");
+    return *a.sched[slot];
+  }
   ProfScope ps(c, P_SCHED);
   auto s = std::make_unique<Sched>();
   s->tile = tile;

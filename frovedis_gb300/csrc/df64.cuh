@@ -239,3 +239,46 @@ __device__ __forceinline__ void glm_row_df(int kind, df eps, df wtx, df lab, df&
 }
 
 }  // namespace fvg
+
+namespace fvg {
+
+// ---------------------------------------------- chunked row segments
+// One lane's chunk of C consecutive entries of a work item (products p + t,
+// zero outside the lane's valid range), for the chunked split kernels.  B
+// marks, relative to the chunk, every entry after the lane's first valid
+// one at which a (non-empty) row starts.  The common case is branch-free:
+// H = the entries before the first mark (the segment continuing the row open
+// at the chunk's start), T = the entries from the last mark on (the segment
+// of the row open at its end, or the whole chunk when nothing is marked).
+template <int C>
+__device__ __forceinline__ void chunk_segments(const float (&p)[C], const float (&t)[C], unsigned B, df& H, df& T) {
+  const int fb = B ? __ffs(B) - 1 : C;   // first mark
+  const int lb = B ? 31 - __clz(B) : -1;  // last mark
+  DfAcc acc, head;
+#pragma unroll
+  for (int k = 0; k < C; k++) {
+    const bool cap = k == fb, rst = k == lb;
+    head.s = cap ? acc.s : head.s;
+    head.c = cap ? acc.c : head.c;
+    acc.s = rst ? 0.f : acc.s;
+    acc.c = rst ? 0.f : acc.c;
+    acc.add(p[k], t[k]);
+  }
+  H = B ? head.get() : df{0.f, 0.f};
+  T = acc.get();
+}
+
+// Sum of the chunk's entries [a, b): rows that start and end between two
+// marks (a second path, rarely taken where rows are longer than a chunk).
+template <int C>
+__device__ __forceinline__ df chunk_range(const float (&p)[C], const float (&t)[C], int a, int b) {
+  DfAcc acc;
+#pragma unroll
+  for (int k = 0; k < C; k++) {
+    const bool in = k >= a && k < b;
+    acc.add(in ? p[k] : 0.f, in ? t[k] : 0.f);
+  }
+  return acc.get();
+}
+
+}  // namespace fvg

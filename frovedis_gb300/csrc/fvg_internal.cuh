@@ -115,7 +115,7 @@ struct DevCRS {
   DBuf off, idx;  // int32
   DBuf val[3];    // indexed by fvg_dtype
   DBuf lo;        // bf16 [nnz+kPad]: value - FP32 value (split storage; with val[FVG_F32])
-  std::unique_ptr<Sched> sched[2];  // built once (slot 0)
+  std::unique_ptr<Sched> sched[2];  // work items: slot 0 kWarpTile, slot 1 the split kernel's size
   i64 max_row = 0;
 };
 
@@ -266,9 +266,10 @@ inline void count_launch(fvg_ctx* c, int n = 1) { c->launches += n; }
 void check_launch(const char* what);
 // Default poll budgets of the bounded device-side waits: the L-BFGS
 // direction's grid barriers (2^24 polls of ~32 ns) and the panel kernels'
-// bulk-copy waits (2^22 polls); a context may lower them for testing.
+// bulk-copy waits (2^16 polls, each a sleep of at most 20 us in the
+// barrier: ~1.3 s); a context may lower them for testing.
 constexpr unsigned kBarrierPolls = 1u << 24;
-constexpr unsigned kCopyPolls = 1u << 22;
+constexpr unsigned kCopyPolls = 1u << 16;
 inline unsigned barrier_polls(const fvg_ctx* c) { return c->wait_limit < 0 ? kBarrierPolls : (unsigned)c->wait_limit; }
 inline unsigned copy_polls(const fvg_ctx* c) { return c->wait_limit < 0 ? kCopyPolls : (unsigned)c->wait_limit; }
 // Reads (and clears) the device error word; fails when a kernel reported one.

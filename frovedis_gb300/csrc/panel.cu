@@ -322,12 +322,15 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
+// One poll: the thread may sleep in the barrier until the phase completes,
+// for at most kCopyPollNs (a suspend-time hint), instead of spinning.
+constexpr unsigned kCopyPollNs = 20000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kCopyPollNs)
       : "memory");
   return ok != 0;
 }
@@ -347,7 +350,7 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 // Bounded wait of a whole warp: gives up after `limit` polls (by default
-// 2^22, far beyond any copy's time) and reports it in the device error word
+// 2^16 polls of up to kCopyPollNs each, far beyond any copy's time) and reports it in the device error word
 // instead of spinning forever.  The lanes vote on every poll (a completed
 // phase stays completed), so the outcome is the same for the whole warp.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned* err, unsigned limit) {
@@ -727,10 +730,24 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         __syncwarp();  // soff
         for (int j = lane; j < R; j += 32)
           if (soff[j] == soff[j + 1]) p.ypan[it.r0 + j] = make_float2(0.f, 0.f);  // empty rows
-        DfAcc acc;
-        df H = {0.f, 0.f};
+        // the lane's 8 products (zero outside its valid range)
+        float pp[8], tt[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int e = lane * 8 + k;
+          const bool ok = e >= lo_e && e < hi_e;
+          const unsigned c = ok ? (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu : 0u;
+          const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+          float a, b;
+          df_prod(hv[k], vl, make_float2(xh[c], xl[c]), a, b);
+          pp[k] = ok ? a : 0.f;
+          tt[k] = ok ? b : 0.f;
+        }
+        // rows: j0 holds the first valid entry; B marks the rows starting after it
+        unsigned B = 0;
         int j = 0, j0 = 0, nb = 0;
-        bool starts = false, hasb = false, any = lo_e < hi_e;
+        bool starts = false;
+        const bool any = lo_e < hi_e;
         if (any) {
           int a = 0, b = R;  // the last row starting at or before lo_e (the non-empty one holding it)
           while (b - a > 1) {
@@ -741,38 +758,37 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           j = j0 = a;
           starts = (int)soff[j] == lo_e;
           nb = soff[j + 1];
-        }
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-          const int e = lane * 8 + k;
-          if (e >= lo_e && e < hi_e) {
-            if (e == nb) {  // row j ended before e
-              if (!hasb) {
-                H = acc.get();
-                hasb = true;
-              } else {
-                p.ypan[it.r0 + j] = df_pack(acc.get());  // started and ended in this chunk
-              }
-              acc = DfAcc();
-              do {
-                j++;
-                nb = soff[j + 1];
-              } while (nb == e);
-            }
-            const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
-            const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
-            float pp, tt;
-            df_prod(hv[k], vl, make_float2(xh[c], xl[c]), pp, tt);
-            acc.add(pp, tt);
+          while (nb < hi_e) {
+            B |= 1u << (nb - lane * 8);
+            do {
+              j++;
+              nb = soff[j + 1];
+            } while (nb == (int)soff[j]);
           }
         }
-        // the tail segment (row j) starts inside this lane when a row ended
-        // here or the lane's first entry starts its row
-        const df T = acc.get();
-        const df S = seg_scan_df(any ? T : df{0.f, 0.f}, any && (hasb || starts), lane);
+        df H, T;
+        chunk_segments<8>(pp, tt, B, H, T);
+        if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
+          unsigned rest = B & (B - 1);
+          int a = __ffs(B) - 1, jj = j0;
+          do {
+            jj++;
+          } while (soff[jj + 1] == soff[jj]);
+          while (rest) {
+            const int b = __ffs(rest) - 1;
+            rest &= rest - 1;
+            p.ypan[it.r0 + jj] = df_pack(chunk_range<8>(pp, tt, a, b));
+            a = b;
+            do {
+              jj++;
+            } while (soff[jj + 1] == soff[jj]);
+          }
+        }
+        // the tail segment starts inside this lane when a row starts here
+        const df S = seg_scan_df(any ? T : df{0.f, 0.f}, any && (B != 0 || starts), lane);
         df carry = shfl_up_df(S, 1);
         if (lane == 0) carry = {0.f, 0.f};
-        if (hasb) p.ypan[it.r0 + j0] = df_pack(starts ? H : df_add(carry, H));
+        if (B) p.ypan[it.r0 + j0] = df_pack(starts ? H : df_add(carry, H));
         if (any && nb == hi_e) p.ypan[it.r0 + j] = df_pack(S);  // the tail row ends with this lane's range
       }
       __syncwarp();

@@ -43,6 +43,8 @@ void df64_init(fvg_ctx* c) {
 namespace {
 
 constexpr int kSplitThreads = 256;
+// CRS work items of the split kernel: a staged item (16-aligned ends) fits 32 lanes x 16 entries
+constexpr int kSplitCrsTile = 480;
 
 unsigned grid_rows(fvg_ctx* c, i64 n, int per_sm = 8) {
   i64 g = (n + kSplitThreads - 1) / kSplitThreads;
@@ -93,23 +95,40 @@ template <> __device__ __forceinline__ void store_row<float2>(void* y, i64 row, 
 __device__ __forceinline__ df shfl_df(df a, int o) {
   return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
 }
+__device__ __forceinline__ df shfl_up_df1(df a) {
+  return {__shfl_up_sync(0xffffffffu, a.h, 1), __shfl_up_sync(0xffffffffu, a.l, 1)};
+}
 
-// Persistent kernel over the CRS work items (the schedule of k_crs: tiles of
-// short rows, pieces of long rows).  Phase 1: lane L streams nonzeros L,
-// L+32, ... (column id, FP32 value, BF16 residual), gathers x's pair and
-// stages the exact product (p, t) in the warp's shared-memory slice.  Phase
-// 2: each row is summed by 1..32 lanes with TwoSum, the lanes combined by a
-// butterfly of df additions (commutative, so every lane of a row holds the
-// same sum); a piece is summed by the whole warp.
+// Segmented inclusive scan over the warp's lanes, in lane order:
+// S_L = v_L + (reset_L ? 0 : S_{L-1}).
+__device__ __forceinline__ df seg_scan(df v, bool reset, int lane) {
+  bool f = reset;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const df u = {__shfl_up_sync(0xffffffffu, v.h, o), __shfl_up_sync(0xffffffffu, v.l, o)};
+    const bool fu = __shfl_up_sync(0xffffffffu, (int)f, o) != 0;
+    if (lane >= o) {
+      if (!f) v = df_add(u, v);
+      f = f || fu;
+    }
+  }
+  return v;
+}
+
+// Persistent kernel over CRS work items of at most kSplitCrsTile entries
+// (tiles of short rows, pieces of long rows; the packing of k_crs).  Lane L
+// takes the 16 entries q0 + 16L .. q0 + 16L + 15 (q0 = the item's first entry
+// rounded down to 16): column ids, FP32 values and BF16 residuals come in
+// 128-bit loads, x's pairs are gathered, each product is made exact (p + t)
+// and added to the lane's current row segment with TwoSum.  A row that
+// starts and ends inside the chunk is written at once; the segments open at
+// the chunk's two ends join the neighbouring lanes' through a segmented scan
+// in lane order.  A piece of a long row is one warp reduction.  Every sum has
+// a fixed order, so results are identical run to run.
 template <class YT>
-__global__ void __launch_bounds__(kThreads, 4) k_crs_split(const SplitK p) {
-  constexpr int SPAN = kWarpTile;
-  constexpr int NR = SPAN / 32;
-  constexpr int RG = 4;
-  __shared__ float2 sprod[kThreads / 32][SPAN];
+__global__ void __launch_bounds__(kThreads, 2) k_crs_split(const SplitK p) {
   __shared__ int soffs[kThreads / 32][kTileRows + 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float2* prod = sprod[w];
   int* soff = soffs[w];
   const i64 W = (i64)gridDim.x * (kThreads / 32);
   const i64 n = p.nitems;
@@ -118,64 +137,119 @@ __global__ void __launch_bounds__(kThreads, 4) k_crs_split(const SplitK p) {
   for (; t < n; t += W) {
     const Item it = nx;
     if (t + W < n) nx = p.items[t + W];
-    const int a0 = it.e0;
-    const int span = it.e1 - a0;
-    if (it.r1 >= 0)
-      for (int k = lane; k <= it.r1 - it.r0; k += 32) soff[k] = __ldg(p.off + it.r0 + k);
+    const int q0 = it.e0 & ~15;
+    const bool tile = it.r1 >= 0;
+    const int R = tile ? it.r1 - it.r0 : 0;
+    if (tile)
+      for (int k = lane; k <= R; k += 32) soff[k] = __ldg(p.off + it.r0 + k) - q0;
+    const int lo_e = max(it.e0 - q0, lane * 16), hi_e = min(it.e1 - q0, lane * 16 + 16);
+    // the chunk (the arrays are padded past the last nonzero, and q0 + 16L
+    // stays below it whenever the lane has entries)
+    int c[16];
+    float hv[16];
+    unsigned lw[8];
+    if (lo_e < hi_e) {
+      const i64 b = (i64)q0 + lane * 16;
+      const int4* ip = reinterpret_cast<const int4*>(p.idx + b);
+      const float4* hp = reinterpret_cast<const float4*>(p.vh + b);
+      const uint4* lp = reinterpret_cast<const uint4*>(p.vl + b);
 #pragma unroll
-    for (int g = 0; g < NR; g += RG) {
-      int c[RG];
-      float vh[RG];
-      unsigned short vl[RG];
-#pragma unroll
-      for (int q = 0; q < RG; q++) {
-        const int k = (g + q) * 32 + lane;
-        if (k < span) {
-          c[q] = __ldcs(p.idx + a0 + k);
-          vh[q] = __ldcs(p.vh + a0 + k);
-          vl[q] = __ldcs(p.vl + a0 + k);
-        }
+      for (int q = 0; q < 4; q++) {
+        const int4 iv = __ldcs(ip + q);
+        const float4 fv = __ldcs(hp + q);
+        c[4 * q] = iv.x; c[4 * q + 1] = iv.y; c[4 * q + 2] = iv.z; c[4 * q + 3] = iv.w;
+        hv[4 * q] = fv.x; hv[4 * q + 1] = fv.y; hv[4 * q + 2] = fv.z; hv[4 * q + 3] = fv.w;
       }
 #pragma unroll
-      for (int q = 0; q < RG; q++) {
-        const int k = (g + q) * 32 + lane;
-        if (k < span) {
-          const float2 xv = __ldg(p.x + c[q]);
-          float pp, tt;
-          df_prod(vh[q], __uint_as_float((unsigned)vl[q] << 16), xv, pp, tt);
-          prod[k] = make_float2(pp, tt);
-        }
+      for (int q = 0; q < 2; q++) {
+        const uint4 lv = __ldcs(lp + q);
+        lw[4 * q] = lv.x; lw[4 * q + 1] = lv.y; lw[4 * q + 2] = lv.z; lw[4 * q + 3] = lv.w;
       }
     }
-    __syncwarp();
-    if (it.r1 >= 0) {
-      const int R = it.r1 - it.r0;
-      const int Gl = lanes_per_row(R);
-      const int per_round = 32 / Gl;
-      for (int rb = 0; rb < R; rb += per_round) {
-        const int j = rb + lane / Gl, sub = lane % Gl;
-        DfAcc acc;
-        if (j < R) {
-          const int s = soff[j] - a0, e = soff[j + 1] - a0;
-          for (int k = s + sub; k < e; k += Gl) {
-            const float2 v = prod[k];
-            acc.add(v.x, v.y);
-          }
-        }
-        df a = acc.get();
-        for (int o = Gl >> 1; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
-        if (j < R && sub == 0) store_row<YT>(p.y, it.r0 + j, a);
-      }
-    } else {
+    float2 xv[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const int e = lane * 16 + k;
+      xv[k] = (e >= lo_e && e < hi_e) ? __ldg(p.x + c[k]) : make_float2(0.f, 0.f);
+    }
+    if (!tile) {
       DfAcc acc;
-      for (int k = lane; k < span; k += 32) {
-        const float2 v = prod[k];
-        acc.add(v.x, v.y);
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        const int e = lane * 16 + k;
+        if (e >= lo_e && e < hi_e) {
+          const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+          float pp, tt;
+          df_prod(hv[k], vl, xv[k], pp, tt);
+          acc.add(pp, tt);
+        }
       }
       df a = acc.get();
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_df(a, o));
       if (lane == 0) p.partials[-1 - it.r1] = df_pack(a);
+    } else {
+      __syncwarp();  // soff
+      for (int j = lane; j < R; j += 32)
+        if (soff[j] == soff[j + 1]) store_row<YT>(p.y, it.r0 + j, df{0.f, 0.f});  // empty rows
+      // the lane's 16 products (zero outside its valid range)
+      float pp[16], tt[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        const int e = lane * 16 + k;
+        const bool ok = e >= lo_e && e < hi_e;
+        const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+        float a, b;
+        df_prod(hv[k], vl, xv[k], a, b);
+        pp[k] = ok ? a : 0.f;
+        tt[k] = ok ? b : 0.f;
+      }
+      // rows: j0 holds the first valid entry; B marks the rows starting after it
+      unsigned B = 0;
+      int j = 0, j0 = 0, nb = 0;
+      bool starts = false;
+      const bool any = lo_e < hi_e;
+      if (any) {
+        int a = 0, b = R;  // the last row starting at or before lo_e (the non-empty one holding it)
+        while (b - a > 1) {
+          const int mid = (a + b) >> 1;
+          if (soff[mid] <= lo_e) a = mid;
+          else b = mid;
+        }
+        j = j0 = a;
+        starts = soff[j] == lo_e;
+        nb = soff[j + 1];
+        while (nb < hi_e) {
+          B |= 1u << (nb - lane * 16);
+          do {
+            j++;
+            nb = soff[j + 1];
+          } while (nb == soff[j]);
+        }
+      }
+      df H, T;
+      chunk_segments<16>(pp, tt, B, H, T);
+      if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
+        unsigned rest = B & (B - 1);
+        int a = __ffs(B) - 1, jj = j0;
+        do {
+          jj++;
+        } while (soff[jj + 1] == soff[jj]);
+        while (rest) {
+          const int b = __ffs(rest) - 1;
+          rest &= rest - 1;
+          store_row<YT>(p.y, it.r0 + jj, chunk_range<16>(pp, tt, a, b));
+          a = b;
+          do {
+            jj++;
+          } while (soff[jj + 1] == soff[jj]);
+        }
+      }
+      const df S = seg_scan(any ? T : df{0.f, 0.f}, any && (B != 0 || starts), lane);
+      df carry = shfl_up_df1(S);
+      if (lane == 0) carry = {0.f, 0.f};
+      if (B) store_row<YT>(p.y, it.r0 + j0, starts ? H : df_add(carry, H));
+      if (any && nb == hi_e) store_row<YT>(p.y, it.r0 + j, S);  // the tail row ends with this lane's range
     }
     __syncwarp();
   }
@@ -315,12 +389,12 @@ void split_vector(fvg_ctx* c, const double* x, void* y, i64 n) {
 }
 
 i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a) {
-  const Sched& s = crs_sched(c, a, kWarpTile);
+  const Sched& s = crs_sched(c, a, kSplitCrsTile);
   return (i64)sizeof(float2) * std::max<i64>(s.npieces, 1);
 }
 
 void crs_pass_split(fvg_ctx* c, DevCRS& a, const void* x, bool y_df, void* y, void* scratch, int prof_key) {
-  const Sched& s = crs_sched(c, a, kWarpTile);
+  const Sched& s = crs_sched(c, a, kSplitCrsTile);
   if (!a.val[FVG_F32].p || !a.lo.p) fail(FVG_ERR_INTERNAL, "split storage planes missing");
   DBuf tmp;
   if (!scratch) {

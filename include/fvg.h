@@ -91,9 +91,9 @@ FVG_API int64_t fvg_ctx_kernel_launches(fvg_ctx* ctx);
  * kernels' bulk-copy waits).  A wait that runs out is abandoned: the kernel
  * records it in the context's error word and finishes (a copy in flight is
  * still drained), and the call returns FVG_ERR_INTERNAL; the context stays
- * usable.  polls < 0 restores the defaults (2^24 barrier polls, 2^22 copy
- * polls, far beyond any healthy wait); 0 makes every wait that is not
- * already complete give up at once.  No reference counterpart (the
+ * usable.  polls < 0 restores the defaults (2^24 barrier polls, 2^16 copy
+ * polls of up to 20 us each — about a second, far beyond any healthy wait);
+ * 0 makes every wait that is not already complete give up at once.  No reference counterpart (the
  * reference's ranks report failures through MPI, core/mpi_rpc.cc:471-491);
  * a small budget lets a test exercise the give-up path. */
 FVG_API fvg_status fvg_ctx_set_wait_limit(fvg_ctx* ctx, int64_t polls);

@@ -79,6 +79,9 @@ def lib():
         L.orc_problem_lbfgs.restype = _int
         L.orc_problem_destroy.argtypes = [_p]
         L.orc_problem_destroy.restype = None
+        L.orc_softmax_lbfgs_f64.argtypes = [_i64, _i64, _p, _p, _p, _p, _p, _i64, _i64, _i64, _dbl, _int, _dbl,
+                                            _p, _p, _p, _p]
+        L.orc_softmax_lbfgs_f64.restype = _int
         L.orc_ell_width.argtypes = [_i64, _p]
         L.orc_ell_width.restype = _i64
         L.orc_glm_lbfgs_f64.restype = _int
@@ -357,6 +360,27 @@ def softmax_train(a: CRS, label, K, num_iter=1000, alpha=0.01, reg_param=0.01, r
     if rc != 0:
         raise ValueError(f"oracle softmax rejected the arguments (code {rc})")
     return dict(W=W, b=b, n_iter=int(n_iter[0]))
+
+
+def softmax_lbfgs(a: CRS, label, K, num_iter=100, hist_size=10, reg_param=0.01, reg_type="ZERO", tol=0.001,
+                  sw=None, W0=None):
+    """Multinomial logistic regression by L-BFGS: the reference's softmax
+    gradient (softmax_gradient_descent.hpp:119-136) with its L-BFGS driver,
+    the cross-entropy as the line search's loss, no intercept.  Returns W
+    (n, K), n_iter, loss and the per-iteration trace."""
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sw is None else np.ascontiguousarray(sw, dtype=np.float64)
+    W = np.zeros((a.n, K)) if W0 is None else np.array(W0, dtype=np.float64).reshape(a.n, K)
+    W = np.ascontiguousarray(W)
+    n_iter = np.zeros(1, dtype=np.int64)
+    fl = np.zeros(1)
+    trace = np.zeros(4 * num_iter)
+    rc = lib().orc_softmax_lbfgs_f64(*a.args(), _ptr(label), _ptr(sw), int(K), num_iter, hist_size, reg_param,
+                                     REG[reg_type], tol, _ptr(W), _ptr(n_iter), _ptr(fl), _ptr(trace))
+    if rc != 0:
+        raise ValueError(f"oracle softmax lbfgs rejected the arguments (code {rc})")
+    it = int(n_iter[0])
+    return dict(W=W, n_iter=it, loss=float(fl[0]), trace=trace.reshape(-1, 4)[:it])
 
 
 def softmax_probability(a: CRS, W, b, intercept=False) -> np.ndarray:

@@ -680,16 +680,17 @@ template <class T> struct LBFGS {
 };
 
 // lbfgs_parallelizer::do_train  (ml/glm/lbfgs_parallelizer.hpp:267-364 with
-// trans; 366-462 without).  Constants 153-156.
-template <class T>
-void lbfgs_train(const Problem<T>& pr, int fmt, std::vector<T>& w, T& b, i64 num_iter, i64 hist,
-                 T lambda, int rtype, bool icpt, double tol, i64& n_iter, double& final_loss,
-                 double* trace /* per iteration: loss, trials, rms, factor */, bool no_eta = false) {
+// trans; 366-462 without).  Constants 153-156.  eval(w, b, loss) returns the
+// gradient [g, bias] (the GLM evaluation, or the softmax one below).
+template <class T, class Eval>
+void lbfgs_driver(Eval&& eval, int fmt, std::vector<T>& w, T& b, i64 num_iter, i64 hist, T lambda, int rtype,
+                  double tol, i64& n_iter, double& final_loss,
+                  double* trace /* per iteration: loss, trials, rms, factor */, bool no_eta = false) {
   const double MAX_STEP = 1e20, SEARCH_TOL = 1e-4;
   const i64 MAX_SEARCH = 10;
   LBFGS<T> opt(hist);
   double loss = 0.0;
-  auto grad = evaluate(pr, w, b, icpt, loss);
+  auto grad = eval(w, b, loss);
   opt.old_model = w;
   opt.old_model.push_back(b);
   opt.old_grad = grad;
@@ -712,7 +713,7 @@ void lbfgs_train(const Problem<T>& pr, int fmt, std::vector<T>& w, T& b, i64 num
       // CRS/HYBRID pass the step factor as eta (321); the no-trans ELL
       // path calls regularize(w) with the default eta = 1 (419).
       regularize(nw, rtype, lambda, fmt == ELL_F ? 1.0 : (double)factor, no_eta);
-      ng = evaluate(pr, nw, nb, icpt, nloss);
+      ng = eval(nw, nb, nloss);
       if (nloss - loss < SEARCH_TOL) break;
       factor /= T(10.0);
     }
@@ -734,6 +735,14 @@ void lbfgs_train(const Problem<T>& pr, int fmt, std::vector<T>& w, T& b, i64 num
   }
   n_iter = (i == num_iter + 1) ? num_iter : i;
   final_loss = loss;
+}
+
+template <class T>
+void lbfgs_train(const Problem<T>& pr, int fmt, std::vector<T>& w, T& b, i64 num_iter, i64 hist,
+                 T lambda, int rtype, bool icpt, double tol, i64& n_iter, double& final_loss,
+                 double* trace /* per iteration: loss, trials, rms, factor */, bool no_eta = false) {
+  lbfgs_driver<T>([&](const std::vector<T>& ww, T bb, double& l) { return evaluate(pr, ww, bb, icpt, l); }, fmt, w, b,
+                  num_iter, hist, lambda, rtype, tol, n_iter, final_loss, trace, no_eta);
 }
 
 // ------------------------------------------------------------------ SGD
@@ -940,6 +949,56 @@ void softmax_train(const CRS<T>& a, const T* label, const T* sw, i64 K, i64 num_
     if (rmse <= tol) break;
   }
   n_iter = (i == num_iter + 1) ? num_iter : i;
+}
+
+// Multinomial logistic regression by L-BFGS.  The reference trains the
+// softmax model by gradient descent only (softmax_parallelizer.hpp); this
+// composes its gradient — softmax_gradient_descent::compute_gradient with the
+// transposed copy (softmax_gradient_descent.hpp:119-136): G = X^T ((softmax(X
+// W) - onehot(label)) * sw), the softmax as compute_exp_matrix /
+// compute_softmax_probability (159-215) — with the L-BFGS driver above.  The
+// line search needs a loss, which the reference's softmax path does not
+// compute: the cross-entropy sum_i -log p[i, label_i] = log(sum_j exp(z_ij -
+// max_i)) - (z_i,label - max_i), unweighted as logistic_gradient's loss is
+// while its dloss is weighted (gradient_descent.hpp:209); G is its gradient
+// for unit weights.  The model vector is W row-major (n x K), no intercept.
+template <class T>
+void softmax_lbfgs_train(const CRS<T>& a, const T* label, const T* sw, i64 K, i64 num_iter, i64 hist, T lambda,
+                         int rtype, double tol, std::vector<T>& W, i64& n_iter, double& final_loss, double* trace) {
+  const i64 m = a.nrow, n = a.ncol;
+  const CRS<T> t = transpose(a);
+  auto eval = [&](const std::vector<T>& w, T, double& loss) {
+    std::vector<T> Z((size_t)(m * K), T(0));
+    crs_spmm(a, w.data(), K, Z.data());
+    double sumloss = 0.0;
+    for (i64 i = 0; i < m; i++) {
+      T* row = &Z[(size_t)(i * K)];
+      T mx = row[0];
+      for (i64 j = 1; j < K; j++)
+        if (row[j] > mx) mx = row[j];
+      const i64 y = (i64)label[i];
+      const T zy = row[y] - mx;
+      T sum = 0;
+      for (i64 j = 0; j < K; j++) {
+        row[j] = std::exp(row[j] - mx);
+        sum = sum + row[j];
+      }
+      const T inv = 1 / sum;
+      for (i64 j = 0; j < K; j++) {
+        T pr = inv * row[j];
+        pr -= (y == j) ? T(1) : T(0);
+        row[j] = pr * sw[i];
+      }
+      sumloss += (double)(std::log(sum) - zy);
+    }
+    loss = sumloss;
+    std::vector<T> G((size_t)(n * K), T(0));
+    crs_spmm(t, Z.data(), K, G.data());
+    G.push_back(T(0));  // no intercept
+    return G;
+  };
+  T b = 0;
+  lbfgs_driver<T>(eval, CRS_F, W, b, num_iter, hist, lambda, rtype, tol, n_iter, final_loss, trace);
 }
 
 template <class T>
@@ -1190,6 +1249,18 @@ void orc_predict_probability_f64(i64 m, i64 n, const i32* off, const i32* idx, c
 // multinomial_logistic_regression::train main API
 // (ml/glm/multinomial_logistic_regression.hpp:342-378) with CRS data:
 // W[n*K] row-major and b[K] hold the initial model and receive the result.
+int orc_softmax_lbfgs_f64(i64 m, i64 n, const i32* off, const i32* idx, const double* val, const double* label,
+                          const double* sw, i64 K, i64 num_iter, i64 hist, double lambda, int rtype, double tol,
+                          double* W, i64* n_iter, double* final_loss, double* trace) {
+  if (K < 1 || num_iter < 1 || hist < 1 || lambda < 0 || tol < 0) return 1;
+  auto a = make_crs<double>(m, n, off, idx, val);
+  std::vector<double> w(W, W + n * K), swv(sw ? sw : nullptr, sw ? sw + m : nullptr);
+  if (!sw) swv.assign((size_t)m, 1.0);
+  softmax_lbfgs_train(a, label, swv.data(), K, num_iter, hist, lambda, rtype, tol, w, *n_iter, *final_loss, trace);
+  std::copy(w.begin(), w.end(), W);
+  return 0;
+}
+
 int orc_softmax_train_f64(i64 m, i64 n, const i32* off, const i32* idx, const double* val, const double* label,
                           const double* sw, i64 K, i64 num_iter, double alpha, double lambda, int rtype, int icpt,
                           double tol, double* W, double* b, i64* n_iter) {

@@ -65,6 +65,12 @@ int orc_glm_sgd_f64(int fmt, int64_t m, int64_t n, const int32_t* off, const int
                     double* w, double* b, int64_t* n_iter, double* final_loss, int flags, int lkind, double eps);
 void orc_predict_probability_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx,
                                  const double* val, const double* w, double b, double* out);
+// multinomial logistic regression by L-BFGS (the softmax gradient with the
+// L-BFGS driver, cross-entropy loss, no intercept); W row-major n x K in/out
+int orc_softmax_lbfgs_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
+                          const double* label, const double* sw, int64_t K, int64_t num_iter, int64_t hist,
+                          double lambda, int rtype, double tol, double* W, int64_t* n_iter, double* final_loss,
+                          double* trace);
 int orc_softmax_train_f64(int64_t m, int64_t n, const int32_t* off, const int32_t* idx, const double* val,
                           const double* label, const double* sw, int64_t K, int64_t num_iter, double alpha,
                           double lambda, int rtype, int icpt, double tol, double* W, double* b, int64_t* n_iter);
