@@ -586,27 +586,34 @@ def run_regpath(args):
     print(json.dumps(regpath(args, args.datasets, args.iters)), flush=True)
 
 
-def run_multinomial(args):
-    """Multinomial logistic regression: 5,000,000 x 2,000,000, nnz/row
-    1+Poisson(99), Zipf(1.1) columns, |N(0,1)| values, 128 classes sampled
-    from softmax(X W*) with W* ~ N(0, 0.1^2) (Gumbel-max on the device),
-    `--iters` iterations (default 30) of the reference's gradient descent.
-    BF16 (or --storage) values against the plain FP64 path on the same data."""
+def multinomial_lbfgs_run(args, scale=None, iters=None):
+    """Multinomial logistic regression by L-BFGS (the softmax gradient with
+    the L-BFGS loop): 5,000,000 x 2,000,000, nnz/row 1+Poisson(99), Zipf(1.1)
+    columns, values |N(0,1)| rounded to BF16 (the configuration's BF16 data,
+    so BF16 storage holds them exactly), 128 classes sampled from
+    softmax(X W*) with W* ~ N(0, 0.1^2) (Gumbel-max on the device), 30
+    iterations from zero weights.  The --storage arm (BF16 unless FP32 / FP64
+    is asked for) against the FP64 path on the same values: iterations/s,
+    final loss and weight difference."""
     import torch
 
     import frovedis_gb300 as fv
     from frovedis_gb300 import datagen
+    scale = args.scale if scale is None else scale
+    iters = args.iters if iters is None else iters
     K = 128
-    spec = datagen.Spec(m=int(5_000_000 * args.scale), n=int(2_000_000 * args.scale), lam=99.0, col_kind="zipf",
+    spec = datagen.Spec(m=int(5_000_000 * scale), n=int(2_000_000 * scale), lam=99.0, col_kind="zipf",
                         s_col=1.1, val_kind="absnormal", labels=False, seed=5)
     off, idx, val, _ = datagen.generate(spec)
+    val = (fv.bf16_bits(val).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
     m, n, nnz = spec.m, spec.n, int(off[-1])
     ctx = fv.Context(0)
     A = ctx.matrix(m, n, off, idx, val)
     del val
     A.prepare("CRS", transpose=True)
     A.add_storage("f32")
-    if args.storage == "bf16":
+    storage = "bf16" if args.storage in ("split", "bf16") else args.storage
+    if storage == "bf16":
         A.add_storage("bf16")
     g = torch.Generator(device="cuda").manual_seed(7)
     Wt = (torch.randn(n, K, device="cuda", generator=g) * 0.1).contiguous()
@@ -617,45 +624,52 @@ def run_multinomial(args):
     label = torch.argmax(Z + gum, dim=1).to(torch.float64).cpu().numpy()
     del Wt, Z, gum
     torch.cuda.empty_cache()
-    kw = dict(num_iter=args.iters, alpha=1e-5, tol=0.0)
+    kw = dict(num_iter=iters, reg_type="L2", reg_param=1e-6, tol=0.0)
     out = {}
-    for storage in (args.storage, "f64"):
-        fv.multinomial_train(A, label, K, storage=storage, **dict(kw, num_iter=1))
+    Ws = {}
+    for st in (storage, "f64"):
+        fv.multinomial_lbfgs(A, label, K, storage=st, **dict(kw, num_iter=1))
         ctx.reset_profile()
         ctx.set_profiling(True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = fv.multinomial_train(A, label, K, storage=storage, **kw)
+        r = fv.multinomial_lbfgs(A, label, K, storage=st, **kw)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         ctx.set_profiling(False)
         p1, n1 = ctx.profile("batch_pass1")
         p2, n2 = ctx.profile("batch_pass2")
         vec_ms, _ = ctx.profile("lbfgs_vec")
-        s_v = {"f64": 8, "f32": 4, "bf16": 2}[storage]
-        s_x = 8 if storage == "f64" else 4
+        s_v = {"f64": 8, "f32": 4, "bf16": 2}[st]
+        s_x = 8 if st == "f64" else 4
         b1 = nnz * (s_v + 4) + (m + 1) * 4 + n * K * s_x + m * K * s_x + m * 8   # X W, P written
         b2 = nnz * (s_v + 4) + (n + 1) * 4 + m * K * s_x + n * K * 8             # X^T P, G written
-        out[storage] = {"iters_per_s": r["n_iter"] / dt, "n_iter": r["n_iter"], "W": r["W"],
-                        "pass1_ms_avg": p1 / max(n1, 1), "pass2_ms_avg": p2 / max(n2, 1),
-                        "update_ms_avg": vec_ms / max(r["n_iter"], 1),
-                        "pass1_gbs": b1 * n1 / max(p1, 1e-9) / 1e6, "pass2_gbs": b2 * n2 / max(p2, 1e-9) / 1e6,
-                        "tflops_fp32_equiv": 4.0 * nnz * K * n1 / max(p1 + p2, 1e-9) / 1e9}
-    w64 = out["f64"].pop("W")
-    wlo = out[args.storage].pop("W")
+        out[st] = {"iters_per_s": r["n_iter"] / dt, "n_iter": r["n_iter"], "final_loss": r["loss"],
+                   "evaluations": n1, "pass1_ms_avg": p1 / max(n1, 1), "pass2_ms_avg": p2 / max(n2, 1),
+                   "lbfgs_vector_ms": vec_ms,
+                   "pass1_gbs": b1 * n1 / max(p1, 1e-9) / 1e6, "pass2_gbs": b2 * n2 / max(p2, 1e-9) / 1e6,
+                   "tflops_fp32_equiv": 4.0 * nnz * K * n1 / max(p1 + p2, 1e-9) / 1e9}
+        Ws[st] = r["W"]
     A.close()
     ctx.close()
-    peak, peak_kind = load_peak()
-    line = {
-        "metric": "multinomial logistic regression iterations/s (128 classes)", "value": out[args.storage]["iters_per_s"],
-        "unit": "iters/s", "higher_is_better": True,
-        "config": {"workload": "multinomial-5Mx2M-128classes", "rows": m, "cols": n, "nnz": nnz, "classes": K,
-                   "iterations": args.iters, "storage": args.storage, "alpha": kw["alpha"]},
-        "modes": out, "speedup_vs_fp64": out[args.storage]["iters_per_s"] / out["f64"]["iters_per_s"],
-        "weight_rel_diff_vs_fp64": float(np.max(np.abs(wlo - w64)) / max(np.max(np.abs(w64)), 1e-300)),
-        "hbm_peak_gbs": peak, "peak_kind": peak_kind,
+    w64 = Ws["f64"]
+    return {
+        "metric": "multinomial logistic regression L-BFGS iterations/s (128 classes)",
+        "value": out[storage]["iters_per_s"], "unit": "iters/s", "higher_is_better": True,
+        "config": {"workload": "multinomial-lbfgs-5Mx2M-128classes", "rows": m, "cols": n, "nnz": nnz, "classes": K,
+                   "iterations": iters, "storage": storage, "values": "BF16-representable |N(0,1)|",
+                   "solver": "L-BFGS (softmax gradient, cross-entropy line search), no intercept"},
+        "modes": out, "speedup_vs_fp64": out[storage]["iters_per_s"] / out["f64"]["iters_per_s"],
+        "loss_rel_diff_vs_fp64": abs(out[storage]["final_loss"] - out["f64"]["final_loss"]) / abs(out["f64"]["final_loss"]),
+        "weight_rel_diff_vs_fp64": float(np.max(np.abs(Ws[storage] - w64)) / max(np.max(np.abs(w64)), 1.0)),
+        "parity_note": "the FP64 path equals the FP64 oracle to 1e-6 / 1e-5 in tests/test_gpu_multinomial.py "
+                       "(the CPU oracle is too slow for this size); this line states the reduced-precision arm's "
+                       "difference from the FP64 path on the same values",
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_multinomial(args):
+    print(json.dumps(multinomial_lbfgs_run(args)), flush=True)
 
 
 def cpu_oracle_full(off, idx, val, label, spec, args, threads=0):

@@ -66,6 +66,7 @@ EXPORTS = [
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
     "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info", "fvg_matrix_set_head",
     "fvg_matrix_head_info", "fvg_ctx_set_wait_limit", "fvg_debug_inject_alloc_failure", "fvg_matrix_autotune",
+    "fvg_multinomial_lbfgs",
 ]
 
 _lib = None
@@ -125,6 +126,8 @@ def load(build_if_needed: bool = True):
         "fvg_spmv_no_alloc": ([_p, _p, _int, _int, _p, _p], _int),
         "fvg_logreg_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
         "fvg_multinomial_train": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, C.POINTER(_i64)], _int),
+        "fvg_multinomial_lbfgs": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, C.POINTER(_i64), C.POINTER(_dbl)],
+                                  _int),
         "fvg_multinomial_probability": ([_p, _p, _p, _p, _i64, _int, _p], _int),
         "fvg_matrix_get_crs": ([_p, _p, _p, _p, _p], _int),
         "fvg_matrix_load_text": ([_p, C.c_char_p, _int, _i64, C.POINTER(_p)], _int),
@@ -534,6 +537,32 @@ def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=
     ctx.check(fn(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam), _ptr(w), _ptr(b), _ptr(n_iter),
                  _ptr(loss)))
     return dict(w=w, b=b, n_iter=n_iter, loss=loss)
+
+
+def multinomial_lbfgs(mat: Matrix, label, nclasses, sample_weight=None, W0=None, trace=False, **kw):
+    """Multinomial logistic regression by L-BFGS (fvg_multinomial_lbfgs): the
+    reference's softmax gradient with the binary trainers' L-BFGS loop and the
+    cross-entropy as the line search's loss; no intercept.  W0 (n, nclasses)
+    defaults to zeros.  Returns W, n_iter, loss (and trace)."""
+    ctx = mat.ctx
+    K = int(nclasses)
+    label = np.ascontiguousarray(label, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, dtype=np.float64)
+    W = np.zeros((mat.n, K)) if W0 is None else np.array(W0, dtype=np.float64).reshape(mat.n, K)
+    W = np.ascontiguousarray(W)
+    p = glm_params(**kw)
+    tr = None
+    if trace:
+        tr = np.zeros(4 * p.num_iteration)
+        p.trace = tr.ctypes.data_as(C.POINTER(C.c_double))
+    n_iter = _i64()
+    loss = _dbl()
+    ctx.check(ctx.L.fvg_multinomial_lbfgs(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), K, _ptr(W),
+                                          C.byref(n_iter), C.byref(loss)))
+    out = dict(W=W, n_iter=n_iter.value, loss=loss.value)
+    if trace:
+        out["trace"] = tr.reshape(-1, 4)[: n_iter.value]
+    return out
 
 
 def multinomial_train(mat: Matrix, label, nclasses, sample_weight=None, W0=None, b0=None, **kw):

@@ -18,6 +18,8 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
 void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                          const fvg_glm_params* p, i64 k, const double* lam_h, double* w_h, double* b_h,
                          i64* n_iter_h, double* loss_h);
+void multinomial_lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
+                             const fvg_glm_params* p, i64 K, double* w_h, i64* n_iter, double* loss_out);
 void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                        const fvg_glm_params* p, i64 K, double* w_h, double* b_h, i64* n_iter);
 void multinomial_probability(fvg_ctx* c, fvg_matrix* M, const double* w_h, const double* b_h, i64 K, int icpt_on,
@@ -839,6 +841,17 @@ FVG_API fvg_status fvg_multinomial_train(fvg_ctx* c, fvg_matrix* M, const double
   API_BEGIN
   own(c, M);
   multinomial_train(c, M, label, sample_weight, p, nclasses, weight, intercept, n_iter);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_multinomial_lbfgs(fvg_ctx* c, fvg_matrix* M, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* p, int64_t nclasses,
+                                         double* weight, int64_t* n_iter, double* final_loss) {
+  if (!c || !M || !weight || !n_iter || !final_loss) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  own(c, M);
+  multinomial_lbfgs_train(c, M, label, sample_weight, p, nclasses, weight, n_iter, final_loss);
   check_device_error(c);
   API_END(c)
 }

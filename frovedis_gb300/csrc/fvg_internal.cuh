@@ -391,6 +391,22 @@ int glm_split_grid(fvg_ctx* c, i64 m);
 // per-row loss/gradient over z = wtx (+ head) + intercept (float2 pairs)
 void glm_split_rows(fvg_ctx* c, const void* wtx, const void* head, i64 m, const GlmSplitArgs& e);
 
+// The device L-BFGS loop over an evaluation: eval() evaluates the model whose
+// n weights are w64 (device FP64) and whose intercept is *b (device) into the
+// gradient g[0..n] (bias last) and out[0] = loss, out[1] = bias sum;
+// refine() may switch the value precision after an iteration (the accepted
+// model is then evaluated again).  eta_one: regularise with eta = 1 (ELL).
+struct LbfgsEval {
+  virtual void eval(const double* w64, const double* b, double* g, double* out) = 0;
+  virtual bool refine(double rms) {
+    (void)rms;
+    return false;
+  }
+  virtual ~LbfgsEval() = default;
+};
+void lbfgs_core(fvg_ctx* c, i64 n, const fvg_glm_params* p, int eta_one, LbfgsEval& ev, double* w_h, double* b_h,
+                i64* n_iter, double* loss_out);
+
 // Times the candidate training layouts of a matrix and leaves the fastest set.
 void autotune(fvg_ctx* c, fvg_matrix* M, int storage, const double* label_h, int reps,
               std::vector<fvg_tune_choice>& tried, fvg_tune_choice& best);

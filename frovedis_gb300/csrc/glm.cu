@@ -836,35 +836,14 @@ struct HostPinned {
   ~HostPinned() { if (p) cudaFreeHost(p); }
 };
 
-// ============================================================== L-BFGS
-void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
-                 double* w_h, double* b_h, i64* n_iter, double* loss_out) {
-  check_common(p, M, label_h);
-  const int fmt = p->mat_type;
-  if (fmt == FVG_JDS || fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
-  if (p->hist_size < 1 || p->hist_size > kMaxHist)
-    fail(FVG_ERR_INVALID_ARG, "hist_size must be in [1, " + std::to_string(kMaxHist) + "]");
-  const i64 m = M->A.m, n = M->A.n, n1 = n + 1;
+// The device L-BFGS loop (lbfgs_parallelizer::do_train, lbfgs_parallelizer.hpp:
+// 267-364, with lbfgs.hpp:79-143) over an evaluation (LbfgsEval).
+void lbfgs_core(fvg_ctx* c, i64 n, const fvg_glm_params* p, int eta_one, LbfgsEval& ev, double* w_h,
+                       double* b_h, i64* n_iter, double* loss_out) {
+  const i64 n1 = n + 1;
   const int h = (int)p->hist_size;
   cudaStream_t s = c->stream;
-
-  Operand op;
-  build_operand(c, M, fmt, op);
-  DBuf label, sw;
-  label.alloc(sizeof(double) * m, s);
-  FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
-  if (sw_h) {
-    sw.alloc(sizeof(double) * m, s);
-    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
-  }
-  int storage = p->storage;
-  Evaluator ev;
-  ev.init(c, &op, storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, p->intercept);
-  ev.loss = p->loss;
-  ev.eps = p->epsilon;
-
-  // device vectors
-  DBuf W, NW, NWF, G, NG, Q, Z, STEP, S, Y, part, stbuf;
+  DBuf W, NW, G, NG, Q, Z, STEP, S, Y, part, stbuf;
   W.alloc(sizeof(double) * n1, s);
   NW.alloc(sizeof(double) * n1, s);
   G.alloc(sizeof(double) * n1, s);
@@ -874,7 +853,6 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   STEP.alloc(sizeof(double) * n1, s);
   S.alloc(sizeof(double) * n1 * h, s);
   Y.alloc(sizeof(double) * n1 * h, s);
-  NWF.alloc(sizeof(float) * n1, s);
   const int vgrid = (int)std::max<i64>(1, std::min<i64>((n1 + kVecThreads - 1) / kVecThreads, 6 * c->num_sms));
   part.alloc(sizeof(double) * 2 * vgrid + 256, s);
   stbuf.alloc(sizeof(LbState) + 256, s);
@@ -899,24 +877,8 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   DirArgs dargs{G.as<double>(), Q.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(), Y.as<double>(),
                 va, dpart.as<double>(), dbar.as<unsigned long long>(), c->dev_err, barrier_polls(c)};
 
-  const double* W_ = W.as<double>();
-  // split storage: the model as df pairs for the products
-  const bool split = storage == FVG_SPLIT;
-  DBuf W2;
-  if (split) W2.alloc(sizeof(float2) * n1, s);
-  auto weights_for = [&](const double* w64, float* wf) -> const void* {
-    if (storage == FVG_F64) return w64;
-    if (split) {
-      split_vector(c, w64, W2.p, n);
-      return W2.p;
-    }
-    k_d2f<<<vgrid, kVecThreads, 0, s>>>(w64, wf, n);
-    check_launch("d2f");
-    count_launch(c);
-    return wf;
-  };
-  auto evaluate = [&](const void* x, const double* b, double* g, int accepted) {
-    ev.eval(x, b, g, st->eval);
+  auto evaluate = [&](const double* w64, const double* b, double* g, int accepted) {
+    ev.eval(w64, b, g, st->eval);
     ProfScope ps(c, P_LBFGS);
     k_gmax<<<vgrid, kVecThreads, 0, s>>>(g, va);
     k_gnorm<<<vgrid, kVecThreads, 0, s>>>(g, va, accepted);
@@ -929,13 +891,10 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   };
 
   // initial evaluation (lbfgs_parallelizer.hpp:286-295)
-  evaluate(weights_for(W_, NWF.as<float>()), &st->b[0], G.as<double>(), 1);
+  evaluate(W.as<double>(), &st->b[0], G.as<double>(), 1);
   read_host();
   double loss = hp.p[0];
 
-  const bool ell = (fmt == FVG_ELL);
-  const bool mixed = storage == FVG_F32 || storage == FVG_BF16;
-  std::vector<double> rms_hist;
   i64 i = 1;
   for (; i <= p->num_iteration; i++) {
     {
@@ -951,14 +910,12 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
     for (; j <= 10; j++) {
       {
         ProfScope ps(c, P_LBFGS);
-        k_trial<<<vgrid, kVecThreads, 0, s>>>(j, W_, STEP.as<double>(), NW.as<double>(),
-                                              mixed ? NWF.as<float>() : nullptr, p->reg_type, p->reg_param,
-                                              ell ? 1 : 0, p->l2_no_eta, va);
+        k_trial<<<vgrid, kVecThreads, 0, s>>>(j, W.as<double>(), STEP.as<double>(), NW.as<double>(), nullptr,
+                                              p->reg_type, p->reg_param, eta_one, p->l2_no_eta, va);
         check_launch("trial");
         count_launch(c);
       }
-      evaluate(mixed ? (const void*)NWF.p : split ? weights_for(NW.as<double>(), nullptr) : NW.p, &st->b[1],
-               NG.as<double>(), 0);
+      evaluate(NW.as<double>(), &st->b[1], NG.as<double>(), 0);
       read_host();
       newloss = hp.p[0];
       rms_t = hp.p[2];
@@ -982,22 +939,11 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
       p->trace[4 * (i - 1) + 3] = fac;
     }
     if (rms_t <= p->convergence_tol) break;
-    // refinement: leave BF16 values for FP32 once the gradient norm stalls
-    if (mixed && storage == FVG_BF16 && p->refine) {
-      rms_hist.push_back(rms_t);
-      bool stall = false;
-      if (rms_hist.size() >= 4) {
-        double best = *std::min_element(rms_hist.end() - 4, rms_hist.end() - 1);
-        stall = rms_t > p->refine_stall * best;
-      }
-      if (stall) {
-        storage = FVG_F32;
-        ev.set_storage(storage);
-        // re-evaluate the accepted model with FP32 values
-        evaluate(weights_for(W_, NWF.as<float>()), &st->b[0], G.as<double>(), 1);
-        read_host();
-        loss = hp.p[0];
-      }
+    if (ev.refine(rms_t)) {
+      // re-evaluate the accepted model with the new values
+      evaluate(W.as<double>(), &st->b[0], G.as<double>(), 1);
+      read_host();
+      loss = hp.p[0];
     }
   }
   *n_iter = (i == p->num_iteration + 1) ? p->num_iteration : i;
@@ -1005,6 +951,78 @@ void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double*
   FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(b_h, &st->b[0], sizeof(double), cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ============================================================== L-BFGS
+// The GLM evaluation of the loop: the model converted for the value storage
+// (FP64 as is, an FP32 copy for FP32 / BF16 values, df pairs for split
+// values), then the two fused passes (Evaluator::eval); BF16 runs leave for
+// FP32 values once the gradient-norm decrease stalls (refinement).
+struct GlmLbfgsEval : LbfgsEval {
+  fvg_ctx* c = nullptr;
+  Evaluator* ev = nullptr;
+  const fvg_glm_params* p = nullptr;
+  int storage = FVG_F64;
+  i64 n = 0;
+  DBuf x;  // the converted model
+  std::vector<double> rms_hist;
+  void eval(const double* w64, const double* b, double* g, double* out) override {
+    const void* xp = w64;
+    if (storage == FVG_SPLIT) {
+      split_vector(c, w64, x.p, n);
+      xp = x.p;
+    } else if (storage != FVG_F64) {
+      const int vg = (int)std::max<i64>(1, std::min<i64>((n + kVecThreads - 1) / kVecThreads, 6 * c->num_sms));
+      k_d2f<<<vg, kVecThreads, 0, c->stream>>>(w64, x.as<float>(), n);
+      check_launch("d2f");
+      count_launch(c);
+      xp = x.p;
+    }
+    ev->eval(xp, b, g, out);
+  }
+  bool refine(double rms_t) override {
+    if (storage != FVG_BF16 || !p->refine) return false;
+    rms_hist.push_back(rms_t);
+    if (rms_hist.size() < 4) return false;
+    const double best = *std::min_element(rms_hist.end() - 4, rms_hist.end() - 1);
+    if (!(rms_t > p->refine_stall * best)) return false;
+    storage = FVG_F32;
+    ev->set_storage(storage);
+    return true;
+  }
+};
+
+void lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h, const fvg_glm_params* p,
+                 double* w_h, double* b_h, i64* n_iter, double* loss_out) {
+  check_common(p, M, label_h);
+  const int fmt = p->mat_type;
+  if (fmt == FVG_JDS || fmt < 0 || fmt > 3) fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (p->hist_size < 1 || p->hist_size > kMaxHist)
+    fail(FVG_ERR_INVALID_ARG, "hist_size must be in [1, " + std::to_string(kMaxHist) + "]");
+  const i64 m = M->A.m, n = M->A.n;
+  cudaStream_t s = c->stream;
+  Operand op;
+  build_operand(c, M, fmt, op);
+  DBuf label, sw;
+  label.alloc(sizeof(double) * m, s);
+  FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (sw_h) {
+    sw.alloc(sizeof(double) * m, s);
+    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  Evaluator ev;
+  ev.init(c, &op, p->storage, label.as<double>(), sw_h ? sw.as<double>() : nullptr, p->intercept);
+  ev.loss = p->loss;
+  ev.eps = p->epsilon;
+  GlmLbfgsEval ge;
+  ge.c = c;
+  ge.ev = &ev;
+  ge.p = p;
+  ge.storage = p->storage;
+  ge.n = n;
+  if (p->storage != FVG_F64) ge.x.alloc(sizeof(float2) * (n + 1), s);
+  // ELL: the no-trans driver regularises with eta = 1 (lbfgs_parallelizer.hpp:419)
+  lbfgs_core(c, n, p, fmt == FVG_ELL ? 1 : 0, ge, w_h, b_h, n_iter, loss_out);
 }
 
 // ============================================================ SGD

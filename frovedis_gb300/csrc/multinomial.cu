@@ -25,7 +25,7 @@ constexpr int kMT = 256;
 
 void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int K, const double* label,
                       const double* sw, const float* label_f, const float* sw_f, int icpt, const double* icpt_v,
-                      void* P, i64 ldp, void* scratch);
+                      void* P, i64 ldp, void* scratch, double* loss_out = nullptr);
 
 template <class T> __device__ __forceinline__ T exp_t(T x);
 template <> __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
@@ -295,6 +295,93 @@ void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const d
   FVG_CUDA(cudaMemcpyAsync(w_h, W.p, sizeof(double) * nk, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(b_h, ICPT.p, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));
+}
+
+// Multinomial logistic regression by L-BFGS (no reference counterpart: the
+// reference trains the softmax model by gradient descent only).  The
+// gradient is the reference's, softmax_gradient_descent::compute_gradient
+// with the transposed copy (softmax_gradient_descent.hpp:119-136); the loss
+// the line search needs, which the reference's softmax path does not
+// compute, is the cross-entropy sum_i -log p[i, label_i] (unweighted, as
+// logistic_gradient's loss is), accumulated in the forward pass's softmax
+// epilogue.  The device L-BFGS loop (lbfgs.hpp:79-143, lbfgs_parallelizer.hpp
+// :267-364) runs on the weights W (num_col x K row-major, FP64) as one vector
+// of num_col * K entries; no intercept.
+struct SoftmaxLbfgsEval : LbfgsEval {
+  fvg_ctx* c = nullptr;
+  fvg_matrix* M = nullptr;
+  Softmax sm;
+  int storage = FVG_F64;
+  i64 n = 0;
+  int K = 0;
+  const double* label = nullptr;
+  const double* sw = nullptr;
+  DBuf WF, s2, lossbuf;
+  void eval(const double* w64, const double* b, double* g, double* out) override {
+    (void)b;
+    const bool mixed = storage != FVG_F64;
+    const void* wx = w64;
+    const i64 nk = n * K;
+    if (mixed) {
+      const unsigned dg = (unsigned)std::max<i64>(1, std::min<i64>((nk + 255) / 256, 4 * (i64)c->num_sms));
+      km_d2f<<<dg, 256, 0, c->stream>>>(w64, WF.as<float>(), nk);
+      check_launch("km_d2f");
+      count_launch(c);
+      wx = WF.p;
+    }
+    {
+      ProfScope ps(c, P_BATCH_PASS1);
+      crs_spmm_softmax(c, *sm.A, storage, wx, K, K, label, sw, label ? sm.label_f.as<float>() : nullptr,
+                       sw ? sm.sw_f.as<float>() : nullptr, 0, nullptr, sm.Z.p, K, sm.scratch.p, lossbuf.as<double>());
+    }
+    {
+      ProfScope ps(c, P_BATCH_PASS2);
+      crs_spmm_block(c, *M->AT, storage, sm.Z.p, K, K, FVG_F64, g, K, s2.p);
+    }
+    FVG_CUDA(cudaMemsetAsync(g + nk, 0, sizeof(double), c->stream));
+    FVG_CUDA(cudaMemcpyAsync(out, lossbuf.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    FVG_CUDA(cudaMemsetAsync(out + 1, 0, sizeof(double), c->stream));
+  }
+};
+
+void multinomial_lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
+                             const fvg_glm_params* p, i64 K, double* w_h, i64* n_iter, double* loss_out) {
+  check_common(p, M, label_h);
+  if (K < 2 || K > 128) fail(FVG_ERR_INVALID_ARG, "the L-BFGS multinomial solver takes 2 to 128 classes");
+  if (p->intercept) fail(FVG_ERR_UNSUPPORTED, "the L-BFGS multinomial solver trains no intercept");
+  if (p->mat_type != FVG_CRS && p->mat_type != FVG_HYBRID)
+    fail(FVG_ERR_UNSUPPORTED, "Unsupported input matrix type!!\n");
+  if (p->hist_size < 1 || p->hist_size > 32) fail(FVG_ERR_INVALID_ARG, "hist_size must be in [1, 32]");
+  const int storage = p->storage;
+  if (storage == FVG_SPLIT) fail(FVG_ERR_UNSUPPORTED, "split storage is offered by the binary L-BFGS trainers, single evaluations and the products");
+  const i64 m = M->A.m, n = M->A.n;
+  cudaStream_t s = c->stream;
+  if (!M->AT) {
+    M->AT.reset(new DevCRS());
+    crs_build_transpose(c, M->A, *M->AT, M->master);
+  }
+  crs_ensure_plane(c, *M->AT, storage, M->master);
+  DBuf label, sw;
+  label.alloc(sizeof(double) * m, s);
+  FVG_CUDA(cudaMemcpyAsync(label.p, label_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (sw_h) {
+    sw.alloc(sizeof(double) * m, s);
+    FVG_CUDA(cudaMemcpyAsync(sw.p, sw_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  SoftmaxLbfgsEval ev;
+  ev.c = c;
+  ev.M = M;
+  ev.storage = storage;
+  ev.n = n;
+  ev.K = (int)K;
+  ev.label = label.as<double>();
+  ev.sw = sw_h ? sw.as<double>() : nullptr;
+  ev.sm.init(c, &M->A, M->master, storage, (int)K, ev.label, ev.sw);
+  if (storage != FVG_F64) ev.WF.alloc(sizeof(float) * (size_t)n * K, s);
+  ev.s2.alloc((size_t)spmm_scratch_bytes(c, *M->AT, storage), s);
+  ev.lossbuf.alloc(sizeof(double) * 2 * 128, s);
+  double b = 0.0;
+  lbfgs_core(c, n * K, p, 0, ev, w_h, &b, n_iter, loss_out);
 }
 
 // multinomial_logistic_regression_model<T>::compute_probability_matrix

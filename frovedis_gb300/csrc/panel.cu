@@ -574,12 +574,14 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
 // the next and, unlike the fixed rounding of the values, does not cancel in
 // the L-BFGS gradient differences).  To fit a panel beside the staging
 // buffers, one CTA of kSplitWarps warps per SM walks its own work items of at
-// most kSplitTile entries, so that one item is one pass of 32 lanes x 8
-// entries: no products are staged and no second pass re-reads them.
-constexpr int kSplitWarps = 20;
-constexpr int kSplitTile = 240;  // an item's staged copy (8-aligned ends) fits 32 lanes x 8 entries
+// most kSplitTile entries, so that one item is one pass of 32 lanes x
+// kSplitChunk entries: no products are staged and no second pass re-reads
+// them.
+constexpr int kSplitWarps = 12;
+constexpr int kSplitTile = 480;  // an item's staged copy (8-aligned ends) fits 32 lanes x 16 entries
+constexpr int kSplitChunk = 16;  // entries per lane
 struct SplitSmem {
-  static constexpr int kCap = 256;                     // entries of one copy
+  static constexpr int kCap = 32 * kSplitChunk;        // entries of one copy
   static constexpr int kHiB = kCap * 2;                // offset of the FP32 values
   static constexpr int kLoB = kHiB + kCap * 4;         // offset of the BF16 residuals
   static constexpr int kStageB = kLoB + kCap * 2;      // = kCap * 8
@@ -635,7 +637,8 @@ __device__ __forceinline__ df seg_scan_df(df v, bool reset, int lane) {
 // One CTA of kSplitWarps warps per SM takes units of `group` consecutive
 // panels (as k_panel).  Per work item (at most kSplitTile entries) a bulk
 // copy stages the entries (uint16 slots, FP32 values, BF16 residuals); lane L
-// then takes the 8 staged entries 8L..8L+7 (16-byte shared loads), makes each
+// then takes the kSplitChunk staged entries from kSplitChunk*L on (16-byte
+// shared loads), makes each
 // product exact (p + t), and adds its row segments in registers with TwoSum:
 // a row that ends inside the chunk is written at once when it also started
 // there; the row that was open at the chunk's start and the one open at its
@@ -645,6 +648,7 @@ __device__ __forceinline__ df seg_scan_df(df v, bool reset, int lane) {
 __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK p) {
   using SM = SplitSmem;
   constexpr int NW = kSplitWarps;
+  constexpr int CH = kSplitChunk;
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + 2 * w;
@@ -702,18 +706,27 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
       pend = false;
       __syncwarp();
       // this lane's 8 staged entries
-      const uint4 s4 = reinterpret_cast<const uint4*>(area)[lane];
-      const float4 h0 = reinterpret_cast<const float4*>(area + SM::kHiB)[2 * lane];
-      const float4 h1 = reinterpret_cast<const float4*>(area + SM::kHiB)[2 * lane + 1];
-      const uint4 l4 = reinterpret_cast<const uint4*>(area + SM::kLoB)[lane];
-      const unsigned sw[4] = {s4.x, s4.y, s4.z, s4.w}, lw[4] = {l4.x, l4.y, l4.z, l4.w};
-      const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
-      const int lo_e = max(it.e0 - q0, lane * 8), hi_e = min(it.e1 - q0, lane * 8 + 8);
+      // this lane's CH staged entries (16-byte shared loads)
+      unsigned sw[CH / 2], lw[CH / 2];
+      float hv[CH];
+#pragma unroll
+      for (int q = 0; q < CH / 8; q++) {
+        const uint4 s4 = reinterpret_cast<const uint4*>(area)[lane * (CH / 8) + q];
+        const uint4 l4 = reinterpret_cast<const uint4*>(area + SM::kLoB)[lane * (CH / 8) + q];
+        sw[4 * q] = s4.x; sw[4 * q + 1] = s4.y; sw[4 * q + 2] = s4.z; sw[4 * q + 3] = s4.w;
+        lw[4 * q] = l4.x; lw[4 * q + 1] = l4.y; lw[4 * q + 2] = l4.z; lw[4 * q + 3] = l4.w;
+      }
+#pragma unroll
+      for (int q = 0; q < CH / 4; q++) {
+        const float4 h = reinterpret_cast<const float4*>(area + SM::kHiB)[lane * (CH / 4) + q];
+        hv[4 * q] = h.x; hv[4 * q + 1] = h.y; hv[4 * q + 2] = h.z; hv[4 * q + 3] = h.w;
+      }
+      const int lo_e = max(it.e0 - q0, lane * CH), hi_e = min(it.e1 - q0, lane * CH + CH);
       if (!tile) {
         DfAcc acc;
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-          const int e = lane * 8 + k;
+        for (int k = 0; k < CH; k++) {
+          const int e = lane * CH + k;
           if (e >= lo_e && e < hi_e) {
             const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
             const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
@@ -731,10 +744,10 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         for (int j = lane; j < R; j += 32)
           if (soff[j] == soff[j + 1]) p.ypan[it.r0 + j] = make_float2(0.f, 0.f);  // empty rows
         // the lane's 8 products (zero outside its valid range)
-        float pp[8], tt[8];
+        float pp[CH], tt[CH];
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-          const int e = lane * 8 + k;
+        for (int k = 0; k < CH; k++) {
+          const int e = lane * CH + k;
           const bool ok = e >= lo_e && e < hi_e;
           const unsigned c = ok ? (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu : 0u;
           const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
@@ -759,7 +772,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           starts = (int)soff[j] == lo_e;
           nb = soff[j + 1];
           while (nb < hi_e) {
-            B |= 1u << (nb - lane * 8);
+            B |= 1u << (nb - lane * CH);
             do {
               j++;
               nb = soff[j + 1];
@@ -767,7 +780,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           }
         }
         df H, T;
-        chunk_segments<8>(pp, tt, B, H, T);
+        chunk_segments<CH>(pp, tt, B, H, T);
         if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
           unsigned rest = B & (B - 1);
           int a = __ffs(B) - 1, jj = j0;
@@ -777,7 +790,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           while (rest) {
             const int b = __ffs(rest) - 1;
             rest &= rest - 1;
-            p.ypan[it.r0 + jj] = df_pack(chunk_range<8>(pp, tt, a, b));
+            p.ypan[it.r0 + jj] = df_pack(chunk_range<CH>(pp, tt, a, b));
             a = b;
             do {
               jj++;

@@ -142,6 +142,9 @@ __device__ __forceinline__ void row_dot(const SpmmK& p, i32 e0, i32 e1, int lane
 template <class AT> __device__ __forceinline__ AT exp_acc(AT x);
 template <> __device__ __forceinline__ double exp_acc<double>(double x) { return exp(x); }
 template <> __device__ __forceinline__ float exp_acc<float>(float x) { return expf(x); }
+template <class AT> __device__ __forceinline__ AT log_acc(AT x);
+template <> __device__ __forceinline__ double log_acc<double>(double x) { return log(x); }
+template <> __device__ __forceinline__ float log_acc<float>(float x) { return logf(x); }
 
 template <class AT, class YT, int EPI, int CPL, bool VEC, class S>
 __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[CPL], const AT (&b)[CPL], int lane,
@@ -201,6 +204,12 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    // the label's margin z_label - max, for the cross-entropy
+    AT zy = 0;
+    if (has_label)
+#pragma unroll
+      for (int q = 0; q < CPL; q++)
+        if (ON(q) && lab == (AT)colof<VEC, CPL>(lane, q)) zy = z[q] - mx;
     AT sum = 0;
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
@@ -209,6 +218,13 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    // cross-entropy -log p[label] = log(sum) - (z_label - max), unweighted,
+    // into lane 0's first partial (the L-BFGS line search's loss)
+    if (has_label && p.cta_part) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) zy += __shfl_xor_sync(0xffffffffu, zy, o);
+      if (lane == 0) ls[0].add(log_acc<AT>(sum) - zy);
+    }
     const AT inv = (AT)1 / sum;
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
@@ -260,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm(const SpmmK p) {
       }
     }
   }
-  if constexpr (EPI == EPI_LOGREG) {
+  if constexpr (EPI == EPI_LOGREG || EPI == EPI_SOFTMAX) if (EPI == EPI_LOGREG || p.cta_part) {
     __shared__ double red[kThreads / 32][NC][2];
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
@@ -319,7 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
     }
     spmm_epi<AT, YT, EPI, CPL, VEC>(p, f.long_rows[i], a, b, lane, ls, bs);
   }
-  if constexpr (EPI == EPI_LOGREG) {
+  if constexpr (EPI == EPI_LOGREG || EPI == EPI_SOFTMAX) if (EPI == EPI_LOGREG || p.cta_part) {
     __shared__ double red[kThreads / 32][NC][2];
     __shared__ double half[2][2 * NC];
     __shared__ bool last;
@@ -342,9 +358,24 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
     __syncthreads();
     if (!last) return;
     __threadfence();
+    if constexpr (EPI == EPI_SOFTMAX) {
+      // the cross-entropy sits in column 0's loss partials: thread t adds
+      // CTAs t, t + 256, ... of both kernels, then a fixed tree
+      CSum t;
+      for (i64 bb = threadIdx.x; bb < f.ncta; bb += kThreads) t.add(__ldcg(&p.cta_part[(bb * NC) * 2]));
+      for (i64 bb = threadIdx.x; bb < gridDim.x; bb += kThreads) t.add(__ldcg(&f.fin_part[(bb * NC) * 2]));
+      double tl = 0.0, tb = 0.0;
+      block_csum2(t.total(), 0.0, &tl, &tb);
+      if (threadIdx.x == 0) {
+        f.out[0] = tl;
+        f.out[1] = 0.0;
+        *f.ticket = 0u;
+      }
+      return;
+    } else {
     // (column, quantity) pairs over the threads, two halves of the partials
     // each; 2*NC pairs must fit in half the CTA
-    static_assert(4 * NC <= kThreads, "logistic epilogue: too many columns per launch");
+    static_assert(EPI != EPI_LOGREG || 4 * NC <= kThreads, "logistic epilogue: too many columns per launch");
     const int pair = threadIdx.x % (2 * NC), hf = threadIdx.x / (2 * NC);
     const int col = pair % NC, qq = pair / NC;
     CSum t;
@@ -364,6 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
       }
     }
     if (threadIdx.x == 0) *f.ticket = 0u;
+    }
   }
 }
 
@@ -405,13 +437,15 @@ static void launch_spmm_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, Sp
   p.val = a.val[storage].p;
   p.items = s.items.as<Item>();
   p.nitems = s.nitems;
-  p.cta_part = cta;
+  // softmax: the cross-entropy is reduced only when the caller asks for it
+  const bool reduce = EPI == EPI_LOGREG || (EPI == EPI_SOFTMAX && out);
+  p.cta_part = reduce ? cta : nullptr;
   if (s.nitems > 0) {
     k_spmm<VT, XT, AT, YT, EPI, CPL, VEC><<<grid, kThreads, 0, c->stream>>>(p);
     check_launch("k_spmm");
     count_launch(c);
   }
-  if (s.nlong > 0 || EPI == EPI_LOGREG) {
+  if (s.nlong > 0 || reduce) {
     SpmmFin f;
     f.k = p;
     f.long_rows = s.long_rows.as<i32>();
@@ -514,10 +548,11 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
 }
 
 // Multinomial forward pass, K <= 128 classes: P = (softmax(A W + icpt) -
-// onehot(label)) * sw, row-major [m][ldp] of the accumulator type.
+// onehot(label)) * sw, row-major [m][ldp] of the accumulator type; with
+// loss_out (device, 2 * K doubles) also the cross-entropy sum in loss_out[0].
 void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int K, const double* label,
                       const double* sw, const float* label_f, const float* sw_f, int icpt, const double* icpt_v,
-                      void* P, i64 ldp, void* scratch) {
+                      void* P, i64 ldp, void* scratch, double* loss_out) {
   if (K < 1 || K > kSpmmMaxCols) fail(FVG_ERR_INTERNAL, "softmax block width out of range");
   const Sched& s = crs_sched(c, a, tile_for_storage(storage));
   SpmmK p = {};
@@ -535,11 +570,11 @@ void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw
   char* sc = (char*)scratch;
   FVG_CUDA(cudaMemsetAsync(sc, 0, 256, c->stream));
   if (storage == FVG_F64)
-    launch_spmm<double, double, double, double, EPI_SOFTMAX, 4>(c, a, s, storage, p, nullptr, nullptr, sc);
+    launch_spmm<double, double, double, double, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
   else if (storage == FVG_F32)
-    launch_spmm<float, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, nullptr, nullptr, sc);
+    launch_spmm<float, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
   else
-    launch_spmm<bf16, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, nullptr, nullptr, sc);
+    launch_spmm<bf16, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
 }
 
 // Y = A X, X row-major num_col x k, Y row-major num_row x k, in blocks of 128

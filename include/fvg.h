@@ -339,6 +339,21 @@ FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const
 FVG_API fvg_status fvg_multinomial_train(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
                                          const double* sample_weight, const fvg_glm_params* params, int64_t nclasses,
                                          double* weight, double* intercept, int64_t* n_iter);
+/* Multinomial logistic regression by L-BFGS: no reference counterpart (the
+ * reference trains it by gradient descent only).  The gradient is the
+ * reference's softmax gradient with the transposed copy
+ * (ml/glm/softmax_gradient_descent.hpp:119-136), the L-BFGS loop that of the
+ * binary trainers (lbfgs.hpp:79-143, lbfgs_parallelizer.hpp:267-364), and
+ * the line search's loss the cross-entropy sum_i -log p[i, label_i]
+ * (unweighted, as logistic_gradient's loss).  No intercept; 2 <= nclasses
+ * <= 128.  label[num_row] holds class ids; weight[num_col*nclasses]
+ * (row-major) the initial model on entry, the trained one on return.
+ * params: num_iteration, hist_size, reg_param, reg_type, convergence_tol,
+ * mat_type (CRS or HYBRID, computed on the CRS layout), storage (FP64, FP32
+ * or BF16 values), trace. */
+FVG_API fvg_status fvg_multinomial_lbfgs(fvg_ctx* ctx, fvg_matrix* mat, const double* label,
+                                         const double* sample_weight, const fvg_glm_params* params, int64_t nclasses,
+                                         double* weight, int64_t* n_iter, double* final_loss);
 /* multinomial_logistic_regression_model<T>::compute_probability_matrix
  * (multinomial_logistic_regression_model.hpp:82-89): prob[num_row*nclasses],
  * FP64. */

@@ -139,3 +139,61 @@ def test_multinomial_errors(ctx):
         fv.multinomial_train(A, label, 0)
     with pytest.raises(fv.FvgError):
         fv.multinomial_train(A, label, 3, alpha=0.0)
+
+
+# ------------------------------------------------ multinomial by L-BFGS
+def _mlr_data(m=3000, n=200, K=5, seed=3):
+    from frovedis_gb300 import datagen
+    off, idx, val, _ = datagen.generate(datagen.Spec(m=m, n=n, lam=15.0, seed=seed, labels=False))
+    a = oracle.CRS(m, n, off, idx, val)
+    rng = np.random.default_rng(seed)
+    Z = oracle.spmm(a, rng.standard_normal((n, K)) * 0.3)
+    label = np.argmax(Z + rng.gumbel(size=Z.shape), axis=1).astype(np.float64)
+    return a, label
+
+
+@pytest.mark.parametrize("K,reg", [(5, "L2"), (5, "ZERO"), (37, "L1"), (128, "L2")])
+def test_multinomial_lbfgs_matches_oracle(ctx, K, reg):
+    # the reference's softmax gradient with the L-BFGS driver, FP64: the same
+    # line-search decisions, loss within 1e-6, weights within 1e-5
+    a, label = _mlr_data(m=2500, n=150, K=K, seed=K)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    kw = dict(num_iter=25, reg_type=reg, reg_param=1e-4)
+    r = fv.multinomial_lbfgs(A, label, K, trace=True, **kw)
+    ro = oracle.softmax_lbfgs(a, label, K, **kw)
+    assert r["n_iter"] == ro["n_iter"]
+    assert np.array_equal(r["trace"][:, 1], ro["trace"][:, 1]), "line-search trial counts differ"
+    assert abs(r["loss"] - ro["loss"]) <= 1e-6 * abs(ro["loss"])
+    assert np.max(np.abs(r["W"] - ro["W"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["W"])))
+
+
+def test_multinomial_lbfgs_sample_weights_and_start(ctx):
+    a, label = _mlr_data(m=2000, n=120, K=7, seed=11)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, a.val)
+    rng = np.random.default_rng(2)
+    sw = rng.uniform(0.5, 2.0, a.m)
+    W0 = rng.standard_normal((a.n, 7)) * 0.05
+    kw = dict(num_iter=15, reg_type="L2", reg_param=1e-3)
+    r = fv.multinomial_lbfgs(A, label, 7, sample_weight=sw, W0=W0, **kw)
+    ro = oracle.softmax_lbfgs(a, label, 7, sw=sw, W0=W0, **kw)
+    assert r["n_iter"] == ro["n_iter"]
+    assert abs(r["loss"] - ro["loss"]) <= 1e-6 * abs(ro["loss"])
+    assert np.max(np.abs(r["W"] - ro["W"])) <= 1e-5 * max(1.0, np.max(np.abs(ro["W"])))
+
+
+def test_multinomial_lbfgs_reduced_precision_and_errors(ctx):
+    # FP32 / BF16 values (FP32 accumulation): the loss within 1e-3 of the
+    # FP64 oracle on the same rounded values; unsupported settings rejected
+    a, label = _mlr_data(m=3000, n=200, K=10, seed=5)
+    vb = (fv.bf16_bits(a.val).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    ab = oracle.CRS(a.m, a.n, a.off, a.idx, vb)
+    A = ctx.matrix(a.m, a.n, a.off, a.idx, vb)
+    kw = dict(num_iter=15, reg_type="L2", reg_param=1e-4)
+    ro = oracle.softmax_lbfgs(ab, label, 10, **kw)
+    for storage in ("f32", "bf16"):
+        r = fv.multinomial_lbfgs(A, label, 10, storage=storage, **kw)
+        assert abs(r["loss"] - ro["loss"]) <= 1e-3 * abs(ro["loss"]), storage
+    with pytest.raises(fv.FvgError):
+        fv.multinomial_lbfgs(A, label, 10, intercept=True, **kw)
+    with pytest.raises(fv.FvgError):
+        fv.multinomial_lbfgs(A, label, 200, **kw)
