@@ -346,8 +346,9 @@ def run_gpu(args):
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
     spmv = None if args.skip_spmv else spmv_suite(ctx, args)
-    rp = None if args.skip_regpath else regpath(args, args.regpath_datasets, 20)
     ctx.close()
+    rp = None if args.skip_regpath else regpath(args, args.regpath_datasets, 20)
+    mlr = None if args.skip_mlr else multinomial_lbfgs_run(args, iters=30)
     # the FP64 oracle (the reference's loops) on the whole matrix: the CPU
     # baseline and the parity reference of every arm
     cpu = None
@@ -406,6 +407,7 @@ def run_gpu(args):
         "precision_modes": modes,
         "spmv_2m": spmv,
         "batched_regpath": rp,
+        "multinomial_lbfgs": mlr,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -495,11 +497,14 @@ def spmv_suite(ctx, args, reps=10):
 
 
 def regpath(args, datasets, iters):
-    """Batched regularisation path: 16 datasets (500,000 columns, 1.4e7 rows
-    in all, 7e8 nonzeros), 64 L2 values log-spaced 1e-6..1 trained together
-    per dataset, `iters` iterations.  Compared with the plain FP64 GPU path
-    run one model at a time (timed on 4 of the 64 values per dataset and
-    scaled by 16) at the same final losses."""
+    """Batched regularisation path over uneven datasets in one launch: 16
+    datasets (500,000 columns, 1.4e7 rows in all, 7e8 nonzeros), 64 L2
+    values log-spaced 1e-6..1 per dataset, every (dataset, value) model
+    trained together by fvg_logreg_lbfgs_multi (the datasets stacked
+    block-diagonally, the whole training one CUDA-graph launch), `iters`
+    iterations.  Compared with the plain FP64 GPU path run one model at a
+    time (timed on 4 of the 64 values per dataset and scaled by 16) at the
+    same final losses."""
     import torch
 
     import frovedis_gb300 as fv
@@ -508,78 +513,86 @@ def regpath(args, datasets, iters):
     lams = np.logspace(-6, 0, 64)
     probe = [0, 21, 42, 63]
     ctx = fv.Context(0)
-    tot = {"batched_s": 0.0, "batched_model_iters": 0, "fp64_single_s_est": 0.0, "nnz": 0, "rows": 0,
-           "pass1_ms": 0.0, "pass1_n": 0, "pass2_ms": 0.0, "pass2_n": 0, "alg_bytes": 0.0, "flops": 0.0}
-    loss_err = []
     # the batched trainer keeps FP64 / FP32 / BF16 values (split storage is a
     # single-model path): BF16 when the headline arm is split
     storage = "bf16" if args.storage == "split" else args.storage
     s_v = {"f64": 8, "f32": 4, "bf16": 2}[storage]
+    s_x = 8 if storage == "f64" else 4
+    mats, labels, nnzs = [], [], []
     for spec in specs:
         off, idx, val, label = datagen.generate(spec)
-        m, n, nnz = spec.m, spec.n, int(off[-1])
-        A = ctx.matrix(m, n, off, idx, val)
+        A = ctx.matrix(spec.m, spec.n, off, idx, val)
         A.prepare("CRS", transpose=True)
         if storage != "f64":
             A.add_storage(storage)
             A.add_storage("f32")
-        kw = dict(num_iter=iters, reg_type="L2", w0=np.zeros(n))
-        fv.logreg_lbfgs_batched(A, label, lams[:2], storage=storage, **dict(kw, num_iter=2))
-        torch.cuda.synchronize()
-        ctx.reset_profile()
-        ctx.set_profiling(True)
-        t0 = time.perf_counter()
-        rb = fv.logreg_lbfgs_batched(A, label, lams, storage=storage, **kw)
-        torch.cuda.synchronize()
-        tot["batched_s"] += time.perf_counter() - t0
-        ctx.set_profiling(False)
-        for key in ("pass1", "pass2"):
-            ms, cnt = ctx.profile("batch_" + key)
-            tot[key + "_ms"] += ms
-            tot[key + "_n"] += cnt
-        tot["vec_ms"] = tot.get("vec_ms", 0.0) + ctx.profile("lbfgs_vec")[0]
-        evals = ctx.profile("batch_pass1")[1]
-        s_x = 8 if storage == "f64" else 4
-        per_eval = (2 * nnz * (s_v + 4) + (m + n + 2) * 4 + n * 64 * s_x + 2 * m * 64 * s_x + m * 8
-                    + (n + 1) * 64 * 8)
-        tot["alg_bytes"] += per_eval * evals
-        tot["flops"] += 4.0 * nnz * 64 * evals
-        tot["batched_model_iters"] += int(rb["n_iter"].sum())
-        ts = 0.0
+        mats.append(A)
+        labels.append(label)
+        nnzs.append(int(off[-1]))
+        del off, idx, val
+    nd, k = len(mats), len(lams)
+    kw = dict(num_iter=iters, reg_type="L2", w0=[np.zeros(A.n) for A in mats])
+    fv.logreg_lbfgs_multi(mats, labels, lams, storage=storage, **dict(kw, num_iter=2))  # warm-up
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches
+    t0 = time.perf_counter()
+    rb = fv.logreg_lbfgs_multi(mats, labels, lams, storage=storage, **kw)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = ctx.kernel_launches - l0
+    # the same training with per-phase events (launches issued one by one)
+    ctx.reset_profile()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    rp = fv.logreg_lbfgs_multi(mats, labels, lams, storage=storage, **kw)
+    torch.cuda.synchronize()
+    wall_eager = time.perf_counter() - t0
+    ctx.set_profiling(False)
+    prof = {key: ctx.profile("batch_" + key) for key in ("pass1", "pass2")}
+    vec_ms = ctx.profile("lbfgs_vec")[0]
+    evals = prof["pass1"][1]
+    m_tot, nnz = sum(sp.m for sp in specs), sum(nnzs)
+    n1_tot = sum(sp.n + 1 for sp in specs)
+    per_eval = (2 * nnz * (s_v + 4) + (m_tot + n1_tot + 2) * 4 + n1_tot * 64 * s_x + 2 * m_tot * 64 * s_x
+                + m_tot * 8 + n1_tot * 64 * 8)
+    kms = prof["pass1"][0] + prof["pass2"][0]
+    value = int(rb["n_iter"].sum()) / wall
+    loss_err, ts = [], 0.0
+    for d, A in enumerate(mats):
         for j in probe:
             t0 = time.perf_counter()
-            rs = fv.logreg_lbfgs(A, label, reg_param=lams[j], storage="f64", **kw)
+            rs = fv.logreg_lbfgs(A, labels[d], reg_param=lams[j], storage="f64", num_iter=iters, reg_type="L2",
+                                 w0=np.zeros(A.n))
             torch.cuda.synchronize()
             ts += time.perf_counter() - t0
-            loss_err.append(abs(rb["loss"][j] - rs["loss"]) / abs(rs["loss"]))
-        tot["fp64_single_s_est"] += ts * len(lams) / len(probe)
-        tot["nnz"] += nnz
-        tot["rows"] += m
+            loss_err.append(abs(rb["loss"][d, j] - rs["loss"]) / abs(rs["loss"]))
+    for A in mats:
         A.close()
     ctx.close()
-    value = tot["batched_model_iters"] / tot["batched_s"]
-    base = len(specs) * len(lams) * iters / tot["fp64_single_s_est"]
-    kms = tot["pass1_ms"] + tot["pass2_ms"]
+    base = nd * k * iters / (ts * k / len(probe))
     peak, peak_kind = load_peak()
-    line = {
-        "metric": "batched L-BFGS model-iterations/s (64 regularisation values per dataset)",
+    return {
+        "metric": "batched L-BFGS model-iterations/s (64 regularisation values x 16 uneven datasets, one launch)",
         "value": value, "unit": "model-iters/s", "higher_is_better": True,
-        "config": {"workload": "logreg-regpath-16x500k-64lambda", "datasets": len(specs), "rows": tot["rows"],
-                   "cols": specs[0].n, "nnz": tot["nnz"], "models_per_dataset": 64,
-                   "iterations": iters, "storage": storage},
+        "config": {"workload": "logreg-regpath-16x500k-64lambda", "datasets": nd, "rows": m_tot,
+                   "rows_per_dataset": [sp.m for sp in specs], "cols": specs[0].n, "nnz": nnz,
+                   "models_per_dataset": k, "models": nd * k, "iterations": iters, "storage": storage,
+                   "launch": "one CUDA graph: all datasets stacked, line searches and stops decided on the device"},
+        "models_trained": int(rb["n_iter"].size), "model_iterations": int(rb["n_iter"].sum()),
+        "gpu_launches": launches,
         "fp64_single_model_gpu": {"value": base, "unit": "model-iters/s",
                                   "note": "plain FP64 path, one model per call; 4 of 64 values timed per dataset"},
         "speedup_vs_fp64_single": value / base,
         "loss_rel_diff_vs_fp64_single": {"max": max(loss_err), "median": statistics.median(loss_err)},
-        "kernels": {"ms": kms, "launches": tot["pass1_n"] + tot["pass2_n"],
-                    "achieved_gbs": tot["alg_bytes"] / (kms / 1e3) / 1e9 if kms else None, "hbm_peak_gbs": peak,
+        "eager_run_same_losses": bool(np.array_equal(rp["loss"], rb["loss"])),
+        "kernels": {"ms": kms, "evaluations": evals,
+                    "achieved_gbs": per_eval * evals / (kms / 1e3) / 1e9 if kms else None, "hbm_peak_gbs": peak,
                     "peak_kind": peak_kind,
-                    "achieved_tflops_fp32": tot["flops"] / (kms / 1e3) / 1e12 if kms else None,
-                    "pass1_ms": tot["pass1_ms"], "pass2_ms": tot["pass2_ms"],
-                    "lbfgs_vector_ms": tot.get("vec_ms")},
-        "wall_s": tot["batched_s"],
+                    "achieved_tflops_fp32": 4.0 * nnz * 64 * evals / (kms / 1e3) / 1e12 if kms else None,
+                    "pass1_ms": prof["pass1"][0], "pass2_ms": prof["pass2"][0], "lbfgs_vector_ms": vec_ms,
+                    "eager_wall_s": wall_eager},
+        "wall_s": wall,
     }
-    return line
 
 
 def run_regpath(args):
@@ -769,7 +782,8 @@ def main():
     ap.add_argument("--spmv-only", action="store_true", help="run only the SpMV kernel suite")
     ap.add_argument("--workload", default="lbfgs", choices=["lbfgs", "regpath", "multinomial"])
     ap.add_argument("--datasets", type=int, default=16, help="regpath: number of datasets")
-    ap.add_argument("--regpath-datasets", type=int, default=4, help="datasets of the batched summary line")
+    ap.add_argument("--regpath-datasets", type=int, default=16, help="datasets of the batched summary line")
+    ap.add_argument("--skip-mlr", action="store_true", help="leave out the multinomial L-BFGS summary")
     ap.add_argument("--skip-regpath", action="store_true")
     ap.add_argument("--skip-glm", action="store_true", help="skip the ridge / SVM summary")
     ap.add_argument("--panels", default="auto",

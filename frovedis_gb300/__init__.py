@@ -66,7 +66,7 @@ EXPORTS = [
     "fvg_matrix_load_binary", "fvg_glm_lbfgs", "fvg_glm_sgd", "fvg_glm_lbfgs_batched", "fvg_glm_eval",
     "fvg_logreg_shrink_sgd", "fvg_matrix_set_panels", "fvg_matrix_panel_info", "fvg_matrix_set_head",
     "fvg_matrix_head_info", "fvg_ctx_set_wait_limit", "fvg_debug_inject_alloc_failure", "fvg_matrix_autotune",
-    "fvg_multinomial_lbfgs",
+    "fvg_multinomial_lbfgs", "fvg_logreg_lbfgs_multi", "fvg_glm_lbfgs_multi",
 ]
 
 _lib = None
@@ -139,6 +139,8 @@ def load(build_if_needed: bool = True):
         "fvg_glm_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
                          C.POINTER(_dbl)], _int),
         "fvg_glm_lbfgs_batched": ([_p, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
+        "fvg_logreg_lbfgs_multi": ([_p, _i64, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
+        "fvg_glm_lbfgs_multi": ([_p, _i64, _p, _p, _p, C.POINTER(GlmParams), _i64, _p, _p, _p, _p, _p], _int),
         "fvg_logreg_shrink_sgd": ([_p, _p, _p, _p, C.POINTER(GlmParams), _p, C.POINTER(_dbl), C.POINTER(_i64),
                                    C.POINTER(_dbl)], _int),
         "fvg_glm_eval": ([_p, _p, _int, _int, _int, _dbl, _p, _p, _p, _dbl, _int, _p, C.POINTER(_dbl)], _int),
@@ -537,6 +539,51 @@ def logreg_lbfgs_batched(mat: Matrix, label, reg_params, sample_weight=None, w0=
     ctx.check(fn(ctx.h, mat.h, _ptr(label), _ptr(sw), C.byref(p), k, _ptr(lam), _ptr(w), _ptr(b), _ptr(n_iter),
                  _ptr(loss)))
     return dict(w=w, b=b, n_iter=n_iter, loss=loss)
+
+
+def logreg_lbfgs_multi(mats, labels, reg_params, sample_weights=None, w0=None, b0=None, _fn=None, **kw):
+    """The batched trainer over several datasets in one launch
+    (fvg_logreg_lbfgs_multi): the k models of every dataset, model (d, j) on
+    mats[d] with reg_param = reg_params[j].  w0[d]: (k, n_d) initial weights
+    of dataset d (default all 1), b0: (nd, k) initial intercepts.  Returns
+    w (a list of (k, n_d) arrays), b, n_iter, loss ((nd, k) arrays)."""
+    mats = list(mats)
+    nd = len(mats)
+    ctx = mats[0].ctx
+    lam = np.ascontiguousarray(reg_params, dtype=np.float64)
+    k = len(lam)
+    labs = [np.ascontiguousarray(l, dtype=np.float64) for l in labels]
+    sws = None if sample_weights is None else [
+        None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in sample_weights]
+    icpt = bool(kw.get("intercept", False))
+    ns = [m.n for m in mats]
+    wflat = np.empty(sum(k * n for n in ns))
+    o = 0
+    for d, n in enumerate(ns):
+        wd = np.ones((k, n)) if w0 is None else np.broadcast_to(np.asarray(w0[d], dtype=np.float64), (k, n))
+        wflat[o:o + k * n] = wd.reshape(-1)
+        o += k * n
+    b = (np.full((nd, k), 1.0 if icpt else 0.0) if b0 is None
+         else np.array(np.broadcast_to(b0, (nd, k)), dtype=np.float64, order="C"))
+    kw["intercept"] = int(icpt)
+    p = glm_params(**kw)
+    n_iter = np.zeros((nd, k), dtype=np.int64)
+    loss = np.zeros((nd, k))
+    mh = (_p * nd)(*[m.h for m in mats])
+    lh = (_p * nd)(*[_ptr(x) for x in labs])
+    sh = None if sws is None else (_p * nd)(*[_ptr(x) for x in sws])
+    fn = ctx.L.fvg_logreg_lbfgs_multi if _fn is None else _fn
+    ctx.check(fn(ctx.h, nd, mh, lh, sh, C.byref(p), k, _ptr(lam), _ptr(wflat), _ptr(b), _ptr(n_iter), _ptr(loss)))
+    w, o = [], 0
+    for n in ns:
+        w.append(wflat[o:o + k * n].reshape(k, n))
+        o += k * n
+    return dict(w=w, b=b, n_iter=n_iter, loss=loss)
+
+
+def glm_lbfgs_multi(mats, labels, reg_params, loss="linear", **kw):
+    """The multi-dataset batched trainer for any GLM loss (fvg_glm_lbfgs_multi)."""
+    return logreg_lbfgs_multi(mats, labels, reg_params, loss=loss, _fn=mats[0].ctx.L.fvg_glm_lbfgs_multi, **kw)
 
 
 def multinomial_lbfgs(mat: Matrix, label, nclasses, sample_weight=None, W0=None, trace=False, **kw):

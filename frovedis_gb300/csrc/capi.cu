@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "fvg_internal.cuh"
 
@@ -18,6 +19,9 @@ void logreg_eval(fvg_ctx* c, fvg_matrix* M, int fmt, int storage, const double* 
 void lbfgs_batched_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                          const fvg_glm_params* p, i64 k, const double* lam_h, double* w_h, double* b_h,
                          i64* n_iter_h, double* loss_h);
+void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const std::vector<const double*>& labels_h,
+                       const std::vector<const double*>& sws_h, const fvg_glm_params* p, i64 k, const double* lam_h,
+                       double* w_h, double* b_h, i64* n_iter_h, double* loss_h);
 void multinomial_lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
                              const fvg_glm_params* p, i64 K, double* w_h, i64* n_iter, double* loss_out);
 void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const double* sw_h,
@@ -830,6 +834,49 @@ FVG_API fvg_status fvg_glm_lbfgs_batched(fvg_ctx* c, fvg_matrix* M, const double
   API_BEGIN
   own(c, M);
   lbfgs_batched_train(c, M, label, sample_weight, p, k, reg_params, weight, intercept, n_iter, final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+static void multi_call(fvg_ctx* c, int64_t nd, fvg_matrix* const* mats, const double* const* labels,
+                       const double* const* sws, const fvg_glm_params* p, int64_t k, const double* reg_params,
+                       double* weight, double* intercept, int64_t* n_iter, double* final_loss) {
+  need(nd >= 1 && nd <= 65535, FVG_ERR_INVALID_ARG, "number of datasets must be in [1, 65535]");
+  need(mats != nullptr && labels != nullptr, FVG_ERR_INVALID_ARG, "null dataset arrays");
+  std::vector<fvg_matrix*> ms((size_t)nd);
+  std::vector<const double*> ls((size_t)nd), ws((size_t)nd, nullptr);
+  for (int64_t d = 0; d < nd; d++) {
+    need(mats[d] != nullptr, FVG_ERR_INVALID_ARG, "null matrix");
+    own(c, mats[d]);
+    ms[(size_t)d] = mats[d];
+    ls[(size_t)d] = labels[d];
+    if (sws) ws[(size_t)d] = sws[d];
+  }
+  lbfgs_multi_train(c, ms, ls, ws, p, k, reg_params, weight, intercept, n_iter, final_loss);
+}
+
+FVG_API fvg_status fvg_logreg_lbfgs_multi(fvg_ctx* c, int64_t num_datasets, fvg_matrix* const* mats,
+                                          const double* const* labels, const double* const* sample_weights,
+                                          const fvg_glm_params* p, int64_t k, const double* reg_params,
+                                          double* weight, double* intercept, int64_t* n_iter, double* final_loss) {
+  if (!c || !weight || !intercept || !n_iter || !final_loss || !reg_params) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  need(p != nullptr, FVG_ERR_INVALID_ARG, "null params");
+  const fvg_glm_params q = logistic_of(p);
+  multi_call(c, num_datasets, mats, labels, sample_weights, &q, k, reg_params, weight, intercept, n_iter,
+             final_loss);
+  check_device_error(c);
+  API_END(c)
+}
+
+FVG_API fvg_status fvg_glm_lbfgs_multi(fvg_ctx* c, int64_t num_datasets, fvg_matrix* const* mats,
+                                       const double* const* labels, const double* const* sample_weights,
+                                       const fvg_glm_params* p, int64_t k, const double* reg_params, double* weight,
+                                       double* intercept, int64_t* n_iter, double* final_loss) {
+  if (!c || !weight || !intercept || !n_iter || !final_loss || !reg_params) return FVG_ERR_INVALID_ARG;
+  API_BEGIN
+  multi_call(c, num_datasets, mats, labels, sample_weights, p, k, reg_params, weight, intercept, n_iter,
+             final_loss);
   check_device_error(c);
   API_END(c)
 }

@@ -332,11 +332,40 @@ void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k
 // column; ldx / ldy row strides); scratch of spmm_scratch_bytes().
 i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage);
 void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, int y_dt, void* Y, i64 ldy,
-                    void* scratch);
+                    void* scratch, const int* gate = nullptr);
 void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
                            const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
                            void* R, i64 ldr, double* out, double* gbias, void* scratch, int loss = 0,
                            double eps = 0.0);
+// Logistic forward pass over datasets stacked block-diagonally in one CRS
+// (rows of dataset d: [seg_row[d], seg_row[d+1])): per-dataset intercepts
+// (bias + d * ldb) and loss / bias sums, out[2 * (d * ldo + j)] and
+// out[2 * (d * ldo + j) + 1]; the bias sums also land in gb[grow[d] * ldg +
+// j] (crs_spmm_seg_finish).  W, R and their strides must be 16-byte aligned
+// with kb a multiple of 4.  The whole pass does nothing while *gate == 0
+// (gate may be null).
+struct SpmmSeg {
+  int nseg = 0;
+  const i32* seg_row = nullptr;  // device [nseg + 1]
+  i64 ldb = 0;
+  double* slots = nullptr;       // device scratch, spmm_seg_slot_bytes()
+  int kout = 0;                  // models of this block with results
+  double* out = nullptr;
+  i64 ldo = 0;
+  double* gb = nullptr;
+  const i64* grow = nullptr;     // device [nseg]
+  i64 ldg = 0;
+  const int* gate = nullptr;
+  // set by the pass for crs_spmm_seg_finish
+  i64 nw1 = 0, nw2 = 0;
+  int nc = 0, icpt = 0;
+};
+i64 spmm_seg_slot_bytes(fvg_ctx* c, int nseg, int kb);
+void crs_spmm_logreg_seg(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
+                         const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
+                         void* R, i64 ldr, void* scratch, SpmmSeg& sg, int loss = 0, double eps = 0.0);
+// The per-dataset sums of the pass (launch after the backward product).
+void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg);
 
 // Row-panel backward product (FP32/BF16 storage): builds the layout when the
 // matrix's column counts make it pay (or as forced); returns null when the

@@ -46,7 +46,19 @@ struct SpmmK {
   double* cta_part;  // logistic: [grid][64][2] loss, bias
   int loss;          // GLM loss kind of the per-model epilogue
   double eps;
+  // Stacked datasets (logistic epilogue): rows [seg_row[d], seg_row[d+1])
+  // belong to dataset d, whose intercepts sit at bias + d * ldb.  Every warp
+  // leaves one loss / bias partial per dataset in seg_part[d][warp] (zero
+  // for the datasets it saw no row of); nseg = 0: one dataset, per-CTA
+  // partials in cta_part.
+  const i32* seg_row;
+  int nseg;
+  i64 ldb;
+  double* seg_part;
+  const int* gate;  // the launch does nothing while *gate == 0 (null: always runs)
 };
+
+__device__ __forceinline__ bool gated_off(const int* gate) { return gate && __ldcg(gate) == 0; }
 
 // Lane layouts of the block's columns.  Strided (VEC = false): lane L owns
 // columns L, L+32, ...; every load is one element.  Packed (VEC = true):
@@ -250,6 +262,7 @@ template <class VT, class XT, class AT, class YT, int EPI, int CPL, bool VEC>
 __global__ void __launch_bounds__(kThreads, 4) k_spmm(const SpmmK p) {
   using Sum = typename SumOf<AT>::type;
   constexpr int NC = 32 * CPL;
+  if (gated_off(p.gate)) return;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const i64 gw = (i64)blockIdx.x * (kThreads / 32) + wib;
@@ -304,6 +317,56 @@ struct SpmmFin {
   double* out;       // [kb][2]: loss, bias
   double* gbias;     // [kb] or null: where each column's bias lands
   unsigned* ticket;
+  double* seg_fpart;  // stacked datasets: [nseg][warps][NC][2] of this kernel
+};
+
+// ------------------------------------------------ stacked-dataset partials
+// A warp meets its rows in increasing order, so the datasets it visits come
+// in order too: SegWalk keeps the current one, and when a row of a later
+// dataset arrives it stores the warp's loss / bias sums of the current one
+// in its slot, zeros in the slots of the datasets skipped, and loads the
+// next dataset's intercepts.  finish() stores the last sums and zeros the
+// remaining slots: every warp writes each of its nseg slots exactly once, so
+// the reduction reads all of them in warp order without a memset.
+template <class AT, int QN> struct SegWalk {
+  using Sum = typename SumOf<AT>::type;
+  int d = 0;
+  i32 end = 0;
+  double* slots;  // this warp's slot of dataset 0; slot d at + d * stride
+  i64 stride;
+  __device__ __forceinline__ SegWalk(const SpmmK& p, double* base, i64 warp, i64 nwarps, int nc)
+      : end(p.nseg > 0 ? __ldg(p.seg_row + 1) : 0), slots(base + warp * nc * 2), stride(nwarps * nc * 2) {}
+  __device__ __forceinline__ void put(int dd, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
+    double* s = slots + dd * stride;
+#pragma unroll
+    for (int q = 0; q < QN; q++) {
+      s[2 * col[q]] = ls[q].total();
+      s[2 * col[q] + 1] = bs[q].total();
+      ls[q] = Sum();
+      bs[q] = Sum();
+    }
+  }
+  __device__ __forceinline__ void zero(int dd, const int (&col)[QN]) {
+    double* s = slots + dd * stride;
+#pragma unroll
+    for (int q = 0; q < QN; q++) {
+      s[2 * col[q]] = 0.0;
+      s[2 * col[q] + 1] = 0.0;
+    }
+  }
+  // row r (warp-uniform) is next; true when the dataset changed
+  __device__ __forceinline__ bool to_row(const SpmmK& p, i32 r, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
+    if (r < end) return false;
+    put(d, col, ls, bs);
+    d++;
+    while (r >= __ldg(p.seg_row + d + 1)) zero(d++, col);
+    end = __ldg(p.seg_row + d + 1);
+    return true;
+  }
+  __device__ __forceinline__ void finish(const SpmmK& p, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
+    put(d, col, ls, bs);
+    for (int dd = d + 1; dd < p.nseg; dd++) zero(dd, col);
+  }
 };
 
 // Long rows (a warp each): add the pieces' partials in piece order, apply the
@@ -314,17 +377,29 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
   using Sum = typename SumOf<AT>::type;
   constexpr int NC = 32 * CPL;
   const SpmmK& p = f.k;
+  if (gated_off(p.gate)) return;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
+  const bool seg = EPI == EPI_LOGREG && p.nseg > 0;
   AT b[CPL];
+  auto load_bias = [&](const double* bias) {
 #pragma unroll
-  for (int q = 0; q < CPL; q++) {
-    const int c = colof<VEC, CPL>(lane, q);
-    b[q] = (EPI != EPI_STORE && p.icpt && c < p.kb) ? (AT)p.bias[c] : (AT)0;
-  }
+    for (int q = 0; q < CPL; q++) {
+      const int c = colof<VEC, CPL>(lane, q);
+      b[q] = (EPI != EPI_STORE && p.icpt && c < p.kb) ? (AT)bias[c] : (AT)0;
+    }
+  };
+  load_bias(p.bias);
   Sum ls[CPL], bs[CPL];
-  for (i64 i = (i64)blockIdx.x * (kThreads / 32) + wib; i < f.nlong; i += (i64)gridDim.x * (kThreads / 32)) {
+  int cols[CPL];
+#pragma unroll
+  for (int q = 0; q < CPL; q++) cols[q] = colof<VEC, CPL>(lane, q);
+  const i64 gw = (i64)blockIdx.x * (kThreads / 32) + wib, nw = (i64)gridDim.x * (kThreads / 32);
+  SegWalk<AT, CPL> sw(p, f.seg_fpart, gw, nw, NC);
+  for (i64 i = gw; i < f.nlong; i += nw) {
     const i64 q0 = f.long_piece0[i], q1 = f.long_piece0[i + 1];
+    const i32 row = f.long_rows[i];
+    if (seg && sw.to_row(p, row, cols, ls, bs)) load_bias(p.bias + sw.d * p.ldb);
     AT a[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; q++) a[q] = 0;
@@ -333,7 +408,11 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 #pragma unroll
       for (int q = 0; q < CPL; q++) a[q] += part[colof<VEC, CPL>(lane, q)];
     }
-    spmm_epi<AT, YT, EPI, CPL, VEC>(p, f.long_rows[i], a, b, lane, ls, bs);
+    spmm_epi<AT, YT, EPI, CPL, VEC>(p, row, a, b, lane, ls, bs);
+  }
+  if (seg) {
+    sw.finish(p, cols, ls, bs);
+    return;
   }
   if constexpr (EPI == EPI_LOGREG || EPI == EPI_SOFTMAX) if (EPI == EPI_LOGREG || p.cta_part) {
     __shared__ double red[kThreads / 32][NC][2];
@@ -396,6 +475,198 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
     }
     if (threadIdx.x == 0) *f.ticket = 0u;
     }
+  }
+}
+
+// ------------------------------------------------ grouped lane layout
+// For the store and logistic epilogues with 16-byte aligned rows of X: lane
+// (group g, sub-lane s) of G groups of LPR = 32 / G lanes reads columns
+// s*CPL .. s*CPL+CPL-1 of a row of X with one 16-byte load (CPL = 4 FP32 or
+// 2 FP64 values), and group g takes nonzeros g, g+G, g+2G, ... of every
+// 32-entry chunk, so a warp gathers G rows of X per step.  At the end of a
+// row the groups' sums meet in a fixed butterfly that leaves lane (g, s)
+// with the QG = CPL / G columns s*CPL + g*QG ... of the row (reduce-scatter),
+// which it runs the epilogue on.  A launch covers NC = LPR * CPL columns;
+// pieces and the per-CTA partials use the column order of the finalize
+// kernel with NC / 32 columns a lane.  Each column's sum is the group sums
+// added in the butterfly's fixed order (deterministic; it differs from the
+// one-nonzero-at-a-time order only by rounding).
+template <class XT, int G> struct GLay {
+  static constexpr int CPL = 16 / (int)sizeof(XT);
+  static constexpr int LPR = 32 / G;
+  static constexpr int NC = LPR * CPL;
+  static constexpr int QG = CPL / G;
+  static_assert(G >= 1 && G <= CPL, "groups per warp");
+};
+
+template <class VT, class XT, class AT, int G>
+__device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[GLay<XT, G>::CPL]) {
+  using L = GLay<XT, G>;
+  constexpr int CPL = L::CPL;
+  const int sub = lane % L::LPR, grp = lane / L::LPR;
+  const XT* X = (const XT*)p.X + sub * CPL;
+  const VT* val = (const VT*)p.val;
+  const bool mine = sub * CPL < p.kb;
+#pragma unroll
+  for (int q = 0; q < CPL; q++) a[q] = 0;
+  for (i32 e = e0; e < e1; e += 32) {
+    const int cnt = min(32, e1 - e);
+    i32 mi = 0;
+    AT mv = 0;
+    if (lane < cnt) {
+      mi = __ldcs(p.idx + e + lane);
+      mv = ld_val<VT, AT>(val + e + lane);
+    }
+#pragma unroll 4
+    for (int t = 0; t < cnt; t += G) {
+      const int src = t + grp;
+      const i32 col = __shfl_sync(0xffffffffu, mi, src & 31);
+      const AT v = __shfl_sync(0xffffffffu, mv, src & 31);
+      if (mine && src < cnt) {
+        XT x[CPL];
+        VecLd<XT, CPL>::ld(X + (i64)col * p.ldx, x);
+#pragma unroll
+        for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
+      }
+    }
+  }
+  // reduce-scatter over the groups: at offset o the lane keeps the half of
+  // its columns picked by bit o of its lane id and sends the other half
+#pragma unroll
+  for (int o = 16, h = CPL / 2; o >= L::LPR; o >>= 1, h >>= 1) {
+    const bool hi = (lane & o) != 0;
+#pragma unroll
+    for (int q = 0; q < h; q++) {
+      const AT keep = hi ? a[h + q] : a[q];
+      const AT send = hi ? a[q] : a[h + q];
+      a[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+}
+
+template <class VT, class XT, class AT, class YT, int EPI, int G>
+__global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
+  using L = GLay<XT, G>;
+  using Sum = typename SumOf<AT>::type;
+  constexpr int CPL = L::CPL, NC = L::NC, QG = L::QG;
+  if (gated_off(p.gate)) return;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int c0 = (lane % L::LPR) * CPL + (lane / L::LPR) * QG;  // first of the lane's epilogue columns
+  const i64 gw = (i64)blockIdx.x * (kThreads / 32) + wib;
+  const i64 nw = (i64)gridDim.x * (kThreads / 32);
+  const bool seg = EPI == EPI_LOGREG && p.nseg > 0;
+  int cols[QG];
+#pragma unroll
+  for (int q = 0; q < QG; q++) cols[q] = c0 + q;
+  AT b[QG];
+  auto load_bias = [&](const double* bias) {
+#pragma unroll
+    for (int q = 0; q < QG; q++) b[q] = (EPI == EPI_LOGREG && p.icpt && cols[q] < p.kb) ? (AT)bias[cols[q]] : (AT)0;
+  };
+  load_bias(p.bias);
+  Sum ls[QG], bs[QG];
+  SegWalk<AT, QG> walk(p, p.seg_part, gw, nw, NC);
+  AT lab = 0, w = 1;
+  for (i64 it = gw; it < p.nitems; it += nw) {
+    const Item item = p.items[it];
+    AT a[CPL];
+    if (item.r1 < 0) {  // piece of a long row
+      row_dot_g<VT, XT, AT, G>(p, item.e0, item.e1, lane, a);
+      AT* part = (AT*)p.partials + (i64)(-1 - item.r1) * NC;
+#pragma unroll
+      for (int q = 0; q < QG; q++) part[cols[q]] = a[q];
+      continue;
+    }
+    for (i32 r = item.r0; r < item.r1; r++) {
+      if (seg && walk.to_row(p, r, cols, ls, bs)) load_bias(p.bias + walk.d * p.ldb);
+      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a);
+      if constexpr (EPI == EPI_STORE) {
+        YT* y = (YT*)p.Y + (i64)r * p.ldy;
+#pragma unroll
+        for (int q = 0; q < QG; q++)
+          if (cols[q] < p.kb) y[cols[q]] = (YT)a[q];
+      } else {
+        bool has_sw;
+        if constexpr (sizeof(AT) == 8) {
+          lab = p.label[r];
+          has_sw = p.sw != nullptr;
+          if (has_sw) w = p.sw[r];
+        } else {
+          lab = p.label_f[r];
+          has_sw = p.sw_f != nullptr;
+          if (has_sw) w = p.sw_f[r];
+        }
+        AT* rr = (AT*)p.R + (i64)r * p.ldr;
+#pragma unroll
+        for (int q = 0; q < QG; q++) {
+          if (cols[q] >= p.kb) continue;
+          AT loss, d;
+          glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
+          if (has_sw) d = d * w;
+          rr[cols[q]] = d;
+          ls[q].add(loss);
+          bs[q].add(d);
+        }
+      }
+    }
+  }
+  if constexpr (EPI == EPI_LOGREG) {
+    if (seg) {
+      walk.finish(p, cols, ls, bs);
+      return;
+    }
+    __shared__ double red[kThreads / 32][NC][2];
+#pragma unroll
+    for (int q = 0; q < QG; q++) {
+      red[wib][cols[q]][0] = ls[q].total();
+      red[wib][cols[q]][1] = bs[q].total();
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * NC) {
+      const int col = threadIdx.x % NC, qq = threadIdx.x / NC;
+      double t = 0;
+#pragma unroll
+      for (int w8 = 0; w8 < kThreads / 32; w8++) t += red[w8][col][qq];
+      p.cta_part[((i64)blockIdx.x * NC + col) * 2 + qq] = t;
+    }
+  }
+}
+
+// Stacked datasets: loss / bias sums of dataset blockIdx.x from the warp
+// slots of the main kernel (nw1 warps) and the finalize kernel (nw2), each
+// in warp order: 1024 threads = (column, quantity) pairs x stripes, stripe
+// s adds warps s, s + S, ...; the stripes are added in order.  out[2 * (d *
+// ldo + col) + q]; the bias sums also go to gb[grow[d] * ldg + col].
+template <int NC>
+__global__ void __launch_bounds__(1024) k_spmm_seg_reduce(const double* __restrict__ s1, i64 nw1,
+                                                          const double* __restrict__ s2, i64 nw2, int kout, int icpt,
+                                                          double* __restrict__ out, i64 ldo, double* __restrict__ gb,
+                                                          const i64* __restrict__ grow, i64 ldg, const int* gate) {
+  constexpr int P = 2 * NC, S = 1024 / P;
+  static_assert(1024 % P == 0, "pairs per CTA");
+  __shared__ double part[S][P];
+  if (gated_off(gate)) return;
+  const int d = blockIdx.x;
+  const int pr = threadIdx.x % P, st = threadIdx.x / P;
+  CSum t;
+  const double* b1 = s1 + (i64)d * nw1 * P;
+  for (i64 w = st; w < nw1; w += S) t.add(__ldcg(b1 + w * P + pr));
+  const double* b2 = s2 + (i64)d * nw2 * P;
+  for (i64 w = st; w < nw2; w += S) t.add(__ldcg(b2 + w * P + pr));
+  part[st][pr] = t.total();
+  __syncthreads();
+  if (st != 0) return;
+  double tot = 0.0;
+#pragma unroll
+  for (int q = 0; q < S; q++) tot += part[q][pr];
+  const int col = pr >> 1, qq = pr & 1;
+  if (col >= kout) return;
+  if (qq == 0) {
+    out[2 * ((i64)d * ldo + col)] = tot;
+  } else {
+    out[2 * ((i64)d * ldo + col) + 1] = icpt ? tot : 0.0;
+    if (gb) gb[grow[d] * ldg + col] = icpt ? tot : 0.0;
   }
 }
 
@@ -464,6 +735,94 @@ static void launch_spmm_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, Sp
 
 static bool aligned_to(const void* ptr, size_t b) { return ((uintptr_t)ptr % b) == 0; }
 
+// Grouped layout launch: k_spmm_g and its finalize kernel (NC / 32
+// columns a lane); for stacked datasets the slot reduction is left to
+// crs_spmm_seg_finish.
+template <class VT, class XT, class AT, class YT, int EPI, int G>
+static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, SpmmK p, double* out,
+                             double* gbias, char* scratch, SpmmSeg* sg) {
+  using L = GLay<XT, G>;
+  constexpr int NC = L::NC, CF = NC / 32;
+  const int grid = (int)std::max<i64>(
+      1, std::min<i64>(occupancy_blocks((const void*)k_spmm_g<VT, XT, AT, YT, EPI, G>, kThreads) * c->num_sms,
+                       (s.nitems + 7) / 8));
+  const int fg = spmm_fin_grid(c, s.nlong);
+  unsigned* ticket = (unsigned*)scratch;
+  double* cta = (double*)(scratch + al256(256));
+  double* fin = (double*)((char*)cta + al256(sizeof(double) * 2 * kSpmmMaxCols * 8 * (i64)c->num_sms));
+  p.partials = (char*)fin + al256(sizeof(double) * 2 * kSpmmMaxCols * fg);
+  p.off = a.off.as<i32>();
+  p.idx = a.idx.as<i32>();
+  p.val = a.val[storage].p;
+  p.items = s.items.as<Item>();
+  p.nitems = s.nitems;
+  p.cta_part = EPI == EPI_LOGREG ? cta : nullptr;
+  const bool seg = EPI == EPI_LOGREG && sg && sg->nseg > 0;
+  const i64 nw1 = (i64)grid * (kThreads / 32), nw2 = (i64)fg * (kThreads / 32);
+  if (seg) {
+    if (!sg->seg_row || !sg->slots || sg->nseg > 65535) fail(FVG_ERR_INTERNAL, "stacked-dataset pass without slots");
+    p.nseg = sg->nseg;
+    p.seg_row = sg->seg_row;
+    p.ldb = sg->ldb;
+    p.seg_part = sg->slots;
+    p.gate = sg->gate;
+  }
+  if (s.nitems > 0 || seg) {
+    k_spmm_g<VT, XT, AT, YT, EPI, G><<<grid, kThreads, 0, c->stream>>>(p);
+    check_launch("k_spmm_g");
+    count_launch(c);
+  }
+  if (s.nlong > 0 || EPI == EPI_LOGREG) {
+    SpmmFin f;
+    f.k = p;
+    f.long_rows = s.long_rows.as<i32>();
+    f.long_piece0 = s.long_piece0.as<i32>();
+    f.nlong = s.nlong;
+    f.ncta = s.nitems > 0 ? grid : 0;
+    f.fin_part = fin;
+    f.out = out;
+    f.gbias = gbias;
+    f.ticket = ticket;
+    f.seg_fpart = seg ? sg->slots + (i64)sg->nseg * nw1 * NC * 2 : nullptr;
+    k_spmm_fin<AT, YT, EPI, CF, true><<<fg, kThreads, 0, c->stream>>>(f);
+    check_launch("k_spmm_fin");
+    count_launch(c);
+  }
+  if (seg) {
+    sg->nw1 = nw1;
+    sg->nw2 = nw2;
+    sg->nc = NC;
+    sg->icpt = p.icpt;
+  }
+}
+
+// Grouped layout when its 16-byte accesses are aligned; false: not taken.
+template <class VT, class XT, class AT, class YT, int EPI>
+static bool launch_grouped(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const SpmmK& p, double* out,
+                           double* gbias, char* scratch, SpmmSeg* sg = nullptr) {
+  constexpr int CPL = 16 / (int)sizeof(XT);
+  bool ok = p.kb % CPL == 0 && p.kb <= 32 * CPL && p.ldx % CPL == 0 && aligned_to(p.X, 16);
+  if (EPI == EPI_STORE) ok = ok && p.ldy % CPL == 0 && aligned_to(p.Y, 16);
+  else ok = ok && p.ldr % CPL == 0 && aligned_to(p.R, 16);
+  if (!ok) return false;
+  if constexpr (CPL >= 4) {
+    if (p.kb <= 8 * CPL) {
+      launch_grouped_l<VT, XT, AT, YT, EPI, 4>(c, a, s, storage, p, out, gbias, scratch, sg);
+      return true;
+    }
+  }
+  if (p.kb <= 16 * CPL) {
+    launch_grouped_l<VT, XT, AT, YT, EPI, 2>(c, a, s, storage, p, out, gbias, scratch, sg);
+    return true;
+  }
+  // the logistic epilogue's finalize reduction takes at most 64 columns
+  if constexpr (EPI != EPI_LOGREG || 32 * CPL <= 64) {
+    launch_grouped_l<VT, XT, AT, YT, EPI, 1>(c, a, s, storage, p, out, gbias, scratch, sg);
+    return true;
+  }
+  return false;
+}
+
 // Packed lane layout when every access it makes is aligned: the block's
 // width and the strides of X and of the output are multiples of CPL and the
 // bases are aligned to CPL elements.
@@ -491,7 +850,7 @@ static void launch_store(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, con
 
 // Y[:, c0:c0+kb] = A X[:, c0:c0+kb] (X, Y pointers already offset to c0).
 void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, int y_dt, void* Y, i64 ldy,
-                    void* scratch) {
+                    void* scratch, const int* gate) {
   if (kb < 1 || kb > kSpmmMaxCols) fail(FVG_ERR_INTERNAL, "spmm block width out of range");
   if (!a.val[storage].p) fail(FVG_ERR_INTERNAL, "missing value plane for the requested storage");
   const Sched& s = crs_sched(c, a, tile_for_storage(storage));
@@ -501,16 +860,25 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
   p.kb = kb;
   p.Y = Y;
   p.ldy = ldy;
+  p.gate = gate;
   char* sc = (char*)scratch;
-  FVG_CUDA(cudaMemsetAsync(sc, 0, 256, c->stream));
   if (storage == FVG_F64) {
-    launch_store<double, double, double, double>(c, a, s, storage, p, sc);
+    if (!launch_grouped<double, double, double, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc))
+      launch_store<double, double, double, double>(c, a, s, storage, p, sc);
   } else if (storage == FVG_F32) {
-    if (y_dt == FVG_F64) launch_store<float, float, float, double>(c, a, s, storage, p, sc);
-    else launch_store<float, float, float, float>(c, a, s, storage, p, sc);
+    if (y_dt == FVG_F64) {
+      if (!launch_grouped<float, float, float, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc))
+        launch_store<float, float, float, double>(c, a, s, storage, p, sc);
+    } else if (!launch_grouped<float, float, float, float, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc)) {
+      launch_store<float, float, float, float>(c, a, s, storage, p, sc);
+    }
   } else {
-    if (y_dt == FVG_F64) launch_store<bf16, float, float, double>(c, a, s, storage, p, sc);
-    else launch_store<bf16, float, float, float>(c, a, s, storage, p, sc);
+    if (y_dt == FVG_F64) {
+      if (!launch_grouped<bf16, float, float, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc))
+        launch_store<bf16, float, float, double>(c, a, s, storage, p, sc);
+    } else if (!launch_grouped<bf16, float, float, float, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc)) {
+      launch_store<bf16, float, float, float>(c, a, s, storage, p, sc);
+    }
   }
 }
 
@@ -539,12 +907,71 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
   p.eps = eps;
   char* sc = (char*)scratch;
   FVG_CUDA(cudaMemsetAsync(sc, 0, 256, c->stream));
-  if (storage == FVG_F64)
-    launch_spmm<double, double, double, double, EPI_LOGREG, 2>(c, a, s, storage, p, out, gbias, sc);
-  else if (storage == FVG_F32)
-    launch_spmm<float, float, float, float, EPI_LOGREG, 2>(c, a, s, storage, p, out, gbias, sc);
-  else
+  if (storage == FVG_F64) {
+    if (!launch_grouped<double, double, double, double, EPI_LOGREG>(c, a, s, storage, p, out, gbias, sc))
+      launch_spmm<double, double, double, double, EPI_LOGREG, 2>(c, a, s, storage, p, out, gbias, sc);
+  } else if (storage == FVG_F32) {
+    if (!launch_grouped<float, float, float, float, EPI_LOGREG>(c, a, s, storage, p, out, gbias, sc))
+      launch_spmm<float, float, float, float, EPI_LOGREG, 2>(c, a, s, storage, p, out, gbias, sc);
+  } else if (!launch_grouped<bf16, float, float, float, EPI_LOGREG>(c, a, s, storage, p, out, gbias, sc)) {
     launch_spmm<bf16, float, float, float, EPI_LOGREG, 2>(c, a, s, storage, p, out, gbias, sc);
+  }
+}
+
+// Warp slots of a stacked-dataset pass: main kernel (at most 8 CTAs an SM)
+// and finalize kernel, NC = the launch's columns, two doubles each.
+i64 spmm_seg_slot_bytes(fvg_ctx* c, int nseg, int kb) {
+  const i64 nc = kb <= 32 ? 32 : (kb <= 64 ? 64 : 128);
+  const i64 warps = (8 * (i64)c->num_sms + 2 * (i64)c->num_sms) * (kThreads / 32);
+  return (i64)std::max(nseg, 1) * warps * nc * 2 * (i64)sizeof(double);
+}
+
+void crs_spmm_logreg_seg(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
+                         const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
+                         void* R, i64 ldr, void* scratch, SpmmSeg& sg, int loss, double eps) {
+  if (kb < 1 || kb > 64 || sg.nseg < 1) fail(FVG_ERR_INTERNAL, "stacked pass: block width or datasets out of range");
+  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
+  SpmmK p = {};
+  p.X = W;
+  p.ldx = ldw;
+  p.kb = kb;
+  p.label = label;
+  p.sw = sw;
+  p.label_f = label_f;
+  p.sw_f = sw_f;
+  p.icpt = icpt;
+  p.bias = bias;
+  p.R = R;
+  p.ldr = ldr;
+  p.loss = loss;
+  p.eps = eps;
+  char* sc = (char*)scratch;
+  bool ok;
+  if (storage == FVG_F64)
+    ok = launch_grouped<double, double, double, double, EPI_LOGREG>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  else if (storage == FVG_F32)
+    ok = launch_grouped<float, float, float, float, EPI_LOGREG>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  else
+    ok = launch_grouped<bf16, float, float, float, EPI_LOGREG>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  if (!ok) fail(FVG_ERR_INTERNAL, "stacked pass needs 16-byte aligned rows");
+}
+
+// Per-dataset loss / bias sums of the last crs_spmm_logreg_seg pass (after
+// the backward product, which writes the bias rows of the gradient as 0).
+void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg) {
+  if (sg.nw1 <= 0) fail(FVG_ERR_INTERNAL, "stacked-dataset reduction without its pass");
+  const double* s2 = sg.slots + (i64)sg.nseg * sg.nw1 * sg.nc * 2;
+  if (sg.nc == 32)
+    k_spmm_seg_reduce<32><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+  else if (sg.nc == 64)
+    k_spmm_seg_reduce<64><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+  else
+    k_spmm_seg_reduce<128><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+                                                            sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+  check_launch("k_spmm_seg_reduce");
+  count_launch(c);
 }
 
 // Multinomial forward pass, K <= 128 classes: P = (softmax(A W + icpt) -

@@ -325,6 +325,26 @@ FVG_API fvg_status fvg_logreg_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const
                                             const double* sample_weight, const fvg_glm_params* params, int64_t k,
                                             const double* reg_params, double* weight, double* intercept,
                                             int64_t* n_iter, double* final_loss);
+/* The batched trainer over several datasets at once: the k models of every
+ * dataset (num_datasets x k in all, model (d, j) on mats[d] with regParam =
+ * reg_params[j]) train together, the datasets' matrices stacked
+ * block-diagonally so that one forward and one backward product per
+ * evaluation serve all of them.  Each model takes its own line-search
+ * decisions and stops on its own, so its result is that of a separate
+ * fvg_logreg_lbfgs run on its dataset up to summation order.  The whole
+ * training is one CUDA-graph launch (the line-search and stop decisions are
+ * taken on the device).  labels[d] / sample_weights[d] (the array or any
+ * entry may be NULL = all ones) have mats[d]'s num_row entries;
+ * weight: dataset d's models follow those of datasets 0..d-1, model j at
+ * offset j*num_col(d) inside them; intercept, n_iter, final_loss:
+ * [num_datasets][k].  The stacked matrices must stay below 2^31 rows,
+ * columns (sum of num_col + 1) and nonzeros; 1 <= k <= 256.  No counterpart
+ * in the reference, which trains one model per train() call
+ * (logistic_regression_with_lbfgs.hpp:395-437). */
+FVG_API fvg_status fvg_logreg_lbfgs_multi(fvg_ctx* ctx, int64_t num_datasets, fvg_matrix* const* mats,
+                                          const double* const* labels, const double* const* sample_weights,
+                                          const fvg_glm_params* params, int64_t k, const double* reg_params,
+                                          double* weight, double* intercept, int64_t* n_iter, double* final_loss);
 /* multinomial_logistic_regression::train main API
  * (ml/glm/multinomial_logistic_regression.hpp:342-378 → softmax_parallelizer::
  * parallelize / do_train, softmax_parallelizer.hpp:210-242, 277-345):
@@ -408,6 +428,10 @@ FVG_API fvg_status fvg_glm_lbfgs_batched(fvg_ctx* ctx, fvg_matrix* mat, const do
                                          const double* sample_weight, const fvg_glm_params* params, int64_t k,
                                          const double* reg_params, double* weight, double* intercept,
                                          int64_t* n_iter, double* final_loss);
+FVG_API fvg_status fvg_glm_lbfgs_multi(fvg_ctx* ctx, int64_t num_datasets, fvg_matrix* const* mats,
+                                       const double* const* labels, const double* const* sample_weights,
+                                       const fvg_glm_params* params, int64_t k, const double* reg_params,
+                                       double* weight, double* intercept, int64_t* n_iter, double* final_loss);
 /* One loss/gradient evaluation for any fvg_loss (compute_gradient with the
  * kind's compute_dloss, gradient.hpp). */
 FVG_API fvg_status fvg_glm_eval(fvg_ctx* ctx, fvg_matrix* mat, fvg_format fmt, fvg_dtype storage, int32_t loss,
