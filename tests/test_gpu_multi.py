@@ -95,7 +95,7 @@ def test_multi_sample_weights_initial_models_and_early_stop(ctx):
     lams = list(np.logspace(-4, 0, 5))
     w0 = [rng.standard_normal((len(lams), a.n)) * 0.01 for a, _ in data]
     b0 = rng.standard_normal((2, len(lams))) * 0.1
-    kw = dict(num_iter=40, reg_type="L2", intercept=True, tol=1e-3)
+    kw = dict(num_iter=40, reg_type="L2", intercept=True, tol=3e-2)
     r = fv.logreg_lbfgs_multi(mats, [l for _, l in data], lams, sample_weights=sws, w0=w0, b0=b0, **kw)
     stopped = 0
     for d, (a, label) in enumerate(data):
