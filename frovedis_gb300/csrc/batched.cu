@@ -90,7 +90,35 @@ struct BArgs {
   ColState* st;      // [nd][ld]
   const int* ctl;
   int gate;          // control word gating the launch (< 0: none)
+  const unsigned long long* mask;  // [nd][nwd] models the launch serves (null: all)
+  int nwd;
 };
+
+__device__ __forceinline__ bool model_on(const BArgs& a, int ds, int j) {
+  if (!a.mask) return true;
+  return (__ldcg(a.mask + (i64)ds * a.nwd + (j >> 6)) >> (j & 63)) & 1ull;
+}
+__device__ __forceinline__ bool dataset_on(const BArgs& a, int ds) {
+  if (!a.mask) return true;
+  unsigned long long any = 0;
+  for (int w = 0; w < a.nwd; w++) any |= __ldcg(a.mask + (i64)ds * a.nwd + w);
+  return any != 0;
+}
+
+// model masks of nd datasets from the state flag picked by `field`
+// (0: searching, 1: active), a 64-bit word per 64 models
+__device__ __forceinline__ void build_masks(const ColState* st, int nd, int ld, int nwd, int field,
+                                            unsigned long long* out) {
+  for (int w = threadIdx.x; w < nd * nwd; w += blockDim.x) {
+    const int d = w / nwd, j0 = (w % nwd) * 64;
+    unsigned long long m = 0;
+    for (int b = 0; b < 64 && j0 + b < ld; b++) {
+      const ColState& s = st[(i64)d * ld + j0 + b];
+      if (field == 0 ? s.searching : s.active) m |= 1ull << b;
+    }
+    out[w] = m;
+  }
+}
 
 // Fixed-order reduction of NV values per column; fin(j, totals) runs once
 // per column in the dataset's last CTA.
@@ -391,14 +419,19 @@ __global__ void __launch_bounds__(kBT, 4) kb_trial(int t, const double* __restri
   if (r0 == 0) B1[mj] = __dadd_rn(B0[mj], __dmul_rn(f, s.bstep));
 }
 
+// (a.mask: only the models evaluated last; the others keep their norms)
 __global__ void __launch_bounds__(kBT, 4) kb_gmax(const double* __restrict__ G, BArgs a) {
   BCOL;
+  if (!dataset_on(a, ds)) return;
+  const bool use = on && model_on(a, ds, j);
   double v[1] = {0.0};
-  if (on)
+  if (use)
     rows_grouped<kRowGroup>(r0, rstep, n1, [&](i64 r) { return G[e0 + r * ld]; },
                             [&](i64, double x) { v[0] = fmax(v[0], fabs(x)); });
   const bool mx[1] = {true};
-  col_reduce<1>(v, mx, a, [&](int c, double* t) { a.st[ds * ld + c].gmax_t = t[0]; });
+  col_reduce<1>(v, mx, a, [&](int c, double* t) {
+    if (model_on(a, ds, c)) a.st[ds * ld + c].gmax_t = t[0];
+  });
 }
 
 // gradient norm and rms; `accepted`: the evaluation is of the accepted
@@ -406,10 +439,12 @@ __global__ void __launch_bounds__(kBT, 4) kb_gmax(const double* __restrict__ G, 
 __global__ void __launch_bounds__(kBT, 4) kb_gnorm(const double* __restrict__ G, const double* __restrict__ EV,
                                                 int accepted, BArgs a) {
   BCOL;
-  const double mxv = on ? a.st[mj].gmax_t : 0.0;
+  if (!dataset_on(a, ds)) return;
+  const bool use = on && model_on(a, ds, j);
+  const double mxv = use ? a.st[mj].gmax_t : 0.0;
   const double inv = mxv == 0 ? 0.0 : 1.0 / mxv;
   double v[1] = {0.0};
-  if (on)
+  if (use)
     rows_grouped<kRowGroup>(r0, rstep, n1, [&](i64 r) { return G[e0 + r * ld]; },
                             [&](i64, double x) {
                               const double t = x * inv;
@@ -417,6 +452,7 @@ __global__ void __launch_bounds__(kBT, 4) kb_gnorm(const double* __restrict__ G,
                             });
   const bool mx[1] = {false};
   col_reduce<1>(v, mx, a, [&](int c, double* t) {
+    if (!model_on(a, ds, c)) return;
     const i64 mc = ds * ld + c;
     ColState& s = a.st[mc];
     const double m = s.gmax_t;
@@ -449,9 +485,11 @@ __device__ __forceinline__ void count_into(int n, int* ctl, int w) {
 
 // accept decision of trial t (LBFGS_SEARCH_TOL, lbfgs_parallelizer.hpp:
 // 155, 329; the 10th trial is taken whatever its loss)
-__global__ void __launch_bounds__(kBT, 4) kb_decide(int t, const double* __restrict__ EV, int nm, ColState* st,
-                                                 int* ctl) {
+// (the models still searching: their masks in smask)
+__global__ void __launch_bounds__(kBT, 4) kb_decide(int t, const double* __restrict__ EV, int nd, int ld, int nwd,
+                                                 ColState* st, int* ctl, unsigned long long* smask) {
   if (ctl[C_TRIAL] == 0) return;
+  const int nm = nd * ld;
   int n = 0;
   for (int j = threadIdx.x; j < nm; j += kBT) {
     ColState& s = st[j];
@@ -464,15 +502,21 @@ __global__ void __launch_bounds__(kBT, 4) kb_decide(int t, const double* __restr
     }
   }
   count_into(n, ctl, C_SEARCH);
+  __syncthreads();
+  build_masks(st, nd, ld, nwd, 0, smask);
 }
 
-__global__ void __launch_bounds__(kBT, 4) kb_begin_search(int nm, ColState* st, int* ctl) {
+__global__ void __launch_bounds__(kBT, 4) kb_begin_search(int nd, int ld, int nwd, ColState* st, int* ctl,
+                                                       unsigned long long* smask) {
+  const int nm = nd * ld;
   int n = 0;
   for (int j = threadIdx.x; j < nm; j += kBT) {
     st[j].searching = st[j].active;
     n += st[j].active;
   }
   count_into(n, ctl, C_SEARCH);
+  __syncthreads();
+  build_masks(st, nd, ld, nwd, 0, smask);
 }
 
 // accept + history push (see k_accept); convergence: rms <= tol stops the model
@@ -531,7 +575,9 @@ __global__ void __launch_bounds__(kBT, 4) kb_accept(int nf, int it, double tol, 
 // every active model's gradient rms — above `stall` times the smallest of
 // its three previous values switches all models to FP32 values and asks for
 // the accepted models' re-evaluation.
-__global__ void __launch_bounds__(kBT, 4) kb_status(int nm, ColState* st, int* ctl, int refine, double stall) {
+__global__ void __launch_bounds__(kBT, 4) kb_status(int nd, int ld, int nwd, ColState* st, int* ctl, int refine,
+                                                 double stall, unsigned long long* amask) {
+  const int nm = nd * ld;
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
   __syncthreads();
@@ -556,6 +602,8 @@ __global__ void __launch_bounds__(kBT, 4) kb_status(int nm, ColState* st, int* c
     ctl[C_REEVAL] = 1;
   }
   count_into(n, ctl, C_ACTIVE);
+  __syncthreads();
+  build_masks(st, nd, ld, nwd, 1, amask);
 }
 
 __global__ void kb_clear_reeval(int* ctl) {
@@ -667,7 +715,8 @@ struct BatchEval {
   double eps = 0.0;
   const double* label = nullptr;
   const double* sw = nullptr;
-  DBuf label_f, sw_f, R, s1, s2, slots, seg_row, grow;
+  DBuf label_f, sw_f, R, s1, s2, slots, seg_row, seg_rowT, grow;
+  int nwd = 1;
 
   void init(fvg_ctx* c_, DevCRS* A_, DevCRS* AT_, int k_, int ld_, const double* label_, const double* sw_,
             int icpt_, const std::vector<i64>& roff, const std::vector<i64>& doff, const std::vector<int>& planes) {
@@ -705,16 +754,24 @@ struct BatchEval {
     std::vector<i64> gr((size_t)nd);
     for (int d = 0; d <= nd; d++) sr[d] = (i32)roff[d];
     for (int d = 0; d < nd; d++) gr[d] = doff[d + 1] - 1;  // the dataset's bias row
+    std::vector<i32> srT((size_t)nd + 1);  // the transposed matrix's rows: the vector rows
+    for (int d = 0; d <= nd; d++) srT[d] = (i32)doff[d];
     seg_row.alloc(sizeof(i32) * (nd + 1), s);
+    seg_rowT.alloc(sizeof(i32) * (nd + 1), s);
     grow.alloc(sizeof(i64) * nd, s);
     FVG_CUDA(cudaMemcpyAsync(seg_row.p, sr.data(), sizeof(i32) * (nd + 1), cudaMemcpyHostToDevice, s));
+    FVG_CUDA(cudaMemcpyAsync(seg_rowT.p, srT.data(), sizeof(i32) * (nd + 1), cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaMemcpyAsync(grow.p, gr.data(), sizeof(i64) * nd, cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaStreamSynchronize(s));
+    nwd = (ld + 63) / 64;
   }
   // x: weight vectors (FP64 for FP64 storage, FP32 otherwise) of all
   // datasets; bias[nd][ld]; g: gradient vectors; ev[nd][ld][2] = loss, bias
-  // sum.  Nothing runs while *gate == 0.
-  void eval(int storage, const void* x, const double* bias, double* g, double* ev, const int* gate) {
+  // sum.  Nothing runs while *gate == 0; with `mask` ([nd][nwd] model bits)
+  // only those models are evaluated, the others' g and ev columns keep what
+  // they held.
+  void eval(int storage, const void* x, const double* bias, double* g, double* ev, const int* gate,
+            const unsigned long long* mask) {
     const size_t xs = storage == FVG_F64 ? 8 : 4;
     for (int c0 = 0; c0 < ld; c0 += 64) {
       const int kb = std::min(64, ld - c0);
@@ -730,6 +787,9 @@ struct BatchEval {
       sg.grow = grow.as<i64>();
       sg.ldg = ld;
       sg.gate = gate;
+      sg.mask = mask;
+      sg.mstride = nwd;
+      sg.mword = c0 / 64;
       {
         ProfScope ps(c, P_BATCH_PASS1);
         crs_spmm_logreg_seg(c, *A, storage, (const char*)x + c0 * xs, ld, kb, label, sw, label_f.as<float>(),
@@ -738,7 +798,14 @@ struct BatchEval {
       }
       {
         ProfScope ps(c, P_BATCH_PASS2);
-        crs_spmm_block(c, *AT, storage, (const char*)R.p + c0 * xs, ld, kb, FVG_F64, g + c0, ld, s2.p, gate);
+        SpmmSeg st;
+        st.nseg = nd;
+        st.seg_row = seg_rowT.as<i32>();
+        st.gate = gate;
+        st.mask = mask;
+        st.mstride = nwd;
+        st.mword = c0 / 64;
+        crs_spmm_store_seg(c, *AT, storage, (const char*)R.p + c0 * xs, ld, kb, g + c0, ld, s2.p, st);
       }
       crs_spmm_seg_finish(c, sg);
     }
@@ -844,7 +911,7 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
   const i64 plane = N1 * ld;
   const size_t vec = sizeof(double) * (size_t)plane;
   const int nm = nd * ld;  // model states, the padding columns inactive
-  DBuf W, NW, G, NG, Q, Z, STEP, S, Y, WF, B, EV, ST, part, ctl, dof;
+  DBuf W, NW, G, NG, Q, Z, STEP, S, Y, WF, B, EV, ST, part, ctl, dof, MSK;
   for (DBuf* b : {&W, &NW, &G, &NG, &Q, &Z, &STEP}) b->alloc(vec, s);
   S.alloc(vec * h, s);
   Y.alloc(vec * h, s);
@@ -865,6 +932,11 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
   part.alloc(sizeof(double) * 2 * (size_t)vgx * kk * nd, s);
   ctl.alloc(sizeof(int) * C_NCTL + sizeof(unsigned) * (size_t)nd, s);
   dof.alloc(sizeof(i64) * (nd + 1), s);
+  const int nwd = (ld + 63) / 64;
+  MSK.alloc(sizeof(unsigned long long) * 2 * (size_t)nd * nwd, s);
+  FVG_CUDA(cudaMemsetAsync(MSK.p, 0, sizeof(unsigned long long) * 2 * (size_t)nd * nwd, s));
+  unsigned long long* smask = MSK.as<unsigned long long>();  // models searching
+  unsigned long long* amask = smask + (size_t)nd * nwd;       // models active
   int* ctl_i = ctl.as<int>();
   unsigned* ticket = (unsigned*)(ctl_i + C_NCTL);
   double* B0 = B.as<double>();
@@ -906,10 +978,12 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
     FVG_CUDA(cudaStreamSynchronize(s));  // the host vectors above go out of scope
   }
   FVG_CUDA(cudaMemsetAsync(NW.p, 0, vec, s));  // staging done
-  BArgs a{kk, ld, kp, rpb, h, dof.as<i64>(), plane, part.as<double>(), ticket, ST.as<ColState>(), ctl_i, -1};
-  auto gated = [&](int w) {
+  BArgs a{kk, ld, kp, rpb, h, dof.as<i64>(), plane, part.as<double>(), ticket, ST.as<ColState>(), ctl_i, -1,
+          nullptr, nwd};
+  auto gated = [&](int w, const unsigned long long* mask = nullptr) {
     BArgs g = a;
     g.gate = w;
+    g.mask = mask;
     return g;
   };
   const unsigned dg = grid_for(c, plane);
@@ -921,10 +995,10 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
     count_launch(c);
     return WF.p;
   };
-  auto norms = [&](const double* g, int accepted, int gate) {
+  auto norms = [&](const double* g, int accepted, int gate, const unsigned long long* mask) {
     ProfScope ps(c, P_LBFGS);
-    kb_gmax<<<vgrid, kBT, 0, s>>>(g, gated(gate));
-    kb_gnorm<<<vgrid, kBT, 0, s>>>(g, EV.as<double>(), accepted, gated(gate));
+    kb_gmax<<<vgrid, kBT, 0, s>>>(g, gated(gate, mask));
+    kb_gnorm<<<vgrid, kBT, 0, s>>>(g, EV.as<double>(), accepted, gated(gate, mask));
     check_launch("kb_gnorm");
     count_launch(c, 2);
   };
@@ -932,8 +1006,8 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
 
   // the whole training as one launch sequence
   auto run = [&]() {
-    ev.eval(storage, weights_for(storage, W.as<double>(), one), B0, G.as<double>(), EV.as<double>(), one);
-    norms(G.as<double>(), 1, C_ONE);
+    ev.eval(storage, weights_for(storage, W.as<double>(), one), B0, G.as<double>(), EV.as<double>(), one, nullptr);
+    norms(G.as<double>(), 1, C_ONE, nullptr);
     int rear = 0, front = 0;
     for (i64 it = 1; it <= p->num_iteration; it++) {
       const int kh = (int)std::min<i64>(it - 1, h);
@@ -948,7 +1022,7 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
         kb_step<<<vgrid, kBT, 0, s>>>(kh, rear, G.as<double>(), Z.as<double>(), STEP.as<double>(), S.as<double>(),
                                       gated(C_ACTIVE));
         kb_step_norm<<<vgrid, kBT, 0, s>>>(STEP.as<double>(), gated(C_ACTIVE));
-        kb_begin_search<<<1, kBT, 0, s>>>(nm, a.st, ctl_i);
+        kb_begin_search<<<1, kBT, 0, s>>>(nd, ld, nwd, a.st, ctl_i, smask);
         check_launch("batched two-loop");
         count_launch(c, 2 * kh + 3);
       }
@@ -962,10 +1036,12 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
           count_launch(c);
         }
         const void* x = mixed ? WF.p : NW.p;
-        ev.eval(storage, x, B1, NG.as<double>(), EV.as<double>(), ctl_i + C_EVAL_LO);
-        if (refine) ev.eval(FVG_F32, x, B1, NG.as<double>(), EV.as<double>(), ctl_i + C_EVAL_HI);
-        norms(NG.as<double>(), 0, C_TRIAL);
-        kb_decide<<<1, kBT, 0, s>>>(t, EV.as<double>(), nm, a.st, ctl_i);
+        // the models still searching only: the others keep their accepted
+        // trial's loss and gradient
+        ev.eval(storage, x, B1, NG.as<double>(), EV.as<double>(), ctl_i + C_EVAL_LO, smask);
+        if (refine) ev.eval(FVG_F32, x, B1, NG.as<double>(), EV.as<double>(), ctl_i + C_EVAL_HI, smask);
+        norms(NG.as<double>(), 0, C_TRIAL, smask);
+        kb_decide<<<1, kBT, 0, s>>>(t, EV.as<double>(), nd, ld, nwd, a.st, ctl_i, smask);
         check_launch("kb_decide");
         count_launch(c);
       }
@@ -975,7 +1051,7 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
         kb_accept<<<vgrid, kBT, 0, s>>>(nf, (int)it, p->convergence_tol, W.as<double>(), G.as<double>(),
                                         NW.as<double>(), NG.as<double>(), S.as<double>(), Y.as<double>(), B0, B1,
                                         EV.as<double>(), gated(C_ACTIVE));
-        kb_status<<<1, kBT, 0, s>>>(nm, a.st, ctl_i, refine ? 1 : 0, p->refine_stall);
+        kb_status<<<1, kBT, 0, s>>>(nd, ld, nwd, a.st, ctl_i, refine ? 1 : 0, p->refine_stall, amask);
         check_launch("kb_accept");
         count_launch(c, 2);
       }
@@ -990,8 +1066,8 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
       }
       if (refine) {  // re-evaluation of the accepted models right after the switch
         const int* re = ctl_i + C_REEVAL;
-        ev.eval(FVG_F32, weights_for(FVG_F32, W.as<double>(), re), B0, G.as<double>(), EV.as<double>(), re);
-        norms(G.as<double>(), 1, C_REEVAL);
+        ev.eval(FVG_F32, weights_for(FVG_F32, W.as<double>(), re), B0, G.as<double>(), EV.as<double>(), re, amask);
+        norms(G.as<double>(), 1, C_REEVAL, amask);
         kb_clear_reeval<<<1, 32, 0, s>>>(ctl_i);
         check_launch("kb_clear_reeval");
         count_launch(c);

@@ -370,14 +370,50 @@ static void jds_fill(fvg_ctx* c, const DevCRS& a, int master, const i32* perm, i
   else launch_jds_fill<bf16>(c, a, master, perm, rows, joff, cap, jidx, jval);
 }
 
-// Leading permuted rows with more than kJdsWarpLen diagonals (the rows of
-// diagonal kJdsWarpLen): the JDS product gives each of them a warp.
-static i64 jds_warp_rows(fvg_ctx* c, const DevJDS& j) {
-  if (j.ndiag <= kJdsWarpLen) return 0;
-  i64 h[2];
-  FVG_CUDA(cudaMemcpyAsync(h, j.off.as<i64>() + kJdsWarpLen, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+// Work items of the JDS product from the diagonal lengths (off is
+// non-increasing in length): row block b has len(32b) diagonals, cut into
+// kJdsSeg-diagonal items; the blocks cut in several get partial slots.
+static void jds_items(fvg_ctx* c, DevJDS& j) {
+  const i64 nb = (j.m + 31) / 32;
+  std::vector<i64> off((size_t)j.ndiag + 1);
+  FVG_CUDA(cudaMemcpyAsync(off.data(), j.off.p, sizeof(i64) * (j.ndiag + 1), cudaMemcpyDeviceToHost, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));
-  return h[1] - h[0];
+  std::vector<JdsItem> items;
+  std::vector<JdsSplit> splits;
+  items.reserve((size_t)nb + 16);
+  i32 slots = 0;
+  for (i64 b = 0; b < nb; b++) {
+    const i64 p0 = 32 * b;
+    // diagonals longer than p0: the first d with length <= p0
+    i64 lo = 0, hi = j.ndiag;
+    while (lo < hi) {
+      const i64 mid = (lo + hi) >> 1;
+      if (off[mid + 1] - off[mid] > p0) lo = mid + 1;
+      else hi = mid;
+    }
+    const i64 D = lo;
+    if (D <= kJdsSeg) {
+      items.push_back(JdsItem{(i32)b, 0, (i32)D, -1});
+      continue;
+    }
+    const i32 ns = (i32)((D + kJdsSeg - 1) / kJdsSeg);
+    splits.push_back(JdsSplit{(i32)b, slots, ns, 0});
+    for (i32 q = 0; q < ns; q++)
+      items.push_back(JdsItem{(i32)b, (i32)(q * kJdsSeg), (i32)std::min<i64>(D, (q + 1) * kJdsSeg), slots + q});
+    slots += ns;
+  }
+  j.nitems = (i64)items.size();
+  j.nsplits = (i64)splits.size();
+  j.nslots = slots;
+  j.items.alloc(sizeof(JdsItem) * std::max<size_t>(items.size(), 1), c->stream);
+  j.splits.alloc(sizeof(JdsSplit) * std::max<size_t>(splits.size(), 1), c->stream);
+  if (!items.empty())
+    FVG_CUDA(cudaMemcpyAsync(j.items.p, items.data(), sizeof(JdsItem) * items.size(), cudaMemcpyHostToDevice,
+                             c->stream));
+  if (!splits.empty())
+    FVG_CUDA(cudaMemcpyAsync(j.splits.p, splits.data(), sizeof(JdsSplit) * splits.size(), cudaMemcpyHostToDevice,
+                             c->stream));
+  FVG_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
 }
 
 void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master) {
@@ -400,7 +436,7 @@ void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master) {
   FVG_CUDA(cudaMemsetAsync(j.idx.as<i32>() + a.nnz, 0, sizeof(i32) * kPad, c->stream));
   alloc_plane(c, j.val[master], a.nnz, master);
   jds_fill(c, a, master, j.perm.as<i32>(), a.m, j.off.as<i64>(), j.ndiag, j.idx.as<i32>(), j.val[master].p);
-  j.warp_rows = jds_warp_rows(c, j);
+  jds_items(c, j);
 }
 
 // ------------------------------------------------------------------ hybrid
@@ -514,7 +550,7 @@ void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 thr) {
   alloc_plane(c, h.jds.val[master], h.jds.nnz, master);
   jds_fill(c, a, master, h.jds.perm.as<i32>(), a.m, h.jds.off.as<i64>(), start, h.jds.idx.as<i32>(),
            h.jds.val[master].p);
-  h.jds.warp_rows = jds_warp_rows(c, h.jds);
+  jds_items(c, h.jds);
   // CRS tail of the crs_rows longest rows, in sorted order
   h.crs.m = crs_rows;
   h.crs.n = a.n;

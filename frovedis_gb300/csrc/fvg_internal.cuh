@@ -132,9 +132,23 @@ struct DevJDS {  // jds_matrix_local (jds_matrix.hpp:15-146)
   DBuf idx;      // int32 [nnz]
   DBuf val[3];
   bool empty_perm = false;  // all-zero matrix: the reference leaves perm empty
-  i64 warp_rows = 0;        // leading permuted rows longer than kJdsWarpLen (a warp each)
+  // Work items of the product (JdsItem): a warp per block of 32 permuted rows
+  // and at most kJdsSeg diagonals; blocks with more diagonals are cut into
+  // several items whose per-row partials (nslots x 32 accumulators) are added
+  // in diagonal order by the split blocks' finalize (JdsSplit).
+  DBuf items, splits;
+  i64 nitems = 0, nsplits = 0, nslots = 0;
 };
-constexpr i64 kJdsWarpLen = 128;
+constexpr i64 kJdsSeg = 128;
+struct JdsItem {
+  int32_t b;     // row block: permuted rows 32b .. 32b+31
+  int32_t d0;    // diagonals [d0, d1)
+  int32_t d1;
+  int32_t slot;  // partial slot, -1: the item covers the whole block
+};
+struct JdsSplit {
+  int32_t b, slot0, nslot, pad;
+};
 
 struct DevHYB {  // jds_crs_hybrid_local (jds_crs_hybrid.hpp:8-153)
   i64 m = 0, n = 0, crs_rows = 0;
@@ -356,6 +370,12 @@ struct SpmmSeg {
   const i64* grow = nullptr;     // device [nseg]
   i64 ldg = 0;
   const int* gate = nullptr;
+  // column masks (null: all): bit j of mask[d * mstride + mword] set =
+  // column j of the block is computed for dataset d; masked outputs keep
+  // their contents (kb <= 64)
+  const unsigned long long* mask = nullptr;
+  i64 mstride = 0;
+  int mword = 0;
   // set by the pass for crs_spmm_seg_finish
   i64 nw1 = 0, nw2 = 0;
   int nc = 0, icpt = 0;
@@ -366,6 +386,9 @@ void crs_spmm_logreg_seg(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 
                          void* R, i64 ldr, void* scratch, SpmmSeg& sg, int loss = 0, double eps = 0.0);
 // The per-dataset sums of the pass (launch after the backward product).
 void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg);
+// Y = A X (FP64 Y) over stacked datasets with sg's row bounds, masks, gate.
+void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
+                        void* scratch, SpmmSeg& sg);
 
 // Row-panel backward product (FP32/BF16 storage): builds the layout when the
 // matrix's column counts make it pay (or as forced); returns null when the

@@ -56,7 +56,27 @@ struct SpmmK {
   i64 ldb;
   double* seg_part;
   const int* gate;  // the launch does nothing while *gate == 0 (null: always runs)
+  // Column masks of stacked datasets (null: every column): bit c of
+  // mask[d * mstride + mword] set = column c of dataset d is computed;
+  // masked columns are neither gathered nor written (their outputs keep
+  // what they held) and their loss / bias sums are left out.
+  const unsigned long long* mask;
+  i64 mstride;
+  int mword;
 };
+
+__device__ __forceinline__ unsigned long long mask_of(const SpmmK& p, int d) {
+  return p.mask ? __ldcg(p.mask + (i64)d * p.mstride + p.mword) : ~0ull;
+}
+// column c (< 64 whenever a mask is given) is computed under mask word mw;
+// all-ones = no mask
+__device__ __forceinline__ bool col_on(unsigned long long mw, int c) {
+  return mw == ~0ull || (c < 64 && ((mw >> c) & 1ull));
+}
+// any of the n columns c .. c + n - 1
+__device__ __forceinline__ bool cols_on(unsigned long long mw, int c, int n) {
+  return mw == ~0ull || (c < 64 && ((mw >> c) & ((1ull << n) - 1)) != 0);
+}
 
 __device__ __forceinline__ bool gated_off(const int* gate) { return gate && __ldcg(gate) == 0; }
 
@@ -160,12 +180,16 @@ template <> __device__ __forceinline__ float log_acc<float>(float x) { return lo
 
 template <class AT, class YT, int EPI, int CPL, bool VEC, class S>
 __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[CPL], const AT (&b)[CPL], int lane,
-                                         S (&ls)[CPL], S (&bs)[CPL]) {
-#define ON(q) (colof<VEC, CPL>(lane, q) < p.kb)
+                                         S (&ls)[CPL], S (&bs)[CPL], unsigned long long mw = ~0ull) {
+#define ON(q) (colof<VEC, CPL>(lane, q) < p.kb && col_on(mw, colof<VEC, CPL>(lane, q)))
   if (EPI == EPI_STORE) {
     YT* y = (YT*)p.Y + (i64)row * p.ldy;
     if constexpr (VEC) {
-      if (lane * CPL < p.kb) {
+      if (mw != ~0ull) {
+#pragma unroll
+        for (int q = 0; q < CPL; q++)
+          if (ON(q)) y[colof<VEC, CPL>(lane, q)] = (YT)a[q];
+      } else if (lane * CPL < p.kb) {
         YT o[CPL];
 #pragma unroll
         for (int q = 0; q < CPL; q++) o[q] = (YT)a[q];
@@ -335,8 +359,10 @@ template <class AT, int QN> struct SegWalk {
   double* slots;  // this warp's slot of dataset 0; slot d at + d * stride
   i64 stride;
   __device__ __forceinline__ SegWalk(const SpmmK& p, double* base, i64 warp, i64 nwarps, int nc)
-      : end(p.nseg > 0 ? __ldg(p.seg_row + 1) : 0), slots(base + warp * nc * 2), stride(nwarps * nc * 2) {}
+      : end(p.nseg > 0 ? __ldg(p.seg_row + 1) : 0x7fffffff), slots(base ? base + warp * nc * 2 : nullptr),
+        stride(nwarps * nc * 2) {}
   __device__ __forceinline__ void put(int dd, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
+    if (!slots) return;
     double* s = slots + dd * stride;
 #pragma unroll
     for (int q = 0; q < QN; q++) {
@@ -347,6 +373,7 @@ template <class AT, int QN> struct SegWalk {
     }
   }
   __device__ __forceinline__ void zero(int dd, const int (&col)[QN]) {
+    if (!slots) return;
     double* s = slots + dd * stride;
 #pragma unroll
     for (int q = 0; q < QN; q++) {
@@ -364,6 +391,7 @@ template <class AT, int QN> struct SegWalk {
     return true;
   }
   __device__ __forceinline__ void finish(const SpmmK& p, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
+    if (!slots) return;
     put(d, col, ls, bs);
     for (int dd = d + 1; dd < p.nseg; dd++) zero(dd, col);
   }
@@ -380,7 +408,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
   if (gated_off(p.gate)) return;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const bool seg = EPI == EPI_LOGREG && p.nseg > 0;
+  const bool track = p.nseg > 0;                  // stacked datasets
+  const bool seg = EPI == EPI_LOGREG && track;    // per-dataset loss slots
   AT b[CPL];
   auto load_bias = [&](const double* bias) {
 #pragma unroll
@@ -395,11 +424,16 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 #pragma unroll
   for (int q = 0; q < CPL; q++) cols[q] = colof<VEC, CPL>(lane, q);
   const i64 gw = (i64)blockIdx.x * (kThreads / 32) + wib, nw = (i64)gridDim.x * (kThreads / 32);
-  SegWalk<AT, CPL> sw(p, f.seg_fpart, gw, nw, NC);
+  SegWalk<AT, CPL> sw(p, seg ? f.seg_fpart : nullptr, gw, nw, NC);
+  unsigned long long mw = mask_of(p, 0);
   for (i64 i = gw; i < f.nlong; i += nw) {
     const i64 q0 = f.long_piece0[i], q1 = f.long_piece0[i + 1];
     const i32 row = f.long_rows[i];
-    if (seg && sw.to_row(p, row, cols, ls, bs)) load_bias(p.bias + sw.d * p.ldb);
+    if (track && sw.to_row(p, row, cols, ls, bs)) {
+      if (EPI == EPI_LOGREG) load_bias(p.bias + sw.d * p.ldb);
+      mw = mask_of(p, sw.d);
+    }
+    if (mw == 0) continue;
     AT a[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; q++) a[q] = 0;
@@ -408,8 +442,9 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 #pragma unroll
       for (int q = 0; q < CPL; q++) a[q] += part[colof<VEC, CPL>(lane, q)];
     }
-    spmm_epi<AT, YT, EPI, CPL, VEC>(p, row, a, b, lane, ls, bs);
+    spmm_epi<AT, YT, EPI, CPL, VEC>(p, row, a, b, lane, ls, bs, mw);
   }
+  if (track && !seg) return;
   if (seg) {
     sw.finish(p, cols, ls, bs);
     return;
@@ -500,13 +535,14 @@ template <class XT, int G> struct GLay {
 };
 
 template <class VT, class XT, class AT, int G>
-__device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[GLay<XT, G>::CPL]) {
+__device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[GLay<XT, G>::CPL],
+                                          bool lane_on = true) {
   using L = GLay<XT, G>;
   constexpr int CPL = L::CPL;
   const int sub = lane % L::LPR, grp = lane / L::LPR;
   const XT* X = (const XT*)p.X + sub * CPL;
   const VT* val = (const VT*)p.val;
-  const bool mine = sub * CPL < p.kb;
+  const bool mine = lane_on && sub * CPL < p.kb;
 #pragma unroll
   for (int q = 0; q < CPL; q++) a[q] = 0;
   for (i32 e = e0; e < e1; e += 32) {
@@ -555,7 +591,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   const int c0 = (lane % L::LPR) * CPL + (lane / L::LPR) * QG;  // first of the lane's epilogue columns
   const i64 gw = (i64)blockIdx.x * (kThreads / 32) + wib;
   const i64 nw = (i64)gridDim.x * (kThreads / 32);
-  const bool seg = EPI == EPI_LOGREG && p.nseg > 0;
+  const bool track = p.nseg > 0;                // stacked datasets
+  const bool seg = EPI == EPI_LOGREG && track;  // per-dataset loss slots
   int cols[QG];
 #pragma unroll
   for (int q = 0; q < QG; q++) cols[q] = c0 + q;
@@ -566,7 +603,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   };
   load_bias(p.bias);
   Sum ls[QG], bs[QG];
-  SegWalk<AT, QG> walk(p, p.seg_part, gw, nw, NC);
+  SegWalk<AT, QG> walk(p, seg ? p.seg_part : nullptr, gw, nw, NC);
+  const int lsh = (lane % L::LPR) * CPL;  // the lane's gathered columns: lsh .. lsh + CPL - 1
+  unsigned long long mw = mask_of(p, 0);
   AT lab = 0, w = 1;
   for (i64 it = gw; it < p.nitems; it += nw) {
     const Item item = p.items[it];
@@ -579,13 +618,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
       continue;
     }
     for (i32 r = item.r0; r < item.r1; r++) {
-      if (seg && walk.to_row(p, r, cols, ls, bs)) load_bias(p.bias + walk.d * p.ldb);
-      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a);
+      if (track && walk.to_row(p, r, cols, ls, bs)) {
+        if (EPI == EPI_LOGREG) load_bias(p.bias + walk.d * p.ldb);
+        mw = mask_of(p, walk.d);
+      }
+      if (mw == 0) continue;  // no column of this dataset is computed
+      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a, cols_on(mw, lsh, CPL));
       if constexpr (EPI == EPI_STORE) {
         YT* y = (YT*)p.Y + (i64)r * p.ldy;
 #pragma unroll
         for (int q = 0; q < QG; q++)
-          if (cols[q] < p.kb) y[cols[q]] = (YT)a[q];
+          if (cols[q] < p.kb && col_on(mw, cols[q])) y[cols[q]] = (YT)a[q];
       } else {
         bool has_sw;
         if constexpr (sizeof(AT) == 8) {
@@ -600,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
         AT* rr = (AT*)p.R + (i64)r * p.ldr;
 #pragma unroll
         for (int q = 0; q < QG; q++) {
-          if (cols[q] >= p.kb) continue;
+          if (cols[q] >= p.kb || !col_on(mw, cols[q])) continue;
           AT loss, d;
           glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
           if (has_sw) d = d * w;
@@ -611,6 +654,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
       }
     }
   }
+  if (track && !seg) return;
   if constexpr (EPI == EPI_LOGREG) {
     if (seg) {
       walk.finish(p, cols, ls, bs);
@@ -642,7 +686,8 @@ template <int NC>
 __global__ void __launch_bounds__(1024) k_spmm_seg_reduce(const double* __restrict__ s1, i64 nw1,
                                                           const double* __restrict__ s2, i64 nw2, int kout, int icpt,
                                                           double* __restrict__ out, i64 ldo, double* __restrict__ gb,
-                                                          const i64* __restrict__ grow, i64 ldg, const int* gate) {
+                                                          const i64* __restrict__ grow, i64 ldg, const int* gate,
+                                                          const unsigned long long* mask, i64 mstride, int mword) {
   constexpr int P = 2 * NC, S = 1024 / P;
   static_assert(1024 % P == 0, "pairs per CTA");
   __shared__ double part[S][P];
@@ -662,6 +707,7 @@ __global__ void __launch_bounds__(1024) k_spmm_seg_reduce(const double* __restri
   for (int q = 0; q < S; q++) tot += part[q][pr];
   const int col = pr >> 1, qq = pr & 1;
   if (col >= kout) return;
+  if (mask && !col_on(__ldcg(mask + (i64)d * mstride + mword), col)) return;  // not evaluated: keep
   if (qq == 0) {
     out[2 * ((i64)d * ldo + col)] = tot;
   } else {
@@ -757,15 +803,21 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
   p.items = s.items.as<Item>();
   p.nitems = s.nitems;
   p.cta_part = EPI == EPI_LOGREG ? cta : nullptr;
-  const bool seg = EPI == EPI_LOGREG && sg && sg->nseg > 0;
+  const bool track = sg && sg->nseg > 0;
+  const bool seg = EPI == EPI_LOGREG && track;
   const i64 nw1 = (i64)grid * (kThreads / 32), nw2 = (i64)fg * (kThreads / 32);
-  if (seg) {
-    if (!sg->seg_row || !sg->slots || sg->nseg > 65535) fail(FVG_ERR_INTERNAL, "stacked-dataset pass without slots");
+  if (track) {
+    if (!sg->seg_row || (seg && !sg->slots) || sg->nseg > 65535)
+      fail(FVG_ERR_INTERNAL, "stacked-dataset pass without its row bounds or slots");
+    if (sg->mask && p.kb > 64) fail(FVG_ERR_INTERNAL, "column masks cover 64 columns");
     p.nseg = sg->nseg;
     p.seg_row = sg->seg_row;
     p.ldb = sg->ldb;
-    p.seg_part = sg->slots;
+    p.seg_part = seg ? sg->slots : nullptr;
     p.gate = sg->gate;
+    p.mask = sg->mask;
+    p.mstride = sg->mstride;
+    p.mword = sg->mword;
   }
   if (s.nitems > 0 || seg) {
     k_spmm_g<VT, XT, AT, YT, EPI, G><<<grid, kThreads, 0, c->stream>>>(p);
@@ -882,6 +934,32 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
   }
 }
 
+// Y = A X over stacked datasets (rows [seg_row[d], seg_row[d+1]) of A belong
+// to dataset d) with the column masks and the gate of sg; masked columns of
+// Y keep what they held.  X, Y and their strides 16-byte aligned, kb a
+// multiple of 4 (of 2 for FP64) and at most 64.
+void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
+                        void* scratch, SpmmSeg& sg) {
+  if (kb < 1 || kb > 64 || sg.nseg < 1) fail(FVG_ERR_INTERNAL, "stacked store: block width or datasets out of range");
+  if (!a.val[storage].p) fail(FVG_ERR_INTERNAL, "missing value plane for the requested storage");
+  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
+  SpmmK p = {};
+  p.X = X;
+  p.ldx = ldx;
+  p.kb = kb;
+  p.Y = Y;
+  p.ldy = ldy;
+  char* sc = (char*)scratch;
+  bool ok;
+  if (storage == FVG_F64)
+    ok = launch_grouped<double, double, double, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  else if (storage == FVG_F32)
+    ok = launch_grouped<float, float, float, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  else
+    ok = launch_grouped<bf16, float, float, double, EPI_STORE>(c, a, s, storage, p, nullptr, nullptr, sc, &sg);
+  if (!ok) fail(FVG_ERR_INTERNAL, "stacked store needs 16-byte aligned rows");
+}
+
 // Batched GLM forward pass over a block of kb <= 64 models: R = dloss(A W +
 // b) * sw per (row, model) for the loss kind `loss`; out[2j] = loss of model
 // j, out[2j+1] = its bias sum (0 without intercept), also written to gbias[j]
@@ -963,13 +1041,16 @@ void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg) {
   const double* s2 = sg.slots + (i64)sg.nseg * sg.nw1 * sg.nc * 2;
   if (sg.nc == 32)
     k_spmm_seg_reduce<32><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
-                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
+                                                           sg.mstride, sg.mword);
   else if (sg.nc == 64)
     k_spmm_seg_reduce<64><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
-                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+                                                           sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
+                                                           sg.mstride, sg.mword);
   else
     k_spmm_seg_reduce<128><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
-                                                            sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate);
+                                                            sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
+                                                           sg.mstride, sg.mword);
   check_launch("k_spmm_seg_reduce");
   count_launch(c);
 }

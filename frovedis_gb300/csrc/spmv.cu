@@ -454,70 +454,76 @@ size_t crs_spmv_no_alloc(fvg_ctx* c, DevCRS& a, int storage, const void* x, void
 }
 
 // ------------------------------------------------------------------- JDS
-// Thread per permuted row; diagonal d of row p sits at off[d] + p, so a warp
-// reads each diagonal contiguously.  Diagonal lengths never increase, so row
-// p has exactly the diagonals d with off[d+1] - off[d] > p (binary search).
-// part (hybrid) adds the CRS tail of the first npart permuted rows after the
-// JDS sum, as jds_crs_hybrid_spmv_impl does (jds_crs_hybrid.hpp:198-211).
-// Rows with more than kJdsWarpLen diagonals (the first `nrows` permuted rows)
-// are read by a warp each instead: lanes stride over the row's diagonals.
+// Work items (JdsItem): a warp per block of 32 consecutive permuted rows
+// (lane = row) and at most kJdsSeg of the block's diagonals.  Diagonal d of
+// row p sits at off[d] + p, so the warp reads each diagonal's 32 entries
+// with one coalesced access; row p has diagonal d iff the diagonal's length
+// off[d+1] - off[d] exceeds p.  Four diagonals are summed into four
+// accumulators, added as (a0 + a1) + (a2 + a3) at the item's end.  A block
+// with more diagonals than one item holds leaves per-row partials, which
+// k_jds_split adds in diagonal order.  part (hybrid) adds the CRS tail of
+// the first npart permuted rows after the JDS sum, as
+// jds_crs_hybrid_spmv_impl does (jds_crs_hybrid.hpp:198-211).
+template <class VT, class XT, class AT>
+__device__ __forceinline__ AT jds_term(const VT* __restrict__ val, const i32* __restrict__ idx,
+                                       const XT* __restrict__ x, i64 q) {
+  return (AT)val[q] * (AT)__ldg(x + __ldg(idx + q));
+}
+
 template <class VT, class XT, class AT, class YT>
-__global__ void __launch_bounds__(256) k_jds_warp(const i32* __restrict__ perm, const i64* __restrict__ off,
-                                                  const i32* __restrict__ idx, const VT* __restrict__ val,
-                                                  i64 nrows, i64 ndiag, const XT* __restrict__ x,
-                                                  YT* __restrict__ y, const AT* __restrict__ part, i64 npart) {
+__global__ void __launch_bounds__(256) k_jds(const JdsItem* __restrict__ items, i64 nitems,
+                                             const i32* __restrict__ perm, const i64* __restrict__ off,
+                                             const i32* __restrict__ idx, const VT* __restrict__ val, i64 m,
+                                             const XT* __restrict__ x, YT* __restrict__ y,
+                                             const AT* __restrict__ part, i64 npart, AT* __restrict__ partials) {
   const int lane = threadIdx.x & 31;
   const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
-  for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nrows; p += nw) {
-    i64 lo = 0, hi = ndiag;
-    while (lo < hi) {
-      i64 mid = (lo + hi) >> 1;
-      if (off[mid + 1] - off[mid] > p) lo = mid + 1;
-      else hi = mid;
+  for (i64 it = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < nitems; it += nw) {
+    const JdsItem t = items[it];
+    const i64 p = (i64)t.b * 32 + lane;
+    AT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    i64 d = t.d0;
+    i64 o = __ldg(off + d);
+    for (; d + 3 < t.d1; d += 4) {
+      const i64 o1 = __ldg(off + d + 1), o2 = __ldg(off + d + 2), o3 = __ldg(off + d + 3), o4 = __ldg(off + d + 4);
+      if (p < o1 - o) a0 += jds_term<VT, XT, AT>(val, idx, x, o + p);
+      if (p < o2 - o1) a1 += jds_term<VT, XT, AT>(val, idx, x, o1 + p);
+      if (p < o3 - o2) a2 += jds_term<VT, XT, AT>(val, idx, x, o2 + p);
+      if (p < o4 - o3) a3 += jds_term<VT, XT, AT>(val, idx, x, o3 + p);
+      o = o4;
     }
-    AT acc = 0;
-    for (i64 d = lane; d < lo; d += 32) {
-      i64 q = off[d] + p;
-      acc += (AT)val[q] * (AT)__ldg(x + idx[q]);
+    for (; d < t.d1; d++) {
+      const i64 o1 = __ldg(off + d + 1);
+      if (p < o1 - o) a0 += jds_term<VT, XT, AT>(val, idx, x, o + p);
+      o = o1;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
+    AT acc = (a0 + a1) + (a2 + a3);
+    if (t.slot >= 0) {
+      partials[(i64)t.slot * 32 + lane] = acc;
+    } else if (p < m) {
       if (p < npart) acc = acc + part[p];
       y[perm[p]] = (YT)acc;
     }
   }
 }
 
-template <class VT, class XT, class AT, class YT>
-__global__ void __launch_bounds__(256) k_jds(const i32* __restrict__ perm, const i64* __restrict__ off,
-                                             const i32* __restrict__ idx, const VT* __restrict__ val,
-                                             i64 m, i64 ndiag, const XT* __restrict__ x, YT* __restrict__ y,
-                                             const AT* __restrict__ part, i64 npart, i64 p0) {
-  for (i64 p = p0 + (i64)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (i64)gridDim.x * blockDim.x) {
-    i64 lo = 0, hi = ndiag;
-    while (lo < hi) {
-      i64 mid = (lo + hi) >> 1;
-      if (off[mid + 1] - off[mid] > p) lo = mid + 1;
-      else hi = mid;
+// blocks cut into several items: their partials in diagonal order
+template <class AT, class YT>
+__global__ void __launch_bounds__(256) k_jds_split(const JdsSplit* __restrict__ sp, i64 nsplits,
+                                                   const i32* __restrict__ perm, i64 m, YT* __restrict__ y,
+                                                   const AT* __restrict__ part, i64 npart,
+                                                   const AT* __restrict__ partials) {
+  const int lane = threadIdx.x & 31;
+  const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
+  for (i64 i = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nsplits; i += nw) {
+    const JdsSplit s = sp[i];
+    const i64 p = (i64)s.b * 32 + lane;
+    AT acc = 0;
+    for (int q = 0; q < s.nslot; q++) acc += partials[(i64)(s.slot0 + q) * 32 + lane];
+    if (p < m) {
+      if (p < npart) acc = acc + part[p];
+      y[perm[p]] = (YT)acc;
     }
-    const i64 len = lo;
-    AT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    i64 d = 0;
-    for (; d + 3 < len; d += 4) {
-      i64 q0 = off[d] + p, q1 = off[d + 1] + p, q2 = off[d + 2] + p, q3 = off[d + 3] + p;
-      a0 += (AT)val[q0] * (AT)__ldg(x + idx[q0]);
-      a1 += (AT)val[q1] * (AT)__ldg(x + idx[q1]);
-      a2 += (AT)val[q2] * (AT)__ldg(x + idx[q2]);
-      a3 += (AT)val[q3] * (AT)__ldg(x + idx[q3]);
-    }
-    for (; d < len; d++) {
-      i64 q = off[d] + p;
-      a0 += (AT)val[q] * (AT)__ldg(x + idx[q]);
-    }
-    AT acc = (a0 + a1) + (a2 + a3);
-    if (p < npart) acc = acc + part[p];
-    y[perm[p]] = (YT)acc;
   }
 }
 
@@ -537,18 +543,17 @@ static void launch_jds(fvg_ctx* c, DevJDS& j, int storage, const void* x, void* 
   if (j.empty_perm) {
     k_zero<YT><<<grid_rows(j.m), 256, 0, c->stream>>>((YT*)y, j.m);
   } else {
-    const i64 L = j.warp_rows;
-    if (L > 0) {
-      k_jds_warp<VT, XT, AT, YT><<<grid_rows(L * 32), 256, 0, c->stream>>>(
-          j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(), L, j.ndiag, (const XT*)x,
-          (YT*)y, (const AT*)part, npart);
-      check_launch("k_jds_warp");
+    DBuf partials;
+    if (j.nslots > 0) partials.alloc(sizeof(AT) * 32 * (size_t)j.nslots, c->stream);
+    k_jds<VT, XT, AT, YT><<<grid_rows(j.nitems * 32), 256, 0, c->stream>>>(
+        j.items.as<JdsItem>(), j.nitems, j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(),
+        j.m, (const XT*)x, (YT*)y, (const AT*)part, npart, partials.as<AT>());
+    if (j.nsplits > 0) {
+      check_launch("k_jds");
       count_launch(c);
-    }
-    if (j.m > L) {
-      k_jds<VT, XT, AT, YT><<<grid_rows(j.m - L), 256, 0, c->stream>>>(
-          j.perm.as<i32>(), j.off.as<i64>(), j.idx.as<i32>(), j.val[storage].as<VT>(), j.m, j.ndiag, (const XT*)x,
-          (YT*)y, (const AT*)part, npart, L);
+      k_jds_split<AT, YT><<<grid_rows(j.nsplits * 32), 256, 0, c->stream>>>(
+          j.splits.as<JdsSplit>(), j.nsplits, j.perm.as<i32>(), j.m, (YT*)y, (const AT*)part, npart,
+          partials.as<AT>());
     }
   }
   check_launch("k_jds");
