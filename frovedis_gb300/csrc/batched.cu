@@ -71,6 +71,8 @@ enum BCtl {
   C_EVAL_HI,     // trial evaluation in FP32 after the switch
   C_TRIAL,       // C_SEARCH > 0
   C_ONE,         // always 1
+  C_NEVAL,       // evaluations run
+  C_NMODEL,      // (dataset, model) evaluations run
   C_NCTL = 16
 };
 
@@ -490,6 +492,10 @@ __global__ void __launch_bounds__(kBT, 4) kb_decide(int t, const double* __restr
                                                  ColState* st, int* ctl, unsigned long long* smask) {
   if (ctl[C_TRIAL] == 0) return;
   const int nm = nd * ld;
+  if (threadIdx.x == 0) {  // the trial's evaluation ran
+    ctl[C_NEVAL] += 1;
+    ctl[C_NMODEL] += ctl[C_SEARCH];
+  }
   int n = 0;
   for (int j = threadIdx.x; j < nm; j += kBT) {
     ColState& s = st[j];
@@ -607,7 +613,11 @@ __global__ void __launch_bounds__(kBT, 4) kb_status(int nd, int ld, int nwd, Col
 }
 
 __global__ void kb_clear_reeval(int* ctl) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) ctl[C_REEVAL] = 0;
+  if (threadIdx.x == 0 && blockIdx.x == 0 && ctl[C_REEVAL]) {
+    ctl[C_NEVAL] += 1;
+    ctl[C_NMODEL] += ctl[C_ACTIVE];
+    ctl[C_REEVAL] = 0;
+  }
 }
 
 // model-major [k][n] <-> column layout (one dataset's rows, stride ld; the
@@ -970,6 +980,8 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
     }
     hc[C_ACTIVE] = nact;
     hc[C_ONE] = 1;
+    hc[C_NEVAL] = 1;  // the initial evaluation
+    hc[C_NMODEL] = nact;
     FVG_CUDA(cudaMemcpyAsync(ST.p, cs.data(), sizeof(ColState) * nm, cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaMemcpyAsync(B0, bb.data(), sizeof(double) * 2 * nm, cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaMemcpyAsync(ctl_i, hc.data(), sizeof(int) * C_NCTL, cudaMemcpyHostToDevice, s));
@@ -1105,9 +1117,13 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
     FVG_CUDA(cudaMemcpyAsync(w_h + woff[d], NW.p, sizeof(double) * (size_t)(nd_ * kk), cudaMemcpyDeviceToHost, s));
     FVG_CUDA(cudaStreamSynchronize(s));
   }
+  std::vector<int> hctl(C_NCTL);
   FVG_CUDA(cudaMemcpyAsync(cs.data(), ST.p, sizeof(ColState) * nm, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaMemcpyAsync(bb.data(), B0, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
+  FVG_CUDA(cudaMemcpyAsync(hctl.data(), ctl_i, sizeof(int) * C_NCTL, cudaMemcpyDeviceToHost, s));
   FVG_CUDA(cudaStreamSynchronize(s));
+  c->batch_evals += hctl[C_NEVAL];
+  c->batch_model_evals += hctl[C_NMODEL];
   for (int d = 0; d < nd; d++)
     for (int j = 0; j < kk; j++) {
       const ColState& x = cs[(size_t)d * ld + j];

@@ -181,6 +181,11 @@ FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* c, int enable) {
 FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* c, const char* name, double* total_ms, int64_t* launches) {
   if (!c || !name || !total_ms || !launches) return FVG_ERR_INVALID_ARG;
   API_BEGIN
+  if (!strcmp(name, "batch_evals")) {  // counters, not timings
+    *total_ms = (double)c->batch_model_evals;
+    *launches = c->batch_evals;
+    return FVG_OK;
+  }
   int key = -1;
   for (int k = 0; k < P_NKEYS; k++)
     if (!strcmp(name, kProfNames[k])) key = k;

@@ -232,6 +232,10 @@ struct fvg_ctx {
   unsigned* dev_err = nullptr;
   // poll budget of the bounded device-side waits (< 0: the defaults below)
   int64_t wait_limit = -1;
+  // batched trainers: evaluations run (the line-search trials that had a
+  // model searching, initial and precision-switch evaluations) and the
+  // (dataset, model) evaluations inside them, since the context was made
+  int64_t batch_evals = 0, batch_model_evals = 0;
 };
 
 struct fvg_matrix {

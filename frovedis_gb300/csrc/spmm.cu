@@ -610,8 +610,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   for (i64 it = gw; it < p.nitems; it += nw) {
     const Item item = p.items[it];
     AT a[CPL];
-    if (item.r1 < 0) {  // piece of a long row
-      row_dot_g<VT, XT, AT, G>(p, item.e0, item.e1, lane, a);
+    if (item.r1 < 0) {  // piece of a long row (item.r0)
+      if (track && walk.to_row(p, item.r0, cols, ls, bs)) {
+        if (EPI == EPI_LOGREG) load_bias(p.bias + walk.d * p.ldb);
+        mw = mask_of(p, walk.d);
+      }
+      if (mw == 0) continue;  // the finalize skips the row too
+      row_dot_g<VT, XT, AT, G>(p, item.e0, item.e1, lane, a, cols_on(mw, lsh, CPL));
       AT* part = (AT*)p.partials + (i64)(-1 - item.r1) * NC;
 #pragma unroll
       for (int q = 0; q < QG; q++) part[cols[q]] = a[q];

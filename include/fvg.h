@@ -80,7 +80,10 @@ FVG_API fvg_status fvg_ctx_synchronize(fvg_ctx* ctx);
  * Names: "spmv_crs", "pass1", "pass2", "finalize", "lbfgs_vec", "transpose",
  * "spmv_ell", "spmv_jds", "spmv_hyb", "spmm", "pass1_f32", "pass2_f32"
  * ("pass1"/"pass2" are the training passes over FP64 or BF16 values, the
- * "_f32" keys those over FP32 values, e.g. after the refinement switch). */
+ * "_f32" keys those over FP32 values, e.g. after the refinement switch).
+ * "batch_evals" is a counter kept whether timing is on or not: *launches =
+ * evaluations run by the batched trainers since the context was created,
+ * *total_ms = the (dataset, model) evaluations inside them (a count). */
 FVG_API fvg_status fvg_ctx_set_profiling(fvg_ctx* ctx, int enable);
 FVG_API fvg_status fvg_ctx_get_profile(fvg_ctx* ctx, const char* name, double* total_ms, int64_t* launches);
 FVG_API fvg_status fvg_ctx_reset_profile(fvg_ctx* ctx);

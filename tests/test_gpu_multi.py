@@ -116,7 +116,14 @@ def test_multi_equals_separate_batched_runs(ctx):
     lams = np.logspace(-6, 0, 64)
     kw = dict(num_iter=10, reg_type="L2", intercept=True)
     w0 = [np.zeros(a.n) for a, _ in data]
+    e0 = ctx.profile("batch_evals")
     r = fv.logreg_lbfgs_multi(mats, [l for _, l in data], lams, w0=w0, **kw)
+    e1 = ctx.profile("batch_evals")
+    evals, model_evals = e1[1] - e0[1], e1[0] - e0[0]
+    # the initial evaluation and at least one trial per iteration; the later
+    # trials evaluate only the models still searching
+    assert evals >= kw["num_iter"] + 1
+    assert 3 * 64 * (kw["num_iter"] + 1) <= model_evals < evals * 3 * 64
     for d, (A, (a, label)) in enumerate(zip(mats, data)):
         rb = fv.logreg_lbfgs_batched(A, label, lams, w0=np.zeros(a.n), **kw)
         assert np.array_equal(r["n_iter"][d], rb["n_iter"])
