@@ -531,7 +531,7 @@ def regpath(args, datasets, iters):
         nnzs.append(int(off[-1]))
         del off, idx, val
     nd, k = len(mats), len(lams)
-    kw = dict(num_iter=iters, reg_type="L2", w0=[np.zeros(A.n) for A in mats])
+    kw = dict(num_iter=iters, reg_type="L2", hist_size=args.hist, w0=[np.zeros(A.n) for A in mats])
     fv.logreg_lbfgs_multi(mats, labels, lams, storage=storage, **dict(kw, num_iter=2))  # warm-up
     torch.cuda.synchronize()
     l0 = ctx.kernel_launches
@@ -577,7 +577,7 @@ def regpath(args, datasets, iters):
         for j in probe:
             t0 = time.perf_counter()
             rs = fv.logreg_lbfgs(A, labels[d], reg_param=lams[j], storage="f64", num_iter=iters, reg_type="L2",
-                                 w0=np.zeros(A.n))
+                                 hist_size=args.hist, w0=np.zeros(A.n))
             torch.cuda.synchronize()
             ts += time.perf_counter() - t0
             loss_err.append(abs(rb["loss"][d, j] - rs["loss"]) / abs(rs["loss"]))
@@ -792,6 +792,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cols", type=int, default=0, help="override the column count (profiling cases)")
     ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--hist", type=int, default=10, help="L-BFGS history size of the regularisation path")
     ap.add_argument("--storage", default="split", choices=["split", "bf16", "f32", "f64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--ref-iters", type=int, default=6, help="reference arm: iterations timed per step")
