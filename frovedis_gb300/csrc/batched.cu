@@ -17,7 +17,7 @@
 //
 // Vectors are row-major with the models as columns: dataset d owns rows
 // [doff[d], doff[d+1]) = its num_col weight rows and one bias row, ld = k
-// rounded up to 4 columns (16-byte rows for the products).  The per-model
+// rounded up to 8 columns (whole 32-byte lane groups for the products).  The per-model
 // reductions of the two-loop recursion run as column reductions: a CTA of 256
 // threads covers 256/kp rows x kp columns (kp = k rounded up to a power of
 // two), blockIdx.y is the dataset, and partial sums per (dataset, CTA,
@@ -861,7 +861,7 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
   const bool sw_any = std::any_of(sws_h.begin(), sws_h.end(), [](const double* x) { return x != nullptr; });
   const int h = (int)p->hist_size;
   const int kk = (int)k;
-  const int ld = (kk + 3) & ~3;
+  const int ld = (kk + 7) & ~7;  // whole 8-column groups of the products' lanes
   cudaStream_t s = c->stream;
 
   // layout: dataset d's matrix rows from roff[d], its vector rows from doff[d]

@@ -359,8 +359,8 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
 // (rows of dataset d: [seg_row[d], seg_row[d+1])): per-dataset intercepts
 // (bias + d * ldb) and loss / bias sums, out[2 * (d * ldo + j)] and
 // out[2 * (d * ldo + j) + 1]; the bias sums also land in gb[grow[d] * ldg +
-// j] (crs_spmm_seg_finish).  W, R and their strides must be 16-byte aligned
-// with kb a multiple of 4.  The whole pass does nothing while *gate == 0
+// j] (crs_spmm_seg_finish).  W, R 16-byte aligned, kb and the strides
+// multiples of 8.  The whole pass does nothing while *gate == 0
 // (gate may be null).
 struct SpmmSeg {
   int nseg = 0;
@@ -390,7 +390,8 @@ void crs_spmm_logreg_seg(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 
                          void* R, i64 ldr, void* scratch, SpmmSeg& sg, int loss = 0, double eps = 0.0);
 // The per-dataset sums of the pass (launch after the backward product).
 void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg);
-// Y = A X (FP64 Y) over stacked datasets with sg's row bounds, masks, gate.
+// Y = A X (FP64 Y) over stacked datasets with sg's row bounds, masks, gate
+// (the same alignment as crs_spmm_logreg_seg).
 void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
                         void* scratch, SpmmSeg& sg);
 

@@ -516,35 +516,54 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 // ------------------------------------------------ grouped lane layout
 // For the store and logistic epilogues with 16-byte aligned rows of X: lane
 // (group g, sub-lane s) of G groups of LPR = 32 / G lanes reads columns
-// s*CPL .. s*CPL+CPL-1 of a row of X with one 16-byte load (CPL = 4 FP32 or
-// 2 FP64 values), and group g takes nonzeros g, g+G, g+2G, ... of every
-// 32-entry chunk, so a warp gathers G rows of X per step.  At the end of a
-// row the groups' sums meet in a fixed butterfly that leaves lane (g, s)
-// with the QG = CPL / G columns s*CPL + g*QG ... of the row (reduce-scatter),
-// which it runs the epilogue on.  A launch covers NC = LPR * CPL columns;
-// pieces and the per-CTA partials use the column order of the finalize
-// kernel with NC / 32 columns a lane.  Each column's sum is the group sums
-// added in the butterfly's fixed order (deterministic; it differs from the
+// s*CPL .. s*CPL+CPL-1 of a row of X with 16-byte loads (CPL = 8 FP32
+// values, two loads, or 2 FP64 values, one), and group g takes nonzeros g,
+// g+G, g+2G, ... of every 32-entry chunk, so a warp gathers G rows of X per
+// step.  FP32 products are accumulated with packed two-lane FMAs
+// (fma.rn.f32x2: each half rounds like a scalar FMA).  At the end of a row
+// the groups' sums meet in a fixed butterfly that leaves lane (g, s) with the
+// QG = CPL / G columns s*CPL + g*QG ... of the row (reduce-scatter), which it
+// runs the epilogue on.  A launch covers NC = LPR * CPL columns; pieces and
+// the per-CTA partials use the column order of the finalize kernel with
+// NC / 32 columns a lane.  Each column's sum is the group sums added in the
+// butterfly's fixed order (deterministic; it differs from the
 // one-nonzero-at-a-time order only by rounding).
 template <class XT, int G> struct GLay {
-  static constexpr int CPL = 16 / (int)sizeof(XT);
+  static constexpr int CPL = sizeof(XT) == 4 ? 8 : 2;
   static constexpr int LPR = 32 / G;
   static constexpr int NC = LPR * CPL;
   static constexpr int QG = CPL / G;
-  static_assert(G >= 1 && G <= CPL, "groups per warp");
+  static_assert(G >= 1 && G <= CPL && NC <= 128, "groups per warp");
 };
+
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// acc = v * x + acc on both FP32 halves
+__device__ __forceinline__ void fma2(unsigned long long& acc, unsigned long long v, unsigned long long x) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(v), "l"(x));
+}
 
 template <class VT, class XT, class AT, int G>
 __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[GLay<XT, G>::CPL],
                                           bool lane_on = true) {
   using L = GLay<XT, G>;
   constexpr int CPL = L::CPL;
+  constexpr bool PACK = sizeof(XT) == 4 && sizeof(AT) == 4;
   const int sub = lane % L::LPR, grp = lane / L::LPR;
   const XT* X = (const XT*)p.X + sub * CPL;
   const VT* val = (const VT*)p.val;
   const bool mine = lane_on && sub * CPL < p.kb;
+  unsigned long long acc[CPL / 2];  // packed FP32 pairs
 #pragma unroll
   for (int q = 0; q < CPL; q++) a[q] = 0;
+#pragma unroll
+  for (int q = 0; q < CPL / 2; q++) acc[q] = 0ull;
   for (i32 e = e0; e < e1; e += 32) {
     const int cnt = min(32, e1 - e);
     i32 mi = 0;
@@ -559,11 +578,31 @@ __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int la
       const i32 col = __shfl_sync(0xffffffffu, mi, src & 31);
       const AT v = __shfl_sync(0xffffffffu, mv, src & 31);
       if (mine && src < cnt) {
-        XT x[CPL];
-        VecLd<XT, CPL>::ld(X + (i64)col * p.ldx, x);
+        if constexpr (PACK) {
+          const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(X + (i64)col * p.ldx);
+          const unsigned long long vv = pack2((float)v, (float)v);
 #pragma unroll
-        for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
+          for (int h = 0; h < CPL / 4; h++) {
+            const ulonglong2 x = __ldg(xr + h);
+            fma2(acc[2 * h], vv, x.x);
+            fma2(acc[2 * h + 1], vv, x.y);
+          }
+        } else {
+          XT x[CPL];
+          VecLd<XT, CPL>::ld(X + (i64)col * p.ldx, x);
+#pragma unroll
+          for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
+        }
       }
+    }
+  }
+  if constexpr (PACK) {
+#pragma unroll
+    for (int q = 0; q < CPL / 2; q++) {
+      float lo, hi;
+      unpack2(acc[q], lo, hi);
+      a[2 * q] = lo;
+      a[2 * q + 1] = hi;
     }
   }
   // reduce-scatter over the groups: at offset o the lane keeps the half of
@@ -857,27 +896,37 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
 template <class VT, class XT, class AT, class YT, int EPI>
 static bool launch_grouped(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const SpmmK& p, double* out,
                            double* gbias, char* scratch, SpmmSeg* sg = nullptr) {
-  constexpr int CPL = 16 / (int)sizeof(XT);
-  bool ok = p.kb % CPL == 0 && p.kb <= 32 * CPL && p.ldx % CPL == 0 && aligned_to(p.X, 16);
-  if (EPI == EPI_STORE) ok = ok && p.ldy % CPL == 0 && aligned_to(p.Y, 16);
-  else ok = ok && p.ldr % CPL == 0 && aligned_to(p.R, 16);
+  // 16-byte loads: column blocks in whole vectors, 4-element multiples of
+  // the strides (the FP32 lanes read 8 columns, the FP64 ones 2)
+  constexpr int VW = 16 / (int)sizeof(XT);
+  bool ok = p.kb % VW == 0 && p.ldx % VW == 0 && aligned_to(p.X, 16);
+  if (EPI == EPI_STORE) ok = ok && p.ldy % VW == 0 && aligned_to(p.Y, 16);
+  else ok = ok && p.ldr % VW == 0 && aligned_to(p.R, 16);
   if (!ok) return false;
-  if constexpr (CPL >= 4) {
-    if (p.kb <= 8 * CPL) {
+  if constexpr (sizeof(XT) == 4) {
+    // FP32: 8 columns a lane; the packed layout reads 32 bytes of a row, so
+    // the row stride must hold whole 8-column groups
+    if (p.kb % 8 != 0 || p.ldx % 8 != 0 || p.kb > 128) return false;
+    if (p.kb <= 32) {
+      launch_grouped_l<VT, XT, AT, YT, EPI, 8>(c, a, s, storage, p, out, gbias, scratch, sg);
+      return true;
+    }
+    if (p.kb <= 64) {
       launch_grouped_l<VT, XT, AT, YT, EPI, 4>(c, a, s, storage, p, out, gbias, scratch, sg);
       return true;
     }
-  }
-  if (p.kb <= 16 * CPL) {
-    launch_grouped_l<VT, XT, AT, YT, EPI, 2>(c, a, s, storage, p, out, gbias, scratch, sg);
+    // the logistic epilogue's finalize reduction takes at most 64 columns
+    if constexpr (EPI != EPI_LOGREG) {
+      launch_grouped_l<VT, XT, AT, YT, EPI, 2>(c, a, s, storage, p, out, gbias, scratch, sg);
+      return true;
+    }
+    return false;
+  } else {
+    if (p.kb > 64) return false;
+    if (p.kb <= 32) launch_grouped_l<VT, XT, AT, YT, EPI, 2>(c, a, s, storage, p, out, gbias, scratch, sg);
+    else launch_grouped_l<VT, XT, AT, YT, EPI, 1>(c, a, s, storage, p, out, gbias, scratch, sg);
     return true;
   }
-  // the logistic epilogue's finalize reduction takes at most 64 columns
-  if constexpr (EPI != EPI_LOGREG || 32 * CPL <= 64) {
-    launch_grouped_l<VT, XT, AT, YT, EPI, 1>(c, a, s, storage, p, out, gbias, scratch, sg);
-    return true;
-  }
-  return false;
 }
 
 // Packed lane layout when every access it makes is aligned: the block's
@@ -942,7 +991,7 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
 // Y = A X over stacked datasets (rows [seg_row[d], seg_row[d+1]) of A belong
 // to dataset d) with the column masks and the gate of sg; masked columns of
 // Y keep what they held.  X, Y and their strides 16-byte aligned, kb a
-// multiple of 4 (of 2 for FP64) and at most 64.
+// multiple of 8 (of 2 for FP64) and at most 64.
 void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
                         void* scratch, SpmmSeg& sg) {
   if (kb < 1 || kb > 64 || sg.nseg < 1) fail(FVG_ERR_INTERNAL, "stacked store: block width or datasets out of range");
