@@ -157,12 +157,12 @@ __device__ __forceinline__ void row_dot(const SpmmK& p, i32 e0, i32 e1, int lane
       if constexpr (VEC) {
         if (mine) {
           XT x[CPL];
-          VecLd<XT, CPL>::ld(X + (i64)col * p.ldx + lane * CPL, x);
+          VecLd<XT, CPL>::ld(X + (long long)col * (int)p.ldx + lane * CPL, x);
 #pragma unroll
           for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
         }
       } else {
-        const XT* xr = X + (i64)col * p.ldx + lane;
+        const XT* xr = X + (long long)col * (int)p.ldx + lane;
 #pragma unroll
         for (int q = 0; q < CPL; q++)
           if (lane + 32 * q < p.kb) a[q] += v * (AT)__ldg(xr + 32 * q);
@@ -557,6 +557,8 @@ __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int la
   constexpr bool PACK = sizeof(XT) == 4 && sizeof(AT) == 4;
   const int sub = lane % L::LPR, grp = lane / L::LPR;
   const XT* X = (const XT*)p.X + sub * CPL;
+  const XT* X0 = (const XT*)p.X;
+  const int ldx = (int)p.ldx;  // a row stride of X fits 32 bits: one 32 x 32 -> 64-bit multiply per gather
   const VT* val = (const VT*)p.val;
   const bool mine = lane_on && sub * CPL < p.kb;
   unsigned long long acc[CPL / 2];  // packed FP32 pairs
@@ -572,27 +574,31 @@ __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int la
       mi = __ldcs(p.idx + e + lane);
       mv = ld_val<VT, AT>(val + e + lane);
     }
+    // lanes without a nonzero (past the chunk, masked or unused columns)
+    // multiply 0 by the first CPL entries of X (always inside X, finite,
+    // cached) instead of branching: the warp's control flow stays uniform
 #pragma unroll 4
     for (int t = 0; t < cnt; t += G) {
       const int src = t + grp;
       const i32 col = __shfl_sync(0xffffffffu, mi, src & 31);
-      const AT v = __shfl_sync(0xffffffffu, mv, src & 31);
-      if (mine && src < cnt) {
-        if constexpr (PACK) {
-          const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(X + (i64)col * p.ldx);
-          const unsigned long long vv = pack2((float)v, (float)v);
+      const AT v0 = __shfl_sync(0xffffffffu, mv, src & 31);
+      const bool act = mine && src < cnt;
+      const AT v = act ? v0 : (AT)0;
+      const XT* xp = act ? X + (long long)col * ldx : X0;
+      if constexpr (PACK) {
+        const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(xp);
+        const unsigned long long vv = pack2((float)v, (float)v);
 #pragma unroll
-          for (int h = 0; h < CPL / 4; h++) {
-            const ulonglong2 x = __ldg(xr + h);
-            fma2(acc[2 * h], vv, x.x);
-            fma2(acc[2 * h + 1], vv, x.y);
-          }
-        } else {
-          XT x[CPL];
-          VecLd<XT, CPL>::ld(X + (i64)col * p.ldx, x);
-#pragma unroll
-          for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
+        for (int h = 0; h < CPL / 4; h++) {
+          const ulonglong2 x = __ldg(xr + h);
+          fma2(acc[2 * h], vv, x.x);
+          fma2(acc[2 * h + 1], vv, x.y);
         }
+      } else {
+        XT x[CPL];
+        VecLd<XT, CPL>::ld(xp, x);
+#pragma unroll
+        for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
       }
     }
   }
@@ -963,6 +969,7 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
   SpmmK p = {};
   p.X = X;
   p.ldx = ldx;
+  if (ldx > 0x7fffffffll) fail(FVG_ERR_INVALID_ARG, "dense operand row stride beyond 2^31 - 1");
   p.kb = kb;
   p.Y = Y;
   p.ldy = ldy;
@@ -1000,6 +1007,7 @@ void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 l
   SpmmK p = {};
   p.X = X;
   p.ldx = ldx;
+  if (ldx > 0x7fffffffll) fail(FVG_ERR_INVALID_ARG, "dense operand row stride beyond 2^31 - 1");
   p.kb = kb;
   p.Y = Y;
   p.ldy = ldy;
@@ -1026,6 +1034,7 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
   SpmmK p = {};
   p.X = W;
   p.ldx = ldw;
+  if (ldw > 0x7fffffffll) fail(FVG_ERR_INVALID_ARG, "dense operand row stride beyond 2^31 - 1");
   p.kb = kb;
   p.label = label;
   p.sw = sw;
@@ -1066,6 +1075,7 @@ void crs_spmm_logreg_seg(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 
   SpmmK p = {};
   p.X = W;
   p.ldx = ldw;
+  if (ldw > 0x7fffffffll) fail(FVG_ERR_INVALID_ARG, "dense operand row stride beyond 2^31 - 1");
   p.kb = kb;
   p.label = label;
   p.sw = sw;
@@ -1120,6 +1130,7 @@ void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw
   SpmmK p = {};
   p.X = W;
   p.ldx = ldw;
+  if (ldw > 0x7fffffffll) fail(FVG_ERR_INVALID_ARG, "dense operand row stride beyond 2^31 - 1");
   p.kb = K;
   p.label = label;
   p.sw = sw;
