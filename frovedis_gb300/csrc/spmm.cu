@@ -549,16 +549,22 @@ __device__ __forceinline__ void fma2(unsigned long long& acc, unsigned long long
   asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(v), "l"(x));
 }
 
+// A chunk of 32 entries staged for the warp: the row offset of the gathered
+// row of X (column id x stride) and the value, zero past the chunk's end.
+template <class AT> struct alignas(16) StageE {
+  long long off;
+  AT v;
+};
+
 template <class VT, class XT, class AT, int G>
 __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int lane, AT (&a)[GLay<XT, G>::CPL],
-                                          bool lane_on = true) {
+                                          StageE<AT>* st, bool lane_on = true) {
   using L = GLay<XT, G>;
   constexpr int CPL = L::CPL;
   constexpr bool PACK = sizeof(XT) == 4 && sizeof(AT) == 4;
   const int sub = lane % L::LPR, grp = lane / L::LPR;
   const XT* X = (const XT*)p.X + sub * CPL;
-  const XT* X0 = (const XT*)p.X;
-  const int ldx = (int)p.ldx;  // a row stride of X fits 32 bits: one 32 x 32 -> 64-bit multiply per gather
+  const int ldx = (int)p.ldx;  // a row stride of X fits 32 bits
   const VT* val = (const VT*)p.val;
   const bool mine = lane_on && sub * CPL < p.kb;
   unsigned long long acc[CPL / 2];  // packed FP32 pairs
@@ -568,37 +574,41 @@ __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int la
   for (int q = 0; q < CPL / 2; q++) acc[q] = 0ull;
   for (i32 e = e0; e < e1; e += 32) {
     const int cnt = min(32, e1 - e);
-    i32 mi = 0;
-    AT mv = 0;
+    // stage the chunk (offsets computed once per entry); the padding
+    // entries (offset 0, value 0) round the chunk up to whole steps
+    StageE<AT> se;
+    se.off = 0;
+    se.v = 0;
     if (lane < cnt) {
-      mi = __ldcs(p.idx + e + lane);
-      mv = ld_val<VT, AT>(val + e + lane);
+      se.off = (long long)__ldcs(p.idx + e + lane) * ldx;
+      se.v = ld_val<VT, AT>(val + e + lane);
     }
-    // lanes without a nonzero (past the chunk, masked or unused columns)
-    // multiply 0 by the first CPL entries of X (always inside X, finite,
-    // cached) instead of branching: the warp's control flow stays uniform
+    __syncwarp();
+    st[lane] = se;
+    __syncwarp();
+    // group grp takes entries grp, grp + G, ...; lanes whose columns are
+    // not computed skip the chunk
+    if (mine) {
+      const int steps = (cnt + G - 1) / G;
 #pragma unroll 4
-    for (int t = 0; t < cnt; t += G) {
-      const int src = t + grp;
-      const i32 col = __shfl_sync(0xffffffffu, mi, src & 31);
-      const AT v0 = __shfl_sync(0xffffffffu, mv, src & 31);
-      const bool act = mine && src < cnt;
-      const AT v = act ? v0 : (AT)0;
-      const XT* xp = act ? X + (long long)col * ldx : X0;
-      if constexpr (PACK) {
-        const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(xp);
-        const unsigned long long vv = pack2((float)v, (float)v);
+      for (int k = 0; k < steps; k++) {
+        const StageE<AT> t = st[k * G + grp];
+        const XT* xp = X + t.off;
+        if constexpr (PACK) {
+          const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(xp);
+          const unsigned long long vv = pack2((float)t.v, (float)t.v);
 #pragma unroll
-        for (int h = 0; h < CPL / 4; h++) {
-          const ulonglong2 x = __ldg(xr + h);
-          fma2(acc[2 * h], vv, x.x);
-          fma2(acc[2 * h + 1], vv, x.y);
+          for (int h = 0; h < CPL / 4; h++) {
+            const ulonglong2 x = __ldg(xr + h);
+            fma2(acc[2 * h], vv, x.x);
+            fma2(acc[2 * h + 1], vv, x.y);
+          }
+        } else {
+          XT x[CPL];
+          VecLd<XT, CPL>::ld(xp, x);
+#pragma unroll
+          for (int q = 0; q < CPL; q++) a[q] += t.v * (AT)x[q];
         }
-      } else {
-        XT x[CPL];
-        VecLd<XT, CPL>::ld(xp, x);
-#pragma unroll
-        for (int q = 0; q < CPL; q++) a[q] += v * (AT)x[q];
       }
     }
   }
@@ -650,6 +660,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   Sum ls[QG], bs[QG];
   SegWalk<AT, QG> walk(p, seg ? p.seg_part : nullptr, gw, nw, NC);
   const int lsh = (lane % L::LPR) * CPL;  // the lane's gathered columns: lsh .. lsh + CPL - 1
+  __shared__ StageE<AT> stage[kThreads / 32][32];
   unsigned long long mw = mask_of(p, 0);
   AT lab = 0, w = 1;
   for (i64 it = gw; it < p.nitems; it += nw) {
@@ -661,7 +672,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
         mw = mask_of(p, walk.d);
       }
       if (mw == 0) continue;  // the finalize skips the row too
-      row_dot_g<VT, XT, AT, G>(p, item.e0, item.e1, lane, a, cols_on(mw, lsh, CPL));
+      row_dot_g<VT, XT, AT, G>(p, item.e0, item.e1, lane, a, stage[wib], cols_on(mw, lsh, CPL));
       AT* part = (AT*)p.partials + (i64)(-1 - item.r1) * NC;
 #pragma unroll
       for (int q = 0; q < QG; q++) part[cols[q]] = a[q];
@@ -673,7 +684,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
         mw = mask_of(p, walk.d);
       }
       if (mw == 0) continue;  // no column of this dataset is computed
-      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a, cols_on(mw, lsh, CPL));
+      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a, stage[wib], cols_on(mw, lsh, CPL));
       if constexpr (EPI == EPI_STORE) {
         YT* y = (YT*)p.Y + (i64)r * p.ldy;
 #pragma unroll
