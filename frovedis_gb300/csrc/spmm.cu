@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   AT b[QG];
   auto load_bias = [&](const double* bias) {
 #pragma unroll
-    for (int q = 0; q < QG; q++) b[q] = (EPI == EPI_LOGREG && p.icpt && cols[q] < p.kb) ? (AT)bias[cols[q]] : (AT)0;
+    for (int q = 0; q < QG; q++) b[q] = (EPI != EPI_STORE && p.icpt && cols[q] < p.kb) ? (AT)bias[cols[q]] : (AT)0;
   };
   load_bias(p.bias);
   Sum ls[QG], bs[QG];
@@ -702,21 +702,60 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
           if (has_sw) w = p.sw_f[r];
         }
         AT* rr = (AT*)p.R + (i64)r * p.ldr;
+        if constexpr (EPI == EPI_LOGREG) {
 #pragma unroll
-        for (int q = 0; q < QG; q++) {
-          if (cols[q] >= p.kb || !col_on(mw, cols[q])) continue;
-          AT loss, d;
-          glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
-          if (has_sw) d = d * w;
-          rr[cols[q]] = d;
-          ls[q].add(loss);
-          bs[q].add(d);
+          for (int q = 0; q < QG; q++) {
+            if (cols[q] >= p.kb || !col_on(mw, cols[q])) continue;
+            AT loss, d;
+            glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
+            if (has_sw) d = d * w;
+            rr[cols[q]] = d;
+            ls[q].add(loss);
+            bs[q].add(d);
+          }
+        } else {  // softmax over the row's classes, every class held by one lane
+          const bool has_label = (sizeof(AT) == 8) ? p.label != nullptr : p.label_f != nullptr;
+          AT z[QG], mx = -INFINITY;
+#pragma unroll
+          for (int q = 0; q < QG; q++) {
+            z[q] = a[q] + b[q];
+            if (cols[q] < p.kb) mx = fmax(mx, z[q]);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+          AT zy = 0, sum = 0;
+#pragma unroll
+          for (int q = 0; q < QG; q++) {
+            if (has_label && cols[q] < p.kb && lab == (AT)cols[q]) zy = z[q] - mx;
+            z[q] = cols[q] < p.kb ? exp_acc<AT>(z[q] - mx) : (AT)0;
+            sum += z[q];
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+          // cross-entropy -log p[label] = log(sum) - (z_label - max), unweighted
+          if (has_label && p.cta_part) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) zy += __shfl_xor_sync(0xffffffffu, zy, o);
+            if (lane == 0) ls[0].add(log_acc<AT>(sum) - zy);
+          }
+          const AT inv = (AT)1 / sum;
+#pragma unroll
+          for (int q = 0; q < QG; q++) {
+            if (cols[q] >= p.kb) continue;
+            AT pr = inv * z[q];
+            if (has_label) {
+              pr -= (lab == (AT)cols[q]) ? (AT)1 : (AT)0;
+              if (has_sw) pr *= w;
+            }
+            rr[cols[q]] = pr;
+          }
         }
       }
     }
   }
   if (track && !seg) return;
-  if constexpr (EPI == EPI_LOGREG) {
+  if constexpr (EPI == EPI_LOGREG || EPI == EPI_SOFTMAX) {
+    if (EPI == EPI_SOFTMAX && !p.cta_part) return;
     if (seg) {
       walk.finish(p, cols, ls, bs);
       return;
@@ -863,7 +902,9 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
   p.val = a.val[storage].p;
   p.items = s.items.as<Item>();
   p.nitems = s.nitems;
-  p.cta_part = EPI == EPI_LOGREG ? cta : nullptr;
+  // softmax: the cross-entropy is reduced only when the caller asks for it
+  const bool reduce = EPI == EPI_LOGREG || (EPI == EPI_SOFTMAX && out);
+  p.cta_part = reduce ? cta : nullptr;
   const bool track = sg && sg->nseg > 0;
   const bool seg = EPI == EPI_LOGREG && track;
   const i64 nw1 = (i64)grid * (kThreads / 32), nw2 = (i64)fg * (kThreads / 32);
@@ -885,7 +926,7 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
     check_launch("k_spmm_g");
     count_launch(c);
   }
-  if (s.nlong > 0 || EPI == EPI_LOGREG) {
+  if (s.nlong > 0 || reduce) {
     SpmmFin f;
     f.k = p;
     f.long_rows = s.long_rows.as<i32>();
@@ -1153,12 +1194,15 @@ void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw
   p.ldr = ldp;
   char* sc = (char*)scratch;
   FVG_CUDA(cudaMemsetAsync(sc, 0, 256, c->stream));
-  if (storage == FVG_F64)
-    launch_spmm<double, double, double, double, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
-  else if (storage == FVG_F32)
-    launch_spmm<float, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
-  else
+  if (storage == FVG_F64) {
+    if (!launch_grouped<double, double, double, double, EPI_SOFTMAX>(c, a, s, storage, p, loss_out, nullptr, sc))
+      launch_spmm<double, double, double, double, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
+  } else if (storage == FVG_F32) {
+    if (!launch_grouped<float, float, float, float, EPI_SOFTMAX>(c, a, s, storage, p, loss_out, nullptr, sc))
+      launch_spmm<float, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
+  } else if (!launch_grouped<bf16, float, float, float, EPI_SOFTMAX>(c, a, s, storage, p, loss_out, nullptr, sc)) {
     launch_spmm<bf16, float, float, float, EPI_SOFTMAX, 4>(c, a, s, storage, p, loss_out, nullptr, sc);
+  }
 }
 
 // Y = A X, X row-major num_col x k, Y row-major num_row x k, in blocks of 128
