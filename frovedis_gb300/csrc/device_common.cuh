@@ -106,6 +106,21 @@ __device__ __forceinline__ void logistic_row(float wtx, float lab, float& loss, 
   else if (d < -1e12f) d = -1e12f;
 }
 
+// The FP32 logistic row of the multi-model products with one exponential:
+// e = exp(-|z|), 1 / (1 + exp(z)) = (z > 0 ? e : 1) / (1 + e) and
+// log(1 + exp(-z)) = max(-z, 0) + log1p(e).  Every branch of
+// gradient.hpp:24-50 is the same function: beyond |z| = 18 the reference's
+// e and -z differ from these forms by less than e / 2 relative (below FP32
+// resolution), so the result differs from logistic_row(float) by rounding.
+__device__ __forceinline__ void logistic_row_1exp(float wtx, float lab, float& loss, float& d) {
+  const float z = lab * wtx;
+  const float e = expf(-fabsf(z));
+  loss = fmaxf(-z, 0.0f) + log1pf(e);
+  d = -lab * __fdividef(z > 0.0f ? e : 1.0f, 1.0f + e);
+  if (d > 1e12f) d = 1e12f;
+  else if (d < -1e12f) d = -1e12f;
+}
+
 // ------------------------------------------------------ GLM loss kinds
 // compute_dloss of the GLM family for one row (ml/glm/gradient.hpp):
 // 0 logistic_gradient, 1 linear_gradient (55-87), 2 hinge_gradient

@@ -707,7 +707,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
           for (int q = 0; q < QG; q++) {
             if (cols[q] >= p.kb || !col_on(mw, cols[q])) continue;
             AT loss, d;
-            glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
+            if constexpr (sizeof(AT) == 4) {
+              if (p.loss == LOSS_LOGISTIC) logistic_row_1exp(a[q] + b[q], lab, loss, d);
+              else glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
+            } else {
+              glm_row<AT>(p.loss, (AT)p.eps, a[q] + b[q], lab, loss, d);
+            }
             if (has_sw) d = d * w;
             rr[cols[q]] = d;
             ls[q].add(loss);
