@@ -691,15 +691,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
         for (int q = 0; q < QG; q++)
           if (cols[q] < p.kb && col_on(mw, cols[q])) y[cols[q]] = (YT)a[q];
       } else {
-        bool has_sw;
-        if constexpr (sizeof(AT) == 8) {
-          lab = p.label[r];
-          has_sw = p.sw != nullptr;
-          if (has_sw) w = p.sw[r];
-        } else {
-          lab = p.label_f[r];
-          has_sw = p.sw_f != nullptr;
-          if (has_sw) w = p.sw_f[r];
+        // labels: always with the logistic epilogue; the softmax one runs
+        // without them for the probability matrix alone
+        const bool has_label = (sizeof(AT) == 8) ? p.label != nullptr : p.label_f != nullptr;
+        bool has_sw = false;
+        if (has_label) {
+          if constexpr (sizeof(AT) == 8) {
+            lab = p.label[r];
+            has_sw = p.sw != nullptr;
+            if (has_sw) w = p.sw[r];
+          } else {
+            lab = p.label_f[r];
+            has_sw = p.sw_f != nullptr;
+            if (has_sw) w = p.sw_f[r];
+          }
         }
         AT* rr = (AT*)p.R + (i64)r * p.ldr;
         if constexpr (EPI == EPI_LOGREG) {
@@ -719,7 +724,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
             bs[q].add(d);
           }
         } else {  // softmax over the row's classes, every class held by one lane
-          const bool has_label = (sizeof(AT) == 8) ? p.label != nullptr : p.label_f != nullptr;
           AT z[QG], mx = -INFINITY;
 #pragma unroll
           for (int q = 0; q < QG; q++) {
