@@ -788,32 +788,34 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
 
 // Stacked datasets: loss / bias sums of dataset blockIdx.x from the warp
 // slots of the main kernel (nw1 warps) and the finalize kernel (nw2), each
-// in warp order: 1024 threads = (column, quantity) pairs x stripes, stripe
-// s adds warps s, s + S, ...; the stripes are added in order.  out[2 * (d *
-// ldo + col) + q]; the bias sums also go to gb[grow[d] * ldg + col].
+// in warp order.  A CTA of 1024 threads takes 32 (column, quantity) pairs
+// (blockIdx.y: which 32) x 32 stripes; stripe s adds warps s, s + 32, ...;
+// the stripes are added in order.  out[2 * (d * ldo + col) + q]; the bias
+// sums also go to gb[grow[d] * ldg + col].
 template <int NC>
 __global__ void __launch_bounds__(1024) k_spmm_seg_reduce(const double* __restrict__ s1, i64 nw1,
                                                           const double* __restrict__ s2, i64 nw2, int kout, int icpt,
                                                           double* __restrict__ out, i64 ldo, double* __restrict__ gb,
                                                           const i64* __restrict__ grow, i64 ldg, const int* gate,
                                                           const unsigned long long* mask, i64 mstride, int mword) {
-  constexpr int P = 2 * NC, S = 1024 / P;
-  static_assert(1024 % P == 0, "pairs per CTA");
-  __shared__ double part[S][P];
+  constexpr int P = 2 * NC, S = 32;
+  static_assert(P % 32 == 0, "pairs per CTA");
+  __shared__ double part[S][33];
   if (gated_off(gate)) return;
   const int d = blockIdx.x;
-  const int pr = threadIdx.x % P, st = threadIdx.x / P;
+  const int pl = threadIdx.x & 31, st = threadIdx.x >> 5;
+  const int pr = blockIdx.y * 32 + pl;
   CSum t;
   const double* b1 = s1 + (i64)d * nw1 * P;
   for (i64 w = st; w < nw1; w += S) t.add(__ldcg(b1 + w * P + pr));
   const double* b2 = s2 + (i64)d * nw2 * P;
   for (i64 w = st; w < nw2; w += S) t.add(__ldcg(b2 + w * P + pr));
-  part[st][pr] = t.total();
+  part[st][pl] = t.total();
   __syncthreads();
   if (st != 0) return;
   double tot = 0.0;
 #pragma unroll
-  for (int q = 0; q < S; q++) tot += part[q][pr];
+  for (int q = 0; q < S; q++) tot += part[q][pl];
   const int col = pr >> 1, qq = pr & 1;
   if (col >= kout) return;
   if (mask && !col_on(__ldcg(mask + (i64)d * mstride + mword), col)) return;  // not evaluated: keep
@@ -1165,15 +1167,15 @@ void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg) {
   if (sg.nw1 <= 0) fail(FVG_ERR_INTERNAL, "stacked-dataset reduction without its pass");
   const double* s2 = sg.slots + (i64)sg.nseg * sg.nw1 * sg.nc * 2;
   if (sg.nc == 32)
-    k_spmm_seg_reduce<32><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+    k_spmm_seg_reduce<32><<<dim3(sg.nseg, 2), 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
                                                            sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
                                                            sg.mstride, sg.mword);
   else if (sg.nc == 64)
-    k_spmm_seg_reduce<64><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+    k_spmm_seg_reduce<64><<<dim3(sg.nseg, 4), 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
                                                            sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
                                                            sg.mstride, sg.mword);
   else
-    k_spmm_seg_reduce<128><<<sg.nseg, 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
+    k_spmm_seg_reduce<128><<<dim3(sg.nseg, 8), 1024, 0, c->stream>>>(sg.slots, sg.nw1, s2, sg.nw2, sg.kout, sg.icpt, sg.out,
                                                             sg.ldo, sg.gb, sg.grow, sg.ldg, sg.gate, sg.mask,
                                                            sg.mstride, sg.mword);
   check_launch("k_spmm_seg_reduce");
