@@ -359,8 +359,8 @@ void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i6
 // (rows of dataset d: [seg_row[d], seg_row[d+1])): per-dataset intercepts
 // (bias + d * ldb) and loss / bias sums, out[2 * (d * ldo + j)] and
 // out[2 * (d * ldo + j) + 1]; the bias sums also land in gb[grow[d] * ldg +
-// j] (crs_spmm_seg_finish).  W, R 16-byte aligned, kb and the strides
-// multiples of 8.  The whole pass does nothing while *gate == 0
+// j] (crs_spmm_seg_finish).  W (32-byte aligned for FP32) and R 16-byte
+// aligned, kb and the strides multiples of 8.  The whole pass does nothing while *gate == 0
 // (gate may be null).
 struct SpmmSeg {
   int nseg = 0;

@@ -514,10 +514,10 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fin(const SpmmFin f) {
 }
 
 // ------------------------------------------------ grouped lane layout
-// For the store and logistic epilogues with 16-byte aligned rows of X: lane
+// For the store, logistic and softmax epilogues with aligned rows of X: lane
 // (group g, sub-lane s) of G groups of LPR = 32 / G lanes reads columns
-// s*CPL .. s*CPL+CPL-1 of a row of X with 16-byte loads (CPL = 8 FP32
-// values, two loads, or 2 FP64 values, one), and group g takes nonzeros g,
+// s*CPL .. s*CPL+CPL-1 of a row of X with one load (CPL = 8 FP32 values,
+// 32 bytes, or 2 FP64 values, 16 bytes), and group g takes nonzeros g,
 // g+G, g+2G, ... of every 32-entry chunk, so a warp gathers G rows of X per
 // step.  FP32 products are accumulated with packed two-lane FMAs
 // (fma.rn.f32x2: each half rounds like a scalar FMA).  At the end of a row
@@ -595,14 +595,17 @@ __device__ __forceinline__ void row_dot_g(const SpmmK& p, i32 e0, i32 e1, int la
         const StageE<AT> t = st[k * G + grp];
         const XT* xp = X + t.off;
         if constexpr (PACK) {
-          const ulonglong2* xr = reinterpret_cast<const ulonglong2*>(xp);
+          // the lane's 8 FP32 columns in one 32-byte load, as 4 packed pairs
+          static_assert(CPL == 8, "one 32-byte load a lane");
+          unsigned long long x0, x1, x2, x3;
+          asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
+              : "=l"(x0), "=l"(x1), "=l"(x2), "=l"(x3)
+              : "l"(xp));
           const unsigned long long vv = pack2((float)t.v, (float)t.v);
-#pragma unroll
-          for (int h = 0; h < CPL / 4; h++) {
-            const ulonglong2 x = __ldg(xr + h);
-            fma2(acc[2 * h], vv, x.x);
-            fma2(acc[2 * h + 1], vv, x.y);
-          }
+          fma2(acc[0], vv, x0);
+          fma2(acc[1], vv, x1);
+          fma2(acc[2], vv, x2);
+          fma2(acc[3], vv, x3);
         } else {
           XT x[CPL];
           VecLd<XT, CPL>::ld(xp, x);
@@ -965,17 +968,17 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
 template <class VT, class XT, class AT, class YT, int EPI>
 static bool launch_grouped(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, const SpmmK& p, double* out,
                            double* gbias, char* scratch, SpmmSeg* sg = nullptr) {
-  // 16-byte loads: column blocks in whole vectors, 4-element multiples of
-  // the strides (the FP32 lanes read 8 columns, the FP64 ones 2)
+  // vector loads: column blocks and strides in whole vectors (the FP32
+  // lanes read 8 columns, the FP64 ones 2), 16-byte aligned bases
   constexpr int VW = 16 / (int)sizeof(XT);
   bool ok = p.kb % VW == 0 && p.ldx % VW == 0 && aligned_to(p.X, 16);
   if (EPI == EPI_STORE) ok = ok && p.ldy % VW == 0 && aligned_to(p.Y, 16);
   else ok = ok && p.ldr % VW == 0 && aligned_to(p.R, 16);
   if (!ok) return false;
   if constexpr (sizeof(XT) == 4) {
-    // FP32: 8 columns a lane; the packed layout reads 32 bytes of a row, so
-    // the row stride must hold whole 8-column groups
-    if (p.kb % 8 != 0 || p.ldx % 8 != 0 || p.kb > 128) return false;
+    // FP32: 8 columns a lane read with one 32-byte load: whole 8-column
+    // groups, 32-byte aligned rows
+    if (p.kb % 8 != 0 || p.ldx % 8 != 0 || p.kb > 128 || !aligned_to(p.X, 32)) return false;
     if (p.kb <= 32) {
       launch_grouped_l<VT, XT, AT, YT, EPI, 8>(c, a, s, storage, p, out, gbias, scratch, sg);
       return true;
