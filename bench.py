@@ -53,8 +53,9 @@ TRAFFIC_SOURCE = {"bf16": "ncu dram bytes / algorithmic bytes per pass (1/10-row
                   "f32": "ncu dram bytes / algorithmic bytes per pass (full-size capture), x this run's "
                          "algorithmic bytes per launch"}
 PASS_KERNELS = {
-    "split": "pass1 A*w: k_crs_split (df64 products, rows as FP32 pairs) + k_fin_split + k_glm_split "
-             "(df64 logistic rows); pass2 A^T*r: k_crs_split on the transposed copy + k_fin_split",
+    "split": "pass1 A*w: forward head k_panel_split (the frequent columns' w as FP32 pairs in shared memory) + "
+             "k_crs_split over the row tails + k_fin_split + k_glm_split (df64 logistic rows); pass2 A^T*r: row "
+             "panels k_panel_split + k_panel_colsum_split + k_crs_split over the rare columns + k_fin_split",
     "bf16": "pass1 A*w: k_panel (forward head) + k_crs (row tails, logistic epilogue); pass2 A^T*r: k_panel "
             "(row panels) + k_crs (rare columns) + k_panel_colsum",
     "f32": "as bf16, FP32 values",
