@@ -46,9 +46,12 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # row panels (rare-column k_crs + k_panel + k_panel_colsum) 288.54 MB /
 # 376.01 MB.  FP32 values, full size: pass 1 4060.5 MB / 4964.0 MB, pass 2
 # 4150.6 MB / 4852.0 MB.
-NCU_TRAFFIC_RATIO = {"bf16": {"pass1": 285.42 / 380.01, "pass2": 288.54 / 376.01},
+NCU_TRAFFIC_RATIO = {"split": {"pass1": 532.6 / 620.81, "pass2": 529.5 / 609.21},
+                     "bf16": {"pass1": 285.42 / 380.01, "pass2": 288.54 / 376.01},
                      "f32": {"pass1": 4060.5 / 4964.0, "pass2": 4150.6 / 4852.0}}
-TRAFFIC_SOURCE = {"bf16": "ncu dram bytes / algorithmic bytes per pass (1/10-row capture), x this run's "
+TRAFFIC_SOURCE = {"split": "ncu dram bytes of every kernel of a pass / algorithmic bytes per pass (1/10-row "
+                           "capture, all columns), x this run's algorithmic bytes per launch",
+                  "bf16": "ncu dram bytes / algorithmic bytes per pass (1/10-row capture), x this run's "
                           "algorithmic bytes per launch",
                   "f32": "ncu dram bytes / algorithmic bytes per pass (full-size capture), x this run's "
                          "algorithmic bytes per launch"}

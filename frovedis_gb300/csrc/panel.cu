@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
 // most kSplitTile entries, so that one item is one pass of 32 lanes x
 // kSplitChunk entries: no products are staged and no second pass re-reads
 // them.
-constexpr int kSplitWarps = 12;
+constexpr int kSplitWarps = 16;
 constexpr int kSplitTile = 480;  // an item's staged copy (8-aligned ends) fits 32 lanes x 16 entries
 constexpr int kSplitChunk = 16;  // entries per lane
 struct SplitSmem {
