@@ -38,7 +38,6 @@
 // once any model's gradient norm stalls.
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <vector>
 
 #include "fvg_internal.cuh"
@@ -663,11 +662,12 @@ void shift_copy(fvg_ctx* c, const i32* src, i64 n, i64 add, i32* dst) {
   count_launch(c);
 }
 
-// Block-diagonal stack of the datasets' matrices: the rows of all datasets,
-// column ids shifted by each dataset's first vector row, with the value
-// planes `planes`.
+// Block-diagonal stack of the datasets' matrices (A: rows of all datasets,
+// column ids shifted by each dataset's first vector row; AT: the vector rows
+// of all datasets, each dataset's bias row empty, column ids shifted by its
+// first matrix row), with the value planes `planes`.
 void stack_datasets(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const std::vector<i64>& doff,
-                    const std::vector<i64>& roff, const std::vector<int>& planes, DevCRS& A) {
+                    const std::vector<i64>& roff, const std::vector<int>& planes, DevCRS& A, DevCRS& AT) {
   const int nd = (int)mats.size();
   cudaStream_t s = c->stream;
   i64 nnz = 0;
@@ -677,73 +677,62 @@ void stack_datasets(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const std:
   A.m = roff[nd];
   A.n = doff[nd];
   A.nnz = nnz;
-  A.off.alloc(sizeof(i32) * (A.m + 1), s);
-  A.idx.alloc(sizeof(i32) * (nnz + kPad), s);
-  FVG_CUDA(cudaMemsetAsync(A.idx.as<i32>() + nnz, 0, sizeof(i32) * kPad, s));
-  for (int dt : planes) {
-    A.val[dt].alloc((size_t)(nnz + kPad) * dtype_size(dt), s);
-    FVG_CUDA(cudaMemsetAsync((char*)A.val[dt].p + (size_t)nnz * dtype_size(dt), 0, (size_t)kPad * dtype_size(dt), s));
+  AT.m = doff[nd];
+  AT.n = roff[nd];
+  AT.nnz = nnz;
+  for (DevCRS* X : {&A, &AT}) {
+    X->off.alloc(sizeof(i32) * (X->m + 1), s);
+    X->idx.alloc(sizeof(i32) * (nnz + kPad), s);
+    FVG_CUDA(cudaMemsetAsync(X->idx.as<i32>() + nnz, 0, sizeof(i32) * kPad, s));
+    for (int dt : planes) {
+      X->val[dt].alloc((size_t)(nnz + kPad) * dtype_size(dt), s);
+      FVG_CUDA(cudaMemsetAsync((char*)X->val[dt].p + (size_t)nnz * dtype_size(dt), 0, (size_t)kPad * dtype_size(dt), s));
+    }
   }
   i64 base = 0;
   for (int d = 0; d < nd; d++) {
     DevCRS& a = mats[d]->A;
-    // rows roff[d] .. roff[d] + m_d (the last entry is rewritten by the next
-    // dataset with the same value)
+    DevCRS& t = *mats[d]->AT;
+    // A: rows roff[d] .. roff[d] + m_d (the last entry is rewritten by the
+    // next dataset with the same value)
     shift_copy(c, a.off.as<i32>(), a.m + 1, base, A.off.as<i32>() + roff[d]);
     shift_copy(c, a.idx.as<i32>(), a.nnz, doff[d], A.idx.as<i32>() + base);
+    // AT: rows doff[d] .. doff[d] + n_d, then the empty bias row (its end is
+    // the next dataset's first offset, or the total)
+    shift_copy(c, t.off.as<i32>(), t.m + 1, base, AT.off.as<i32>() + doff[d]);
+    shift_copy(c, t.idx.as<i32>(), t.nnz, roff[d], AT.idx.as<i32>() + base);
     for (int dt : planes) {
       const size_t es = (size_t)dtype_size(dt);
       FVG_CUDA(cudaMemcpyAsync((char*)A.val[dt].p + base * es, a.val[dt].p, a.nnz * es, cudaMemcpyDeviceToDevice, s));
+      FVG_CUDA(cudaMemcpyAsync((char*)AT.val[dt].p + base * es, t.val[dt].p, t.nnz * es, cudaMemcpyDeviceToDevice, s));
     }
     A.max_row = std::max(A.max_row, a.max_row);
+    AT.max_row = std::max(AT.max_row, t.max_row);
     base += a.nnz;
   }
+  const i32 tot = (i32)nnz;
+  FVG_CUDA(cudaMemcpyAsync(AT.off.as<i32>() + doff[nd], &tot, sizeof(i32), cudaMemcpyHostToDevice, s));
+  FVG_CUDA(cudaStreamSynchronize(s));  // `tot` goes out of scope
 }
-
-// Sample rows of one backward block: R's slab of this many rows stays in L2
-// (48 MiB) while the block's transposed entries gather from it.  The
-// FVG_BATCH_CHUNK_ROWS environment variable overrides it (tests).
-i64 backward_chunk_rows(int ld, size_t xs) {
-  if (const char* e = std::getenv("FVG_BATCH_CHUNK_ROWS")) {
-    const long long v = std::atoll(e);
-    if (v > 0) return v;
-  }
-  return std::max<i64>(4096, (i64)((48ull << 20) / ((size_t)ld * xs)));
-}
-
-// The backward product A^T R in sample blocks: for each dataset, its rows in
-// slabs of backward_chunk_rows(); a block is the transposed CRS of one slab
-// (rows = the dataset's features, column ids = the slab's rows of R), so a
-// block gathers only from its slab of R, which stays in L2.  A dataset's
-// first block stores its gradient rows, the later ones add to them (in
-// slab order: deterministic).
-struct BackBlock {
-  int d = 0;
-  bool first = true;
-  std::unique_ptr<DevCRS> t;
-};
 
 struct BatchEval {
   fvg_ctx* c = nullptr;
   DevCRS* A = nullptr;
-  std::vector<BackBlock> blocks;
-  std::vector<i64> doff;
-  DBuf bseg;  // [nd][2]: {0, num_col} of each dataset's blocks
+  DevCRS* AT = nullptr;
   i64 m = 0;
   int k = 0, ld = 0, nd = 1, icpt = 0;
   int loss = 0;  // GLM loss kind shared by the models
   double eps = 0.0;
   const double* label = nullptr;
   const double* sw = nullptr;
-  DBuf label_f, sw_f, R, s1, s2, slots, seg_row, grow;
+  DBuf label_f, sw_f, R, s1, s2, slots, seg_row, seg_rowT, grow;
   int nwd = 1;
 
-  void init(fvg_ctx* c_, DevCRS* A_, const std::vector<fvg_matrix*>& mats, int k_, int ld_, const double* label_,
-            const double* sw_, int icpt_, const std::vector<i64>& roff, const std::vector<i64>& doff_,
-            const std::vector<int>& planes) {
+  void init(fvg_ctx* c_, DevCRS* A_, DevCRS* AT_, int k_, int ld_, const double* label_, const double* sw_,
+            int icpt_, const std::vector<i64>& roff, const std::vector<i64>& doff, const std::vector<int>& planes) {
     c = c_;
     A = A_;
-    doff = doff_;
+    AT = AT_;
     m = A->m;
     k = k_;
     ld = ld_;
@@ -760,26 +749,12 @@ struct BatchEval {
     }
     i64 s1b = 0, s2b = 0;
     bool f64 = false;
-    for (int st : planes) f64 = f64 || st == FVG_F64;
-    const i64 chunk = backward_chunk_rows(ld, f64 ? 8 : 4);
-    for (int d = 0; d < nd; d++) {
-      const i64 md = roff[d + 1] - roff[d];
-      for (i64 r = 0; r < md; r += chunk) {
-        BackBlock b;
-        b.d = d;
-        b.first = r == 0;
-        b.t.reset(new DevCRS());
-        crs_transpose_range(c, mats[d]->A, r, std::min(md, r + chunk), roff[d], planes, *b.t);
-        blocks.push_back(std::move(b));
-      }
-    }
     for (int st : planes) {
       crs_sched(c, *A, tile_for_storage(st));  // built before any capture
+      crs_sched(c, *AT, tile_for_storage(st));
       s1b = std::max(s1b, spmm_scratch_bytes(c, *A, st));
-      for (auto& b : blocks) {
-        crs_sched(c, *b.t, tile_for_storage(st));
-        s2b = std::max(s2b, spmm_scratch_bytes(c, *b.t, st));
-      }
+      s2b = std::max(s2b, spmm_scratch_bytes(c, *AT, st));
+      f64 = f64 || st == FVG_F64;
     }
     R.alloc((size_t)(f64 ? 8 : 4) * std::max<i64>(m * ld, 1), s);
     s1.alloc((size_t)s1b, s);
@@ -789,16 +764,13 @@ struct BatchEval {
     std::vector<i64> gr((size_t)nd);
     for (int d = 0; d <= nd; d++) sr[d] = (i32)roff[d];
     for (int d = 0; d < nd; d++) gr[d] = doff[d + 1] - 1;  // the dataset's bias row
-    std::vector<i32> bs((size_t)2 * nd);  // each dataset's blocks: one dataset of num_col rows
-    for (int d = 0; d < nd; d++) {
-      bs[2 * d] = 0;
-      bs[2 * d + 1] = (i32)(doff[d + 1] - doff[d] - 1);
-    }
+    std::vector<i32> srT((size_t)nd + 1);  // the transposed matrix's rows: the vector rows
+    for (int d = 0; d <= nd; d++) srT[d] = (i32)doff[d];
     seg_row.alloc(sizeof(i32) * (nd + 1), s);
-    bseg.alloc(sizeof(i32) * 2 * nd, s);
+    seg_rowT.alloc(sizeof(i32) * (nd + 1), s);
     grow.alloc(sizeof(i64) * nd, s);
     FVG_CUDA(cudaMemcpyAsync(seg_row.p, sr.data(), sizeof(i32) * (nd + 1), cudaMemcpyHostToDevice, s));
-    FVG_CUDA(cudaMemcpyAsync(bseg.p, bs.data(), sizeof(i32) * 2 * nd, cudaMemcpyHostToDevice, s));
+    FVG_CUDA(cudaMemcpyAsync(seg_rowT.p, srT.data(), sizeof(i32) * (nd + 1), cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaMemcpyAsync(grow.p, gr.data(), sizeof(i64) * nd, cudaMemcpyHostToDevice, s));
     FVG_CUDA(cudaStreamSynchronize(s));
     nwd = (ld + 63) / 64;
@@ -836,18 +808,14 @@ struct BatchEval {
       }
       {
         ProfScope ps(c, P_BATCH_PASS2);
-        for (auto& b : blocks) {
-          SpmmSeg st;
-          st.nseg = 1;
-          st.seg_row = bseg.as<i32>() + 2 * b.d;
-          st.gate = gate;
-          st.mask = mask ? mask + (i64)b.d * nwd : nullptr;
-          st.mstride = nwd;
-          st.mword = c0 / 64;
-          st.accum = b.first ? 0 : 1;
-          crs_spmm_store_seg(c, *b.t, storage, (const char*)R.p + c0 * xs, ld, kb, g + doff[b.d] * ld + c0, ld,
-                             s2.p, st);
-        }
+        SpmmSeg st;
+        st.nseg = nd;
+        st.seg_row = seg_rowT.as<i32>();
+        st.gate = gate;
+        st.mask = mask;
+        st.mstride = nwd;
+        st.mword = c0 / 64;
+        crs_spmm_store_seg(c, *AT, storage, (const char*)R.p + c0 * xs, ld, kb, g + c0, ld, s2.p, st);
       }
       crs_spmm_seg_finish(c, sg);
     }
@@ -909,15 +877,24 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
   const bool refine = storage == FVG_BF16 && p->refine;
   std::vector<int> planes{storage};
   if (refine) planes.push_back(FVG_F32);
-  for (fvg_matrix* M : mats)
-    for (int st : planes) crs_ensure_plane(c, M->A, st, M->master);
-  // one dataset: its own matrix; several: the stacked copy (the backward
-  // product runs on sample blocks of each dataset's matrix)
-  DevCRS SA;
+  for (fvg_matrix* M : mats) {
+    if (!M->AT) {
+      M->AT.reset(new DevCRS());
+      crs_build_transpose(c, M->A, *M->AT, M->master);
+    }
+    for (int st : planes) {
+      crs_ensure_plane(c, M->A, st, M->master);
+      crs_ensure_plane(c, *M->AT, st, M->master);
+    }
+  }
+  // one dataset: its own matrix and transpose; several: the stacked copies
+  DevCRS SA, SAT;
   DevCRS* A = &mats[0]->A;
+  DevCRS* AT = mats[0]->AT.get();
   if (nd > 1) {
-    stack_datasets(c, mats, doff, roff, planes, SA);
+    stack_datasets(c, mats, doff, roff, planes, SA, SAT);
     A = &SA;
+    AT = &SAT;
   }
 
   DBuf label, sw;
@@ -937,8 +914,7 @@ void lbfgs_multi_train(fvg_ctx* c, const std::vector<fvg_matrix*>& mats, const s
     }
   }
   BatchEval ev;
-  ev.init(c, A, mats, kk, ld, label.as<double>(), sw_any ? sw.as<double>() : nullptr, p->intercept, roff, doff,
-          planes);
+  ev.init(c, A, AT, kk, ld, label.as<double>(), sw_any ? sw.as<double>() : nullptr, p->intercept, roff, doff, planes);
   ev.loss = p->loss;
   ev.eps = p->epsilon;
 

@@ -220,83 +220,6 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
   t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
 }
 
-// Transposed CRS of rows [r0, r1) of a: rows = a's columns, column ids =
-// source row + row_shift, every value plane in `planes` (present in a),
-// entries of a row in source-row order (the stable sort as in
-// crs_build_transpose).  The blocks of a sample-blocked backward product.
-__global__ void k_rows_of_range(const i32* __restrict__ off, i64 rows, i64 base, i32 shift, i32* __restrict__ row_of) {
-  const int lane = threadIdx.x & 31;
-  const i64 w = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
-  for (i64 r = w; r < rows; r += nw)
-    for (i64 e = (i64)off[r] + lane; e < off[r + 1]; e += 32) row_of[e - base] = (i32)r + shift;
-}
-__global__ void k_fill_idx_perm(const uint32_t* __restrict__ src, const i32* __restrict__ row_of, i64 n,
-                                i32* __restrict__ tidx) {
-  GRID_STRIDE(p, n) tidx[p] = row_of[src[p]];
-}
-template <class T>
-__global__ void k_gather_perm(const T* __restrict__ v, const uint32_t* __restrict__ src, i64 n, T* __restrict__ out) {
-  GRID_STRIDE(p, n) out[p] = v[src[p]];
-}
-
-void crs_transpose_range(fvg_ctx* c, const DevCRS& a, i64 r0, i64 r1, i64 row_shift, const std::vector<int>& planes,
-                         DevCRS& t) {
-  ProfScope ps(c, P_TRANSPOSE);
-  if (r0 < 0 || r1 < r0 || r1 > a.m) fail(FVG_ERR_INTERNAL, "row range out of the matrix");
-  if (row_shift + r1 >= (1ll << 31)) fail(FVG_ERR_INTERNAL, "shifted row ids beyond 2^31 - 1");
-  i32 hb[2];
-  FVG_CUDA(cudaMemcpyAsync(&hb[0], a.off.as<i32>() + r0, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaMemcpyAsync(&hb[1], a.off.as<i32>() + r1, sizeof(i32), cudaMemcpyDeviceToHost, c->stream));
-  FVG_CUDA(cudaStreamSynchronize(c->stream));
-  const i64 base = hb[0], nnz = (i64)hb[1] - hb[0];
-  t.m = a.n;
-  t.n = row_shift + r1;
-  t.nnz = nnz;
-  t.off.alloc(sizeof(i32) * (t.m + 1), c->stream);
-  t.idx.alloc(sizeof(i32) * (nnz + kPad), c->stream);
-  FVG_CUDA(cudaMemsetAsync(t.idx.as<i32>() + nnz, 0, sizeof(i32) * kPad, c->stream));
-  for (int dt : planes) {
-    if (!a.val[dt].p) fail(FVG_ERR_INTERNAL, "range transpose: missing value plane");
-    alloc_plane(c, t.val[dt], nnz, dt);
-  }
-  if (nnz == 0) {
-    fill_i32(c, t.off.as<i32>(), 0, t.m + 1);
-    t.max_row = 0;
-    return;
-  }
-  DBuf keys, src, rows;
-  keys.alloc(sizeof(uint32_t) * nnz, c->stream);
-  src.alloc(sizeof(uint32_t) * nnz, c->stream);
-  rows.alloc(sizeof(i32) * nnz, c->stream);
-  FVG_CUDA(cudaMemcpyAsync(keys.p, a.idx.as<i32>() + base, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToDevice,
-                           c->stream));
-  k_iota_u32<<<grid_n(nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), nnz);
-  k_rows_of_range<<<grid_n(32 * (r1 - r0)), 256, 0, c->stream>>>(a.off.as<i32>() + r0, r1 - r0, base,
-                                                                   (i32)(row_shift + r0), rows.as<i32>());
-  check_launch("range transpose set-up");
-  count_launch(c, 2);
-  radix_sort_pairs(c, keys.as<uint32_t>(), src.as<uint32_t>(), nnz, bits_for(a.n - 1));
-  k_boundaries<<<grid_n(nnz + 1), 256, 0, c->stream>>>(keys.as<uint32_t>(), nnz, a.n, t.off.as<i32>());
-  k_fill_idx_perm<<<grid_n(nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), rows.as<i32>(), nnz, t.idx.as<i32>());
-  check_launch("range transpose");
-  count_launch(c, 2);
-  for (int dt : planes) {
-    if (dt == FVG_F64)
-      k_gather_perm<double><<<grid_n(nnz), 256, 0, c->stream>>>(a.val[dt].as<double>() + base, src.as<uint32_t>(),
-                                                                nnz, t.val[dt].as<double>());
-    else if (dt == FVG_F32)
-      k_gather_perm<float><<<grid_n(nnz), 256, 0, c->stream>>>(a.val[dt].as<float>() + base, src.as<uint32_t>(), nnz,
-                                                               t.val[dt].as<float>());
-    else
-      k_gather_perm<bf16><<<grid_n(nnz), 256, 0, c->stream>>>(a.val[dt].as<bf16>() + base, src.as<uint32_t>(), nnz,
-                                                              t.val[dt].as<bf16>());
-    check_launch("range transpose values");
-    count_launch(c);
-  }
-  t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
-}
-
 // ---------------------------------------------------------------- schedule
 // Packs rows, in row order, into work items (see Sched): consecutive short
 // rows share a row tile while the tile stays within `tile` nonzeros,

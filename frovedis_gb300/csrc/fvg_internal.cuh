@@ -302,10 +302,6 @@ int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem = 0);
 void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n);
 // stable LSD radix sort of (key,val) u32 pairs by the low `bits` bits of key
 void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bits);
-// Transposed CRS of rows [r0, r1) of a (column ids = source row + row_shift)
-// with the value planes `planes`.
-void crs_transpose_range(fvg_ctx* c, const DevCRS& a, i64 r0, i64 r1, i64 row_shift, const std::vector<int>& planes,
-                         DevCRS& t);
 void fill_i32(fvg_ctx* c, i32* p, i32 v, i64 n);
 void convert_values(fvg_ctx* c, const void* src, int sdt, void* dst, int ddt, i64 n);
 void gather_values(fvg_ctx* c, const void* src, const uint32_t* perm, void* dst, int dt, i64 n);
@@ -384,7 +380,6 @@ struct SpmmSeg {
   const unsigned long long* mask = nullptr;
   i64 mstride = 0;
   int mword = 0;
-  int accum = 0;  // crs_spmm_store_seg: Y += A X instead of Y = A X
   // set by the pass for crs_spmm_seg_finish
   i64 nw1 = 0, nw2 = 0;
   int nc = 0, icpt = 0;

@@ -63,7 +63,6 @@ struct SpmmK {
   const unsigned long long* mask;
   i64 mstride;
   int mword;
-  int accum;  // store epilogue: Y += A X (rows without nonzeros left as they are)
 };
 
 __device__ __forceinline__ unsigned long long mask_of(const SpmmK& p, int d) {
@@ -185,12 +184,6 @@ __device__ __forceinline__ void spmm_epi(const SpmmK& p, i32 row, const AT (&a)[
 #define ON(q) (colof<VEC, CPL>(lane, q) < p.kb && col_on(mw, colof<VEC, CPL>(lane, q)))
   if (EPI == EPI_STORE) {
     YT* y = (YT*)p.Y + (i64)row * p.ldy;
-    if (p.accum) {
-#pragma unroll
-      for (int q = 0; q < CPL; q++)
-        if (ON(q)) y[colof<VEC, CPL>(lane, q)] += (YT)a[q];
-      return;
-    }
     if constexpr (VEC) {
       if (mw != ~0ull) {
 #pragma unroll
@@ -694,14 +687,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
         mw = mask_of(p, walk.d);
       }
       if (mw == 0) continue;  // no column of this dataset is computed
-      const i32 e0 = __ldg(p.off + r), e1 = __ldg(p.off + r + 1);
-      if (EPI == EPI_STORE && p.accum && e0 == e1) continue;  // adds nothing
-      row_dot_g<VT, XT, AT, G>(p, e0, e1, lane, a, stage[wib], cols_on(mw, lsh, CPL));
+      row_dot_g<VT, XT, AT, G>(p, __ldg(p.off + r), __ldg(p.off + r + 1), lane, a, stage[wib], cols_on(mw, lsh, CPL));
       if constexpr (EPI == EPI_STORE) {
         YT* y = (YT*)p.Y + (i64)r * p.ldy;
 #pragma unroll
         for (int q = 0; q < QG; q++)
-          if (cols[q] < p.kb && col_on(mw, cols[q])) y[cols[q]] = p.accum ? y[cols[q]] + (YT)a[q] : (YT)a[q];
+          if (cols[q] < p.kb && col_on(mw, cols[q])) y[cols[q]] = (YT)a[q];
       } else {
         // labels: always with the logistic epilogue; the softmax one runs
         // without them for the probability matrix alone
@@ -943,7 +934,6 @@ static void launch_grouped_l(fvg_ctx* c, DevCRS& a, const Sched& s, int storage,
     p.mask = sg->mask;
     p.mstride = sg->mstride;
     p.mword = sg->mword;
-    p.accum = EPI == EPI_STORE ? sg->accum : 0;
   }
   if (s.nitems > 0 || seg) {
     k_spmm_g<VT, XT, AT, YT, EPI, G><<<grid, kThreads, 0, c->stream>>>(p);

@@ -169,21 +169,3 @@ def test_multi_errors(ctx):
     # the context still works after the refusals
     r = fv.logreg_lbfgs_multi([A, B], [label, label], [1e-3], num_iter=3)
     assert np.allclose(r["loss"][0], r["loss"][1], rtol=1e-12)
-
-
-def test_multi_backward_in_sample_blocks(ctx, monkeypatch):
-    # the backward product in several sample blocks per dataset (the first
-    # stores the gradient rows, the later ones add to them): same models
-    data = [_ds(110 + i, m, n, long_rows=lr) for i, (m, n, lr) in enumerate([(3100, 900, 2), (800, 120, 0)])]
-    mats = [ctx.matrix(a.m, a.n, a.off, a.idx, a.val) for a, _ in data]
-    lams = [1e-4, 1e-2, 0.3]
-    kw = dict(num_iter=12, reg_type="L2", intercept=True)
-    w0 = [np.zeros(a.n) for a, _ in data]
-    whole = fv.logreg_lbfgs_multi(mats, [l for _, l in data], lams, w0=w0, **kw)
-    monkeypatch.setenv("FVG_BATCH_CHUNK_ROWS", "700")
-    blocked = fv.logreg_lbfgs_multi(mats, [l for _, l in data], lams, w0=w0, **kw)
-    assert np.array_equal(whole["n_iter"], blocked["n_iter"])
-    assert np.max(np.abs(whole["loss"] - blocked["loss"]) / np.abs(whole["loss"])) <= 1e-9
-    for d, (a, label) in enumerate(data):
-        for j, lam in enumerate(lams):
-            _check(blocked, d, j, a, label, lam, w0=np.zeros(a.n), **kw)
