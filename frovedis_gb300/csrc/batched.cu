@@ -727,6 +727,7 @@ struct BatchEval {
   const double* sw = nullptr;
   DBuf label_f, sw_f, R, s1, s2, slots, seg_row, seg_rowT, grow;
   int nwd = 1;
+  i64 slab = 0;  // rows of R in one slab of the backward product's pieces
 
   void init(fvg_ctx* c_, DevCRS* A_, DevCRS* AT_, int k_, int ld_, const double* label_, const double* sw_,
             int icpt_, const std::vector<i64>& roff, const std::vector<i64>& doff, const std::vector<int>& planes) {
@@ -749,12 +750,15 @@ struct BatchEval {
     }
     i64 s1b = 0, s2b = 0;
     bool f64 = false;
+    for (int st : planes) f64 = f64 || st == FVG_F64;
+    // the backward product gathers rows of R (ld columns): its long rows in
+    // pieces listed by slabs of R that fit in L2 (48 MiB)
+    slab = std::max<i64>(4096, (i64)((48ull << 20) / ((size_t)ld * (f64 ? 8 : 4))));
     for (int st : planes) {
       crs_sched(c, *A, tile_for_storage(st));  // built before any capture
-      crs_sched(c, *AT, tile_for_storage(st));
+      crs_sched_slabs(c, *AT, tile_for_storage(st), slab);
       s1b = std::max(s1b, spmm_scratch_bytes(c, *A, st));
-      s2b = std::max(s2b, spmm_scratch_bytes(c, *AT, st));
-      f64 = f64 || st == FVG_F64;
+      s2b = std::max(s2b, spmm_scratch_bytes(c, *AT, st, slab));
     }
     R.alloc((size_t)(f64 ? 8 : 4) * std::max<i64>(m * ld, 1), s);
     s1.alloc((size_t)s1b, s);
@@ -815,7 +819,7 @@ struct BatchEval {
         st.mask = mask;
         st.mstride = nwd;
         st.mword = c0 / 64;
-        crs_spmm_store_seg(c, *AT, storage, (const char*)R.p + c0 * xs, ld, kb, g + c0, ld, s2.p, st);
+        crs_spmm_store_seg(c, *AT, storage, (const char*)R.p + c0 * xs, ld, kb, g + c0, ld, s2.p, st, slab);
       }
       crs_spmm_seg_finish(c, sg);
     }

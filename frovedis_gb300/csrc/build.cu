@@ -254,6 +254,128 @@ const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
   return *a.sched[slot];
 }
 
+// ------------------------------------------------------ slab-ordered pieces
+// Work items of a transposed product whose gathered vector rows are larger
+// than L2 (the batched and multinomial backward products, A^T R with R's
+// rows 256-512 bytes): the rows longer than a tile are cut into pieces at
+// every slab boundary of their column ids (slab = `slab` consecutive rows
+// of R) as well as every `tile` entries, and those pieces are listed slab by
+// slab, so that the warps sweeping the item list gather from one slab of R
+// at a time (an L2-sized slab stays in L2).  Short rows stay in their tiles
+// (after the pieces).  Pieces of a row keep consecutive numbers in slab
+// order, so the finalize kernel adds them in a fixed order.
+__device__ __forceinline__ i64 first_at_least(const i32* __restrict__ idx, i64 lo, i64 hi, i64 v) {
+  while (lo < hi) {
+    const i64 mid = (lo + hi) >> 1;
+    if ((i64)idx[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_slab_pieces(const i32* __restrict__ long_rows, i64 nlong, const i32* __restrict__ off,
+                              const i32* __restrict__ idx, int tile, i64 slab, const i32* __restrict__ piece0,
+                              i32* __restrict__ cnt, Item* __restrict__ items, uint32_t* __restrict__ keys) {
+  GRID_STRIDE(i, nlong) {
+    const i32 r = long_rows[i];
+    i64 e = off[r];
+    const i64 end = off[r + 1];
+    i64 q = piece0 ? piece0[i] : 0;
+    i32 n = 0;
+    while (e < end) {
+      const i64 b = (i64)idx[e] / slab;
+      const i64 be = first_at_least(idx, e, end, (b + 1) * slab);
+      for (i64 s = e; s < be; s += tile) {
+        const i64 t = s + tile < be ? s + tile : be;
+        if (items) {
+          items[q] = Item{r, (i32)(-1 - q), (i32)s, (i32)t};
+          keys[q] = (uint32_t)b;
+        }
+        q++;
+        n++;
+      }
+      e = be;
+    }
+    if (cnt) cnt[i] = n;
+  }
+}
+
+__global__ void k_gather_items(const Item* __restrict__ src, const uint32_t* __restrict__ order, i64 n,
+                               Item* __restrict__ dst) {
+  GRID_STRIDE(i, n) dst[i] = src[order[i]];
+}
+
+const Sched& crs_sched_slabs(fvg_ctx* c, DevCRS& a, int tile, i64 slab) {
+  if (a.slab_sched && a.slab_rows == slab && a.slab_sched->tile == tile) return *a.slab_sched;
+  const Sched& s0 = crs_sched(c, a, tile);
+  ProfScope ps(c, P_SCHED);
+  auto s = std::make_unique<Sched>();
+  s->tile = tile;
+  s->nlong = s0.nlong;
+  cudaStream_t st = c->stream;
+  // tiles of the plain schedule (its items whose r1 >= 0)
+  std::vector<Item> h0((size_t)s0.nitems);
+  if (s0.nitems)
+    FVG_CUDA(cudaMemcpyAsync(h0.data(), s0.items.p, sizeof(Item) * s0.nitems, cudaMemcpyDeviceToHost, st));
+  DBuf cnt;
+  cnt.alloc(sizeof(i32) * std::max<i64>(s0.nlong, 1), st);
+  if (s0.nlong) {
+    k_slab_pieces<<<grid_n(s0.nlong), 256, 0, st>>>(s0.long_rows.as<i32>(), s0.nlong, a.off.as<i32>(),
+                                                     a.idx.as<i32>(), tile, slab, nullptr, cnt.as<i32>(), nullptr,
+                                                     nullptr);
+    check_launch("slab piece count");
+    count_launch(c);
+  }
+  std::vector<i32> hc((size_t)s0.nlong);
+  if (s0.nlong) FVG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(i32) * s0.nlong, cudaMemcpyDeviceToHost, st));
+  FVG_CUDA(cudaStreamSynchronize(st));
+  std::vector<i32> p0((size_t)s0.nlong + 1, 0);
+  i64 np = 0;
+  for (i64 i = 0; i < s0.nlong; i++) {
+    p0[(size_t)i] = (i32)np;
+    np += hc[(size_t)i];
+  }
+  if (np >= (1ll << 31) - 1) fail(FVG_ERR_INTERNAL, "slab schedule too large");
+  p0[(size_t)s0.nlong] = (i32)np;
+  i64 ntiles = 0;
+  for (const Item& it : h0) ntiles += it.r1 >= 0;
+  s->npieces = np;
+  s->nitems = np + ntiles;
+  s->long_rows.alloc(sizeof(i32) * std::max<i64>(s0.nlong, 1), st);
+  s->long_piece0.alloc(sizeof(i32) * (s0.nlong + 1), st);
+  s->items.alloc(sizeof(Item) * std::max<i64>(s->nitems, 1), st);
+  if (s0.nlong)
+    FVG_CUDA(cudaMemcpyAsync(s->long_rows.p, s0.long_rows.p, sizeof(i32) * s0.nlong, cudaMemcpyDeviceToDevice, st));
+  FVG_CUDA(cudaMemcpyAsync(s->long_piece0.p, p0.data(), sizeof(i32) * (s0.nlong + 1), cudaMemcpyHostToDevice, st));
+  if (np) {
+    DBuf tmp, keys, order;
+    tmp.alloc(sizeof(Item) * np, st);
+    keys.alloc(sizeof(uint32_t) * np, st);
+    order.alloc(sizeof(uint32_t) * np, st);
+    k_slab_pieces<<<grid_n(s0.nlong), 256, 0, st>>>(s0.long_rows.as<i32>(), s0.nlong, a.off.as<i32>(),
+                                                     a.idx.as<i32>(), tile, slab, s->long_piece0.as<i32>(), nullptr,
+                                                     tmp.as<Item>(), keys.as<uint32_t>());
+    k_iota_u32<<<grid_n(np), 256, 0, st>>>(order.as<uint32_t>(), np);
+    check_launch("slab pieces");
+    count_launch(c, 2);
+    // stable by slab: within a slab the pieces keep row order
+    radix_sort_pairs(c, keys.as<uint32_t>(), order.as<uint32_t>(), np, bits_for((a.n - 1) / slab));
+    k_gather_items<<<grid_n(np), 256, 0, st>>>(tmp.as<Item>(), order.as<uint32_t>(), np, s->items.as<Item>());
+    check_launch("slab order");
+    count_launch(c);
+  }
+  std::vector<Item> ht;
+  ht.reserve((size_t)ntiles);
+  for (const Item& it : h0)
+    if (it.r1 >= 0) ht.push_back(it);
+  if (ntiles)
+    FVG_CUDA(cudaMemcpyAsync(s->items.as<Item>() + np, ht.data(), sizeof(Item) * ntiles, cudaMemcpyHostToDevice, st));
+  FVG_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+  a.slab_sched = std::move(s);
+  a.slab_rows = slab;
+  return *a.slab_sched;
+}
+
 // --------------------------------------------------------------------- ELL
 template <class T>
 __global__ void k_ell_fill(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,

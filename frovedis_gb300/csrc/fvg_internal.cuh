@@ -116,6 +116,8 @@ struct DevCRS {
   DBuf val[3];    // indexed by fvg_dtype
   DBuf lo;        // bf16 [nnz+kPad]: value - FP32 value (split storage; with val[FVG_F32])
   std::unique_ptr<Sched> sched[2];  // work items: slot 0 kWarpTile, slot 1 the split kernel's size
+  std::unique_ptr<Sched> slab_sched;  // long rows in slab-ordered pieces (crs_sched_slabs)
+  i64 slab_rows = 0;
   i64 max_row = 0;
 };
 
@@ -312,6 +314,9 @@ void crs_upload(fvg_ctx* c, DevCRS& a, i64 m, i64 n, const i32* off, const i32* 
 void crs_ensure_plane(fvg_ctx* c, DevCRS& a, int dt, int master);
 void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master);
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile);
+// The rows longer than a tile cut into pieces also at every slab of `slab`
+// column ids, the pieces listed slab by slab before the tiles (cached).
+const Sched& crs_sched_slabs(fvg_ctx* c, DevCRS& a, int tile, i64 slab);
 void ell_build(fvg_ctx* c, const DevCRS& a, DevELL& e, int master);
 void jds_build(fvg_ctx* c, const DevCRS& a, DevJDS& j, int master);
 void hyb_build(fvg_ctx* c, const DevCRS& a, DevHYB& h, int master, i64 threshold);
@@ -348,9 +353,12 @@ void hyb_spmv(fvg_ctx* c, DevHYB& h, int storage, int x_dt, const void* x, int y
 void crs_spmm(fvg_ctx* c, DevCRS& a, int storage, int x_dt, const void* X, i64 k, void* Y);
 // One block of at most 64 columns (X, Y already offset to the block's first
 // column; ldx / ldy row strides); scratch of spmm_scratch_bytes().
-i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage);
+// slab > 0: the schedule of crs_sched_slabs (long rows in pieces listed by
+// slabs of `slab` rows of X, for X larger than L2); the scratch must be sized
+// with the same slab.
+i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage, i64 slab = 0);
 void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, int y_dt, void* Y, i64 ldy,
-                    void* scratch, const int* gate = nullptr);
+                    void* scratch, const int* gate = nullptr, i64 slab = 0);
 void crs_spmm_logreg_block(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int kb, const double* label,
                            const double* sw, const float* label_f, const float* sw_f, int icpt, const double* bias,
                            void* R, i64 ldr, double* out, double* gbias, void* scratch, int loss = 0,
@@ -393,7 +401,7 @@ void crs_spmm_seg_finish(fvg_ctx* c, const SpmmSeg& sg);
 // Y = A X (FP64 Y) over stacked datasets with sg's row bounds, masks, gate
 // (the same alignment as crs_spmm_logreg_seg).
 void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
-                        void* scratch, SpmmSeg& sg);
+                        void* scratch, SpmmSeg& sg, i64 slab = 0);
 
 // Row-panel backward product (FP32/BF16 storage): builds the layout when the
 // matrix's column counts make it pay (or as forced); returns null when the

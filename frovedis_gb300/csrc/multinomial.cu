@@ -21,6 +21,14 @@
 
 namespace fvg {
 
+// Rows of P (the gathered matrix of the backward product A^T P) in one slab
+// of the backward's slab-ordered pieces: 48 MiB of the gathered block.
+static i64 backward_slab(int K, int storage) {
+  const i64 w = std::min<i64>(K, 128) * (storage == FVG_F64 ? 8 : 4);
+  return std::max<i64>(4096, (i64)(48ll << 20) / w);
+}
+
+
 constexpr int kMT = 256;
 
 void crs_spmm_softmax(fvg_ctx* c, DevCRS& a, int storage, const void* W, i64 ldw, int K, const double* label,
@@ -243,7 +251,8 @@ void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const d
   ICPT.alloc(sizeof(double) * K, s);
   FVG_CUDA(cudaMemcpyAsync(W.p, w_h, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
   FVG_CUDA(cudaMemcpyAsync(ICPT.p, b_h, sizeof(double) * K, cudaMemcpyHostToDevice, s));
-  s2.alloc((size_t)spmm_scratch_bytes(c, *M->AT, storage), s);
+  const i64 slab = backward_slab((int)K, storage);
+  s2.alloc((size_t)spmm_scratch_bytes(c, *M->AT, storage, slab), s);
   int kp = 1;
   while (kp < K && kp < kMT) kp <<= 1;
   const int nblk = (int)std::max<i64>(1, std::min<i64>((n + 63) / 64, 4 * (i64)c->num_sms));
@@ -274,7 +283,7 @@ void multinomial_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, const d
       for (int c0 = 0; c0 < K; c0 += 128) {
         const int kb = (int)std::min<i64>(128, K - c0);
         crs_spmm_block(c, *M->AT, storage, (const char*)sm.Z.p + c0 * es, K, kb, FVG_F64, G.as<double>() + c0, K,
-                       s2.p);
+                       s2.p, nullptr, slab);
       }
     }
     const double ra = p->alpha / std::sqrt((double)i);
@@ -317,6 +326,7 @@ struct SoftmaxLbfgsEval : LbfgsEval {
   const double* label = nullptr;
   const double* sw = nullptr;
   DBuf WF, s2, lossbuf;
+  i64 slab = 0;
   void eval(const double* w64, const double* b, double* g, double* out) override {
     (void)b;
     const bool mixed = storage != FVG_F64;
@@ -336,7 +346,7 @@ struct SoftmaxLbfgsEval : LbfgsEval {
     }
     {
       ProfScope ps(c, P_BATCH_PASS2);
-      crs_spmm_block(c, *M->AT, storage, sm.Z.p, K, K, FVG_F64, g, K, s2.p);
+      crs_spmm_block(c, *M->AT, storage, sm.Z.p, K, K, FVG_F64, g, K, s2.p, nullptr, slab);
     }
     FVG_CUDA(cudaMemsetAsync(g + nk, 0, sizeof(double), c->stream));
     FVG_CUDA(cudaMemcpyAsync(out, lossbuf.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -378,7 +388,8 @@ void multinomial_lbfgs_train(fvg_ctx* c, fvg_matrix* M, const double* label_h, c
   ev.sw = sw_h ? sw.as<double>() : nullptr;
   ev.sm.init(c, &M->A, M->master, storage, (int)K, ev.label, ev.sw);
   if (storage != FVG_F64) ev.WF.alloc(sizeof(float) * (size_t)n * K, s);
-  ev.s2.alloc((size_t)spmm_scratch_bytes(c, *M->AT, storage), s);
+  ev.slab = backward_slab((int)K, storage);
+  ev.s2.alloc((size_t)spmm_scratch_bytes(c, *M->AT, storage, ev.slab), s);
   ev.lossbuf.alloc(sizeof(double) * 2 * 128, s);
   double b = 0.0;
   lbfgs_core(c, n * K, p, 0, ev, w_h, &b, n_iter, loss_out);

@@ -390,6 +390,18 @@ template <class AT, int QN> struct SegWalk {
     end = __ldg(p.seg_row + d + 1);
     return true;
   }
+  // the dataset of row r wherever it lies (schedules whose items are not in
+  // row order; no sums are kept then)
+  __device__ __forceinline__ void seek(const SpmmK& p, i32 r) {
+    int lo = 0, hi = p.nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(p.seg_row + mid) <= r) lo = mid;
+      else hi = mid - 1;
+    }
+    d = lo;
+    end = __ldg(p.seg_row + d + 1);
+  }
   __device__ __forceinline__ void finish(const SpmmK& p, const int (&col)[QN], Sum (&ls)[QN], Sum (&bs)[QN]) {
     if (!slots) return;
     put(d, col, ls, bs);
@@ -669,8 +681,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_spmm_g(const SpmmK p) {
   for (i64 it = gw; it < p.nitems; it += nw) {
     const Item item = p.items[it];
     AT a[CPL];
+    // the store epilogue keeps no per-dataset sums, so its items may come in
+    // any order (slab-ordered pieces): each item looks its dataset up
+    if (EPI == EPI_STORE && track) {
+      walk.seek(p, item.r0);
+      mw = mask_of(p, walk.d);
+    }
     if (item.r1 < 0) {  // piece of a long row (item.r0)
-      if (track && walk.to_row(p, item.r0, cols, ls, bs)) {
+      if (EPI != EPI_STORE && track && walk.to_row(p, item.r0, cols, ls, bs)) {
         if (EPI == EPI_LOGREG) load_bias(p.bias + walk.d * p.ldb);
         mw = mask_of(p, walk.d);
       }
@@ -844,8 +862,9 @@ static int spmm_fin_grid(fvg_ctx* c, i64 nlong) {
 
 // Scratch of one block pass (sized for 128 columns): ticket, per-CTA
 // partials of the main and finalize kernels, long-row piece partials.
-i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage) {
-  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
+i64 spmm_scratch_bytes(fvg_ctx* c, DevCRS& a, int storage, i64 slab) {
+  const Sched& s = slab > 0 ? crs_sched_slabs(c, a, tile_for_storage(storage), slab)
+                            : crs_sched(c, a, tile_for_storage(storage));
   const size_t at = storage == FVG_F64 ? 8 : 4;
   const i64 grid = 8 * (i64)c->num_sms;  // occupancy upper bound (8 CTAs of 256 threads per SM)
   return (i64)(al256(256) + al256(sizeof(double) * 2 * kSpmmMaxCols * grid) +
@@ -1028,10 +1047,11 @@ static void launch_store(fvg_ctx* c, DevCRS& a, const Sched& s, int storage, con
 
 // Y[:, c0:c0+kb] = A X[:, c0:c0+kb] (X, Y pointers already offset to c0).
 void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, int y_dt, void* Y, i64 ldy,
-                    void* scratch, const int* gate) {
+                    void* scratch, const int* gate, i64 slab) {
   if (kb < 1 || kb > kSpmmMaxCols) fail(FVG_ERR_INTERNAL, "spmm block width out of range");
   if (!a.val[storage].p) fail(FVG_ERR_INTERNAL, "missing value plane for the requested storage");
-  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
+  const Sched& s = slab > 0 ? crs_sched_slabs(c, a, tile_for_storage(storage), slab)
+                            : crs_sched(c, a, tile_for_storage(storage));
   SpmmK p = {};
   p.X = X;
   p.ldx = ldx;
@@ -1066,10 +1086,11 @@ void crs_spmm_block(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, 
 // Y keep what they held.  X, Y and their strides 16-byte aligned, kb a
 // multiple of 8 (of 2 for FP64) and at most 64.
 void crs_spmm_store_seg(fvg_ctx* c, DevCRS& a, int storage, const void* X, i64 ldx, int kb, void* Y, i64 ldy,
-                        void* scratch, SpmmSeg& sg) {
+                        void* scratch, SpmmSeg& sg, i64 slab) {
   if (kb < 1 || kb > 64 || sg.nseg < 1) fail(FVG_ERR_INTERNAL, "stacked store: block width or datasets out of range");
   if (!a.val[storage].p) fail(FVG_ERR_INTERNAL, "missing value plane for the requested storage");
-  const Sched& s = crs_sched(c, a, tile_for_storage(storage));
+  const Sched& s = slab > 0 ? crs_sched_slabs(c, a, tile_for_storage(storage), slab)
+                            : crs_sched(c, a, tile_for_storage(storage));
   SpmmK p = {};
   p.X = X;
   p.ldx = ldx;
