@@ -234,7 +234,7 @@ def test_split_panel_long_segments(ctx):
     val = rng.standard_normal(int(off[-1])) * np.exp(rng.uniform(-2, 2, int(off[-1])))
     a = oracle.CRS(m, n, off, idx, val)
     A = ctx.matrix(m, n, off, idx, val)
-    A.set_panels(12000, 1.0)  # within the tallest panel a CTA can stage
+    A.set_panels(8000, 1.0)  # within the tallest panel a CTA can stage
     r = rng.standard_normal(m)
     z = A.trans_mv(r, storage="split")
     at = oracle.transpose(a)
