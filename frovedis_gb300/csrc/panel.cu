@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(1024) k_panel_colsum(const float* __restrict__
 // kSplitChunk entries: no products are staged and no second pass re-reads
 // them.
 #ifndef FVG_SPLIT_WARPS
-#define FVG_SPLIT_WARPS 24
+#define FVG_SPLIT_WARPS 28
 #endif
 constexpr int kSplitWarps = FVG_SPLIT_WARPS;  // one CTA per SM (its shared slice fills the SM)
 constexpr int kSplitTile = 480;  // an item's staged copy (8-aligned ends) fits 32 lanes x 16 entries
