@@ -349,10 +349,11 @@ def run_gpu(args):
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
-    spmv = None if args.skip_spmv else spmv_suite(ctx, args)
+    # the summaries of the other configurations: rank 0 only (the line is its)
+    spmv = None if (args.skip_spmv or rank != 0) else spmv_suite(ctx, args)
     ctx.close()
-    rp = None if args.skip_regpath else regpath(args, args.regpath_datasets, 20)
-    mlr = None if args.skip_mlr else multinomial_lbfgs_run(args, iters=30)
+    rp = None if (args.skip_regpath or rank != 0) else regpath(args, args.regpath_datasets, 20)
+    mlr = None if (args.skip_mlr or rank != 0) else multinomial_lbfgs_run(args, iters=30)
     # the FP64 oracle (the reference's loops) on the whole matrix: the CPU
     # baseline and the parity reference of every arm
     cpu = None
