@@ -139,52 +139,14 @@ __global__ void k_boundaries(const uint32_t* __restrict__ keys, i64 nnz, i64 nco
   }
 }
 
-// Row id and value of a nonzero side by side, so that the transposed fill
-// reads both with one random access (one sector) instead of two.
-template <class T> struct RowVal;
-template <> struct alignas(16) RowVal<double> { uint32_t row, pad; double v; };
-template <> struct alignas(8) RowVal<float> { uint32_t row; float v; };
-template <> struct alignas(8) RowVal<bf16> { uint32_t row; bf16 v; uint16_t pad; };
-
-// (row, value) of every nonzero in A's order: a warp per row, lanes write
+// Row id of every nonzero in A's order: a warp per row, lanes write
 // consecutive entries.
-template <class T>
-__global__ void k_expand_rowval(const i32* __restrict__ off, i64 m, const T* __restrict__ val,
-                                RowVal<T>* __restrict__ rv) {
+__global__ void k_expand_rows(const i32* __restrict__ off, i64 m, uint32_t* __restrict__ rows) {
   const int lane = threadIdx.x & 31;
   const i64 w = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const i64 nw = ((i64)gridDim.x * blockDim.x) >> 5;
   for (i64 r = w; r < m; r += nw)
-    for (i64 e = (i64)off[r] + lane; e < off[r + 1]; e += 32) {
-      RowVal<T> x;
-      x.row = (uint32_t)r;
-      x.v = val[e];
-      rv[e] = x;
-    }
-}
-
-// Transposed entry p comes from source position src[p]: its column id in
-// the transpose is the source row, its value the source value.
-template <class T>
-__global__ void k_trans_fill(const uint32_t* __restrict__ src, const RowVal<T>* __restrict__ rv, i64 nnz,
-                             i32* __restrict__ tidx, T* __restrict__ tval) {
-  GRID_STRIDE(p, nnz) {
-    const RowVal<T> x = rv[src[p]];
-    tidx[p] = (i32)x.row;
-    tval[p] = x.v;
-  }
-}
-
-template <class T>
-static void trans_fill(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master, const uint32_t* src) {
-  DBuf rv;
-  rv.alloc(sizeof(RowVal<T>) * a.nnz, c->stream);
-  k_expand_rowval<T><<<grid_n(32 * a.m), 256, 0, c->stream>>>(a.off.as<i32>(), a.m, a.val[master].as<T>(),
-                                                               rv.as<RowVal<T>>());
-  k_trans_fill<T><<<grid_n(a.nnz), 256, 0, c->stream>>>(src, rv.as<RowVal<T>>(), a.nnz, t.idx.as<i32>(),
-                                                         t.val[master].as<T>());
-  check_launch("transpose");
-  count_launch(c, 2);
+    for (i64 e = (i64)off[r] + lane; e < off[r + 1]; e += 32) rows[e] = (uint32_t)r;
 }
 
 void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
@@ -201,22 +163,32 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
     t.max_row = 0;
     return;
   }
-  DBuf keys, src;
+  // A stable sort of the nonzeros by column (stable = in row order within a
+  // column) that carries each one's row and value, so the sorted rows and
+  // values are the transposed copy's column ids and values.
+  DBuf rows, keys;
+  rows.alloc(sizeof(uint32_t) * a.nnz, c->stream);
   keys.alloc(sizeof(uint32_t) * a.nnz, c->stream);
-  src.alloc(sizeof(uint32_t) * a.nnz, c->stream);
-  FVG_CUDA(cudaMemcpyAsync(keys.p, a.idx.p, sizeof(uint32_t) * a.nnz, cudaMemcpyDeviceToDevice, c->stream));
-  k_iota_u32<<<grid_n(a.nnz), 256, 0, c->stream>>>(src.as<uint32_t>(), a.nnz);
-  check_launch("iota");
+  k_expand_rows<<<grid_n(32 * a.m), 256, 0, c->stream>>>(a.off.as<i32>(), a.m, rows.as<uint32_t>());
+  check_launch("expand_rows");
   count_launch(c);
-  // stable by element position == stable in source-row order
-  radix_sort_pairs(c, keys.as<uint32_t>(), src.as<uint32_t>(), a.nnz, bits_for(a.n - 1));
+  const uint32_t* kin = reinterpret_cast<const uint32_t*>(a.idx.as<i32>());  // ids are in [0, n)
+  uint32_t* tidx = reinterpret_cast<uint32_t*>(t.idx.as<i32>());
+  const int bits = bits_for(a.n - 1);
+  if (master == FVG_F64)
+    radix_sort_rowval<double>(c, kin, rows.as<uint32_t>(), a.val[master].as<double>(), keys.as<uint32_t>(), tidx,
+                              t.val[master].as<double>(), a.nnz, bits);
+  else if (master == FVG_F32)
+    radix_sort_rowval<float>(c, kin, rows.as<uint32_t>(), a.val[master].as<float>(), keys.as<uint32_t>(), tidx,
+                             t.val[master].as<float>(), a.nnz, bits);
+  else
+    radix_sort_rowval<bf16>(c, kin, rows.as<uint32_t>(), a.val[master].as<bf16>(), keys.as<uint32_t>(), tidx,
+                            t.val[master].as<bf16>(), a.nnz, bits);
+  rows.release();
   k_boundaries<<<grid_n(a.nnz + 1), 256, 0, c->stream>>>(keys.as<uint32_t>(), a.nnz, a.n, t.off.as<i32>());
   check_launch("boundaries");
   count_launch(c);
   keys.release();
-  if (master == FVG_F64) trans_fill<double>(c, a, t, master, src.as<uint32_t>());
-  else if (master == FVG_F32) trans_fill<float>(c, a, t, master, src.as<uint32_t>());
-  else trans_fill<bf16>(c, a, t, master, src.as<uint32_t>());
   t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
 }
 
@@ -227,7 +199,7 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 // pieces of at most `tile` nonzeros, cut at 8-element boundaries.  Built on
 // the device once per matrix, in chunks of kSchedChunk rows packed by one
 // warp each (a tile never spans two chunks).
-constexpr i64 kSchedChunk = 4096;
+constexpr i64 kSchedChunk = kPackRows;
 
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {
   // slot 0: the CRS kernel's items (kWarpTile); slot 1: another item size

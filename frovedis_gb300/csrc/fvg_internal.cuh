@@ -72,6 +72,10 @@ constexpr i64 kPad = 32;
 constexpr int kThreads = 256;
 constexpr int kTileRows = 248;  // rows per tile (their offsets are staged in shared memory)
 constexpr int kLaneWork = 32;   // products one lane may sum for one row in a tile
+// Rows one warp of the work-item packer walks in order (a tile never spans
+// two such chunks): short enough that the packers' sequential walks take a
+// fraction of a millisecond, long enough to fill kTileRows-row tiles.
+constexpr i64 kPackRows = 512;
 // Lanes per row when a warp sums a tile of R rows: 32 / R rounded to a power
 // of two; tiles of 32 or more rows take rounds of 32 rows, one lane each.
 __host__ __device__ __forceinline__ int lanes_per_row(int R) {
@@ -304,6 +308,9 @@ int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem = 0);
 void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n);
 // stable LSD radix sort of (key,val) u32 pairs by the low `bits` bits of key
 void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bits);
+template <class T>
+void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, const T* vin, uint32_t* kout,
+                       uint32_t* rout, T* vout, i64 n, int bits);
 void fill_i32(fvg_ctx* c, i32* p, i32 v, i64 n);
 void convert_values(fvg_ctx* c, const void* src, int sdt, void* dst, int ddt, i64 n);
 void gather_values(fvg_ctx* c, const void* src, const uint32_t* perm, void* dst, int dt, i64 n);

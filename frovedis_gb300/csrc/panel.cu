@@ -657,8 +657,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + 2 * w;
   unsigned char* area = smem + 16 * NW + w * SM::kWarpB;
   unsigned short* soff = reinterpret_cast<unsigned short*>(area + SM::kStageB);
-  float* xh = reinterpret_cast<float*>(smem + SM::kStatic);
-  float* xl = reinterpret_cast<float*>(smem + SM::kStatic + p.rows * 4);
+  float2* xs = reinterpret_cast<float2*>(smem + SM::kStatic);  // df pairs: one 8-byte load a gather
   if (lane == 0) mbar_init(bar, 1);
   fence_mbar_init();
   __syncthreads();
@@ -675,8 +674,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
     if (!shared || u == blockIdx.x)
       for (int i = threadIdx.x; i < nr; i += NW * 32) {
         const float2 v = __ldg(p.x + (shared ? (i64)p.xmap[i] : base + i));
-        xh[i] = v.x;
-        xl[i] = v.y;
+        xs[i] = v;
       }
     __syncthreads();
     const int t1 = p.pitem0[pe];
@@ -708,7 +706,27 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
       parity ^= 1u;
       pend = false;
       __syncwarp();
-      // this lane's 8 staged entries
+      // The copy's padding entries (before e0, and from e1 to the end of the
+      // lane chunk holding it: at most 7 and 15) become slot 0, value 0, so
+      // that their products are exact zeros and no entry needs a range test.
+      {
+        const int lead = it.e0 - q0, tz = it.e1 - q0;
+        const int tend = min((tz + CH - 1) / CH * CH, SM::kCap);
+        unsigned short* ss = reinterpret_cast<unsigned short*>(area);
+        float* sh = reinterpret_cast<float*>(area + SM::kHiB);
+        unsigned short* sl = reinterpret_cast<unsigned short*>(area + SM::kLoB);
+        if (lane < lead) {
+          ss[lane] = 0;
+          sh[lane] = 0.f;
+          sl[lane] = 0;
+        }
+        if (lane < tend - tz) {
+          ss[tz + lane] = 0;
+          sh[tz + lane] = 0.f;
+          sl[tz + lane] = 0;
+        }
+        __syncwarp();
+      }
       // this lane's CH staged entries (16-byte shared loads)
       unsigned sw[CH / 2], lw[CH / 2];
       float hv[CH];
@@ -725,19 +743,21 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         hv[4 * q] = h.x; hv[4 * q + 1] = h.y; hv[4 * q + 2] = h.z; hv[4 * q + 3] = h.w;
       }
       const int lo_e = max(it.e0 - q0, lane * CH), hi_e = min(it.e1 - q0, lane * CH + CH);
+      const bool any = lo_e < hi_e;
+      // a lane past the item's end reads stale (or never written) slots: slot 0
+#pragma unroll
+      for (int q = 0; q < CH / 2; q++) sw[q] = any ? sw[q] : 0u;
       if (!tile) {
         DfAcc acc;
 #pragma unroll
         for (int k = 0; k < CH; k++) {
-          const int e = lane * CH + k;
-          if (e >= lo_e && e < hi_e) {
-            const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
-            const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
-            float pp, tt;
-            df_prod(hv[k], vl, make_float2(xh[c], xl[c]), pp, tt);
-            acc.add(pp, tt);
-          }
+          const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+          const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
+          float pp, tt;
+          df_prod(hv[k], vl, xs[c], pp, tt);
+          acc.add(pp, tt);
         }
+        if (!any) acc = DfAcc{};
         df a = acc.get();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a = df_add(a, shfl_xor_df(a, o));
@@ -746,24 +766,19 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         __syncwarp();  // soff
         for (int j = lane; j < R; j += 32)
           if (soff[j] == soff[j + 1]) p.ypan[it.r0 + j] = make_float2(0.f, 0.f);  // empty rows
-        // the lane's 8 products (zero outside its valid range)
+        // the lane's CH products (padding entries give exact zeros; a lane
+        // past the item's end has any == false and its sums are dropped)
         float pp[CH], tt[CH];
 #pragma unroll
         for (int k = 0; k < CH; k++) {
-          const int e = lane * CH + k;
-          const bool ok = e >= lo_e && e < hi_e;
-          const unsigned c = ok ? (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu : 0u;
+          const unsigned c = (sw[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
           const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
-          float a, b;
-          df_prod(hv[k], vl, make_float2(xh[c], xl[c]), a, b);
-          pp[k] = ok ? a : 0.f;
-          tt[k] = ok ? b : 0.f;
+          df_prod(hv[k], vl, xs[c], pp[k], tt[k]);
         }
         // rows: j0 holds the first valid entry; B marks the rows starting after it
         unsigned B = 0;
         int j = 0, j0 = 0, nb = 0;
         bool starts = false;
-        const bool any = lo_e < hi_e;
         if (any) {
           int a = 0, b = R;  // the last row starting at or before lo_e (the non-empty one holding it)
           while (b - a > 1) {
@@ -807,6 +822,7 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         if (B) p.ypan[it.r0 + j0] = df_pack(starts ? H : df_add(carry, H));
         if (any && nb == hi_e) p.ypan[it.r0 + j] = df_pack(S);  // the tail row ends with this lane's range
       }
+      fence_proxy_async();  // the padding stores, before the next copy into the area
       __syncwarp();
     }
     __syncthreads();
@@ -896,9 +912,10 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
   const i64 np = std::max<i64>(nchunks, 1) * sub;
   DBuf cnt, basev;
   cnt.alloc(sizeof(i32) * 3 * np, c->stream);
-  const unsigned pg = (unsigned)std::min<i64>(np, 1 << 20);  // a warp per chunk
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 0, cnt.as<i32>(), nullptr, nullptr,
-                                         nullptr, nullptr);
+  // a warp per chunk, 8 warps a CTA
+  const unsigned pg = (unsigned)std::min<i64>((np + 7) / 8, 1 << 20);
+  k_panel_pack<<<pg, 256, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 0, cnt.as<i32>(), nullptr, nullptr,
+                                          nullptr, nullptr);
   check_launch("pack");
   count_launch(c);
   std::vector<i32> hc((size_t)(3 * np));
@@ -922,8 +939,8 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
   o.items.alloc(sizeof(Item) * std::max<i64>(o.nitems, 1), c->stream);
   o.long_rows.alloc(sizeof(i32) * std::max<i64>(o.nlong, 1), c->stream);
   o.long_piece0.alloc(sizeof(i32) * (o.nlong + 1), c->stream);
-  k_panel_pack<<<pg, 32, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 1, nullptr, basev.as<i32>(),
-                                         o.items.as<Item>(), o.long_rows.as<i32>(), o.long_piece0.as<i32>());
+  k_panel_pack<<<pg, 256, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 1, nullptr, basev.as<i32>(),
+                                          o.items.as<Item>(), o.long_rows.as<i32>(), o.long_piece0.as<i32>());
   check_launch("pack");
   count_launch(c);
   const i32 npc = (i32)o.npieces;
@@ -937,7 +954,7 @@ namespace {
 void pack_split_items(fvg_ctx* c, DevPanels& pn) {
   const i64 nhot = pn.nhot, np = pn.npanels;
   PackOut o;
-  const i64 sub = std::max<i64>(1, (nhot + 4095) / 4096);
+  const i64 sub = std::max<i64>(1, (nhot + kPackRows - 1) / kPackRows);
   device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kSplitTile, o, sub);
   auto it = std::make_unique<PanelItems>();
   it->tile = kSplitTile;
@@ -963,8 +980,8 @@ void pack_split_items(fvg_ctx* c, DevPanels& pn) {
 
 void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
   PackOut o;
-  // each panel's rows in pieces of ~4096 rows, a warp each
-  const i64 sub = std::max<i64>(1, (nhot + 4095) / 4096);
+  // each panel's rows in pieces of ~kPackRows rows, a warp each
+  const i64 sub = std::max<i64>(1, (nhot + kPackRows - 1) / kPackRows);
   device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o, sub);
   pn.nitems = o.nitems;
   pn.nlong = o.nlong;

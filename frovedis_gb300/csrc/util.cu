@@ -284,28 +284,24 @@ __device__ __forceinline__ void scan256_exclusive(int* v) {
   v[threadIdx.x] = before + inc - x;
 }
 
-// Downsweep: ranks as above, then the tile is sorted by digit in shared
-// memory (digit-major, input order within a digit) and written back in that
-// order, so consecutive threads store consecutive positions of a digit's run.
-__global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, i64 n, int shift,
-                               i64 nblocks, const i64* __restrict__ goff) {
-  __shared__ int wcnt[kRsWarps][256];
-  __shared__ int dstart[256];
-  __shared__ uint32_t skey[kRsTile], sval[kRsTile];
+// Ranks of a tile's keys (warp w: keys [w*512, w*512+512) of the tile in 16
+// rounds of 32) and the digit bookkeeping of the downsweeps: on return
+// wcnt[w][d] is warp w's first slot within digit d's run of the tile,
+// dstart[d] the run's first tile slot, rank[r] the key's rank among the
+// warp's keys of its digit (-1 past n).  Ranks follow the input order.
+__device__ __forceinline__ void rs_rank_tile(const uint32_t* __restrict__ kin, i64 n, int shift,
+                                             uint32_t (&key)[kRsRounds], int (&rank)[kRsRounds],
+                                             int (*wcnt)[256], int* dstart) {
   for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
   const i64 base = (i64)blockIdx.x * kRsTile + (i64)w * (kRsRounds * 32);
-  uint32_t key[kRsRounds], val[kRsRounds];
-  int rank[kRsRounds];
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
     i64 i = base + r * 32 + lane;
     bool ok = i < n;
     key[r] = ok ? kin[i] : 0u;
-    val[r] = ok ? vin[i] : 0u;
     int d = ok ? (int)((key[r] >> shift) & 255u) : 256 + lane;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     int before = __popc(peers & lt);
@@ -328,13 +324,29 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
   __syncthreads();
   scan256_exclusive(dstart);  // first tile slot of each digit
   __syncthreads();
+}
+
+// Downsweep: ranks as above, then the tile is sorted by digit in shared
+// memory (digit-major, input order within a digit) and written back in that
+// order, so consecutive threads store consecutive positions of a digit's run.
+__global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, i64 n, int shift,
+                               i64 nblocks, const i64* __restrict__ goff) {
+  __shared__ int wcnt[kRsWarps][256];
+  __shared__ int dstart[256];
+  __shared__ uint32_t skey[kRsTile], sval[kRsTile];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t key[kRsRounds];
+  int rank[kRsRounds];
+  rs_rank_tile(kin, n, shift, key, rank, wcnt, dstart);
+  const i64 base = (i64)blockIdx.x * kRsTile + (i64)w * (kRsRounds * 32);
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
     if (rank[r] < 0) continue;
     const int d = (int)((key[r] >> shift) & 255u);
     const int lp = dstart[d] + wcnt[w][d] + rank[r];
     skey[lp] = key[r];
-    sval[lp] = val[r];
+    sval[lp] = vin[base + r * 32 + lane];
   }
   __syncthreads();
   const i64 t0 = (i64)blockIdx.x * kRsTile;
@@ -345,6 +357,55 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
     const i64 pos = goff[(i64)d * nblocks + blockIdx.x] + (i - dstart[d]);
     kout[pos] = k;
     vout[pos] = sval[i];
+  }
+}
+
+// Downsweep carrying a (row, value) payload: the tile's rows and values are
+// staged in shared memory in input order (coalesced loads), the ranked keys
+// go to their tile slots with their input position, and the write-back
+// reads each slot's row and value from the staged copy.  Dynamic shared
+// memory: kRsTile rows (uint32) + kRsTile values.
+template <class T>
+__global__ void __launch_bounds__(kRsThreads) k_rs_downsweep_rv(const uint32_t* __restrict__ kin,
+                                                                const uint32_t* __restrict__ rin,
+                                                                const T* __restrict__ vin, uint32_t* __restrict__ kout,
+                                                                uint32_t* __restrict__ rout, T* __restrict__ vout,
+                                                                i64 n, int shift, i64 nblocks,
+                                                                const i64* __restrict__ goff) {
+  __shared__ int wcnt[kRsWarps][256];
+  __shared__ int dstart[256];
+  __shared__ uint32_t skey[kRsTile];
+  __shared__ uint16_t spos[kRsTile];
+  extern __shared__ __align__(16) unsigned char rs_dyn[];
+  uint32_t* srow = reinterpret_cast<uint32_t*>(rs_dyn);
+  T* sv = reinterpret_cast<T*>(rs_dyn + sizeof(uint32_t) * kRsTile);
+  const i64 t0 = (i64)blockIdx.x * kRsTile;
+  const int cnt = (int)(n - t0 < kRsTile ? n - t0 : kRsTile);
+  for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
+    srow[i] = rin[t0 + i];
+    sv[i] = vin[t0 + i];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t key[kRsRounds];
+  int rank[kRsRounds];
+  rs_rank_tile(kin, n, shift, key, rank, wcnt, dstart);  // (its barriers also order the staging)
+#pragma unroll
+  for (int r = 0; r < kRsRounds; r++) {
+    if (rank[r] < 0) continue;
+    const int d = (int)((key[r] >> shift) & 255u);
+    const int lp = dstart[d] + wcnt[w][d] + rank[r];
+    skey[lp] = key[r];
+    spos[lp] = (uint16_t)(w * (kRsRounds * 32) + r * 32 + lane);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
+    const uint32_t k = skey[i];
+    const int s = spos[i];
+    const int d = (int)((k >> shift) & 255u);
+    const i64 pos = goff[(i64)d * nblocks + blockIdx.x] + (i - dstart[d]);
+    kout[pos] = k;
+    rout[pos] = srow[s];
+    vout[pos] = sv[s];
   }
 }
 
@@ -373,6 +434,53 @@ void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bit
     FVG_CUDA(cudaMemcpyAsync(vals, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
   }
 }
+
+// Stable sort of (key, row, value) triples by the low `bits` bits of the
+// key, from (kin, rin, vin) into (kout, rout, vout); the inputs are not
+// changed.  Passes alternate between the outputs and one set of temporaries,
+// starting on the side that makes the last pass write the outputs.
+template <class T>
+void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, const T* vin, uint32_t* kout,
+                       uint32_t* rout, T* vout, i64 n, int bits) {
+  if (n <= 0) return;
+  const int passes = std::max(1, (bits + 7) / 8);
+  const i64 nb = (n + kRsTile - 1) / kRsTile;
+  const int dyn = (int)((sizeof(uint32_t) + sizeof(T)) * kRsTile);
+  FVG_CUDA(cudaFuncSetAttribute(k_rs_downsweep_rv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  DBuf kt, rt, vt, hist, goff;
+  if (passes > 1) {
+    kt.alloc(sizeof(uint32_t) * n, c->stream);
+    rt.alloc(sizeof(uint32_t) * n, c->stream);
+    vt.alloc(sizeof(T) * n, c->stream);
+  }
+  hist.alloc(sizeof(i64) * 256 * nb, c->stream);
+  goff.alloc(sizeof(i64) * (256 * nb + 1), c->stream);
+  const uint32_t *ks = kin, *rs = rin;
+  const T* vs = vin;
+  for (int p = 0; p < passes; p++) {
+    const bool to_out = ((passes - 1 - p) & 1) == 0;
+    uint32_t* kd = to_out ? kout : kt.as<uint32_t>();
+    uint32_t* rd = to_out ? rout : rt.as<uint32_t>();
+    T* vd = to_out ? vout : vt.as<T>();
+    const int shift = 8 * p;
+    k_rs_upsweep<<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ks, n, shift, nb, hist.as<i64>());
+    check_launch("rs_upsweep");
+    scan_i64(c, hist.as<i64>(), goff.as<i64>(), 256 * nb);
+    k_rs_downsweep_rv<T><<<(unsigned)nb, kRsThreads, dyn, c->stream>>>(ks, rs, vs, kd, rd, vd, n, shift, nb,
+                                                                      goff.as<i64>());
+    check_launch("rs_downsweep_rv");
+    count_launch(c, 2);
+    ks = kd;
+    rs = rd;
+    vs = vd;
+  }
+}
+template void radix_sort_rowval<double>(fvg_ctx*, const uint32_t*, const uint32_t*, const double*, uint32_t*,
+                                        uint32_t*, double*, i64, int);
+template void radix_sort_rowval<float>(fvg_ctx*, const uint32_t*, const uint32_t*, const float*, uint32_t*,
+                                       uint32_t*, float*, i64, int);
+template void radix_sort_rowval<bf16>(fvg_ctx*, const uint32_t*, const uint32_t*, const bf16*, uint32_t*,
+                                      uint32_t*, bf16*, i64, int);
 
 // ------------------------------------------------------- element kernels
 __global__ void k_fill_i32(i32* p, i32 v, i64 n) {
