@@ -442,6 +442,7 @@ void df64_init(fvg_ctx* c);  // the exp table of the df64 math, once per device
 void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master);
 // lo = BF16(v - FP32 plane) for n values of planes[] (the FP64 and FP32 planes)
 void split_residual_plane(fvg_ctx* c, const DBuf* planes, i64 n, int master, DBuf& lo);
+void ensure_split_planes(fvg_ctx* c, DBuf* planes, i64 n, int master, DBuf& lo);
 void split_vector(fvg_ctx* c, const double* x, void* y, i64 n);  // y: float2[n]
 i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a);
 // y = A x, x float2 pairs; y FP64 (y_df false) or float2 pairs

@@ -1427,8 +1427,7 @@ PanSK split_args(fvg_ctx* c, DevPanels& pn, const void* x) {
 void panel_ensure_split(fvg_ctx* c, DevPanels& pn) {
   if (pn.rows > panel_rows_cap(c))
     fail(FVG_ERR_INTERNAL, "panel layout too tall for the split kernel");
-  ensure_plane_generic(c, pn.val, pn.E, FVG_F32, pn.master);
-  if (!pn.lo.p) split_residual_plane(c, pn.val, pn.E, pn.master, pn.lo);
+  ensure_split_planes(c, pn.val, pn.E, pn.master, pn.lo);
   crs_ensure_split(c, pn.cold, pn.master);
   if (!pn.split_items) pack_split_items(c, pn);
   if (!pn.ypan2.p) {

@@ -25,6 +25,7 @@
 
 #include "device_common.cuh"
 #include "df64.cuh"
+#include "split_bits.h"
 
 namespace fvg {
 
@@ -62,6 +63,30 @@ __global__ void k_split_plane(const double* __restrict__ v, const float* __restr
     const float h = hi[i];
     if (isinf(h) && !isinf(x)) b = 1;
     lo[i] = __double2bfloat16(isinf(h) ? 0.0 : x - (double)h);
+  }
+  if (b) atomicOr(bad, 1u);
+}
+
+// Both planes from the FP64 values in one pass: hi = FP32(v), lo =
+// BF16(v - hi) by integer arithmetic on the FP64 bits (split_bits.h), the
+// FP64 conversions only for values outside its range.
+__global__ void k_split_values(const double* __restrict__ v, float* __restrict__ hi, bf16* __restrict__ lo, i64 n,
+                               unsigned* __restrict__ bad) {
+  unsigned b = 0;
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const double x = v[i];
+    uint32_t hb;
+    uint16_t lb;
+    if (split_bits((uint64_t)__double_as_longlong(x), &hb, &lb)) {
+      if ((hb & 0x7fffffffu) == 0x7f800000u) b = 1;
+      hi[i] = __uint_as_float(hb);
+      lo[i] = __ushort_as_bfloat16(lb);
+    } else {
+      const float h = __double2float_rn(x);
+      if (isinf(h) && !isinf(x)) b = 1;
+      hi[i] = h;
+      lo[i] = __double2bfloat16(isinf(h) ? 0.0 : x - (double)h);
+    }
   }
   if (b) atomicOr(bad, 1u);
 }
@@ -376,10 +401,34 @@ void split_residual_plane(fvg_ctx* c, const DBuf* planes, i64 n, int master, DBu
   lo = std::move(out);
 }
 
-void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) {
-  crs_ensure_plane(c, a, FVG_F32, master);
-  if (!a.lo.p) split_residual_plane(c, a.val, a.nnz, master, a.lo);
+// The FP32 and residual planes of a value set; from FP64 values with neither
+// plane yet, both in one pass.
+void ensure_split_planes(fvg_ctx* c, DBuf* planes, i64 n, int master, DBuf& lo) {
+  if (master == FVG_F64 && !planes[FVG_F32].p && !lo.p && n > 0) {
+    DBuf hi, out, bad;
+    hi.alloc(sizeof(float) * (size_t)(n + kPad), c->stream);
+    out.alloc(sizeof(bf16) * (size_t)(n + kPad), c->stream);
+    FVG_CUDA(cudaMemsetAsync(hi.as<float>() + n, 0, sizeof(float) * kPad, c->stream));
+    FVG_CUDA(cudaMemsetAsync(out.as<bf16>() + n, 0, sizeof(bf16) * kPad, c->stream));
+    bad.alloc(sizeof(unsigned), c->stream);
+    FVG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), c->stream));
+    k_split_values<<<grid_rows(c, n, 16), kSplitThreads, 0, c->stream>>>(planes[FVG_F64].as<double>(), hi.as<float>(),
+                                                                         out.as<bf16>(), n, bad.as<unsigned>());
+    check_launch("split_values");
+    count_launch(c);
+    unsigned hb = 0;
+    FVG_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    FVG_CUDA(cudaStreamSynchronize(c->stream));
+    if (hb) fail(FVG_ERR_INVALID_ARG, "split storage: a value lies outside the FP32 range");
+    planes[FVG_F32] = std::move(hi);
+    lo = std::move(out);
+    return;
+  }
+  ensure_plane_generic(c, planes, n, FVG_F32, master);
+  if (!lo.p) split_residual_plane(c, planes, n, master, lo);
 }
+
+void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master) { ensure_split_planes(c, a.val, a.nnz, master, a.lo); }
 
 void split_vector(fvg_ctx* c, const double* x, void* y, i64 n) {
   if (n <= 0) return;
