@@ -198,7 +198,7 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
 // kTileRows rows and kLaneWork products per lane; a long row becomes its own
 // pieces of at most `tile` nonzeros, cut at 8-element boundaries.  Built on
 // the device once per matrix, in chunks of kSchedChunk rows packed by one
-// warp each (a tile never spans two chunks).
+// thread each (a tile never spans two chunks).
 constexpr i64 kSchedChunk = kPackRows;
 
 const Sched& crs_sched(fvg_ctx* c, DevCRS& a, int tile) {

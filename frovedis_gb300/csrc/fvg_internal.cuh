@@ -72,10 +72,10 @@ constexpr i64 kPad = 32;
 constexpr int kThreads = 256;
 constexpr int kTileRows = 248;  // rows per tile (their offsets are staged in shared memory)
 constexpr int kLaneWork = 32;   // products one lane may sum for one row in a tile
-// Rows one warp of the work-item packer walks in order (a tile never spans
+// Rows one thread of the work-item packer walks in order (a tile never spans
 // two such chunks): short enough that the packers' sequential walks take a
 // fraction of a millisecond, long enough to fill kTileRows-row tiles.
-constexpr i64 kPackRows = 512;
+constexpr i64 kPackRows = 256;
 // Lanes per row when a warp sums a tile of R rows: 32 / R rounded to a power
 // of two; tiles of 32 or more rows take rounds of 32 rows, one lane each.
 __host__ __device__ __forceinline__ int lanes_per_row(int R) {

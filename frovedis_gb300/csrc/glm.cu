@@ -559,12 +559,11 @@ struct Evaluator {
     }
     r.alloc(sizeof(float2) * m1, c->stream);
     wtx2.alloc(sizeof(float2) * m1, c->stream);
-    s1.alloc(crs_split_scratch_bytes(c, *op->A), c->stream);
-    s2.alloc(crs_split_scratch_bytes(c, *op->AT), c->stream);
     const i64 g = glm_split_grid(c, op->m);
     gpart.alloc(sizeof(double) * 2 * g + 256, c->stream);
     FVG_CUDA(cudaMemsetAsync((char*)gpart.p + sizeof(double) * 2 * g, 0, 256, c->stream));
-    // the row-panel layout (backward) and the forward head, when the matrix has them
+    // the row-panel layout (backward) and the forward head, when the matrix
+    // has them; the whole CRS copies' schedules only for the passes without
     if (op->M && op->fmt == FVG_CRS) {
       PT = panels_for(c, op->M);
       if (PT) {
@@ -577,6 +576,8 @@ struct Evaluator {
         s4.alloc(panel_split_scratch_bytes(c, *HD), c->stream);
       }
     }
+    if (!HD) s1.alloc(crs_split_scratch_bytes(c, *op->A), c->stream);
+    if (!PT) s2.alloc(crs_split_scratch_bytes(c, *op->AT), c->stream);
   }
   void eval_split(const void* x, const double* b, double* grad, double* out) {
     const i64 g = glm_split_grid(c, op->m);

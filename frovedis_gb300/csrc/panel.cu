@@ -91,10 +91,27 @@ __global__ void k_i64_to_i32(const i64* __restrict__ s, i32* __restrict__ d, i64
 }
 
 // a warp per panel row: its entries copied with the row made panel-local
+// The source's other value planes (FP32, BF16, split residual) that a fill
+// copies beside the master plane, so that a layout built from a matrix that
+// already holds them needs no conversion afterwards; null where absent.
+struct SidePlanes {
+  const float* s32 = nullptr;
+  float* d32 = nullptr;
+  const bf16* s16 = nullptr;
+  bf16* d16 = nullptr;
+  const bf16* slo = nullptr;
+  bf16* dlo = nullptr;
+  __device__ __forceinline__ void copy(i64 from, i64 to) const {
+    if (s32) d32[to] = s32[from];
+    if (s16) d16[to] = s16[from];
+    if (slo) dlo[to] = slo[from];
+  }
+};
+
 template <class T>
 __global__ void k_panel_fill(const i32* __restrict__ B, const i64* __restrict__ poff, const i32* __restrict__ tidx,
                              const T* __restrict__ tval, i64 nhot, i64 np, i64 rows, uint16_t* __restrict__ prow,
-                             T* __restrict__ pval) {
+                             T* __restrict__ pval, const SidePlanes sp) {
   const int lane = threadIdx.x & 31;
   PWARP_STRIDE(q, np * nhot) {
     const i64 p = q / nhot, h = q - p * nhot;
@@ -103,6 +120,7 @@ __global__ void k_panel_fill(const i32* __restrict__ B, const i64* __restrict__ 
     for (i64 k = lane; k < e - s; k += 32) {
       prow[d + k] = (uint16_t)(tidx[s + k] - r0);
       pval[d + k] = tval[s + k];
+      sp.copy(s + k, d + k);
     }
   }
 }
@@ -114,7 +132,7 @@ __global__ void k_cold_lens(const i32* __restrict__ toff, const i64* __restrict_
 template <class T>
 __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict__ flag, const i64* __restrict__ coff,
                             i64 n, const i32* __restrict__ tidx, const T* __restrict__ tval, i32* __restrict__ cidx,
-                            T* __restrict__ cval) {
+                            T* __restrict__ cval, const SidePlanes sp) {
   const int lane = threadIdx.x & 31;
   PWARP_STRIDE(c, n) {
     if (flag[c]) continue;
@@ -122,91 +140,96 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
     for (i64 k = lane; k < e - s; k += 32) {
       cidx[d + k] = tidx[s + k];
       cval[d + k] = tval[s + k];
+      sp.copy(s + k, d + k);
     }
   }
 }
 
-// Work items of a CRS, one warp per chunk of rows (chunk p: piece p % sub of
-// the stretch of nhot rows p / sub), with the CRS schedule's packing rules
+// Work items of a CRS, one thread per chunk of rows (chunk p: piece p % sub
+// of the stretch of nhot rows p / sub), with the CRS schedule's packing rules
 // (tiles of short rows within `tile` entries, kTileRows rows and kLaneWork
 // products per lane; longer rows in pieces cut at 8-element boundaries).  The
-// greedy packing is sequential: every lane runs it on the same offsets
-// (loaded 32 at a time and broadcast by shuffles, so control flow is
-// uniform); lane 0 writes the tiles, all lanes write a long row's pieces.
-// Pass 0 counts each chunk's items, long rows and pieces; pass 1 writes them
-// at the scanned offsets `base` (chunk-major: a chunk's items, long rows and
-// pieces are contiguous and numbered globally).
+// greedy packing is sequential within a chunk; a thread walks its chunk's
+// offsets in order.  Pass 0 counts each chunk's items, long rows and pieces;
+// pass 1 writes them at the scanned offsets `base` (chunk-major: a chunk's
+// items, long rows and pieces are contiguous and numbered globally).
 __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 sub, i64 np, int tile, int write,
                              i32* __restrict__ cnt, const i32* __restrict__ base, Item* __restrict__ items,
-                             i32* __restrict__ lrows, i32* __restrict__ lpiece0) {
-  const int lane = threadIdx.x & 31;
-  const bool w0 = write && lane == 0;
-  // chunk p: piece j of `sub` of stretch p / sub (stretches of nhot rows)
+                             i32* __restrict__ lrows, i32* __restrict__ lpiece0, i32* __restrict__ lfirst) {
   const i64 step = (nhot + sub - 1) / sub;
-  for (i64 p = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np;
-       p += ((i64)gridDim.x * blockDim.x) >> 5) {
+  for (i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (i64)gridDim.x * blockDim.x) {
     const i64 s0 = (p / sub) * nhot, s1 = min(s0 + nhot, nrows), j = p % sub;
     const i64 r0 = min(s0 + j * step, s1), r1 = min(r0 + step, s1);
     const i32 bi = write ? base[p] : 0, bl = write ? base[(np + 1) + p] : 0, bp = write ? base[2 * (np + 1) + p] : 0;
     i32 ni = 0, nl = 0, npc = 0;
     i64 t0 = r0, tnnz = 0, tmax = 0;
     i32 o_cur = off[r0], o_t0 = o_cur;  // off[r], off[t0]
-    for (i64 rb = r0; rb < r1; rb += 32) {
-      const i32 v = (rb + lane < r1) ? off[rb + lane + 1] : 0;  // off[r + 1] for r = rb + lane
-      const int nrow = (int)min((i64)32, r1 - rb);
-      for (int j = 0; j < nrow; j++) {
-        const i64 r = rb + j;
-        const i32 o_next = __shfl_sync(0xffffffffu, v, j);
-        const i64 len = (i64)o_next - o_cur;
-        if (len > tile) {
-          if (r > t0) {
-            if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
-            ni++;
-          }
-          const i64 st = o_cur, en = o_next, b8 = st & ~7ll;
-          const i64 npr = (en - b8 + tile - 1) / tile;  // pieces: b8 + k*tile < en
-          if (w0) {
-            lrows[bl + nl] = (i32)r;
-            lpiece0[bl + nl] = bp + npc;
-          }
-          if (write)  // the lanes write the pieces of a long row together
-            for (i64 k = lane; k < npr; k += 32) {
-              const i64 e0 = (k == 0) ? st : b8 + k * tile, e1 = min(en, b8 + (k + 1) * tile);
-              items[bi + ni + k] = Item{(int32_t)r, (int32_t)(-1 - (bp + npc + k)), (int32_t)e0, (int32_t)e1};
-            }
-          nl++;
-          ni += (i32)npr;
-          npc += (i32)npr;
-          t0 = r + 1;
-          o_t0 = o_next;
-          tnnz = 0;
-          tmax = 0;
-        } else {
-          if (r > t0) {
-            const i64 R = r - t0 + 1, mx = max(tmax, len);
-            if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) {
-              if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
-              ni++;
-              t0 = r;
-              o_t0 = o_cur;
-              tnnz = 0;
-              tmax = 0;
-            }
-          }
-          tnnz += len;
-          tmax = max(tmax, len);
+    for (i64 r = r0; r < r1; r++) {
+      const i32 o_next = off[r + 1];
+      const i64 len = (i64)o_next - o_cur;
+      if (len > tile) {
+        if (r > t0) {
+          if (write) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
+          ni++;
         }
-        o_cur = o_next;
+        const i64 st = o_cur, en = o_next, b8 = st & ~7ll;
+        const i64 npr = (en - b8 + tile - 1) / tile;  // pieces: b8 + k*tile < en
+        if (write) {  // its pieces' items: k_long_pieces
+          lrows[bl + nl] = (i32)r;
+          lpiece0[bl + nl] = bp + npc;
+          lfirst[bl + nl] = bi + ni;
+        }
+        nl++;
+        ni += (i32)npr;
+        npc += (i32)npr;
+        t0 = r + 1;
+        o_t0 = o_next;
+        tnnz = 0;
+        tmax = 0;
+      } else {
+        if (r > t0) {
+          const i64 R = r - t0 + 1, mx = max(tmax, len);
+          if (tnnz + len > tile || R > kTileRows || mx > (i64)kLaneWork * lanes_per_row((int)R)) {
+            if (write) items[bi + ni] = Item{(int32_t)t0, (int32_t)r, o_t0, o_cur};
+            ni++;
+            t0 = r;
+            o_t0 = o_cur;
+            tnnz = 0;
+            tmax = 0;
+          }
+        }
+        tnnz += len;
+        tmax = max(tmax, len);
       }
+      o_cur = o_next;
     }
     if (r1 > t0) {
-      if (w0) items[bi + ni] = Item{(int32_t)t0, (int32_t)r1, o_t0, o_cur};
+      if (write) items[bi + ni] = Item{(int32_t)t0, (int32_t)r1, o_t0, o_cur};
       ni++;
     }
-    if (!write && lane == 0) {
+    if (!write) {
       cnt[p] = ni;
       cnt[np + p] = nl;
       cnt[2 * np + p] = npc;
+    }
+  }
+}
+
+// The items of the long rows' pieces (piece k of a row starting at st:
+// [st, b8 + tile) for k = 0, then [b8 + k*tile, b8 + (k+1)*tile) cut at the
+// row's end, b8 = st rounded down to 8), a warp per long row.
+__global__ void k_long_pieces(const i32* __restrict__ off, const i32* __restrict__ lrows,
+                              const i32* __restrict__ lpiece0, const i32* __restrict__ lfirst, i64 nlong, int tile,
+                              Item* __restrict__ items) {
+  const int lane = threadIdx.x & 31;
+  PWARP_STRIDE(L, nlong) {
+    const i32 r = lrows[L];
+    const i64 st = off[r], en = off[r + 1], b8 = st & ~7ll;
+    const i64 npr = (en - b8 + tile - 1) / tile;
+    const i64 it0 = lfirst[L], pc0 = lpiece0[L];
+    for (i64 k = lane; k < npr; k += 32) {
+      const i64 e0 = (k == 0) ? st : b8 + k * tile, e1 = min(en, b8 + (k + 1) * tile);
+      items[it0 + k] = Item{(int32_t)r, (int32_t)(-1 - (pc0 + k)), (int32_t)e0, (int32_t)e1};
     }
   }
 }
@@ -262,7 +285,8 @@ template <class T>
 __global__ void k_head_fill(const i32* __restrict__ off, const i32* __restrict__ idx, const T* __restrict__ val,
                             i64 m, const i32* __restrict__ slot, const i64* __restrict__ hoff,
                             const i64* __restrict__ toff, uint16_t* __restrict__ hslot, T* __restrict__ hval,
-                            i32* __restrict__ tidx, T* __restrict__ tval) {
+                            i32* __restrict__ tidx, T* __restrict__ tval, const SidePlanes sph,
+                            const SidePlanes spt) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   PWARP_STRIDE(r, m) {
@@ -280,10 +304,12 @@ __global__ void k_head_fill(const i32* __restrict__ off, const i32* __restrict__
         const i64 q = hp + __popc(hb & lt);
         hslot[q] = (uint16_t)sl;
         hval[q] = val[e];
+        sph.copy(e, q);
       } else if (ok) {
         const i64 q = tp + __popc(tb & lt);
         tidx[q] = col;
         tval[q] = val[e];
+        spt.copy(e, q);
       }
       hp += __popc(hb);
       tp += __popc(tb);
@@ -884,22 +910,47 @@ i64 panel_rows_cap(fvg_ctx* c) {
   return cap & ~3ll;
 }
 
+void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
+  b.alloc((size_t)(n + kPad) * elem, c->stream);
+  FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * elem, 0, (size_t)kPad * elem, c->stream));
+}
+
+// Allocates, for n entries, the planes of `dst` / `dlo` that the source holds
+// besides its master plane and returns the copy pointers.
+SidePlanes side_planes(fvg_ctx* c, const DBuf* src, const DBuf& slo, int master, DBuf* dst, DBuf& dlo, i64 n) {
+  SidePlanes sp;
+  if (master != FVG_F32 && src[FVG_F32].p) {
+    alloc_padded(c, dst[FVG_F32], n, 4);
+    sp.s32 = src[FVG_F32].as<float>();
+    sp.d32 = dst[FVG_F32].as<float>();
+  }
+  if (master != FVG_BF16 && src[FVG_BF16].p) {
+    alloc_padded(c, dst[FVG_BF16], n, 2);
+    sp.s16 = src[FVG_BF16].as<bf16>();
+    sp.d16 = dst[FVG_BF16].as<bf16>();
+  }
+  if (slo.p) {
+    alloc_padded(c, dlo, n, 2);
+    sp.slo = slo.as<bf16>();
+    sp.dlo = dlo.as<bf16>();
+  }
+  return sp;
+}
+
 template <class T>
 void fill_planes(fvg_ctx* c, const DevCRS& at, DevPanels& pn, const i32* B, const i64* poff64, const i64* flag,
                  const i64* coff) {
   const T* tv = at.val[pn.master].as<T>();
+  const SidePlanes spp = side_planes(c, at.val, at.lo, pn.master, pn.val, pn.lo, pn.E);
+  const SidePlanes spc = side_planes(c, at.val, at.lo, pn.master, pn.cold.val, pn.cold.lo, pn.cold.nnz);
   k_panel_fill<T><<<grid_n(32 * pn.npanels * pn.nhot), 256, 0, c->stream>>>(
-      B, poff64, at.idx.as<i32>(), tv, pn.nhot, pn.npanels, pn.rows, pn.prow.as<uint16_t>(), pn.val[pn.master].as<T>());
+      B, poff64, at.idx.as<i32>(), tv, pn.nhot, pn.npanels, pn.rows, pn.prow.as<uint16_t>(), pn.val[pn.master].as<T>(),
+      spp);
   check_launch("panel_fill");
   k_cold_fill<T><<<grid_n(32 * pn.n), 256, 0, c->stream>>>(at.off.as<i32>(), flag, coff, pn.n, at.idx.as<i32>(), tv,
-                                                           pn.cold.idx.as<i32>(), pn.cold.val[pn.master].as<T>());
+                                                           pn.cold.idx.as<i32>(), pn.cold.val[pn.master].as<T>(), spc);
   check_launch("cold_fill");
   count_launch(c, 2);
-}
-
-void alloc_padded(fvg_ctx* c, DBuf& b, i64 n, int elem) {
-  b.alloc((size_t)(n + kPad) * elem, c->stream);
-  FVG_CUDA(cudaMemsetAsync((char*)b.p + (size_t)n * elem, 0, (size_t)kPad * elem, c->stream));
 }
 
 }  // namespace
@@ -912,10 +963,10 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
   const i64 np = std::max<i64>(nchunks, 1) * sub;
   DBuf cnt, basev;
   cnt.alloc(sizeof(i32) * 3 * np, c->stream);
-  // a warp per chunk, 8 warps a CTA
-  const unsigned pg = (unsigned)std::min<i64>((np + 7) / 8, 1 << 20);
+  // a thread per chunk
+  const unsigned pg = (unsigned)std::min<i64>((np + 255) / 256, 1 << 20);
   k_panel_pack<<<pg, 256, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 0, cnt.as<i32>(), nullptr, nullptr,
-                                          nullptr, nullptr);
+                                          nullptr, nullptr, nullptr);
   check_launch("pack");
   count_launch(c);
   std::vector<i32> hc((size_t)(3 * np));
@@ -939,10 +990,20 @@ void device_pack(fvg_ctx* c, const i32* off, i64 nrows, i64 chunk, i64 nchunks, 
   o.items.alloc(sizeof(Item) * std::max<i64>(o.nitems, 1), c->stream);
   o.long_rows.alloc(sizeof(i32) * std::max<i64>(o.nlong, 1), c->stream);
   o.long_piece0.alloc(sizeof(i32) * (o.nlong + 1), c->stream);
+  DBuf lfirst;
+  lfirst.alloc(sizeof(i32) * std::max<i64>(o.nlong, 1), c->stream);
   k_panel_pack<<<pg, 256, 0, c->stream>>>(off, nrows, chunk, sub, np, tile, 1, nullptr, basev.as<i32>(),
-                                          o.items.as<Item>(), o.long_rows.as<i32>(), o.long_piece0.as<i32>());
+                                          o.items.as<Item>(), o.long_rows.as<i32>(), o.long_piece0.as<i32>(),
+                                          lfirst.as<i32>());
   check_launch("pack");
   count_launch(c);
+  if (o.nlong > 0) {
+    const unsigned lg = (unsigned)std::min<i64>((o.nlong + 7) / 8, 1 << 20);
+    k_long_pieces<<<lg, 256, 0, c->stream>>>(off, o.long_rows.as<i32>(), o.long_piece0.as<i32>(), lfirst.as<i32>(),
+                                             o.nlong, tile, o.items.as<Item>());
+    check_launch("long_pieces");
+    count_launch(c);
+  }
   const i32 npc = (i32)o.npieces;
   FVG_CUDA(cudaMemcpyAsync(o.long_piece0.as<i32>() + o.nlong, &npc, sizeof(i32), cudaMemcpyHostToDevice, c->stream));
   FVG_CUDA(cudaStreamSynchronize(c->stream));  // host values go out of scope
@@ -980,7 +1041,7 @@ void pack_split_items(fvg_ctx* c, DevPanels& pn) {
 
 void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
   PackOut o;
-  // each panel's rows in pieces of ~kPackRows rows, a warp each
+  // each panel's rows in pieces of ~kPackRows rows, a packing thread each
   const i64 sub = std::max<i64>(1, (nhot + kPackRows - 1) / kPackRows);
   device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o, sub);
   pn.nitems = o.nitems;
@@ -1228,11 +1289,13 @@ std::unique_ptr<DevPanels> head_build(fvg_ctx* c, const DevCRS& a, const DevCRS&
   count_launch(c);
   alloc_padded(c, tail.idx, tail.nnz, 4);
   alloc_padded(c, tail.val[master], tail.nnz, dtype_size(master));
+  const SidePlanes sph = side_planes(c, a.val, a.lo, master, hd->val, hd->lo, hd->E);
+  const SidePlanes spt = side_planes(c, a.val, a.lo, master, tail.val, tail.lo, tail.nnz);
   auto fill = [&](auto tag) {
     using T = decltype(tag);
     k_head_fill<T><<<grid_n(32 * m), 256, 0, c->stream>>>(
         a.off.as<i32>(), a.idx.as<i32>(), a.val[master].as<T>(), m, dslot.as<i32>(), hoff.as<i64>(), tof.as<i64>(),
-        hd->prow.as<uint16_t>(), hd->val[master].as<T>(), tail.idx.as<i32>(), tail.val[master].as<T>());
+        hd->prow.as<uint16_t>(), hd->val[master].as<T>(), tail.idx.as<i32>(), tail.val[master].as<T>(), sph, spt);
     check_launch("head_fill");
     count_launch(c);
   };

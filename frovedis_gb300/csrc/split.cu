@@ -55,14 +55,23 @@ unsigned grid_rows(fvg_ctx* c, i64 n, int per_sm = 8) {
 
 // residual plane: lo = BF16(v - FP32(v)) (one-off per matrix); flags a value
 // whose FP32 rounding overflows
+// (the FP32 plane holds FP32(v), so the residual follows from v alone: by
+// integer arithmetic on its bits, split_bits.h, where that applies)
 __global__ void k_split_plane(const double* __restrict__ v, const float* __restrict__ hi, bf16* __restrict__ lo,
                               i64 n, unsigned* __restrict__ bad) {
   unsigned b = 0;
   for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     const double x = v[i];
-    const float h = hi[i];
-    if (isinf(h) && !isinf(x)) b = 1;
-    lo[i] = __double2bfloat16(isinf(h) ? 0.0 : x - (double)h);
+    uint32_t hb;
+    uint16_t lb;
+    if (split_bits((uint64_t)__double_as_longlong(x), &hb, &lb)) {
+      if ((hb & 0x7fffffffu) == 0x7f800000u) b = 1;
+      lo[i] = __ushort_as_bfloat16(lb);
+    } else {
+      const float h = hi[i];
+      if (isinf(h) && !isinf(x)) b = 1;
+      lo[i] = __double2bfloat16(isinf(h) ? 0.0 : x - (double)h);
+    }
   }
   if (b) atomicOr(bad, 1u);
 }
