@@ -74,8 +74,11 @@ constexpr int kTileRows = 248;  // rows per tile (their offsets are staged in sh
 constexpr int kLaneWork = 32;   // products one lane may sum for one row in a tile
 // Rows one thread of the work-item packer walks in order (a tile never spans
 // two such chunks): short enough that the packers' sequential walks take a
-// fraction of a millisecond, long enough to fill kTileRows-row tiles.
+// fraction of a millisecond, long enough to fill kTileRows-row tiles.  The
+// panel and head layouts' rows are shorter (their items hold more rows), so
+// they are packed in longer chunks.
 constexpr i64 kPackRows = 256;
+constexpr i64 kPanelPackRows = 1024;
 // Lanes per row when a warp sums a tile of R rows: 32 / R rounded to a power
 // of two; tiles of 32 or more rows take rounds of 32 rows, one lane each.
 __host__ __device__ __forceinline__ int lanes_per_row(int R) {

@@ -1015,7 +1015,7 @@ namespace {
 void pack_split_items(fvg_ctx* c, DevPanels& pn) {
   const i64 nhot = pn.nhot, np = pn.npanels;
   PackOut o;
-  const i64 sub = std::max<i64>(1, (nhot + kPackRows - 1) / kPackRows);
+  const i64 sub = std::max<i64>(1, (nhot + kPanelPackRows - 1) / kPanelPackRows);
   device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kSplitTile, o, sub);
   auto it = std::make_unique<PanelItems>();
   it->tile = kSplitTile;
@@ -1041,8 +1041,8 @@ void pack_split_items(fvg_ctx* c, DevPanels& pn) {
 
 void pack_panels(fvg_ctx* c, DevPanels& pn, i64 nhot, i64 np) {
   PackOut o;
-  // each panel's rows in pieces of ~kPackRows rows, a packing thread each
-  const i64 sub = std::max<i64>(1, (nhot + kPackRows - 1) / kPackRows);
+  // each panel's rows in pieces of ~kPanelPackRows rows, a packing thread each
+  const i64 sub = std::max<i64>(1, (nhot + kPanelPackRows - 1) / kPanelPackRows);
   device_pack(c, pn.poff.as<i32>(), np * nhot, nhot, np, kWarpTile, o, sub);
   pn.nitems = o.nitems;
   pn.nlong = o.nlong;

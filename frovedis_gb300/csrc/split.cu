@@ -159,8 +159,11 @@ __device__ __forceinline__ df seg_scan(df v, bool reset, int lane) {
 // the chunk's two ends join the neighbouring lanes' through a segmented scan
 // in lane order.  A piece of a long row is one warp reduction.  Every sum has
 // a fixed order, so results are identical run to run.
+#ifndef FVG_SPLIT_CRS_CTAS
+#define FVG_SPLIT_CRS_CTAS 2
+#endif
 template <class YT>
-__global__ void __launch_bounds__(kThreads, 2) k_crs_split(const SplitK p) {
+__global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(const SplitK p) {
   __shared__ int soffs[kThreads / 32][kTileRows + 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int* soff = soffs[w];
