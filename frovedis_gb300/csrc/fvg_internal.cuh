@@ -434,7 +434,7 @@ void head_logreg_pass(fvg_ctx* c, DevPanels& hd, int storage, const float* w, co
 // columns from the panels, the rest from the cold CRS); the forward head's
 // partial per row into hd.ypan2 and the tail's product into wtx (df pairs).
 void panel_ensure_split(fvg_ctx* c, DevPanels& pn);
-i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn);
+i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn, bool y_df);
 void panel_trans_mv_split(fvg_ctx* c, DevPanels& pn, const void* r, double* y, void* scratch);
 void head_pass_split(fvg_ctx* c, DevPanels& hd, const void* w, void* wtx, void* scratch);
 
@@ -447,7 +447,7 @@ void crs_ensure_split(fvg_ctx* c, DevCRS& a, int master);
 void split_residual_plane(fvg_ctx* c, const DBuf* planes, i64 n, int master, DBuf& lo);
 void ensure_split_planes(fvg_ctx* c, DBuf* planes, i64 n, int master, DBuf& lo);
 void split_vector(fvg_ctx* c, const double* x, void* y, i64 n);  // y: float2[n]
-i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a);
+i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a, bool y_df);  // y_df: FP32-pair output (forward)
 // y = A x, x float2 pairs; y FP64 (y_df false) or float2 pairs
 void crs_pass_split(fvg_ctx* c, DevCRS& a, const void* x, bool y_df, void* y, void* scratch, int prof_key);
 struct GlmSplitArgs {

@@ -568,16 +568,16 @@ struct Evaluator {
       PT = panels_for(c, op->M);
       if (PT) {
         panel_ensure_split(c, *PT);
-        s3.alloc(panel_split_scratch_bytes(c, *PT), c->stream);
+        s3.alloc(panel_split_scratch_bytes(c, *PT, false), c->stream);
       }
       HD = head_for(c, op->M);
       if (HD) {
         panel_ensure_split(c, *HD);
-        s4.alloc(panel_split_scratch_bytes(c, *HD), c->stream);
+        s4.alloc(panel_split_scratch_bytes(c, *HD, true), c->stream);
       }
     }
-    if (!HD) s1.alloc(crs_split_scratch_bytes(c, *op->A), c->stream);
-    if (!PT) s2.alloc(crs_split_scratch_bytes(c, *op->AT), c->stream);
+    if (!HD) s1.alloc(crs_split_scratch_bytes(c, *op->A, true), c->stream);
+    if (!PT) s2.alloc(crs_split_scratch_bytes(c, *op->AT, false), c->stream);
   }
   void eval_split(const void* x, const double* b, double* grad, double* out) {
     const i64 g = glm_split_grid(c, op->m);

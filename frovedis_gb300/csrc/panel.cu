@@ -1499,7 +1499,9 @@ void panel_ensure_split(fvg_ctx* c, DevPanels& pn) {
   }
 }
 
-i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn) { return crs_split_scratch_bytes(c, pn.cold); }
+i64 panel_split_scratch_bytes(fvg_ctx* c, DevPanels& pn, bool y_df) {
+  return crs_split_scratch_bytes(c, pn.cold, y_df);
+}
 
 void panel_trans_mv_split(fvg_ctx* c, DevPanels& pn, const void* r, double* y, void* scratch) {
   panel_ensure_split(c, pn);

@@ -22,6 +22,7 @@
 // results are identical run to run.
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "device_common.cuh"
 #include "df64.cuh"
@@ -44,8 +45,13 @@ void df64_init(fvg_ctx* c) {
 namespace {
 
 constexpr int kSplitThreads = 256;
-// CRS work items of the split kernel: a staged item (16-aligned ends) fits 32 lanes x 16 entries
-constexpr int kSplitCrsTile = 480;
+// Entries per lane of the split CRS kernel and its work items' size (an item
+// from its first entry rounded down to CH fits 32 lanes x CH).  The forward
+// products (A's rows, the head's row tails: FP32-pair output) run 8 entries a
+// lane at 3 CTAs per SM, the transposed ones (rare columns: FP64 output) 16
+// at 2: the measured best of 8 / 16 entries and 2 / 3 / 4 CTAs for each.
+constexpr int split_crs_ch(bool fwd) { return fwd ? 8 : 16; }
+constexpr int split_crs_tile(bool fwd) { return 30 * split_crs_ch(fwd); }
 
 unsigned grid_rows(fvg_ctx* c, i64 n, int per_sm = 8) {
   i64 g = (n + kSplitThreads - 1) / kSplitThreads;
@@ -151,19 +157,17 @@ __device__ __forceinline__ df seg_scan(df v, bool reset, int lane) {
 
 // Persistent kernel over CRS work items of at most kSplitCrsTile entries
 // (tiles of short rows, pieces of long rows; the packing of k_crs).  Lane L
-// takes the 16 entries q0 + 16L .. q0 + 16L + 15 (q0 = the item's first entry
-// rounded down to 16): column ids, FP32 values and BF16 residuals come in
+// takes the CH entries q0 + CH*L .. q0 + CH*L + CH - 1 (q0 = the item's first
+// entry rounded down to CH): column ids, FP32 values and BF16 residuals come in
 // 128-bit loads, x's pairs are gathered, each product is made exact (p + t)
 // and added to the lane's current row segment with TwoSum.  A row that
 // starts and ends inside the chunk is written at once; the segments open at
 // the chunk's two ends join the neighbouring lanes' through a segmented scan
 // in lane order.  A piece of a long row is one warp reduction.  Every sum has
 // a fixed order, so results are identical run to run.
-#ifndef FVG_SPLIT_CRS_CTAS
-#define FVG_SPLIT_CRS_CTAS 2
-#endif
 template <class YT>
-__global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(const SplitK p) {
+__global__ void __launch_bounds__(kThreads, std::is_same<YT, float2>::value ? 3 : 2) k_crs_split(const SplitK p) {
+  constexpr int CH = split_crs_ch(std::is_same<YT, float2>::value);
   __shared__ int soffs[kThreads / 32][kTileRows + 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int* soff = soffs[w];
@@ -174,46 +178,46 @@ __global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(cons
   for (; t < n; t += W) {
     const Item it = nx;
     if (t + W < n) nx = p.items[t + W];
-    const int q0 = it.e0 & ~15;
+    const int q0 = it.e0 & ~(CH - 1);
     const bool tile = it.r1 >= 0;
     const int R = tile ? it.r1 - it.r0 : 0;
     if (tile)
       for (int k = lane; k <= R; k += 32) soff[k] = __ldg(p.off + it.r0 + k) - q0;
-    const int lo_e = max(it.e0 - q0, lane * 16), hi_e = min(it.e1 - q0, lane * 16 + 16);
+    const int lo_e = max(it.e0 - q0, lane * CH), hi_e = min(it.e1 - q0, lane * CH + CH);
     // the chunk (the arrays are padded past the last nonzero, and q0 + 16L
     // stays below it whenever the lane has entries)
-    int c[16];
-    float hv[16];
-    unsigned lw[8];
+    int c[CH];
+    float hv[CH];
+    unsigned lw[CH / 2];
     if (lo_e < hi_e) {
-      const i64 b = (i64)q0 + lane * 16;
+      const i64 b = (i64)q0 + lane * CH;
       const int4* ip = reinterpret_cast<const int4*>(p.idx + b);
       const float4* hp = reinterpret_cast<const float4*>(p.vh + b);
       const uint4* lp = reinterpret_cast<const uint4*>(p.vl + b);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < CH / 4; q++) {
         const int4 iv = __ldcs(ip + q);
         const float4 fv = __ldcs(hp + q);
         c[4 * q] = iv.x; c[4 * q + 1] = iv.y; c[4 * q + 2] = iv.z; c[4 * q + 3] = iv.w;
         hv[4 * q] = fv.x; hv[4 * q + 1] = fv.y; hv[4 * q + 2] = fv.z; hv[4 * q + 3] = fv.w;
       }
 #pragma unroll
-      for (int q = 0; q < 2; q++) {
+      for (int q = 0; q < CH / 8; q++) {
         const uint4 lv = __ldcs(lp + q);
         lw[4 * q] = lv.x; lw[4 * q + 1] = lv.y; lw[4 * q + 2] = lv.z; lw[4 * q + 3] = lv.w;
       }
     }
-    float2 xv[16];
+    float2 xv[CH];
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const int e = lane * 16 + k;
+    for (int k = 0; k < CH; k++) {
+      const int e = lane * CH + k;
       xv[k] = (e >= lo_e && e < hi_e) ? __ldg(p.x + c[k]) : make_float2(0.f, 0.f);
     }
     if (!tile) {
       DfAcc acc;
 #pragma unroll
-      for (int k = 0; k < 16; k++) {
-        const int e = lane * 16 + k;
+      for (int k = 0; k < CH; k++) {
+        const int e = lane * CH + k;
         if (e >= lo_e && e < hi_e) {
           const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
           float pp, tt;
@@ -229,11 +233,11 @@ __global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(cons
       __syncwarp();  // soff
       for (int j = lane; j < R; j += 32)
         if (soff[j] == soff[j + 1]) store_row<YT>(p.y, it.r0 + j, df{0.f, 0.f});  // empty rows
-      // the lane's 16 products (zero outside its valid range)
-      float pp[16], tt[16];
+      // the lane's CH products (zero outside its valid range)
+      float pp[CH], tt[CH];
 #pragma unroll
-      for (int k = 0; k < 16; k++) {
-        const int e = lane * 16 + k;
+      for (int k = 0; k < CH; k++) {
+        const int e = lane * CH + k;
         const bool ok = e >= lo_e && e < hi_e;
         const float vl = __uint_as_float((k & 1) ? (lw[k >> 1] & 0xffff0000u) : (lw[k >> 1] << 16));
         float a, b;
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(cons
         starts = soff[j] == lo_e;
         nb = soff[j + 1];
         while (nb < hi_e) {
-          B |= 1u << (nb - lane * 16);
+          B |= 1u << (nb - lane * CH);
           do {
             j++;
             nb = soff[j + 1];
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(cons
         }
       }
       df H, T;
-      chunk_segments<16>(pp, tt, B, H, T);
+      chunk_segments<CH>(pp, tt, B, H, T);
       if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
         unsigned rest = B & (B - 1);
         int a = __ffs(B) - 1, jj = j0;
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, FVG_SPLIT_CRS_CTAS) k_crs_split(cons
         while (rest) {
           const int b = __ffs(rest) - 1;
           rest &= rest - 1;
-          store_row<YT>(p.y, it.r0 + jj, chunk_range<16>(pp, tt, a, b));
+          store_row<YT>(p.y, it.r0 + jj, chunk_range<CH>(pp, tt, a, b));
           a = b;
           do {
             jj++;
@@ -449,17 +453,17 @@ void split_vector(fvg_ctx* c, const double* x, void* y, i64 n) {
   count_launch(c);
 }
 
-i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a) {
-  const Sched& s = crs_sched(c, a, kSplitCrsTile);
+i64 crs_split_scratch_bytes(fvg_ctx* c, DevCRS& a, bool y_df) {
+  const Sched& s = crs_sched(c, a, split_crs_tile(y_df));
   return (i64)sizeof(float2) * std::max<i64>(s.npieces, 1);
 }
 
 void crs_pass_split(fvg_ctx* c, DevCRS& a, const void* x, bool y_df, void* y, void* scratch, int prof_key) {
-  const Sched& s = crs_sched(c, a, kSplitCrsTile);
+  const Sched& s = crs_sched(c, a, split_crs_tile(y_df));
   if (!a.val[FVG_F32].p || !a.lo.p) fail(FVG_ERR_INTERNAL, "split storage planes missing");
   DBuf tmp;
   if (!scratch) {
-    tmp.alloc((size_t)crs_split_scratch_bytes(c, a), c->stream);
+    tmp.alloc((size_t)crs_split_scratch_bytes(c, a, y_df), c->stream);
     scratch = tmp.p;
   }
   ProfScope pr(c, prof_key);
