@@ -46,7 +46,7 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # row panels (rare-column k_crs + k_panel + k_panel_colsum) 288.54 MB /
 # 376.01 MB.  FP32 values, full size: pass 1 4060.5 MB / 4964.0 MB, pass 2
 # 4150.6 MB / 4852.0 MB.
-NCU_TRAFFIC_RATIO = {"split": {"pass1": 532.6 / 620.81, "pass2": 529.5 / 609.21},
+NCU_TRAFFIC_RATIO = {"split": {"pass1": 537.6 / 620.81, "pass2": 534.7 / 609.21},
                      "bf16": {"pass1": 285.42 / 380.01, "pass2": 288.54 / 376.01},
                      "f32": {"pass1": 4060.5 / 4964.0, "pass2": 4150.6 / 4852.0}}
 TRAFFIC_SOURCE = {"split": "ncu dram bytes of every kernel of a pass / algorithmic bytes per pass (1/10-row "
@@ -226,6 +226,78 @@ def parity_of(r, ref):
     return out
 
 
+def e2e_steps(ctx, args, m, n, off, idx, val, label, kw):
+    """`args.e2e_steps` end-to-end trainings through the C ABI from pinned host
+    buffers: upload (validated CRS + the arm's value planes), the transposed
+    copy and layouts, training, read-back.  Returns the total ms, iterations,
+    the per-phase seconds (with the library's device-time profile of the
+    set-up and training), and the host-to-device / device-to-host bytes of a
+    step."""
+    import torch
+
+    import frovedis_gb300 as fv
+    nnz = int(off[-1])
+    e2e_ms = 0.0
+    e2e_iters = 0
+    h2d = (m + 1) * 4 + nnz * 12 + m * 8 + n * 8
+    d2h = n * 8 + 16
+    torch.cuda.synchronize()
+    phases = {"upload_s": 0.0, "prepare_s": 0.0, "train_s": 0.0}
+    # the step's inputs come from pinned host memory (a loader's staging
+    # buffers), allocated and filled once before the timed steps
+    pinned = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (off, idx, val, label)] \
+        if args.e2e_steps else []
+    p_off, p_idx, p_val, p_label = (t.numpy() for t in pinned) if pinned else (off, idx, val, label)
+    ctx.reset_profile()
+    ctx.set_profiling(True)
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        B = ctx.matrix(m, n, p_off, p_idx, p_val)
+        set_panels(B, args.panels)
+        if args.storage != "f64":
+            B.add_storage(args.storage)
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        B.prepare("CRS", transpose=True)
+        if args.storage != "f64":
+            B.add_storage(args.storage)
+        ctx.synchronize()
+        t2 = time.perf_counter()
+        rr = fv.logreg_lbfgs(B, p_label, storage=args.storage, **kw)
+        B.close()
+        ctx.synchronize()
+        t3 = time.perf_counter()
+        phases["upload_s"] += t1 - t0
+        phases["prepare_s"] += t2 - t1
+        phases["train_s"] += t3 - t2
+        e2e_ms += (t3 - t0) * 1e3
+        e2e_iters += rr["n_iter"]
+    ctx.set_profiling(False)
+    for key in ("transpose", "panel_build", "head_build", "schedule"):
+        phases[key + "_device_s"] = ctx.profile(key)[0] / 1e3
+    phases["train_products_s"] = sum(ctx.profile(k)[0] for k in ("pass1", "pass2", "pass1_f32", "pass2_f32")) / 1e3
+    phases["train_lbfgs_vector_s"] = ctx.profile("lbfgs_vec")[0] / 1e3
+    return e2e_ms, e2e_iters, phases, h2d, d2h
+
+
+def run_e2e_only(args):
+    """--e2e-only: the headline workload's end-to-end steps alone (set-up and
+    training from host buffers), e.g. for a launch list of the set-up."""
+    import frovedis_gb300 as fv
+    spec, off, idx, val, label = make_data(args.scale, cols=args.cols)
+    m, n = spec.m, spec.n
+    ctx = fv.Context(0)
+    kw = dict(num_iter=args.iters, reg_type="L2", reg_param=1e-4, w0=np.zeros(n))
+    ms, iters, phases, h2d, d2h = e2e_steps(ctx, args, m, n, off, idx, val, label, kw)
+    ctx.close()
+    steps = max(args.e2e_steps, 1)
+    print(json.dumps({"metric": METRIC, "e2e": {"value": iters / (ms / 1e3) if ms > 0 else None, "unit": "iters/s",
+                                                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                                                "phases": {k: v / steps for k, v in phases.items()}},
+                      "config": {"workload": "logreg-lbfgs-10Mx1M-nnz6e8", "scale": args.scale,
+                                 "iterations_per_step": args.iters, "storage": args.storage}}), flush=True)
+
+
 def run_gpu(args):
     import torch
 
@@ -305,47 +377,7 @@ def run_gpu(args):
     # end to end through the C ABI with host buffers: upload (validated CRS +
     # the arm's value planes), the transposed copy, training, read-back
     A.close()
-    e2e_ms = 0.0
-    e2e_iters = 0
-    h2d = (m + 1) * 4 + nnz * 12 + m * 8 + n * 8
-    d2h = n * 8 + 16
-    torch.cuda.synchronize()
-    phases = {"upload_s": 0.0, "prepare_s": 0.0, "train_s": 0.0}
-    # the step's inputs come from pinned host memory (a loader's staging
-    # buffers), allocated and filled once before the timed steps
-    pinned = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (off, idx, val, label)] \
-        if args.e2e_steps else []
-    p_off, p_idx, p_val, p_label = (t.numpy() for t in pinned) if pinned else (off, idx, val, label)
-    ctx.reset_profile()
-    ctx.set_profiling(True)
-    for _ in range(args.e2e_steps):
-        t0 = time.perf_counter()
-        B = ctx.matrix(m, n, p_off, p_idx, p_val)
-        set_panels(B, args.panels)
-        if args.storage != "f64":
-            B.add_storage(args.storage)
-        ctx.synchronize()
-        t1 = time.perf_counter()
-        B.prepare("CRS", transpose=True)
-        if args.storage != "f64":
-            B.add_storage(args.storage)
-        ctx.synchronize()
-        t2 = time.perf_counter()
-        rr = fv.logreg_lbfgs(B, p_label, storage=args.storage, **kw)
-        B.close()
-        ctx.synchronize()
-        t3 = time.perf_counter()
-        phases["upload_s"] += t1 - t0
-        phases["prepare_s"] += t2 - t1
-        phases["train_s"] += t3 - t2
-        e2e_ms += (t3 - t0) * 1e3
-        e2e_iters += rr["n_iter"]
-    ctx.set_profiling(False)
-    for key in ("transpose", "panel_build", "head_build", "schedule"):
-        phases[key + "_device_s"] = ctx.profile(key)[0] / 1e3
-    phases["train_products_s"] = sum(ctx.profile(k)[0] for k in ("pass1", "pass2", "pass1_f32", "pass2_f32")) / 1e3
-    phases["train_lbfgs_vector_s"] = ctx.profile("lbfgs_vec")[0] / 1e3
-    del pinned, p_off, p_idx, p_val, p_label
+    e2e_ms, e2e_iters, phases, h2d, d2h = e2e_steps(ctx, args, m, n, off, idx, val, label, kw)
     e2e_ms = allmax(world, e2e_ms)
     e2e_value = e2e_iters * world / (e2e_ms / 1e3) if e2e_ms > 0 else None
 
@@ -806,6 +838,7 @@ def main():
     ap.add_argument("--skip-spmv", action="store_true")
     ap.add_argument("--spmv-scale", type=float, default=1.0)
     ap.add_argument("--spmv-only", action="store_true", help="run only the SpMV kernel suite")
+    ap.add_argument("--e2e-only", action="store_true", help="run only the end-to-end steps (set-up and training)")
     ap.add_argument("--workload", default="lbfgs", choices=["lbfgs", "regpath", "multinomial"])
     ap.add_argument("--datasets", type=int, default=16, help="regpath: number of datasets")
     ap.add_argument("--regpath-datasets", type=int, default=16, help="datasets of the batched summary line")
@@ -826,6 +859,9 @@ def main():
         if args.storage == "split":  # the multinomial trainer keeps FP64 / FP32 / BF16 values
             args.storage = "bf16"
         run_multinomial(args)
+        return
+    if args.e2e_only:
+        run_e2e_only(args)
         return
     if args.spmv_only:
         import frovedis_gb300 as fv

@@ -167,8 +167,8 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
   // column) that carries each one's row and value, so the sorted rows and
   // values are the transposed copy's column ids and values.
   DBuf rows, keys;
-  rows.alloc(sizeof(uint32_t) * a.nnz, c->stream);
-  keys.alloc(sizeof(uint32_t) * a.nnz, c->stream);
+  rows.alloc(sizeof(uint32_t) * (a.nnz + kRsPad), c->stream);
+  keys.alloc(sizeof(uint32_t) * (a.nnz + kRsPad), c->stream);
   k_expand_rows<<<grid_n(32 * a.m), 256, 0, c->stream>>>(a.off.as<i32>(), a.m, rows.as<uint32_t>());
   check_launch("expand_rows");
   count_launch(c);
@@ -190,6 +190,7 @@ void crs_build_transpose(fvg_ctx* c, const DevCRS& a, DevCRS& t, int master) {
   count_launch(c);
   keys.release();
   t.max_row = max_row_len(c, t.off.as<i32>(), t.m);
+  check_device_error(c);  // the sort's bounded copy waits
 }
 
 // ---------------------------------------------------------------- schedule

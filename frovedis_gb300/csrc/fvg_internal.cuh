@@ -311,6 +311,9 @@ int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem = 0);
 void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n);
 // stable LSD radix sort of (key,val) u32 pairs by the low `bits` bits of key
 void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bits);
+// stable sort of (key, row, value) by key; every array padded by kRsPad elements
+constexpr i64 kRsPad = 16;
+static_assert(kPad >= kRsPad, "CRS arrays carry the sort's padding");
 template <class T>
 void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, const T* vin, uint32_t* kout,
                        uint32_t* rout, T* vout, i64 n, int bits);

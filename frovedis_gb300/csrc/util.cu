@@ -6,6 +6,7 @@
 #include <mutex>
 #include <utility>
 
+#include "bulk_copy.cuh"
 #include "fvg_internal.cuh"
 
 namespace fvg {
@@ -285,11 +286,12 @@ __device__ __forceinline__ void scan256_exclusive(int* v) {
 }
 
 // Ranks of a tile's keys (warp w: keys [w*512, w*512+512) of the tile in 16
-// rounds of 32) and the digit bookkeeping of the downsweeps: on return
+// rounds of 32; key i at kin[i - key_base]) and the digit bookkeeping of the
+// downsweeps: on return
 // wcnt[w][d] is warp w's first slot within digit d's run of the tile,
 // dstart[d] the run's first tile slot, rank[r] the key's rank among the
 // warp's keys of its digit (-1 past n).  Ranks follow the input order.
-__device__ __forceinline__ void rs_rank_tile(const uint32_t* __restrict__ kin, i64 n, int shift,
+__device__ __forceinline__ void rs_rank_tile(const uint32_t* __restrict__ kin, i64 key_base, i64 n, int shift,
                                              uint32_t (&key)[kRsRounds], int (&rank)[kRsRounds],
                                              int (*wcnt)[256], int* dstart) {
   for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
@@ -301,7 +303,7 @@ __device__ __forceinline__ void rs_rank_tile(const uint32_t* __restrict__ kin, i
   for (int r = 0; r < kRsRounds; r++) {
     i64 i = base + r * 32 + lane;
     bool ok = i < n;
-    key[r] = ok ? kin[i] : 0u;
+    key[r] = ok ? kin[i - key_base] : 0u;
     int d = ok ? (int)((key[r] >> shift) & 255u) : 256 + lane;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     int before = __popc(peers & lt);
@@ -338,7 +340,7 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t key[kRsRounds];
   int rank[kRsRounds];
-  rs_rank_tile(kin, n, shift, key, rank, wcnt, dstart);
+  rs_rank_tile(kin, 0, n, shift, key, rank, wcnt, dstart);
   const i64 base = (i64)blockIdx.x * kRsTile + (i64)w * (kRsRounds * 32);
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
@@ -360,35 +362,56 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
   }
 }
 
-// Downsweep carrying a (row, value) payload: the tile's rows and values are
-// staged in shared memory in input order (coalesced loads), the ranked keys
-// go to their tile slots with their input position, and the write-back
-// reads each slot's row and value from the staged copy.  Dynamic shared
-// memory: kRsTile rows (uint32) + kRsTile values.
+// Downsweep carrying a (row, value) payload.  Thread 0 stages the tile's keys,
+// rows and values in shared memory with three bulk copies on one mbarrier
+// (the copies' sizes rounded up to 16 bytes: the arrays are padded past n);
+// the warps rank the staged keys, the ranked keys go to their tile slots with
+// their input position, and the write-back reads each slot's row and value
+// from the staged copy.  Dynamic shared memory: kRsTile keys and rows
+// (uint32) and kRsTile values.  A copy wait that runs out of polls sets bit 2
+// of *err and the CTA returns without writing.
 template <class T>
 __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep_rv(const uint32_t* __restrict__ kin,
                                                                 const uint32_t* __restrict__ rin,
                                                                 const T* __restrict__ vin, uint32_t* __restrict__ kout,
                                                                 uint32_t* __restrict__ rout, T* __restrict__ vout,
                                                                 i64 n, int shift, i64 nblocks,
-                                                                const i64* __restrict__ goff) {
+                                                                const i64* __restrict__ goff, unsigned* err,
+                                                                unsigned limit) {
   __shared__ int wcnt[kRsWarps][256];
   __shared__ int dstart[256];
   __shared__ uint32_t skey[kRsTile];
   __shared__ uint16_t spos[kRsTile];
+  __shared__ __align__(8) uint64_t bar;
   extern __shared__ __align__(16) unsigned char rs_dyn[];
-  uint32_t* srow = reinterpret_cast<uint32_t*>(rs_dyn);
-  T* sv = reinterpret_cast<T*>(rs_dyn + sizeof(uint32_t) * kRsTile);
+  uint32_t* kst = reinterpret_cast<uint32_t*>(rs_dyn);
+  uint32_t* srow = kst + kRsTile;
+  T* sv = reinterpret_cast<T*>(srow + kRsTile);
   const i64 t0 = (i64)blockIdx.x * kRsTile;
   const int cnt = (int)(n - t0 < kRsTile ? n - t0 : kRsTile);
-  for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
-    srow[i] = rin[t0 + i];
-    sv[i] = vin[t0 + i];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned b4 = (unsigned)((cnt * 4 + 15) & ~15), bv = (unsigned)((cnt * (int)sizeof(T) + 15) & ~15);
+    const uint64_t pol = policy_evict_first();
+    mbar_arrive_expect_tx(&bar, 2 * b4 + bv);
+    bulk_g2s(kst, kin + t0, b4, &bar, pol);
+    bulk_g2s(srow, rin + t0, b4, &bar, pol);
+    bulk_g2s(sv, vin + t0, bv, &bar, pol);
+  }
+  const bool ok = mbar_wait_bounded(&bar, 0, err, limit);
+  if (!__syncthreads_and(ok)) {
+    if (ok) return;  // another warp gave up: its error bit is set
+    mbar_wait_bounded(&bar, 0, nullptr, kCopyPolls);  // drain the copies in flight
+    return;
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t key[kRsRounds];
   int rank[kRsRounds];
-  rs_rank_tile(kin, n, shift, key, rank, wcnt, dstart);  // (its barriers also order the staging)
+  rs_rank_tile(kst, t0, n, shift, key, rank, wcnt, dstart);
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
     if (rank[r] < 0) continue;
@@ -437,7 +460,8 @@ void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bit
 
 // Stable sort of (key, row, value) triples by the low `bits` bits of the
 // key, from (kin, rin, vin) into (kout, rout, vout); the inputs are not
-// changed.  Passes alternate between the outputs and one set of temporaries,
+// changed.  All six arrays hold kRsPad elements past n (the tiles are staged
+// with 16-byte bulk copies).  Passes alternate between the outputs and one set of temporaries,
 // starting on the side that makes the last pass write the outputs.
 template <class T>
 void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, const T* vin, uint32_t* kout,
@@ -445,13 +469,13 @@ void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, con
   if (n <= 0) return;
   const int passes = std::max(1, (bits + 7) / 8);
   const i64 nb = (n + kRsTile - 1) / kRsTile;
-  const int dyn = (int)((sizeof(uint32_t) + sizeof(T)) * kRsTile);
+  const int dyn = (int)((2 * sizeof(uint32_t) + sizeof(T)) * kRsTile);
   FVG_CUDA(cudaFuncSetAttribute(k_rs_downsweep_rv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   DBuf kt, rt, vt, hist, goff;
-  if (passes > 1) {
-    kt.alloc(sizeof(uint32_t) * n, c->stream);
-    rt.alloc(sizeof(uint32_t) * n, c->stream);
-    vt.alloc(sizeof(T) * n, c->stream);
+  if (passes > 1) {  // padded: the staging copies read up to 15 bytes past n
+    kt.alloc(sizeof(uint32_t) * (n + kRsPad), c->stream);
+    rt.alloc(sizeof(uint32_t) * (n + kRsPad), c->stream);
+    vt.alloc(sizeof(T) * (n + kRsPad), c->stream);
   }
   hist.alloc(sizeof(i64) * 256 * nb, c->stream);
   goff.alloc(sizeof(i64) * (256 * nb + 1), c->stream);
@@ -467,7 +491,7 @@ void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, con
     check_launch("rs_upsweep");
     scan_i64(c, hist.as<i64>(), goff.as<i64>(), 256 * nb);
     k_rs_downsweep_rv<T><<<(unsigned)nb, kRsThreads, dyn, c->stream>>>(ks, rs, vs, kd, rd, vd, n, shift, nb,
-                                                                      goff.as<i64>());
+                                                                      goff.as<i64>(), c->dev_err, copy_polls(c));
     check_launch("rs_downsweep_rv");
     count_launch(c, 2);
     ks = kd;
