@@ -151,7 +151,7 @@ __global__ void k_cold_fill(const i32* __restrict__ toff, const i64* __restrict_
 // (tiles of short rows within `tile` entries, kTileRows rows and kLaneWork
 // products per lane; longer rows in pieces cut at 8-element boundaries).  The
 // greedy packing is sequential within a chunk; a thread walks its chunk's
-// offsets in order.  Pass 0 counts each chunk's items, long rows and pieces;
+// offsets in order, loading them 8 at a time.  Pass 0 counts each chunk's items, long rows and pieces;
 // pass 1 writes them at the scanned offsets `base` (chunk-major: a chunk's
 // items, long rows and pieces are contiguous and numbered globally).
 __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i64 sub, i64 np, int tile, int write,
@@ -165,8 +165,7 @@ __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i
     i32 ni = 0, nl = 0, npc = 0;
     i64 t0 = r0, tnnz = 0, tmax = 0;
     i32 o_cur = off[r0], o_t0 = o_cur;  // off[r], off[t0]
-    for (i64 r = r0; r < r1; r++) {
-      const i32 o_next = off[r + 1];
+    auto row = [&](i64 r, i32 o_next) {
       const i64 len = (i64)o_next - o_cur;
       if (len > tile) {
         if (r > t0) {
@@ -203,7 +202,17 @@ __global__ void k_panel_pack(const i32* __restrict__ off, i64 nrows, i64 nhot, i
         tmax = max(tmax, len);
       }
       o_cur = o_next;
+    };
+    // the offsets of 8 rows are loaded together, then the rows walked in order
+    i64 r = r0;
+    for (; r + 8 <= r1; r += 8) {
+      i32 o[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) o[q] = off[r + 1 + q];
+#pragma unroll
+      for (int q = 0; q < 8; q++) row(r + q, o[q]);
     }
+    for (; r < r1; r++) row(r, off[r + 1]);
     if (r1 > t0) {
       if (write) items[bi + ni] = Item{(int32_t)t0, (int32_t)r1, o_t0, o_cur};
       ni++;
