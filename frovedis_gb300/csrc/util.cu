@@ -252,14 +252,16 @@ void scan_i64(fvg_ctx* c, const i64* in, i64* out, i64 n) {
 // rounds of 32 consecutive keys with __match_any_sync, so the rank order is
 // the input order (stability).
 constexpr int kRsThreads = 256, kRsWarps = 8, kRsRounds = 16, kRsTile = kRsThreads * kRsRounds;
+constexpr int kRsRoundsRv = 12, kRsTileRv = kRsThreads * kRsRoundsRv;  // the payload-carrying sort
 
+template <int R>
 __global__ void k_rs_upsweep(const uint32_t* __restrict__ keys, i64 n, int shift, i64 nblocks,
                              i64* __restrict__ hist) {
   __shared__ int cnt[256];
   cnt[threadIdx.x] = 0;
   __syncthreads();
-  i64 base = (i64)blockIdx.x * kRsTile;
-  for (int k = 0; k < kRsRounds; k++) {
+  i64 base = (i64)blockIdx.x * (kRsThreads * R);
+  for (int k = 0; k < R; k++) {
     i64 i = base + (i64)k * kRsThreads + threadIdx.x;
     if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1);
   }
@@ -291,16 +293,16 @@ __device__ __forceinline__ void scan256_exclusive(int* v) {
 // wcnt[w][d] is warp w's first slot within digit d's run of the tile,
 // dstart[d] the run's first tile slot, rank[r] the key's rank among the
 // warp's keys of its digit (-1 past n).  Ranks follow the input order.
+template <int R>
 __device__ __forceinline__ void rs_rank_tile(const uint32_t* __restrict__ kin, i64 key_base, i64 n, int shift,
-                                             uint32_t (&key)[kRsRounds], int (&rank)[kRsRounds],
-                                             int (*wcnt)[256], int* dstart) {
+                                             uint32_t (&key)[R], int (&rank)[R], int (*wcnt)[256], int* dstart) {
   for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  const i64 base = (i64)blockIdx.x * kRsTile + (i64)w * (kRsRounds * 32);
+  const i64 base = (i64)blockIdx.x * (kRsThreads * R) + (i64)w * (R * 32);
 #pragma unroll
-  for (int r = 0; r < kRsRounds; r++) {
+  for (int r = 0; r < R; r++) {
     i64 i = base + r * 32 + lane;
     bool ok = i < n;
     key[r] = ok ? kin[i - key_base] : 0u;
@@ -340,7 +342,7 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t key[kRsRounds];
   int rank[kRsRounds];
-  rs_rank_tile(kin, 0, n, shift, key, rank, wcnt, dstart);
+  rs_rank_tile<kRsRounds>(kin, 0, n, shift, key, rank, wcnt, dstart);
   const i64 base = (i64)blockIdx.x * kRsTile + (i64)w * (kRsRounds * 32);
 #pragma unroll
   for (int r = 0; r < kRsRounds; r++) {
@@ -378,17 +380,17 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep_rv(const uint32_t* 
                                                                 i64 n, int shift, i64 nblocks,
                                                                 const i64* __restrict__ goff, unsigned* err,
                                                                 unsigned limit) {
+  constexpr int R = kRsRoundsRv, TILE = kRsTileRv;
   __shared__ int wcnt[kRsWarps][256];
   __shared__ int dstart[256];
-  __shared__ uint32_t skey[kRsTile];
-  __shared__ uint16_t spos[kRsTile];
+  __shared__ uint16_t spos[TILE];
   __shared__ __align__(8) uint64_t bar;
   extern __shared__ __align__(16) unsigned char rs_dyn[];
-  uint32_t* kst = reinterpret_cast<uint32_t*>(rs_dyn);
-  uint32_t* srow = kst + kRsTile;
-  T* sv = reinterpret_cast<T*>(srow + kRsTile);
-  const i64 t0 = (i64)blockIdx.x * kRsTile;
-  const int cnt = (int)(n - t0 < kRsTile ? n - t0 : kRsTile);
+  uint32_t* kst = reinterpret_cast<uint32_t*>(rs_dyn);  // staged keys, then the tile's sorted keys
+  uint32_t* srow = kst + TILE;
+  T* sv = reinterpret_cast<T*>(srow + TILE);
+  const i64 t0 = (i64)blockIdx.x * TILE;
+  const int cnt = (int)(n - t0 < TILE ? n - t0 : TILE);
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     fence_mbar_init();
@@ -409,20 +411,20 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep_rv(const uint32_t* 
     return;
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t key[kRsRounds];
-  int rank[kRsRounds];
-  rs_rank_tile(kst, t0, n, shift, key, rank, wcnt, dstart);
+  uint32_t key[R];
+  int rank[R];
+  rs_rank_tile<R>(kst, t0, n, shift, key, rank, wcnt, dstart);  // ends with a barrier: kst is free
 #pragma unroll
-  for (int r = 0; r < kRsRounds; r++) {
+  for (int r = 0; r < R; r++) {
     if (rank[r] < 0) continue;
     const int d = (int)((key[r] >> shift) & 255u);
     const int lp = dstart[d] + wcnt[w][d] + rank[r];
-    skey[lp] = key[r];
-    spos[lp] = (uint16_t)(w * (kRsRounds * 32) + r * 32 + lane);
+    kst[lp] = key[r];
+    spos[lp] = (uint16_t)(w * (R * 32) + r * 32 + lane);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
-    const uint32_t k = skey[i];
+    const uint32_t k = kst[i];
     const int s = spos[i];
     const int d = (int)((k >> shift) & 255u);
     const i64 pos = goff[(i64)d * nblocks + blockIdx.x] + (i - dstart[d]);
@@ -443,7 +445,7 @@ void radix_sort_pairs(fvg_ctx* c, uint32_t* keys, uint32_t* vals, i64 n, int bit
   uint32_t *ka = keys, *va = vals, *kb = k2.as<uint32_t>(), *vb = v2.as<uint32_t>();
   int passes = 0;
   for (int shift = 0; shift < bits; shift += 8, passes++) {
-    k_rs_upsweep<<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ka, n, shift, nb, hist.as<i64>());
+    k_rs_upsweep<kRsRounds><<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ka, n, shift, nb, hist.as<i64>());
     check_launch("rs_upsweep");
     scan_i64(c, hist.as<i64>(), goff.as<i64>(), 256 * nb);
     k_rs_downsweep<<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ka, va, kb, vb, n, shift, nb, goff.as<i64>());
@@ -468,8 +470,8 @@ void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, con
                        uint32_t* rout, T* vout, i64 n, int bits) {
   if (n <= 0) return;
   const int passes = std::max(1, (bits + 7) / 8);
-  const i64 nb = (n + kRsTile - 1) / kRsTile;
-  const int dyn = (int)((2 * sizeof(uint32_t) + sizeof(T)) * kRsTile);
+  const i64 nb = (n + kRsTileRv - 1) / kRsTileRv;
+  const int dyn = (int)((2 * sizeof(uint32_t) + sizeof(T)) * kRsTileRv);
   FVG_CUDA(cudaFuncSetAttribute(k_rs_downsweep_rv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   DBuf kt, rt, vt, hist, goff;
   if (passes > 1) {  // padded: the staging copies read up to 15 bytes past n
@@ -487,7 +489,7 @@ void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, con
     uint32_t* rd = to_out ? rout : rt.as<uint32_t>();
     T* vd = to_out ? vout : vt.as<T>();
     const int shift = 8 * p;
-    k_rs_upsweep<<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ks, n, shift, nb, hist.as<i64>());
+    k_rs_upsweep<kRsRoundsRv><<<(unsigned)nb, kRsThreads, 0, c->stream>>>(ks, n, shift, nb, hist.as<i64>());
     check_launch("rs_upsweep");
     scan_i64(c, hist.as<i64>(), goff.as<i64>(), 256 * nb);
     k_rs_downsweep_rv<T><<<(unsigned)nb, kRsThreads, dyn, c->stream>>>(ks, rs, vs, kd, rd, vd, n, shift, nb,
