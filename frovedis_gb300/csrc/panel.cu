@@ -91,7 +91,6 @@ __global__ void k_i64_to_i32(const i64* __restrict__ s, i32* __restrict__ d, i64
   PGRID_STRIDE(i, n) d[i] = (i32)s[i];
 }
 
-// a warp per panel row: its entries copied with the row made panel-local
 // The source's other value planes (FP32, BF16, split residual) that a fill
 // copies beside the master plane, so that a layout built from a matrix that
 // already holds them needs no conversion afterwards; null where absent.
@@ -109,6 +108,7 @@ struct SidePlanes {
   }
 };
 
+// a warp per panel row: its entries copied with the row made panel-local
 template <class T>
 __global__ void k_panel_fill(const i32* __restrict__ B, const i64* __restrict__ poff, const i32* __restrict__ tidx,
                              const T* __restrict__ tval, i64 nhot, i64 np, i64 rows, uint16_t* __restrict__ prow,
