@@ -155,7 +155,7 @@ __device__ __forceinline__ df seg_scan(df v, bool reset, int lane) {
   return v;
 }
 
-// Persistent kernel over CRS work items of at most kSplitCrsTile entries
+// Persistent kernel over CRS work items of at most split_crs_tile() entries
 // (tiles of short rows, pieces of long rows; the packing of k_crs).  Lane L
 // takes the CH entries q0 + CH*L .. q0 + CH*L + CH - 1 (q0 = the item's first
 // entry rounded down to CH): column ids, FP32 values and BF16 residuals come in
