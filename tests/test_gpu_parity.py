@@ -123,6 +123,26 @@ def test_transpose_bit_exact(ctx):
         assert np.array_equal(tval, t.val), name
 
 
+def test_transpose_bit_exact_fp32_bf16_values(ctx):
+    # the transposed copy's sort carries 4- and 2-byte values for matrices
+    # uploaded with FP32 or BF16 values (odd tile tails included)
+    rng = np.random.default_rng(15)
+    for name, a in _cases(rng):
+        for kind in ("f32", "bf16"):
+            if kind == "f32":
+                v = a.val.astype(np.float32)
+                exact = v.astype(np.float64)
+            else:
+                v = fv.bf16_bits(a.val)
+                exact = (v.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+            A = ctx.matrix(a.m, a.n, a.off, a.idx, v)
+            toff, tidx, tval = A.get_transpose()
+            t = oracle.transpose(oracle.CRS(a.m, a.n, a.off, a.idx, exact))
+            assert np.array_equal(toff, t.off), (name, kind)
+            assert np.array_equal(tidx, t.idx), (name, kind)
+            assert np.array_equal(tval, t.val), (name, kind)
+
+
 def test_ell_jds_hybrid_layouts_bit_exact(ctx):
     rng = np.random.default_rng(6)
     for name, a in _cases(rng):
