@@ -469,6 +469,10 @@ template <class T>
 void radix_sort_rowval(fvg_ctx* c, const uint32_t* kin, const uint32_t* rin, const T* vin, uint32_t* kout,
                        uint32_t* rout, T* vout, i64 n, int bits) {
   if (n <= 0) return;
+  // the tiles are staged by bulk copies, which need 16-byte aligned sources
+  // (tile starts are multiples of 16 bytes from each array's base)
+  if (((uintptr_t)kin | (uintptr_t)rin | (uintptr_t)vin | (uintptr_t)kout | (uintptr_t)rout | (uintptr_t)vout) & 15u)
+    fail(FVG_ERR_INTERNAL, "radix sort arrays must be 16-byte aligned");
   const int passes = std::max(1, (bits + 7) / 8);
   const i64 nb = (n + kRsTileRv - 1) / kRsTileRv;
   const int dyn = (int)((2 * sizeof(uint32_t) + sizeof(T)) * kRsTileRv);
