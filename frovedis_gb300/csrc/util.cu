@@ -367,11 +367,13 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
 // Downsweep carrying a (row, value) payload.  Thread 0 stages the tile's keys,
 // rows and values in shared memory with three bulk copies on one mbarrier
 // (the copies' sizes rounded up to 16 bytes: the arrays are padded past n);
-// the warps rank the staged keys, the ranked keys go to their tile slots with
-// their input position, and the write-back reads each slot's row and value
-// from the staged copy.  Dynamic shared memory: kRsTile keys and rows
-// (uint32) and kRsTile values.  A copy wait that runs out of polls sets bit 2
-// of *err and the CTA returns without writing.
+// the warps rank the staged keys, the ranked keys go to their tile slots (over
+// the staged keys, which the ranking no longer needs) with their input
+// position, and the write-back reads each slot's row and value from the
+// staged copy.  Tiles of kRsTileRv entries (12 rounds: three CTAs per SM with
+// FP64 values); dynamic shared memory: kRsTileRv keys and rows (uint32) and
+// kRsTileRv values.  A copy wait that runs out of polls sets bit 2 of *err
+// and the CTA returns without writing.
 template <class T>
 __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep_rv(const uint32_t* __restrict__ kin,
                                                                 const uint32_t* __restrict__ rin,
