@@ -268,6 +268,33 @@ __device__ __forceinline__ void chunk_segments(const float (&p)[C], const float 
   T = acc.get();
 }
 
+// chunk_segments that also records the rows starting and ending between two
+// marks ("middle rows", for layouts whose rows are often shorter than a
+// chunk): at every mark after the first, the sum since the previous mark is
+// stored unnormalised as (s, c) at mid[pos0 + previous mark], one pass over
+// the chunk instead of one chunk_range per middle row.
+template <int C>
+__device__ __forceinline__ void chunk_segments_mid(const float (&p)[C], const float (&t)[C], unsigned B, df& H,
+                                                   df& T, float2* mid, int pos0) {
+  const int fb = B ? __ffs(B) - 1 : C;  // first mark
+  DfAcc acc, head;
+  int prev = 0;  // the current segment's first entry (after the first mark)
+#pragma unroll
+  for (int k = 0; k < C; k++) {
+    const bool mk = (B >> k) & 1u;
+    const bool cap = k == fb;
+    if (mk && !cap) mid[pos0 + prev] = make_float2(acc.s, acc.c);
+    head.s = cap ? acc.s : head.s;
+    head.c = cap ? acc.c : head.c;
+    acc.s = mk ? 0.f : acc.s;
+    acc.c = mk ? 0.f : acc.c;
+    prev = mk ? k : prev;
+    acc.add(p[k], t[k]);
+  }
+  H = B ? head.get() : df{0.f, 0.f};
+  T = acc.get();
+}
+
 // Sum of the chunk's entries [a, b): rows that start and end between two
 // marks (a second path, rarely taken where rows are longer than a chunk).
 template <int C>

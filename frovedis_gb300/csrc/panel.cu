@@ -639,6 +639,12 @@ __device__ __forceinline__ df seg_scan_df(df v, bool reset, int lane) {
 // end join the neighbouring lanes' segments through a segmented scan in lane
 // order.  Pieces of long rows: a warp reduction, added after the CTA barrier
 // in piece order.  Every sum has a fixed order.
+// MID (the row panels, whose rows are often shorter than a lane's chunk): the
+// rows that start and end inside one lane's chunk are summed in the chunk's
+// single pass, parked in the warp's staging area (free once the entries are
+// in registers) and written after it; without MID (the forward head, rows
+// longer than a chunk) each such row is re-summed over the chunk.
+template <bool MID>
 __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK p) {
   using SM = SplitSmem;
   constexpr int NW = kSplitWarps;
@@ -789,21 +795,26 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
           }
         }
         df H, T;
-        chunk_segments<CH>(pp, tt, B, H, T);
-        if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
-          unsigned rest = B & (B - 1);
-          int a = __ffs(B) - 1, jj = j0;
-          do {
-            jj++;
-          } while (soff[jj + 1] == soff[jj]);
-          while (rest) {
-            const int b = __ffs(rest) - 1;
-            rest &= rest - 1;
-            p.ypan[it.r0 + jj] = df_pack(chunk_range<CH>(pp, tt, a, b));
-            a = b;
+        float2* mid = reinterpret_cast<float2*>(area);  // kCap pairs: the staging area's 8 bytes an entry
+        if constexpr (MID) {
+          chunk_segments_mid<CH>(pp, tt, B, H, T, mid, lane * CH);
+        } else {
+          chunk_segments<CH>(pp, tt, B, H, T);
+          if (__popc(B) >= 2) {  // rows between two marks: started and ended in this chunk
+            unsigned rest = B & (B - 1);
+            int a = __ffs(B) - 1, jj = j0;
             do {
               jj++;
             } while (soff[jj + 1] == soff[jj]);
+            while (rest) {
+              const int b = __ffs(rest) - 1;
+              rest &= rest - 1;
+              p.ypan[it.r0 + jj] = df_pack(chunk_range<CH>(pp, tt, a, b));
+              a = b;
+              do {
+                jj++;
+              } while (soff[jj + 1] == soff[jj]);
+            }
           }
         }
         // the tail segment starts inside this lane when a row starts here
@@ -812,6 +823,22 @@ __global__ void __launch_bounds__(kSplitWarps * 32, 1) k_panel_split(const PanSK
         if (lane == 0) carry = {0.f, 0.f};
         if (B) p.ypan[it.r0 + j0] = df_pack(starts ? H : df_add(carry, H));
         if (any && nb == hi_e) p.ypan[it.r0 + j] = df_pack(S);  // the tail row ends with this lane's range
+        if constexpr (MID) {
+          // the middle rows: non-empty rows whose start and end are both marks
+          // of one lane (start after the lane's first entry, end before its
+          // range ends)
+          __syncwarp();
+          const int ie0 = it.e0 - q0, ie1 = it.e1 - q0;
+          for (int jr = lane; jr < R; jr += 32) {
+            const int s0 = soff[jr], s1 = soff[jr + 1];
+            if (s1 == s0) continue;
+            const int L = s0 / CH;
+            if (s0 > max(ie0, L * CH) && s1 < min(ie1, L * CH + CH)) {
+              const float2 v = mid[s0];
+              p.ypan[it.r0 + jr] = df_pack(fast_two_sum(v.x, v.y));
+            }
+          }
+        }
       }
       fence_proxy_async();  // the padding stores, before the next copy into the area
       __syncwarp();
@@ -1414,14 +1441,19 @@ void launch_panel_split(fvg_ctx* c, const PanSK& k, i64 rows) {
     if (std::find(attr_set.begin(), attr_set.end(), c->device) == attr_set.end()) {
       int optin = 0;
       FVG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-      FVG_CUDA(cudaFuncSetAttribute(k_panel_split, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+      FVG_CUDA(cudaFuncSetAttribute(k_panel_split<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+      FVG_CUDA(cudaFuncSetAttribute(k_panel_split<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
       attr_set.push_back(c->device);
     }
   }
-  const int blocks = occupancy_blocks((const void*)k_panel_split, threads, (size_t)smem);
+  // the row panels (no shared slice map) take the middle-row pass
+  const bool panels = k.xmap == nullptr;
+  const void* kfn = panels ? (const void*)k_panel_split<true> : (const void*)k_panel_split<false>;
+  const int blocks = occupancy_blocks(kfn, threads, (size_t)smem);
   const i64 nunits = (k.npanels + k.group - 1) / k.group;
   const int grid = (int)std::max<i64>(1, std::min<i64>(nunits, (i64)blocks * c->num_sms));
-  k_panel_split<<<grid, threads, smem, c->stream>>>(k);
+  if (panels) k_panel_split<true><<<grid, threads, smem, c->stream>>>(k);
+  else k_panel_split<false><<<grid, threads, smem, c->stream>>>(k);
   check_launch("k_panel_split");
   count_launch(c);
 }
